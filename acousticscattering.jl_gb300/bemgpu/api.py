@@ -1,0 +1,537 @@
+"""Host-side mirror of AcousticScattering.jl's full-3D BEM interface over libbemgpu.
+
+Names, arguments and error behaviour follow the reference:
+
+  mesh(nodes, triangles)                        geometry/surface.jl:271-298 (validation
+                                                 surface.jl:341-405)
+  bem(surface, boundary, k; incidence_angle=pi/2, incidence_azimuth=0, ...)
+                                                solvers/bem/surface.jl:10-23 with the
+                                                 options of full.jl:52-58 and :273-279
+  scattering_amplitude(sol; direction)          solvers/bem/postprocessing.jl:1-13
+  target_strength(sol_or_f; direction)          postprocessing/target_strength.jl:8, 26
+  diagnostics(sol)                              solvers/shared/postprocessing.jl:17
+  incidence_angle_sweep(surface, boundary, k, angles)   postprocessing/sweeps.jl:626-701
+  frequency_sweep(solve, frequencies, c)        postprocessing/sweeps.jl:103-110
+  Rigid / PressureRelease / FluidFilled         core/materials.jl:16-76
+
+Invalid arguments raise ArgumentError (a ValueError), as the reference's ArgumentError;
+non-convergence of the double-precision fallback raises RuntimeError, as its error().
+Every numerical operation runs in libbemgpu on the GPU; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as C
+
+
+class ArgumentError(ValueError):
+    """Invalid argument (the reference's ArgumentError)."""
+
+
+class BEMGPUError(RuntimeError):
+    """Device-side failure reported by libbemgpu."""
+
+
+# ------------------------------------------------------------------ boundary conditions
+class AbstractBoundaryCondition:
+    pass
+
+
+class Rigid(AbstractBoundaryCondition):
+    """Zero total normal velocity (core/materials.jl:16)."""
+
+    code = C.RIGID
+
+    def __repr__(self):
+        return "Rigid()"
+
+
+class PressureRelease(AbstractBoundaryCondition):
+    """Zero total pressure (core/materials.jl:23)."""
+
+    code = C.PRESSURE_RELEASE
+
+    def __repr__(self):
+        return "PressureRelease()"
+
+
+class FluidFilled(AbstractBoundaryCondition):
+    """Homogeneous fluid interior: density_contrast g = rho_i/rho_e, soundspeed_contrast
+    h = c_i/c_e (core/materials.jl:62-76)."""
+
+    code = C.FLUID
+
+    def __init__(self, density_contrast: float, soundspeed_contrast: float):
+        self.density_contrast = float(density_contrast)
+        self.soundspeed_contrast = float(soundspeed_contrast)
+
+    def __repr__(self):
+        return f"FluidFilled({self.density_contrast}, {self.soundspeed_contrast})"
+
+
+GasFilled = FluidFilled
+
+_FORMULATIONS = {None: C.FORMULATION_DEFAULT, "burton_miller": C.BURTON_MILLER,
+                 "cbie": C.CBIE, "muller": C.MULLER}
+_FORMULATION_NAMES = {C.BURTON_MILLER: "burton_miller", C.CBIE: "cbie", C.MULLER: "muller"}
+
+
+# ------------------------------------------------------------------ errors / context
+def _last_error(ctx=None) -> str:
+    buf = ctypes.create_string_buffer(512)
+    C.lib().bemgpu_last_error(ctx, buf, 512)
+    return buf.value.decode(errors="replace")
+
+
+def _check(status: int, ctx=None):
+    if status == C.OK:
+        return
+    msg = _last_error(ctx)
+    if status in (C.EINVAL, C.ETOPOLOGY):
+        raise ArgumentError(msg)
+    if status == C.ENOTCONVERGED:
+        raise RuntimeError(msg)
+    name = C.lib().bemgpu_status_string(status).decode()
+    raise BEMGPUError(f"{name}: {msg}")
+
+
+class Context:
+    """One device context (stream, HBM budget, caching allocator)."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        h = ctypes.c_void_p()
+        _check(C.lib().bemgpu_ctx_create(device, hbm_budget_bytes, ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def memory(self):
+        used, budget = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(C.lib().bemgpu_ctx_memory(self.handle, ctypes.byref(used), ctypes.byref(budget)),
+               self.handle)
+        return used.value, budget.value
+
+    def synchronize(self):
+        _check(C.lib().bemgpu_ctx_synchronize(self.handle), self.handle)
+
+    def profile(self, enable: bool = True):
+        _check(C.lib().bemgpu_profile_enable(self.handle, int(enable)), self.handle)
+
+    def profile_reset(self):
+        _check(C.lib().bemgpu_profile_reset(self.handle), self.handle)
+
+    def profile_read(self, family: str):
+        n, ms = ctypes.c_int64(), ctypes.c_double()
+        _check(C.lib().bemgpu_profile_read(self.handle, family.encode(), ctypes.byref(n),
+                                           ctypes.byref(ms)), self.handle)
+        return n.value, ms.value
+
+    @staticmethod
+    def launch_count() -> int:
+        n = ctypes.c_int64()
+        C.lib().bemgpu_launch_count(None, ctypes.byref(n))
+        return n.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            C.lib().bemgpu_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_DEFAULT: Context | None = None
+
+
+def context() -> Context:
+    """The process-wide default context on device 0 (created on first use)."""
+    global _DEFAULT
+    if _DEFAULT is None:
+        _DEFAULT = Context(0)
+    return _DEFAULT
+
+
+# ------------------------------------------------------------------ surfaces
+class Mesh:
+    """A validated closed flat-triangle surface (the reference's Mesh of a supplied
+    surface).  ``nodes`` 3 x N float64, ``triangles`` 3 x M int64 (1-based)."""
+
+    def __init__(self, nodes, triangles, units: str = "m", provenance="supplied triangles"):
+        nodes = np.asarray(nodes, dtype=np.float64)
+        tris = np.asarray(triangles)
+        if nodes.ndim != 2 or nodes.shape[0] != 3:
+            raise ArgumentError("nodes must have three rows")
+        if tris.ndim != 2 or tris.shape[0] != 3:
+            raise ArgumentError("triangles must have 3 rows in Gmsh ordering (flat triangles)")
+        if not np.issubdtype(tris.dtype, np.integer):
+            raise ArgumentError("triangles must be integer node indices")
+        scale = {"m": 1.0, "cm": 0.01, "mm": 0.001}.get(units)
+        if scale is None:
+            raise ArgumentError("units must be :m, :cm or :mm")
+        self.nodes = np.asfortranarray(nodes * scale)
+        self.triangles = np.asfortranarray(tris.astype(np.int64))
+        if self.triangles.shape[1] == 0:
+            raise ArgumentError("surface must contain triangles")
+        res = ctypes.c_double()
+        err = ctypes.create_string_buffer(256)
+        st = C.lib().bemgpu_mesh_validate(C.dptr(self.nodes), self.nodes.shape[1],
+                                          C.i64ptr(self.triangles), self.triangles.shape[1],
+                                          ctypes.byref(res), err, 256)
+        if st != C.OK:
+            raise ArgumentError(err.value.decode())
+        self.resolution = res.value
+        h = ctypes.create_string_buffer(65)
+        C.lib().bemgpu_mesh_hash(C.dptr(self.nodes), self.nodes.shape[1],
+                                 C.i64ptr(self.triangles), self.triangles.shape[1], h)
+        self.hash = h.value.decode()
+        self.provenance = provenance
+        self._handles: dict[int, ctypes.c_void_p] = {}
+
+    @property
+    def n_panels(self) -> int:
+        return int(self.triangles.shape[1])
+
+    def handle(self, ctx: Context):
+        key = id(ctx)
+        if key not in self._handles:
+            h = ctypes.c_void_p()
+            _check(C.lib().bemgpu_mesh_upload(ctx.handle, C.dptr(self.nodes), self.nodes.shape[1],
+                                              C.i64ptr(self.triangles), self.triangles.shape[1],
+                                              ctypes.byref(h)), ctx.handle)
+            self._handles[key] = (ctx, h)
+        return self._handles[key][1]
+
+    def release(self):
+        for ctx, h in self._handles.values():
+            C.lib().bemgpu_mesh_destroy(h)
+        self._handles.clear()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+def mesh(nodes, triangles, *, units: str = "m") -> Mesh:
+    """Supplied closed surface (geometry/surface.jl:271-298)."""
+    return Mesh(nodes, triangles, units=units)
+
+
+# ------------------------------------------------------------------ problems
+def _problem(boundary, k, formulation=None, precision="double", equilibrate=True,
+             refinement=None, near_eta=2.0, assembly=None) -> C.Problem:
+    if not isinstance(boundary, AbstractBoundaryCondition):
+        raise ArgumentError("boundary must be Rigid(), PressureRelease() or FluidFilled(g, h)")
+    if formulation not in _FORMULATIONS:
+        raise ArgumentError("formulation must be :burton_miller, :cbie or :muller")
+    if precision not in ("double", "mixed"):
+        raise ArgumentError("precision must be :double or :mixed")
+    if assembly not in C.ASSEMBLY:
+        raise ArgumentError("assembly must be :double or :single")
+    refinement = dict(refinement or {})
+    unknown = set(refinement) - {"tolerance", "maxiter", "condition_guard"}
+    if unknown:
+        raise ArgumentError("unknown refinement option")
+    if refinement and precision != "mixed":
+        raise ArgumentError("refinement options require precision=:mixed")
+    maxiter = refinement.get("maxiter", 8)
+    if not isinstance(maxiter, (int, np.integer)) or maxiter < 0:
+        raise ArgumentError("maxiter must be a nonnegative integer")
+    p = C.Problem()
+    C.lib().bemgpu_problem_init(ctypes.byref(p))
+    p.boundary = boundary.code
+    p.formulation = _FORMULATIONS[formulation]
+    p.precision = C.MIXED if precision == "mixed" else C.DOUBLE
+    p.equilibrate = int(bool(equilibrate))
+    p.k = float(k)
+    if isinstance(boundary, FluidFilled):
+        p.density_contrast = boundary.density_contrast
+        p.soundspeed_contrast = boundary.soundspeed_contrast
+    p.refine_tolerance = float(refinement.get("tolerance", 1e-13))
+    p.refine_maxiter = int(maxiter)
+    p.condition_guard = float(refinement.get("condition_guard", 10 * np.finfo(np.float32).eps))
+    p.near_eta = float(near_eta)
+    p.assembly = C.ASSEMBLY[assembly]
+    return p
+
+
+def _direction(beta, alpha):
+    """Polar angle from +x, azimuth from +y toward +z (solvers/bem/full.jl:14-18)."""
+    return np.array([math.cos(beta), math.sin(beta) * math.cos(alpha),
+                     math.sin(beta) * math.sin(alpha)])
+
+
+def _diag_dict(d: C.Diagnostics, extra=None) -> dict:
+    out = {f: getattr(d, f) for f, _ in C.Diagnostics._fields_}
+    out["formulation"] = _FORMULATION_NAMES.get(d.formulation, "cbie")
+    out["precision"] = "mixed" if d.precision == C.MIXED else "double"
+    out["factor_precision"] = "single" if d.factor_precision == 0 else "double"
+    out["refinement_reason"] = C.REASONS[d.refinement_reason]
+    out["coupling"] = complex(d.coupling_re, d.coupling_im)
+    out["method"] = "mixed_refinement" if d.precision == C.MIXED else "direct"
+    out["equilibrate"] = bool(d.equilibrate)
+    if extra:
+        out.update(extra)
+    return out
+
+
+# ------------------------------------------------------------------ factor / solution
+class Factor:
+    """Assembled and factored system of one (surface, boundary, k): serves any number
+    of incidence directions (the reuse of incidence_angle_sweep, sweeps.jl:680-701)."""
+
+    def __init__(self, surface: Mesh, boundary, k, ctx: Context | None = None, **options):
+        self.ctx = ctx or context()
+        self.surface, self.boundary, self.k = surface, boundary, float(k)
+        self.problem = _problem(boundary, k, **options)
+        h = ctypes.c_void_p()
+        _check(C.lib().bemgpu_factor_create(self.ctx.handle, surface.handle(self.ctx),
+                                            ctypes.byref(self.problem), ctypes.byref(h)),
+               self.ctx.handle)
+        self.handle = h
+
+    def solve(self, angles, azimuths=0.0) -> "BEMSolution":
+        angles = np.atleast_1d(np.asarray(angles, dtype=np.float64))
+        az = np.broadcast_to(np.asarray(azimuths, dtype=np.float64), angles.shape)
+        inc = np.ascontiguousarray(np.stack([angles, az], axis=1).reshape(-1))
+        h = ctypes.c_void_p()
+        _check(C.lib().bemgpu_factor_solve(self.handle, len(angles), C.dptr(inc),
+                                           ctypes.byref(h)), self.ctx.handle)
+        return BEMSolution(self.ctx, h, self.surface, self.boundary, self.k, angles, az)
+
+    def diagnostics(self) -> dict:
+        d = C.Diagnostics()
+        _check(C.lib().bemgpu_factor_diagnostics(self.handle, ctypes.byref(d)))
+        return _diag_dict(d)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            C.lib().bemgpu_factor_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BEMSolution:
+    """Result of bem(): surface traces of one or more incidence directions
+    (the reference's BEMSolution{_FullBEMSurfaceData}, solvers/bem/types.jl:2-36)."""
+
+    method = "full"
+
+    def __init__(self, ctx, handle, surface, boundary, k, angles, azimuths):
+        self.ctx, self.handle = ctx, handle
+        self.body = surface
+        self.boundary = boundary
+        self.k = float(k)
+        self.incidence_angles = np.asarray(angles, dtype=np.float64)
+        self.incidence_azimuths = np.asarray(azimuths, dtype=np.float64)
+
+    @property
+    def incidence_angle(self):
+        return float(self.incidence_angles[0])
+
+    @property
+    def incidence_azimuth(self):
+        return float(self.incidence_azimuths[0])
+
+    @property
+    def nrhs(self):
+        return len(self.incidence_angles)
+
+    def far_field(self, directions=None, rhs: int = 0) -> np.ndarray:
+        if directions is None:
+            out = np.zeros(1, dtype=np.complex128)
+            _check(C.lib().bemgpu_far_field(self.handle, rhs, 1, None, C.dptr(out)),
+                   self.ctx.handle)
+            return out
+        d = np.ascontiguousarray(np.asarray(directions, dtype=np.float64).reshape(-1, 3))
+        out = np.zeros(d.shape[0], dtype=np.complex128)
+        _check(C.lib().bemgpu_far_field(self.handle, rhs, d.shape[0], C.dptr(d), C.dptr(out)),
+               self.ctx.handle)
+        return out
+
+    def traces(self, rhs: int = 0):
+        n = self.body.n_panels
+        p = np.zeros(n, dtype=np.complex128)
+        q = np.zeros(n, dtype=np.complex128)
+        _check(C.lib().bemgpu_traces(self.handle, rhs, C.dptr(p), C.dptr(q)), self.ctx.handle)
+        return p, q
+
+    @property
+    def p_scat(self):
+        return self.traces(0)[0]
+
+    @property
+    def dpdn_scat(self):
+        return self.traces(0)[1]
+
+    def diagnostics(self) -> dict:
+        d = C.Diagnostics()
+        _check(C.lib().bemgpu_solution_diagnostics(self.handle, ctypes.byref(d)))
+        return _diag_dict(d, {"meshsize": self.body.resolution,
+                              "illumination": "plane_wave", "mesh_hash": self.body.hash})
+
+    def close(self):
+        if getattr(self, "handle", None):
+            C.lib().bemgpu_solution_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------ reference-named API
+def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_azimuth=0.0,
+        formulation=None, precision="double", equilibrate=True, refinement=None,
+        assembly=None, ctx: Context | None = None, **unsupported) -> BEMSolution:
+    """Full-3D BEM on a supplied surface (solvers/bem/surface.jl:10-23)."""
+    if unsupported:
+        raise ArgumentError(f"unsupported option(s): {sorted(unsupported)}")
+    if not isinstance(surface, Mesh):
+        raise ArgumentError("surface must be a Mesh from mesh(nodes, triangles)")
+    if not (math.isfinite(incidence_angle) and math.isfinite(incidence_azimuth)):
+        raise ArgumentError("incidence angles must be finite")
+    k = float(k)
+    if not (math.isfinite(k) and k > 0):
+        raise ArgumentError("k must be finite and positive")
+    f = Factor(surface, boundary, k, ctx=ctx, formulation=formulation, precision=precision,
+               equilibrate=equilibrate, refinement=refinement, assembly=assembly)
+    try:
+        return f.solve([incidence_angle], [incidence_azimuth])
+    finally:
+        f.close()
+
+
+def scattering_amplitude(sol: BEMSolution, *, direction=None, rhs: int = 0) -> complex:
+    """Far-field amplitude f(x_hat) [m]; default backscatter x_hat = -d
+    (solvers/bem/postprocessing.jl:1-13)."""
+    if direction is not None:
+        d = np.asarray(direction, dtype=np.float64).reshape(-1)
+        if d.size != 3 or not np.all(np.isfinite(d)) or abs(np.linalg.norm(d) - 1) > 1e-8:
+            raise ArgumentError("direction must be a finite unit vector with three components")
+        return complex(sol.far_field(d, rhs)[0])
+    return complex(sol.far_field(None, rhs)[0])
+
+
+def target_strength(x, *, direction=None, rhs: int = 0) -> float:
+    """20 log10 |f| (postprocessing/target_strength.jl:8, 26)."""
+    if isinstance(x, BEMSolution):
+        x = scattering_amplitude(x, direction=direction, rhs=rhs)
+    return 20.0 * math.log10(abs(x))
+
+
+def diagnostics(sol) -> dict:
+    return sol.diagnostics()
+
+
+@dataclass
+class SweepResult:
+    angles: np.ndarray
+    amplitudes: np.ndarray
+    target_strength: np.ndarray
+    diagnostics: dict = field(default_factory=dict)
+
+
+def incidence_angle_sweep(surface: Mesh, boundary, k, angles, *, incidence_azimuth=0.0,
+                          formulation=None, precision="double", equilibrate=True,
+                          refinement=None, assembly=None, ctx=None) -> SweepResult:
+    """Backscatter at many polar incidence angles from one factorisation
+    (postprocessing/sweeps.jl:626-701): assembled and factored once, all angles
+    solved as one multi-right-hand-side batch."""
+    angles = np.asarray(angles, dtype=np.float64)
+    if angles.ndim != 1 or angles.size == 0 or not np.all(np.isfinite(angles)):
+        raise ArgumentError("angles must be a nonempty vector of finite values")
+    if not math.isfinite(incidence_azimuth):
+        raise ArgumentError("incidence_azimuth must be finite")
+    f = Factor(surface, boundary, k, ctx=ctx, formulation=formulation, precision=precision,
+               equilibrate=equilibrate, refinement=refinement, assembly=assembly)
+    try:
+        sol = f.solve(angles, incidence_azimuth)
+        amps = np.array([scattering_amplitude(sol, rhs=r) for r in range(len(angles))])
+        diag = sol.diagnostics()
+        sol.close()
+    finally:
+        f.close()
+    return SweepResult(angles, amps, 20 * np.log10(np.abs(amps)), diag)
+
+
+@dataclass
+class FrequencySweep:
+    frequencies: np.ndarray
+    k: np.ndarray
+    target_strength: np.ndarray
+    amplitudes: np.ndarray
+
+
+def frequency_sweep(solve, frequencies, sound_speed) -> FrequencySweep:
+    """Call ``solve(k)`` for each frequency (postprocessing/sweeps.jl:103-110)."""
+    if not (math.isfinite(sound_speed) and sound_speed > 0):
+        raise ArgumentError("sound_speed must be finite and positive")
+    freqs = np.asarray(frequencies, dtype=np.float64)
+    if not np.all(freqs > 0):
+        raise ArgumentError("frequencies must be positive")
+    ks = 2 * math.pi * freqs / sound_speed
+    amps = []
+    for k in ks:
+        s = solve(k)
+        amps.append(scattering_amplitude(s) if isinstance(s, BEMSolution) else complex(s))
+    amps = np.array(amps)
+    return FrequencySweep(freqs, ks, 20 * np.log10(np.abs(amps)), amps)
+
+
+def dense_solve(A, B, *, precision="double", equilibrate=True, refinement=None, ctx=None):
+    """Solve A X = B with the BEM factor path (full.jl:364-440; fluid_system.jl:172-309)
+    for a hand-built complex matrix; returns (X, diagnostics)."""
+    ctx = ctx or context()
+    A = np.asfortranarray(np.asarray(A, dtype=np.complex128))
+    B = np.asarray(B, dtype=np.complex128)
+    vec = B.ndim == 1
+    X = np.asfortranarray(B.reshape(B.shape[0], -1).copy())
+    n = A.shape[0]
+    if A.ndim != 2 or A.shape[1] != n or n == 0:
+        raise ArgumentError("expected a nonempty square matrix")
+    if X.shape[0] != n:
+        raise ArgumentError("right-hand side length")
+    p = _problem(Rigid(), 1.0, precision=precision, equilibrate=equilibrate,
+                 refinement=refinement)
+    d = C.Diagnostics()
+    _check(C.lib().bemgpu_dense_solve(ctx.handle, n, C.dptr(A), X.shape[1], C.dptr(X),
+                                      p.precision, p.equilibrate, p.refine_tolerance,
+                                      p.refine_maxiter, p.condition_guard, ctypes.byref(d)),
+           ctx.handle)
+    return (X[:, 0] if vec else X), _diag_dict(d)
+
+
+def assemble(surface: Mesh, boundary, k, *, formulation=None, precision="double",
+             assembly=None, ctx=None):
+    """The assembled operators (rigid/soft: M1 = 1/2 I - D - a H and
+    M2 = S + a (1/2 I + K'); fluid: the 2n x 2n system) as complex128 arrays."""
+    ctx = ctx or context()
+    p = _problem(boundary, k, formulation=formulation, precision=precision, assembly=assembly)
+    n = surface.n_panels
+    if isinstance(boundary, FluidFilled):
+        M1 = np.zeros((2 * n, 2 * n), dtype=np.complex128, order="F")
+        _check(C.lib().bemgpu_assemble_dense(ctx.handle, surface.handle(ctx), ctypes.byref(p),
+                                             C.dptr(M1), None), ctx.handle)
+        return M1
+    M1 = np.zeros((n, n), dtype=np.complex128, order="F")
+    M2 = np.zeros((n, n), dtype=np.complex128, order="F")
+    _check(C.lib().bemgpu_assemble_dense(ctx.handle, surface.handle(ctx), ctypes.byref(p),
+                                         C.dptr(M1), C.dptr(M2)), ctx.handle)
+    return M1, M2

@@ -1,0 +1,1991 @@
+// C ABI of libbemgpu: contexts, meshes, factors, solutions and queries.
+//
+// Host orchestration of the device kernels.  Every batched operation builds device
+// arrays of per-instance descriptors and issues one launch sequence for all instances;
+// the only host decisions are the ones the reference makes between LAPACK calls
+// (promotion of the mixed-precision factor, refinement acceptance).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "bemgpu_internal.h"
+#include "linalg.cuh"
+#include "refine.cuh"
+#include "solve_kernels.cuh"
+
+namespace bemgpu {
+static std::atomic<long long> g_launches{0};
+void count_launch(int kernels) { g_launches.fetch_add(kernels, std::memory_order_relaxed); }
+long long launch_total() { return g_launches.load(std::memory_order_relaxed); }
+}  // namespace bemgpu
+
+using namespace bemgpu;
+
+namespace {
+thread_local std::string g_err;
+const double kPi = 3.14159265358979323846;
+}  // namespace
+
+// ===================================================================== context + memory
+struct bemgpu_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t budget = 0;
+  uint64_t live = 0;
+  std::string err;
+  int* d_err = nullptr;
+  std::multimap<size_t, void*> cache;
+  uint64_t cached = 0;
+  bool prof = false;
+  std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
+  std::recursive_mutex mu;
+  Launch launch() const { return Launch{stream, d_err}; }
+};
+
+namespace {
+
+int fail(bemgpu_ctx* c, int code, const std::string& msg) {
+  if (c)
+    c->err = msg;
+  else
+    g_err = msg;
+  return code;
+}
+
+int cuda_fail(bemgpu_ctx* c, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  return fail(c, BEMGPU_ECUDA, m);
+}
+
+#define CUDA_TRY(c, call)                                   \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return cuda_fail((c), e_, #call); \
+  } while (0)
+#define TRY(x)                          \
+  do {                                  \
+    int s_ = (x);                       \
+    if (s_ != BEMGPU_OK) return s_;     \
+  } while (0)
+
+size_t round_bytes(size_t b) {
+  if (b == 0) b = 1;
+  const size_t kSmall = size_t(1) << 20, kLarge = size_t(2) << 20;
+  if (b <= kSmall) return (b + 4095) & ~size_t(4095);
+  return (b + kLarge - 1) / kLarge * kLarge;
+}
+
+// Device buffer drawn from the context's caching pool and counted against its budget.
+struct Buf {
+  bemgpu_ctx* c = nullptr;
+  void* p = nullptr;
+  size_t bytes = 0;
+  Buf() = default;
+  Buf(const Buf&) = delete;
+  Buf& operator=(const Buf&) = delete;
+  Buf(Buf&& o) noexcept : c(o.c), p(o.p), bytes(o.bytes) {
+    o.p = nullptr;
+    o.bytes = 0;
+  }
+  Buf& operator=(Buf&& o) noexcept {
+    if (this != &o) {
+      release();
+      c = o.c;
+      p = o.p;
+      bytes = o.bytes;
+      o.p = nullptr;
+      o.bytes = 0;
+    }
+    return *this;
+  }
+  ~Buf() { release(); }
+  void release() {
+    if (p && c) {
+      c->cache.emplace(bytes, p);
+      c->cached += bytes;
+      c->live -= bytes;
+    }
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+void drop_cache(bemgpu_ctx* c) {
+  for (auto& kv : c->cache) cudaFree(kv.second);
+  c->cache.clear();
+  c->cached = 0;
+}
+
+int alloc(bemgpu_ctx* c, size_t bytes, Buf* out) {
+  out->release();
+  size_t rb = round_bytes(bytes);
+  if (c->live + rb > c->budget) {
+    char m[200];
+    std::snprintf(m, sizeof m, "HBM budget exceeded: %.3f GB live + %.3f GB requested > %.3f GB",
+                  c->live / 1e9, rb / 1e9, c->budget / 1e9);
+    return fail(c, BEMGPU_ENOMEM_BUDGET, m);
+  }
+  auto it = c->cache.find(rb);
+  void* p = nullptr;
+  if (it != c->cache.end()) {
+    p = it->second;
+    c->cache.erase(it);
+    c->cached -= rb;
+  } else {
+    cudaError_t e = cudaMalloc(&p, rb);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      drop_cache(c);
+      e = cudaMalloc(&p, rb);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_fail(c, e, "cudaMalloc");
+      }
+    }
+  }
+  out->c = c;
+  out->p = p;
+  out->bytes = rb;
+  c->live += rb;
+  return BEMGPU_OK;
+}
+
+template <class T>
+int upload(bemgpu_ctx* c, const std::vector<T>& h, Buf* out) {
+  TRY(alloc(c, h.size() * sizeof(T), out));
+  if (!h.empty())
+    CUDA_TRY(c, cudaMemcpyAsync(out->p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice,
+                                c->stream));
+  return BEMGPU_OK;
+}
+
+template <class T>
+int download(bemgpu_ctx* c, const Buf& b, std::vector<T>* h, size_t count) {
+  h->resize(count);
+  if (count)
+    CUDA_TRY(c, cudaMemcpyAsync(h->data(), b.p, count * sizeof(T), cudaMemcpyDeviceToHost,
+                                c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return BEMGPU_OK;
+}
+
+int check_device_error(bemgpu_ctx* c) {
+  int h = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  CUDA_TRY(c, cudaGetLastError());
+  if (h != 0) {
+    cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+    return fail(c, BEMGPU_ETIMEOUT, "a bounded device wait gave up (kernel returned early)");
+  }
+  return BEMGPU_OK;
+}
+
+// Event pair around a family of launches when profiling is on.
+struct Prof {
+  bemgpu_ctx* c;
+  const char* fam;
+  cudaEvent_t a = nullptr, b = nullptr;
+  Prof(bemgpu_ctx* c_, const char* f) : c(c_), fam(f) {
+    if (c->prof) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, c->stream);
+    }
+  }
+  ~Prof() {
+    if (a) {
+      cudaEventRecord(b, c->stream);
+      c->events[fam].emplace_back(a, b);
+    }
+  }
+};
+
+// Phase timer (always on): elapsed device time between construction and stop().
+struct Timer {
+  cudaStream_t s;
+  cudaEvent_t a = nullptr, b = nullptr;
+  explicit Timer(cudaStream_t st) : s(st) {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+  }
+  double stop() {
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+  }
+  ~Timer() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
+
+}  // namespace
+
+// ===================================================================== meshes
+namespace {
+struct MeshData {
+  bemgpu_ctx* c = nullptr;
+  int64_t n = 0, nn = 0;
+  double resolution = 0.0;
+  char hash[65] = {0};
+  double center[3] = {0, 0, 0};
+  std::vector<double> panels_h;  // FP64 records
+  Buf panels, panelsf, verts, near_i, near_j;
+  int64_t n_near = 0;
+  double eta = 2.0;
+};
+}  // namespace
+
+struct bemgpu_mesh {
+  std::shared_ptr<MeshData> d;
+};
+
+namespace {
+// Panel records of the device layout (bemgpu_internal.h).  Host arithmetic with
+// separately rounded operations (built with -ffp-contract=off).
+void build_panels(const double* nodes, const int64_t* tris, int64_t M, std::vector<double>* rec,
+                  std::vector<float>* recf, std::vector<double>* verts, double center[3]) {
+  rec->assign(static_cast<size_t>(M * kPanelDoubles), 0.0);
+  recf->assign(static_cast<size_t>(M * kPanelFloats), 0.0f);
+  verts->assign(static_cast<size_t>(M * kVertDoubles), 0.0);
+  double cs[3] = {0, 0, 0};
+  for (int64_t t = 0; t < M; ++t) {
+    double v[3][3];
+    for (int a = 0; a < 3; ++a)
+      for (int d = 0; d < 3; ++d) v[a][d] = nodes[3 * (tris[3 * t + a] - 1) + d];
+    double e1[3], e2[3], cr[3];
+    for (int d = 0; d < 3; ++d) {
+      e1[d] = v[1][d] - v[0][d];
+      e2[d] = v[2][d] - v[0][d];
+    }
+    cr[0] = e1[1] * e2[2] - e1[2] * e2[1];
+    cr[1] = e1[2] * e2[0] - e1[0] * e2[2];
+    cr[2] = e1[0] * e2[1] - e1[1] * e2[0];
+    double len = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    double* r = rec->data() + t * kPanelDoubles;
+    for (int d = 0; d < 3; ++d) {
+      r[d] = (v[0][d] + v[1][d] + v[2][d]) / 3.0;
+      r[3 + d] = cr[d] / len;
+    }
+    r[6] = 0.5 * len;
+    double dm = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      double e[3];
+      for (int d = 0; d < 3; ++d) e[d] = v[(a + 1) % 3][d] - v[a][d];
+      double l = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+      if (l > dm) dm = l;
+    }
+    r[7] = dm;
+    for (int q = 0; q < 7; ++q)
+      for (int d = 0; d < 3; ++d)
+        r[8 + 3 * q + d] =
+            kRuleB[q][0] * v[0][d] + kRuleB[q][1] * v[1][d] + kRuleB[q][2] * v[2][d];
+    double* vv = verts->data() + t * kVertDoubles;
+    for (int a = 0; a < 3; ++a)
+      for (int d = 0; d < 3; ++d) vv[3 * a + d] = v[a][d];
+    for (int d = 0; d < 3; ++d) cs[d] += r[d];
+  }
+  for (int d = 0; d < 3; ++d) center[d] = M ? cs[d] / (double)M : 0.0;
+  for (int64_t t = 0; t < M; ++t) {
+    const double* r = rec->data() + t * kPanelDoubles;
+    float* f = recf->data() + t * kPanelFloats;
+    for (int d = 0; d < 3; ++d) {
+      f[d] = (float)(r[d] - center[d]);
+      f[3 + d] = (float)r[3 + d];
+    }
+    f[6] = (float)r[6];
+    f[7] = (float)r[7];
+    for (int q = 0; q < 7; ++q)
+      for (int d = 0; d < 3; ++d) f[8 + 3 * q + d] = (float)(r[8 + 3 * q + d] - center[d]);
+  }
+}
+
+int make_mesh(bemgpu_ctx* c, const double* nodes, int64_t N, const int64_t* tris, int64_t M,
+              double eta, std::shared_ptr<MeshData>* out) {
+  std::string err;
+  double res = 0.0;
+  int s = validate_surface(nodes, N, tris, M, &res, &err);
+  if (s != BEMGPU_OK) return fail(c, s, err);
+  auto m = std::make_shared<MeshData>();
+  m->c = c;
+  m->n = M;
+  m->nn = N;
+  m->resolution = res;
+  m->eta = eta;
+  mesh_hash(nodes, N, tris, M, m->hash);
+  std::vector<float> recf;
+  std::vector<double> verts;
+  build_panels(nodes, tris, M, &m->panels_h, &recf, &verts, m->center);
+  std::vector<double> cent, diam;
+  panel_centroids(nodes, tris, M, &cent, &diam);
+  std::vector<int64_t> rowptr, cols;
+  near_pairs(cent, diam, eta, &rowptr, &cols);
+  std::vector<int32_t> ni(cols.size()), nj(cols.size());
+  for (int64_t i = 0; i < M; ++i)
+    for (int64_t p = rowptr[i]; p < rowptr[i + 1]; ++p) {
+      ni[p] = (int32_t)i;
+      nj[p] = (int32_t)cols[p];
+    }
+  m->n_near = (int64_t)cols.size();
+  TRY(upload(c, m->panels_h, &m->panels));
+  TRY(upload(c, recf, &m->panelsf));
+  TRY(upload(c, verts, &m->verts));
+  TRY(upload(c, ni, &m->near_i));
+  TRY(upload(c, nj, &m->near_j));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  *out = m;
+  return BEMGPU_OK;
+}
+}  // namespace
+
+// ===================================================================== factors
+namespace {
+struct FactorData {
+  bemgpu_ctx* c = nullptr;
+  std::shared_ptr<MeshData> mesh;  // null for dense user matrices
+  bemgpu_problem prob{};
+  int kind = kAsmBM;
+  int64_t n = 0, N = 0;
+  bool rhs_is_m2 = true;   // rigid: b = M2 q_inc; soft: b = M1 p_inc
+  Buf A, Mrhs;             // complex128 system, rhs operator
+  Buf LU, ipiv, info;      // working factor (complex64 when single)
+  Buf LU64, ipiv64, info64;  // complex128 factor after promotion
+  Buf rows, cols, rowsum;
+  bool single = false;     // current factor precision
+  bool mixed = false;      // requested precision
+  bool fp32_regular = false;  // regular pairs assembled in FP32
+  int reason = BEMGPU_REASON_NONE;
+  double rcond = NAN;
+  double matrix_norm = 0.0, anorm = 0.0;
+  int32_t info_h = 0;
+  double assemble_ms = 0.0, factor_ms = 0.0;
+  void* factor_ptr() const { return single ? LU.p : (mixed ? LU64.p : LU.p); }
+  int32_t* ipiv_ptr() const { return single ? ipiv.as<int32_t>() : (mixed ? ipiv64.as<int32_t>() : ipiv.as<int32_t>()); }
+  int32_t* info_ptr() const { return single ? info.as<int32_t>() : (mixed ? info64.as<int32_t>() : info.as<int32_t>()); }
+  size_t bytes() const {
+    return A.bytes + Mrhs.bytes + LU.bytes + LU64.bytes + ipiv.bytes + ipiv64.bytes + rows.bytes +
+           cols.bytes + rowsum.bytes;
+  }
+};
+}  // namespace
+
+struct bemgpu_factor {
+  std::shared_ptr<FactorData> d;
+};
+
+namespace {
+struct SolutionData {
+  bemgpu_ctx* c = nullptr;
+  std::shared_ptr<MeshData> mesh;
+  int boundary = 0;
+  double k = 0.0, g = 1.0, h = 1.0;
+  int32_t nrhs = 0;
+  std::vector<double> dirs;  // incidence direction vectors, 3 per rhs
+  Buf ps, qs;                // scattered traces, complex128 n x nrhs
+  bemgpu_diagnostics diag{};
+};
+}  // namespace
+
+struct bemgpu_solution {
+  std::shared_ptr<SolutionData> d;
+};
+
+namespace {
+
+int check_problem(bemgpu_ctx* c, const bemgpu_problem& p, int* kind) {
+  if (!(std::isfinite(p.k) && p.k > 0)) return fail(c, BEMGPU_EINVAL, "k must be finite and positive");
+  if (p.precision != BEMGPU_DOUBLE && p.precision != BEMGPU_MIXED)
+    return fail(c, BEMGPU_EINVAL, "precision must be :double or :mixed");
+  if (p.precision == BEMGPU_MIXED) {
+    if (!p.equilibrate) return fail(c, BEMGPU_EINVAL, "mixed precision requires equilibrate=true");
+    if (!(std::isfinite(p.refine_tolerance) && p.refine_tolerance > 0 && p.refine_tolerance < 1))
+      return fail(c, BEMGPU_EINVAL, "invalid refinement tolerance");
+    if (p.refine_maxiter < 0) return fail(c, BEMGPU_EINVAL, "maxiter must be a nonnegative integer");
+    if (!(std::isfinite(p.condition_guard) && p.condition_guard >= 0))
+      return fail(c, BEMGPU_EINVAL, "invalid condition guard");
+  }
+  if (p.assembly < BEMGPU_ASSEMBLY_DEFAULT || p.assembly > BEMGPU_ASSEMBLY_SINGLE)
+    return fail(c, BEMGPU_EINVAL, "assembly must be :default, :double or :single");
+  if (!(std::isfinite(p.near_eta) && p.near_eta > 0))
+    return fail(c, BEMGPU_EINVAL, "near_eta must be finite and positive");
+  if (p.boundary == BEMGPU_RIGID || p.boundary == BEMGPU_PRESSURE_RELEASE) {
+    int f = p.formulation == BEMGPU_FORMULATION_DEFAULT ? BEMGPU_BURTON_MILLER : p.formulation;
+    if (f != BEMGPU_BURTON_MILLER && f != BEMGPU_CBIE)
+      return fail(c, BEMGPU_EINVAL, "formulation must be :cbie or :burton_miller");
+    *kind = f == BEMGPU_BURTON_MILLER ? kAsmBM : kAsmCBIE;
+  } else if (p.boundary == BEMGPU_FLUID) {
+    int f = p.formulation == BEMGPU_FORMULATION_DEFAULT ? BEMGPU_MULLER : p.formulation;
+    if (f != BEMGPU_MULLER && f != BEMGPU_CBIE)
+      return fail(c, BEMGPU_EINVAL, "fluid formulation must be :muller or :cbie");
+    const double g = p.density_contrast, h = p.soundspeed_contrast;
+    if (!(std::isfinite(g) && g > 0 && std::isfinite(h) && h > 0))
+      return fail(c, BEMGPU_EINVAL,
+                  "fluid density and soundspeed contrasts must be finite and positive");
+    *kind = f == BEMGPU_MULLER ? kAsmMuller : kAsmFluidCBIE;
+  } else {
+    return fail(c, BEMGPU_EINVAL, "unknown boundary condition");
+  }
+  return BEMGPU_OK;
+}
+
+int formulation_of(int kind) {
+  switch (kind) {
+    case kAsmBM: return BEMGPU_BURTON_MILLER;
+    case kAsmCBIE: return BEMGPU_CBIE;
+    case kAsmMuller: return BEMGPU_MULLER;
+    default: return BEMGPU_CBIE;
+  }
+}
+
+template <class T>
+int to_device(bemgpu_ctx* c, const std::vector<T>& h, Buf* out) {
+  return upload(c, h, out);
+}
+
+// ------------------------------------------------------------------ assembly
+int assemble_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
+  const Launch L = c->launch();
+  std::vector<AsmInst> ai(fs.size());
+  for (size_t t = 0; t < fs.size(); ++t) {
+    FactorData* f = fs[t];
+    MeshData* m = f->mesh.get();
+    const bool fluid = f->kind == kAsmMuller || f->kind == kAsmFluidCBIE;
+    f->n = m->n;
+    f->N = fluid ? 2 * m->n : m->n;
+    TRY(alloc(c, (size_t)f->N * f->N * 16, &f->A));
+    if (!fluid) TRY(alloc(c, (size_t)f->n * f->n * 16, &f->Mrhs));
+    AsmInst& I = ai[t];
+    std::memset(&I, 0, sizeof I);
+    I.panels = m->panels.as<double>();
+    I.panelsf = m->panelsf.as<float>();
+    I.verts = m->verts.as<double>();
+    I.near_i = m->near_i.as<int32_t>();
+    I.near_j = m->near_j.as<int32_t>();
+    I.n = m->n;
+    I.n_near = m->n_near;
+    I.lda = f->N;
+    I.k_e = f->prob.k;
+    I.k_i = fluid ? f->prob.k / f->prob.soundspeed_contrast : f->prob.k;
+    I.g = fluid ? f->prob.density_contrast : 1.0;
+    I.a_re = 0.0;
+    I.a_im = f->kind == kAsmBM ? 1.0 / f->prob.k : 0.0;
+    I.kind = f->kind;
+    if (fluid) {
+      I.out1 = f->A.p;
+      I.out2 = nullptr;
+    } else {
+      // rigid: system M1, rhs M2; pressure release: system M2, rhs M1
+      f->rhs_is_m2 = f->prob.boundary == BEMGPU_RIGID;
+      I.out1 = f->rhs_is_m2 ? f->A.p : f->Mrhs.p;
+      I.out2 = f->rhs_is_m2 ? f->Mrhs.p : f->A.p;
+    }
+  }
+  // group by (kind, regular precision) so each group is one launch
+  std::vector<size_t> order(fs.size());
+  for (size_t t = 0; t < order.size(); ++t) order[t] = t;
+  auto key = [&](size_t t) { return fs[t]->kind * 2 + (fs[t]->fp32_regular ? 1 : 0); };
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return key(a) < key(b); });
+  std::vector<AsmInst> sorted(fs.size());
+  for (size_t t = 0; t < order.size(); ++t) sorted[t] = ai[order[t]];
+  Buf d_ai;
+  TRY(to_device(c, sorted, &d_ai));
+  {
+    Prof pr(c, "assemble");
+    size_t s = 0;
+    while (s < order.size()) {
+      size_t e = s;
+      int64_t nmax = 0;
+      while (e < order.size() && key(order[e]) == key(order[s])) {
+        nmax = std::max(nmax, fs[order[e]]->n);
+        ++e;
+      }
+      launch_assemble_regular(L, d_ai.as<AsmInst>() + s, (int)(e - s), nmax, fs[order[s]]->kind,
+                              fs[order[s]]->fp32_regular);
+      s = e;
+    }
+  }
+  {
+    Prof pr(c, "near");
+    size_t s = 0;
+    while (s < order.size()) {
+      size_t e = s;
+      int64_t nmax = 0;
+      while (e < order.size() && fs[order[e]]->kind == fs[order[s]]->kind) {
+        nmax = std::max(nmax, fs[order[e]]->mesh->n_near);
+        ++e;
+      }
+      launch_assemble_near(L, d_ai.as<AsmInst>() + s, (int)(e - s), nmax, fs[order[s]]->kind);
+      s = e;
+    }
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  return BEMGPU_OK;
+}
+
+// ------------------------------------------------------------------ factorisation
+// zlacn2 (Higham 1988, LAPACK) reverse-communication state for one instance.
+struct Lacn2 {
+  int n = 0, kase = 0, isave1 = 0, isave2 = 0, isave3 = 0;
+  double est = 0.0;
+  std::vector<std::complex<double>> v;
+  static double sum1(const std::vector<std::complex<double>>& x) {
+    double s = 0.0;
+    for (auto& z : x) s += std::abs(z);
+    return s;
+  }
+  static int imax(const std::vector<std::complex<double>>& x) {
+    int b = 0;
+    double bv = -1.0;
+    for (int i = 0; i < (int)x.size(); ++i)
+      if (std::abs(x[i]) > bv) {
+        bv = std::abs(x[i]);
+        b = i;
+      }
+    return b;
+  }
+  static void normalise(std::vector<std::complex<double>>& x) {
+    const double safmin = 2.2250738585072014e-308;
+    for (auto& z : x) {
+      double a = std::abs(z);
+      z = a > safmin ? z / a : std::complex<double>(1.0, 0.0);
+    }
+  }
+  // One reverse-communication step: x in/out.  Returns kase (0 = done).
+  int step(std::vector<std::complex<double>>& x) {
+    const int itmax = 5;
+    if (kase == 0) {
+      for (auto& z : x) z = std::complex<double>(1.0 / n, 0.0);
+      kase = 1;
+      isave1 = 1;
+      return kase;
+    }
+    switch (isave1) {
+      case 1:
+        if (n == 1) {
+          v = x;
+          est = std::abs(v[0]);
+          kase = 0;
+          return 0;
+        }
+        est = sum1(x);
+        normalise(x);
+        kase = 2;
+        isave1 = 2;
+        return kase;
+      case 2:
+        isave2 = imax(x);
+        isave3 = 2;
+        goto main_loop;
+      case 3: {
+        v = x;
+        double estold = est;
+        est = sum1(v);
+        if (est <= estold) goto final_stage;
+        normalise(x);
+        kase = 2;
+        isave1 = 4;
+        return kase;
+      }
+      case 4: {
+        int jlast = isave2;
+        isave2 = imax(x);
+        if (std::abs(x[jlast]) != std::abs(x[isave2]) && isave3 < itmax) {
+          ++isave3;
+          goto main_loop;
+        }
+        goto final_stage;
+      }
+      case 5: {
+        double temp = 2.0 * (sum1(x) / (3.0 * n));
+        if (temp > est) {
+          v = x;
+          est = temp;
+        }
+        kase = 0;
+        return 0;
+      }
+    }
+  main_loop:
+    for (auto& z : x) z = 0.0;
+    x[isave2] = 1.0;
+    kase = 1;
+    isave1 = 3;
+    return kase;
+  final_stage : {
+    double alt = 1.0;
+    for (int i = 0; i < n; ++i) {
+      x[i] = std::complex<double>(alt * (1.0 + (double)i / (double)(n - 1)), 0.0);
+      alt = -alt;
+    }
+  }
+    kase = 1;
+    isave1 = 5;
+    return kase;
+  }
+};
+
+// Infinity-norm reciprocal condition of the complex64 factors (LAPACK cgecon('I'):
+// kase 2 applies (LU)^{-1}, kase 1 applies (LU)^{-H}; rcond = 1 / (anorm ||A^-1||)).
+int estimate_rcond(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
+  if (fs.empty()) return BEMGPU_OK;
+  const Launch L = c->launch();
+  const size_t F = fs.size();
+  std::vector<Lacn2> st(F);
+  std::vector<Buf> work(F);
+  std::vector<std::vector<std::complex<double>>> xs(F);
+  int64_t nmax = 0;
+  for (size_t t = 0; t < F; ++t) {
+    st[t].n = (int)fs[t]->N;
+    xs[t].assign((size_t)fs[t]->N, 0.0);
+    TRY(alloc(c, (size_t)fs[t]->N * 8, &work[t]));
+    nmax = std::max(nmax, fs[t]->N);
+  }
+  std::vector<int> kase(F);
+  for (size_t t = 0; t < F; ++t) kase[t] = st[t].step(xs[t]);
+  Buf d_mi;
+  std::vector<float> tmp;
+  for (int round = 0; round < 64; ++round) {
+    bool any = false;
+    for (int want : {1, 2}) {
+      std::vector<MatInst> mi;
+      std::vector<size_t> who;
+      for (size_t t = 0; t < F; ++t) {
+        if (kase[t] != want) continue;
+        tmp.resize(2 * xs[t].size());
+        for (size_t i = 0; i < xs[t].size(); ++i) {
+          tmp[2 * i] = (float)xs[t][i].real();
+          tmp[2 * i + 1] = (float)xs[t][i].imag();
+        }
+        CUDA_TRY(c, cudaMemcpyAsync(work[t].p, tmp.data(), tmp.size() * 4, cudaMemcpyHostToDevice,
+                                    c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        MatInst m{};
+        m.a = fs[t]->LU.p;
+        m.n = fs[t]->N;
+        m.lda = fs[t]->N;
+        m.ipiv = fs[t]->ipiv.as<int32_t>();
+        m.info = fs[t]->info.as<int32_t>();
+        m.x = work[t].p;
+        m.ldx = fs[t]->N;
+        m.nrhs = 1;
+        m.active = 1;
+        mi.push_back(m);
+        who.push_back(t);
+      }
+      if (mi.empty()) continue;
+      any = true;
+      TRY(to_device(c, mi, &d_mi));
+      {
+        Prof pr(c, "getrs");
+        launch_getrs(L, d_mi.as<MatInst>(), (int)mi.size(), nmax, 1, want == 1 ? 1 : 0, 1, 0);
+      }
+      for (size_t w : who) {
+        tmp.resize(2 * xs[w].size());
+        CUDA_TRY(c, cudaMemcpyAsync(tmp.data(), work[w].p, tmp.size() * 4, cudaMemcpyDeviceToHost,
+                                    c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        for (size_t i = 0; i < xs[w].size(); ++i)
+          xs[w][i] = std::complex<double>(tmp[2 * i], tmp[2 * i + 1]);
+        kase[w] = st[w].step(xs[w]);
+      }
+    }
+    if (!any) break;
+  }
+  for (size_t t = 0; t < F; ++t) {
+    double ainv = st[t].est;
+    fs[t]->rcond = (ainv != 0.0) ? (1.0 / ainv) / fs[t]->anorm : 0.0;
+  }
+  return BEMGPU_OK;
+}
+
+// LU of a batch of same-precision factors (prec 1: complex64 in LU, 0: complex128).
+int getrf_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, int prec, bool promoted) {
+  if (fs.empty()) return BEMGPU_OK;
+  const Launch L = c->launch();
+  std::vector<MatInst> mi(fs.size());
+  int64_t nmax = 0;
+  for (size_t t = 0; t < fs.size(); ++t) {
+    FactorData* f = fs[t];
+    MatInst& m = mi[t];
+    std::memset(&m, 0, sizeof m);
+    m.a = promoted ? f->LU64.p : f->LU.p;
+    m.n = f->N;
+    m.lda = f->N;
+    m.ipiv = promoted ? f->ipiv64.as<int32_t>() : f->ipiv.as<int32_t>();
+    m.info = promoted ? f->info64.as<int32_t>() : f->info.as<int32_t>();
+    m.active = 1;
+    CUDA_TRY(c, cudaMemsetAsync(m.info, 0, sizeof(int32_t), c->stream));
+    nmax = std::max(nmax, f->N);
+  }
+  Buf d;
+  TRY(to_device(c, mi, &d));
+  {
+    Prof pr(c, prec ? "getrf_c64" : "getrf_c128");
+    launch_getrf_simt(L, d.as<MatInst>(), (int)fs.size(), nmax, prec);
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  for (size_t t = 0; t < fs.size(); ++t) {
+    int32_t h = 0;
+    CUDA_TRY(c, cudaMemcpyAsync(&h, mi[t].info, 4, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    fs[t]->info_h = h;
+  }
+  return BEMGPU_OK;
+}
+
+// Scaled copy of A into a factor buffer (single -> LU as complex64, else complex128).
+int scale_copy_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, std::vector<Buf>& part,
+                     bool to_promoted, std::vector<int32_t>* flags) {
+  if (fs.empty()) return BEMGPU_OK;
+  const Launch L = c->launch();
+  std::vector<VecInst> vi(fs.size());
+  Buf d_flags, d_stats;
+  TRY(alloc(c, fs.size() * 4, &d_flags));
+  TRY(alloc(c, fs.size() * 2 * 8, &d_stats));
+  CUDA_TRY(c, cudaMemsetAsync(d_flags.p, 0, fs.size() * 4, c->stream));
+  int64_t nmax = 0;
+  for (size_t t = 0; t < fs.size(); ++t) {
+    FactorData* f = fs[t];
+    VecInst& v = vi[t];
+    std::memset(&v, 0, sizeof v);
+    v.A = f->A.p;
+    v.n = f->N;
+    v.lda = f->N;
+    v.rows = f->rows.as<double>();
+    v.cols = f->cols.as<double>();
+    v.rowsum = f->rowsum.as<double>();
+    v.part = part[t].as<double>();
+    v.out = to_promoted ? f->LU64.p : f->LU.p;
+    v.out_single = (!to_promoted && f->single) ? 1 : 0;
+    v.flag = d_flags.as<int32_t>() + t;
+    v.stats = d_stats.as<double>() + 2 * t;
+    nmax = std::max(nmax, f->N);
+  }
+  Buf d;
+  TRY(to_device(c, vi, &d));
+  {
+    Prof pr(c, "scale_copy");
+    launch_scale_copy(L, d.as<VecInst>(), (int)fs.size(), nmax);
+  }
+  std::vector<double> stats;
+  std::vector<int32_t> fl;
+  TRY(download(c, d_stats, &stats, fs.size() * 2));
+  TRY(download(c, d_flags, &fl, fs.size()));
+  for (size_t t = 0; t < fs.size(); ++t) {
+    fs[t]->matrix_norm = stats[2 * t];
+    if (!to_promoted) fs[t]->anorm = stats[2 * t + 1];
+  }
+  if (flags) *flags = fl;
+  return BEMGPU_OK;
+}
+
+int promote(bemgpu_ctx* c, std::vector<FactorData*>& fs, std::vector<Buf>& part) {
+  if (fs.empty()) return BEMGPU_OK;
+  for (FactorData* f : fs) {
+    f->LU.release();  // free the low-precision factor first (fluid_system.jl:186-190)
+    f->ipiv.release();
+    TRY(alloc(c, (size_t)f->N * f->N * 16, &f->LU64));
+    TRY(alloc(c, (size_t)f->N * 4, &f->ipiv64));
+    TRY(alloc(c, 4, &f->info64));
+    f->single = false;
+  }
+  TRY(scale_copy_batch(c, fs, part, true, nullptr));
+  TRY(getrf_batch(c, fs, 0, true));
+  for (FactorData* f : fs)
+    if (f->info_h > 0)
+      return fail(c, BEMGPU_ESINGULAR, "double-precision factor is exactly singular");
+  return BEMGPU_OK;
+}
+
+int factorize_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
+  const Launch L = c->launch();
+  std::vector<Buf> part(fs.size());
+  std::vector<VecInst> vi(fs.size());
+  int64_t nmax = 0;
+  for (size_t t = 0; t < fs.size(); ++t) {
+    FactorData* f = fs[t];
+    f->single = f->mixed;
+    f->reason = BEMGPU_REASON_NONE;
+    TRY(alloc(c, (size_t)f->N * 8, &f->rows));
+    TRY(alloc(c, (size_t)f->N * 8, &f->cols));
+    TRY(alloc(c, (size_t)f->N * 8, &f->rowsum));
+    TRY(alloc(c, (size_t)kChunks * f->N * 2 * 8, &part[t]));
+    TRY(alloc(c, (size_t)f->N * f->N * (f->single ? 8 : 16), &f->LU));
+    TRY(alloc(c, (size_t)f->N * 4, &f->ipiv));
+    TRY(alloc(c, 4, &f->info));
+    VecInst& v = vi[t];
+    std::memset(&v, 0, sizeof v);
+    v.A = f->A.p;
+    v.n = f->N;
+    v.lda = f->N;
+    v.rows = f->rows.as<double>();
+    v.cols = f->cols.as<double>();
+    v.rowsum = f->rowsum.as<double>();
+    v.part = part[t].as<double>();
+    nmax = std::max(nmax, f->N);
+  }
+  Buf d;
+  TRY(to_device(c, vi, &d));
+  {
+    Prof pr(c, "equilibrate");
+    launch_equilibrate(L, d.as<VecInst>(), (int)fs.size(), nmax);
+  }
+  for (FactorData* f : fs)
+    if (!f->prob.equilibrate) {
+      launch_fill(L, f->rows.as<double>(), f->N, 1.0);
+      launch_fill(L, f->cols.as<double>(), f->N, 1.0);
+    }
+  std::vector<int32_t> flags;
+  TRY(scale_copy_batch(c, fs, part, false, &flags));
+  std::vector<FactorData*> single, dbl, prom;
+  for (size_t t = 0; t < fs.size(); ++t) {
+    FactorData* f = fs[t];
+    if (f->single && flags[t]) {
+      f->reason = BEMGPU_REASON_CONVERSION;
+      prom.push_back(f);
+    } else if (f->single) {
+      single.push_back(f);
+    } else {
+      dbl.push_back(f);
+    }
+  }
+  TRY(getrf_batch(c, single, 1, false));
+  TRY(getrf_batch(c, dbl, 0, false));
+  for (FactorData* f : dbl)
+    if (f->info_h > 0)
+      return fail(c, BEMGPU_ESINGULAR, "double-precision factor is exactly singular");
+  std::vector<FactorData*> ok;
+  for (FactorData* f : single) {
+    if (f->info_h > 0) {
+      f->reason = BEMGPU_REASON_SINGLE_SINGULAR;
+      prom.push_back(f);
+    } else {
+      ok.push_back(f);
+    }
+  }
+  {
+    Prof pr(c, "gecon");
+    TRY(estimate_rcond(c, ok));
+  }
+  for (FactorData* f : ok)
+    if (!std::isfinite(f->rcond) || f->rcond <= f->prob.condition_guard) {
+      f->reason = BEMGPU_REASON_CONDITION;
+      prom.push_back(f);
+    }
+  // promotion needs the part scratch of each promoted instance
+  std::vector<Buf> ppart;
+  for (FactorData* f : prom) {
+    Buf b;
+    TRY(alloc(c, (size_t)kChunks * f->N * 2 * 8, &b));
+    ppart.push_back(std::move(b));
+  }
+  TRY(promote(c, prom, ppart));
+  return BEMGPU_OK;
+}
+
+int factor_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, bool assemble) {
+  Timer ta(c->stream);
+  if (assemble) TRY(assemble_batch(c, fs));
+  double asm_ms = ta.stop();
+  TRY(check_device_error(c));
+  Timer tf(c->stream);
+  TRY(factorize_batch(c, fs));
+  double fac_ms = tf.stop();
+  TRY(check_device_error(c));
+  for (FactorData* f : fs) {
+    f->assemble_ms = assemble ? asm_ms : 0.0;
+    f->factor_ms = fac_ms;
+  }
+  return BEMGPU_OK;
+}
+
+// ------------------------------------------------------------------ solve chain
+struct RhsState {
+  double previous = INFINITY;
+  int corrections = 0, attempts = 0, stalls = 0;
+  bool done = false, init = true;
+  double nw = INFINITY, cw = INFINITY;
+  int reason = BEMGPU_REASON_NONE;
+};
+
+struct SolveInst {
+  FactorData* f;
+  int32_t R;
+  Buf dirs, pinc, qinc, b, x, y, den, work, stats, part, active, changed, tmp;
+  std::vector<RhsState> rs;
+};
+
+void fill_vec(VecInst& v, SolveInst& s, const void* A, int64_t N) {
+  std::memset(&v, 0, sizeof v);
+  v.A = A;
+  v.n = N;
+  v.lda = N;
+  v.rows = s.f->rows.as<double>();
+  v.cols = s.f->cols.as<double>();
+  v.part = s.part.as<double>();
+  v.nrhs = s.R;
+  v.x = s.x.as<double>();
+  v.ldx = N;
+  v.b = s.b.as<double>();
+  v.ldb = N;
+  v.y = s.y.as<double>();
+  v.ldy = N;
+  v.den = s.den.as<double>();
+  v.stats = s.stats.as<double>();
+  v.active = s.active.as<int32_t>();
+  v.changed = s.changed.as<int32_t>();
+  v.out = s.work.p;
+  v.out_single = s.f->single ? 1 : 0;
+}
+
+// x (mode 0) or x += (mode 1) the scaled solve of the vectors in `src` (b or residual)
+// for the rhs flagged in `mask`; corrections go through the current factor precision.
+int correction_pass(bemgpu_ctx* c, std::vector<SolveInst*>& ss, bool from_b,
+                    const std::vector<std::vector<int32_t>>& mask, int mode) {
+  const Launch L = c->launch();
+  std::vector<VecInst> vi;
+  std::vector<SolveInst*> who;
+  for (size_t t = 0; t < ss.size(); ++t) {
+    bool any = false;
+    for (int32_t m : mask[t]) any |= (m != 0);
+    if (!any) continue;
+    SolveInst& s = *ss[t];
+    CUDA_TRY(c, cudaMemcpyAsync(s.active.p, mask[t].data(), mask[t].size() * 4,
+                                cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(s.changed.p, 0, (size_t)s.R * 4, c->stream));
+    VecInst v;
+    fill_vec(v, s, s.f->A.p, s.f->N);
+    if (from_b) v.y = s.b.as<double>();
+    vi.push_back(v);
+    who.push_back(&s);
+  }
+  if (who.empty()) return BEMGPU_OK;
+  Buf d;
+  TRY(to_device(c, vi, &d));
+  int64_t nmax = 0;
+  int32_t rmax = 0;
+  for (SolveInst* s : who) {
+    nmax = std::max(nmax, s->f->N);
+    rmax = std::max(rmax, s->R);
+  }
+  launch_corr_prep(L, d.as<VecInst>(), (int)vi.size(), nmax, rmax);
+  for (int prec : {1, 0}) {
+    std::vector<MatInst> mi;
+    int64_t pn = 0;
+    int32_t pr = 0;
+    for (SolveInst* s : who) {
+      if ((s->f->single ? 1 : 0) != prec) continue;
+      MatInst m{};
+      m.a = s->f->factor_ptr();
+      m.n = s->f->N;
+      m.lda = s->f->N;
+      m.ipiv = s->f->ipiv_ptr();
+      m.info = s->f->info_ptr();
+      m.x = s->work.p;
+      m.ldx = s->f->N;
+      m.nrhs = s->R;
+      m.active = 1;
+      mi.push_back(m);
+      pn = std::max(pn, s->f->N);
+      pr = std::max(pr, s->R);
+    }
+    if (mi.empty()) continue;
+    Buf dm;
+    TRY(to_device(c, mi, &dm));
+    Prof p(c, "getrs");
+    launch_getrs(L, dm.as<MatInst>(), (int)mi.size(), pn, pr, 0, prec, 1);
+  }
+  launch_corr_apply(L, d.as<VecInst>(), (int)vi.size(), nmax, rmax, mode);
+  CUDA_TRY(c, cudaGetLastError());
+  return BEMGPU_OK;
+}
+
+// residual y = b - A x, den, statistics for all rhs of the given instances
+int residual_pass(bemgpu_ctx* c, std::vector<SolveInst*>& ss,
+                  std::vector<std::vector<double>>* stats) {
+  const Launch L = c->launch();
+  std::vector<VecInst> vi(ss.size());
+  int64_t nmax = 0;
+  int32_t rmax = 0;
+  for (size_t t = 0; t < ss.size(); ++t) {
+    fill_vec(vi[t], *ss[t], ss[t]->f->A.p, ss[t]->f->N);
+    nmax = std::max(nmax, ss[t]->f->N);
+    rmax = std::max(rmax, ss[t]->R);
+  }
+  Buf d;
+  TRY(to_device(c, vi, &d));
+  {
+    Prof p(c, "residual");
+    launch_gemv(L, d.as<VecInst>(), (int)vi.size(), nmax, rmax, 1);
+    launch_resid_stats(L, d.as<VecInst>(), (int)vi.size(), rmax);
+  }
+  stats->resize(ss.size());
+  for (size_t t = 0; t < ss.size(); ++t)
+    TRY(download(c, ss[t]->stats, &(*stats)[t], (size_t)ss[t]->R * kStats));
+  return BEMGPU_OK;
+}
+
+void normwise(const double* st, double matrix_norm, double* nw, double* cw) {
+  if (st[8] != 0.0) {
+    *nw = *cw = INFINITY;
+    return;
+  }
+  const double rn = st[0], xn = st[2], bn = st[3];
+  const double scale = matrix_norm * xn + bn;
+  if (!std::isfinite(scale))
+    *nw = INFINITY;
+  else if (scale == 0.0)
+    *nw = rn == 0.0 ? 0.0 : INFINITY;
+  else
+    *nw = rn / scale;
+  *cw = st[1];
+}
+
+int solve_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<int32_t>& nrhs,
+                const std::vector<const double*>& incidence, std::vector<SolutionData*>& out) {
+  const Launch L = c->launch();
+  Timer tsolve(c->stream);
+  const size_t F = fs.size();
+  std::vector<SolveInst> si(F);
+  std::vector<WaveInst> wi(F);
+  int64_t nmax = 0;
+  int32_t rmax = 0;
+  for (size_t t = 0; t < F; ++t) {
+    FactorData* f = fs[t];
+    SolveInst& s = si[t];
+    s.f = f;
+    s.R = nrhs[t];
+    if (s.R <= 0) return fail(c, BEMGPU_EINVAL, "nrhs must be positive");
+    std::vector<double> dirs(3 * (size_t)s.R);
+    for (int r = 0; r < s.R; ++r) {
+      const double be = incidence[t][2 * r], al = incidence[t][2 * r + 1];
+      if (!(std::isfinite(be) && std::isfinite(al)))
+        return fail(c, BEMGPU_EINVAL, "incidence angles must be finite");
+      dirs[3 * r] = std::cos(be);
+      dirs[3 * r + 1] = std::sin(be) * std::cos(al);
+      dirs[3 * r + 2] = std::sin(be) * std::sin(al);
+    }
+    out[t]->dirs = dirs;
+    const int64_t n = f->n, N = f->N;
+    TRY(upload(c, dirs, &s.dirs));
+    TRY(alloc(c, (size_t)n * s.R * 16, &s.pinc));
+    TRY(alloc(c, (size_t)n * s.R * 16, &s.qinc));
+    TRY(alloc(c, (size_t)N * s.R * 16, &s.b));
+    TRY(alloc(c, (size_t)N * s.R * 16, &s.x));
+    TRY(alloc(c, (size_t)N * s.R * 16, &s.y));
+    TRY(alloc(c, (size_t)N * s.R * 8, &s.den));
+    TRY(alloc(c, (size_t)N * s.R * 16, &s.work));
+    TRY(alloc(c, (size_t)kStats * s.R * 8, &s.stats));
+    TRY(alloc(c, (size_t)std::max<int64_t>(kChunks * (int64_t)s.R * N * 3, kChunks * N * 2) * 8,
+              &s.part));
+    TRY(alloc(c, (size_t)s.R * 4, &s.active));
+    TRY(alloc(c, (size_t)s.R * 4, &s.changed));
+    TRY(alloc(c, (size_t)n * s.R * 16, &out[t]->ps));
+    TRY(alloc(c, (size_t)n * s.R * 16, &out[t]->qs));
+    s.rs.assign((size_t)s.R, RhsState{});
+    WaveInst& w = wi[t];
+    std::memset(&w, 0, sizeof w);
+    w.panels = f->mesh->panels.as<double>();
+    w.n = n;
+    w.k = f->prob.k;
+    w.nrhs = s.R;
+    w.dirs = s.dirs.as<double>();
+    w.p = s.pinc.as<double>();
+    w.q = s.qinc.as<double>();
+    w.ldp = n;
+    nmax = std::max(nmax, N);
+    rmax = std::max(rmax, s.R);
+  }
+  Buf d_wi;
+  TRY(to_device(c, wi, &d_wi));
+  {
+    Prof p(c, "incident");
+    launch_incident(L, d_wi.as<WaveInst>(), (int)F, nmax, rmax);
+  }
+  // ---- forcing b
+  {
+    std::vector<VecInst> gv;  // products with a matrix
+    std::vector<TraceInst> stack, cbie;
+    for (size_t t = 0; t < F; ++t) {
+      SolveInst& s = si[t];
+      FactorData* f = s.f;
+      if (f->kind == kAsmBM || f->kind == kAsmCBIE) {
+        VecInst v;
+        fill_vec(v, s, f->Mrhs.p, f->n);
+        v.x = f->rhs_is_m2 ? s.qinc.as<double>() : s.pinc.as<double>();
+        v.ldx = f->n;
+        v.y = s.b.as<double>();
+        v.ldy = f->N;
+        gv.push_back(v);
+      } else {
+        TraceInst tr{};
+        tr.pinc = s.pinc.as<double>();
+        tr.qinc = s.qinc.as<double>();
+        tr.n = f->n;
+        tr.nrhs = s.R;
+        tr.ps = f->kind == kAsmMuller ? s.b.as<double>() : s.x.as<double>();
+        stack.push_back(tr);
+        if (f->kind == kAsmFluidCBIE) {
+          VecInst v;
+          fill_vec(v, s, f->A.p, f->N);
+          v.x = s.x.as<double>();
+          v.y = s.y.as<double>();
+          gv.push_back(v);
+          TraceInst cb{};
+          cb.x = s.y.as<double>();
+          cb.n = f->n;
+          cb.nrhs = s.R;
+          cb.ps = s.b.as<double>();
+          cbie.push_back(cb);
+        }
+      }
+    }
+    Prof p(c, "forcing");
+    Buf d1, d2, d3;
+    if (!stack.empty()) {
+      TRY(to_device(c, stack, &d1));
+      launch_stack(L, d1.as<TraceInst>(), (int)stack.size(), nmax, rmax);
+    }
+    if (!gv.empty()) {
+      TRY(to_device(c, gv, &d2));
+      launch_gemv(L, d2.as<VecInst>(), (int)gv.size(), nmax, rmax, 0);
+    }
+    if (!cbie.empty()) {
+      TRY(to_device(c, cbie, &d3));
+      launch_cbie_forcing(L, d3.as<TraceInst>(), (int)cbie.size(), nmax, rmax);
+    }
+  }
+  // ---- solve / refine
+  std::vector<SolveInst*> all;
+  for (auto& s : si) all.push_back(&s);
+  std::vector<std::vector<int32_t>> mask(F);
+  for (size_t t = 0; t < F; ++t) mask[t].assign((size_t)si[t].R, 1);
+  TRY(correction_pass(c, all, true, mask, 0));
+  for (auto& s : si)
+    for (auto& r : s.rs) r.init = false;
+  const int kMaxRounds = 64;
+  for (int round = 0; round < kMaxRounds; ++round) {
+    std::vector<SolveInst*> pend;
+    for (auto& s : si)
+      if (s.f->mixed)
+        for (auto& r : s.rs)
+          if (!r.done) {
+            pend.push_back(&s);
+            break;
+          }
+    if (pend.empty()) break;
+    std::vector<std::vector<double>> st;
+    TRY(residual_pass(c, pend, &st));
+    std::vector<FactorData*> to_promote;
+    std::vector<std::vector<int32_t>> init_mask(pend.size()), corr_mask(pend.size());
+    for (size_t t = 0; t < pend.size(); ++t) {
+      SolveInst& s = *pend[t];
+      init_mask[t].assign((size_t)s.R, 0);
+      corr_mask[t].assign((size_t)s.R, 0);
+      bool promote_me = false;
+      for (int r = 0; r < s.R; ++r) {
+        RhsState& q = s.rs[r];
+        if (q.done) continue;
+        double nw, cw;
+        normwise(&st[t][(size_t)r * kStats], s.f->matrix_norm, &nw, &cw);
+        q.nw = nw;
+        q.cw = cw;
+        const double metric = std::max(nw, cw);
+        if (std::isfinite(metric) && metric <= s.f->prob.refine_tolerance) {
+          q.done = true;
+          continue;
+        }
+        q.stalls = metric >= q.previous * 0.9 ? q.stalls + 1 : 0;
+        int reason = !std::isfinite(metric) ? BEMGPU_REASON_NONFINITE
+                     : q.attempts >= s.f->prob.refine_maxiter ? BEMGPU_REASON_ITERATION_LIMIT
+                     : q.stalls >= 2 ? BEMGPU_REASON_STAGNATION
+                                     : BEMGPU_REASON_NONE;
+        if (reason != BEMGPU_REASON_NONE) {
+          if (!s.f->single)
+            return fail(c, BEMGPU_ENOTCONVERGED,
+                        "double-precision fallback failed backward-error acceptance");
+          if (!promote_me) s.f->reason = reason;
+          promote_me = true;
+          q.previous = INFINITY;
+          q.attempts = 0;
+          q.stalls = 0;
+          init_mask[t][r] = 1;
+        } else {
+          corr_mask[t][r] = 1;
+          q.previous = metric;
+        }
+      }
+      if (promote_me) to_promote.push_back(s.f);
+    }
+    if (!to_promote.empty()) {
+      std::vector<Buf> ppart;
+      for (FactorData* f : to_promote) {
+        Buf b;
+        TRY(alloc(c, (size_t)kChunks * f->N * 2 * 8, &b));
+        ppart.push_back(std::move(b));
+      }
+      TRY(promote(c, to_promote, ppart));
+    }
+    TRY(correction_pass(c, pend, true, init_mask, 0));
+    TRY(correction_pass(c, pend, false, corr_mask, 1));
+    // stagnation check on the corrected rhs
+    for (size_t t = 0; t < pend.size(); ++t) {
+      SolveInst& s = *pend[t];
+      bool anyc = false;
+      for (int32_t m : corr_mask[t]) anyc |= m != 0;
+      if (!anyc) continue;
+      std::vector<int32_t> ch;
+      TRY(download(c, s.changed, &ch, (size_t)s.R));
+      std::vector<FactorData*> stag;
+      std::vector<int32_t> redo((size_t)s.R, 0);
+      for (int r = 0; r < s.R; ++r) {
+        if (!corr_mask[t][r]) continue;
+        RhsState& q = s.rs[r];
+        if (!ch[r]) {
+          if (!s.f->single)
+            return fail(c, BEMGPU_ENOTCONVERGED, "double-precision correction stagnated");
+          if (stag.empty()) stag.push_back(s.f);
+          s.f->reason = BEMGPU_REASON_STAGNATION;
+          q.previous = INFINITY;
+          q.attempts = 0;
+          q.stalls = 0;
+          redo[r] = 1;
+        } else {
+          q.corrections++;
+          q.attempts++;
+        }
+      }
+      if (!stag.empty()) {
+        std::vector<Buf> ppart;
+        Buf b;
+        TRY(alloc(c, (size_t)kChunks * s.f->N * 2 * 8, &b));
+        ppart.push_back(std::move(b));
+        TRY(promote(c, stag, ppart));
+        std::vector<SolveInst*> one{&s};
+        std::vector<std::vector<int32_t>> m1{redo};
+        TRY(correction_pass(c, one, true, m1, 0));
+      }
+    }
+    if (round == kMaxRounds - 1)
+      return fail(c, BEMGPU_ENOTCONVERGED, "refinement did not terminate");
+  }
+  // ---- traces and residual diagnostics
+  {
+    std::vector<TraceInst> ti(F);
+    int64_t n_max = 0;
+    for (size_t t = 0; t < F; ++t) {
+      SolveInst& s = si[t];
+      TraceInst& tr = ti[t];
+      std::memset(&tr, 0, sizeof tr);
+      tr.x = s.x.as<double>();
+      tr.ldx = s.f->N;
+      tr.pinc = s.pinc.as<double>();
+      tr.qinc = s.qinc.as<double>();
+      tr.n = s.f->n;
+      tr.ps = out[t]->ps.as<double>();
+      tr.qs = out[t]->qs.as<double>();
+      tr.nrhs = s.R;
+      tr.kind = s.f->kind == kAsmMuller ? 2
+                : s.f->kind == kAsmFluidCBIE ? 3
+                : (s.f->prob.boundary == BEMGPU_RIGID ? 0 : 1);
+      n_max = std::max(n_max, s.f->n);
+    }
+    Buf d;
+    TRY(to_device(c, ti, &d));
+    launch_traces(L, d.as<TraceInst>(), (int)F, n_max, rmax);
+  }
+  std::vector<std::vector<double>> st;
+  TRY(residual_pass(c, all, &st));
+  double solve_ms = tsolve.stop();
+  TRY(check_device_error(c));
+  for (size_t t = 0; t < F; ++t) {
+    SolveInst& s = si[t];
+    FactorData* f = s.f;
+    bemgpu_diagnostics& dg = out[t]->diag;
+    std::memset(&dg, 0, sizeof dg);
+    dg.unknown_count = f->N;
+    dg.quadrature_nodes = f->n;
+    dg.near_pairs = f->mesh ? f->mesh->n_near : 0;
+    dg.formulation = formulation_of(f->kind);
+    dg.precision = f->prob.precision;
+    dg.factor_precision = f->single ? 0 : 1;
+    dg.refinement_reason = f->reason;
+    dg.equilibrate = f->prob.equilibrate;
+    dg.coupling_re = 0.0;
+    dg.coupling_im = f->kind == kAsmBM ? 1.0 / f->prob.k : 0.0;
+    dg.single_reciprocal_condition = f->rcond;
+    dg.assemble_ms = f->assemble_ms;
+    dg.factor_ms = f->factor_ms;
+    dg.solve_ms = solve_ms;
+    dg.total_ms = f->assemble_ms + f->factor_ms + solve_ms;
+    dg.device_bytes = (int64_t)f->bytes();
+    dg.nrhs = s.R;
+    dg.info = f->info_h;
+    for (int r = 0; r < s.R; ++r) {
+      const double* q = &st[t][(size_t)r * kStats];
+      double an = std::sqrt(q[4]), bn = std::sqrt(q[5]);
+      double rel = bn == 0.0 ? (an == 0.0 ? 0.0 : INFINITY) : an / bn;
+      double san = std::sqrt(q[6]), sbn = std::sqrt(q[7]);
+      double srel = sbn == 0.0 ? (san == 0.0 ? 0.0 : INFINITY) : san / sbn;
+      double nw, cw;
+      normwise(q, f->matrix_norm, &nw, &cw);
+      dg.absolute_residual = std::max(dg.absolute_residual, an);
+      dg.relative_residual = std::max(dg.relative_residual, rel);
+      dg.scaled_absolute_residual = std::max(dg.scaled_absolute_residual, san);
+      dg.scaled_relative_residual = std::max(dg.scaled_relative_residual, srel);
+      dg.normwise_backward_error = std::max(dg.normwise_backward_error, nw);
+      dg.componentwise_backward_error = std::max(dg.componentwise_backward_error, cw);
+      dg.refinement_iterations = std::max(dg.refinement_iterations, s.rs[r].corrections);
+    }
+    out[t]->nrhs = s.R;
+    out[t]->mesh = f->mesh;
+    out[t]->k = f->prob.k;
+    out[t]->boundary = f->prob.boundary;
+    out[t]->g = f->prob.density_contrast;
+    out[t]->h = f->prob.soundspeed_contrast;
+  }
+  return BEMGPU_OK;
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+extern "C" {
+
+const char* bemgpu_version(void) { return "bemgpu 0.1.0 (sm_103a)"; }
+
+const char* bemgpu_status_string(int s) {
+  switch (s) {
+    case BEMGPU_OK: return "ok";
+    case BEMGPU_EINVAL: return "invalid argument";
+    case BEMGPU_ETOPOLOGY: return "invalid surface topology";
+    case BEMGPU_ENOMEM_BUDGET: return "HBM budget exceeded";
+    case BEMGPU_ESINGULAR: return "singular matrix";
+    case BEMGPU_ENOTCONVERGED: return "refinement did not converge";
+    case BEMGPU_ETIMEOUT: return "device wait timed out";
+    case BEMGPU_ECUDA: return "CUDA error";
+    case BEMGPU_ENODEV: return "no CUDA device";
+    case BEMGPU_EBUSY: return "busy";
+    default: return "unknown status";
+  }
+}
+
+void bemgpu_problem_init(bemgpu_problem* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof *p);
+  p->boundary = BEMGPU_RIGID;
+  p->formulation = BEMGPU_FORMULATION_DEFAULT;
+  p->precision = BEMGPU_DOUBLE;
+  p->equilibrate = 1;
+  p->k = 1.0;
+  p->density_contrast = 1.0;
+  p->soundspeed_contrast = 1.0;
+  p->refine_tolerance = 1e-13;
+  p->refine_maxiter = 8;
+  p->condition_guard = 10.0 * 1.1920928955078125e-07;
+  p->near_eta = 2.0;
+}
+
+int bemgpu_mesh_validate(const double* nodes, int64_t n_nodes, const int64_t* triangles,
+                         int64_t n_triangles, double* resolution, char* err, size_t errlen) {
+  std::string e;
+  int s = validate_surface(nodes, n_nodes, triangles, n_triangles, resolution, &e);
+  if (err && errlen) {
+    std::snprintf(err, errlen, "%s", e.c_str());
+  }
+  if (s != BEMGPU_OK) g_err = e;
+  return s;
+}
+
+int bemgpu_mesh_hash(const double* nodes, int64_t n_nodes, const int64_t* triangles,
+                     int64_t n_triangles, char out_hex[65]) {
+  if (!nodes || !triangles || !out_hex || n_nodes < 0 || n_triangles < 0)
+    return fail(nullptr, BEMGPU_EINVAL, "null argument");
+  mesh_hash(nodes, n_nodes, triangles, n_triangles, out_hex);
+  return BEMGPU_OK;
+}
+
+int bemgpu_near_pairs(const double* nodes, int64_t n_nodes, const int64_t* triangles,
+                      int64_t n_triangles, double eta, int64_t* rowptr, int64_t* cols,
+                      int64_t cap, int64_t* count) {
+  std::string e;
+  double res;
+  int s = validate_surface(nodes, n_nodes, triangles, n_triangles, &res, &e);
+  if (s != BEMGPU_OK) return fail(nullptr, s, e);
+  std::vector<double> cent, diam;
+  panel_centroids(nodes, triangles, n_triangles, &cent, &diam);
+  std::vector<int64_t> rp, cl;
+  near_pairs(cent, diam, eta, &rp, &cl);
+  if (count) *count = (int64_t)cl.size();
+  if ((int64_t)cl.size() > cap) return fail(nullptr, BEMGPU_EINVAL, "capacity too small");
+  if (rowptr) std::copy(rp.begin(), rp.end(), rowptr);
+  if (cols) std::copy(cl.begin(), cl.end(), cols);
+  return BEMGPU_OK;
+}
+
+int bemgpu_ctx_create(int device, uint64_t hbm_budget_bytes, bemgpu_ctx** out) {
+  if (!out) return fail(nullptr, BEMGPU_EINVAL, "null output");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return fail(nullptr, BEMGPU_ENODEV, "no CUDA device available");
+  }
+  if (device < 0 || device >= count) return fail(nullptr, BEMGPU_EINVAL, "invalid device index");
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+  auto* c = new bemgpu_ctx();
+  c->device = device;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_fail(nullptr, e, "cudaStreamCreate");
+  }
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  c->budget = hbm_budget_bytes ? hbm_budget_bytes : (uint64_t)(0.9 * (double)fr);
+  e = cudaMalloc(&c->d_err, sizeof(int));
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return cuda_fail(nullptr, e, "cudaMalloc");
+  }
+  cudaMemset(c->d_err, 0, sizeof(int));
+  cudaDeviceSynchronize();
+  *out = c;
+  return BEMGPU_OK;
+}
+
+int bemgpu_ctx_destroy(bemgpu_ctx* c) {
+  if (!c) return BEMGPU_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->events)
+    for (auto& pr : kv.second) {
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+  drop_cache(c);
+  cudaFree(c->d_err);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return BEMGPU_OK;
+}
+
+int bemgpu_last_error(const bemgpu_ctx* c, char* buf, size_t len) {
+  if (!buf || !len) return BEMGPU_EINVAL;
+  std::snprintf(buf, len, "%s", c ? c->err.c_str() : g_err.c_str());
+  return BEMGPU_OK;
+}
+
+int bemgpu_ctx_memory(const bemgpu_ctx* c, uint64_t* used, uint64_t* budget) {
+  if (!c) return fail(nullptr, BEMGPU_EINVAL, "null context");
+  if (used) *used = c->live;
+  if (budget) *budget = c->budget;
+  return BEMGPU_OK;
+}
+
+int bemgpu_ctx_synchronize(bemgpu_ctx* c) {
+  if (!c) return fail(nullptr, BEMGPU_EINVAL, "null context");
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return BEMGPU_OK;
+}
+
+int bemgpu_mesh_upload(bemgpu_ctx* c, const double* nodes, int64_t n_nodes,
+                       const int64_t* triangles, int64_t n_triangles, bemgpu_mesh** out) {
+  if (!c || !out) return fail(c, BEMGPU_EINVAL, "null argument");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  std::shared_ptr<MeshData> m;
+  TRY(make_mesh(c, nodes, n_nodes, triangles, n_triangles, 2.0, &m));
+  *out = new bemgpu_mesh{m};
+  return BEMGPU_OK;
+}
+
+int bemgpu_mesh_info(const bemgpu_mesh* m, int64_t* n_panels, double* resolution,
+                     char hash_hex[65]) {
+  if (!m) return fail(nullptr, BEMGPU_EINVAL, "null mesh");
+  if (n_panels) *n_panels = m->d->n;
+  if (resolution) *resolution = m->d->resolution;
+  if (hash_hex) std::memcpy(hash_hex, m->d->hash, 65);
+  return BEMGPU_OK;
+}
+
+int bemgpu_mesh_destroy(bemgpu_mesh* m) {
+  if (m) {
+    std::lock_guard<std::recursive_mutex> lk(m->d->c->mu);
+    delete m;
+  }
+  return BEMGPU_OK;
+}
+
+int bemgpu_factor_create_batch(bemgpu_ctx* c, int32_t count, const bemgpu_mesh* const* meshes,
+                               const bemgpu_problem* problems, bemgpu_factor** factors) {
+  if (!c || !meshes || !problems || !factors || count <= 0)
+    return fail(c, BEMGPU_EINVAL, "invalid batch arguments");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  std::vector<std::shared_ptr<FactorData>> own;
+  std::vector<FactorData*> fs;
+  for (int32_t t = 0; t < count; ++t) {
+    if (!meshes[t]) return fail(c, BEMGPU_EINVAL, "null mesh");
+    int kind = 0;
+    TRY(check_problem(c, problems[t], &kind));
+    auto f = std::make_shared<FactorData>();
+    f->c = c;
+    f->mesh = meshes[t]->d;
+    f->prob = problems[t];
+    f->kind = kind;
+    f->mixed = problems[t].precision == BEMGPU_MIXED;
+    f->fp32_regular = problems[t].assembly == BEMGPU_ASSEMBLY_SINGLE ||
+                      (problems[t].assembly == BEMGPU_ASSEMBLY_DEFAULT && f->mixed);
+    // near pairs are a mesh property; a different eta rebuilds them once
+    if (std::fabs(f->prob.near_eta - f->mesh->eta) > 0) {
+      return fail(c, BEMGPU_EINVAL, "near_eta differs from the mesh's (upload with that eta)");
+    }
+    own.push_back(f);
+    fs.push_back(f.get());
+  }
+  TRY(factor_batch(c, fs, true));
+  for (int32_t t = 0; t < count; ++t) factors[t] = new bemgpu_factor{own[t]};
+  return BEMGPU_OK;
+}
+
+int bemgpu_factor_create(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_problem* problem,
+                         bemgpu_factor** factor) {
+  return bemgpu_factor_create_batch(c, 1, &mesh, problem, factor);
+}
+
+int bemgpu_factor_solve_batch(bemgpu_ctx* c, int32_t count, bemgpu_factor* const* factors,
+                              const int32_t* nrhs, const double* const* incidence,
+                              bemgpu_solution** solutions) {
+  if (!c || !factors || !nrhs || !incidence || !solutions || count <= 0)
+    return fail(c, BEMGPU_EINVAL, "invalid batch arguments");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  std::vector<FactorData*> fs;
+  std::vector<int32_t> nr;
+  std::vector<const double*> inc;
+  std::vector<std::shared_ptr<SolutionData>> own;
+  std::vector<SolutionData*> outs;
+  for (int32_t t = 0; t < count; ++t) {
+    if (!factors[t] || !incidence[t]) return fail(c, BEMGPU_EINVAL, "null factor or incidence");
+    if (!factors[t]->d->mesh) return fail(c, BEMGPU_EINVAL, "factor has no mesh");
+    fs.push_back(factors[t]->d.get());
+    nr.push_back(nrhs[t]);
+    inc.push_back(incidence[t]);
+    auto s = std::make_shared<SolutionData>();
+    s->c = c;
+    own.push_back(s);
+    outs.push_back(s.get());
+  }
+  TRY(solve_batch(c, fs, nr, inc, outs));
+  for (int32_t t = 0; t < count; ++t) solutions[t] = new bemgpu_solution{own[t]};
+  return BEMGPU_OK;
+}
+
+int bemgpu_factor_solve(bemgpu_factor* f, int32_t nrhs, const double* incidence,
+                        bemgpu_solution** solution) {
+  if (!f) return fail(nullptr, BEMGPU_EINVAL, "null factor");
+  return bemgpu_factor_solve_batch(f->d->c, 1, &f, &nrhs, &incidence, solution);
+}
+
+int bemgpu_factor_destroy(bemgpu_factor* f) {
+  if (f) {
+    std::lock_guard<std::recursive_mutex> lk(f->d->c->mu);
+    delete f;
+  }
+  return BEMGPU_OK;
+}
+
+int bemgpu_factor_diagnostics(const bemgpu_factor* f, bemgpu_diagnostics* out) {
+  if (!f || !out) return fail(nullptr, BEMGPU_EINVAL, "null argument");
+  const FactorData* d = f->d.get();
+  std::memset(out, 0, sizeof *out);
+  out->unknown_count = d->N;
+  out->quadrature_nodes = d->n;
+  out->near_pairs = d->mesh ? d->mesh->n_near : 0;
+  out->formulation = formulation_of(d->kind);
+  out->precision = d->prob.precision;
+  out->factor_precision = d->single ? 0 : 1;
+  out->refinement_reason = d->reason;
+  out->equilibrate = d->prob.equilibrate;
+  out->coupling_im = d->kind == kAsmBM ? 1.0 / d->prob.k : 0.0;
+  out->single_reciprocal_condition = d->rcond;
+  out->assemble_ms = d->assemble_ms;
+  out->factor_ms = d->factor_ms;
+  out->device_bytes = (int64_t)d->bytes();
+  out->info = d->info_h;
+  return BEMGPU_OK;
+}
+
+int bemgpu_solve(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_problem* problem,
+                 int32_t nrhs, const double* incidence, bemgpu_solution** solution) {
+  bemgpu_factor* f = nullptr;
+  TRY(bemgpu_factor_create(c, mesh, problem, &f));
+  int s = bemgpu_factor_solve(f, nrhs, incidence, solution);
+  bemgpu_factor_destroy(f);
+  return s;
+}
+
+int bemgpu_far_field(bemgpu_solution* sol, int32_t rhs, int64_t ndir, const double* dirs,
+                     double* out) {
+  if (!sol || !out) return fail(nullptr, BEMGPU_EINVAL, "null argument");
+  SolutionData* s = sol->d.get();
+  bemgpu_ctx* c = s->c;
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  if (rhs < 0 || rhs >= s->nrhs) return fail(c, BEMGPU_EINVAL, "rhs index out of range");
+  std::vector<double> d;
+  if (!dirs) {
+    ndir = 1;
+    d = {-s->dirs[3 * rhs], -s->dirs[3 * rhs + 1], -s->dirs[3 * rhs + 2]};
+  } else {
+    if (ndir < 0) return fail(c, BEMGPU_EINVAL, "ndir must be nonnegative");
+    d.assign(dirs, dirs + 3 * ndir);
+    for (int64_t i = 0; i < ndir; ++i) {
+      double a = d[3 * i], b = d[3 * i + 1], e = d[3 * i + 2];
+      double nr = std::sqrt(a * a + b * b + e * e);
+      if (!(std::isfinite(nr) && std::fabs(nr - 1.0) < 1e-8))
+        return fail(c, BEMGPU_EINVAL, "direction must be a finite unit vector with three components");
+    }
+  }
+  if (ndir == 0) return BEMGPU_OK;
+  Buf dd, dout, dw;
+  TRY(upload(c, d, &dd));
+  TRY(alloc(c, (size_t)ndir * 16, &dout));
+  WaveInst w{};
+  w.panels = s->mesh->panels.as<double>();
+  w.n = s->mesh->n;
+  w.k = s->k;
+  w.nrhs = 1;
+  w.ndir = (int32_t)ndir;
+  w.dirs = dd.as<double>();
+  w.p = s->ps.as<double>() + 2 * (size_t)s->mesh->n * rhs;
+  w.q = s->qs.as<double>() + 2 * (size_t)s->mesh->n * rhs;
+  w.out = dout.as<double>();
+  w.ldp = s->mesh->n;
+  std::vector<WaveInst> wv{w};
+  TRY(upload(c, wv, &dw));
+  {
+    Prof p(c, "far_field");
+    launch_far_field(c->launch(), dw.as<WaveInst>(), 1, 1, (int32_t)ndir);
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  CUDA_TRY(c, cudaMemcpyAsync(out, dout.p, (size_t)ndir * 16, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return BEMGPU_OK;
+}
+
+int bemgpu_target_strength(bemgpu_solution* sol, int32_t rhs, int64_t ndir, const double* dirs,
+                           double* out) {
+  if (!out) return fail(nullptr, BEMGPU_EINVAL, "null output");
+  int64_t nd = dirs ? ndir : 1;
+  std::vector<double> f((size_t)std::max<int64_t>(nd, 0) * 2);
+  TRY(bemgpu_far_field(sol, rhs, ndir, dirs, f.data()));
+  for (int64_t i = 0; i < nd; ++i) out[i] = 20.0 * std::log10(std::hypot(f[2 * i], f[2 * i + 1]));
+  return BEMGPU_OK;
+}
+
+int bemgpu_traces(const bemgpu_solution* sol, int32_t rhs, double* p, double* q) {
+  if (!sol) return fail(nullptr, BEMGPU_EINVAL, "null solution");
+  SolutionData* s = sol->d.get();
+  bemgpu_ctx* c = s->c;
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  if (rhs < 0 || rhs >= s->nrhs) return fail(c, BEMGPU_EINVAL, "rhs index out of range");
+  const size_t n = (size_t)s->mesh->n;
+  if (p)
+    CUDA_TRY(c, cudaMemcpyAsync(p, s->ps.as<double>() + 2 * n * rhs, n * 16, cudaMemcpyDeviceToHost,
+                                c->stream));
+  if (q)
+    CUDA_TRY(c, cudaMemcpyAsync(q, s->qs.as<double>() + 2 * n * rhs, n * 16, cudaMemcpyDeviceToHost,
+                                c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return BEMGPU_OK;
+}
+
+int bemgpu_solution_diagnostics(const bemgpu_solution* sol, bemgpu_diagnostics* out) {
+  if (!sol || !out) return fail(nullptr, BEMGPU_EINVAL, "null argument");
+  *out = sol->d->diag;
+  return BEMGPU_OK;
+}
+
+int bemgpu_solution_destroy(bemgpu_solution* sol) {
+  if (sol) {
+    std::lock_guard<std::recursive_mutex> lk(sol->d->c->mu);
+    delete sol;
+  }
+  return BEMGPU_OK;
+}
+
+int bemgpu_pressure(bemgpu_solution* sol, int32_t rhs, int64_t npts, const double* points,
+                    int32_t field, double* out) {
+  (void)rhs;
+  (void)npts;
+  (void)points;
+  (void)field;
+  (void)out;
+  if (!sol) return fail(nullptr, BEMGPU_EINVAL, "null solution");
+  return fail(sol->d->c, BEMGPU_EINVAL, "pressure evaluation is not available in this build");
+}
+
+int bemgpu_dense_solve(bemgpu_ctx* c, int64_t n, const double* A, int32_t nrhs, double* B,
+                       int32_t precision, int32_t equilibrate, double refine_tolerance,
+                       int32_t refine_maxiter, double condition_guard,
+                       bemgpu_diagnostics* diag) {
+  if (!c || !A || !B || n <= 0 || nrhs <= 0) return fail(c, BEMGPU_EINVAL, "invalid arguments");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  for (int64_t i = 0; i < 2 * n * n; ++i)
+    if (!std::isfinite(A[i])) return fail(c, BEMGPU_EINVAL, "matrix must be finite");
+  for (int64_t i = 0; i < 2 * n * nrhs; ++i)
+    if (!std::isfinite(B[i])) return fail(c, BEMGPU_EINVAL, "right-hand side must be finite");
+  bemgpu_problem p;
+  bemgpu_problem_init(&p);
+  p.precision = precision;
+  p.equilibrate = equilibrate;
+  p.refine_tolerance = refine_tolerance;
+  p.refine_maxiter = refine_maxiter;
+  p.condition_guard = condition_guard;
+  p.boundary = BEMGPU_FLUID;  // no assembly; validation of the solver options only
+  p.density_contrast = p.soundspeed_contrast = 1.0;
+  int kind = 0;
+  TRY(check_problem(c, p, &kind));
+  auto f = std::make_shared<FactorData>();
+  f->c = c;
+  f->prob = p;
+  f->kind = kAsmFluidCBIE;
+  f->mixed = precision == BEMGPU_MIXED;
+  f->n = n;
+  f->N = n;
+  TRY(alloc(c, (size_t)n * n * 16, &f->A));
+  CUDA_TRY(c, cudaMemcpyAsync(f->A.p, A, (size_t)n * n * 16, cudaMemcpyHostToDevice, c->stream));
+  std::vector<FactorData*> fs{f.get()};
+  TRY(factor_batch(c, fs, false));
+  // solve with the generic chain: b given, x out
+  SolveInst s;
+  s.f = f.get();
+  s.R = nrhs;
+  TRY(alloc(c, (size_t)n * nrhs * 16, &s.b));
+  TRY(alloc(c, (size_t)n * nrhs * 16, &s.x));
+  TRY(alloc(c, (size_t)n * nrhs * 16, &s.y));
+  TRY(alloc(c, (size_t)n * nrhs * 8, &s.den));
+  TRY(alloc(c, (size_t)n * nrhs * 16, &s.work));
+  TRY(alloc(c, (size_t)kStats * nrhs * 8, &s.stats));
+  TRY(alloc(c, (size_t)std::max<int64_t>(kChunks * (int64_t)nrhs * n * 3, kChunks * n * 2) * 8,
+            &s.part));
+  TRY(alloc(c, (size_t)nrhs * 4, &s.active));
+  TRY(alloc(c, (size_t)nrhs * 4, &s.changed));
+  CUDA_TRY(c, cudaMemcpyAsync(s.b.p, B, (size_t)n * nrhs * 16, cudaMemcpyHostToDevice, c->stream));
+  s.rs.assign((size_t)nrhs, RhsState{});
+  std::vector<SolveInst*> all{&s};
+  std::vector<std::vector<int32_t>> mask{std::vector<int32_t>((size_t)nrhs, 1)};
+  TRY(correction_pass(c, all, true, mask, 0));
+  // refinement loop (same state machine as solve_batch, one instance)
+  if (f->mixed) {
+    for (int round = 0; round < 64; ++round) {
+      bool pending = false;
+      for (auto& r : s.rs) pending |= !r.done;
+      if (!pending) break;
+      std::vector<std::vector<double>> st;
+      TRY(residual_pass(c, all, &st));
+      std::vector<int32_t> im((size_t)nrhs, 0), cm((size_t)nrhs, 0);
+      bool prom = false;
+      for (int r = 0; r < nrhs; ++r) {
+        RhsState& q = s.rs[r];
+        if (q.done) continue;
+        double nw, cw;
+        normwise(&st[0][(size_t)r * kStats], f->matrix_norm, &nw, &cw);
+        q.nw = nw;
+        q.cw = cw;
+        double metric = std::max(nw, cw);
+        if (std::isfinite(metric) && metric <= refine_tolerance) {
+          q.done = true;
+          continue;
+        }
+        q.stalls = metric >= q.previous * 0.9 ? q.stalls + 1 : 0;
+        int reason = !std::isfinite(metric) ? BEMGPU_REASON_NONFINITE
+                     : q.attempts >= refine_maxiter ? BEMGPU_REASON_ITERATION_LIMIT
+                     : q.stalls >= 2 ? BEMGPU_REASON_STAGNATION
+                                     : BEMGPU_REASON_NONE;
+        if (reason != BEMGPU_REASON_NONE) {
+          if (!f->single)
+            return fail(c, BEMGPU_ENOTCONVERGED,
+                        "double-precision fallback failed backward-error acceptance");
+          if (!prom) f->reason = reason;
+          prom = true;
+          q.previous = INFINITY;
+          q.attempts = q.stalls = 0;
+          im[r] = 1;
+        } else {
+          cm[r] = 1;
+          q.previous = metric;
+        }
+      }
+      if (prom) {
+        std::vector<Buf> pp;
+        Buf b;
+        TRY(alloc(c, (size_t)kChunks * n * 2 * 8, &b));
+        pp.push_back(std::move(b));
+        TRY(promote(c, fs, pp));
+      }
+      std::vector<std::vector<int32_t>> m1{im}, m2{cm};
+      TRY(correction_pass(c, all, true, m1, 0));
+      TRY(correction_pass(c, all, false, m2, 1));
+      bool anyc = false;
+      for (int32_t v : cm) anyc |= v != 0;
+      if (anyc) {
+        std::vector<int32_t> ch;
+        TRY(download(c, s.changed, &ch, (size_t)nrhs));
+        for (int r = 0; r < nrhs; ++r) {
+          if (!cm[r]) continue;
+          if (!ch[r]) {
+            if (!f->single) return fail(c, BEMGPU_ENOTCONVERGED, "double-precision correction stagnated");
+            f->reason = BEMGPU_REASON_STAGNATION;
+            std::vector<Buf> pp;
+            Buf b;
+            TRY(alloc(c, (size_t)kChunks * n * 2 * 8, &b));
+            pp.push_back(std::move(b));
+            TRY(promote(c, fs, pp));
+            s.rs[r].previous = INFINITY;
+            s.rs[r].attempts = s.rs[r].stalls = 0;
+            std::vector<std::vector<int32_t>> m3{std::vector<int32_t>((size_t)nrhs, 0)};
+            m3[0][r] = 1;
+            TRY(correction_pass(c, all, true, m3, 0));
+          } else {
+            s.rs[r].corrections++;
+            s.rs[r].attempts++;
+          }
+        }
+      }
+    }
+  }
+  std::vector<std::vector<double>> st;
+  TRY(residual_pass(c, all, &st));
+  CUDA_TRY(c, cudaMemcpyAsync(B, s.x.p, (size_t)n * nrhs * 16, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  TRY(check_device_error(c));
+  if (diag) {
+    std::memset(diag, 0, sizeof *diag);
+    diag->unknown_count = n;
+    diag->precision = precision;
+    diag->factor_precision = f->single ? 0 : 1;
+    diag->refinement_reason = f->reason;
+    diag->equilibrate = equilibrate;
+    diag->single_reciprocal_condition = f->rcond;
+    diag->factor_ms = f->factor_ms;
+    diag->nrhs = nrhs;
+    diag->info = f->info_h;
+    for (int r = 0; r < nrhs; ++r) {
+      const double* q = &st[0][(size_t)r * kStats];
+      double an = std::sqrt(q[4]), bn = std::sqrt(q[5]);
+      double nw, cw;
+      normwise(q, f->matrix_norm, &nw, &cw);
+      diag->absolute_residual = std::max(diag->absolute_residual, an);
+      diag->relative_residual = std::max(diag->relative_residual,
+                                         bn == 0.0 ? (an == 0.0 ? 0.0 : INFINITY) : an / bn);
+      diag->normwise_backward_error = std::max(diag->normwise_backward_error, nw);
+      diag->componentwise_backward_error = std::max(diag->componentwise_backward_error, cw);
+      diag->refinement_iterations = std::max(diag->refinement_iterations, s.rs[r].corrections);
+    }
+  }
+  return BEMGPU_OK;
+}
+
+int bemgpu_assemble_dense(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_problem* problem,
+                          double* M1, double* M2) {
+  if (!c || !mesh || !problem || !M1) return fail(c, BEMGPU_EINVAL, "null argument");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  int kind = 0;
+  TRY(check_problem(c, *problem, &kind));
+  auto f = std::make_shared<FactorData>();
+  f->c = c;
+  f->mesh = mesh->d;
+  f->prob = *problem;
+  f->kind = kind;
+  f->mixed = problem->precision == BEMGPU_MIXED;
+  f->fp32_regular = problem->assembly == BEMGPU_ASSEMBLY_SINGLE ||
+                    (problem->assembly == BEMGPU_ASSEMBLY_DEFAULT && f->mixed);
+  std::vector<FactorData*> fs{f.get()};
+  TRY(assemble_batch(c, fs));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  TRY(check_device_error(c));
+  const bool fluid = kind == kAsmMuller || kind == kAsmFluidCBIE;
+  // M1 / M2 in the reference's naming: rigid system is M1, pressure release system is M2
+  if (fluid) {
+    CUDA_TRY(c, cudaMemcpy(M1, f->A.p, (size_t)f->N * f->N * 16, cudaMemcpyDeviceToHost));
+  } else {
+    const void* m1 = f->rhs_is_m2 ? f->A.p : f->Mrhs.p;
+    const void* m2 = f->rhs_is_m2 ? f->Mrhs.p : f->A.p;
+    CUDA_TRY(c, cudaMemcpy(M1, m1, (size_t)f->n * f->n * 16, cudaMemcpyDeviceToHost));
+    if (M2) CUDA_TRY(c, cudaMemcpy(M2, m2, (size_t)f->n * f->n * 16, cudaMemcpyDeviceToHost));
+  }
+  return BEMGPU_OK;
+}
+
+int bemgpu_profile_enable(bemgpu_ctx* c, int32_t enable) {
+  if (!c) return fail(nullptr, BEMGPU_EINVAL, "null context");
+  c->prof = enable != 0;
+  return BEMGPU_OK;
+}
+
+int bemgpu_profile_reset(bemgpu_ctx* c) {
+  if (!c) return fail(nullptr, BEMGPU_EINVAL, "null context");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->events)
+    for (auto& pr : kv.second) {
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+  c->events.clear();
+  return BEMGPU_OK;
+}
+
+int bemgpu_profile_read(bemgpu_ctx* c, const char* family, int64_t* launches, double* total_ms) {
+  if (!c || !family) return fail(c, BEMGPU_EINVAL, "null argument");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  int64_t cnt = 0;
+  double ms = 0.0;
+  auto it = c->events.find(family);
+  if (it != c->events.end())
+    for (auto& pr : it->second) {
+      float m = 0.f;
+      cudaEventElapsedTime(&m, pr.first, pr.second);
+      ms += m;
+      ++cnt;
+    }
+  if (launches) *launches = cnt;
+  if (total_ms) *total_ms = ms;
+  return BEMGPU_OK;
+}
+
+int bemgpu_launch_count(const bemgpu_ctx* c, int64_t* count) {
+  (void)c;
+  if (!count) return BEMGPU_EINVAL;
+  *count = launch_total();
+  return BEMGPU_OK;
+}
+
+}  // extern "C"

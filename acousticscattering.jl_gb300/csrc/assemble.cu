@@ -1,0 +1,354 @@
+// Assembly, incident-field and far-field kernels of the collocation BEM.
+//
+// Regular pairs: each CTA owns a tile of kAsmRows collocation points (one per thread)
+// and a chunk of source panels whose records (centroid, normal, area, Gauss points)
+// are staged in shared memory by one bulk asynchronous copy (TMA engine).  All threads
+// of a warp read the same source record (shared-memory broadcast) and write the
+// column-major matrix entry of their own row, so every warp store is 32 consecutive
+// complex128 values (512 contiguous bytes).
+// Near pairs: one thread per listed pair evaluates the FP64 singular rules and
+// overwrites the regular value (stream order guarantees the regular kernel ran first).
+#include <cstdio>
+
+#include "bemgpu_internal.h"
+#include "quad_math.cuh"
+#include "tma.cuh"
+
+namespace bemgpu {
+
+constexpr int kAsmRows = 128;      // threads per CTA = collocation points per tile
+constexpr int kAsmCols64 = 64;     // FP64 source records per chunk (64 x 256 B = 16 KB)
+constexpr int kAsmCols32 = 128;    // FP32 source records per chunk (128 x 128 B = 16 KB)
+
+template <typename R>
+struct Prec;
+template <>
+struct Prec<double> {
+  static constexpr int kCols = kAsmCols64;
+  static constexpr int kRec = kPanelDoubles;
+  __device__ static __forceinline__ void sc(double z, double* s, double* c) { sincos(z, s, c); }
+  __device__ static __forceinline__ double rs(double x) { return rsqrt(x); }
+  __device__ static __forceinline__ const double* recs(const AsmInst& I) { return I.panels; }
+};
+template <>
+struct Prec<float> {
+  static constexpr int kCols = kAsmCols32;
+  static constexpr int kRec = kPanelFloats;
+  // sin/cos of pi * t with exact argument reduction
+  __device__ static __forceinline__ void sc(float z, float* s, float* c) {
+    sincospif(z * 0.31830988618379067154f, s, c);
+  }
+  __device__ static __forceinline__ float rs(float x) { return rsqrtf(x); }
+  __device__ static __forceinline__ const float* recs(const AsmInst& I) { return I.panelsf; }
+};
+
+template <typename R>
+struct Acc {
+  cx<R> S, D, K, H;
+};
+
+// Full Helmholtz kernels of one source panel (7 points) at one wavenumber.
+template <typename R, bool NEED_KH>
+__device__ __forceinline__ void regular_panel(const R* rec, const R x[3], const R nx[3], R k,
+                                              Acc<R>& a) {
+  const R ny0 = rec[3], ny1 = rec[4], ny2 = rec[5];
+  const R area = rec[6];
+  const R nn = nx[0] * ny0 + nx[1] * ny1 + nx[2] * ny2;
+#pragma unroll
+  for (int q = 0; q < 7; ++q) {
+    const R u0 = rec[8 + 3 * q] - x[0];
+    const R u1 = rec[9 + 3 * q] - x[1];
+    const R u2 = rec[10 + 3 * q] - x[2];
+    const R r2 = u0 * u0 + u1 * u1 + u2 * u2;
+    const R ir = Prec<R>::rs(r2);
+    const R r = r2 * ir;
+    const R z = k * r;
+    R sn, cs;
+    Prec<R>::sc(z, &sn, &cs);
+    const R w = (R)dRuleW[q] * area * (R)kInv4Pi;
+    const R wir = w * ir;
+    const R ir2 = ir * ir;
+    a.S += wir * cx<R>{cs, sn};
+    const R uny = u0 * ny0 + u1 * ny1 + u2 * ny2;
+    // e^{iz} (iz - 1) w / (4 pi r^3)
+    const cx<R> gp = (wir * ir2) * cx<R>{-cs - z * sn, -sn + z * cs};
+    a.D += uny * gp;
+    if (NEED_KH) {
+      const R unx = u0 * nx[0] + u1 * nx[1] + u2 * nx[2];
+      a.K -= unx * gp;
+      const R c = unx * uny * ir2;
+      // e^{iz} [(nn - c (3 - z^2)) + i z (3c - nn)] w / (4 pi r^3)
+      const cx<R> br = {nn - c * ((R)3 - z * z), z * ((R)3 * c - nn)};
+      a.H += (wir * ir2) * (cx<R>{cs, sn} * br);
+    }
+  }
+}
+
+__device__ __forceinline__ void store_c(void* base, int64_t idx, cd v) {
+  reinterpret_cast<double2*>(base)[idx] = make_double2(v.x, v.y);
+}
+
+template <typename R, int KIND>
+__global__ void __launch_bounds__(kAsmRows) k_assemble_regular(const AsmInst* __restrict__ insts,
+                                                               int* err) {
+  constexpr int kCols = Prec<R>::kCols;
+  constexpr int kRec = Prec<R>::kRec;
+  __shared__ alignas(128) R srec[kCols * kRec];
+  __shared__ alignas(8) uint64_t bar;
+  const AsmInst& I = insts[blockIdx.z];
+  const int64_t n = I.n;
+  const int64_t i0 = (int64_t)blockIdx.x * kAsmRows;
+  const int64_t j0 = (int64_t)blockIdx.y * kCols;
+  if (i0 >= n || j0 >= n) return;  // uniform over the CTA
+  const int cnt = (int)min((int64_t)kCols, n - j0);
+  const R* recs = Prec<R>::recs(I);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t bytes = (uint32_t)(cnt * kRec * sizeof(R));
+    mbar_arrive_expect_tx(&bar, bytes);
+    bulk_g2s(srec, recs + j0 * kRec, bytes, &bar);
+  }
+  const int64_t i = i0 + threadIdx.x;
+  const bool row_ok = i < n;
+  R x[3] = {0, 0, 0}, nx[3] = {0, 0, 1};
+  if (row_ok) {
+    const R* ri = recs + i * kRec;
+    x[0] = ri[0]; x[1] = ri[1]; x[2] = ri[2];
+    nx[0] = ri[3]; nx[1] = ri[4]; nx[2] = ri[5];
+  }
+  const bool ok = mbar_wait(&bar, 0, err);
+  if (!ok || !row_ok) return;
+  const R ke = (R)I.k_e, ki = (R)I.k_i;
+  const int64_t lda = I.lda;
+  for (int jj = 0; jj < cnt; ++jj) {
+    const int64_t j = j0 + jj;
+    if (j == i) continue;  // self pair: near kernel
+    const R* rec = srec + jj * kRec;
+    if (KIND == kAsmBM || KIND == kAsmCBIE) {
+      Acc<R> a;
+      a.S = a.D = a.K = a.H = cx<R>{0, 0};
+      regular_panel<R, KIND == kAsmBM>(rec, x, nx, ke, a);
+      cd S = {a.S.x, a.S.y}, D = {a.D.x, a.D.y};
+      cd m1 = cd{-D.x, -D.y}, m2 = S;
+      if (KIND == kAsmBM) {
+        cd K = {a.K.x, a.K.y}, H = {a.H.x, a.H.y};
+        cd al = {I.a_re, I.a_im};
+        m1 -= al * H;
+        m2 += al * K;
+      }
+      store_c(I.out1, i + j * lda, m1);
+      store_c(I.out2, i + j * lda, m2);
+    } else {
+      Acc<R> e, t;
+      e.S = e.D = e.K = e.H = cx<R>{0, 0};
+      t = e;
+      constexpr bool kh = (KIND == kAsmMuller);
+      regular_panel<R, kh>(rec, x, nx, ke, e);
+      regular_panel<R, kh>(rec, x, nx, ki, t);
+      const double g = I.g;
+      cd a11, a12, a21, a22;
+      if (KIND == kAsmMuller) {
+        a11 = cd{(double)t.D.x - (double)e.D.x, (double)t.D.y - (double)e.D.y};
+        a12 = cd{(double)e.S.x - g * (double)t.S.x, (double)e.S.y - g * (double)t.S.y};
+        a21 = cd{(double)t.H.x / g - (double)e.H.x, (double)t.H.y / g - (double)e.H.y};
+        a22 = cd{(double)e.K.x - (double)t.K.x, (double)e.K.y - (double)t.K.y};
+      } else {
+        a11 = cd{-(double)e.D.x, -(double)e.D.y};
+        a12 = cd{(double)e.S.x, (double)e.S.y};
+        a21 = cd{(double)t.D.x, (double)t.D.y};
+        a22 = cd{-g * (double)t.S.x, -g * (double)t.S.y};
+      }
+      store_c(I.out1, i + j * lda, a11);
+      store_c(I.out1, i + (n + j) * lda, a12);
+      store_c(I.out1, (n + i) + j * lda, a21);
+      store_c(I.out1, (n + i) + (n + j) * lda, a22);
+    }
+  }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(128) k_assemble_near(const AsmInst* __restrict__ insts) {
+  const AsmInst& I = insts[blockIdx.z];
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= I.n_near) return;
+  const int64_t i = I.near_i[p], j = I.near_j[p];
+  const double* ri = I.panels + i * kPanelDoubles;
+  const double* rj = I.panels + j * kPanelDoubles;
+  double v[9];
+#pragma unroll
+  for (int t = 0; t < 9; ++t) v[t] = I.verts[j * kVertDoubles + t];
+  double x[3] = {ri[0], ri[1], ri[2]}, nx[3] = {ri[3], ri[4], ri[5]};
+  const bool self = (i == j);
+  double S0, D0, K0, H0;
+  laplace_parts(v, rj + 3, x, nx, self, S0, D0, K0, H0);
+  const int64_t n = I.n, lda = I.lda;
+  const double delta = self ? 1.0 : 0.0;
+  if (KIND == kAsmBM || KIND == kAsmCBIE) {
+    Ops o = near_ops(v, rj, x, nx, self, I.k_e, S0, D0, K0, H0);
+    cd m1 = cd{0.5 * delta - o.D.x, -o.D.y};
+    cd m2 = o.S;
+    if (KIND == kAsmBM) {
+      cd al = {I.a_re, I.a_im};
+      m1 -= al * o.H;
+      m2 += al * (o.K + cd{0.5 * delta, 0.0});
+    }
+    store_c(I.out1, i + j * lda, m1);
+    store_c(I.out2, i + j * lda, m2);
+  } else {
+    Ops e = near_ops(v, rj, x, nx, self, I.k_e, S0, D0, K0, H0);
+    Ops t = near_ops(v, rj, x, nx, self, I.k_i, S0, D0, K0, H0);
+    const double g = I.g;
+    cd a11, a12, a21, a22;
+    if (KIND == kAsmMuller) {
+      a11 = cd{delta - e.D.x + t.D.x, -e.D.y + t.D.y};
+      a12 = e.S - g * t.S;
+      a21 = cd{t.H.x / g - e.H.x, t.H.y / g - e.H.y};
+      a22 = cd{delta + e.K.x - t.K.x, e.K.y - t.K.y};
+    } else {
+      a11 = cd{0.5 * delta - e.D.x, -e.D.y};
+      a12 = e.S;
+      a21 = cd{0.5 * delta + t.D.x, t.D.y};
+      a22 = cd{-g * t.S.x, -g * t.S.y};
+    }
+    store_c(I.out1, i + j * lda, a11);
+    store_c(I.out1, i + (n + j) * lda, a12);
+    store_c(I.out1, (n + i) + j * lda, a21);
+    store_c(I.out1, (n + i) + (n + j) * lda, a22);
+  }
+}
+
+// ------------------------------------------------------------------ launch wrappers
+template <typename R>
+static void launch_regular_t(const Launch& L, const AsmInst* d, int ninst, int64_t nmax,
+                             int kind) {
+  constexpr int kCols = Prec<R>::kCols;
+  dim3 grid((unsigned)((nmax + kAsmRows - 1) / kAsmRows), (unsigned)((nmax + kCols - 1) / kCols),
+            (unsigned)ninst);
+  switch (kind) {
+    case kAsmBM: k_assemble_regular<R, kAsmBM><<<grid, kAsmRows, 0, L.stream>>>(d, L.err_flag); count_launch(1); break;
+    case kAsmCBIE: k_assemble_regular<R, kAsmCBIE><<<grid, kAsmRows, 0, L.stream>>>(d, L.err_flag); count_launch(1); break;
+    case kAsmMuller: k_assemble_regular<R, kAsmMuller><<<grid, kAsmRows, 0, L.stream>>>(d, L.err_flag); count_launch(1); break;
+    default: k_assemble_regular<R, kAsmFluidCBIE><<<grid, kAsmRows, 0, L.stream>>>(d, L.err_flag); count_launch(1); break;
+  }
+}
+
+void launch_assemble_regular(const Launch& L, const AsmInst* d_inst, int ninst, int64_t nmax,
+                             int kind, bool fp32) {
+  if (nmax <= 0 || ninst <= 0) return;
+  if (fp32)
+    launch_regular_t<float>(L, d_inst, ninst, nmax, kind);
+  else
+    launch_regular_t<double>(L, d_inst, ninst, nmax, kind);
+}
+
+void launch_assemble_near(const Launch& L, const AsmInst* d_inst, int ninst, int64_t max_near,
+                          int kind) {
+  if (max_near <= 0 || ninst <= 0) return;
+  dim3 grid((unsigned)((max_near + 127) / 128), 1, (unsigned)ninst);
+  switch (kind) {
+    case kAsmBM: k_assemble_near<kAsmBM><<<grid, 128, 0, L.stream>>>(d_inst); count_launch(1); break;
+    case kAsmCBIE: k_assemble_near<kAsmCBIE><<<grid, 128, 0, L.stream>>>(d_inst); count_launch(1); break;
+    case kAsmMuller: k_assemble_near<kAsmMuller><<<grid, 128, 0, L.stream>>>(d_inst); count_launch(1); break;
+    default: k_assemble_near<kAsmFluidCBIE><<<grid, 128, 0, L.stream>>>(d_inst); count_launch(1); break;
+  }
+}
+
+// ------------------------------------------------------------------ incident traces
+// p = e^{ik d.c}, q = ik (d.n) p at every collocation point (core/incident.jl:64-76).
+__global__ void k_incident(const WaveInst* __restrict__ insts) {
+  const WaveInst& W = insts[blockIdx.z];
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y;
+  if (i >= W.n || r >= W.nrhs) return;
+  const double* rec = W.panels + i * kPanelDoubles;
+  const double* d = W.dirs + 3 * r;
+  const double ph = W.k * (d[0] * rec[0] + d[1] * rec[1] + d[2] * rec[2]);
+  double sn, cs;
+  sincos(ph, &sn, &cs);
+  const double dn = W.k * (d[0] * rec[3] + d[1] * rec[4] + d[2] * rec[5]);
+  const int64_t o = 2 * (i + r * W.ldp);
+  W.p[o] = cs;
+  W.p[o + 1] = sn;
+  W.q[o] = -dn * sn;
+  W.q[o + 1] = dn * cs;
+}
+
+void launch_incident(const Launch& L, const WaveInst* d_inst, int ninst, int64_t nmax,
+                     int32_t max_rhs) {
+  if (nmax <= 0 || ninst <= 0 || max_rhs <= 0) return;
+  dim3 grid((unsigned)((nmax + 255) / 256), (unsigned)max_rhs, (unsigned)ninst);
+  k_incident<<<grid, 256, 0, L.stream>>>(d_inst); count_launch(1);
+}
+
+// ------------------------------------------------------------------ far field
+// f(xh) = -(1/4pi) sum_j area_j (ik xh.n_j p_j + q_j) sum_g W_g e^{-ik xh.y_jg}
+// (solvers/bem/full.jl:509-519).  One CTA per (direction, rhs, instance); fixed-order
+// per-thread sums, warp shuffles and a shared-memory pass make the result independent
+// of what else runs on the GPU.
+constexpr int kFarThreads = 256;
+
+__global__ void __launch_bounds__(kFarThreads) k_far_field(const WaveInst* __restrict__ insts) {
+  const WaveInst& W = insts[blockIdx.z];
+  const int d = blockIdx.x, r = blockIdx.y;
+  if (d >= W.ndir || r >= W.nrhs) return;
+  const double* xh = W.dirs + 3 * ((int64_t)r * W.ndir + d);
+  const double k = W.k;
+  const double x0 = xh[0], x1 = xh[1], x2 = xh[2];
+  double ar = 0.0, ai = 0.0;
+  for (int64_t j = threadIdx.x; j < W.n; j += kFarThreads) {
+    const double* rec = W.panels + j * kPanelDoubles;
+    const int64_t o = 2 * (j + r * W.ldp);
+    const double pr = W.p[o], pi = W.p[o + 1];
+    const double qr = W.q[o], qi = W.q[o + 1];
+    const double kxn = k * (x0 * rec[3] + x1 * rec[4] + x2 * rec[5]);
+    // a = i kxn p + q
+    const double a_r = -kxn * pi + qr, a_i = kxn * pr + qi;
+    double sr = 0.0, si = 0.0;
+#pragma unroll
+    for (int g = 0; g < 7; ++g) {
+      const double ph = -k * (x0 * rec[8 + 3 * g] + x1 * rec[9 + 3 * g] + x2 * rec[10 + 3 * g]);
+      double sn, cs;
+      sincos(ph, &sn, &cs);
+      sr += dRuleW[g] * cs;
+      si += dRuleW[g] * sn;
+    }
+    const double area = rec[6];
+    ar += area * (a_r * sr - a_i * si);
+    ai += area * (a_r * si + a_i * sr);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    ar += __shfl_down_sync(0xffffffffu, ar, off);
+    ai += __shfl_down_sync(0xffffffffu, ai, off);
+  }
+  __shared__ double red[2][kFarThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][wid] = ar;
+    red[1][wid] = ai;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tr = 0.0, ti = 0.0;
+    for (int w = 0; w < kFarThreads / 32; ++w) {
+      tr += red[0][w];
+      ti += red[1][w];
+    }
+    const int64_t o = 2 * ((int64_t)r * W.ndir + d);
+    W.out[o] = -tr * kInv4Pi;
+    W.out[o + 1] = -ti * kInv4Pi;
+  }
+}
+
+void launch_far_field(const Launch& L, const WaveInst* d_inst, int ninst, int32_t max_rhs,
+                      int32_t max_dirs) {
+  if (ninst <= 0 || max_dirs <= 0 || max_rhs <= 0) return;
+  dim3 grid((unsigned)max_dirs, (unsigned)max_rhs, (unsigned)ninst);
+  k_far_field<<<grid, kFarThreads, 0, L.stream>>>(d_inst); count_launch(1);
+}
+
+}  // namespace bemgpu

@@ -1,0 +1,123 @@
+// Internal declarations of libbemgpu (not part of the C ABI).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/bemgpu.h"
+
+#ifdef __CUDACC__
+#include <cuda_runtime.h>
+#endif
+
+namespace bemgpu {
+
+// ------------------------------------------------------------------ host utilities
+int validate_surface(const double* nodes, int64_t N, const int64_t* tris, int64_t M,
+                     double* resolution, std::string* err);
+void mesh_hash(const double* nodes, int64_t N, const int64_t* tris, int64_t M, char out[65]);
+void panel_centroids(const double* nodes, const int64_t* tris, int64_t M,
+                     std::vector<double>* cent, std::vector<double>* diam);
+void near_pairs(const std::vector<double>& cent, const std::vector<double>& diam, double eta,
+                std::vector<int64_t>* rowptr, std::vector<int64_t>* cols);
+
+// Kernel launch accounting (every <<<>>> of the library increments the counter).
+void count_launch(int kernels);
+long long launch_total();
+
+// ------------------------------------------------------------------ device records
+// FP64 panel record, 32 doubles = 256 B (16-byte multiple for bulk async copies):
+//   [0..2] centroid (collocation point)  [3..5] unit normal  [6] area  [7] longest edge
+//   [8..28] the seven Gauss points (xyz)  [29..31] padding
+constexpr int kPanelDoubles = 32;
+// FP32 panel record, 32 floats = 128 B, coordinates relative to the mesh centre.
+constexpr int kPanelFloats = 32;
+// Vertex record, 12 doubles = 96 B: v0, v1, v2 (xyz) + padding.
+constexpr int kVertDoubles = 12;
+
+// Radon's 7-point degree-5 rule on the triangle (barycentric, weights sum to 1).
+constexpr double kRuleW[7] = {0.225,
+                              0.13239415278850618074, 0.13239415278850618074,
+                              0.13239415278850618074, 0.12593918054482715260,
+                              0.12593918054482715260, 0.12593918054482715260};
+constexpr double kRuleB[7][3] = {
+    {1.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0},
+    {0.05971587178976982046, 0.47014206410511508977, 0.47014206410511508977},
+    {0.47014206410511508977, 0.05971587178976982046, 0.47014206410511508977},
+    {0.47014206410511508977, 0.47014206410511508977, 0.05971587178976982046},
+    {0.79742698535308732240, 0.10128650732345633880, 0.10128650732345633880},
+    {0.10128650732345633880, 0.79742698535308732240, 0.10128650732345633880},
+    {0.10128650732345633880, 0.10128650732345633880, 0.79742698535308732240}};
+
+// Assembly kinds.
+enum AsmKind : int32_t {
+  kAsmBM = 0,        // rigid/soft Burton-Miller: M1 = 1/2 I - D - a H, M2 = S + a(1/2 I + K')
+  kAsmCBIE = 1,      // rigid/soft CBIE:           M1 = 1/2 I - D,        M2 = S
+  kAsmMuller = 2,    // fluid Mueller 2n x 2n
+  kAsmFluidCBIE = 3  // fluid CBIE 2n x 2n
+};
+
+// One assembly instance (device-resident array of these drives a batched launch).
+struct AsmInst {
+  const double* panels;    // FP64 panel records
+  const float* panelsf;    // FP32 panel records (mixed precision regular pairs)
+  const double* verts;     // vertex records
+  const int32_t* near_i;   // near pair rows (collocation panel)
+  const int32_t* near_j;   // near pair columns (source panel)
+  int64_t n;               // panels
+  int64_t n_near;          // near pairs
+  int64_t lda;             // leading dimension of the outputs (n or 2n)
+  double k_e, k_i, g;      // exterior/interior wavenumber, density contrast
+  double a_re, a_im;       // Burton-Miller coupling (0 for CBIE)
+  int32_t kind;            // AsmKind
+  int32_t pad;
+  void* out1;              // complex128 M1 (or A for fluid)
+  void* out2;              // complex128 M2 (rigid/soft), null for fluid
+};
+
+// Incident field / far-field instance.
+struct WaveInst {
+  const double* panels;
+  int64_t n;
+  double k;
+  int32_t nrhs;
+  int32_t ndir;
+  const double* dirs;      // incidence directions (3 * nrhs) or observation (3 * ndir)
+  double* p;               // complex128 n x nrhs (traces) ...
+  double* q;
+  double* out;             // complex128 results
+  int64_t ldp;             // leading dimension of p / q
+};
+
+// Dense-matrix instance for the batched factor / solve kernels.
+struct MatInst {
+  void* a;          // column-major matrix (complex128 or complex64)
+  int64_t n;        // order
+  int64_t lda;
+  int32_t* ipiv;    // 0-based pivot rows
+  int32_t* info;    // first zero pivot (1-based), 0 if none
+  void* x;          // right-hand sides / solutions (n x nrhs, ld = ldx)
+  int64_t ldx;
+  int32_t nrhs;
+  int32_t active;
+};
+
+// ------------------------------------------------------------------ launch wrappers
+#ifdef __CUDACC__
+struct Launch {
+  cudaStream_t stream;
+  int* err_flag;  // device word set by bounded waits that give up
+};
+
+void launch_assemble_regular(const Launch& L, const AsmInst* d_inst, int ninst, int64_t nmax,
+                             int kind, bool fp32);
+void launch_assemble_near(const Launch& L, const AsmInst* d_inst, int ninst, int64_t max_near,
+                          int kind);
+void launch_incident(const Launch& L, const WaveInst* d_inst, int ninst, int64_t nmax,
+                     int32_t max_rhs);
+void launch_far_field(const Launch& L, const WaveInst* d_inst, int ninst, int32_t max_rhs,
+                      int32_t max_dirs);
+#endif
+
+}  // namespace bemgpu

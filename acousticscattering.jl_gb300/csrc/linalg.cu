@@ -1,0 +1,486 @@
+// Batched dense complex linear algebra for the BEM systems (complex128 and complex64).
+//
+// Every kernel takes a device array of MatInst descriptors and handles all instances
+// of a batch in one launch (blockIdx.z or blockIdx.y selects the instance); instances
+// whose order is exhausted at the current step return at once, so batches of uneven
+// size share one launch sequence.
+//
+// LU: right-looking blocked partial pivoting (LAPACK zgetrf semantics: pivot = first
+// row of largest |re| + |im| in the column, P A = L U with unit lower L):
+//   getf2   panel of kPanelNB columns, one CTA per instance, column by column;
+//   laswp   the panel's row interchanges applied to the columns outside it;
+//   trsm    U12 = L11^{-1} A12, one warp per column of A12;
+//   gemm    A22 -= L21 U12 (SIMT tile kernel; the complex64 factor of the mixed path
+//           uses the tensor-core kernel in gemm_tc.cu instead).
+// getrs: row interchanges, then blocked triangular solves: a diagonal-block solve
+// (one CTA per instance and right-hand side) followed by a rank-update of the rows
+// still to solve, for L, U, U^H and L^H (the last two for condition estimation).
+#include <cfloat>
+#include <cstdio>
+
+#include "bemgpu_internal.h"
+#include "linalg.cuh"
+
+namespace bemgpu {
+
+// ------------------------------------------------------------------ helpers
+template <typename R>
+__device__ __forceinline__ cx<R> ld(const void* base, int64_t idx) {
+  if constexpr (sizeof(R) == 8) {
+    double2 v = reinterpret_cast<const double2*>(base)[idx];
+    return {v.x, v.y};
+  } else {
+    float2 v = reinterpret_cast<const float2*>(base)[idx];
+    return {v.x, v.y};
+  }
+}
+template <typename R>
+__device__ __forceinline__ void st(void* base, int64_t idx, cx<R> v) {
+  if constexpr (sizeof(R) == 8)
+    reinterpret_cast<double2*>(base)[idx] = make_double2(v.x, v.y);
+  else
+    reinterpret_cast<float2*>(base)[idx] = make_float2(v.x, v.y);
+}
+template <typename R>
+__device__ __forceinline__ R cabs1(cx<R> a) {
+  return fabs(a.x) + fabs(a.y);
+}
+template <typename R>
+__device__ __forceinline__ cx<R> cinv(cx<R> a) {
+  R s = fmax(fabs(a.x), fabs(a.y));
+  R ar = a.x / s, ai = a.y / s;
+  R d = (ar * ar + ai * ai) * s;
+  return {ar / d, -ai / d};
+}
+template <typename R>
+__device__ __forceinline__ cx<R> cconj(cx<R> a) {
+  return {a.x, -a.y};
+}
+
+// ------------------------------------------------------------------ getf2 (panel)
+constexpr int kGetf2Threads = 512;
+
+template <typename R>
+__global__ void __launch_bounds__(kGetf2Threads) k_getf2(const MatInst* __restrict__ insts,
+                                                         int64_t k0, int nb) {
+  const MatInst& M = insts[blockIdx.x];
+  const int64_t n = M.n;
+  if (!M.active || k0 >= n) return;
+  const int nbe = (int)min((int64_t)nb, n - k0);
+  const int64_t lda = M.lda;
+  void* A = M.a;
+  __shared__ R s_val[kGetf2Threads / 32];
+  __shared__ int64_t s_idx[kGetf2Threads / 32];
+  __shared__ cx<R> s_u[kPanelNB];
+  __shared__ int64_t s_piv;
+  __shared__ R s_pmax;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int c = 0; c < nbe; ++c) {
+    const int64_t col = k0 + c;
+    // pivot search: largest |re|+|im|, first index on ties
+    R best = (R)-1;
+    int64_t bidx = col;
+    for (int64_t r = col + tid; r < n; r += kGetf2Threads) {
+      R v = cabs1(ld<R>(A, r + col * lda));
+      if (v > best) {
+        best = v;
+        bidx = r;
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      R ov = __shfl_down_sync(0xffffffffu, best, off);
+      int64_t oi = __shfl_down_sync(0xffffffffu, bidx, off);
+      if (ov > best || (ov == best && oi < bidx)) {
+        best = ov;
+        bidx = oi;
+      }
+    }
+    if (lane == 0) {
+      s_val[wid] = best;
+      s_idx[wid] = bidx;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      R bv = s_val[0];
+      int64_t bi = s_idx[0];
+      for (int w = 1; w < kGetf2Threads / 32; ++w)
+        if (s_val[w] > bv || (s_val[w] == bv && s_idx[w] < bi)) {
+          bv = s_val[w];
+          bi = s_idx[w];
+        }
+      s_piv = bi;
+      s_pmax = bv;
+      M.ipiv[col] = (int32_t)bi;
+      if (!(bv > (R)0) && *M.info == 0) *M.info = (int32_t)(col + 1);
+    }
+    __syncthreads();
+    const int64_t piv = s_piv;
+    const bool nonzero = s_pmax > (R)0;
+    if (nonzero && piv != col && tid < nbe) {
+      const int64_t cc = k0 + tid;
+      cx<R> a = ld<R>(A, col + cc * lda), b = ld<R>(A, piv + cc * lda);
+      st<R>(A, col + cc * lda, b);
+      st<R>(A, piv + cc * lda, a);
+    }
+    __syncthreads();
+    if (tid < nbe) s_u[tid] = ld<R>(A, col + (k0 + tid) * lda);
+    __syncthreads();
+    const cx<R> inv = nonzero ? cinv(s_u[c]) : cx<R>{(R)1, (R)0};
+    for (int64_t r = col + 1 + tid; r < n; r += kGetf2Threads) {
+      cx<R> l = ld<R>(A, r + col * lda);
+      if (nonzero) {
+        l = l * inv;
+        st<R>(A, r + col * lda, l);
+      }
+      for (int cc = c + 1; cc < nbe; ++cc) {
+        const int64_t idx = r + (k0 + cc) * lda;
+        st<R>(A, idx, ld<R>(A, idx) - l * s_u[cc]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ laswp
+template <typename R>
+__global__ void k_laswp(const MatInst* __restrict__ insts, int64_t k0, int nb) {
+  const MatInst& M = insts[blockIdx.y];
+  const int64_t n = M.n;
+  if (!M.active || k0 >= n) return;
+  const int nbe = (int)min((int64_t)nb, n - k0);
+  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // columns outside the panel: [0, k0) then [k0 + nbe, n)
+  if (j >= k0) j += nbe;
+  if (j >= n) return;
+  const int64_t lda = M.lda;
+  for (int c = 0; c < nbe; ++c) {
+    const int64_t row = k0 + c, p = M.ipiv[row];
+    if (p != row) {
+      cx<R> a = ld<R>(M.a, row + j * lda), b = ld<R>(M.a, p + j * lda);
+      st<R>(M.a, row + j * lda, b);
+      st<R>(M.a, p + j * lda, a);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ trsm (U12)
+constexpr int kTrsmWarps = 8;
+
+template <typename R>
+__global__ void __launch_bounds__(kTrsmWarps * 32) k_trsm_panel(const MatInst* __restrict__ insts,
+                                                               int64_t k0, int nb) {
+  const MatInst& M = insts[blockIdx.y];
+  const int64_t n = M.n;
+  if (!M.active || k0 >= n) return;
+  const int nbe = (int)min((int64_t)nb, n - k0);
+  const int64_t lda = M.lda;
+  __shared__ cx<R> sL[kPanelNB][kPanelNB + 1];
+  for (int t = threadIdx.x; t < nbe * nbe; t += blockDim.x) {
+    int r = t % nbe, c = t / nbe;
+    sL[r][c] = ld<R>(M.a, (k0 + r) + (k0 + c) * lda);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t j = k0 + nbe + (int64_t)blockIdx.x * kTrsmWarps + wid;
+  if (j >= n) return;
+  constexpr int kPer = kPanelNB / 32;
+  cx<R> x[kPer];
+#pragma unroll
+  for (int t = 0; t < kPer; ++t) {
+    int r = lane + 32 * t;
+    x[t] = r < nbe ? ld<R>(M.a, (k0 + r) + j * lda) : cx<R>{0, 0};
+  }
+  for (int c = 0; c < nbe; ++c) {
+    cx<R> xc;
+    xc.x = __shfl_sync(0xffffffffu, x[c / 32].x, c % 32);
+    xc.y = __shfl_sync(0xffffffffu, x[c / 32].y, c % 32);
+#pragma unroll
+    for (int t = 0; t < kPer; ++t) {
+      int r = lane + 32 * t;
+      if (r > c && r < nbe) x[t] -= sL[r][c] * xc;
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < kPer; ++t) {
+    int r = lane + 32 * t;
+    if (r < nbe) st<R>(M.a, (k0 + r) + j * lda, x[t]);
+  }
+}
+
+// ------------------------------------------------------------------ SIMT gemm update
+// C(m x m') -= A(m x kk) B(kk x m') with A = L21, B = U12, C = A22 of each instance.
+constexpr int kGT = 64;   // tile edge
+constexpr int kGK = 8;    // k chunk
+constexpr int kGThreads = 256;
+
+template <typename R>
+__global__ void __launch_bounds__(kGThreads) k_gemm_update(const MatInst* __restrict__ insts,
+                                                          int64_t k0, int nb, int64_t tiles_max) {
+  const MatInst& M = insts[blockIdx.y];
+  const int64_t n = M.n;
+  if (!M.active || k0 >= n) return;
+  const int nbe = (int)min((int64_t)nb, n - k0);
+  const int64_t s = k0 + nbe;  // first trailing row/column
+  const int64_t m = n - s;
+  if (m <= 0) return;
+  const int64_t tiles = (m + kGT - 1) / kGT;
+  const int64_t t = blockIdx.x;
+  if (t >= tiles * tiles) return;
+  const int64_t ti = t % tiles, tj = t / tiles;
+  const int64_t r0 = s + ti * kGT, c0 = s + tj * kGT;
+  const int64_t lda = M.lda;
+  __shared__ cx<R> sA[kGK][kGT + 1];
+  __shared__ cx<R> sB[kGK][kGT + 1];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  cx<R> acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = cx<R>{0, 0};
+  for (int kc = 0; kc < nbe; kc += kGK) {
+    for (int e = threadIdx.x; e < kGK * kGT; e += kGThreads) {
+      int rr = e % kGT, kk = e / kGT;
+      int64_t gr = r0 + rr, gk = k0 + kc + kk;
+      sA[kk][rr] = (gr < n && kc + kk < nbe) ? ld<R>(M.a, gr + gk * lda) : cx<R>{0, 0};
+      int kb = e % kGK;
+      int cc = e / kGK;
+      int64_t gc = c0 + cc, gkb = k0 + kc + kb;
+      sB[kb][cc] = (gc < n && kc + kb < nbe) ? ld<R>(M.a, gkb + gc * lda) : cx<R>{0, 0};
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kGK; ++kk) {
+      cx<R> av[4], bv[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) av[a] = sA[kk][tx + 16 * a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) bv[b] = sB[kk][ty + 16 * b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      int64_t gr = r0 + tx + 16 * a, gc = c0 + ty + 16 * b;
+      if (gr < n && gc < n) {
+        int64_t idx = gr + gc * lda;
+        st<R>(M.a, idx, ld<R>(M.a, idx) - acc[a][b]);
+      }
+    }
+}
+
+// ------------------------------------------------------------------ getrs pieces
+// Row interchanges on the right-hand sides (forward: ipiv in order; back: reverse).
+template <typename R>
+__global__ void k_rhs_swap(const MatInst* __restrict__ insts, int reverse) {
+  const MatInst& M = insts[blockIdx.y];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!M.active || r >= M.nrhs) return;
+  const int64_t n = M.n;
+  void* X = M.x;
+  const int64_t off = (int64_t)r * M.ldx;
+  if (!reverse) {
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t p = M.ipiv[i];
+      if (p != i) {
+        cx<R> a = ld<R>(X, off + i), b = ld<R>(X, off + p);
+        st<R>(X, off + i, b);
+        st<R>(X, off + p, a);
+      }
+    }
+  } else {
+    for (int64_t i = n - 1; i >= 0; --i) {
+      int64_t p = M.ipiv[i];
+      if (p != i) {
+        cx<R> a = ld<R>(X, off + i), b = ld<R>(X, off + p);
+        st<R>(X, off + i, b);
+        st<R>(X, off + p, a);
+      }
+    }
+  }
+}
+
+// element (r, c) of op(A): A or A^H
+template <typename R, bool TRANS>
+__device__ __forceinline__ cx<R> opel(const void* A, int64_t lda, int64_t r, int64_t c) {
+  if (TRANS) return cconj(ld<R>(A, c + r * lda));
+  return ld<R>(A, r + c * lda);
+}
+
+// Diagonal block solve: rows [r0, r0 + nbs) of op(T) x = x, op(T) lower when
+// EFF_LOWER.  One CTA (kTrsvNB threads) per (rhs, instance).
+template <typename R, bool EFF_LOWER, bool TRANS, bool UNIT>
+__global__ void __launch_bounds__(kTrsvNB) k_trsv_block(const MatInst* __restrict__ insts,
+                                                        int64_t r0) {
+  const MatInst& M = insts[blockIdx.y];
+  const int rhs = blockIdx.x;
+  const int64_t n = M.n;
+  if (!M.active || rhs >= M.nrhs || r0 >= n) return;
+  const int nbs = (int)min((int64_t)kTrsvNB, n - r0);
+  const int64_t lda = M.lda, off = (int64_t)rhs * M.ldx;
+  __shared__ cx<R> sx[kTrsvNB];
+  const int t = threadIdx.x;
+  if (t < nbs) sx[t] = ld<R>(M.x, off + r0 + t);
+  __syncthreads();
+  if (EFF_LOWER) {
+    for (int c = 0; c < nbs; ++c) {
+      if (!UNIT && t == c) sx[c] = sx[c] * cinv(opel<R, TRANS>(M.a, lda, r0 + c, r0 + c));
+      __syncthreads();
+      if (t > c && t < nbs) sx[t] -= opel<R, TRANS>(M.a, lda, r0 + t, r0 + c) * sx[c];
+      __syncthreads();
+    }
+  } else {
+    for (int c = nbs - 1; c >= 0; --c) {
+      if (!UNIT && t == c) sx[c] = sx[c] * cinv(opel<R, TRANS>(M.a, lda, r0 + c, r0 + c));
+      __syncthreads();
+      if (t < c) sx[t] -= opel<R, TRANS>(M.a, lda, r0 + t, r0 + c) * sx[c];
+      __syncthreads();
+    }
+  }
+  if (t < nbs) st<R>(M.x, off + r0 + t, sx[t]);
+}
+
+// Update of the unsolved rows by the solved block [r0, r0 + nbs): thread per row.
+template <typename R, bool EFF_LOWER, bool TRANS>
+__global__ void __launch_bounds__(256) k_trsv_update(const MatInst* __restrict__ insts,
+                                                     int64_t r0) {
+  const MatInst& M = insts[blockIdx.z];
+  const int rhs = blockIdx.y;
+  const int64_t n = M.n;
+  if (!M.active || rhs >= M.nrhs || r0 >= n) return;
+  const int nbs = (int)min((int64_t)kTrsvNB, n - r0);
+  const int64_t lda = M.lda, off = (int64_t)rhs * M.ldx;
+  __shared__ cx<R> sx[kTrsvNB];
+  if (threadIdx.x < nbs) sx[threadIdx.x] = ld<R>(M.x, off + r0 + threadIdx.x);
+  __syncthreads();
+  int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (EFF_LOWER)
+    row += r0 + nbs;
+  if (EFF_LOWER ? row >= n : row >= r0) return;
+  cx<R> acc = {0, 0};
+  for (int c = 0; c < nbs; ++c) acc += opel<R, TRANS>(M.a, lda, row, r0 + c) * sx[c];
+  st<R>(M.x, off + row, ld<R>(M.x, off + row) - acc);
+}
+
+// ------------------------------------------------------------------ launch wrappers
+static int prec_is_single(int prec) { return prec == 1; }
+
+void launch_getf2(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb, int prec) {
+  if (prec_is_single(prec))
+    k_getf2<float><<<ninst, kGetf2Threads, 0, L.stream>>>(d, k0, nb);
+  else
+    k_getf2<double><<<ninst, kGetf2Threads, 0, L.stream>>>(d, k0, nb);
+  count_launch(1);
+}
+
+void launch_laswp(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb, int64_t nmax,
+                  int prec) {
+  // upper bound of the columns outside the panel over all instances
+  const int64_t cols = nmax;
+  dim3 grid((unsigned)((cols + 255) / 256), (unsigned)ninst);
+  if (prec_is_single(prec))
+    k_laswp<float><<<grid, 256, 0, L.stream>>>(d, k0, nb);
+  else
+    k_laswp<double><<<grid, 256, 0, L.stream>>>(d, k0, nb);
+  count_launch(1);
+}
+
+void launch_trsm_panel(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb,
+                       int64_t nmax, int prec) {
+  int64_t cols = nmax - k0 - nb;
+  if (cols <= 0) return;
+  dim3 grid((unsigned)((cols + kTrsmWarps - 1) / kTrsmWarps), (unsigned)ninst);
+  if (prec_is_single(prec))
+    k_trsm_panel<float><<<grid, kTrsmWarps * 32, 0, L.stream>>>(d, k0, nb);
+  else
+    k_trsm_panel<double><<<grid, kTrsmWarps * 32, 0, L.stream>>>(d, k0, nb);
+  count_launch(1);
+}
+
+void launch_gemm_update(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb,
+                        int64_t nmax, int prec) {
+  int64_t m = nmax - k0 - nb;
+  if (m <= 0) return;
+  int64_t tiles = (m + kGT - 1) / kGT;
+  dim3 grid((unsigned)(tiles * tiles), (unsigned)ninst);
+  if (prec_is_single(prec))
+    k_gemm_update<float><<<grid, kGThreads, 0, L.stream>>>(d, k0, nb, tiles);
+  else
+    k_gemm_update<double><<<grid, kGThreads, 0, L.stream>>>(d, k0, nb, tiles);
+  count_launch(1);
+}
+
+void launch_rhs_swap(const Launch& L, const MatInst* d, int ninst, int32_t max_rhs, int reverse,
+                     int prec) {
+  dim3 grid((unsigned)((max_rhs + 63) / 64), (unsigned)ninst);
+  if (prec_is_single(prec))
+    k_rhs_swap<float><<<grid, 64, 0, L.stream>>>(d, reverse);
+  else
+    k_rhs_swap<double><<<grid, 64, 0, L.stream>>>(d, reverse);
+  count_launch(1);
+}
+
+template <typename R, bool EL, bool TR, bool UN>
+static void trsv_t(const Launch& L, const MatInst* d, int ninst, int64_t nmax, int32_t max_rhs) {
+  const int64_t nblk = (nmax + kTrsvNB - 1) / kTrsvNB;
+  for (int64_t b = 0; b < nblk; ++b) {
+    const int64_t blk = EL ? b : nblk - 1 - b;
+    const int64_t r0 = blk * kTrsvNB;
+    k_trsv_block<R, EL, TR, UN><<<dim3((unsigned)max_rhs, (unsigned)ninst), kTrsvNB, 0,
+                                  L.stream>>>(d, r0); count_launch(1);
+    const int64_t rows = EL ? (nmax - r0 - kTrsvNB) : r0;
+    if (rows > 0) {
+      k_trsv_update<R, EL, TR><<<dim3((unsigned)((rows + 255) / 256), (unsigned)max_rhs,
+                                      (unsigned)ninst),
+                                 256, 0, L.stream>>>(d, r0);
+      count_launch(1);
+    }
+  }
+}
+
+// Solve op(LU) x = b in place on MatInst.x.  trans = 0: A x = b; trans = 1: A^H x = b.
+// swaps = 0 leaves out the row interchanges (the (LU)^{-1} and (LU)^{-H} products that
+// LAPACK's condition estimator applies).
+void launch_getrs(const Launch& L, const MatInst* d, int ninst, int64_t nmax, int32_t max_rhs,
+                  int trans, int prec, int swaps) {
+  if (nmax <= 0 || ninst <= 0 || max_rhs <= 0) return;
+  if (!trans) {
+    if (swaps) launch_rhs_swap(L, d, ninst, max_rhs, 0, prec);
+    if (prec_is_single(prec)) {
+      trsv_t<float, true, false, true>(L, d, ninst, nmax, max_rhs);
+      trsv_t<float, false, false, false>(L, d, ninst, nmax, max_rhs);
+    } else {
+      trsv_t<double, true, false, true>(L, d, ninst, nmax, max_rhs);
+      trsv_t<double, false, false, false>(L, d, ninst, nmax, max_rhs);
+    }
+  } else {
+    // A^H = U^H L^H P: solve U^H (lower, non-unit), then L^H (upper, unit), then P^T.
+    if (prec_is_single(prec)) {
+      trsv_t<float, true, true, false>(L, d, ninst, nmax, max_rhs);
+      trsv_t<float, false, true, true>(L, d, ninst, nmax, max_rhs);
+    } else {
+      trsv_t<double, true, true, false>(L, d, ninst, nmax, max_rhs);
+      trsv_t<double, false, true, true>(L, d, ninst, nmax, max_rhs);
+    }
+    if (swaps) launch_rhs_swap(L, d, ninst, max_rhs, 1, prec);
+  }
+}
+
+// Full SIMT LU of a batch (used by the complex128 path and by the complex64 path when
+// the tensor-core trailing update is not selected).
+void launch_getrf_simt(const Launch& L, const MatInst* d, int ninst, int64_t nmax, int prec) {
+  for (int64_t k0 = 0; k0 < nmax; k0 += kPanelNB) {
+    launch_getf2(L, d, ninst, k0, kPanelNB, prec);
+    launch_laswp(L, d, ninst, k0, kPanelNB, nmax, prec);
+    launch_trsm_panel(L, d, ninst, k0, kPanelNB, nmax, prec);
+    launch_gemm_update(L, d, ninst, k0, kPanelNB, nmax, prec);
+  }
+}
+
+}  // namespace bemgpu

@@ -1,0 +1,49 @@
+// Descriptors and launch declarations of the matrix-vector kernels in refine.cu.
+#pragma once
+
+#include "bemgpu_internal.h"
+
+namespace bemgpu {
+
+constexpr int kChunks = 8;   // column chunks of the row-wise sweeps
+constexpr int kGemvR = 4;    // right-hand sides per gemv pass
+constexpr int kStats = 9;    // residual statistics per right-hand side
+
+struct VecInst {
+  const void* A;     // complex128 matrix, column-major
+  int64_t n;         // order
+  int64_t lda;
+  double* rows;      // row scales (n), or null for unit scales
+  double* cols;      // column scales (n), or null
+  double* rowsum;    // row sums of |A| (n)
+  double* part;      // scratch: kChunks * nrhs * n * 3 doubles (>= kChunks * n * 2)
+  void* out;         // scaled copy / correction work buffer (ld n)
+  int32_t out_single;
+  int32_t nrhs;
+  int32_t* flag;     // nonfinite conversion flag
+  const double* x;   // complex128 vectors (n x nrhs, ld ldx)
+  int64_t ldx;
+  const double* b;   // complex128 right-hand sides
+  int64_t ldb;
+  double* y;         // complex128 output / input vectors
+  int64_t ldy;
+  double* den;       // componentwise denominators (n x nrhs, ld ldy)
+  double* stats;     // kStats doubles per right-hand side
+  int32_t* active;   // per rhs: still refining (null = all)
+  int32_t* changed;  // per rhs: last correction changed x
+};
+
+#ifdef __CUDACC__
+void launch_equilibrate(const Launch& L, const VecInst* d, int ninst, int64_t nmax);
+void launch_scale_copy(const Launch& L, const VecInst* d, int ninst, int64_t nmax);
+// mode 0: y = A x; mode 1: y = b - A x and den = |b| + |A||x|
+void launch_gemv(const Launch& L, const VecInst* d, int ninst, int64_t nmax, int32_t max_rhs,
+                 int mode);
+void launch_resid_stats(const Launch& L, const VecInst* d, int ninst, int32_t max_rhs);
+void launch_corr_prep(const Launch& L, const VecInst* d, int ninst, int64_t nmax,
+                      int32_t max_rhs);
+void launch_corr_apply(const Launch& L, const VecInst* d, int ninst, int64_t nmax,
+                       int32_t max_rhs, int mode);
+#endif
+
+}  // namespace bemgpu

@@ -1,0 +1,28 @@
+// Descriptors and launch declarations of the elementwise solve-chain kernels.
+#pragma once
+
+#include "bemgpu_internal.h"
+
+namespace bemgpu {
+
+struct TraceInst {
+  const double* x;     // solution (N x nrhs, ld ldx) or product y for the CBIE forcing
+  int64_t ldx;
+  const double* pinc;  // incident traces (n x nrhs, ld n)
+  const double* qinc;
+  int64_t n;
+  double* ps;          // scattered traces out (n x nrhs) / forcing out (2n x nrhs)
+  double* qs;
+  int32_t nrhs;
+  int32_t kind;
+};
+
+#ifdef __CUDACC__
+void launch_traces(const Launch& L, const TraceInst* d, int ninst, int64_t nmax, int32_t max_rhs);
+void launch_cbie_forcing(const Launch& L, const TraceInst* d, int ninst, int64_t nmax,
+                         int32_t max_rhs);
+void launch_stack(const Launch& L, const TraceInst* d, int ninst, int64_t nmax, int32_t max_rhs);
+void launch_fill(const Launch& L, double* p, int64_t count, double v);
+#endif
+
+}  // namespace bemgpu

@@ -1,0 +1,302 @@
+/*
+ * bemgpu.h -- C ABI of libbemgpu.so, the GB300 (sm_103a) full-3D Helmholtz BEM library.
+ *
+ * The library replaces, for the dense full-3D boundary-element path of
+ * AcousticScattering.jl, the reference's solve and its result queries:
+ *
+ *   bem(surface::Mesh, boundary, k; ...)         solvers/bem/surface.jl:10-23
+ *   solve_full_bem(::Rigid|::PressureRelease)    solvers/bem/full.jl:52-184
+ *   solve_full_bem(::FluidFilled)                solvers/bem/full.jl:273-495
+ *   MixedRefinement (precision=:mixed)           solvers/bem/fluid_system.jl:172-309
+ *   scattering_amplitude / far_field             solvers/bem/postprocessing.jl:1-13,
+ *                                                solvers/bem/full.jl:509-519
+ *   target_strength                              postprocessing/target_strength.jl:8,26
+ *   pressure (full-BEM branch)                   fields/pressure.jl:404-471
+ *   incidence_angle_sweep (full mesh)            postprocessing/sweeps.jl:626-701
+ *   mesh(nodes, triangles) + topology checks     geometry/surface.jl:271-298, 341-405
+ *
+ * Discretisation: one unknown per flat triangle (centroid collocation), 7-point
+ * degree-5 triangle rule for regular pairs, closed-form Laplace parts plus bounded
+ * Helmholtz remainders for near pairs.  Kernel exp(ikr)/(4 pi r), exp(-i w t).
+ *
+ * Conventions shared with the reference:
+ *   - nodes are 3 x N float64 column-major (one column per vertex), triangles 3 x M
+ *     int64 column-major with 1-based vertex indices, (b-a)x(c-a) pointing outward;
+ *   - incidence direction (cos b, sin b cos a, sin b sin a): polar angle b from +x,
+ *     azimuth a from +y toward +z (solvers/bem/full.jl:14-18);
+ *   - the default observation is backscatter, x_hat = -d (postprocessing.jl:4-6);
+ *   - complex numbers are interleaved (re, im) float64 pairs.
+ *
+ * Every entry point returns a bemgpu_status; no entry point aborts the process.
+ * Functions marked [host] run without a GPU.  Objects created from one context must
+ * not be used from two host threads at the same time.
+ */
+#ifndef BEMGPU_H
+#define BEMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BEMGPU_API_VERSION 1
+
+typedef enum {
+  BEMGPU_OK = 0,
+  BEMGPU_EINVAL = 1,        /* invalid argument (reference: ArgumentError) */
+  BEMGPU_ETOPOLOGY = 2,     /* surface fails the closed/oriented/manifold checks */
+  BEMGPU_ENOMEM_BUDGET = 3, /* request exceeds the context's HBM budget */
+  BEMGPU_ESINGULAR = 4,     /* exact zero pivot in the double-precision factor */
+  BEMGPU_ENOTCONVERGED = 5, /* refinement failed even after promotion */
+  BEMGPU_ETIMEOUT = 6,      /* a bounded device wait gave up */
+  BEMGPU_ECUDA = 7,         /* CUDA runtime error */
+  BEMGPU_ENODEV = 8,        /* no usable CUDA device */
+  BEMGPU_EBUSY = 9          /* request queue full */
+} bemgpu_status;
+
+typedef enum { BEMGPU_RIGID = 0, BEMGPU_PRESSURE_RELEASE = 1, BEMGPU_FLUID = 2 } bemgpu_boundary;
+
+typedef enum {
+  BEMGPU_FORMULATION_DEFAULT = -1, /* burton_miller (rigid/soft) or muller (fluid) */
+  BEMGPU_BURTON_MILLER = 0,
+  BEMGPU_CBIE = 1,
+  BEMGPU_MULLER = 2
+} bemgpu_formulation;
+
+typedef enum { BEMGPU_DOUBLE = 0, BEMGPU_MIXED = 1 } bemgpu_precision;
+
+/*
+ * Precision of the regular (far) panel-pair quadrature.  Near and singular pairs, the
+ * hypersingular term and every residual are always FP64.  DEFAULT means FP64 for
+ * precision DOUBLE and FP32 for precision MIXED (the GB300 mixed pattern: every result
+ * then states its error against the FP64 system); ASSEMBLY_DOUBLE with precision MIXED
+ * reduces only the factorisation, which is the reference's precision=:mixed contract.
+ */
+typedef enum {
+  BEMGPU_ASSEMBLY_DEFAULT = 0,
+  BEMGPU_ASSEMBLY_DOUBLE = 1,
+  BEMGPU_ASSEMBLY_SINGLE = 2
+} bemgpu_assembly;
+
+/* Refinement outcome, reference symbols of fluid_system.jl:186-307. */
+typedef enum {
+  BEMGPU_REASON_NONE = 0,
+  BEMGPU_REASON_CONVERSION = 1,
+  BEMGPU_REASON_SINGLE_SINGULAR = 2,
+  BEMGPU_REASON_CONDITION = 3,
+  BEMGPU_REASON_NONFINITE = 4,
+  BEMGPU_REASON_ITERATION_LIMIT = 5,
+  BEMGPU_REASON_STAGNATION = 6
+} bemgpu_reason;
+
+/* Field selector of pressure(); reference fields/pressure.jl:42-53. */
+typedef enum {
+  BEMGPU_FIELD_TOTAL = 0,
+  BEMGPU_FIELD_SCATTERED = 1,
+  BEMGPU_FIELD_INCIDENT = 2,
+  BEMGPU_FIELD_INTERIOR = 3
+} bemgpu_field;
+
+typedef struct bemgpu_ctx bemgpu_ctx;
+typedef struct bemgpu_mesh bemgpu_mesh;
+typedef struct bemgpu_factor bemgpu_factor;
+typedef struct bemgpu_solution bemgpu_solution;
+
+/*
+ * One boundary-value problem on one surface.  Keyword arguments of the reference's
+ * solve_full_bem (full.jl:52-58, 273-279) map to fields here.
+ */
+typedef struct {
+  int32_t boundary;            /* bemgpu_boundary */
+  int32_t formulation;         /* bemgpu_formulation */
+  int32_t precision;           /* bemgpu_precision; mixed: complex64 factor + refinement */
+  int32_t equilibrate;         /* row/column max scaling before the factor (default 1) */
+  double k;                    /* exterior wavenumber [1/m], finite and > 0 */
+  double density_contrast;     /* g = rho_int / rho_ext (fluid) */
+  double soundspeed_contrast;  /* h = c_int / c_ext (fluid); k_int = k / h */
+  double refine_tolerance;     /* backward-error acceptance (default 1e-13) */
+  int32_t refine_maxiter;      /* corrections before promotion (default 8) */
+  int32_t assembly;            /* bemgpu_assembly: precision of the regular-pair quadrature */
+  double condition_guard;      /* single rcond guard (default 10 eps(float32)) */
+  double near_eta;             /* near-pair radius in source diameters (default 2) */
+} bemgpu_problem;
+
+/* Diagnostics of one solution; names follow the reference's diagnostics() fields. */
+typedef struct {
+  int64_t unknown_count;           /* n (rigid/soft) or 2n (fluid) */
+  int64_t quadrature_nodes;        /* collocation points = panels */
+  int64_t near_pairs;              /* pairs integrated with the singular rules */
+  int32_t formulation;
+  int32_t precision;               /* requested bemgpu_precision */
+  int32_t factor_precision;        /* 0 single (complex64), 1 double (complex128) */
+  int32_t refinement_reason;       /* bemgpu_reason (max severity over right-hand sides) */
+  int32_t refinement_iterations;   /* corrections (max over right-hand sides) */
+  int32_t equilibrate;
+  double coupling_re, coupling_im; /* Burton-Miller alpha = i/k */
+  double absolute_residual;        /* ||A x - b||_2 (max over right-hand sides) */
+  double relative_residual;        /* ... / ||b||_2 */
+  double scaled_absolute_residual; /* in the equilibrated equations */
+  double scaled_relative_residual;
+  double normwise_backward_error;
+  double componentwise_backward_error;
+  double single_reciprocal_condition; /* infinity-norm rcond of the complex64 factor */
+  double assemble_ms, factor_ms, solve_ms, total_ms;
+  int64_t device_bytes;            /* bytes held by the factor */
+  int32_t nrhs;
+  int32_t info;                    /* first exact zero pivot (1-based) of the factor, 0 if none */
+} bemgpu_diagnostics;
+
+/* ------------------------------------------------------------------ host utilities */
+/* [host] Library version string. */
+const char *bemgpu_version(void);
+/* [host] Text of a status code. */
+const char *bemgpu_status_string(int status);
+/* [host] Fill a problem with the reference's defaults (rigid, Burton-Miller, double). */
+void bemgpu_problem_init(bemgpu_problem *p);
+
+/*
+ * [host] Topology validation of a supplied flat-triangle surface, replacing
+ * mesh(nodes, triangles) input checks (geometry/surface.jl:275-283) and
+ * _validate_surface_topology (geometry/surface.jl:341-405): finite nodes, valid
+ * indices, no repeated node, no degenerate triangle, exactly two triangles per edge
+ * with opposite orientation, one connected component, manifold vertices, positive
+ * enclosed volume.  resolution receives the longest edge.  BEMGPU_ETOPOLOGY or
+ * BEMGPU_EINVAL with a message in err.
+ */
+int bemgpu_mesh_validate(const double *nodes, int64_t n_nodes, const int64_t *triangles,
+                         int64_t n_triangles, double *resolution, char *err, size_t errlen);
+
+/* [host] SHA-256 over (N, M, nodes, triangles) as little-endian int64/float64, hex. */
+int bemgpu_mesh_hash(const double *nodes, int64_t n_nodes, const int64_t *triangles,
+                     int64_t n_triangles, char out_hex[65]);
+
+/*
+ * [host] Near-pair list in CSR form: pair (i, j) is near when i == j or the squared
+ * centroid distance is below eta^2 times the squared longest edge of panel j.
+ * rowptr has n_triangles + 1 entries; *count receives the number of pairs; returns
+ * BEMGPU_EINVAL (with *count set) when cap is too small.
+ */
+int bemgpu_near_pairs(const double *nodes, int64_t n_nodes, const int64_t *triangles,
+                      int64_t n_triangles, double eta, int64_t *rowptr, int64_t *cols,
+                      int64_t cap, int64_t *count);
+
+/* ------------------------------------------------------------------ context */
+/* Create a context on a device; hbm_budget_bytes = 0 means 90% of free memory. */
+int bemgpu_ctx_create(int device, uint64_t hbm_budget_bytes, bemgpu_ctx **ctx);
+int bemgpu_ctx_destroy(bemgpu_ctx *ctx);
+/* Last error message of the context (or of the process when ctx is NULL). */
+int bemgpu_last_error(const bemgpu_ctx *ctx, char *buf, size_t len);
+/* Bytes currently held against the budget, and the budget. */
+int bemgpu_ctx_memory(const bemgpu_ctx *ctx, uint64_t *used, uint64_t *budget);
+/* Block until all work of the context has finished. */
+int bemgpu_ctx_synchronize(bemgpu_ctx *ctx);
+
+/* ------------------------------------------------------------------ meshes */
+/* Validate (as bemgpu_mesh_validate), hash and upload a surface; panel geometry is
+ * derived on the device. */
+int bemgpu_mesh_upload(bemgpu_ctx *ctx, const double *nodes, int64_t n_nodes,
+                       const int64_t *triangles, int64_t n_triangles, bemgpu_mesh **mesh);
+int bemgpu_mesh_info(const bemgpu_mesh *mesh, int64_t *n_panels, double *resolution,
+                     char hash_hex[65]);
+int bemgpu_mesh_destroy(bemgpu_mesh *mesh);
+
+/* ------------------------------------------------------------------ factor and solve */
+/*
+ * Assemble and factor the system of one problem (the reference's
+ * _assemble_full_boundary / _assemble_full_fluid followed by _factor_fluid_system or
+ * MixedRefinement.factorize_refined).  The factor keeps the complex128 system for
+ * residuals and can serve any number of incidence directions.
+ */
+int bemgpu_factor_create(bemgpu_ctx *ctx, const bemgpu_mesh *mesh,
+                         const bemgpu_problem *problem, bemgpu_factor **factor);
+
+/*
+ * Batched assembly + factorisation of `count` problems in fused launches (one CUDA
+ * graph over all instances; meshes may differ in size).  factors[i] receives the
+ * factor of problems[i].
+ */
+int bemgpu_factor_create_batch(bemgpu_ctx *ctx, int32_t count,
+                               const bemgpu_mesh *const *meshes,
+                               const bemgpu_problem *problems, bemgpu_factor **factors);
+
+/*
+ * Solve for nrhs plane waves with incidence (polar, azimuth) pairs in `incidence`
+ * (2 * nrhs doubles).  Replaces _solve_full_boundary (full.jl:130-184) and
+ * _solve_full_fluid (full.jl:456-495), including mixed refinement.
+ */
+int bemgpu_factor_solve(bemgpu_factor *factor, int32_t nrhs, const double *incidence,
+                        bemgpu_solution **solution);
+
+/* Solve many (factor, incidence set) pairs with batched kernels. */
+int bemgpu_factor_solve_batch(bemgpu_ctx *ctx, int32_t count, bemgpu_factor *const *factors,
+                              const int32_t *nrhs, const double *const *incidence,
+                              bemgpu_solution **solutions);
+
+int bemgpu_factor_destroy(bemgpu_factor *factor);
+int bemgpu_factor_diagnostics(const bemgpu_factor *factor, bemgpu_diagnostics *out);
+
+/* factor_create + factor_solve + factor_destroy: the reference's bem(surface, ...). */
+int bemgpu_solve(bemgpu_ctx *ctx, const bemgpu_mesh *mesh, const bemgpu_problem *problem,
+                 int32_t nrhs, const double *incidence, bemgpu_solution **solution);
+
+/* ------------------------------------------------------------------ queries */
+/*
+ * Far-field amplitude f(x_hat) of right-hand side `rhs` at ndir unit directions
+ * (3 * ndir doubles); out receives 2 * ndir doubles.  dirs == NULL means backscatter.
+ * Replaces far_field (full.jl:509-519) / scattering_amplitude (postprocessing.jl:1-13).
+ */
+int bemgpu_far_field(bemgpu_solution *sol, int32_t rhs, int64_t ndir, const double *dirs,
+                     double *out);
+/* 20 log10 |f| at the same directions (target_strength.jl:8, 26). */
+int bemgpu_target_strength(bemgpu_solution *sol, int32_t rhs, int64_t ndir,
+                           const double *dirs, double *out);
+/* Scattered surface traces p_scat, dpdn_scat of one right-hand side (2 * n doubles each). */
+int bemgpu_traces(const bemgpu_solution *sol, int32_t rhs, double *p_scat, double *dpdn_scat);
+int bemgpu_solution_diagnostics(const bemgpu_solution *sol, bemgpu_diagnostics *out);
+/*
+ * Pressure at npts points (3 * npts doubles, out 2 * npts doubles) by the layer
+ * potentials of the surface traces, fields/pressure.jl:404-471.  Points on the
+ * surface or on the wrong side for `field` give BEMGPU_EINVAL.
+ */
+int bemgpu_pressure(bemgpu_solution *sol, int32_t rhs, int64_t npts, const double *points,
+                    int32_t field, double *out);
+int bemgpu_solution_destroy(bemgpu_solution *sol);
+
+/* ------------------------------------------------------------------ dense linear algebra */
+/*
+ * Solve A X = B for a caller-supplied dense complex matrix (n x n column-major,
+ * interleaved complex128) and nrhs right-hand sides (n x nrhs, overwritten by X), with
+ * the same equilibrated factor / mixed refinement the BEM systems use.  Replaces
+ * _factor_fluid_system + _solve_fluid_system (full.jl:364-440) for hand-built
+ * matrices; diag (optional) receives the refinement report.
+ */
+int bemgpu_dense_solve(bemgpu_ctx *ctx, int64_t n, const double *A, int32_t nrhs, double *B,
+                       int32_t precision, int32_t equilibrate, double refine_tolerance,
+                       int32_t refine_maxiter, double condition_guard,
+                       bemgpu_diagnostics *diag);
+
+/* Assembled operators of a problem for inspection (rigid/soft: M1 and M2 n x n; fluid:
+ * A 2n x 2n in M1, M2 unused).  Column-major interleaved complex128. */
+int bemgpu_assemble_dense(bemgpu_ctx *ctx, const bemgpu_mesh *mesh,
+                          const bemgpu_problem *problem, double *M1, double *M2);
+
+/* ------------------------------------------------------------------ profiling */
+/*
+ * Kernel timing with CUDA events recorded on the launching stream around every launch
+ * of the named kernel family ("assemble", "near", "getf2", "trsm", "gemm", "gemm_tc",
+ * "far_field", "residual", ...).  enable = 0 stops recording; read returns the number
+ * of launches and their summed device time since the last reset.
+ */
+int bemgpu_profile_enable(bemgpu_ctx *ctx, int32_t enable);
+int bemgpu_profile_reset(bemgpu_ctx *ctx);
+int bemgpu_profile_read(bemgpu_ctx *ctx, const char *family, int64_t *launches,
+                        double *total_ms);
+/* Number of library kernel launches issued since the context was created. */
+int bemgpu_launch_count(const bemgpu_ctx *ctx, int64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BEMGPU_H */

@@ -1,0 +1,379 @@
+"""CPU FP64 oracle for the full-3D collocation BEM (test infrastructure only).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import this
+module, always as the checker of the CUDA library, never as a product path.
+
+Layers:
+  * ``Panels``          -- ctypes view of the C restatement in ``bem_oracle.c``;
+  * ``assemble_*``      -- dense system operators (reference block algebra,
+                           solvers/bem/full.jl:68-128 and :289-346);
+  * ``factor_fluid`` / ``solve_fluid`` -- equilibration + LAPACK LU
+                           (full.jl:364-409, :422-440);
+  * ``MixedRefinement`` -- complex64 LU with complex128 residual refinement and the
+                           promotion state machine (solvers/bem/fluid_system.jl:172-309);
+  * ``solve``           -- the ``bem`` call chain for one mesh, boundary and k
+                           (full.jl:52-184, :273-495), returning scattered traces;
+  * ``far_field``       -- full.jl:509-519;  ``target_strength`` -- target_strength.jl:8.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+
+import numpy as np
+import scipy.linalg as sla
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+NEAR_ETA = 2.0
+
+
+def build() -> str:
+    """Compile liboracle.so in place (make); returns its path."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return os.path.join(_HERE, "liboracle.so")
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = ctypes.CDLL(path)
+        dp, i64, vp = ctypes.POINTER(ctypes.c_double), ctypes.c_int64, ctypes.c_void_p
+        L.oracle_panel_size.restype = ctypes.c_int
+        L.oracle_panels.argtypes = [dp, i64, ctypes.POINTER(ctypes.c_int64), i64, vp]
+        L.oracle_panels.restype = ctypes.c_int
+        L.oracle_near_pairs.argtypes = [vp, i64, ctypes.c_double,
+                                        ctypes.POINTER(ctypes.c_int64),
+                                        ctypes.POINTER(ctypes.c_int64), i64]
+        L.oracle_near_pairs.restype = ctypes.c_int64
+        L.oracle_assemble_bm.argtypes = [vp, i64, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_int, dp, dp]
+        L.oracle_assemble_fluid.argtypes = [vp, i64, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_int, dp]
+        L.oracle_incident.argtypes = [vp, i64, ctypes.c_double, dp, dp, dp]
+        L.oracle_far_field.argtypes = [vp, i64, ctypes.c_double, dp, dp, dp, dp]
+        L.oracle_pair_ops.argtypes = [vp, i64, i64, ctypes.c_int, ctypes.c_double, dp]
+        L.oracle_laplace_parts.argtypes = [vp, dp, dp, ctypes.c_int, dp]
+        _LIB = L
+    return _LIB
+
+
+def _dp(a):
+    """Raw double* of a contiguous (C or Fortran order) float64 or complex128 array."""
+    assert a.flags.c_contiguous or a.flags.f_contiguous
+    return ctypes.cast(a.ctypes.data, ctypes.POINTER(ctypes.c_double))
+
+
+class Panels:
+    """Panel geometry of a validated (nodes 3xN, triangles 3xM 1-based) surface."""
+
+    def __init__(self, nodes, triangles):
+        L = lib()
+        self.nodes = np.asfortranarray(nodes, dtype=np.float64)
+        self.tris = np.asfortranarray(triangles, dtype=np.int64)
+        self.n = self.tris.shape[1]
+        self._buf = ctypes.create_string_buffer(L.oracle_panel_size() * self.n)
+        rc = L.oracle_panels(_dp(self.nodes), self.nodes.shape[1],
+                             self.tris.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                             self.n, self._buf)
+        if rc != 0:
+            raise ValueError(f"invalid surface (code {rc})")
+        raw = np.frombuffer(self._buf, dtype=np.float64).reshape(self.n, -1)
+        # record layout: v[3][3], c[3], n[3], area, diam, g[7][3]
+        self.vertices = raw[:, 0:9].reshape(self.n, 3, 3)
+        self.centroids = raw[:, 9:12]
+        self.normals = raw[:, 12:15]
+        self.areas = raw[:, 15]
+        self.diams = raw[:, 16]
+        self.gauss = raw[:, 17:38].reshape(self.n, 7, 3)
+
+    @property
+    def ptr(self):
+        return self._buf
+
+    def near_pairs(self, eta=NEAR_ETA):
+        rowptr = np.zeros(self.n + 1, dtype=np.int64)
+        cap = 64 * self.n
+        while True:
+            cols = np.zeros(cap, dtype=np.int64)
+            cnt = lib().oracle_near_pairs(
+                self._buf, self.n, eta,
+                rowptr.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                cols.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), cap)
+            if cnt >= 0:
+                return rowptr, cols[:cnt].copy()
+            cap *= 4
+
+    def pair_ops(self, i, j, near, k):
+        out = np.zeros(8)
+        lib().oracle_pair_ops(self._buf, i, j, int(near), k, _dp(out))
+        return out[0::2] + 1j * out[1::2]
+
+    def laplace_parts(self, j, x, nx, self_panel=False):
+        out = np.zeros(4)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        nx = np.ascontiguousarray(nx, dtype=np.float64)
+        rec = ctypes.byref(self._buf, j * lib().oracle_panel_size())
+        lib().oracle_laplace_parts(rec, _dp(x), _dp(nx), int(self_panel), _dp(out))
+        return out
+
+
+def incidence_direction(beta, alpha):
+    """Polar angle from +x, azimuth from +y toward +z (solvers/bem/full.jl:14-18)."""
+    return np.array([math.cos(beta), math.sin(beta) * math.cos(alpha),
+                     math.sin(beta) * math.sin(alpha)])
+
+
+def assemble_bm(P: Panels, k, burton_miller=True, eta=NEAR_ETA):
+    n = P.n
+    M1 = np.zeros((n, n), dtype=np.complex128, order="F")
+    M2 = np.zeros((n, n), dtype=np.complex128, order="F")
+    lib().oracle_assemble_bm(P.ptr, n, eta, float(k), int(burton_miller),
+                             _dp(M1), _dp(M2))
+    return M1, M2
+
+
+def assemble_fluid(P: Panels, k, g, h, formulation="muller", eta=NEAR_ETA):
+    n = P.n
+    A = np.zeros((2 * n, 2 * n), dtype=np.complex128, order="F")
+    lib().oracle_assemble_fluid(P.ptr, n, eta, float(k), float(g), float(h),
+                                0 if formulation == "muller" else 1,
+                                _dp(A))
+    return A
+
+
+def incident(P: Panels, k, direction):
+    d = np.ascontiguousarray(direction, dtype=np.float64)
+    p = np.zeros(P.n, dtype=np.complex128)
+    q = np.zeros(P.n, dtype=np.complex128)
+    lib().oracle_incident(P.ptr, P.n, float(k), _dp(d), _dp(p),
+                          _dp(q))
+    return p, q
+
+
+def far_field(P: Panels, k, xhat, p, q):
+    out = np.zeros(2)
+    xh = np.ascontiguousarray(xhat, dtype=np.float64)
+    p = np.ascontiguousarray(p, dtype=np.complex128)
+    q = np.ascontiguousarray(q, dtype=np.complex128)
+    lib().oracle_far_field(P.ptr, P.n, float(k), _dp(xh), _dp(p),
+                           _dp(q), _dp(out))
+    return complex(out[0], out[1])
+
+
+def target_strength(f):
+    """20 log10 |f| (postprocessing/target_strength.jl:8)."""
+    return 20.0 * math.log10(abs(f))
+
+
+# ---------------------------------------------------------------- dense factor/solve
+def equilibrate(A):
+    """Row max, then column max of the row-scaled matrix (full.jl:388-394)."""
+    rows = np.max(np.abs(A), axis=1)
+    rows[rows == 0] = 1.0
+    scaled = A / rows[:, None]
+    cols = np.max(np.abs(scaled), axis=0)
+    cols[cols == 0] = 1.0
+    return rows, cols, scaled / cols[None, :]
+
+
+class DoubleFactor:
+    """Equilibrated complex128 LU (full.jl:364-409 with precision=:double)."""
+
+    def __init__(self, A, equilibrate_rows=True):
+        self.A = A
+        if equilibrate_rows:
+            self.rows, self.cols, S = equilibrate(A)
+        else:
+            self.rows = self.cols = None
+            S = A.copy()
+        self.lu = sla.lu_factor(S, check_finite=False)
+
+    def solve(self, b):
+        sb = b if self.rows is None else b / self.rows[:, None] if b.ndim == 2 else b / self.rows
+        sx = sla.lu_solve(self.lu, sb, check_finite=False)
+        if self.cols is None:
+            return sx
+        return sx / (self.cols[:, None] if sx.ndim == 2 else self.cols)
+
+
+class MixedRefinement:
+    """Guarded complex64 factorisation with complex128 residual refinement.
+
+    Restates MixedRefinement in solvers/bem/fluid_system.jl:172-309: equilibration
+    (:196-211), conversion check (:218), single LU + singular check (:219-221),
+    infinity-norm reciprocal condition guard (:222-225), corrections (:229-239),
+    backward errors (:241-262) and the accept / promote loop (:264-307).
+    """
+
+    def __init__(self, A, condition_guard=10 * np.finfo(np.float32).eps):
+        n, m = A.shape
+        if n != m or n == 0:
+            raise ValueError("expected a nonempty square matrix")
+        if not np.all(np.isfinite(A)):
+            raise ValueError("matrix must be finite")
+        self.A = A
+        rows = np.max(np.abs(A), axis=1)
+        rows[rows == 0] = 1.0
+        cols = np.max(np.abs(A / rows[:, None]), axis=0)
+        cols[cols == 0] = 1.0
+        self.rows, self.cols = rows, cols
+        self.matrix_norm = float(np.max(np.sum(np.abs(A), axis=1)))
+        self.precision, self.reason = "single", "none"
+        self.rcond = float("nan")
+        with np.errstate(over="ignore", invalid="ignore"):
+            low = (A / rows[:, None] / cols[None, :]).astype(np.complex64)
+        if not np.all(np.isfinite(low)):
+            self.promote("conversion")
+            return
+        anorm = float(np.max(np.sum(np.abs(low), axis=1)))
+        lu, piv, info = sla.lapack.cgetrf(low)
+        if info > 0:
+            self.promote("single_singular")
+            return
+        self.lu = (lu, piv)
+        rc, info = sla.lapack.cgecon(lu, anorm, norm="I")
+        self.rcond = float(rc)
+        if not math.isfinite(self.rcond) or self.rcond <= condition_guard:
+            self.promote("condition")
+
+    def promote(self, reason):
+        scaled = self.A / self.rows[:, None] / self.cols[None, :]
+        self.lu = sla.lu_factor(scaled, check_finite=False)
+        self.precision, self.reason = "double", reason
+
+    def correction(self, rhs):
+        scaled = rhs / self.rows
+        mag = float(np.max(np.abs(scaled))) if scaled.size else 0.0
+        if not math.isfinite(mag):
+            return np.full(rhs.shape, complex("nan"), dtype=np.complex128)
+        if mag == 0.0:
+            return np.zeros_like(rhs)
+        work = scaled / mag
+        if self.precision == "single":
+            lu, piv = self.lu
+            x, info = sla.lapack.cgetrs(lu, piv, work.astype(np.complex64))
+            v = x.astype(np.complex128)
+        else:
+            v = sla.lu_solve(self.lu, work, check_finite=False)
+        return v * mag / self.cols
+
+    def backward_errors(self, x, b):
+        residual = b - self.A @ x
+        den = np.abs(b) + np.abs(self.A) @ np.abs(x)
+        if not (np.all(np.isfinite(residual)) and np.all(np.isfinite(den))):
+            return residual, math.inf, math.inf
+        ar = np.abs(residual)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            ratio = np.where(den == 0, np.where(ar == 0, 0.0, np.inf), ar / den)
+        comp = float(np.max(ratio)) if ratio.size else 0.0
+        scale = self.matrix_norm * float(np.max(np.abs(x))) + float(np.max(np.abs(b)))
+        rn = float(np.max(ar))
+        if not math.isfinite(scale):
+            norm = math.inf
+        elif scale == 0.0:
+            norm = 0.0 if rn == 0.0 else math.inf
+        else:
+            norm = rn / scale
+        return residual, norm, comp
+
+    def solve(self, b, tolerance=1e-13, maxiter=8):
+        x = self.correction(b)
+        history = []
+        corrections = attempts = stalls = 0
+        previous = math.inf
+        while True:
+            residual, nw, cw = self.backward_errors(x, b)
+            metric = max(nw, cw)
+            history.append((self.precision, nw, cw))
+            if math.isfinite(metric) and metric <= tolerance:
+                return dict(x=x, precision=self.precision, reason=self.reason,
+                            corrections=corrections, history=history, normwise=nw,
+                            componentwise=cw)
+            stalls = stalls + 1 if metric >= previous * 0.9 else 0
+            reason = ("nonfinite" if not math.isfinite(metric) else
+                      "iteration_limit" if attempts >= maxiter else
+                      "stagnation" if stalls >= 2 else None)
+            if reason is not None:
+                if self.precision == "double":
+                    raise RuntimeError(f"double-precision fallback failed: {reason}")
+                self.promote(reason)
+                x = self.correction(b)
+                previous, attempts, stalls = math.inf, 0, 0
+                continue
+            updated = x + self.correction(residual)
+            if np.array_equal(updated, x):
+                if self.precision == "double":
+                    raise RuntimeError("double-precision correction stagnated")
+                self.promote("stagnation")
+                x = self.correction(b)
+                previous, attempts, stalls = math.inf, 0, 0
+                continue
+            x = updated
+            previous = metric
+            corrections += 1
+            attempts += 1
+
+
+# ---------------------------------------------------------------- the solve chain
+def solve(nodes, triangles, boundary, k, incidence_angle=math.pi / 2,
+          incidence_azimuth=0.0, formulation=None, g=1.0, h=1.0, precision="double",
+          equilibrate_rows=True, directions=None, eta=NEAR_ETA, panels=None):
+    """Scattered traces and far-field amplitudes for one (mesh, boundary, k, incidence).
+
+    boundary: "rigid", "pressure_release" or "fluid".  Returns a dict with p_scat,
+    dpdn_scat, the amplitudes at ``directions`` (default backscatter) and the panels.
+    """
+    if not (math.isfinite(k) and k > 0):
+        raise ValueError("k must be finite and positive")
+    P = panels if panels is not None else Panels(nodes, triangles)
+    n = P.n
+    d = incidence_direction(incidence_angle, incidence_azimuth)
+    p_inc, q_inc = incident(P, k, d)
+    info = {}
+    if boundary in ("rigid", "pressure_release"):
+        formulation = formulation or "burton_miller"
+        M1, M2 = assemble_bm(P, k, formulation == "burton_miller", eta)
+        if boundary == "rigid":
+            A, b = M1, M2 @ q_inc
+        else:
+            A, b = M2, M1 @ p_inc
+        F = DoubleFactor(A, equilibrate_rows)
+        x = F.solve(b)
+        if boundary == "rigid":
+            p_s, q_s = x, -q_inc
+        else:
+            p_s, q_s = -p_inc, x
+    elif boundary == "fluid":
+        formulation = formulation or "muller"
+        A = assemble_fluid(P, k, g, h, formulation, eta)
+        if formulation == "muller":
+            b = np.concatenate([p_inc, q_inc])
+        else:
+            b = np.zeros(2 * n, dtype=np.complex128)
+            b[n:] = -(A[n:, :] @ np.concatenate([p_inc, q_inc]))
+        if precision == "mixed":
+            F = MixedRefinement(A)
+            res = F.solve(b)
+            x = res["x"]
+            info.update(res)
+        else:
+            F = DoubleFactor(A, equilibrate_rows)
+            x = F.solve(b)
+        p_s, q_s = x[:n], x[n:]
+        if formulation == "muller":
+            p_s, q_s = p_s - p_inc, q_s - q_inc
+    else:
+        raise ValueError(f"unknown boundary {boundary!r}")
+    if directions is None:
+        directions = [-d]
+    amps = np.array([far_field(P, k, xh, p_s, q_s) for xh in directions])
+    info.update(p_scat=p_s, dpdn_scat=q_s, amplitudes=amps, panels=P, A=A, b=b, x=x)
+    return info
