@@ -9,11 +9,13 @@ from . import meshes
 from ._lib import lib, LIB_PATH
 from .api import (ArgumentError, BEMGPUError, BEMSolution, Context, Factor, FluidFilled,
                   FrequencySweep, GasFilled, Mesh, PressureRelease, Rigid, SweepResult,
-                  assemble, bem, context, dense_solve, diagnostics, frequency_sweep,
+                  assemble, bem, context, dense_solve, diagnostics, factor_batch,
+                  frequency_sweep, solve_batch,
                   incidence_angle_sweep, mesh, scattering_amplitude, target_strength)
 
 __all__ = ["ArgumentError", "BEMGPUError", "BEMSolution", "Context", "Factor", "FluidFilled",
            "FrequencySweep", "GasFilled", "Mesh", "PressureRelease", "Rigid", "SweepResult",
-           "assemble", "bem", "context", "dense_solve", "diagnostics", "frequency_sweep",
+           "assemble", "bem", "context", "dense_solve", "diagnostics", "factor_batch",
+           "frequency_sweep", "solve_batch",
            "incidence_angle_sweep", "mesh", "meshes", "scattering_amplitude",
            "target_strength", "lib", "LIB_PATH"]

@@ -101,6 +101,8 @@ SIGNATURES = {
     "bemgpu_profile_reset": (ctypes.c_int, [_vp]),
     "bemgpu_profile_read": (ctypes.c_int, [_vp, ctypes.c_char_p, _i64p, _dp]),
     "bemgpu_launch_count": (ctypes.c_int, [_vp, _i64p]),
+    "bemgpu_timer_start": (ctypes.c_int, [_vp]),
+    "bemgpu_timer_stop": (ctypes.c_int, [_vp, _dp]),
 }
 
 _LIB = None

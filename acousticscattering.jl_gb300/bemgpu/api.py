@@ -130,6 +130,14 @@ class Context:
                                            ctypes.byref(ms)), self.handle)
         return n.value, ms.value
 
+    def timer_start(self):
+        _check(C.lib().bemgpu_timer_start(self.handle), self.handle)
+
+    def timer_stop(self) -> float:
+        ms = ctypes.c_double()
+        _check(C.lib().bemgpu_timer_stop(self.handle, ctypes.byref(ms)), self.handle)
+        return ms.value
+
     @staticmethod
     def launch_count() -> int:
         n = ctypes.c_int64()
@@ -246,6 +254,26 @@ def _problem(boundary, k, formulation=None, precision="double", equilibrate=True
     maxiter = refinement.get("maxiter", 8)
     if not isinstance(maxiter, (int, np.integer)) or maxiter < 0:
         raise ArgumentError("maxiter must be a nonnegative integer")
+    k = float(k)
+    if not (math.isfinite(k) and k > 0):
+        raise ArgumentError("k must be finite and positive")
+    if precision == "mixed" and not equilibrate:
+        raise ArgumentError("mixed precision requires equilibrate=true")
+    tol = refinement.get("tolerance", 1e-13)
+    if not (math.isfinite(tol) and 0 < tol < 1):
+        raise ArgumentError("invalid refinement tolerance")
+    guard = refinement.get("condition_guard", 10 * float(np.finfo(np.float32).eps))
+    if not (math.isfinite(guard) and guard >= 0):
+        raise ArgumentError("invalid condition guard")
+    if isinstance(boundary, FluidFilled):
+        g, h = boundary.density_contrast, boundary.soundspeed_contrast
+        if not (math.isfinite(g) and g > 0 and math.isfinite(h) and h > 0):
+            raise ArgumentError(
+                "fluid density and soundspeed contrasts must be finite and positive")
+        if formulation not in (None, "muller", "cbie"):
+            raise ArgumentError("fluid formulation must be :muller or :cbie")
+    elif formulation not in (None, "burton_miller", "cbie"):
+        raise ArgumentError("formulation must be :cbie or :burton_miller")
     p = C.Problem()
     C.lib().bemgpu_problem_init(ctypes.byref(p))
     p.boundary = boundary.code
@@ -290,14 +318,21 @@ class Factor:
     of incidence directions (the reuse of incidence_angle_sweep, sweeps.jl:680-701)."""
 
     def __init__(self, surface: Mesh, boundary, k, ctx: Context | None = None, **options):
+        self.problem = _problem(boundary, k, **options)
         self.ctx = ctx or context()
         self.surface, self.boundary, self.k = surface, boundary, float(k)
-        self.problem = _problem(boundary, k, **options)
         h = ctypes.c_void_p()
         _check(C.lib().bemgpu_factor_create(self.ctx.handle, surface.handle(self.ctx),
                                             ctypes.byref(self.problem), ctypes.byref(h)),
                self.ctx.handle)
         self.handle = h
+
+    @classmethod
+    def _wrap(cls, ctx, handle, surface, boundary, k, problem):
+        f = cls.__new__(cls)
+        f.ctx, f.handle, f.surface, f.boundary, f.k, f.problem = (ctx, handle, surface,
+                                                                  boundary, float(k), problem)
+        return f
 
     def solve(self, angles, azimuths=0.0) -> "BEMSolution":
         angles = np.atleast_1d(np.asarray(angles, dtype=np.float64))
@@ -416,6 +451,52 @@ def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_az
         return f.solve([incidence_angle], [incidence_azimuth])
     finally:
         f.close()
+
+
+def factor_batch(items, ctx: Context | None = None):
+    """Assemble and factor many problems in fused batched launches.
+
+    ``items``: sequence of (surface, boundary, k, options-dict).  Returns Factors in order.
+    """
+    ctx = ctx or context()
+    items = list(items)
+    if not items:
+        raise ArgumentError("empty batch")
+    probs = (C.Problem * len(items))()
+    meshes = (ctypes.c_void_p * len(items))()
+    for t, (surf, bc, k, opts) in enumerate(items):
+        probs[t] = _problem(bc, k, **(opts or {}))
+        meshes[t] = surf.handle(ctx)
+    outs = (ctypes.c_void_p * len(items))()
+    _check(C.lib().bemgpu_factor_create_batch(ctx.handle, len(items), meshes, probs, outs),
+           ctx.handle)
+    return [Factor._wrap(ctx, ctypes.c_void_p(outs[t]), items[t][0], items[t][1], items[t][2],
+                         probs[t]) for t in range(len(items))]
+
+
+def solve_batch(factors, angles, azimuths=None):
+    """Solve every factor for its incidence set in one batched launch sequence.
+
+    ``angles[i]`` (and ``azimuths[i]``) are the polar (azimuthal) angles of factor i."""
+    factors = list(factors)
+    ctx = factors[0].ctx
+    n = len(factors)
+    incs, keep = [], []
+    nr = (ctypes.c_int32 * n)()
+    ptrs = (ctypes.POINTER(ctypes.c_double) * n)()
+    for t, f in enumerate(factors):
+        a = np.atleast_1d(np.asarray(angles[t], dtype=np.float64))
+        z = np.broadcast_to(np.asarray(0.0 if azimuths is None else azimuths[t],
+                                       dtype=np.float64), a.shape)
+        inc = np.ascontiguousarray(np.stack([a, z], axis=1).reshape(-1))
+        keep.append((a, z, inc))
+        nr[t] = len(a)
+        ptrs[t] = C.dptr(inc)
+    fh = (ctypes.c_void_p * n)(*[f.handle for f in factors])
+    outs = (ctypes.c_void_p * n)()
+    _check(C.lib().bemgpu_factor_solve_batch(ctx.handle, n, fh, nr, ptrs, outs), ctx.handle)
+    return [BEMSolution(ctx, ctypes.c_void_p(outs[t]), factors[t].surface, factors[t].boundary,
+                        factors[t].k, keep[t][0], keep[t][1]) for t in range(n)]
 
 
 def scattering_amplitude(sol: BEMSolution, *, direction=None, rhs: int = 0) -> complex:

@@ -47,6 +47,7 @@ struct bemgpu_ctx {
   std::multimap<size_t, void*> cache;
   uint64_t cached = 0;
   bool prof = false;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
   std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
   std::recursive_mutex mu;
   Launch launch() const { return Launch{stream, d_err}; }
@@ -738,8 +739,27 @@ int getrf_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, int prec, bool prom
   Buf d;
   TRY(to_device(c, mi, &d));
   {
-    Prof pr(c, prec ? "getrf_c64" : "getrf_c128");
-    launch_getrf_simt(L, d.as<MatInst>(), (int)fs.size(), nmax, prec);
+    // right-looking blocked LU; each kernel family is timed on its own
+    const MatInst* dm = d.as<MatInst>();
+    const int ni = (int)fs.size();
+    for (int64_t k0 = 0; k0 < nmax; k0 += kPanelNB) {
+      {
+        Prof pr(c, "getf2");
+        launch_getf2(L, dm, ni, k0, kPanelNB, prec);
+      }
+      {
+        Prof pr(c, "laswp");
+        launch_laswp(L, dm, ni, k0, kPanelNB, nmax, prec);
+      }
+      {
+        Prof pr(c, "trsm");
+        launch_trsm_panel(L, dm, ni, k0, kPanelNB, nmax, prec);
+      }
+      {
+        Prof pr(c, prec ? "gemm_c64" : "gemm_c128");
+        launch_gemm_update(L, dm, ni, k0, kPanelNB, nmax, prec);
+      }
+    }
   }
   CUDA_TRY(c, cudaGetLastError());
   for (size_t t = 0; t < fs.size(); ++t) {
@@ -1485,6 +1505,8 @@ int bemgpu_ctx_destroy(bemgpu_ctx* c) {
       cudaEventDestroy(pr.second);
     }
   drop_cache(c);
+  if (c->t0) cudaEventDestroy(c->t0);
+  if (c->t1) cudaEventDestroy(c->t1);
   cudaFree(c->d_err);
   cudaStreamDestroy(c->stream);
   delete c;
@@ -1978,6 +2000,28 @@ int bemgpu_profile_read(bemgpu_ctx* c, const char* family, int64_t* launches, do
     }
   if (launches) *launches = cnt;
   if (total_ms) *total_ms = ms;
+  return BEMGPU_OK;
+}
+
+int bemgpu_timer_start(bemgpu_ctx* c) {
+  if (!c) return fail(nullptr, BEMGPU_EINVAL, "null context");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  if (!c->t0) {
+    CUDA_TRY(c, cudaEventCreate(&c->t0));
+    CUDA_TRY(c, cudaEventCreate(&c->t1));
+  }
+  CUDA_TRY(c, cudaEventRecord(c->t0, c->stream));
+  return BEMGPU_OK;
+}
+
+int bemgpu_timer_stop(bemgpu_ctx* c, double* ms) {
+  if (!c || !ms || !c->t0) return fail(c, BEMGPU_EINVAL, "timer not started");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  CUDA_TRY(c, cudaEventRecord(c->t1, c->stream));
+  CUDA_TRY(c, cudaEventSynchronize(c->t1));
+  float m = 0.f;
+  CUDA_TRY(c, cudaEventElapsedTime(&m, c->t0, c->t1));
+  *ms = m;
   return BEMGPU_OK;
 }
 

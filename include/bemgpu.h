@@ -293,8 +293,12 @@ int bemgpu_profile_enable(bemgpu_ctx *ctx, int32_t enable);
 int bemgpu_profile_reset(bemgpu_ctx *ctx);
 int bemgpu_profile_read(bemgpu_ctx *ctx, const char *family, int64_t *launches,
                         double *total_ms);
-/* Number of library kernel launches issued since the context was created. */
+/* Number of library kernel launches issued by the process so far. */
 int bemgpu_launch_count(const bemgpu_ctx *ctx, int64_t *count);
+/* Device timer on the context's stream: start records a CUDA event; stop records a
+ * second one, waits for it and returns the elapsed device time in milliseconds. */
+int bemgpu_timer_start(bemgpu_ctx *ctx);
+int bemgpu_timer_stop(bemgpu_ctx *ctx, double *ms);
 
 #ifdef __cplusplus
 }
