@@ -102,6 +102,11 @@ SIGNATURES = {
     "bemgpu_profile_read": (ctypes.c_int, [_vp, ctypes.c_char_p, _i64p, _dp]),
     "bemgpu_launch_count": (ctypes.c_int, [_vp, _i64p]),
     "bemgpu_timer_start": (ctypes.c_int, [_vp]),
+    "bemgpu_ctx_set_tensor_lu": (ctypes.c_int, [_vp, _i32]),
+    "bemgpu_debug_cgemm": (ctypes.c_int, [_vp, _i64, _i64, _i32,
+                                          ctypes.POINTER(ctypes.c_float),
+                                          ctypes.POINTER(ctypes.c_float),
+                                          ctypes.POINTER(ctypes.c_float)]),
     "bemgpu_timer_stop": (ctypes.c_int, [_vp, _dp]),
 }
 
@@ -129,6 +134,12 @@ def dptr(a):
     """double* of a contiguous float64 / complex128 numpy array (any memory order)."""
     assert a.flags.c_contiguous or a.flags.f_contiguous
     return ctypes.cast(a.ctypes.data, _dp)
+
+
+def fptr(a):
+    """float* of a contiguous float32 / complex64 numpy array (any memory order)."""
+    assert a.flags.c_contiguous or a.flags.f_contiguous
+    return ctypes.cast(a.ctypes.data, ctypes.POINTER(ctypes.c_float))
 
 
 def i64ptr(a):

@@ -130,6 +130,21 @@ class Context:
                                            ctypes.byref(ms)), self.handle)
         return n.value, ms.value
 
+    def set_tensor_lu(self, enable: bool):
+        """Complex64 LU trailing updates on the tensor cores (default) or CUDA cores."""
+        _check(C.lib().bemgpu_ctx_set_tensor_lu(self.handle, int(enable)), self.handle)
+
+    def debug_cgemm(self, A, B, C_):
+        """C - A B through the split-BF16 tensor-core update (complex64 testing hook)."""
+        A = np.asfortranarray(A, dtype=np.complex64)
+        B = np.asfortranarray(B, dtype=np.complex64)
+        out = np.asfortranarray(np.array(C_, dtype=np.complex64))
+        m, k = A.shape
+        n = B.shape[1]
+        _check(C.lib().bemgpu_debug_cgemm(self.handle, m, n, k, C.fptr(A), C.fptr(B),
+                                          C.fptr(out)), self.handle)
+        return out
+
     def timer_start(self):
         _check(C.lib().bemgpu_timer_start(self.handle), self.handle)
 

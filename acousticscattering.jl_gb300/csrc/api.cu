@@ -21,9 +21,11 @@
 #include "bemgpu_internal.h"
 #include "linalg.cuh"
 #include "refine.cuh"
+#include "gemm_tc.cuh"
 #include "solve_kernels.cuh"
 
 namespace bemgpu {
+constexpr int kTcPanel = 128;  // outer panel width of the tensor-core LU
 static std::atomic<long long> g_launches{0};
 void count_launch(int kernels) { g_launches.fetch_add(kernels, std::memory_order_relaxed); }
 long long launch_total() { return g_launches.load(std::memory_order_relaxed); }
@@ -47,6 +49,7 @@ struct bemgpu_ctx {
   std::multimap<size_t, void*> cache;
   uint64_t cached = 0;
   bool prof = false;
+  bool tensor_lu = true;  // complex64 trailing updates on the tensor cores
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
   std::recursive_mutex mu;
@@ -249,7 +252,7 @@ struct MeshData {
   char hash[65] = {0};
   double center[3] = {0, 0, 0};
   std::vector<double> panels_h;  // FP64 records
-  Buf panels, panelsf, verts, near_i, near_j;
+  Buf panels, panelsf, verts, near_i, near_j, near_lap;
   int64_t n_near = 0;
   double eta = 2.0;
 };
@@ -351,6 +354,11 @@ int make_mesh(bemgpu_ctx* c, const double* nodes, int64_t N, const int64_t* tris
   TRY(upload(c, verts, &m->verts));
   TRY(upload(c, ni, &m->near_i));
   TRY(upload(c, nj, &m->near_j));
+  TRY(alloc(c, (size_t)std::max<int64_t>(1, m->n_near) * 32, &m->near_lap));
+  launch_near_laplace(c->launch(), m->panels.as<double>(), m->verts.as<double>(),
+                      m->near_i.as<int32_t>(), m->near_j.as<int32_t>(), m->n_near,
+                      m->near_lap.as<double>());
+  CUDA_TRY(c, cudaGetLastError());
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   *out = m;
   return BEMGPU_OK;
@@ -369,7 +377,7 @@ struct FactorData {
   Buf A, Mrhs;             // complex128 system, rhs operator
   Buf LU, ipiv, info;      // working factor (complex64 when single)
   Buf LU64, ipiv64, info64;  // complex128 factor after promotion
-  Buf rows, cols, rowsum;
+  Buf rows, cols, rowsum, cols_inv;
   bool single = false;     // current factor precision
   bool mixed = false;      // requested precision
   bool fp32_regular = false;  // regular pairs assembled in FP32
@@ -480,6 +488,7 @@ int assemble_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
     I.verts = m->verts.as<double>();
     I.near_i = m->near_i.as<int32_t>();
     I.near_j = m->near_j.as<int32_t>();
+    I.near_lap = m->near_lap.as<double>();
     I.n = m->n;
     I.n_near = m->n_near;
     I.lda = f->N;
@@ -717,6 +726,109 @@ int estimate_rcond(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
   return BEMGPU_OK;
 }
 
+// Complex64 LU with 128-column outer panels: the panel is factored by the SIMT kernels
+// in 32-column steps, the trailing matrix is updated on the tensor cores (split-BF16
+// tcgen05 GEMM, gemm_tc.cu) from packed operand images of L21 and U12.
+int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatInst>& mi,
+             Buf& d, int64_t nmax) {
+  const Launch L = c->launch();
+  const MatInst* dm = d.as<MatInst>();
+  const int ni = (int)fs.size();
+  const int NB = kTcPanel;
+  // packed operand buffers per instance (sized for the first step, the largest)
+  std::vector<Buf> apack(fs.size()), bpack(fs.size());
+  for (size_t t = 0; t < fs.size(); ++t) {
+    const size_t bytes = tc_pack_bytes(fs[t]->N, NB);
+    TRY(alloc(c, bytes, &apack[t]));
+    TRY(alloc(c, bytes, &bpack[t]));
+  }
+  // descriptors of every outer step, uploaded once
+  const int64_t steps = (nmax + NB - 1) / NB;
+  std::vector<TcPackInst> packs((size_t)steps * 2 * ni);
+  std::vector<TcGemmInst> gems((size_t)steps * ni);
+  std::vector<int64_t> tiles((size_t)steps, 0);
+  for (int64_t st = 0; st < steps; ++st) {
+    const int64_t K0 = st * NB;
+    for (int t = 0; t < ni; ++t) {
+      const int64_t n = mi[t].n;
+      const int64_t m = n - K0 - NB;
+      const int kk = (int)std::max<int64_t>(0, std::min<int64_t>(NB, n - K0));
+      TcPackInst& pa = packs[(size_t)(st * 2 * ni + t)];
+      TcPackInst& pb = packs[(size_t)(st * 2 * ni + ni + t)];
+      std::memset(&pa, 0, sizeof pa);
+      std::memset(&pb, 0, sizeof pb);
+      pa.a = pb.a = mi[t].a;
+      pa.lda = pb.lda = mi[t].lda;
+      pa.r0 = pb.r0 = K0 + NB;
+      pa.k0 = pb.k0 = K0;
+      pa.rows = pb.rows = std::max<int64_t>(0, m);
+      pa.kk = pb.kk = kk;
+      pa.trans = 0;
+      pb.trans = 1;
+      pa.out = apack[t].p;
+      pb.out = bpack[t].p;
+      pa.active = pb.active = m > 0 ? 1 : 0;
+      TcGemmInst& g = gems[(size_t)(st * ni + t)];
+      std::memset(&g, 0, sizeof g);
+      g.apack = apack[t].p;
+      g.bpack = bpack[t].p;
+      g.c = mi[t].a;
+      g.ldc = mi[t].lda;
+      g.c_r0 = g.c_c0 = K0 + NB;
+      g.m = g.n = std::max<int64_t>(0, m);
+      g.kk = kk;
+      g.active = m > 0 ? 1 : 0;
+      if (m > 0) tiles[(size_t)st] += ((m + 127) / 128) * ((m + 127) / 128);
+    }
+  }
+  Buf dpack, dgem;
+  TRY(to_device(c, packs, &dpack));
+  TRY(to_device(c, gems, &dgem));
+  for (int64_t st = 0; st < steps; ++st) {
+    const int64_t K0 = st * NB;
+    for (int64_t k0 = K0; k0 < K0 + NB && k0 < nmax; k0 += kPanelNB) {
+      {
+        Prof pr(c, "getf2");
+        launch_getf2(L, dm, ni, k0, kPanelNB, 1);
+      }
+      {
+        Prof pr(c, "laswp");
+        launch_laswp(L, dm, ni, k0, kPanelNB, K0, K0 + NB, k0, k0 + kPanelNB, 1);
+      }
+      {
+        Prof pr(c, "trsm");
+        launch_trsm_panel(L, dm, ni, k0, kPanelNB, k0 + kPanelNB, K0 + NB, 1);
+      }
+      {
+        Prof pr(c, "gemm_panel");
+        launch_gemm_update(L, dm, ni, k0, kPanelNB, nmax, k0 + kPanelNB, K0 + NB, 1);
+      }
+    }
+    if (K0 + NB >= nmax) break;
+    {
+      Prof pr(c, "laswp");
+      launch_laswp(L, dm, ni, K0, NB, 0, nmax, K0, K0 + NB, 1);
+    }
+    {
+      Prof pr(c, "trsm");
+      launch_trsm_panel(L, dm, ni, K0, NB, K0 + NB, nmax, 1);
+    }
+    int64_t max_rows = 0;
+    for (int t = 0; t < ni; ++t) max_rows = std::max(max_rows, mi[t].n - K0 - NB);
+    {
+      Prof pr(c, "tc_pack");
+      launch_tc_pack(L, dpack.as<TcPackInst>() + st * 2 * ni, 2 * ni, max_rows, NB);
+    }
+    {
+      Prof pr(c, "gemm_tc");
+      launch_tc_cgemm(L, dgem.as<TcGemmInst>() + st * ni, ni, tiles[(size_t)st]);
+    }
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  TRY(check_device_error(c));
+  return BEMGPU_OK;
+}
+
 // LU of a batch of same-precision factors (prec 1: complex64 in LU, 0: complex128).
 int getrf_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, int prec, bool promoted) {
   if (fs.empty()) return BEMGPU_OK;
@@ -738,8 +850,10 @@ int getrf_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, int prec, bool prom
   }
   Buf d;
   TRY(to_device(c, mi, &d));
-  {
-    // right-looking blocked LU; each kernel family is timed on its own
+  if (prec == 1 && c->tensor_lu) {
+    TRY(getrf_tc(c, fs, mi, d, nmax));
+  } else {
+    // right-looking blocked LU, 32-column panels; each kernel family timed on its own
     const MatInst* dm = d.as<MatInst>();
     const int ni = (int)fs.size();
     for (int64_t k0 = 0; k0 < nmax; k0 += kPanelNB) {
@@ -749,15 +863,15 @@ int getrf_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, int prec, bool prom
       }
       {
         Prof pr(c, "laswp");
-        launch_laswp(L, dm, ni, k0, kPanelNB, nmax, prec);
+        launch_laswp(L, dm, ni, k0, kPanelNB, 0, nmax, k0, k0 + kPanelNB, prec);
       }
       {
         Prof pr(c, "trsm");
-        launch_trsm_panel(L, dm, ni, k0, kPanelNB, nmax, prec);
+        launch_trsm_panel(L, dm, ni, k0, kPanelNB, k0 + kPanelNB, nmax, prec);
       }
       {
         Prof pr(c, prec ? "gemm_c64" : "gemm_c128");
-        launch_gemm_update(L, dm, ni, k0, kPanelNB, nmax, prec);
+        launch_gemm_update(L, dm, ni, k0, kPanelNB, nmax, k0 + kPanelNB, nmax, prec);
       }
     }
   }
@@ -792,6 +906,7 @@ int scale_copy_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, std::vector<Bu
     v.rows = f->rows.as<double>();
     v.cols = f->cols.as<double>();
     v.rowsum = f->rowsum.as<double>();
+    v.cols_inv = f->cols_inv.as<double>();
     v.part = part[t].as<double>();
     v.out = to_promoted ? f->LU64.p : f->LU.p;
     v.out_single = (!to_promoted && f->single) ? 1 : 0;
@@ -847,6 +962,7 @@ int factorize_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
     TRY(alloc(c, (size_t)f->N * 8, &f->rows));
     TRY(alloc(c, (size_t)f->N * 8, &f->cols));
     TRY(alloc(c, (size_t)f->N * 8, &f->rowsum));
+    TRY(alloc(c, (size_t)f->N * 8, &f->cols_inv));
     TRY(alloc(c, (size_t)kChunks * f->N * 2 * 8, &part[t]));
     TRY(alloc(c, (size_t)f->N * f->N * (f->single ? 8 : 16), &f->LU));
     TRY(alloc(c, (size_t)f->N * 4, &f->ipiv));
@@ -939,6 +1055,8 @@ int factor_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, bool assemble) {
 
 // ------------------------------------------------------------------ solve chain
 struct RhsState {
+  double final_stats[kStats] = {0};  // residual statistics of the accepted iterate
+  bool have_final = false;
   double previous = INFINITY;
   int corrections = 0, attempts = 0, stalls = 0;
   bool done = false, init = true;
@@ -1231,6 +1349,8 @@ int solve_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<i
         const double metric = std::max(nw, cw);
         if (std::isfinite(metric) && metric <= s.f->prob.refine_tolerance) {
           q.done = true;
+          std::memcpy(q.final_stats, &st[t][(size_t)r * kStats], sizeof q.final_stats);
+          q.have_final = true;
           continue;
         }
         q.stalls = metric >= q.previous * 0.9 ? q.stalls + 1 : 0;
@@ -1332,8 +1452,31 @@ int solve_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<i
     TRY(to_device(c, ti, &d));
     launch_traces(L, d.as<TraceInst>(), (int)F, n_max, rmax);
   }
-  std::vector<std::vector<double>> st;
-  TRY(residual_pass(c, all, &st));
+  // residual diagnostics: refined right-hand sides reuse the statistics of their
+  // accepted iterate; the others get one residual pass
+  std::vector<SolveInst*> need;
+  std::vector<size_t> need_idx;
+  for (size_t t = 0; t < F; ++t) {
+    bool all_final = si[t].f->mixed;
+    for (auto& r : si[t].rs) all_final &= r.have_final;
+    if (!all_final) {
+      need.push_back(&si[t]);
+      need_idx.push_back(t);
+    }
+  }
+  std::vector<std::vector<double>> st(F);
+  if (!need.empty()) {
+    std::vector<std::vector<double>> st2;
+    TRY(residual_pass(c, need, &st2));
+    for (size_t u = 0; u < need.size(); ++u) st[need_idx[u]] = st2[u];
+  }
+  for (size_t t = 0; t < F; ++t)
+    if (st[t].empty()) {
+      st[t].resize((size_t)si[t].R * kStats);
+      for (int r = 0; r < si[t].R; ++r)
+        std::memcpy(&st[t][(size_t)r * kStats], si[t].rs[r].final_stats,
+                    sizeof(double) * kStats);
+    }
   double solve_ms = tsolve.stop();
   TRY(check_device_error(c));
   for (size_t t = 0; t < F; ++t) {
@@ -2000,6 +2143,68 @@ int bemgpu_profile_read(bemgpu_ctx* c, const char* family, int64_t* launches, do
     }
   if (launches) *launches = cnt;
   if (total_ms) *total_ms = ms;
+  return BEMGPU_OK;
+}
+
+int bemgpu_ctx_set_tensor_lu(bemgpu_ctx* c, int32_t enable) {
+  if (!c) return fail(nullptr, BEMGPU_EINVAL, "null context");
+  c->tensor_lu = enable != 0;
+  return BEMGPU_OK;
+}
+
+int bemgpu_debug_cgemm(bemgpu_ctx* c, int64_t m, int64_t n, int32_t k, const float* A,
+                       const float* B, float* C) {
+  if (!c || !A || !B || !C || m <= 0 || n <= 0 || k <= 0)
+    return fail(c, BEMGPU_EINVAL, "invalid arguments");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  Buf dA, dB, dC, pa, pb, dpi, dgi;
+  TRY(alloc(c, (size_t)m * k * 8, &dA));
+  TRY(alloc(c, (size_t)k * n * 8, &dB));
+  TRY(alloc(c, (size_t)m * n * 8, &dC));
+  TRY(alloc(c, tc_pack_bytes(m, k), &pa));
+  TRY(alloc(c, tc_pack_bytes(n, k), &pb));
+  CUDA_TRY(c, cudaMemcpyAsync(dA.p, A, (size_t)m * k * 8, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(dB.p, B, (size_t)k * n * 8, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(dC.p, C, (size_t)m * n * 8, cudaMemcpyHostToDevice, c->stream));
+  std::vector<TcPackInst> pk(2);
+  std::memset(pk.data(), 0, sizeof(TcPackInst) * 2);
+  pk[0].a = dA.p;
+  pk[0].lda = m;
+  pk[0].rows = m;
+  pk[0].kk = k;
+  pk[0].trans = 0;
+  pk[0].out = pa.p;
+  pk[0].active = 1;
+  pk[1].a = dB.p;
+  pk[1].lda = k;
+  pk[1].rows = n;
+  pk[1].kk = k;
+  pk[1].trans = 1;
+  pk[1].out = pb.p;
+  pk[1].active = 1;
+  std::vector<TcGemmInst> g(1);
+  std::memset(g.data(), 0, sizeof(TcGemmInst));
+  g[0].apack = pa.p;
+  g[0].bpack = pb.p;
+  g[0].c = dC.p;
+  g[0].ldc = m;
+  g[0].m = m;
+  g[0].n = n;
+  g[0].kk = k;
+  g[0].active = 1;
+  TRY(to_device(c, pk, &dpi));
+  TRY(to_device(c, g, &dgi));
+  const Launch L = c->launch();
+  launch_tc_pack(L, dpi.as<TcPackInst>(), 2, std::max(m, n), k);
+  {
+    Prof pr(c, "gemm_tc");
+    launch_tc_cgemm(L, dgi.as<TcGemmInst>(), 1, ((m + 127) / 128) * ((n + 127) / 128));
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  CUDA_TRY(c, cudaMemcpyAsync(C, dC.p, (size_t)m * n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  TRY(check_device_error(c));
   return BEMGPU_OK;
 }
 

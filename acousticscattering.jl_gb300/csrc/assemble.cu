@@ -183,8 +183,8 @@ __global__ void __launch_bounds__(128) k_assemble_near(const AsmInst* __restrict
   for (int t = 0; t < 9; ++t) v[t] = I.verts[j * kVertDoubles + t];
   double x[3] = {ri[0], ri[1], ri[2]}, nx[3] = {ri[3], ri[4], ri[5]};
   const bool self = (i == j);
-  double S0, D0, K0, H0;
-  laplace_parts(v, rj + 3, x, nx, self, S0, D0, K0, H0);
+  const double4 lp = reinterpret_cast<const double4*>(I.near_lap)[p];
+  const double S0 = lp.x, D0 = lp.y, K0 = lp.z, H0 = lp.w;
   const int64_t n = I.n, lda = I.lda;
   const double delta = self ? 1.0 : 0.0;
   if (KIND == kAsmBM || KIND == kAsmCBIE) {
@@ -219,6 +219,33 @@ __global__ void __launch_bounds__(128) k_assemble_near(const AsmInst* __restrict
     store_c(I.out1, (n + i) + j * lda, a21);
     store_c(I.out1, (n + i) + (n + j) * lda, a22);
   }
+}
+
+// Laplace parts of the near pairs: computed once per mesh, reused by every wavenumber.
+__global__ void k_near_laplace(const double* __restrict__ panels, const double* __restrict__ verts,
+                               const int32_t* __restrict__ near_i,
+                               const int32_t* __restrict__ near_j, int64_t n_near, double* out) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_near) return;
+  const int64_t i = near_i[p], j = near_j[p];
+  const double* ri = panels + i * kPanelDoubles;
+  const double* rj = panels + j * kPanelDoubles;
+  double v[9];
+#pragma unroll
+  for (int t = 0; t < 9; ++t) v[t] = verts[j * kVertDoubles + t];
+  double x[3] = {ri[0], ri[1], ri[2]}, nx[3] = {ri[3], ri[4], ri[5]};
+  double S0, D0, K0, H0;
+  laplace_parts(v, rj + 3, x, nx, i == j, S0, D0, K0, H0);
+  reinterpret_cast<double4*>(out)[p] = make_double4(S0, D0, K0, H0);
+}
+
+void launch_near_laplace(const Launch& L, const double* panels, const double* verts,
+                         const int32_t* near_i, const int32_t* near_j, int64_t n_near,
+                         double* out) {
+  if (n_near <= 0) return;
+  k_near_laplace<<<(unsigned)((n_near + 127) / 128), 128, 0, L.stream>>>(panels, verts, near_i,
+                                                                         near_j, n_near, out);
+  count_launch(1);
 }
 
 // ------------------------------------------------------------------ launch wrappers

@@ -65,6 +65,7 @@ struct AsmInst {
   const double* verts;     // vertex records
   const int32_t* near_i;   // near pair rows (collocation panel)
   const int32_t* near_j;   // near pair columns (source panel)
+  const double* near_lap;  // closed-form Laplace parts S0, D0, K0, H0 per near pair
   int64_t n;               // panels
   int64_t n_near;          // near pairs
   int64_t lda;             // leading dimension of the outputs (n or 2n)
@@ -114,6 +115,10 @@ void launch_assemble_regular(const Launch& L, const AsmInst* d_inst, int ninst, 
                              int kind, bool fp32);
 void launch_assemble_near(const Launch& L, const AsmInst* d_inst, int ninst, int64_t max_near,
                           int kind);
+// closed-form Laplace parts of every near pair of a mesh (wavenumber independent)
+void launch_near_laplace(const Launch& L, const double* panels, const double* verts,
+                         const int32_t* near_i, const int32_t* near_j, int64_t n_near,
+                         double* out);
 void launch_incident(const Launch& L, const WaveInst* d_inst, int ninst, int64_t nmax,
                      int32_t max_rhs);
 void launch_far_field(const Launch& L, const WaveInst* d_inst, int ninst, int32_t max_rhs,

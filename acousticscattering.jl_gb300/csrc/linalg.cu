@@ -143,16 +143,18 @@ __global__ void __launch_bounds__(kGetf2Threads) k_getf2(const MatInst* __restri
 }
 
 // ------------------------------------------------------------------ laswp
+// Interchanges of rows k0 .. k0 + nbe - 1 applied to the columns j in
+// [c_lo, min(c_hi, n)) that lie outside [s_lo, s_hi).
 template <typename R>
-__global__ void k_laswp(const MatInst* __restrict__ insts, int64_t k0, int nb) {
+__global__ void k_laswp(const MatInst* __restrict__ insts, int64_t k0, int nb, int64_t c_lo,
+                        int64_t c_hi, int64_t s_lo, int64_t s_hi) {
   const MatInst& M = insts[blockIdx.y];
   const int64_t n = M.n;
   if (!M.active || k0 >= n) return;
   const int nbe = (int)min((int64_t)nb, n - k0);
-  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  // columns outside the panel: [0, k0) then [k0 + nbe, n)
-  if (j >= k0) j += nbe;
-  if (j >= n) return;
+  int64_t j = c_lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= s_lo) j += (s_hi - s_lo);
+  if (j >= n || j >= c_hi) return;
   const int64_t lda = M.lda;
   for (int c = 0; c < nbe; ++c) {
     const int64_t row = k0 + c, p = M.ipiv[row];
@@ -165,40 +167,51 @@ __global__ void k_laswp(const MatInst* __restrict__ insts, int64_t k0, int nb) {
 }
 
 // ------------------------------------------------------------------ trsm (U12)
+// U12 = L11^{-1} A12 for the columns [c_lo, min(c_hi, n)); L11 = unit lower nbe x nbe
+// block at (k0, k0), staged in shared memory; one warp per column.
 constexpr int kTrsmWarps = 8;
 
-template <typename R>
+template <typename R, int NB>
 __global__ void __launch_bounds__(kTrsmWarps * 32) k_trsm_panel(const MatInst* __restrict__ insts,
-                                                               int64_t k0, int nb) {
+                                                               int64_t k0, int64_t c_lo,
+                                                               int64_t c_hi) {
   const MatInst& M = insts[blockIdx.y];
   const int64_t n = M.n;
   if (!M.active || k0 >= n) return;
-  const int nbe = (int)min((int64_t)nb, n - k0);
+  const int nbe = (int)min((int64_t)NB, n - k0);
   const int64_t lda = M.lda;
-  __shared__ cx<R> sL[kPanelNB][kPanelNB + 1];
+  const int64_t j = c_lo + (int64_t)blockIdx.x * kTrsmWarps + (threadIdx.x >> 5);
+  const int64_t c_end = min(c_hi, n);
+  if (c_lo + (int64_t)blockIdx.x * kTrsmWarps >= c_end) return;  // uniform per CTA
+  extern __shared__ __align__(16) unsigned char trsm_smem[];
+  cx<R>* sL = reinterpret_cast<cx<R>*>(trsm_smem);  // [NB][NB + 1]
   for (int t = threadIdx.x; t < nbe * nbe; t += blockDim.x) {
     int r = t % nbe, c = t / nbe;
-    sL[r][c] = ld<R>(M.a, (k0 + r) + (k0 + c) * lda);
+    sL[r * (NB + 1) + c] = ld<R>(M.a, (k0 + r) + (k0 + c) * lda);
   }
   __syncthreads();
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int64_t j = k0 + nbe + (int64_t)blockIdx.x * kTrsmWarps + wid;
-  if (j >= n) return;
-  constexpr int kPer = kPanelNB / 32;
+  if (j >= c_end) return;
+  const int lane = threadIdx.x & 31;
+  constexpr int kPer = NB / 32;
   cx<R> x[kPer];
 #pragma unroll
   for (int t = 0; t < kPer; ++t) {
     int r = lane + 32 * t;
     x[t] = r < nbe ? ld<R>(M.a, (k0 + r) + j * lda) : cx<R>{0, 0};
   }
-  for (int c = 0; c < nbe; ++c) {
-    cx<R> xc;
-    xc.x = __shfl_sync(0xffffffffu, x[c / 32].x, c % 32);
-    xc.y = __shfl_sync(0xffffffffu, x[c / 32].y, c % 32);
 #pragma unroll
-    for (int t = 0; t < kPer; ++t) {
-      int r = lane + 32 * t;
-      if (r > c && r < nbe) x[t] -= sL[r][c] * xc;
+  for (int t = 0; t < kPer; ++t) {
+    for (int cl = 0; cl < 32; ++cl) {
+      const int c = 32 * t + cl;
+      if (c >= nbe) break;
+      cx<R> xc;
+      xc.x = __shfl_sync(0xffffffffu, x[t].x, cl);
+      xc.y = __shfl_sync(0xffffffffu, x[t].y, cl);
+#pragma unroll
+      for (int u = 0; u < kPer; ++u) {
+        int r = lane + 32 * u;
+        if (r > c && r < nbe) x[u] -= sL[r * (NB + 1) + c] * xc;
+      }
     }
   }
 #pragma unroll
@@ -214,21 +227,25 @@ constexpr int kGT = 64;   // tile edge
 constexpr int kGK = 8;    // k chunk
 constexpr int kGThreads = 256;
 
+// Rows [k0 + nbe, n), columns [c_lo, min(c_hi, n)).
 template <typename R>
 __global__ void __launch_bounds__(kGThreads) k_gemm_update(const MatInst* __restrict__ insts,
-                                                          int64_t k0, int nb, int64_t tiles_max) {
+                                                          int64_t k0, int nb, int64_t c_lo,
+                                                          int64_t c_hi) {
   const MatInst& M = insts[blockIdx.y];
   const int64_t n = M.n;
   if (!M.active || k0 >= n) return;
   const int nbe = (int)min((int64_t)nb, n - k0);
-  const int64_t s = k0 + nbe;  // first trailing row/column
+  const int64_t s = k0 + nbe;  // first trailing row
   const int64_t m = n - s;
-  if (m <= 0) return;
-  const int64_t tiles = (m + kGT - 1) / kGT;
+  const int64_t c_end = min(c_hi, n);
+  const int64_t w = c_end - c_lo;
+  if (m <= 0 || w <= 0) return;
+  const int64_t tiles_m = (m + kGT - 1) / kGT, tiles_n = (w + kGT - 1) / kGT;
   const int64_t t = blockIdx.x;
-  if (t >= tiles * tiles) return;
-  const int64_t ti = t % tiles, tj = t / tiles;
-  const int64_t r0 = s + ti * kGT, c0 = s + tj * kGT;
+  if (t >= tiles_m * tiles_n) return;
+  const int64_t ti = t % tiles_m, tj = t / tiles_m;
+  const int64_t r0 = s + ti * kGT, c0 = c_lo + tj * kGT;
   const int64_t lda = M.lda;
   __shared__ cx<R> sA[kGK][kGT + 1];
   __shared__ cx<R> sB[kGK][kGT + 1];
@@ -246,7 +263,7 @@ __global__ void __launch_bounds__(kGThreads) k_gemm_update(const MatInst* __rest
       int kb = e % kGK;
       int cc = e / kGK;
       int64_t gc = c0 + cc, gkb = k0 + kc + kb;
-      sB[kb][cc] = (gc < n && kc + kb < nbe) ? ld<R>(M.a, gkb + gc * lda) : cx<R>{0, 0};
+      sB[kb][cc] = (gc < c_end && kc + kb < nbe) ? ld<R>(M.a, gkb + gc * lda) : cx<R>{0, 0};
     }
     __syncthreads();
 #pragma unroll
@@ -268,7 +285,7 @@ __global__ void __launch_bounds__(kGThreads) k_gemm_update(const MatInst* __rest
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
       int64_t gr = r0 + tx + 16 * a, gc = c0 + ty + 16 * b;
-      if (gr < n && gc < n) {
+      if (gr < n && gc < c_end) {
         int64_t idx = gr + gc * lda;
         st<R>(M.a, idx, ld<R>(M.a, idx) - acc[a][b]);
       }
@@ -379,40 +396,60 @@ void launch_getf2(const Launch& L, const MatInst* d, int ninst, int64_t k0, int 
   count_launch(1);
 }
 
-void launch_laswp(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb, int64_t nmax,
-                  int prec) {
-  // upper bound of the columns outside the panel over all instances
-  const int64_t cols = nmax;
+void launch_laswp(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb, int64_t c_lo,
+                  int64_t c_hi, int64_t s_lo, int64_t s_hi, int prec) {
+  const int64_t cols = (c_hi - c_lo) - (s_hi - s_lo);
+  if (cols <= 0) return;
   dim3 grid((unsigned)((cols + 255) / 256), (unsigned)ninst);
   if (prec_is_single(prec))
-    k_laswp<float><<<grid, 256, 0, L.stream>>>(d, k0, nb);
+    k_laswp<float><<<grid, 256, 0, L.stream>>>(d, k0, nb, c_lo, c_hi, s_lo, s_hi);
   else
-    k_laswp<double><<<grid, 256, 0, L.stream>>>(d, k0, nb);
+    k_laswp<double><<<grid, 256, 0, L.stream>>>(d, k0, nb, c_lo, c_hi, s_lo, s_hi);
+  count_launch(1);
+}
+
+template <typename R, int NB>
+static void trsm_t(const Launch& L, const MatInst* d, int ninst, int64_t k0, int64_t c_lo,
+                   int64_t c_hi) {
+  const size_t smem = (size_t)NB * (NB + 1) * sizeof(cx<R>);
+  static bool attr = false;
+  if (!attr && smem > 48 * 1024) {
+    cudaFuncSetAttribute(k_trsm_panel<R, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    attr = true;
+  }
+  dim3 grid((unsigned)((c_hi - c_lo + kTrsmWarps - 1) / kTrsmWarps), (unsigned)ninst);
+  k_trsm_panel<R, NB><<<grid, kTrsmWarps * 32, smem, L.stream>>>(d, k0, c_lo, c_hi);
   count_launch(1);
 }
 
 void launch_trsm_panel(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb,
-                       int64_t nmax, int prec) {
-  int64_t cols = nmax - k0 - nb;
-  if (cols <= 0) return;
-  dim3 grid((unsigned)((cols + kTrsmWarps - 1) / kTrsmWarps), (unsigned)ninst);
-  if (prec_is_single(prec))
-    k_trsm_panel<float><<<grid, kTrsmWarps * 32, 0, L.stream>>>(d, k0, nb);
-  else
-    k_trsm_panel<double><<<grid, kTrsmWarps * 32, 0, L.stream>>>(d, k0, nb);
-  count_launch(1);
+                       int64_t c_lo, int64_t c_hi, int prec) {
+  if (c_hi <= c_lo) return;
+  if (nb <= 32) {
+    if (prec_is_single(prec))
+      trsm_t<float, 32>(L, d, ninst, k0, c_lo, c_hi);
+    else
+      trsm_t<double, 32>(L, d, ninst, k0, c_lo, c_hi);
+  } else {
+    if (prec_is_single(prec))
+      trsm_t<float, 128>(L, d, ninst, k0, c_lo, c_hi);
+    else
+      trsm_t<double, 128>(L, d, ninst, k0, c_lo, c_hi);
+  }
 }
 
 void launch_gemm_update(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb,
-                        int64_t nmax, int prec) {
-  int64_t m = nmax - k0 - nb;
-  if (m <= 0) return;
-  int64_t tiles = (m + kGT - 1) / kGT;
-  dim3 grid((unsigned)(tiles * tiles), (unsigned)ninst);
+                        int64_t nmax, int64_t c_lo, int64_t c_hi, int prec) {
+  const int64_t m = nmax - k0 - nb;
+  const int64_t w = c_hi - c_lo;
+  if (m <= 0 || w <= 0) return;
+  const int64_t tiles = ((m + kGT - 1) / kGT) * ((w + kGT - 1) / kGT);
+  dim3 grid((unsigned)tiles, (unsigned)ninst);
   if (prec_is_single(prec))
-    k_gemm_update<float><<<grid, kGThreads, 0, L.stream>>>(d, k0, nb, tiles);
+    k_gemm_update<float><<<grid, kGThreads, 0, L.stream>>>(d, k0, nb, c_lo, c_hi);
   else
-    k_gemm_update<double><<<grid, kGThreads, 0, L.stream>>>(d, k0, nb, tiles);
+    k_gemm_update<double><<<grid, kGThreads, 0, L.stream>>>(d, k0, nb, c_lo, c_hi);
   count_launch(1);
 }
 
@@ -477,9 +514,9 @@ void launch_getrs(const Launch& L, const MatInst* d, int ninst, int64_t nmax, in
 void launch_getrf_simt(const Launch& L, const MatInst* d, int ninst, int64_t nmax, int prec) {
   for (int64_t k0 = 0; k0 < nmax; k0 += kPanelNB) {
     launch_getf2(L, d, ninst, k0, kPanelNB, prec);
-    launch_laswp(L, d, ninst, k0, kPanelNB, nmax, prec);
-    launch_trsm_panel(L, d, ninst, k0, kPanelNB, nmax, prec);
-    launch_gemm_update(L, d, ninst, k0, kPanelNB, nmax, prec);
+    launch_laswp(L, d, ninst, k0, kPanelNB, 0, nmax, k0, k0 + kPanelNB, prec);
+    launch_trsm_panel(L, d, ninst, k0, kPanelNB, k0 + kPanelNB, nmax, prec);
+    launch_gemm_update(L, d, ninst, k0, kPanelNB, nmax, k0 + kPanelNB, nmax, prec);
   }
 }
 

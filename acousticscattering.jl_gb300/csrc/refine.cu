@@ -25,6 +25,12 @@ __device__ __forceinline__ void stc(void* base, int64_t idx, cd v) {
   reinterpret_cast<double2*>(base)[idx] = make_double2(v.x, v.y);
 }
 __device__ __forceinline__ double cabs(cd a) { return hypot(a.x, a.y); }
+// Magnitude for scales, norms and componentwise denominators: single precision is
+// ample there (relative 1e-7), and GB300 issues FP64 at a small fraction of FP32.
+__device__ __forceinline__ float fabs_c(cd a) {
+  const float x = (float)a.x, y = (float)a.y;
+  return sqrtf(fmaf(x, x, y * y));
+}
 
 __device__ __forceinline__ void chunk_range(int64_t n, int ch, int nch, int64_t* j0, int64_t* j1) {
   int64_t w = (n + nch - 1) / nch;
@@ -39,12 +45,21 @@ __global__ void k_rowstats(const VecInst* __restrict__ insts) {
   if (i >= V.n) return;
   int64_t j0, j1;
   chunk_range(V.n, blockIdx.y, kChunks, &j0, &j1);
-  double mx = 0.0, sm = 0.0;
+  float mx = 0.f;
+  double sm = 0.0;
+  float sm32 = 0.f;
+  int cnt = 0;
   for (int64_t j = j0; j < j1; ++j) {
-    double a = cabs(ldc(V.A, i + j * V.lda));
-    mx = fmax(mx, a);
-    sm += a;
+    float a = fabs_c(ldc(V.A, i + j * V.lda));
+    mx = fmaxf(mx, a);
+    sm32 += a;
+    if (++cnt == 256) {  // fold into FP64 every 256 terms
+      sm += sm32;
+      sm32 = 0.f;
+      cnt = 0;
+    }
   }
+  sm += sm32;
   V.part[2 * (blockIdx.y * V.n + i)] = mx;
   V.part[2 * (blockIdx.y * V.n + i) + 1] = sm;
 }
@@ -68,15 +83,20 @@ __global__ void k_colmax(const VecInst* __restrict__ insts) {
   const int64_t j = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (j >= V.n) return;
-  double mx = 0.0;
+  float mx = 0.f;
   for (int64_t i = lane; i < V.n; i += 32) {
     cd a = ldc(V.A, i + j * V.lda);
-    double r = V.rows[i];
-    mx = fmax(mx, hypot(a.x / r, a.y / r));
+    mx = fmaxf(mx, fabs_c(a) * (float)(1.0 / V.rows[i]));
   }
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
-  if (lane == 0) V.cols[j] = (mx == 0.0) ? 1.0 : mx;
+  for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
+  if (lane == 0) V.cols[j] = (mx == 0.f) ? 1.0 : (double)mx;
+}
+
+__global__ void k_cols_inv(const VecInst* __restrict__ insts) {
+  const VecInst& V = insts[blockIdx.y];
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < V.n) V.cols_inv[j] = 1.0 / V.cols[j];
 }
 
 // out_ij = A_ij / rows_i / cols_j (complex64 or complex128); partial row sums of |out|
@@ -86,22 +106,23 @@ __global__ void k_scale_copy(const VecInst* __restrict__ insts) {
   if (i >= V.n) return;
   int64_t j0, j1;
   chunk_range(V.n, blockIdx.y, kChunks, &j0, &j1);
-  const double ri = V.rows[i];
+  const double ri = 1.0 / V.rows[i];
   double sm = 0.0;
   bool bad = false;
   for (int64_t j = j0; j < j1; ++j) {
     cd a = ldc(V.A, i + j * V.lda);
-    const double cj = V.cols[j];
-    cd v = {a.x / ri / cj, a.y / ri / cj};
+    const double sc = ri * V.cols_inv[j];
     if (V.out_single) {
-      float2 f = make_float2((float)v.x, (float)v.y);
+      const float fs = (float)sc;
+      float2 f = make_float2((float)a.x * fs, (float)a.y * fs);
       reinterpret_cast<float2*>(V.out)[i + j * V.n] = f;
       bad |= !(isfinite(f.x) && isfinite(f.y));
-      sm += hypot((double)f.x, (double)f.y);
+      sm += sqrtf(fmaf(f.x, f.x, f.y * f.y));
     } else {
+      cd v = {a.x * sc, a.y * sc};
       stc(V.out, i + j * V.n, v);
       bad |= !(isfinite(v.x) && isfinite(v.y));
-      sm += hypot(v.x, v.y);
+      sm += fabs_c(v);
     }
   }
   V.part[blockIdx.y * V.n + i] = sm;
@@ -148,21 +169,22 @@ __global__ void __launch_bounds__(256) k_gemv_part(const VecInst* __restrict__ i
   int64_t j0, j1;
   chunk_range(V.n, ch, kChunks, &j0, &j1);
   cd acc[kGemvR];
-  double aacc[kGemvR];
+  float aacc[kGemvR];
 #pragma unroll
   for (int r = 0; r < kGemvR; ++r) {
     acc[r] = cd{0.0, 0.0};
-    aacc[r] = 0.0;
+    aacc[r] = 0.f;
   }
   for (int64_t j = j0; j < j1; ++j) {
     cd a = ldc(V.A, i + j * V.lda);
-    double aa = with_abs ? cabs(a) : 0.0;
+    const float aa = with_abs ? fabs_c(a) : 0.f;
 #pragma unroll
     for (int r = 0; r < kGemvR; ++r) {
       if (r < nr) {
         cd x = ldc(V.x, j + (int64_t)(r0 + r) * V.ldx);
-        acc[r] += a * x;
-        if (with_abs) aacc[r] += aa * cabs(x);
+        acc[r].x = fma(a.x, x.x, fma(-a.y, x.y, acc[r].x));
+        acc[r].y = fma(a.x, x.y, fma(a.y, x.x, acc[r].y));
+        if (with_abs) aacc[r] = fmaf(aa, fabs_c(x), aacc[r]);
       }
     }
   }
@@ -171,7 +193,7 @@ __global__ void __launch_bounds__(256) k_gemv_part(const VecInst* __restrict__ i
     int64_t o = 3 * (((int64_t)ch * V.nrhs + r0 + r) * V.n + i);
     V.part[o] = acc[r].x;
     V.part[o + 1] = acc[r].y;
-    V.part[o + 2] = aacc[r];
+    V.part[o + 2] = (double)aacc[r];
   }
 }
 
@@ -338,6 +360,8 @@ void launch_equilibrate(const Launch& L, const VecInst* d, int ninst, int64_t nm
 }
 
 void launch_scale_copy(const Launch& L, const VecInst* d, int ninst, int64_t nmax) {
+  k_cols_inv<<<dim3((unsigned)((nmax + 255) / 256), (unsigned)ninst), 256, 0, L.stream>>>(d);
+  count_launch(1);
   dim3 g1((unsigned)((nmax + 255) / 256), kChunks, (unsigned)ninst);
   k_scale_copy<<<g1, 256, 0, L.stream>>>(d); count_launch(1);
   k_norms_finish<<<ninst, 256, 0, L.stream>>>(d); count_launch(1);

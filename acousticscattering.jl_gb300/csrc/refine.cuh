@@ -16,6 +16,7 @@ struct VecInst {
   double* rows;      // row scales (n), or null for unit scales
   double* cols;      // column scales (n), or null
   double* rowsum;    // row sums of |A| (n)
+  double* cols_inv;  // 1 / cols (n), filled by the scaled-copy launch
   double* part;      // scratch: kChunks * nrhs * n * 3 doubles (>= kChunks * n * 2)
   void* out;         // scaled copy / correction work buffer (ld n)
   int32_t out_single;

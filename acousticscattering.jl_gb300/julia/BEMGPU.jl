@@ -1,0 +1,200 @@
+# BEMGPU.jl -- drop-in full-3D BEM for AcousticScattering.jl on one GB300 through ccall.
+#
+# Adds a BEMSolution payload type, `_GPUBEMData`, and methods of the reference's own
+# generic functions (`scattering_amplitude`, `target_strength`, `diagnostics`) for it;
+# `BEMGPU.bem(surface, boundary, k; ...)` replaces `bem(surface::Mesh, boundary, k; ...)`
+# (solvers/bem/surface.jl:10-23 of AcousticScattering.jl) for supplied flat-triangle
+# surfaces.  Every numerical step runs in libbemgpu.so (C ABI: include/bemgpu.h).
+#
+# Julia is not installed where this library is built and tested; this module is the
+# binding a maintainer adds on the Julia side (the Python mirror in ../bemgpu/ is the
+# tested host of the same C ABI).
+module BEMGPU
+
+using LinearAlgebra
+import AcousticScattering: bem, scattering_amplitude, target_strength, diagnostics,
+    BEMSolution, Rigid, PressureRelease, FluidFilled
+
+const libbemgpu = joinpath(@__DIR__, "..", "bemgpu", "libbemgpu.so")
+
+const OK, EINVAL, ETOPOLOGY = 0, 1, 2
+const ENOTCONVERGED = 5
+
+struct Problem
+    boundary::Int32
+    formulation::Int32
+    precision::Int32
+    equilibrate::Int32
+    k::Float64
+    density_contrast::Float64
+    soundspeed_contrast::Float64
+    refine_tolerance::Float64
+    refine_maxiter::Int32
+    assembly::Int32
+    condition_guard::Float64
+    near_eta::Float64
+end
+
+struct Diagnostics
+    unknown_count::Int64
+    quadrature_nodes::Int64
+    near_pairs::Int64
+    formulation::Int32
+    precision::Int32
+    factor_precision::Int32
+    refinement_reason::Int32
+    refinement_iterations::Int32
+    equilibrate::Int32
+    coupling_re::Float64
+    coupling_im::Float64
+    absolute_residual::Float64
+    relative_residual::Float64
+    scaled_absolute_residual::Float64
+    scaled_relative_residual::Float64
+    normwise_backward_error::Float64
+    componentwise_backward_error::Float64
+    single_reciprocal_condition::Float64
+    assemble_ms::Float64
+    factor_ms::Float64
+    solve_ms::Float64
+    total_ms::Float64
+    device_bytes::Int64
+    nrhs::Int32
+    info::Int32
+end
+
+function last_error(ctx)
+    buf = Vector{UInt8}(undef, 512)
+    ccall((:bemgpu_last_error, libbemgpu), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t),
+        ctx, buf, length(buf))
+    return unsafe_string(pointer(buf))
+end
+
+function check(status, ctx = C_NULL)
+    status == OK && return nothing
+    msg = last_error(ctx)
+    status in (EINVAL, ETOPOLOGY) && throw(ArgumentError(msg))
+    status == ENOTCONVERGED && error(msg)
+    error("libbemgpu: " * msg)
+end
+
+mutable struct Context
+    ptr::Ptr{Cvoid}
+    function Context(device::Integer = 0; hbm_budget::Integer = 0)
+        r = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:bemgpu_ctx_create, libbemgpu), Cint, (Cint, UInt64, Ptr{Ptr{Cvoid}}),
+            device, hbm_budget, r))
+        c = new(r[])
+        finalizer(x -> ccall((:bemgpu_ctx_destroy, libbemgpu), Cint, (Ptr{Cvoid},), x.ptr), c)
+        return c
+    end
+end
+
+const DEFAULT = Ref{Union{Nothing, Context}}(nothing)
+context() = (DEFAULT[] === nothing && (DEFAULT[] = Context()); DEFAULT[])
+
+mutable struct GPUMesh
+    ptr::Ptr{Cvoid}
+    nodes::Matrix{Float64}
+    triangles::Matrix{Int64}
+end
+
+"""
+    upload(ctx, nodes::3xN, triangles::3xM) -> GPUMesh
+
+Validates the surface exactly as `mesh(nodes, triangles)` does (geometry/surface.jl:341-405)
+and uploads it.
+"""
+function upload(ctx::Context, nodes::AbstractMatrix{<:Real}, triangles::AbstractMatrix{<:Integer})
+    n = Matrix{Float64}(nodes)
+    t = Matrix{Int64}(triangles)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:bemgpu_mesh_upload, libbemgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Int64, Ptr{Int64}, Int64, Ptr{Ptr{Cvoid}}),
+        ctx.ptr, n, size(n, 2), t, size(t, 2), r), ctx.ptr)
+    m = GPUMesh(r[], n, t)
+    finalizer(x -> ccall((:bemgpu_mesh_destroy, libbemgpu), Cint, (Ptr{Cvoid},), x.ptr), m)
+    return m
+end
+
+struct _GPUBEMData
+    solution::Ptr{Cvoid}
+    nodes::Matrix{Float64}
+    triangles::Matrix{Int64}
+    incidence_angle::Float64
+    incidence_azimuth::Float64
+    diagnostics::Diagnostics
+end
+
+_boundary_code(::Rigid) = Int32(0)
+_boundary_code(::PressureRelease) = Int32(1)
+_boundary_code(::FluidFilled) = Int32(2)
+const FORMULATIONS = Dict(:burton_miller => Int32(0), :cbie => Int32(1), :muller => Int32(2))
+
+"""
+    bem(gpu_mesh, boundary, k; incidence_angle=π/2, incidence_azimuth=0, formulation,
+        precision=:double, equilibrate=true, refinement=(;), assembly=:default)
+
+The reference's `bem(surface::Mesh, boundary, k; ...)` on the GPU.
+"""
+function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
+        incidence_azimuth::Real = 0.0, formulation::Union{Nothing, Symbol} = nothing,
+        precision::Symbol = :double, equilibrate::Bool = true,
+        refinement::NamedTuple = (;), assembly::Symbol = :default, ctx::Context = context())
+    isfinite(k) && k > 0 || throw(ArgumentError("k must be finite and positive"))
+    g, h = boundary isa FluidFilled ?
+           (boundary.density_contrast, boundary.soundspeed_contrast) : (1.0, 1.0)
+    p = Problem(_boundary_code(boundary),
+        formulation === nothing ? Int32(-1) : FORMULATIONS[formulation],
+        precision === :mixed ? Int32(1) : Int32(0), Int32(equilibrate), Float64(k), g, h,
+        get(refinement, :tolerance, 1e-13), Int32(get(refinement, :maxiter, 8)),
+        assembly === :double ? Int32(1) : assembly === :single ? Int32(2) : Int32(0),
+        get(refinement, :condition_guard, 10eps(Float32)), 2.0)
+    inc = Float64[incidence_angle, incidence_azimuth]
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:bemgpu_solve, libbemgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ref{Problem}, Int32, Ptr{Float64}, Ptr{Ptr{Cvoid}}),
+        ctx.ptr, m.ptr, p, 1, inc, r), ctx.ptr)
+    d = Ref{Diagnostics}()
+    ccall((:bemgpu_solution_diagnostics, libbemgpu), Cint, (Ptr{Cvoid}, Ref{Diagnostics}), r[], d)
+    data = _GPUBEMData(r[], m.nodes, m.triangles, incidence_angle, incidence_azimuth, d[])
+    return BEMSolution(AcousticScattering._SurfaceGeometry(m.nodes, m.triangles), boundary,
+        Float64(k), :full, data)
+end
+
+function scattering_amplitude(sol::BEMSolution{_GPUBEMData};
+        direction::Union{Nothing, AbstractVector} = nothing)
+    out = zeros(Float64, 2)
+    if direction === nothing
+        check(ccall((:bemgpu_far_field, libbemgpu), Cint,
+            (Ptr{Cvoid}, Int32, Int64, Ptr{Float64}, Ptr{Float64}),
+            sol.data.solution, 0, 1, C_NULL, out))
+    else
+        d = Float64.(collect(direction))
+        check(ccall((:bemgpu_far_field, libbemgpu), Cint,
+            (Ptr{Cvoid}, Int32, Int64, Ptr{Float64}, Ptr{Float64}),
+            sol.data.solution, 0, 1, d, out))
+    end
+    return complex(out[1], out[2])
+end
+
+target_strength(sol::BEMSolution{_GPUBEMData}; kwargs...) =
+    20 * log10(abs(scattering_amplitude(sol; kwargs...)))
+
+function diagnostics(sol::BEMSolution{_GPUBEMData})
+    d = sol.data.diagnostics
+    reasons = (:none, :conversion, :single_singular, :condition, :nonfinite,
+        :iteration_limit, :stagnation)
+    return (; unknown_count = d.unknown_count, quadrature_nodes = d.quadrature_nodes,
+        relative_residual = d.relative_residual, absolute_residual = d.absolute_residual,
+        scaled_relative_residual = d.scaled_relative_residual,
+        factor_precision = d.factor_precision == 0 ? :single : :double,
+        refinement_reason = reasons[d.refinement_reason + 1],
+        refinement_iterations = d.refinement_iterations,
+        normwise_backward_error = d.normwise_backward_error,
+        componentwise_backward_error = d.componentwise_backward_error,
+        coupling = complex(d.coupling_re, d.coupling_im), method = d.precision == 1 ?
+                                                                    :mixed_refinement : :direct)
+end
+
+end # module

@@ -129,6 +129,19 @@ def lu_update_flops(N, nb):
     return tot
 
 
+def aggregate_replicas(ms, units, world):
+    """Replicas only: every rank solves its own copy of the workload; the step time is
+    the max over ranks and the throughput counts the units of all ranks."""
+    if world > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("gloo")
+        out = [None] * world
+        dist.all_gather_object(out, float(ms))
+        ms = max(out)
+    return ms, world * units / (ms * 1e-3)
+
+
 # ------------------------------------------------------------------ our arm
 def run_ours(args):
     import bemgpu
@@ -176,7 +189,8 @@ def run_ours(args):
     launches = bemgpu.Context.launch_count() - l0
     prof = {fam: ctx.profile_read(fam) for fam in
             ("assemble", "near", "equilibrate", "scale_copy", "getf2", "laswp", "trsm",
-             "gemm_c64", "gemm_tc", "gecon", "incident", "forcing", "getrs", "residual")}
+             "gemm_panel", "gemm_c64", "tc_pack", "gemm_tc", "gecon", "incident", "forcing",
+             "getrs", "residual")}
     ctx.profile(False)
     clk = clocks.stop()
     ms = float(np.mean(times))
@@ -199,19 +213,11 @@ def run_ours(args):
     # ---- roofline of the dominant kernel (trailing complex update of the LU)
     hbm, bf16, which = measured_peaks()
     fam = "gemm_tc" if prof["gemm_tc"][0] else "gemm_c64"
-    nb = 32
+    nb = 128 if fam == "gemm_tc" else 32
     flops_step = args.freqs * lu_update_flops(N, nb)
     gl, gms = prof[fam]
     achieved = flops_step * args.steps / (gms * 1e-3) / 1e12 if gms else 0.0
-    value = args.freqs / (ms * 1e-3)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
-        t = [ms]
-        out = [None] * world
-        dist.all_gather_object(out, t)
-        ms = max(o[0] for o in out)
-        value = world * args.freqs / (ms * 1e-3)
+    ms, value = aggregate_replicas(ms, args.freqs, world)
     if rank != 0:
         return None
     cpu = None if args.no_cpu else cpu_baseline(ks, args)

@@ -282,6 +282,20 @@ int bemgpu_dense_solve(bemgpu_ctx *ctx, int64_t n, const double *A, int32_t nrhs
 int bemgpu_assemble_dense(bemgpu_ctx *ctx, const bemgpu_mesh *mesh,
                           const bemgpu_problem *problem, double *M1, double *M2);
 
+/*
+ * Complex64 trailing updates of the mixed-precision LU on the tensor cores (split-BF16
+ * tcgen05 GEMM, default 1) or on the CUDA cores (0).  No reference counterpart: a
+ * switch for the precision study and for tests.
+ */
+int bemgpu_ctx_set_tensor_lu(bemgpu_ctx *ctx, int32_t enable);
+
+/*
+ * C -= A B for complex64 column-major A (m x k), B (k x n), C (m x n) through the
+ * tensor-core update used by the mixed-precision LU (testing hook).
+ */
+int bemgpu_debug_cgemm(bemgpu_ctx *ctx, int64_t m, int64_t n, int32_t k, const float *A,
+                       const float *B, float *C);
+
 /* ------------------------------------------------------------------ profiling */
 /*
  * Kernel timing with CUDA events recorded on the launching stream around every launch
