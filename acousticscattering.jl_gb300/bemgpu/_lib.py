@@ -102,6 +102,8 @@ SIGNATURES = {
     "bemgpu_profile_read": (ctypes.c_int, [_vp, ctypes.c_char_p, _i64p, _dp]),
     "bemgpu_launch_count": (ctypes.c_int, [_vp, _i64p]),
     "bemgpu_timer_start": (ctypes.c_int, [_vp]),
+    "bemgpu_cgemm_update_noalloc": (ctypes.c_int, [_vp, _i64, _i64, _i32, _vp, _i64, _vp, _i64,
+                                                   _vp, _i64]),
     "bemgpu_ctx_set_tensor_lu": (ctypes.c_int, [_vp, _i32]),
     "bemgpu_debug_cgemm": (ctypes.c_int, [_vp, _i64, _i64, _i32,
                                           ctypes.POINTER(ctypes.c_float),

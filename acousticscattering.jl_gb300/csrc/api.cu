@@ -35,8 +35,11 @@ using namespace bemgpu;
 
 namespace {
 thread_local std::string g_err;
-const double kPi = 3.14159265358979323846;
 }  // namespace
+
+namespace bemgpu {
+void bemgpu_set_process_error(const char* msg) { g_err = msg ? msg : ""; }
+}  // namespace bemgpu
 
 // ===================================================================== context + memory
 struct bemgpu_ctx {

@@ -22,6 +22,9 @@ void panel_centroids(const double* nodes, const int64_t* tris, int64_t M,
 void near_pairs(const std::vector<double>& cent, const std::vector<double>& diam, double eta,
                 std::vector<int64_t>* rowptr, std::vector<int64_t>* cols);
 
+// Process-level error message (what bemgpu_last_error(NULL, ...) returns).
+void bemgpu_set_process_error(const char* msg);
+
 // Kernel launch accounting (every <<<>>> of the library increments the counter).
 void count_launch(int kernels);
 long long launch_total();

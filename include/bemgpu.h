@@ -296,6 +296,25 @@ int bemgpu_ctx_set_tensor_lu(bemgpu_ctx *ctx, int32_t enable);
 int bemgpu_debug_cgemm(bemgpu_ctx *ctx, int64_t m, int64_t n, int32_t k, const float *A,
                        const float *B, float *C);
 
+/*
+ * C -= A B for complex64 column-major device matrices A (m x k, leading dimension lda),
+ * B (k x n, ldb) and C (m x n, ldc), on `stream` (a cudaStream_t; NULL = default
+ * stream), through the same tensor-core update as the mixed-precision LU -- without
+ * allocating any device memory.  No counterpart in the reference: it exists for callers
+ * that cannot allocate device memory where they need this update, such as hosts whose
+ * free HBM is owned by their own pool allocator and real-time codes that may not
+ * allocate after start-up.  The operand images, descriptors and timeout word live in a
+ * file-scope device array of 4 MiB + 2 KiB that every GPU loading the library holds
+ * until the process exits; hence m, n <= 2048 and k <= 128 (larger sizes return
+ * BEMGPU_EINVAL).  The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress) with the device current; make that first call before any
+ * stream capture.  All calls share the array: calls whose GPU work overlaps race.  The
+ * call waits for its stream and returns BEMGPU_ETIMEOUT if a bounded wait gave up.
+ * Errors are reported through bemgpu_last_error(NULL, ...).
+ */
+int bemgpu_cgemm_update_noalloc(void *stream, int64_t m, int64_t n, int32_t k, const void *A,
+                                int64_t lda, const void *B, int64_t ldb, void *C, int64_t ldc);
+
 /* ------------------------------------------------------------------ profiling */
 /*
  * Kernel timing with CUDA events recorded on the launching stream around every launch
