@@ -11,11 +11,12 @@ from .api import (ArgumentError, BEMGPUError, BEMSolution, Context, Factor, Flui
                   FrequencySweep, GasFilled, Mesh, PressureRelease, Rigid, SweepResult,
                   assemble, bem, context, dense_solve, diagnostics, factor_batch,
                   frequency_sweep, solve_batch,
-                  incidence_angle_sweep, mesh, scattering_amplitude, target_strength)
+                  incidence_angle_sweep, mesh, pressure, scattering_amplitude,
+                  target_strength)
 
 __all__ = ["ArgumentError", "BEMGPUError", "BEMSolution", "Context", "Factor", "FluidFilled",
            "FrequencySweep", "GasFilled", "Mesh", "PressureRelease", "Rigid", "SweepResult",
            "assemble", "bem", "context", "dense_solve", "diagnostics", "factor_batch",
            "frequency_sweep", "solve_batch",
-           "incidence_angle_sweep", "mesh", "meshes", "scattering_amplitude",
+           "incidence_angle_sweep", "mesh", "meshes", "pressure", "scattering_amplitude",
            "target_strength", "lib", "LIB_PATH"]

@@ -428,6 +428,16 @@ class BEMSolution:
     def dpdn_scat(self):
         return self.traces(0)[1]
 
+    def pressure(self, points, field: str = "total", rhs: int = 0) -> np.ndarray:
+        if field not in C.FIELDS:
+            raise ArgumentError("field must be :total, :scattered, :incident or :interior")
+        pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
+        out = np.zeros(pts.shape[0], dtype=np.complex128)
+        if pts.shape[0]:
+            _check(C.lib().bemgpu_pressure(self.handle, rhs, pts.shape[0], C.dptr(pts),
+                                           C.FIELDS[field], C.dptr(out)), self.ctx.handle)
+        return out
+
     def diagnostics(self) -> dict:
         d = C.Diagnostics()
         _check(C.lib().bemgpu_solution_diagnostics(self.handle, ctypes.byref(d)))
@@ -534,6 +544,26 @@ def target_strength(x, *, direction=None, rhs: int = 0) -> float:
 
 def diagnostics(sol) -> dict:
     return sol.diagnostics()
+
+
+def pressure(sol: BEMSolution, points, *, field: str = "total", rhs: int = 0):
+    """Pressure at points (fields/pressure.jl:42-53, full-BEM branch :404-471).
+
+    ``points``: one point (3 numbers) -> complex; a sequence of points or a 3 x N / N x 3
+    array -> complex array.  field: "total" (incident + scattered outside, interior field
+    inside a fluid body), "scattered", "incident" or "interior"."""
+    arr = np.asarray(points, dtype=np.float64)
+    if arr.size == 0:
+        return np.zeros(0, dtype=np.complex128)
+    single = arr.ndim == 1
+    if single and arr.size != 3:
+        raise ArgumentError("a point has three coordinates")
+    if arr.ndim == 2 and arr.shape[0] == 3 and arr.shape[1] != 3:
+        arr = arr.T
+    if not np.all(np.isfinite(arr)):
+        raise ArgumentError("point coordinates must be finite")
+    out = sol.pressure(arr.reshape(-1, 3), field=field, rhs=rhs)
+    return complex(out[0]) if single else out
 
 
 @dataclass

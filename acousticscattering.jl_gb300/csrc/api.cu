@@ -22,6 +22,7 @@
 #include "linalg.cuh"
 #include "refine.cuh"
 #include "gemm_tc.cuh"
+#include "pressure.cuh"
 #include "solve_kernels.cuh"
 
 namespace bemgpu {
@@ -378,8 +379,8 @@ struct FactorData {
   int64_t n = 0, N = 0;
   bool rhs_is_m2 = true;   // rigid: b = M2 q_inc; soft: b = M1 p_inc
   Buf A, Mrhs;             // complex128 system, rhs operator
-  Buf LU, ipiv, info;      // working factor (complex64 when single)
-  Buf LU64, ipiv64, info64;  // complex128 factor after promotion
+  Buf LU, ipiv, info, perm;        // working factor (complex64 when single)
+  Buf LU64, ipiv64, info64, perm64;  // complex128 factor after promotion
   Buf rows, cols, rowsum, cols_inv;
   bool single = false;     // current factor precision
   bool mixed = false;      // requested precision
@@ -392,6 +393,7 @@ struct FactorData {
   void* factor_ptr() const { return single ? LU.p : (mixed ? LU64.p : LU.p); }
   int32_t* ipiv_ptr() const { return single ? ipiv.as<int32_t>() : (mixed ? ipiv64.as<int32_t>() : ipiv.as<int32_t>()); }
   int32_t* info_ptr() const { return single ? info.as<int32_t>() : (mixed ? info64.as<int32_t>() : info.as<int32_t>()); }
+  int32_t* perm_ptr() const { return single ? perm.as<int32_t>() : (mixed ? perm64.as<int32_t>() : perm.as<int32_t>()); }
   size_t bytes() const {
     return A.bytes + Mrhs.bytes + LU.bytes + LU64.bytes + ipiv.bytes + ipiv64.bytes + rows.bytes +
            cols.bytes + rowsum.bytes;
@@ -662,15 +664,17 @@ int estimate_rcond(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
   const Launch L = c->launch();
   const size_t F = fs.size();
   std::vector<Lacn2> st(F);
-  std::vector<Buf> work(F);
+  std::vector<Buf> work(F), work2(F);
   std::vector<std::vector<std::complex<double>>> xs(F);
   int64_t nmax = 0;
   for (size_t t = 0; t < F; ++t) {
     st[t].n = (int)fs[t]->N;
     xs[t].assign((size_t)fs[t]->N, 0.0);
     TRY(alloc(c, (size_t)fs[t]->N * 8, &work[t]));
+    TRY(alloc(c, (size_t)fs[t]->N * 8, &work2[t]));
     nmax = std::max(nmax, fs[t]->N);
   }
+  TrsvWork tw{1};
   std::vector<int> kase(F);
   for (size_t t = 0; t < F; ++t) kase[t] = st[t].step(xs[t]);
   Buf d_mi;
@@ -697,6 +701,7 @@ int estimate_rcond(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
         m.ipiv = fs[t]->ipiv.as<int32_t>();
         m.info = fs[t]->info.as<int32_t>();
         m.x = work[t].p;
+        m.y = work2[t].p;
         m.ldx = fs[t]->N;
         m.nrhs = 1;
         m.active = 1;
@@ -708,7 +713,8 @@ int estimate_rcond(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
       TRY(to_device(c, mi, &d_mi));
       {
         Prof pr(c, "getrs");
-        launch_getrs(L, d_mi.as<MatInst>(), (int)mi.size(), nmax, 1, want == 1 ? 1 : 0, 1, 0);
+        launch_getrs(L, d_mi.as<MatInst>(), (int)mi.size(), nmax, 1, want == 1 ? 1 : 0, 1, 0,
+                     &tw);
       }
       for (size_t w : who) {
         tmp.resize(2 * xs[w].size());
@@ -745,11 +751,24 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
     TRY(alloc(c, bytes, &apack[t]));
     TRY(alloc(c, bytes, &bpack[t]));
   }
+  // -(L11^{-1} - I) per instance and its packed image (the U12 solve on tensor cores)
+  std::vector<Buf> negn(fs.size()), npack(fs.size());
+  std::vector<float2*> negn_ptrs(fs.size());
+  for (size_t t = 0; t < fs.size(); ++t) {
+    TRY(alloc(c, (size_t)NB * NB * 8, &negn[t]));
+    TRY(alloc(c, tc_pack_bytes(NB, NB), &npack[t]));
+    negn_ptrs[t] = negn[t].as<float2>();
+  }
+  Buf d_negn;
+  TRY(to_device(c, negn_ptrs, &d_negn));
   // descriptors of every outer step, uploaded once
   const int64_t steps = (nmax + NB - 1) / NB;
   std::vector<TcPackInst> packs((size_t)steps * 2 * ni);
   std::vector<TcGemmInst> gems((size_t)steps * ni);
   std::vector<int64_t> tiles((size_t)steps, 0);
+  std::vector<TcPackInst> packs1((size_t)steps * 2 * ni);  // (-N, A12)
+  std::vector<TcGemmInst> gems1((size_t)steps * ni);       // A12 -= (-N) A12
+  std::vector<int64_t> tiles1((size_t)steps, 0);
   for (int64_t st = 0; st < steps; ++st) {
     const int64_t K0 = st * NB;
     for (int t = 0; t < ni; ++t) {
@@ -782,11 +801,39 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
       g.kk = kk;
       g.active = m > 0 ? 1 : 0;
       if (m > 0) tiles[(size_t)st] += ((m + 127) / 128) * ((m + 127) / 128);
+      // U12 solve: C = A12 (rows K0.., kk rows; columns K0 + NB..), A = -N (kk x kk)
+      TcPackInst& qa = packs1[(size_t)(st * 2 * ni + t)];
+      TcPackInst& qb = packs1[(size_t)(st * 2 * ni + ni + t)];
+      std::memset(&qa, 0, sizeof qa);
+      std::memset(&qb, 0, sizeof qb);
+      qa.a = negn[t].p;
+      qa.lda = NB;
+      qa.rows = kk;
+      qa.kk = kk;
+      qa.trans = 0;
+      qa.out = npack[t].p;
+      qa.active = m > 0 ? 1 : 0;
+      qb = pb;  // A12 packed exactly like U12 of the trailing update
+      TcGemmInst& g1 = gems1[(size_t)(st * ni + t)];
+      std::memset(&g1, 0, sizeof g1);
+      g1.apack = npack[t].p;
+      g1.bpack = bpack[t].p;
+      g1.c = mi[t].a;
+      g1.ldc = mi[t].lda;
+      g1.c_r0 = K0;
+      g1.c_c0 = K0 + NB;
+      g1.m = kk;
+      g1.n = std::max<int64_t>(0, m);
+      g1.kk = kk;
+      g1.active = m > 0 ? 1 : 0;
+      if (m > 0) tiles1[(size_t)st] += (m + 127) / 128;
     }
   }
-  Buf dpack, dgem;
+  Buf dpack, dgem, dpack1, dgem1;
   TRY(to_device(c, packs, &dpack));
   TRY(to_device(c, gems, &dgem));
+  TRY(to_device(c, packs1, &dpack1));
+  TRY(to_device(c, gems1, &dgem1));
   for (int64_t st = 0; st < steps; ++st) {
     const int64_t K0 = st * NB;
     for (int64_t k0 = K0; k0 < K0 + NB && k0 < nmax; k0 += kPanelNB) {
@@ -812,11 +859,15 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
       Prof pr(c, "laswp");
       launch_laswp(L, dm, ni, K0, NB, 0, nmax, K0, K0 + NB, 1);
     }
+    int64_t max_rows = 0;
+    for (int t = 0; t < ni; ++t) max_rows = std::max(max_rows, mi[t].n - K0 - NB);
     {
       Prof pr(c, "trsm");
-      launch_trsm_panel(L, dm, ni, K0, NB, K0 + NB, nmax, 1);
+      launch_linv_neg(L, dm, ni, K0, d_negn.as<float2* const>());
+      launch_tc_pack(L, dpack1.as<TcPackInst>() + st * 2 * ni, 2 * ni, max_rows, NB);
+      launch_tc_cgemm(L, dgem1.as<TcGemmInst>() + st * ni, ni, tiles1[(size_t)st]);
     }
-    int64_t max_rows = 0;
+    max_rows = 0;
     for (int t = 0; t < ni; ++t) max_rows = std::max(max_rows, mi[t].n - K0 - NB);
     {
       Prof pr(c, "tc_pack");
@@ -847,6 +898,9 @@ int getrf_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, int prec, bool prom
     m.lda = f->N;
     m.ipiv = promoted ? f->ipiv64.as<int32_t>() : f->ipiv.as<int32_t>();
     m.info = promoted ? f->info64.as<int32_t>() : f->info.as<int32_t>();
+    Buf& pb = promoted ? f->perm64 : f->perm;
+    TRY(alloc(c, (size_t)f->N * 4, &pb));
+    m.perm = pb.as<int32_t>();
     m.active = 1;
     CUDA_TRY(c, cudaMemsetAsync(m.info, 0, sizeof(int32_t), c->stream));
     nmax = std::max(nmax, f->N);
@@ -878,6 +932,7 @@ int getrf_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, int prec, bool prom
       }
     }
   }
+  launch_make_perm(L, d.as<MatInst>(), (int)fs.size(), nmax);
   CUDA_TRY(c, cudaGetLastError());
   for (size_t t = 0; t < fs.size(); ++t) {
     int32_t h = 0;
@@ -1070,7 +1125,7 @@ struct RhsState {
 struct SolveInst {
   FactorData* f;
   int32_t R;
-  Buf dirs, pinc, qinc, b, x, y, den, work, stats, part, active, changed, tmp;
+  Buf dirs, pinc, qinc, b, x, y, den, work, work2, stats, part, active, changed, tmp;
   std::vector<RhsState> rs;
 };
 
@@ -1140,7 +1195,10 @@ int correction_pass(bemgpu_ctx* c, std::vector<SolveInst*>& ss, bool from_b,
       m.lda = s->f->N;
       m.ipiv = s->f->ipiv_ptr();
       m.info = s->f->info_ptr();
+      if (!s->work2.p) TRY(alloc(c, (size_t)s->f->N * s->R * 16, &s->work2));
       m.x = s->work.p;
+      m.y = s->work2.p;
+      m.perm = s->f->perm_ptr();
       m.ldx = s->f->N;
       m.nrhs = s->R;
       m.active = 1;
@@ -1151,8 +1209,9 @@ int correction_pass(bemgpu_ctx* c, std::vector<SolveInst*>& ss, bool from_b,
     if (mi.empty()) continue;
     Buf dm;
     TRY(to_device(c, mi, &dm));
+    TrsvWork tw{1};
     Prof p(c, "getrs");
-    launch_getrs(L, dm.as<MatInst>(), (int)mi.size(), pn, pr, 0, prec, 1);
+    launch_getrs(L, dm.as<MatInst>(), (int)mi.size(), pn, pr, 0, prec, 1, &tw);
   }
   launch_corr_apply(L, d.as<VecInst>(), (int)vi.size(), nmax, rmax, mode);
   CUDA_TRY(c, cudaGetLastError());
@@ -1907,13 +1966,63 @@ int bemgpu_solution_destroy(bemgpu_solution* sol) {
 
 int bemgpu_pressure(bemgpu_solution* sol, int32_t rhs, int64_t npts, const double* points,
                     int32_t field, double* out) {
-  (void)rhs;
-  (void)npts;
-  (void)points;
-  (void)field;
-  (void)out;
   if (!sol) return fail(nullptr, BEMGPU_EINVAL, "null solution");
-  return fail(sol->d->c, BEMGPU_EINVAL, "pressure evaluation is not available in this build");
+  SolutionData* s = sol->d.get();
+  bemgpu_ctx* c = s->c;
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  if (rhs < 0 || rhs >= s->nrhs) return fail(c, BEMGPU_EINVAL, "rhs index out of range");
+  if (field < BEMGPU_FIELD_TOTAL || field > BEMGPU_FIELD_INTERIOR)
+    return fail(c, BEMGPU_EINVAL, "field must be :total, :scattered, :incident or :interior");
+  if (npts < 0 || (npts > 0 && (!points || !out)))
+    return fail(c, BEMGPU_EINVAL, "invalid points");
+  if (npts == 0) return BEMGPU_OK;
+  for (int64_t i = 0; i < 3 * npts; ++i)
+    if (!std::isfinite(points[i])) return fail(c, BEMGPU_EINVAL, "point coordinates must be finite");
+  const bool fluid = s->boundary == BEMGPU_FLUID;
+  if (field == BEMGPU_FIELD_INTERIOR && !fluid)
+    return fail(c, BEMGPU_EINVAL, "interior field requires a fluid-filled body");
+  std::vector<double> pts(points, points + 3 * npts);
+  std::vector<double> dir(s->dirs.begin() + 3 * rhs, s->dirs.begin() + 3 * rhs + 3);
+  Buf dp, dd, dout, dreg;
+  TRY(upload(c, pts, &dp));
+  TRY(upload(c, dir, &dd));
+  TRY(alloc(c, (size_t)npts * 16, &dout));
+  TRY(alloc(c, (size_t)npts * 4, &dreg));
+  PressureInst P{};
+  P.panels = s->mesh->panels.as<double>();
+  P.verts = s->mesh->verts.as<double>();
+  P.n = s->mesh->n;
+  P.p = s->ps.as<double>() + 2 * (size_t)s->mesh->n * rhs;
+  P.q = s->qs.as<double>() + 2 * (size_t)s->mesh->n * rhs;
+  P.dir = dd.as<double>();
+  P.points = dp.as<double>();
+  P.npts = npts;
+  P.out = dout.as<double>();
+  P.region = dreg.as<int32_t>();
+  P.k = s->k;
+  P.k_int = fluid ? s->k / s->h : s->k;
+  P.g = fluid ? s->g : 1.0;
+  P.eta = s->mesh->eta;
+  P.field = field;
+  P.fluid = fluid ? 1 : 0;
+  {
+    Prof pr(c, "pressure");
+    launch_pressure(c->launch(), P);
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  std::vector<int32_t> reg;
+  CUDA_TRY(c, cudaMemcpyAsync(out, dout.p, (size_t)npts * 16, cudaMemcpyDeviceToHost, c->stream));
+  TRY(download(c, dreg, &reg, (size_t)npts));
+  for (int64_t i = 0; i < npts; ++i)
+    if (std::isnan(out[2 * i]) && field != BEMGPU_FIELD_INCIDENT) {
+      if (field == BEMGPU_FIELD_INTERIOR)
+        return fail(c, BEMGPU_EINVAL, "interior field requested at an exterior point");
+      return fail(c, BEMGPU_EINVAL,
+                  reg[i] == 1 ? "point lies inside the body, where no exterior field exists"
+                              : "field does not exist at this point");
+    }
+  return BEMGPU_OK;
 }
 
 int bemgpu_dense_solve(bemgpu_ctx* c, int64_t n, const double* A, int32_t nrhs, double* B,

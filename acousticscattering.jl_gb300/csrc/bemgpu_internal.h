@@ -105,6 +105,13 @@ struct MatInst {
   int64_t ldx;
   int32_t nrhs;
   int32_t active;
+  int32_t* perm;    // row permutation of the factor: (P b)[i] = b[perm[i]]
+  void* y;          // second vector buffer of the triangular solves (n x nrhs, ld ldx)
+};
+
+// Selects the blocked triangular solves (MatInst.y / MatInst.perm provided).
+struct TrsvWork {
+  int32_t blocked;
 };
 
 // ------------------------------------------------------------------ launch wrappers

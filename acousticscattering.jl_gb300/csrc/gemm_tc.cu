@@ -41,7 +41,8 @@ constexpr int kTcKC = 32;          // complex K per chunk / stage
 constexpr int kTcStages = 3;
 constexpr int kTcBlock = 16384;    // bytes of one packed 128 x (32 hi + 32 lo) bf16 block
 constexpr int kTcStageBytes = 4 * kTcBlock;  // Ar, Ai, Br, Bi
-constexpr int kTcThreads = 192;
+constexpr int kTcThreads = 320;   // producer, MMA, 8 epilogue warps
+constexpr int kTcEpiThreads = 256;
 constexpr uint32_t kTmemCols = 512;
 
 // ------------------------------------------------------------------ descriptors
@@ -123,11 +124,18 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16* hi, __nv_bflo
   *lo = __float2bfloat16_rn(x - __bfloat162float(*hi));
 }
 
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
 // Packs rows [r0, r0 + rows) x K-columns [k0, k0 + kk) of a column-major complex64
 // matrix (element (r, k) at r + k * lda) as "row-operand" blocks: block
 // (tile, chunk, part) holds 128 rows of 32 complex K values.  trans = 1 reads
 // element (r, k) at k + r * lda instead (the B operand, whose rows are columns of U12).
-__global__ void k_tc_pack(const TcPackInst* __restrict__ insts) {
+// One work item = one row and 8 consecutive K values: it writes the four swizzled
+// 16-byte chunks (re hi, re lo, im hi, im lo) with vector stores.
+__global__ void __launch_bounds__(256) k_tc_pack(const TcPackInst* __restrict__ insts) {
   const TcPackInst& P = insts[blockIdx.z];
   const int64_t tiles = (P.rows + kTcM - 1) / kTcM;
   const int chunks = (P.kk + kTcKC - 1) / kTcKC;
@@ -136,31 +144,47 @@ __global__ void k_tc_pack(const TcPackInst* __restrict__ insts) {
   if (!P.active || tile >= tiles || ch >= chunks) return;
   const float2* A = reinterpret_cast<const float2*>(P.a);
   uint8_t* out = reinterpret_cast<uint8_t*>(P.out) + ((size_t)tile * chunks + ch) * 2 * kTcBlock;
-  // 256 threads: thread = (row r, k-quarter)
-  for (int idx = threadIdx.x; idx < kTcM * kTcKC; idx += blockDim.x) {
-    int r, k;
-    if (P.trans) {  // consecutive threads along k (contiguous in memory)
-      k = idx % kTcKC;
-      r = idx / kTcKC;
-    } else {        // consecutive threads along rows (contiguous in memory)
-      r = idx % kTcM;
-      k = idx / kTcM;
+  for (int item = threadIdx.x; item < kTcM * 4; item += blockDim.x) {
+    int r, q;
+    if (P.trans) {  // 4 consecutive threads cover one row's 32 contiguous values
+      q = item & 3;
+      r = item >> 2;
+    } else {        // consecutive threads on consecutive rows (contiguous per column)
+      r = item % kTcM;
+      q = item / kTcM;
     }
     const int64_t gr = (int64_t)tile * kTcM + r;
-    const int gk = ch * kTcKC + k;
-    float2 v = make_float2(0.f, 0.f);
-    if (gr < P.rows && gk < P.kk) {
-      const int64_t off = P.trans ? (P.k0 + gk) + (P.r0 + gr) * P.lda
-                                  : (P.r0 + gr) + (P.k0 + gk) * P.lda;
-      v = A[off];
+    float re[8], im[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int gk = ch * kTcKC + q * 8 + e;
+      float2 v = make_float2(0.f, 0.f);
+      if (gr < P.rows && gk < P.kk) {
+        const int64_t off = P.trans ? (P.k0 + gk) + (P.r0 + gr) * P.lda
+                                    : (P.r0 + gr) + (P.k0 + gk) * P.lda;
+        v = A[off];
+      }
+      re[e] = v.x;
+      im[e] = v.y;
     }
-    __nv_bfloat16 h, l;
-    split_bf16(v.x, &h, &l);
-    *reinterpret_cast<__nv_bfloat16*>(out + swz_offset(r, k)) = h;
-    *reinterpret_cast<__nv_bfloat16*>(out + swz_offset(r, 32 + k)) = l;
-    split_bf16(v.y, &h, &l);
-    *reinterpret_cast<__nv_bfloat16*>(out + kTcBlock + swz_offset(r, k)) = h;
-    *reinterpret_cast<__nv_bfloat16*>(out + kTcBlock + swz_offset(r, 32 + k)) = l;
+    uint32_t rh[4], rl[4], ih[4], il[4];
+#pragma unroll
+    for (int e = 0; e < 8; e += 2) {
+      __nv_bfloat16 h0, l0, h1, l1;
+      split_bf16(re[e], &h0, &l0);
+      split_bf16(re[e + 1], &h1, &l1);
+      rh[e / 2] = pack2(__bfloat162float(h0), __bfloat162float(h1));
+      rl[e / 2] = pack2(__bfloat162float(l0), __bfloat162float(l1));
+      split_bf16(im[e], &h0, &l0);
+      split_bf16(im[e + 1], &h1, &l1);
+      ih[e / 2] = pack2(__bfloat162float(h0), __bfloat162float(h1));
+      il[e / 2] = pack2(__bfloat162float(l0), __bfloat162float(l1));
+    }
+    const uint32_t ohi = swz_offset(r, q * 8), olo = swz_offset(r, 32 + q * 8);
+    *reinterpret_cast<uint4*>(out + ohi) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+    *reinterpret_cast<uint4*>(out + olo) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+    *reinterpret_cast<uint4*>(out + kTcBlock + ohi) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+    *reinterpret_cast<uint4*>(out + kTcBlock + olo) = make_uint4(il[0], il[1], il[2], il[3]);
   }
 }
 
@@ -222,7 +246,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&S.tfull[b], 1);
-      mbar_init(&S.tempty[b], 128);
+      mbar_init(&S.tempty[b], kTcEpiThreads);
     }
     S.abort_flag = 0;
     S.ninst = ninst;
@@ -355,8 +379,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
     }
   } else {
-    // ------------------------------------------------ epilogue (warps 2..5)
-    const int quad = warp & 3;  // TMEM lane quadrant this warp may access
+    // ------------------------------------------------ epilogue (warps 2..9)
+    // Warp w reads TMEM lane quadrant w % 4 (hardware rule); warps 2..5 take tile
+    // columns 0..63 and warps 6..9 columns 64..127.  The C values of a 16-column chunk
+    // are loaded before they are needed (the first chunk before the accumulators are
+    // ready), so each thread keeps 16 independent loads in flight.
+    const int quad = warp & 3;
+    const int half = (warp - 2) >> 2;
     const int row = quad * 32 + lane;
     int buf = 0;
     uint32_t bphase = 0;
@@ -365,31 +394,48 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       int64_t mt, nt;
       tile_coords(S, insts, t, &inst, &mt, &nt);
       const TcGemmInst& G = insts[inst];
-      if (!tc_wait(&S.tfull[buf], bphase, err, abort_flag)) break;
-      tc_fence_after();
       const int64_t gr = mt * kTcM + row;
       const bool row_ok = gr < G.m;
       float2* C = reinterpret_cast<float2*>(G.c);
-      const uint32_t tl = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * 256);
       const int64_t ncols = G.n - nt * kTcN;
+      const int64_t rbase = G.c_r0 + gr;
+      const int64_t cbase = G.c_c0 + nt * kTcN;
+      const int c0 = half * 64;
+      float2 cur[16], nxt[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j)
+        cur[j] = (row_ok && c0 + j < ncols) ? C[rbase + (cbase + c0 + j) * G.ldc]
+                                            : make_float2(0.f, 0.f);
+      if (!tc_wait(&S.tfull[buf], bphase, err, abort_flag)) break;
+      tc_fence_after();
+      const uint32_t tl = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * 256);
 #pragma unroll 1
-      for (int j0 = 0; j0 < kTcN; j0 += 16) {
+      for (int cc = 0; cc < 4; ++cc) {
+        const int j0 = c0 + cc * 16;
         float vr[16], vi[16];
         tmem_ld16(tl + (uint32_t)j0, vr);
         tmem_ld16(tl + 128u + (uint32_t)j0, vi);
         tmem_wait_ld();
+        if (cc < 3) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            nxt[j] = (row_ok && j0 + 16 + j < ncols)
+                         ? C[rbase + (cbase + j0 + 16 + j) * G.ldc]
+                         : make_float2(0.f, 0.f);
+        }
         if (row_ok) {
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             if (j0 + j < ncols) {
-              const int64_t idx = (G.c_r0 + gr) + (G.c_c0 + nt * kTcN + j0 + j) * G.ldc;
-              float2 cv = C[idx];
-              cv.x -= vr[j];
-              cv.y -= vi[j];
-              C[idx] = cv;
+              float2 v = cur[j];
+              v.x -= vr[j];
+              v.y -= vi[j];
+              C[rbase + (cbase + j0 + j) * G.ldc] = v;
             }
           }
         }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) cur[j] = nxt[j];
       }
       tc_fence_before();
       mbar_arrive(&S.tempty[buf]);

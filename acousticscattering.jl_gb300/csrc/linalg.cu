@@ -58,34 +58,56 @@ __device__ __forceinline__ cx<R> cconj(cx<R> a) {
 }
 
 // ------------------------------------------------------------------ getf2 (panel)
-constexpr int kGetf2Threads = 512;
+// One CTA per instance factors the nbe-column panel at k0 column by column.  The panel
+// lives in global memory (L2); every pass issues independent loads in groups (4 rows
+// in the pivot search, 8 columns in the update) before any dependent store, so each
+// thread keeps several requests in flight.
+template <typename R>
+struct Getf2Cfg;
+template <>
+struct Getf2Cfg<float> {
+  static constexpr int kThreads = 1024;
+};
+template <>
+struct Getf2Cfg<double> {
+  static constexpr int kThreads = 512;
+};
 
 template <typename R>
-__global__ void __launch_bounds__(kGetf2Threads) k_getf2(const MatInst* __restrict__ insts,
-                                                         int64_t k0, int nb) {
+__global__ void __launch_bounds__(Getf2Cfg<R>::kThreads) k_getf2(const MatInst* __restrict__ insts,
+                                                                int64_t k0, int nb) {
+  constexpr int T = Getf2Cfg<R>::kThreads;
   const MatInst& M = insts[blockIdx.x];
   const int64_t n = M.n;
   if (!M.active || k0 >= n) return;
   const int nbe = (int)min((int64_t)nb, n - k0);
   const int64_t lda = M.lda;
   void* A = M.a;
-  __shared__ R s_val[kGetf2Threads / 32];
-  __shared__ int64_t s_idx[kGetf2Threads / 32];
+  __shared__ R s_val[T / 32];
+  __shared__ int64_t s_idx[T / 32];
   __shared__ cx<R> s_u[kPanelNB];
   __shared__ int64_t s_piv;
   __shared__ R s_pmax;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   for (int c = 0; c < nbe; ++c) {
     const int64_t col = k0 + c;
+    const void* colp = static_cast<const cx<R>*>(A) + col * lda;
     // pivot search: largest |re|+|im|, first index on ties
     R best = (R)-1;
     int64_t bidx = col;
-    for (int64_t r = col + tid; r < n; r += kGetf2Threads) {
-      R v = cabs1(ld<R>(A, r + col * lda));
-      if (v > best) {
-        best = v;
-        bidx = r;
+    for (int64_t r = col + tid; r < n; r += 4 * T) {
+      R v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t rr = r + (int64_t)u * T;
+        v[u] = rr < n ? cabs1(ld<R>(colp, rr)) : (R)-1;
       }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (v[u] > best) {
+          best = v[u];
+          bidx = r + (int64_t)u * T;
+        }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -104,7 +126,7 @@ __global__ void __launch_bounds__(kGetf2Threads) k_getf2(const MatInst* __restri
     if (tid == 0) {
       R bv = s_val[0];
       int64_t bi = s_idx[0];
-      for (int w = 1; w < kGetf2Threads / 32; ++w)
+      for (int w = 1; w < T / 32; ++w)
         if (s_val[w] > bv || (s_val[w] == bv && s_idx[w] < bi)) {
           bv = s_val[w];
           bi = s_idx[w];
@@ -127,15 +149,20 @@ __global__ void __launch_bounds__(kGetf2Threads) k_getf2(const MatInst* __restri
     if (tid < nbe) s_u[tid] = ld<R>(A, col + (k0 + tid) * lda);
     __syncthreads();
     const cx<R> inv = nonzero ? cinv(s_u[c]) : cx<R>{(R)1, (R)0};
-    for (int64_t r = col + 1 + tid; r < n; r += kGetf2Threads) {
+    for (int64_t r = col + 1 + tid; r < n; r += T) {
       cx<R> l = ld<R>(A, r + col * lda);
       if (nonzero) {
         l = l * inv;
         st<R>(A, r + col * lda, l);
       }
-      for (int cc = c + 1; cc < nbe; ++cc) {
-        const int64_t idx = r + (k0 + cc) * lda;
-        st<R>(A, idx, ld<R>(A, idx) - l * s_u[cc]);
+      for (int cc0 = c + 1; cc0 < nbe; cc0 += 8) {
+        cx<R> a[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          if (cc0 + e < nbe) a[e] = ld<R>(A, r + (k0 + cc0 + e) * lda);
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          if (cc0 + e < nbe) st<R>(A, r + (k0 + cc0 + e) * lda, a[e] - l * s_u[cc0 + e]);
       }
     }
     __syncthreads();
@@ -168,8 +195,10 @@ __global__ void k_laswp(const MatInst* __restrict__ insts, int64_t k0, int nb, i
 
 // ------------------------------------------------------------------ trsm (U12)
 // U12 = L11^{-1} A12 for the columns [c_lo, min(c_hi, n)); L11 = unit lower nbe x nbe
-// block at (k0, k0), staged in shared memory; one warp per column.
+// block at (k0, k0), staged once per CTA in shared memory; each warp solves kTrsmCols
+// columns (column = warp + kTrsmWarps * t), lane r holding rows r, r + 32, ...
 constexpr int kTrsmWarps = 8;
+constexpr int kTrsmCols = 16;
 
 template <typename R, int NB>
 __global__ void __launch_bounds__(kTrsmWarps * 32) k_trsm_panel(const MatInst* __restrict__ insts,
@@ -180,9 +209,9 @@ __global__ void __launch_bounds__(kTrsmWarps * 32) k_trsm_panel(const MatInst* _
   if (!M.active || k0 >= n) return;
   const int nbe = (int)min((int64_t)NB, n - k0);
   const int64_t lda = M.lda;
-  const int64_t j = c_lo + (int64_t)blockIdx.x * kTrsmWarps + (threadIdx.x >> 5);
   const int64_t c_end = min(c_hi, n);
-  if (c_lo + (int64_t)blockIdx.x * kTrsmWarps >= c_end) return;  // uniform per CTA
+  const int64_t cta0 = c_lo + (int64_t)blockIdx.x * kTrsmWarps * kTrsmCols;
+  if (cta0 >= c_end) return;  // uniform per CTA
   extern __shared__ __align__(16) unsigned char trsm_smem[];
   cx<R>* sL = reinterpret_cast<cx<R>*>(trsm_smem);  // [NB][NB + 1]
   for (int t = threadIdx.x; t < nbe * nbe; t += blockDim.x) {
@@ -190,34 +219,37 @@ __global__ void __launch_bounds__(kTrsmWarps * 32) k_trsm_panel(const MatInst* _
     sL[r * (NB + 1) + c] = ld<R>(M.a, (k0 + r) + (k0 + c) * lda);
   }
   __syncthreads();
-  if (j >= c_end) return;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   constexpr int kPer = NB / 32;
-  cx<R> x[kPer];
+  for (int tcol = 0; tcol < kTrsmCols; ++tcol) {
+    const int64_t j = cta0 + wid + (int64_t)kTrsmWarps * tcol;
+    if (j >= c_end) break;
+    cx<R> x[kPer];
 #pragma unroll
-  for (int t = 0; t < kPer; ++t) {
-    int r = lane + 32 * t;
-    x[t] = r < nbe ? ld<R>(M.a, (k0 + r) + j * lda) : cx<R>{0, 0};
-  }
+    for (int t = 0; t < kPer; ++t) {
+      int r = lane + 32 * t;
+      x[t] = r < nbe ? ld<R>(M.a, (k0 + r) + j * lda) : cx<R>{0, 0};
+    }
 #pragma unroll
-  for (int t = 0; t < kPer; ++t) {
-    for (int cl = 0; cl < 32; ++cl) {
-      const int c = 32 * t + cl;
-      if (c >= nbe) break;
-      cx<R> xc;
-      xc.x = __shfl_sync(0xffffffffu, x[t].x, cl);
-      xc.y = __shfl_sync(0xffffffffu, x[t].y, cl);
+    for (int t = 0; t < kPer; ++t) {
+      for (int cl = 0; cl < 32; ++cl) {
+        const int c = 32 * t + cl;
+        if (c >= nbe) break;
+        cx<R> xc;
+        xc.x = __shfl_sync(0xffffffffu, x[t].x, cl);
+        xc.y = __shfl_sync(0xffffffffu, x[t].y, cl);
 #pragma unroll
-      for (int u = 0; u < kPer; ++u) {
-        int r = lane + 32 * u;
-        if (r > c && r < nbe) x[u] -= sL[r * (NB + 1) + c] * xc;
+        for (int u = t; u < kPer; ++u) {
+          int r = lane + 32 * u;
+          if (r > c && r < nbe) x[u] -= sL[r * (NB + 1) + c] * xc;
+        }
       }
     }
-  }
 #pragma unroll
-  for (int t = 0; t < kPer; ++t) {
-    int r = lane + 32 * t;
-    if (r < nbe) st<R>(M.a, (k0 + r) + j * lda, x[t]);
+    for (int t = 0; t < kPer; ++t) {
+      int r = lane + 32 * t;
+      if (r < nbe) st<R>(M.a, (k0 + r) + j * lda, x[t]);
+    }
   }
 }
 
@@ -385,14 +417,344 @@ __global__ void __launch_bounds__(256) k_trsv_update(const MatInst* __restrict__
   st<R>(M.x, off + row, ld<R>(M.x, off + row) - acc);
 }
 
+// Whole triangular solve in one launch: one CTA per (rhs, instance) holds the
+// right-hand side in shared memory, walks the 32-row diagonal blocks (warp 0 solves a
+// block with shuffles) and lets all threads update the unsolved rows after each block.
+// SWAP 1: LAPACK's forward row interchanges before the solve; 2: the reverse
+// interchanges after it (the P^T of A^H x = b); 0: none.
+constexpr int kTrsvThreads = 512;
+
+template <typename R, bool EFF_LOWER, bool TRANS, bool UNIT, int SWAP>
+__global__ void __launch_bounds__(kTrsvThreads) k_trsv_full(const MatInst* __restrict__ insts) {
+  const MatInst& M = insts[blockIdx.y];
+  const int rhs = blockIdx.x;
+  if (!M.active || rhs >= M.nrhs) return;
+  const int64_t n = M.n, lda = M.lda, off = (int64_t)rhs * M.ldx;
+  extern __shared__ __align__(16) unsigned char trsv_smem[];
+  cx<R>* sx = reinterpret_cast<cx<R>*>(trsv_smem);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int64_t i = tid; i < n; i += kTrsvThreads) sx[i] = ld<R>(M.x, off + i);
+  __syncthreads();
+  if (SWAP == 1 && tid == 0) {
+    for (int64_t i = 0; i < n; ++i) {
+      const int64_t p = M.ipiv[i];
+      if (p != i) {
+        cx<R> t = sx[i];
+        sx[i] = sx[p];
+        sx[p] = t;
+      }
+    }
+  }
+  __syncthreads();
+  const int64_t nblk = (n + 31) / 32;
+  for (int64_t bb = 0; bb < nblk; ++bb) {
+    const int64_t b = EFF_LOWER ? bb : nblk - 1 - bb;
+    const int64_t r0 = b * 32;
+    const int nb = (int)min((int64_t)32, n - r0);
+    if (warp == 0) {
+      cx<R> x = lane < nb ? sx[r0 + lane] : cx<R>{0, 0};
+      if (EFF_LOWER) {
+        for (int c = 0; c < nb; ++c) {
+          if (!UNIT && lane == c) x = x * cinv(opel<R, TRANS>(M.a, lda, r0 + c, r0 + c));
+          cx<R> xc;
+          xc.x = __shfl_sync(0xffffffffu, x.x, c);
+          xc.y = __shfl_sync(0xffffffffu, x.y, c);
+          if (lane > c && lane < nb) x -= opel<R, TRANS>(M.a, lda, r0 + lane, r0 + c) * xc;
+        }
+      } else {
+        for (int c = nb - 1; c >= 0; --c) {
+          if (!UNIT && lane == c) x = x * cinv(opel<R, TRANS>(M.a, lda, r0 + c, r0 + c));
+          cx<R> xc;
+          xc.x = __shfl_sync(0xffffffffu, x.x, c);
+          xc.y = __shfl_sync(0xffffffffu, x.y, c);
+          if (lane < c) x -= opel<R, TRANS>(M.a, lda, r0 + lane, r0 + c) * xc;
+        }
+      }
+      if (lane < nb) sx[r0 + lane] = x;
+    }
+    __syncthreads();
+    const int64_t lo = EFF_LOWER ? r0 + nb : 0, hi = EFF_LOWER ? n : r0;
+    for (int64_t r = lo + tid; r < hi; r += kTrsvThreads) {
+      cx<R> acc = {0, 0};
+#pragma unroll
+      for (int h = 0; h < 32; h += 16) {
+        cx<R> lv[16];  // 16 independent loads in flight per thread
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+          lv[c] = (h + c < nb) ? opel<R, TRANS>(M.a, lda, r, r0 + h + c) : cx<R>{0, 0};
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+          if (h + c < nb) acc += lv[c] * sx[r0 + h + c];
+      }
+      sx[r] -= acc;
+    }
+    __syncthreads();
+  }
+  if (SWAP == 2 && tid == 0) {
+    for (int64_t i = n - 1; i >= 0; --i) {
+      const int64_t p = M.ipiv[i];
+      if (p != i) {
+        cx<R> t = sx[i];
+        sx[i] = sx[p];
+        sx[p] = t;
+      }
+    }
+  }
+  __syncthreads();
+  for (int64_t i = tid; i < n; i += kTrsvThreads) st<R>(M.x, off + i, sx[i]);
+}
+
+template <typename R, bool EL, bool TR, bool UN, int SW>
+static void trsv_full_t(const Launch& L, const MatInst* d, int ninst, int64_t nmax,
+                        int32_t max_rhs) {
+  const size_t smem = (size_t)nmax * sizeof(cx<R>);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_trsv_full<R, EL, TR, UN, SW>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr = true;
+  }
+  k_trsv_full<R, EL, TR, UN, SW><<<dim3((unsigned)max_rhs, (unsigned)ninst), kTrsvThreads, smem,
+                                   L.stream>>>(d);
+  count_launch(1);
+}
+
+// largest order whose right-hand side fits the shared memory of one CTA
+static int64_t trsv_full_max(int prec) { return (int64_t)(220 * 1024) / (prec == 1 ? 8 : 16); }
+
+// ------------------------------------------------------------------ -(L11^{-1} - I)
+// For the tensor-core U12 solve: with L11^{-1} = I + N (N strictly lower),
+// U12 = L11^{-1} A12 = A12 - (-N) A12.  One CTA per instance stages the unit lower
+// block L11 (nbe x nbe at (k0, k0)) in shared memory and solves L11 x = e_j for every
+// column j (one warp per column); out (ld kLinvB, complex64) receives -N.
+constexpr int kLinvB = 128;
+
+__global__ void __launch_bounds__(256) k_linv_neg(const MatInst* __restrict__ insts, int64_t k0,
+                                                  float2* const* outs) {
+  const MatInst& M = insts[blockIdx.x];
+  const int64_t n = M.n;
+  if (!M.active || k0 >= n) return;
+  const int nbe = (int)min((int64_t)kLinvB, n - k0);
+  const int64_t lda = M.lda;
+  extern __shared__ __align__(16) unsigned char linv_smem[];
+  cx<float>* sL = reinterpret_cast<cx<float>*>(linv_smem);  // [kLinvB][kLinvB + 1]
+  for (int t = threadIdx.x; t < nbe * nbe; t += blockDim.x) {
+    int r = t % nbe, c = t / nbe;
+    sL[r * (kLinvB + 1) + c] = ld<float>(M.a, (k0 + r) + (k0 + c) * lda);
+  }
+  __syncthreads();
+  float2* out = outs[blockIdx.x];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr int kPer = kLinvB / 32;
+  for (int j = wid; j < kLinvB; j += 8) {
+    cx<float> x[kPer];
+#pragma unroll
+    for (int t = 0; t < kPer; ++t) {
+      const int r = lane + 32 * t;
+      x[t] = cx<float>{(r == j && j < nbe) ? 1.f : 0.f, 0.f};
+    }
+    if (j < nbe) {
+#pragma unroll
+      for (int t = 0; t < kPer; ++t) {
+        for (int cl = 0; cl < 32; ++cl) {
+          const int c = 32 * t + cl;
+          if (c >= nbe) break;
+          if (c < j) continue;
+          cx<float> xc;
+          xc.x = __shfl_sync(0xffffffffu, x[t].x, cl);
+          xc.y = __shfl_sync(0xffffffffu, x[t].y, cl);
+#pragma unroll
+          for (int u = t; u < kPer; ++u) {
+            const int r = lane + 32 * u;
+            if (r > c && r < nbe) x[u] -= sL[r * (kLinvB + 1) + c] * xc;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < kPer; ++t) {
+      const int r = lane + 32 * t;
+      const bool strict = r > j && r < nbe && j < nbe;
+      out[r + (int64_t)j * kLinvB] = strict ? make_float2(-x[t].x, -x[t].y) : make_float2(0.f, 0.f);
+    }
+  }
+}
+
+void launch_linv_neg(const Launch& L, const MatInst* d, int ninst, int64_t k0, float2* const* outs) {
+  const size_t smem = (size_t)kLinvB * (kLinvB + 1) * sizeof(cx<float>);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_linv_neg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  k_linv_neg<<<ninst, 256, smem, L.stream>>>(d, k0, outs);
+  count_launch(1);
+}
+
+// ------------------------------------------------------------------ blocked solves
+// Two-level triangular solve: diagonal blocks of kBigB rows are solved by one CTA per
+// (rhs, instance) holding the block's slice of the vector in shared memory (32-row
+// sub-blocks by one warp, the rest of the block updated by the CTA); the rows outside the
+// block are then updated by a full-GPU product kernel.  About 2 n / kBigB launches per
+// triangle.
+constexpr int kBigB = 1024;
+constexpr int kDiagThreads = 512;
+
+template <typename R, bool EFF_LOWER, bool TRANS, bool UNIT>
+__global__ void __launch_bounds__(kDiagThreads) k_trsv_diag(const MatInst* __restrict__ insts,
+                                                            int64_t r0) {
+  const MatInst& M = insts[blockIdx.y];
+  const int rhs = blockIdx.x;
+  if (!M.active || rhs >= M.nrhs || r0 >= M.n) return;
+  const int64_t n = M.n, lda = M.lda, off = (int64_t)rhs * M.ldx;
+  const int nbs = (int)min((int64_t)kBigB, n - r0);
+  __shared__ cx<R> sx[kBigB];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < nbs; i += kDiagThreads) sx[i] = ld<R>(M.x, off + r0 + i);
+  __syncthreads();
+  const int nsub = (nbs + 31) / 32;
+  for (int bb = 0; bb < nsub; ++bb) {
+    const int b = EFF_LOWER ? bb : nsub - 1 - bb;
+    const int s0 = b * 32;
+    const int nb = min(32, nbs - s0);
+    if (warp == 0) {
+      cx<R> x = lane < nb ? sx[s0 + lane] : cx<R>{0, 0};
+      if (EFF_LOWER) {
+        for (int c = 0; c < nb; ++c) {
+          if (!UNIT && lane == c)
+            x = x * cinv(opel<R, TRANS>(M.a, lda, r0 + s0 + c, r0 + s0 + c));
+          cx<R> xc;
+          xc.x = __shfl_sync(0xffffffffu, x.x, c);
+          xc.y = __shfl_sync(0xffffffffu, x.y, c);
+          if (lane > c && lane < nb)
+            x -= opel<R, TRANS>(M.a, lda, r0 + s0 + lane, r0 + s0 + c) * xc;
+        }
+      } else {
+        for (int c = nb - 1; c >= 0; --c) {
+          if (!UNIT && lane == c)
+            x = x * cinv(opel<R, TRANS>(M.a, lda, r0 + s0 + c, r0 + s0 + c));
+          cx<R> xc;
+          xc.x = __shfl_sync(0xffffffffu, x.x, c);
+          xc.y = __shfl_sync(0xffffffffu, x.y, c);
+          if (lane < c) x -= opel<R, TRANS>(M.a, lda, r0 + s0 + lane, r0 + s0 + c) * xc;
+        }
+      }
+      if (lane < nb) sx[s0 + lane] = x;
+    }
+    __syncthreads();
+    const int lo = EFF_LOWER ? s0 + nb : 0, hi = EFF_LOWER ? nbs : s0;
+    for (int r = lo + tid; r < hi; r += kDiagThreads) {
+      cx<R> acc = {0, 0};
+      cx<R> lv[16];
+#pragma unroll
+      for (int h = 0; h < 32; h += 16) {
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+          lv[c] = (h + c < nb) ? opel<R, TRANS>(M.a, lda, r0 + r, r0 + s0 + h + c) : cx<R>{0, 0};
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+          if (h + c < nb) acc += lv[c] * sx[s0 + h + c];
+      }
+      sx[r] -= acc;
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < nbs; i += kDiagThreads) st<R>(M.x, off + r0 + i, sx[i]);
+}
+
+// Rows outside the solved block [r0, r0 + kBigB): x_r -= sum_c op(A)[r, c] x_c, one
+// thread per row, the block's solution in shared memory.
+template <typename R, bool EFF_LOWER, bool TRANS>
+__global__ void __launch_bounds__(256) k_trsv_big_update(const MatInst* __restrict__ insts,
+                                                         int64_t r0) {
+  const MatInst& M = insts[blockIdx.z];
+  const int rhs = blockIdx.y;
+  const int64_t n = M.n;
+  if (!M.active || rhs >= M.nrhs || r0 >= n) return;
+  const int nbs = (int)min((int64_t)kBigB, n - r0);
+  const int64_t lda = M.lda, off = (int64_t)rhs * M.ldx;
+  __shared__ cx<R> sx[kBigB];
+  for (int i = threadIdx.x; i < nbs; i += blockDim.x) sx[i] = ld<R>(M.x, off + r0 + i);
+  __syncthreads();
+  int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (EFF_LOWER) row += r0 + nbs;
+  if (EFF_LOWER ? row >= n : row >= r0) return;
+  cx<R> acc = {0, 0};
+  for (int c0 = 0; c0 < nbs; c0 += 8) {
+    cx<R> lv[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      lv[c] = (c0 + c < nbs) ? opel<R, TRANS>(M.a, lda, row, r0 + c0 + c) : cx<R>{0, 0};
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (c0 + c < nbs) acc += lv[c] * sx[c0 + c];
+  }
+  st<R>(M.x, off + row, ld<R>(M.x, off + row) - acc);
+}
+
+// x[i] = y[perm[i]] (forward interchanges as one gather; y holds a copy of x)
+template <typename R>
+__global__ void k_gather_perm(const MatInst* __restrict__ insts) {
+  const MatInst& M = insts[blockIdx.z];
+  const int rhs = blockIdx.y;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!M.active || rhs >= M.nrhs || i >= M.n) return;
+  const int64_t off = (int64_t)rhs * M.ldx;
+  st<R>(M.x, off + i, ld<R>(M.y, off + M.perm[i]));
+}
+
+// (P^T w): x[perm[i]] = y[i] for every stream, then the caller's x holds the result.
+template <typename R>
+__global__ void k_scatter_perm(const MatInst* __restrict__ insts, int max_rhs) {
+  const MatInst& M = insts[blockIdx.z];
+  const int rhs = blockIdx.y;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!M.active || rhs >= M.nrhs || i >= M.n) return;
+  const int64_t off = (int64_t)rhs * M.ldx;
+  st<R>(M.x, off + M.perm[i], ld<R>(M.y, off + i));
+}
+
+// x -> y copy (both ld ldx)
+template <typename R>
+__global__ void k_copy_xy(const MatInst* __restrict__ insts, int to_y) {
+  const MatInst& M = insts[blockIdx.z];
+  const int rhs = blockIdx.y;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!M.active || rhs >= M.nrhs || i >= M.n) return;
+  const int64_t off = (int64_t)rhs * M.ldx;
+  if (to_y)
+    st<R>(M.y, off + i, ld<R>(M.x, off + i));
+  else
+    st<R>(M.x, off + i, ld<R>(M.y, off + i));
+}
+
+// perm from LAPACK pivots: apply the interchanges in order to the identity.
+__global__ void __launch_bounds__(256) k_make_perm(const MatInst* __restrict__ insts) {
+  const MatInst& M = insts[blockIdx.x];
+  if (!M.active || !M.perm) return;
+  extern __shared__ int32_t sperm[];
+  const int64_t n = M.n;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) sperm[i] = (int32_t)i;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int64_t i = 0; i < n; ++i) {
+      const int32_t p = M.ipiv[i];
+      const int32_t t = sperm[i];
+      sperm[i] = sperm[p];
+      sperm[p] = t;
+    }
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) M.perm[i] = sperm[i];
+}
+
 // ------------------------------------------------------------------ launch wrappers
 static int prec_is_single(int prec) { return prec == 1; }
 
 void launch_getf2(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb, int prec) {
   if (prec_is_single(prec))
-    k_getf2<float><<<ninst, kGetf2Threads, 0, L.stream>>>(d, k0, nb);
+    k_getf2<float><<<ninst, Getf2Cfg<float>::kThreads, 0, L.stream>>>(d, k0, nb);
   else
-    k_getf2<double><<<ninst, kGetf2Threads, 0, L.stream>>>(d, k0, nb);
+    k_getf2<double><<<ninst, Getf2Cfg<double>::kThreads, 0, L.stream>>>(d, k0, nb);
   count_launch(1);
 }
 
@@ -418,7 +780,8 @@ static void trsm_t(const Launch& L, const MatInst* d, int ninst, int64_t k0, int
                          (int)smem);
     attr = true;
   }
-  dim3 grid((unsigned)((c_hi - c_lo + kTrsmWarps - 1) / kTrsmWarps), (unsigned)ninst);
+  const int64_t per = (int64_t)kTrsmWarps * kTrsmCols;
+  dim3 grid((unsigned)((c_hi - c_lo + per - 1) / per), (unsigned)ninst);
   k_trsm_panel<R, NB><<<grid, kTrsmWarps * 32, smem, L.stream>>>(d, k0, c_lo, c_hi);
   count_launch(1);
 }
@@ -481,12 +844,106 @@ static void trsv_t(const Launch& L, const MatInst* d, int ninst, int64_t nmax, i
   }
 }
 
+template <typename R, bool EL, bool TR, bool UN>
+static void trsv_big_t(const Launch& L, const MatInst* d, int ninst, int64_t nmax,
+                       int32_t max_rhs) {
+  const int64_t nblk = (nmax + kBigB - 1) / kBigB;
+  for (int64_t b = 0; b < nblk; ++b) {
+    const int64_t blk = EL ? b : nblk - 1 - b;
+    const int64_t r0 = blk * kBigB;
+    k_trsv_diag<R, EL, TR, UN><<<dim3((unsigned)max_rhs, (unsigned)ninst), kDiagThreads, 0,
+                                 L.stream>>>(d, r0);
+    count_launch(1);
+    const int64_t rows = EL ? (nmax - r0 - kBigB) : r0;
+    if (rows > 0) {
+      k_trsv_big_update<R, EL, TR><<<dim3((unsigned)((rows + 255) / 256), (unsigned)max_rhs,
+                                          (unsigned)ninst),
+                                     256, 0, L.stream>>>(d, r0);
+      count_launch(1);
+    }
+  }
+}
+
+template <typename R>
+static void getrs_big_t(const Launch& L, const MatInst* d, int ninst, int64_t nmax,
+                        int32_t max_rhs, int trans, int swaps) {
+  dim3 g((unsigned)((nmax + 255) / 256), (unsigned)max_rhs, (unsigned)ninst);
+  if (!trans) {
+    if (swaps) {
+      k_copy_xy<R><<<g, 256, 0, L.stream>>>(d, 1);
+      k_gather_perm<R><<<g, 256, 0, L.stream>>>(d);
+      count_launch(2);
+    }
+    trsv_big_t<R, true, false, true>(L, d, ninst, nmax, max_rhs);
+    trsv_big_t<R, false, false, false>(L, d, ninst, nmax, max_rhs);
+  } else {
+    trsv_big_t<R, true, true, false>(L, d, ninst, nmax, max_rhs);
+    trsv_big_t<R, false, true, true>(L, d, ninst, nmax, max_rhs);
+    if (swaps) {
+      k_copy_xy<R><<<g, 256, 0, L.stream>>>(d, 1);
+      k_scatter_perm<R><<<g, 256, 0, L.stream>>>(d, max_rhs);
+      count_launch(2);
+    }
+  }
+}
+
+void launch_make_perm(const Launch& L, const MatInst* d, int ninst, int64_t nmax) {
+  const size_t smem = (size_t)nmax * sizeof(int32_t);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_make_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr = true;
+  }
+  k_make_perm<<<ninst, 256, smem, L.stream>>>(d);
+  count_launch(1);
+}
+
 // Solve op(LU) x = b in place on MatInst.x.  trans = 0: A x = b; trans = 1: A^H x = b.
 // swaps = 0 leaves out the row interchanges (the (LU)^{-1} and (LU)^{-H} products that
 // LAPACK's condition estimator applies).
 void launch_getrs(const Launch& L, const MatInst* d, int ninst, int64_t nmax, int32_t max_rhs,
-                  int trans, int prec, int swaps) {
+                  int trans, int prec, int swaps, const TrsvWork* work) {
   if (nmax <= 0 || ninst <= 0 || max_rhs <= 0) return;
+  if (work) {  // blocked two-level solve; needs MatInst.y and MatInst.perm
+    if (prec_is_single(prec))
+      getrs_big_t<float>(L, d, ninst, nmax, max_rhs, trans, swaps);
+    else
+      getrs_big_t<double>(L, d, ninst, nmax, max_rhs, trans, swaps);
+    return;
+  }
+  if (nmax <= trsv_full_max(prec)) {
+    const bool sp = prec_is_single(prec);
+    if (!trans) {
+      if (sp) {
+        if (swaps)
+          trsv_full_t<float, true, false, true, 1>(L, d, ninst, nmax, max_rhs);
+        else
+          trsv_full_t<float, true, false, true, 0>(L, d, ninst, nmax, max_rhs);
+        trsv_full_t<float, false, false, false, 0>(L, d, ninst, nmax, max_rhs);
+      } else {
+        if (swaps)
+          trsv_full_t<double, true, false, true, 1>(L, d, ninst, nmax, max_rhs);
+        else
+          trsv_full_t<double, true, false, true, 0>(L, d, ninst, nmax, max_rhs);
+        trsv_full_t<double, false, false, false, 0>(L, d, ninst, nmax, max_rhs);
+      }
+    } else {
+      if (sp) {
+        trsv_full_t<float, true, true, false, 0>(L, d, ninst, nmax, max_rhs);
+        if (swaps)
+          trsv_full_t<float, false, true, true, 2>(L, d, ninst, nmax, max_rhs);
+        else
+          trsv_full_t<float, false, true, true, 0>(L, d, ninst, nmax, max_rhs);
+      } else {
+        trsv_full_t<double, true, true, false, 0>(L, d, ninst, nmax, max_rhs);
+        if (swaps)
+          trsv_full_t<double, false, true, true, 2>(L, d, ninst, nmax, max_rhs);
+        else
+          trsv_full_t<double, false, true, true, 0>(L, d, ninst, nmax, max_rhs);
+      }
+    }
+    return;
+  }
   if (!trans) {
     if (swaps) launch_rhs_swap(L, d, ninst, max_rhs, 0, prec);
     if (prec_is_single(prec)) {

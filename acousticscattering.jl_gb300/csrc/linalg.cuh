@@ -21,8 +21,17 @@ void launch_gemm_update(const Launch& L, const MatInst* d, int ninst, int64_t k0
                         int64_t nmax, int64_t c_lo, int64_t c_hi, int prec);
 void launch_rhs_swap(const Launch& L, const MatInst* d, int ninst, int32_t max_rhs, int reverse,
                      int prec);
+// Solve with the LU factor in place on MatInst.x (trans 1: A^H x = b; swaps 0 leaves
+// out the row interchanges).  With work != null the flag-synchronised block solve is
+// two-level blocked solve is used (needs MatInst.y and, for swaps, MatInst.perm).
 void launch_getrs(const Launch& L, const MatInst* d, int ninst, int64_t nmax, int32_t max_rhs,
-                  int trans, int prec, int swaps);
+                  int trans, int prec, int swaps, const TrsvWork* work = nullptr);
+// out[i] (kLinvB x kLinvB complex64, column-major) = -(L11^{-1} - I) of the unit lower
+// block at (k0, k0) of instance i (complex64 factors).
+void launch_linv_neg(const Launch& L, const MatInst* d, int ninst, int64_t k0, float2* const* outs);
+// Row permutation of each factor from its pivots (one CTA per instance).
+void launch_make_perm(const Launch& L, const MatInst* d, int ninst, int64_t nmax);
+
 void launch_getrf_simt(const Launch& L, const MatInst* d, int ninst, int64_t nmax, int prec);
 
 }  // namespace bemgpu

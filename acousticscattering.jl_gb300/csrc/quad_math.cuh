@@ -92,26 +92,52 @@ struct Ops {
   cd S, D, K, H;
 };
 
+// Power-series coefficients of the remainder functions in z (i^m folded in):
+// E(z) = sum_m c_m (iz)^m, Re E = sum_j re[j] z^{2j}, Im E = z sum_j im[j] z^{2j}, with
+// c_m = 1/m! (E0), (1-m)/m! (E1), (m-1)/m! (E2), (m-1)(m-3)/m! (E3), m = 0..17.
+struct SeriesTab {
+  double re[4][9];
+  double im[4][9];
+};
+__host__ __device__ constexpr double series_c(int e, int m) {
+  double f = 1.0;
+  for (int t = 2; t <= m; ++t) f *= (double)t;
+  const double num = e == 0 ? (m >= 1 ? 1.0 : 0.0)
+                   : e == 1 ? (m >= 3 ? (double)(1 - m) : 0.0)
+                   : e == 2 ? (m >= 2 ? (double)(m - 1) : 0.0)
+                            : (m >= 2 ? (double)((m - 1) * (m - 3)) : 0.0);
+  return num / f;
+}
+__host__ __device__ constexpr SeriesTab make_series() {
+  SeriesTab t{};
+  for (int e = 0; e < 4; ++e)
+    for (int j = 0; j < 9; ++j) {
+      const int me = 2 * j, mo = 2 * j + 1;
+      t.re[e][j] = ((j & 1) ? -1.0 : 1.0) * series_c(e, me);   // i^{2j} = (-1)^j
+      t.im[e][j] = ((j & 1) ? -1.0 : 1.0) * series_c(e, mo);   // i^{2j+1} = i (-1)^j
+    }
+  return t;
+}
+static __constant__ SeriesTab dSeries = make_series();
+
+__device__ __forceinline__ cd series_eval(int e, double z, double z2) {
+  double re = dSeries.re[e][8], im = dSeries.im[e][8];
+#pragma unroll
+  for (int j = 7; j >= 0; --j) {
+    re = fma(re, z2, dSeries.re[e][j]);
+    im = fma(im, z2, dSeries.im[e][j]);
+  }
+  return cd{re, im * z};
+}
+
 __device__ __forceinline__ void remainder_funcs(double z, cd& E0, cd& E1, cd& E2, cd& E3) {
   if (z < kSeriesZ) {
-    cd t = {1.0, 0.0};
-    cd s0 = {0, 0}, s1 = {0, 0}, s2 = {0, 0}, s3 = {0, 0};
-    // 16 terms: the first omitted term is below z^17/17! < 2e-20 for z < 0.5
-#pragma unroll
-    for (int m = 1; m <= 16; ++m) {
-      double f = z / (double)m;
-      t = cd{-t.y * f, t.x * f};  // t *= i z / m
-      s0 += t;
-      if (m >= 2) {
-        s2 += (double)(m - 1) * t;
-        s3 += (double)((m - 1) * (m - 3)) * t;
-      }
-      if (m >= 3) s1 += (double)(1 - m) * t;
-    }
-    E0 = s0;
-    E1 = s1;
-    E2 = s2;
-    E3 = s3;
+    // 18 terms: the first omitted term is below z^18/18! < 1e-21 for z < 0.5
+    const double z2 = z * z;
+    E0 = series_eval(0, z, z2);
+    E1 = series_eval(1, z, z2);
+    E2 = series_eval(2, z, z2);
+    E3 = series_eval(3, z, z2);
   } else {
     double sn, cs;
     sincos(z, &sn, &cs);

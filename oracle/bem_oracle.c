@@ -433,3 +433,61 @@ void oracle_far_field(const or_panel *P, int64_t n, double k, const double *xhat
 }
 
 int oracle_panel_size(void) { return (int)sizeof(or_panel); }
+
+/*
+ * Layer potentials of the surface traces at a point (fields/pressure.jl:448-471 of the
+ * reference): exterior sum_j D_j p_j - S_j q_j, interior sum_j S_j q_j - D_j p_j, where
+ * S_j, D_j are the unit-density single/double layers of panel j (7-point rule, or closed
+ * form + remainder within eta diameters).  out[2] complex.
+ */
+void oracle_layer_potentials(const or_panel *P, int64_t n, double k, const double *x,
+                             double eta, const double *p, const double *q, int interior,
+                             double *out) {
+  double complex acc = 0.0;
+  const double zero[3] = {0.0, 0.0, 0.0};
+  for (int64_t j = 0; j < n; ++j) {
+    const or_panel *T = &P[j];
+    double complex pj = p[2 * j] + I * p[2 * j + 1], qj = q[2 * j] + I * q[2 * j + 1];
+    double dx = x[0] - T->c[0], dy = x[1] - T->c[1], dz = x[2] - T->c[2];
+    double d2 = dx * dx + dy * dy + dz * dz;
+    double lim = eta * T->diam;
+    double complex S = 0, D = 0, K = 0, H = 0;
+    if (d2 < lim * lim) {
+      double S0, D0, K0, H0;
+      laplace_parts(T, x, zero, 0, &S0, &D0, &K0, &H0);
+      for (int g = 0; g < 7; ++g) {
+        double u[3];
+        sub3(T->g[g], x, u);
+        rem_kernels(k, u, zero, T->n, RW[g] * T->area, &S, &D, &K, &H);
+      }
+      S += S0;
+      D += D0;
+    } else {
+      for (int g = 0; g < 7; ++g) {
+        double u[3];
+        sub3(T->g[g], x, u);
+        full_kernels(k, u, zero, T->n, RW[g] * T->area, &S, &D, &K, &H);
+      }
+    }
+    acc += interior ? (S * qj - D * pj) : (D * pj - S * qj);
+  }
+  out[0] = creal(acc);
+  out[1] = cimag(acc);
+}
+
+/* Sum of the panels' signed solid angles seen from x: 4 pi inside, 0 outside. */
+double oracle_solid_angle(const or_panel *P, int64_t n, const double *x) {
+  double om = 0.0;
+  for (int64_t j = 0; j < n; ++j) {
+    double R0[3], R1[3], R2[3], t[3];
+    sub3(P[j].v[0], x, R0);
+    sub3(P[j].v[1], x, R1);
+    sub3(P[j].v[2], x, R2);
+    double r0 = sqrt(dot3(R0, R0)), r1 = sqrt(dot3(R1, R1)), r2 = sqrt(dot3(R2, R2));
+    cross3(R1, R2, t);
+    double num = dot3(R0, t);
+    double den = r0 * r1 * r2 + dot3(R0, R1) * r2 + dot3(R0, R2) * r1 + dot3(R1, R2) * r0;
+    om += 2.0 * atan2(num, den);
+  }
+  return om;
+}

@@ -61,6 +61,10 @@ def lib():
         L.oracle_far_field.argtypes = [vp, i64, ctypes.c_double, dp, dp, dp, dp]
         L.oracle_pair_ops.argtypes = [vp, i64, i64, ctypes.c_int, ctypes.c_double, dp]
         L.oracle_laplace_parts.argtypes = [vp, dp, dp, ctypes.c_int, dp]
+        L.oracle_layer_potentials.argtypes = [vp, i64, ctypes.c_double, dp, ctypes.c_double,
+                                              dp, dp, ctypes.c_int, dp]
+        L.oracle_solid_angle.argtypes = [vp, i64, dp]
+        L.oracle_solid_angle.restype = ctypes.c_double
         _LIB = L
     return _LIB
 
@@ -166,6 +170,42 @@ def far_field(P: Panels, k, xhat, p, q):
     lib().oracle_far_field(P.ptr, P.n, float(k), _dp(xh), _dp(p),
                            _dp(q), _dp(out))
     return complex(out[0], out[1])
+
+
+def pressure(P: Panels, k, points, p_scat, q_scat, direction, field="scattered", g=1.0,
+             h=1.0, fluid=False, eta=NEAR_ETA):
+    """Field at points from the scattered traces (fields/pressure.jl:404-471): exterior
+    scattered D p - S q (plus the incident wave for "total"), interior S q_i - D p_i with
+    p_i = p + p_inc, q_i = g (q + q_inc) at k / h."""
+    L = lib()
+    out = []
+    p_inc, q_inc = incident(P, k, direction)
+    for x in np.atleast_2d(np.asarray(points, dtype=np.float64)):
+        x = np.ascontiguousarray(x)
+        om = L.oracle_solid_angle(P.ptr, P.n, _dp(x))
+        inside = om > 2 * math.pi
+        if field == "incident":
+            out.append(np.exp(1j * k * direction @ x))
+            continue
+        if inside:
+            if not fluid or field == "scattered":
+                raise ValueError("no exterior field inside the body")
+            pi_, qi_ = np.ascontiguousarray(p_scat + p_inc), np.ascontiguousarray(g * (q_scat + q_inc))
+            r = np.zeros(2)
+            L.oracle_layer_potentials(P.ptr, P.n, k / h, _dp(x), eta, _dp(pi_), _dp(qi_), 1,
+                                      _dp(r))
+            out.append(complex(r[0], r[1]))
+        else:
+            if field == "interior":
+                raise ValueError("interior field at an exterior point")
+            ps, qs = np.ascontiguousarray(p_scat), np.ascontiguousarray(q_scat)
+            r = np.zeros(2)
+            L.oracle_layer_potentials(P.ptr, P.n, k, _dp(x), eta, _dp(ps), _dp(qs), 0, _dp(r))
+            v = complex(r[0], r[1])
+            if field == "total":
+                v += np.exp(1j * k * direction @ x)
+            out.append(v)
+    return np.array(out)
 
 
 def target_strength(f):
