@@ -8,14 +8,16 @@ generators of the benchmark workloads.
 from . import meshes
 from ._lib import lib, LIB_PATH
 from .api import (ArgumentError, BEMGPUError, BEMSolution, Context, Factor, FluidFilled,
-                  FrequencySweep, GasFilled, Mesh, PressureRelease, Rigid, SweepResult,
+                  FrequencySweep, GasFilled, Mesh, PressureRelease, Rigid, Server,
+                  SweepResult,
                   assemble, bem, context, dense_solve, diagnostics, factor_batch,
                   frequency_sweep, solve_batch,
                   incidence_angle_sweep, mesh, pressure, scattering_amplitude,
                   target_strength)
 
 __all__ = ["ArgumentError", "BEMGPUError", "BEMSolution", "Context", "Factor", "FluidFilled",
-           "FrequencySweep", "GasFilled", "Mesh", "PressureRelease", "Rigid", "SweepResult",
+           "FrequencySweep", "GasFilled", "Mesh", "PressureRelease", "Rigid", "Server",
+           "SweepResult",
            "assemble", "bem", "context", "dense_solve", "diagnostics", "factor_batch",
            "frequency_sweep", "solve_batch",
            "incidence_angle_sweep", "mesh", "meshes", "pressure", "scattering_amplitude",

@@ -31,6 +31,19 @@ class Problem(ctypes.Structure):
                 ("near_eta", ctypes.c_double)]
 
 
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("max_batch", ctypes.c_int32), ("queue_limit", ctypes.c_int32),
+                ("cache_bytes", ctypes.c_uint64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64),
+                ("failed", ctypes.c_int64), ("items", ctypes.c_int64),
+                ("factorizations", ctypes.c_int64), ("cache_hits", ctypes.c_int64),
+                ("batches", ctypes.c_int64), ("evictions", ctypes.c_int64),
+                ("busy_ms", ctypes.c_double), ("cached_bytes", ctypes.c_uint64)]
+
+
 class Diagnostics(ctypes.Structure):
     _fields_ = [("unknown_count", ctypes.c_int64), ("quadrature_nodes", ctypes.c_int64),
                 ("near_pairs", ctypes.c_int64), ("formulation", ctypes.c_int32),
@@ -102,6 +115,14 @@ SIGNATURES = {
     "bemgpu_profile_read": (ctypes.c_int, [_vp, ctypes.c_char_p, _i64p, _dp]),
     "bemgpu_launch_count": (ctypes.c_int, [_vp, _i64p]),
     "bemgpu_timer_start": (ctypes.c_int, [_vp]),
+    "bemgpu_server_options_init": (None, [ctypes.POINTER(ServerOptions)]),
+    "bemgpu_server_create": (ctypes.c_int, [_vp, ctypes.POINTER(ServerOptions),
+                                            ctypes.POINTER(_vp)]),
+    "bemgpu_server_submit": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(Problem), _i32, _dp, _i32,
+                                            _dp, _i64p]),
+    "bemgpu_server_wait": (ctypes.c_int, [_vp, _i64, _i32, _dp, _dp]),
+    "bemgpu_server_stats_get": (ctypes.c_int, [_vp, ctypes.POINTER(ServerStats)]),
+    "bemgpu_server_destroy": (ctypes.c_int, [_vp]),
     "bemgpu_cgemm_update_noalloc": (ctypes.c_int, [_vp, _i64, _i64, _i32, _vp, _i64, _vp, _i64,
                                                    _vp, _i64]),
     "bemgpu_ctx_set_tensor_lu": (ctypes.c_int, [_vp, _i32]),

@@ -566,6 +566,68 @@ def pressure(sol: BEMSolution, points, *, field: str = "total", rhs: int = 0):
     return complex(out[0]) if single else out
 
 
+class Server:
+    """Continuous-batching request loop of libbemgpu (one worker thread per server).
+
+    submit() queues one surface / boundary problem at several wavenumbers and incidence
+    directions and returns a ticket; wait() returns the backscatter amplitudes
+    (nfreq x nangles) and the request's latency.  Requests submitted while a batch runs
+    join the next batch; factors are cached across requests (LRU)."""
+
+    def __init__(self, ctx: Context | None = None, max_batch: int = 64, queue_limit: int = 4096,
+                 cache_bytes: int = 0):
+        self.ctx = ctx or context()
+        o = C.ServerOptions()
+        C.lib().bemgpu_server_options_init(ctypes.byref(o))
+        o.max_batch, o.queue_limit, o.cache_bytes = max_batch, queue_limit, cache_bytes
+        h = ctypes.c_void_p()
+        _check(C.lib().bemgpu_server_create(self.ctx.handle, ctypes.byref(o), ctypes.byref(h)),
+               self.ctx.handle)
+        self.handle = h
+        self._shapes = {}
+
+    def submit(self, surface: Mesh, boundary, ks, angles, azimuths=0.0, **options) -> int:
+        ks = np.atleast_1d(np.asarray(ks, dtype=np.float64))
+        a = np.atleast_1d(np.asarray(angles, dtype=np.float64))
+        z = np.broadcast_to(np.asarray(azimuths, dtype=np.float64), a.shape)
+        inc = np.ascontiguousarray(np.stack([a, z], axis=1).reshape(-1))
+        p = _problem(boundary, float(ks[0]), **options)
+        t = ctypes.c_int64()
+        _check(C.lib().bemgpu_server_submit(self.handle, surface.handle(self.ctx), ctypes.byref(p),
+                                            len(ks), C.dptr(np.ascontiguousarray(ks)), len(a),
+                                            C.dptr(inc), ctypes.byref(t)), self.ctx.handle)
+        self._shapes[t.value] = (len(ks), len(a))
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        nf, na = self._shapes.pop(ticket)
+        out = np.zeros((nf, na), dtype=np.complex128)
+        lat = ctypes.c_double()
+        st = C.lib().bemgpu_server_wait(self.handle, ticket, timeout_ms, C.dptr(out),
+                                        ctypes.byref(lat))
+        if st == C.ETIMEOUT:
+            self._shapes[ticket] = (nf, na)
+            raise TimeoutError("request not finished")
+        _check(st, self.ctx.handle)
+        return out, lat.value
+
+    def stats(self) -> dict:
+        s = C.ServerStats()
+        _check(C.lib().bemgpu_server_stats_get(self.handle, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in C.ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            C.lib().bemgpu_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 @dataclass
 class SweepResult:
     angles: np.ndarray

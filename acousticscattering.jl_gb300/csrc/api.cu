@@ -8,6 +8,11 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
+#include <tuple>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -381,7 +386,7 @@ struct FactorData {
   Buf A, Mrhs;             // complex128 system, rhs operator
   Buf LU, ipiv, info, perm;        // working factor (complex64 when single)
   Buf LU64, ipiv64, info64, perm64;  // complex128 factor after promotion
-  Buf rows, cols, rowsum, cols_inv;
+  Buf rows, cols, rowsum, cols_inv, rows_inv;
   bool single = false;     // current factor precision
   bool mixed = false;      // requested precision
   bool fp32_regular = false;  // regular pairs assembled in FP32
@@ -1021,6 +1026,7 @@ int factorize_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
     TRY(alloc(c, (size_t)f->N * 8, &f->cols));
     TRY(alloc(c, (size_t)f->N * 8, &f->rowsum));
     TRY(alloc(c, (size_t)f->N * 8, &f->cols_inv));
+    TRY(alloc(c, (size_t)f->N * 4, &f->rows_inv));
     TRY(alloc(c, (size_t)kChunks * f->N * 2 * 8, &part[t]));
     TRY(alloc(c, (size_t)f->N * f->N * (f->single ? 8 : 16), &f->LU));
     TRY(alloc(c, (size_t)f->N * 4, &f->ipiv));
@@ -1033,6 +1039,7 @@ int factorize_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
     v.rows = f->rows.as<double>();
     v.cols = f->cols.as<double>();
     v.rowsum = f->rowsum.as<double>();
+    v.rows_inv = f->rows_inv.as<float>();
     v.part = part[t].as<double>();
     nmax = std::max(nmax, f->N);
   }
@@ -1592,6 +1599,291 @@ int solve_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<i
 
 }  // namespace
 
+// ===================================================================== serving
+namespace {
+using Clock = std::chrono::steady_clock;
+
+struct ServerReq {
+  int64_t id = 0;
+  std::shared_ptr<MeshData> mesh;
+  bemgpu_problem prob{};
+  std::vector<double> ks, inc, amps;
+  int32_t nfreq = 0, nangles = 0, next_freq = 0, done_freq = 0;
+  int status = BEMGPU_OK;
+  bool finished = false;
+  Clock::time_point t_submit, t_done;
+};
+
+struct FKey {
+  const MeshData* m;
+  double k, g, h;
+  int32_t b, f, p, a;
+  bool operator<(const FKey& o) const {
+    return std::tie(m, k, g, h, b, f, p, a) < std::tie(o.m, o.k, o.g, o.h, o.b, o.f, o.p, o.a);
+  }
+};
+
+struct CacheEnt {
+  std::shared_ptr<FactorData> f;
+  uint64_t last = 0;
+  size_t bytes = 0;
+};
+
+FKey key_of(const ServerReq& r, double k) {
+  const bool fl = r.prob.boundary == BEMGPU_FLUID;
+  return FKey{r.mesh.get(), k, fl ? r.prob.density_contrast : 1.0,
+              fl ? r.prob.soundspeed_contrast : 1.0, r.prob.boundary, r.prob.formulation,
+              r.prob.precision, r.prob.assembly};
+}
+
+// device bytes of one factor plus the solve temporaries of nangles right-hand sides
+size_t item_bytes(const ServerReq& r) {
+  const size_t n = (size_t)r.mesh->n;
+  const bool fl = r.prob.boundary == BEMGPU_FLUID;
+  const size_t N = fl ? 2 * n : n;
+  const bool mixed = r.prob.precision == BEMGPU_MIXED;
+  size_t b = N * N * 16 + N * N * (mixed ? 8 : 16) + (fl ? 0 : n * n * 16);
+  b += 2 * tc_pack_bytes((int64_t)N, 128) + N * 64;
+  const size_t R = (size_t)r.nangles;
+  b += N * R * (16 * 6 + 8) + (size_t)kChunks * R * N * 3 * 8;
+  return b + b / 20;
+}
+}  // namespace
+
+struct bemgpu_server {
+  bemgpu_ctx* c = nullptr;
+  bemgpu_server_options opt{};
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<std::shared_ptr<ServerReq>> queue;
+  std::map<int64_t, std::shared_ptr<ServerReq>> all;
+  std::map<FKey, CacheEnt> cache;
+  uint64_t tick = 0, cached_bytes = 0;
+  int64_t next_id = 1;
+  bemgpu_server_stats st{};
+  bool stop = false;
+  std::thread worker;
+};
+
+namespace {
+
+void finish_req(bemgpu_server* S, ServerReq& r, int status) {
+  if (r.finished) return;
+  r.status = status;
+  r.finished = true;
+  r.t_done = Clock::now();
+  if (status == BEMGPU_OK)
+    S->st.completed++;
+  else
+    S->st.failed++;
+}
+
+struct Item {
+  std::shared_ptr<ServerReq> req;
+  int32_t fi;
+  FKey key;
+};
+
+// One batch: factor the uncached keys, solve every item, read back backscatter.
+int run_batch(bemgpu_server* S, std::vector<Item>& items,
+              std::map<FKey, std::shared_ptr<FactorData>>& factors, int64_t* nfactored) {
+  bemgpu_ctx* c = S->c;
+  std::vector<std::shared_ptr<FactorData>> fresh;
+  std::vector<FactorData*> fs;
+  for (auto& kv : factors)
+    if (!kv.second) {
+      const ServerReq& r = *std::find_if(items.begin(), items.end(), [&](const Item& it) {
+                              return !(it.key < kv.first) && !(kv.first < it.key);
+                            })->req;
+      auto f = std::make_shared<FactorData>();
+      f->c = c;
+      f->mesh = r.mesh;
+      f->prob = r.prob;
+      f->prob.k = kv.first.k;
+      int kind = 0;
+      TRY(check_problem(c, f->prob, &kind));
+      f->kind = kind;
+      f->mixed = f->prob.precision == BEMGPU_MIXED;
+      f->fp32_regular = f->prob.assembly == BEMGPU_ASSEMBLY_SINGLE ||
+                        (f->prob.assembly == BEMGPU_ASSEMBLY_DEFAULT && f->mixed);
+      kv.second = f;
+      fresh.push_back(f);
+      fs.push_back(f.get());
+    }
+  if (!fs.empty()) TRY(factor_batch(c, fs, true));
+  std::vector<FactorData*> sf;
+  std::vector<int32_t> nr;
+  std::vector<const double*> inc;
+  std::vector<std::shared_ptr<SolutionData>> sols;
+  std::vector<SolutionData*> outs;
+  for (auto& it : items) {
+    sf.push_back(factors[it.key].get());
+    nr.push_back(it.req->nangles);
+    inc.push_back(it.req->inc.data());
+    auto sd = std::make_shared<SolutionData>();
+    sd->c = c;
+    sols.push_back(sd);
+    outs.push_back(sd.get());
+  }
+  TRY(solve_batch(c, sf, nr, inc, outs));
+  // backscatter of every (item, angle) in one far-field launch
+  std::vector<WaveInst> wi(items.size());
+  std::vector<Buf> dirs(items.size()), amps(items.size());
+  int32_t rmax = 0;
+  for (size_t t = 0; t < items.size(); ++t) {
+    SolutionData* sd = outs[t];
+    std::vector<double> d(3 * (size_t)sd->nrhs);
+    for (size_t q = 0; q < d.size(); ++q) d[q] = -sd->dirs[q];
+    TRY(upload(c, d, &dirs[t]));
+    TRY(alloc(c, (size_t)sd->nrhs * 16, &amps[t]));
+    WaveInst& w = wi[t];
+    std::memset(&w, 0, sizeof w);
+    w.panels = sd->mesh->panels.as<double>();
+    w.n = sd->mesh->n;
+    w.k = sd->k;
+    w.nrhs = sd->nrhs;
+    w.ndir = 1;
+    w.dirs = dirs[t].as<double>();
+    w.p = sd->ps.as<double>();
+    w.q = sd->qs.as<double>();
+    w.out = amps[t].as<double>();
+    w.ldp = sd->mesh->n;
+    rmax = std::max(rmax, sd->nrhs);
+  }
+  Buf dw;
+  TRY(upload(c, wi, &dw));
+  {
+    Prof p(c, "far_field");
+    launch_far_field(c->launch(), dw.as<WaveInst>(), (int)wi.size(), rmax, 1);
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  for (size_t t = 0; t < items.size(); ++t) {
+    ServerReq& r = *items[t].req;
+    double* dst = r.amps.data() + 2 * (size_t)items[t].fi * r.nangles;
+    CUDA_TRY(c, cudaMemcpyAsync(dst, amps[t].p, (size_t)r.nangles * 16, cudaMemcpyDeviceToHost,
+                                c->stream));
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  TRY(check_device_error(c));
+  *nfactored = (int64_t)fresh.size();
+  return BEMGPU_OK;
+}
+
+void evict_lru(bemgpu_server* S, const std::map<FKey, std::shared_ptr<FactorData>>& keep,
+               uint64_t target_cached) {
+  while (S->cached_bytes > target_cached && !S->cache.empty()) {
+    auto victim = S->cache.end();
+    for (auto it = S->cache.begin(); it != S->cache.end(); ++it) {
+      if (keep.count(it->first)) continue;
+      if (victim == S->cache.end() || it->second.last < victim->second.last) victim = it;
+    }
+    if (victim == S->cache.end()) break;
+    S->cached_bytes -= victim->second.bytes;
+    S->cache.erase(victim);
+    S->st.evictions++;
+  }
+}
+
+void server_loop(bemgpu_server* S) {
+  cudaSetDevice(S->c->device);
+  for (;;) {
+    std::vector<Item> items;
+    std::map<FKey, std::shared_ptr<FactorData>> factors;  // null = to factor
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_work.wait(lk, [&] { return S->stop || !S->queue.empty(); });
+      if (S->stop) break;
+      uint64_t live = 0, budget = 0;
+      {
+        std::lock_guard<std::recursive_mutex> ck(S->c->mu);
+        live = S->c->live;
+        budget = S->c->budget;
+      }
+      // memory the batch may take: the budget minus what is live outside the cache
+      const uint64_t usable = (uint64_t)(0.92 * (double)budget);
+      const uint64_t base = live > S->cached_bytes ? live - S->cached_bytes : 0;
+      uint64_t need = 0;
+      int nnew = 0;
+      bool full = false;
+      while (!S->queue.empty() && !full) {
+        auto r = S->queue.front();
+        while (r->next_freq < r->nfreq) {
+          const FKey key = key_of(*r, r->ks[r->next_freq]);
+          const bool have = S->cache.count(key) || factors.count(key);
+          const size_t b = item_bytes(*r);
+          if (!have && (nnew >= S->opt.max_batch || base + need + b > usable)) {
+            full = true;
+            break;
+          }
+          if (!have) {
+            factors[key] = nullptr;
+            ++nnew;
+            need += b;
+          } else if (S->cache.count(key)) {
+            factors[key] = S->cache[key].f;
+            S->cache[key].last = ++S->tick;
+            S->st.cache_hits++;
+          }
+          items.push_back(Item{r, r->next_freq, key});
+          r->next_freq++;
+        }
+        if (r->next_freq == r->nfreq) S->queue.pop_front();
+      }
+      if (items.empty()) {
+        // the oldest item alone does not fit: fail its request
+        auto r = S->queue.front();
+        S->queue.pop_front();
+        finish_req(S, *r, BEMGPU_ENOMEM_BUDGET);
+        S->cv_done.notify_all();
+        continue;
+      }
+      // make room: cached factors not used by this batch go first
+      const uint64_t room = usable > base + need ? usable - base - need : 0;
+      evict_lru(S, factors, std::min<uint64_t>(room, S->opt.cache_bytes));
+      S->st.items += (int64_t)items.size();
+      S->st.batches++;
+    }
+    int status;
+    int64_t nfactored = 0;
+    Clock::time_point t0 = Clock::now();
+    {
+      std::lock_guard<std::recursive_mutex> ck(S->c->mu);
+      status = run_batch(S, items, factors, &nfactored);
+    }
+    const double ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->st.busy_ms += ms;
+      S->st.factorizations += nfactored;
+      for (auto& it : items) {
+        ServerReq& r = *it.req;
+        if (status != BEMGPU_OK) {
+          finish_req(S, r, status);
+          continue;
+        }
+        if (++r.done_freq == r.nfreq && !r.finished) finish_req(S, r, BEMGPU_OK);
+      }
+      if (status == BEMGPU_OK) {
+        for (auto& kv : factors) {
+          if (S->cache.count(kv.first)) continue;
+          const size_t b = kv.second->bytes();
+          if (b > S->opt.cache_bytes) continue;
+          S->cache[kv.first] = CacheEnt{kv.second, ++S->tick, b};
+          S->cached_bytes += b;
+        }
+        evict_lru(S, {}, S->opt.cache_bytes);
+      } else {
+        // drop the failed requests' remaining items
+        for (auto it = S->queue.begin(); it != S->queue.end();)
+          it = (*it)->finished ? S->queue.erase(it) : it + 1;
+      }
+      S->st.cached_bytes = S->cached_bytes;
+    }
+    S->cv_done.notify_all();
+  }
+}
+}  // namespace
+
 // ===================================================================== C ABI
 extern "C" {
 
@@ -2022,6 +2314,112 @@ int bemgpu_pressure(bemgpu_solution* sol, int32_t rhs, int64_t npts, const doubl
                   reg[i] == 1 ? "point lies inside the body, where no exterior field exists"
                               : "field does not exist at this point");
     }
+  return BEMGPU_OK;
+}
+
+
+void bemgpu_server_options_init(bemgpu_server_options* o) {
+  if (!o) return;
+  o->max_batch = 64;
+  o->queue_limit = 4096;
+  o->cache_bytes = 0;
+}
+
+int bemgpu_server_create(bemgpu_ctx* c, const bemgpu_server_options* opts, bemgpu_server** out) {
+  if (!c || !out) return fail(c, BEMGPU_EINVAL, "null argument");
+  auto* S = new bemgpu_server();
+  S->c = c;
+  bemgpu_server_options_init(&S->opt);
+  if (opts) S->opt = *opts;
+  if (S->opt.max_batch <= 0) S->opt.max_batch = 64;
+  if (S->opt.queue_limit <= 0) S->opt.queue_limit = 4096;
+  if (!S->opt.cache_bytes) S->opt.cache_bytes = c->budget / 4;
+  S->worker = std::thread(server_loop, S);
+  *out = S;
+  return BEMGPU_OK;
+}
+
+int bemgpu_server_submit(bemgpu_server* S, const bemgpu_mesh* mesh, const bemgpu_problem* problem,
+                         int32_t nfreq, const double* ks, int32_t nangles, const double* incidence,
+                         int64_t* ticket) {
+  if (!S || !mesh || !problem || !ks || !incidence || !ticket || nfreq <= 0 || nangles <= 0)
+    return fail(S ? S->c : nullptr, BEMGPU_EINVAL, "invalid request");
+  int kind = 0;
+  for (int32_t i = 0; i < nfreq; ++i) {
+    bemgpu_problem p = *problem;
+    p.k = ks[i];
+    TRY(check_problem(S->c, p, &kind));
+  }
+  for (int32_t i = 0; i < 2 * nangles; ++i)
+    if (!std::isfinite(incidence[i])) return fail(S->c, BEMGPU_EINVAL, "incidence angles must be finite");
+  auto r = std::make_shared<ServerReq>();
+  r->mesh = mesh->d;
+  r->prob = *problem;
+  r->ks.assign(ks, ks + nfreq);
+  r->inc.assign(incidence, incidence + 2 * nangles);
+  r->nfreq = nfreq;
+  r->nangles = nangles;
+  r->amps.assign(2 * (size_t)nfreq * nangles, 0.0);
+  r->t_submit = Clock::now();
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if ((int32_t)S->queue.size() >= S->opt.queue_limit)
+      return fail(S->c, BEMGPU_EBUSY, "request queue full");
+    r->id = S->next_id++;
+    S->all[r->id] = r;
+    S->queue.push_back(r);
+    S->st.submitted++;
+    *ticket = r->id;
+  }
+  S->cv_work.notify_one();
+  return BEMGPU_OK;
+}
+
+int bemgpu_server_wait(bemgpu_server* S, int64_t ticket, int32_t timeout_ms, double* amplitudes,
+                       double* latency_ms) {
+  if (!S) return fail(nullptr, BEMGPU_EINVAL, "null server");
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto it = S->all.find(ticket);
+  if (it == S->all.end()) return fail(S->c, BEMGPU_EINVAL, "unknown ticket");
+  auto r = it->second;
+  auto pred = [&] { return r->finished; };
+  if (timeout_ms < 0)
+    S->cv_done.wait(lk, pred);
+  else if (!S->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred))
+    return BEMGPU_ETIMEOUT;
+  if (amplitudes) std::copy(r->amps.begin(), r->amps.end(), amplitudes);
+  if (latency_ms)
+    *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+  const int st = r->status;
+  S->all.erase(it);
+  if (st != BEMGPU_OK) return fail(S->c, st, "request failed");
+  return BEMGPU_OK;
+}
+
+int bemgpu_server_stats_get(bemgpu_server* S, bemgpu_server_stats* out) {
+  if (!S || !out) return fail(nullptr, BEMGPU_EINVAL, "null argument");
+  std::lock_guard<std::mutex> lk(S->mu);
+  *out = S->st;
+  out->cached_bytes = S->cached_bytes;
+  return BEMGPU_OK;
+}
+
+int bemgpu_server_destroy(bemgpu_server* S) {
+  if (!S) return BEMGPU_OK;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+    for (auto& r : S->queue) finish_req(S, *r, BEMGPU_EBUSY);
+    S->queue.clear();
+  }
+  S->cv_work.notify_all();
+  if (S->worker.joinable()) S->worker.join();
+  S->cv_done.notify_all();
+  {
+    std::lock_guard<std::recursive_mutex> ck(S->c->mu);
+    S->cache.clear();
+  }
+  delete S;
   return BEMGPU_OK;
 }
 

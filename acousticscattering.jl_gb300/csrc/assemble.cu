@@ -132,16 +132,14 @@ __global__ void __launch_bounds__(kAsmRows) k_assemble_regular(const AsmInst* __
       Acc<R> a;
       a.S = a.D = a.K = a.H = cx<R>{0, 0};
       regular_panel<R, KIND == kAsmBM>(rec, x, nx, ke, a);
-      cd S = {a.S.x, a.S.y}, D = {a.D.x, a.D.y};
-      cd m1 = cd{-D.x, -D.y}, m2 = S;
+      cx<R> m1 = cx<R>{-a.D.x, -a.D.y}, m2 = a.S;
       if (KIND == kAsmBM) {
-        cd K = {a.K.x, a.K.y}, H = {a.H.x, a.H.y};
-        cd al = {I.a_re, I.a_im};
-        m1 -= al * H;
-        m2 += al * K;
+        const cx<R> al = {(R)I.a_re, (R)I.a_im};
+        m1 -= al * a.H;
+        m2 += al * a.K;
       }
-      store_c(I.out1, i + j * lda, m1);
-      store_c(I.out2, i + j * lda, m2);
+      store_c(I.out1, i + j * lda, cd{(double)m1.x, (double)m1.y});
+      store_c(I.out2, i + j * lda, cd{(double)m2.x, (double)m2.y});
     } else {
       Acc<R> e, t;
       e.S = e.D = e.K = e.H = cx<R>{0, 0};
@@ -149,23 +147,24 @@ __global__ void __launch_bounds__(kAsmRows) k_assemble_regular(const AsmInst* __
       constexpr bool kh = (KIND == kAsmMuller);
       regular_panel<R, kh>(rec, x, nx, ke, e);
       regular_panel<R, kh>(rec, x, nx, ki, t);
-      const double g = I.g;
-      cd a11, a12, a21, a22;
+      // block combinations in the quadrature precision (no FP64 work on the FP32 path)
+      const R g = (R)I.g, ginv = (R)(1.0 / I.g);
+      cx<R> a11, a12, a21, a22;
       if (KIND == kAsmMuller) {
-        a11 = cd{(double)t.D.x - (double)e.D.x, (double)t.D.y - (double)e.D.y};
-        a12 = cd{(double)e.S.x - g * (double)t.S.x, (double)e.S.y - g * (double)t.S.y};
-        a21 = cd{(double)t.H.x / g - (double)e.H.x, (double)t.H.y / g - (double)e.H.y};
-        a22 = cd{(double)e.K.x - (double)t.K.x, (double)e.K.y - (double)t.K.y};
+        a11 = t.D - e.D;
+        a12 = e.S - g * t.S;
+        a21 = ginv * t.H - e.H;
+        a22 = e.K - t.K;
       } else {
-        a11 = cd{-(double)e.D.x, -(double)e.D.y};
-        a12 = cd{(double)e.S.x, (double)e.S.y};
-        a21 = cd{(double)t.D.x, (double)t.D.y};
-        a22 = cd{-g * (double)t.S.x, -g * (double)t.S.y};
+        a11 = cx<R>{-e.D.x, -e.D.y};
+        a12 = e.S;
+        a21 = t.D;
+        a22 = cx<R>{-g * t.S.x, -g * t.S.y};
       }
-      store_c(I.out1, i + j * lda, a11);
-      store_c(I.out1, i + (n + j) * lda, a12);
-      store_c(I.out1, (n + i) + j * lda, a21);
-      store_c(I.out1, (n + i) + (n + j) * lda, a22);
+      store_c(I.out1, i + j * lda, cd{(double)a11.x, (double)a11.y});
+      store_c(I.out1, i + (n + j) * lda, cd{(double)a12.x, (double)a12.y});
+      store_c(I.out1, (n + i) + j * lda, cd{(double)a21.x, (double)a21.y});
+      store_c(I.out1, (n + i) + (n + j) * lda, cd{(double)a22.x, (double)a22.y});
     }
   }
 }

@@ -74,6 +74,7 @@ __global__ void k_rowstats_finish(const VecInst* __restrict__ insts) {
     sm += V.part[2 * (c * V.n + i) + 1];
   }
   V.rows[i] = (mx == 0.0) ? 1.0 : mx;
+  V.rows_inv[i] = (float)(1.0 / V.rows[i]);
   V.rowsum[i] = sm;
 }
 
@@ -86,7 +87,7 @@ __global__ void k_colmax(const VecInst* __restrict__ insts) {
   float mx = 0.f;
   for (int64_t i = lane; i < V.n; i += 32) {
     cd a = ldc(V.A, i + j * V.lda);
-    mx = fmaxf(mx, fabs_c(a) * (float)(1.0 / V.rows[i]));
+    mx = fmaxf(mx, fabs_c(a) * V.rows_inv[i]);
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));

@@ -17,6 +17,7 @@ struct VecInst {
   double* cols;      // column scales (n), or null
   double* rowsum;    // row sums of |A| (n)
   double* cols_inv;  // 1 / cols (n), filled by the scaled-copy launch
+  float* rows_inv;   // 1 / rows (n), filled by the row-statistics launch
   double* part;      // scratch: kChunks * nrhs * n * 3 doubles (>= kChunks * n * 2)
   void* out;         // scaled copy / correction work buffer (ld n)
   int32_t out_single;

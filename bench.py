@@ -119,14 +119,28 @@ def measured_peaks():
     return 6800.0, 1900.0, "fallback"
 
 
-def lu_update_flops(N, nb):
-    """Algorithmic real flops of the trailing updates of one complex LU (8 per MAC)."""
-    tot = 0.0
+def lu_update_work(N, nb):
+    """Algorithmic real flops (8 per complex MAC) and bytes of the trailing updates
+    C -= A B of one complex LU: C (m x m complex64) read and written, the packed
+    split-bf16 operand images A (m x nb) and B (nb x m) read, 8 bytes per complex element."""
+    flops = byts = 0.0
     for k0 in range(0, N, nb):
         nbe = min(nb, N - k0)
         m = N - k0 - nbe
-        tot += 8.0 * m * m * nbe
-    return tot
+        flops += 8.0 * m * m * nbe
+        byts += 16.0 * m * m + 8.0 * nbe * 2 * m
+    return flops, byts
+
+
+def lu_update_flops(N, nb):
+    return lu_update_work(N, nb)[0]
+
+
+# DRAM traffic of one k_tc_cgemm launch over its algorithmic bytes, from one ncu capture
+# (--set full) of `bench.py --freqs 2 --nlon 48 --nrings 30`: 4th launch = trailing
+# update of outer step 1 of 2 x 5760 unknowns (m = n = 5504, k = 128),
+# dram__bytes_read.sum + dram__bytes_write.sum = 507.54 + 423.62 MB.
+NCU_GEMM_TRAFFIC = (507.543808e6 + 423.618560e6) / (2 * (16.0 * 5504 ** 2 + 8.0 * 128 * 2 * 5504))
 
 
 def aggregate_replicas(ms, units, world):
@@ -214,9 +228,13 @@ def run_ours(args):
     hbm, bf16, which = measured_peaks()
     fam = "gemm_tc" if prof["gemm_tc"][0] else "gemm_c64"
     nb = 128 if fam == "gemm_tc" else 32
-    flops_step = args.freqs * lu_update_flops(N, nb)
+    flops_one, bytes_one = lu_update_work(N, nb)
+    flops_step, bytes_step = args.freqs * flops_one, args.freqs * bytes_one
     gl, gms = prof[fam]
-    achieved = flops_step * args.steps / (gms * 1e-3) / 1e12 if gms else 0.0
+    secs = gms * 1e-3 / args.steps if gms else 0.0
+    achieved_gbs = bytes_step / secs / 1e9 if secs else 0.0
+    achieved_tf = flops_step / secs / 1e12 if secs else 0.0
+    launches_step = max(1, gl // args.steps)
     ms, value = aggregate_replicas(ms, args.freqs, world)
     if rank != 0:
         return None
@@ -244,10 +262,22 @@ def run_ours(args):
                        "factor_precision": sorted({d["factor_precision"] for d in diags_mixed})},
         "e2e": {"value": args.freqs / (e2e_ms * 1e-3), "unit": "solves/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(16 * args.freqs)},
-        "roofline": {"bound": "tensor", "kernel": fam, "achieved": achieved, "peak": bf16,
-                     "unit": "TFLOP/s", "frac": achieved / bf16 if bf16 else None,
-                     "peak_source": f"{which} bf16 dense", "traffic": None,
-                     "launches": gl, "kernel_ms_per_step": gms / args.steps},
+        # rank-nb complex update: 8 nb flops per 16 bytes of C = nb / 2 flops/byte, below
+        # the ridge of the split-bf16 tensor path (3 bf16 MMAs per real product), so HBM
+        # bounds it; the tensor view is kept beside it
+        "roofline": {"bound": "hbm", "kernel": "k_tc_cgemm (LU trailing update)",
+                     "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved_gbs / hbm if hbm else None,
+                     "peak_source": f"{which} HBM copy",
+                     "traffic": NCU_GEMM_TRAFFIC * bytes_step / launches_step,
+                     "algorithmic_bytes_per_launch": bytes_step / launches_step,
+                     "traffic_note": "ncu dram bytes of a smaller capture, scaled by C size",
+                     "launches": gl, "kernel_ms_per_step": gms / args.steps,
+                     "tensor_view": {"achieved_tflops": achieved_tf,
+                                     "ceiling_tflops": bf16 / 3.0,
+                                     "frac": achieved_tf / (bf16 / 3.0) if bf16 else None,
+                                     "note": "algorithmic complex flops; ceiling = measured "
+                                             "bf16 / 3 split products"}},
         "phase_ms_per_step": {k: v[1] / args.steps for k, v in prof.items() if v[0]},
         "gpu_launches": int(launches // max(1, args.steps)),
         "clocks": clk,

@@ -264,6 +264,53 @@ int bemgpu_pressure(bemgpu_solution *sol, int32_t rhs, int64_t npts, const doubl
                     int32_t field, double *out);
 int bemgpu_solution_destroy(bemgpu_solution *sol);
 
+/* ------------------------------------------------------------------ serving */
+/*
+ * Request loop over one context (a worker thread inside the library).  A request is one
+ * surface and boundary problem at nfreq wavenumbers and nangles incidence directions;
+ * each (request, wavenumber) is one work item.  Continuous batching: the worker
+ * repeatedly takes every pending item that fits the HBM budget (oldest first, at most
+ * max_batch factorisations per batch), factors the ones whose (mesh, k, boundary,
+ * precision) factor is not cached, solves all of them in one batched launch sequence
+ * and completes the requests whose items are all done; requests submitted while a
+ * batch runs join the next one.  Factors stay cached (LRU, cache_bytes) for reuse by
+ * later requests on the same mesh and wavenumber (sweeps.jl:680-701 reuses a factor
+ * across angles within one call).  Every item is computed exactly as alone: batching
+ * changes which launch carries it, not its arithmetic.
+ */
+typedef struct bemgpu_server bemgpu_server;
+
+typedef struct {
+  int32_t max_batch;     /* factorisations per batch (default 64) */
+  int32_t queue_limit;   /* pending requests before submit returns BEMGPU_EBUSY (4096) */
+  uint64_t cache_bytes;  /* bytes of cached factors kept between batches (default budget/4) */
+} bemgpu_server_options;
+
+typedef struct {
+  int64_t submitted, completed, failed;
+  int64_t items, factorizations, cache_hits, batches;
+  int64_t evictions;
+  double busy_ms;        /* device time of all batches */
+  uint64_t cached_bytes;
+} bemgpu_server_stats;
+
+void bemgpu_server_options_init(bemgpu_server_options *o);
+int bemgpu_server_create(bemgpu_ctx *ctx, const bemgpu_server_options *opts,
+                         bemgpu_server **server);
+/* ks: nfreq wavenumbers (problem->k is ignored); incidence: 2 * nangles (polar, azimuth). */
+int bemgpu_server_submit(bemgpu_server *server, const bemgpu_mesh *mesh,
+                         const bemgpu_problem *problem, int32_t nfreq, const double *ks,
+                         int32_t nangles, const double *incidence, int64_t *ticket);
+/* Wait up to timeout_ms (< 0: forever) for a request.  amplitudes receives the
+ * backscatter amplitudes (2 * nfreq * nangles doubles, frequency-major), latency_ms the
+ * time from submit to completion.  BEMGPU_ETIMEOUT if not done in time; the request's
+ * own failure status otherwise.  A waited request is released. */
+int bemgpu_server_wait(bemgpu_server *server, int64_t ticket, int32_t timeout_ms,
+                       double *amplitudes, double *latency_ms);
+int bemgpu_server_stats_get(bemgpu_server *server, bemgpu_server_stats *stats);
+/* Stops the worker after the running batch; pending requests fail with BEMGPU_EBUSY. */
+int bemgpu_server_destroy(bemgpu_server *server);
+
 /* ------------------------------------------------------------------ dense linear algebra */
 /*
  * Solve A X = B for a caller-supplied dense complex matrix (n x n column-major,

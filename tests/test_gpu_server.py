@@ -1,0 +1,78 @@
+"""Continuous-batching server: every result is the same alone and in the mix, factors are
+reused across requests, and the budget-driven admission completes everything."""
+import math
+
+import numpy as np
+import pytest
+
+import bemgpu
+from bemgpu import meshes
+
+pytestmark = pytest.mark.gpu
+
+
+def _surfaces():
+    a = bemgpu.mesh(*meshes.icosphere(0.01, 2))
+    b = bemgpu.mesh(*meshes.uv_spheroid(0.02, 0.008, 24, 16, jitter=0.02, seed=5))
+    c = bemgpu.mesh(*meshes.body_of_revolution(0.01, 2.5, [0.03, -0.02, 0.01, 0.04], 16, 20))
+    return a, b, c
+
+
+def test_same_alone_and_in_the_mix(ctx):
+    a, b, c = _surfaces()
+    srv = bemgpu.Server(ctx, max_batch=8)
+    try:
+        req = (a, bemgpu.Rigid(), [300.0, 420.0], [0.3, 1.1, 2.0])
+        t = srv.submit(*req, precision="mixed")
+        alone, lat = srv.wait(t)
+        assert lat > 0 and np.all(np.isfinite(alone))
+        # the same request among others of different sizes and kinds, submitted together
+        tickets = [srv.submit(b, bemgpu.FluidFilled(1.0357, 1.0279), [500.0, 700.0], [0.5],
+                              precision="mixed"),
+                   srv.submit(*req, precision="mixed"),
+                   srv.submit(c, bemgpu.PressureRelease(), [250.0], [0.2, 0.4],
+                              precision="mixed"),
+                   srv.submit(a, bemgpu.Rigid(), [300.0], [0.7], precision="double")]
+        res = [srv.wait(tk)[0] for tk in tickets]
+        assert np.array_equal(res[1], alone)   # bit-identical: batching is not arithmetic
+        st = srv.stats()
+        assert st["completed"] == 5 and st["failed"] == 0
+        assert st["cache_hits"] >= 2           # the repeated request reused its factors
+    finally:
+        srv.close()
+
+
+def test_server_matches_direct_solve(ctx):
+    a, _, _ = _surfaces()
+    srv = bemgpu.Server(ctx)
+    try:
+        angles = [0.3, 1.2]
+        t = srv.submit(a, bemgpu.Rigid(), [350.0], angles)
+        got, _ = srv.wait(t)
+    finally:
+        srv.close()
+    for r, ang in enumerate(angles):
+        sol = bemgpu.bem(a, bemgpu.Rigid(), 350.0, incidence_angle=ang, ctx=ctx)
+        want = bemgpu.scattering_amplitude(sol)
+        assert abs(got[0, r] - want) <= 1e-12 * abs(want)
+
+
+def test_server_many_requests_complete(ctx):
+    a, b, c = _surfaces()
+    srv = bemgpu.Server(ctx, max_batch=4, cache_bytes=1 << 20)
+    rng = np.random.default_rng(3)
+    try:
+        tickets = []
+        for i in range(12):
+            s = (a, b, c)[i % 3]
+            bc = bemgpu.Rigid() if i % 2 else bemgpu.PressureRelease()
+            ks = rng.uniform(200, 600, size=1 + i % 3)
+            tickets.append(srv.submit(s, bc, ks, rng.uniform(0, math.pi, size=1 + i % 2),
+                                      precision="mixed"))
+        for tk in tickets:
+            out, lat = srv.wait(tk, timeout_ms=120000)
+            assert np.all(np.isfinite(out)) and lat > 0
+        st = srv.stats()
+        assert st["completed"] == 12 and st["batches"] >= 2
+    finally:
+        srv.close()
