@@ -261,7 +261,7 @@ struct MeshData {
   char hash[65] = {0};
   double center[3] = {0, 0, 0};
   std::vector<double> panels_h;  // FP64 records
-  Buf panels, panelsf, verts, near_i, near_j, near_lap;
+  Buf panels, panelsf, verts, near_i, near_j, near_ptr, near_lap;
   int64_t n_near = 0;
   double eta = 2.0;
 };
@@ -358,11 +358,13 @@ int make_mesh(bemgpu_ctx* c, const double* nodes, int64_t N, const int64_t* tris
       nj[p] = (int32_t)cols[p];
     }
   m->n_near = (int64_t)cols.size();
+  std::vector<int32_t> np(rowptr.begin(), rowptr.end());
   TRY(upload(c, m->panels_h, &m->panels));
   TRY(upload(c, recf, &m->panelsf));
   TRY(upload(c, verts, &m->verts));
   TRY(upload(c, ni, &m->near_i));
   TRY(upload(c, nj, &m->near_j));
+  TRY(upload(c, np, &m->near_ptr));
   TRY(alloc(c, (size_t)std::max<int64_t>(1, m->n_near) * 32, &m->near_lap));
   launch_near_laplace(c->launch(), m->panels.as<double>(), m->verts.as<double>(),
                       m->near_i.as<int32_t>(), m->near_j.as<int32_t>(), m->n_near,
@@ -383,10 +385,12 @@ struct FactorData {
   int kind = kAsmBM;
   int64_t n = 0, N = 0;
   bool rhs_is_m2 = true;   // rigid: b = M2 q_inc; soft: b = M1 p_inc
-  Buf A, Mrhs;             // complex128 system, rhs operator
+  Buf A, Mrhs;             // system (complex128, or complex64 when a32), rhs operator
+  bool a32 = false;        // system stored compact: complex64 + FP64 near corrections
+  Buf dnear;               // near corrections of the compact system
   Buf LU, ipiv, info, perm;        // working factor (complex64 when single)
   Buf LU64, ipiv64, info64, perm64;  // complex128 factor after promotion
-  Buf rows, cols, rowsum, cols_inv, rows_inv;
+  Buf rows, cols, rowsum, cols_inv, rows_inv, cols_inv32;
   bool single = false;     // current factor precision
   bool mixed = false;      // requested precision
   bool fp32_regular = false;  // regular pairs assembled in FP32
@@ -400,8 +404,8 @@ struct FactorData {
   int32_t* info_ptr() const { return single ? info.as<int32_t>() : (mixed ? info64.as<int32_t>() : info.as<int32_t>()); }
   int32_t* perm_ptr() const { return single ? perm.as<int32_t>() : (mixed ? perm64.as<int32_t>() : perm.as<int32_t>()); }
   size_t bytes() const {
-    return A.bytes + Mrhs.bytes + LU.bytes + LU64.bytes + ipiv.bytes + ipiv64.bytes + rows.bytes +
-           cols.bytes + rowsum.bytes;
+    return A.bytes + dnear.bytes + Mrhs.bytes + LU.bytes + LU64.bytes + ipiv.bytes +
+           ipiv64.bytes + rows.bytes + cols.bytes + rowsum.bytes;
   }
 };
 }  // namespace
@@ -489,8 +493,11 @@ int assemble_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
     const bool fluid = f->kind == kAsmMuller || f->kind == kAsmFluidCBIE;
     f->n = m->n;
     f->N = fluid ? 2 * m->n : m->n;
-    TRY(alloc(c, (size_t)f->N * f->N * 16, &f->A));
+    f->a32 = f->fp32_regular;
+    TRY(alloc(c, (size_t)f->N * f->N * (f->a32 ? 8 : 16), &f->A));
     if (!fluid) TRY(alloc(c, (size_t)f->n * f->n * 16, &f->Mrhs));
+    if (f->a32)
+      TRY(alloc(c, (size_t)std::max<int64_t>(1, m->n_near) * (fluid ? 4 : 1) * 16, &f->dnear));
     AsmInst& I = ai[t];
     std::memset(&I, 0, sizeof I);
     I.panels = m->panels.as<double>();
@@ -511,12 +518,15 @@ int assemble_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
     if (fluid) {
       I.out1 = f->A.p;
       I.out2 = nullptr;
+      I.c64 = f->a32 ? 1 : 0;
     } else {
       // rigid: system M1, rhs M2; pressure release: system M2, rhs M1
       f->rhs_is_m2 = f->prob.boundary == BEMGPU_RIGID;
       I.out1 = f->rhs_is_m2 ? f->A.p : f->Mrhs.p;
       I.out2 = f->rhs_is_m2 ? f->Mrhs.p : f->A.p;
+      I.c64 = f->a32 ? (f->rhs_is_m2 ? 1 : 2) : 0;
     }
+    I.dnear = f->a32 ? f->dnear.as<double>() : nullptr;
   }
   // group by (kind, regular precision) so each group is one launch
   std::vector<size_t> order(fs.size());
@@ -548,11 +558,12 @@ int assemble_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
     while (s < order.size()) {
       size_t e = s;
       int64_t nmax = 0;
-      while (e < order.size() && fs[order[e]]->kind == fs[order[s]]->kind) {
+      while (e < order.size() && key(order[e]) == key(order[s])) {
         nmax = std::max(nmax, fs[order[e]]->mesh->n_near);
         ++e;
       }
-      launch_assemble_near(L, d_ai.as<AsmInst>() + s, (int)(e - s), nmax, fs[order[s]]->kind);
+      launch_assemble_near(L, d_ai.as<AsmInst>() + s, (int)(e - s), nmax, fs[order[s]]->kind,
+                           fs[order[s]]->fp32_regular);
       s = e;
     }
   }
@@ -948,6 +959,20 @@ int getrf_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, int prec, bool prom
   return BEMGPU_OK;
 }
 
+// Compact-storage fields of a product / sweep over the system matrix of f.
+void set_compact(VecInst& v, const FactorData* f) {
+  if (!f->a32) return;
+  const MeshData* m = f->mesh.get();
+  v.a32 = 1;
+  v.nbc = f->N == 2 * f->n ? 2 : 1;
+  v.n_mesh = f->n;
+  v.n_near = m->n_near;
+  v.near_ptr = m->near_ptr.as<int32_t>();
+  v.near_i = m->near_i.as<int32_t>();
+  v.near_j = m->near_j.as<int32_t>();
+  v.dnear = f->dnear.as<double>();
+}
+
 // Scaled copy of A into a factor buffer (single -> LU as complex64, else complex128).
 int scale_copy_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, std::vector<Buf>& part,
                      bool to_promoted, std::vector<int32_t>* flags) {
@@ -970,6 +995,9 @@ int scale_copy_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, std::vector<Bu
     v.cols = f->cols.as<double>();
     v.rowsum = f->rowsum.as<double>();
     v.cols_inv = f->cols_inv.as<double>();
+    v.cols_inv32 = f->cols_inv32.as<float>();
+    v.rows_inv = f->rows_inv.as<float>();
+    set_compact(v, f);
     v.part = part[t].as<double>();
     v.out = to_promoted ? f->LU64.p : f->LU.p;
     v.out_single = (!to_promoted && f->single) ? 1 : 0;
@@ -982,6 +1010,11 @@ int scale_copy_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, std::vector<Bu
   {
     Prof pr(c, "scale_copy");
     launch_scale_copy(L, d.as<VecInst>(), (int)fs.size(), nmax);
+    if (to_promoted) {  // complex128 factor: exact near values of compact systems
+      int64_t mn = 0;
+      for (size_t t = 0; t < fs.size(); ++t) mn = std::max(mn, vi[t].a32 ? vi[t].n_near : 0);
+      launch_near_add(L, d.as<VecInst>(), (int)fs.size(), mn, 0);
+    }
   }
   std::vector<double> stats;
   std::vector<int32_t> fl;
@@ -1027,6 +1060,7 @@ int factorize_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
     TRY(alloc(c, (size_t)f->N * 8, &f->rowsum));
     TRY(alloc(c, (size_t)f->N * 8, &f->cols_inv));
     TRY(alloc(c, (size_t)f->N * 4, &f->rows_inv));
+    TRY(alloc(c, (size_t)f->N * 4, &f->cols_inv32));
     TRY(alloc(c, (size_t)kChunks * f->N * 2 * 8, &part[t]));
     TRY(alloc(c, (size_t)f->N * f->N * (f->single ? 8 : 16), &f->LU));
     TRY(alloc(c, (size_t)f->N * 4, &f->ipiv));
@@ -1040,6 +1074,7 @@ int factorize_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
     v.cols = f->cols.as<double>();
     v.rowsum = f->rowsum.as<double>();
     v.rows_inv = f->rows_inv.as<float>();
+    set_compact(v, f);
     v.part = part[t].as<double>();
     nmax = std::max(nmax, f->N);
   }
@@ -1133,6 +1168,7 @@ struct SolveInst {
   FactorData* f;
   int32_t R;
   Buf dirs, pinc, qinc, b, x, y, den, work, work2, stats, part, active, changed, tmp;
+  Buf xs, xa;  // split x of compact products
   std::vector<RhsState> rs;
 };
 
@@ -1157,6 +1193,11 @@ void fill_vec(VecInst& v, SolveInst& s, const void* A, int64_t N) {
   v.changed = s.changed.as<int32_t>();
   v.out = s.work.p;
   v.out_single = s.f->single ? 1 : 0;
+  if (A == s.f->A.p && s.f->a32) {
+    set_compact(v, s.f);
+    v.xs = s.xs.as<float4>();
+    v.xa = s.xa.as<float>();
+  }
 }
 
 // x (mode 0) or x += (mode 1) the scaled solve of the vectors in `src` (b or residual)
@@ -1299,6 +1340,10 @@ int solve_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<i
     TRY(alloc(c, (size_t)N * s.R * 16, &s.x));
     TRY(alloc(c, (size_t)N * s.R * 16, &s.y));
     TRY(alloc(c, (size_t)N * s.R * 8, &s.den));
+    if (f->a32) {
+      TRY(alloc(c, (size_t)N * s.R * 16, &s.xs));
+      TRY(alloc(c, (size_t)N * s.R * 4, &s.xa));
+    }
     TRY(alloc(c, (size_t)N * s.R * 16, &s.work));
     TRY(alloc(c, (size_t)kStats * s.R * 8, &s.stats));
     TRY(alloc(c, (size_t)std::max<int64_t>(kChunks * (int64_t)s.R * N * 3, kChunks * N * 2) * 8,
@@ -1642,7 +1687,10 @@ size_t item_bytes(const ServerReq& r) {
   const bool fl = r.prob.boundary == BEMGPU_FLUID;
   const size_t N = fl ? 2 * n : n;
   const bool mixed = r.prob.precision == BEMGPU_MIXED;
-  size_t b = N * N * 16 + N * N * (mixed ? 8 : 16) + (fl ? 0 : n * n * 16);
+  const bool a32 = r.prob.assembly == BEMGPU_ASSEMBLY_SINGLE ||
+                   (r.prob.assembly == BEMGPU_ASSEMBLY_DEFAULT && mixed);
+  size_t b = N * N * (a32 ? 8 : 16) + N * N * (mixed ? 8 : 16) + (fl ? 0 : n * n * 16);
+  b += a32 ? (size_t)r.mesh->n_near * (fl ? 4 : 1) * 16 : 0;
   b += 2 * tc_pack_bytes((int64_t)N, 128) + N * 64;
   const size_t R = (size_t)r.nangles;
   b += N * R * (16 * 6 + 8) + (size_t)kChunks * R * N * 3 * 8;
@@ -2606,12 +2654,33 @@ int bemgpu_assemble_dense(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_p
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   TRY(check_device_error(c));
   const bool fluid = kind == kAsmMuller || kind == kAsmFluidCBIE;
+  // the compact system expanded to complex128 (value + near correction)
+  Buf full;
+  const void* sys = f->A.p;
+  if (f->a32) {
+    TRY(alloc(c, (size_t)f->N * f->N * 16, &full));
+    VecInst v;
+    std::memset(&v, 0, sizeof v);
+    v.A = f->A.p;
+    v.n = f->N;
+    v.lda = f->N;
+    v.out = full.p;
+    set_compact(v, f.get());
+    std::vector<VecInst> vi{v};
+    Buf d;
+    TRY(to_device(c, vi, &d));
+    const Launch L = c->launch();
+    launch_expand_a32(L, d.as<VecInst>(), 1, f->N);
+    launch_near_add(L, d.as<VecInst>(), 1, v.n_near, 1);
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    sys = full.p;
+  }
   // M1 / M2 in the reference's naming: rigid system is M1, pressure release system is M2
   if (fluid) {
-    CUDA_TRY(c, cudaMemcpy(M1, f->A.p, (size_t)f->N * f->N * 16, cudaMemcpyDeviceToHost));
+    CUDA_TRY(c, cudaMemcpy(M1, sys, (size_t)f->N * f->N * 16, cudaMemcpyDeviceToHost));
   } else {
-    const void* m1 = f->rhs_is_m2 ? f->A.p : f->Mrhs.p;
-    const void* m2 = f->rhs_is_m2 ? f->Mrhs.p : f->A.p;
+    const void* m1 = f->rhs_is_m2 ? sys : f->Mrhs.p;
+    const void* m2 = f->rhs_is_m2 ? f->Mrhs.p : sys;
     CUDA_TRY(c, cudaMemcpy(M1, m1, (size_t)f->n * f->n * 16, cudaMemcpyDeviceToHost));
     if (M2) CUDA_TRY(c, cudaMemcpy(M2, m2, (size_t)f->n * f->n * 16, cudaMemcpyDeviceToHost));
   }

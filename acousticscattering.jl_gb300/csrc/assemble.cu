@@ -5,7 +5,9 @@
 // are staged in shared memory by one bulk asynchronous copy (TMA engine).  All threads
 // of a warp read the same source record (shared-memory broadcast) and write the
 // column-major matrix entry of their own row, so every warp store is 32 consecutive
-// complex128 values (512 contiguous bytes).
+// complex values (256 or 512 contiguous bytes).  The mixed-precision system is stored
+// as complex64 (exact for the FP32 rule); the FP64 near values it cannot hold exactly
+// keep their rounding error in a sparse correction list.
 // Near pairs: one thread per listed pair evaluates the FP64 singular rules and
 // overwrites the regular value (stream order guarantees the regular kernel ran first).
 #include <cstdio>
@@ -87,6 +89,25 @@ __device__ __forceinline__ void regular_panel(const R* rec, const R x[3], const 
 __device__ __forceinline__ void store_c(void* base, int64_t idx, cd v) {
   reinterpret_cast<double2*>(base)[idx] = make_double2(v.x, v.y);
 }
+// regular entry: complex64 outputs take the value as computed (exact for the FP32 rule)
+template <typename R>
+__device__ __forceinline__ void store_r(void* base, bool c64, int64_t idx, cx<R> v) {
+  if (c64)
+    reinterpret_cast<float2*>(base)[idx] = make_float2((float)v.x, (float)v.y);
+  else
+    reinterpret_cast<double2*>(base)[idx] = make_double2((double)v.x, (double)v.y);
+}
+// near entry: complex64 outputs keep the FP64 rounding error as a correction
+__device__ __forceinline__ void store_n(void* base, bool c64, double* dnear, int64_t dpos,
+                                        int64_t idx, cd v) {
+  if (c64) {
+    const float2 f = make_float2((float)v.x, (float)v.y);
+    reinterpret_cast<float2*>(base)[idx] = f;
+    reinterpret_cast<double2*>(dnear)[dpos] = make_double2(v.x - (double)f.x, v.y - (double)f.y);
+  } else {
+    store_c(base, idx, v);
+  }
+}
 
 template <typename R, int KIND>
 __global__ void __launch_bounds__(kAsmRows) k_assemble_regular(const AsmInst* __restrict__ insts,
@@ -138,8 +159,8 @@ __global__ void __launch_bounds__(kAsmRows) k_assemble_regular(const AsmInst* __
         m1 -= al * a.H;
         m2 += al * a.K;
       }
-      store_c(I.out1, i + j * lda, cd{(double)m1.x, (double)m1.y});
-      store_c(I.out2, i + j * lda, cd{(double)m2.x, (double)m2.y});
+      store_r(I.out1, I.c64 == 1, i + j * lda, m1);
+      store_r(I.out2, I.c64 == 2, i + j * lda, m2);
     } else {
       Acc<R> e, t;
       e.S = e.D = e.K = e.H = cx<R>{0, 0};
@@ -161,15 +182,26 @@ __global__ void __launch_bounds__(kAsmRows) k_assemble_regular(const AsmInst* __
         a21 = t.D;
         a22 = cx<R>{-g * t.S.x, -g * t.S.y};
       }
-      store_c(I.out1, i + j * lda, cd{(double)a11.x, (double)a11.y});
-      store_c(I.out1, i + (n + j) * lda, cd{(double)a12.x, (double)a12.y});
-      store_c(I.out1, (n + i) + j * lda, cd{(double)a21.x, (double)a21.y});
-      store_c(I.out1, (n + i) + (n + j) * lda, cd{(double)a22.x, (double)a22.y});
+      const bool c64 = I.c64 == 1;
+      store_r(I.out1, c64, i + j * lda, a11);
+      store_r(I.out1, c64, i + (n + j) * lda, a12);
+      store_r(I.out1, c64, (n + i) + j * lda, a21);
+      store_r(I.out1, c64, (n + i) + (n + j) * lda, a22);
     }
   }
 }
 
-template <int KIND>
+template <int KIND, bool F32>
+__device__ __forceinline__ Ops near_pair(const double* v, const double* rj, const double* x,
+                                         const double* nx, bool self, double k, double S0,
+                                         double D0, double K0, double H0) {
+  if (F32) return near_ops_f(v, rj, x, nx, self, k, S0, D0, K0, H0);
+  return near_ops(v, rj, x, nx, self, k, S0, D0, K0, H0);
+}
+
+// F32: remainders in FP32 (mixed-precision assembly); the Laplace parts and the block
+// combinations stay FP64.
+template <int KIND, bool F32>
 __global__ void __launch_bounds__(128) k_assemble_near(const AsmInst* __restrict__ insts) {
   const AsmInst& I = insts[blockIdx.z];
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -187,7 +219,7 @@ __global__ void __launch_bounds__(128) k_assemble_near(const AsmInst* __restrict
   const int64_t n = I.n, lda = I.lda;
   const double delta = self ? 1.0 : 0.0;
   if (KIND == kAsmBM || KIND == kAsmCBIE) {
-    Ops o = near_ops(v, rj, x, nx, self, I.k_e, S0, D0, K0, H0);
+    Ops o = near_pair<KIND, F32>(v, rj, x, nx, self, I.k_e, S0, D0, K0, H0);
     cd m1 = cd{0.5 * delta - o.D.x, -o.D.y};
     cd m2 = o.S;
     if (KIND == kAsmBM) {
@@ -195,11 +227,11 @@ __global__ void __launch_bounds__(128) k_assemble_near(const AsmInst* __restrict
       m1 -= al * o.H;
       m2 += al * (o.K + cd{0.5 * delta, 0.0});
     }
-    store_c(I.out1, i + j * lda, m1);
-    store_c(I.out2, i + j * lda, m2);
+    store_n(I.out1, I.c64 == 1, I.dnear, p, i + j * lda, m1);
+    store_n(I.out2, I.c64 == 2, I.dnear, p, i + j * lda, m2);
   } else {
-    Ops e = near_ops(v, rj, x, nx, self, I.k_e, S0, D0, K0, H0);
-    Ops t = near_ops(v, rj, x, nx, self, I.k_i, S0, D0, K0, H0);
+    Ops e = near_pair<KIND, F32>(v, rj, x, nx, self, I.k_e, S0, D0, K0, H0);
+    Ops t = near_pair<KIND, F32>(v, rj, x, nx, self, I.k_i, S0, D0, K0, H0);
     const double g = I.g;
     cd a11, a12, a21, a22;
     if (KIND == kAsmMuller) {
@@ -213,10 +245,12 @@ __global__ void __launch_bounds__(128) k_assemble_near(const AsmInst* __restrict
       a21 = cd{0.5 * delta + t.D.x, t.D.y};
       a22 = cd{-g * t.S.x, -g * t.S.y};
     }
-    store_c(I.out1, i + j * lda, a11);
-    store_c(I.out1, i + (n + j) * lda, a12);
-    store_c(I.out1, (n + i) + j * lda, a21);
-    store_c(I.out1, (n + i) + (n + j) * lda, a22);
+    const bool c64 = I.c64 == 1;
+    const int64_t nn = I.n_near;
+    store_n(I.out1, c64, I.dnear, p, i + j * lda, a11);
+    store_n(I.out1, c64, I.dnear, nn + p, i + (n + j) * lda, a12);
+    store_n(I.out1, c64, I.dnear, 2 * nn + p, (n + i) + j * lda, a21);
+    store_n(I.out1, c64, I.dnear, 3 * nn + p, (n + i) + (n + j) * lda, a22);
   }
 }
 
@@ -271,16 +305,26 @@ void launch_assemble_regular(const Launch& L, const AsmInst* d_inst, int ninst, 
     launch_regular_t<double>(L, d_inst, ninst, nmax, kind);
 }
 
-void launch_assemble_near(const Launch& L, const AsmInst* d_inst, int ninst, int64_t max_near,
+template <bool F32>
+static void launch_near_t(const Launch& L, const AsmInst* d_inst, int ninst, int64_t max_near,
                           int kind) {
-  if (max_near <= 0 || ninst <= 0) return;
   dim3 grid((unsigned)((max_near + 127) / 128), 1, (unsigned)ninst);
   switch (kind) {
-    case kAsmBM: k_assemble_near<kAsmBM><<<grid, 128, 0, L.stream>>>(d_inst); count_launch(1); break;
-    case kAsmCBIE: k_assemble_near<kAsmCBIE><<<grid, 128, 0, L.stream>>>(d_inst); count_launch(1); break;
-    case kAsmMuller: k_assemble_near<kAsmMuller><<<grid, 128, 0, L.stream>>>(d_inst); count_launch(1); break;
-    default: k_assemble_near<kAsmFluidCBIE><<<grid, 128, 0, L.stream>>>(d_inst); count_launch(1); break;
+    case kAsmBM: k_assemble_near<kAsmBM, F32><<<grid, 128, 0, L.stream>>>(d_inst); break;
+    case kAsmCBIE: k_assemble_near<kAsmCBIE, F32><<<grid, 128, 0, L.stream>>>(d_inst); break;
+    case kAsmMuller: k_assemble_near<kAsmMuller, F32><<<grid, 128, 0, L.stream>>>(d_inst); break;
+    default: k_assemble_near<kAsmFluidCBIE, F32><<<grid, 128, 0, L.stream>>>(d_inst); break;
   }
+  count_launch(1);
+}
+
+void launch_assemble_near(const Launch& L, const AsmInst* d_inst, int ninst, int64_t max_near,
+                          int kind, bool fp32) {
+  if (max_near <= 0 || ninst <= 0) return;
+  if (fp32)
+    launch_near_t<true>(L, d_inst, ninst, max_near, kind);
+  else
+    launch_near_t<false>(L, d_inst, ninst, max_near, kind);
 }
 
 // ------------------------------------------------------------------ incident traces

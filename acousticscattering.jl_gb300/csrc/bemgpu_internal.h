@@ -75,9 +75,10 @@ struct AsmInst {
   double k_e, k_i, g;      // exterior/interior wavenumber, density contrast
   double a_re, a_im;       // Burton-Miller coupling (0 for CBIE)
   int32_t kind;            // AsmKind
-  int32_t pad;
-  void* out1;              // complex128 M1 (or A for fluid)
-  void* out2;              // complex128 M2 (rigid/soft), null for fluid
+  int32_t c64;             // 0: both outputs complex128; 1 / 2: out1 / out2 is complex64
+  void* out1;              // M1 (or A for fluid)
+  void* out2;              // M2 (rigid/soft), null for fluid
+  double* dnear;           // complex64 output: FP64 near corrections [block][n_near]
 };
 
 // Incident field / far-field instance.
@@ -124,7 +125,7 @@ struct Launch {
 void launch_assemble_regular(const Launch& L, const AsmInst* d_inst, int ninst, int64_t nmax,
                              int kind, bool fp32);
 void launch_assemble_near(const Launch& L, const AsmInst* d_inst, int ninst, int64_t max_near,
-                          int kind);
+                          int kind, bool fp32);
 // closed-form Laplace parts of every near pair of a mesh (wavenumber independent)
 void launch_near_laplace(const Launch& L, const double* panels, const double* verts,
                          const int32_t* near_i, const int32_t* near_j, int64_t n_near,

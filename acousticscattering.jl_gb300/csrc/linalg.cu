@@ -593,12 +593,23 @@ void launch_linv_neg(const Launch& L, const MatInst* d, int ninst, int64_t k0, f
 
 // ------------------------------------------------------------------ blocked solves
 // Two-level triangular solve: diagonal blocks of kBigB rows are solved by one CTA per
-// (rhs, instance) holding the block's slice of the vector in shared memory (32-row
-// sub-blocks by one warp, the rest of the block updated by the CTA); the rows outside the
-// block are then updated by a full-GPU product kernel.  About 2 n / kBigB launches per
-// triangle.
+// (rhs, instance) holding the block's slice of the vector in shared memory; the rows
+// outside the block are then updated by a full-GPU product kernel.  About 2 n / kBigB
+// launches per triangle.
+//
+// Inside a diagonal block the 32 x 32 triangle of each sub-block is staged in shared
+// memory (double-buffered: the next sub-block's triangle is fetched while warp 0 solves
+// the current one from shared memory with shuffles), then all warps update the rest of
+// the block.  op(A) = A^H reads A along its columns in both phases (a warp per row,
+// lanes along the column), so every global access is coalesced.
 constexpr int kBigB = 1024;
 constexpr int kDiagThreads = 512;
+constexpr int kTilePad = 33;
+
+template <typename R>
+constexpr size_t diag_smem_bytes() {
+  return sizeof(cx<R>) * (kBigB + 2 * 32 * kTilePad);
+}
 
 template <typename R, bool EFF_LOWER, bool TRANS, bool UNIT>
 __global__ void __launch_bounds__(kDiagThreads) k_trsv_diag(const MatInst* __restrict__ insts,
@@ -608,54 +619,94 @@ __global__ void __launch_bounds__(kDiagThreads) k_trsv_diag(const MatInst* __res
   if (!M.active || rhs >= M.nrhs || r0 >= M.n) return;
   const int64_t n = M.n, lda = M.lda, off = (int64_t)rhs * M.ldx;
   const int nbs = (int)min((int64_t)kBigB, n - r0);
-  __shared__ cx<R> sx[kBigB];
+  extern __shared__ __align__(16) unsigned char diag_smem[];
+  cx<R>* sx = reinterpret_cast<cx<R>*>(diag_smem);
+  cx<R>* tiles = sx + kBigB;  // [2][32][kTilePad], tile[i][j] = op(A)[s0 + i, s0 + j]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int i = tid; i < nbs; i += kDiagThreads) sx[i] = ld<R>(M.x, off + r0 + i);
-  __syncthreads();
   const int nsub = (nbs + 31) / 32;
+  auto sub_of = [&](int bb) { return EFF_LOWER ? bb : nsub - 1 - bb; };
+  // stage the triangle of sub-block b in tile buffer buf (threads [t0, kDiagThreads))
+  auto stage = [&](int buf, int b, int t0) {
+    const int s0 = b * 32, nb = min(32, nbs - s0);
+    cx<R>* T = tiles + buf * 32 * kTilePad;
+    for (int e = tid - t0; e < 1024; e += kDiagThreads - t0) {
+      const int p = e & 31, q = e >> 5;  // physical A[s0 + p, s0 + q], coalesced in p
+      cx<R> v = {0, 0};
+      if (p < nb && q < nb) v = ld<R>(M.a, (r0 + s0 + p) + (r0 + s0 + q) * lda);
+      if (TRANS)
+        T[q * kTilePad + p] = cconj(v);
+      else
+        T[p * kTilePad + q] = v;
+    }
+  };
+  for (int i = tid; i < nbs; i += kDiagThreads) sx[i] = ld<R>(M.x, off + r0 + i);
+  stage(0, sub_of(0), 0);
+  __syncthreads();
   for (int bb = 0; bb < nsub; ++bb) {
-    const int b = EFF_LOWER ? bb : nsub - 1 - bb;
+    const int b = sub_of(bb);
     const int s0 = b * 32;
     const int nb = min(32, nbs - s0);
+    const cx<R>* T = tiles + (bb & 1) * 32 * kTilePad;
     if (warp == 0) {
       cx<R> x = lane < nb ? sx[s0 + lane] : cx<R>{0, 0};
       if (EFF_LOWER) {
         for (int c = 0; c < nb; ++c) {
-          if (!UNIT && lane == c)
-            x = x * cinv(opel<R, TRANS>(M.a, lda, r0 + s0 + c, r0 + s0 + c));
+          if (!UNIT && lane == c) x = x * cinv(T[c * kTilePad + c]);
           cx<R> xc;
           xc.x = __shfl_sync(0xffffffffu, x.x, c);
           xc.y = __shfl_sync(0xffffffffu, x.y, c);
-          if (lane > c && lane < nb)
-            x -= opel<R, TRANS>(M.a, lda, r0 + s0 + lane, r0 + s0 + c) * xc;
+          if (lane > c && lane < nb) x -= T[lane * kTilePad + c] * xc;
         }
       } else {
         for (int c = nb - 1; c >= 0; --c) {
-          if (!UNIT && lane == c)
-            x = x * cinv(opel<R, TRANS>(M.a, lda, r0 + s0 + c, r0 + s0 + c));
+          if (!UNIT && lane == c) x = x * cinv(T[c * kTilePad + c]);
           cx<R> xc;
           xc.x = __shfl_sync(0xffffffffu, x.x, c);
           xc.y = __shfl_sync(0xffffffffu, x.y, c);
-          if (lane < c) x -= opel<R, TRANS>(M.a, lda, r0 + s0 + lane, r0 + s0 + c) * xc;
+          if (lane < c) x -= T[lane * kTilePad + c] * xc;
         }
       }
       if (lane < nb) sx[s0 + lane] = x;
+    } else if (bb + 1 < nsub) {
+      stage((bb + 1) & 1, sub_of(bb + 1), 32);
     }
     __syncthreads();
     const int lo = EFF_LOWER ? s0 + nb : 0, hi = EFF_LOWER ? nbs : s0;
-    for (int r = lo + tid; r < hi; r += kDiagThreads) {
-      cx<R> acc = {0, 0};
-      cx<R> lv[16];
+    if (!TRANS) {
+      for (int r = lo + tid; r < hi; r += kDiagThreads) {
+        cx<R> acc = {0, 0};
+        cx<R> lv[16];
 #pragma unroll
-      for (int h = 0; h < 32; h += 16) {
+        for (int h = 0; h < 32; h += 16) {
 #pragma unroll
-        for (int c = 0; c < 16; ++c)
-          lv[c] = (h + c < nb) ? opel<R, TRANS>(M.a, lda, r0 + r, r0 + s0 + h + c) : cx<R>{0, 0};
+          for (int c = 0; c < 16; ++c)
+            lv[c] = (h + c < nb) ? ld<R>(M.a, (r0 + r) + (r0 + s0 + h + c) * lda) : cx<R>{0, 0};
 #pragma unroll
-        for (int c = 0; c < 16; ++c)
-          if (h + c < nb) acc += lv[c] * sx[s0 + h + c];
+          for (int c = 0; c < 16; ++c)
+            if (h + c < nb) acc += lv[c] * sx[s0 + h + c];
+        }
+        sx[r] -= acc;
       }
-      sx[r] -= acc;
+    } else {
+      // op(A)[r, s0 + c] = conj(A[s0 + c, r]): lanes along c, 4 rows per warp pass
+      const cx<R> xv = lane < nb ? sx[s0 + lane] : cx<R>{0, 0};
+      for (int r = lo + warp * 4; r < hi; r += (kDiagThreads / 32) * 4) {
+        cx<R> v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          v[u] = (r + u < hi && lane < nb) ? ld<R>(M.a, (r0 + s0 + lane) + (r0 + r + u) * lda)
+                                           : cx<R>{0, 0};
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          cx<R> t = cconj(v[u]) * xv;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            t.x += __shfl_xor_sync(0xffffffffu, t.x, o);
+            t.y += __shfl_xor_sync(0xffffffffu, t.y, o);
+          }
+          if (lane == 0 && r + u < hi) sx[r + u] -= t;
+        }
+      }
     }
     __syncthreads();
   }
@@ -663,7 +714,7 @@ __global__ void __launch_bounds__(kDiagThreads) k_trsv_diag(const MatInst* __res
 }
 
 // Rows outside the solved block [r0, r0 + kBigB): x_r -= sum_c op(A)[r, c] x_c, one
-// thread per row, the block's solution in shared memory.
+// thread per row, the block's solution in shared memory (op(A) = A, coalesced along r).
 template <typename R, bool EFF_LOWER, bool TRANS>
 __global__ void __launch_bounds__(256) k_trsv_big_update(const MatInst* __restrict__ insts,
                                                          int64_t r0) {
@@ -690,6 +741,47 @@ __global__ void __launch_bounds__(256) k_trsv_big_update(const MatInst* __restri
       if (c0 + c < nbs) acc += lv[c] * sx[c0 + c];
   }
   st<R>(M.x, off + row, ld<R>(M.x, off + row) - acc);
+}
+
+// The same update for op(A) = A^H: x_r -= sum_c conj(A[c, r]) x_c reads column r of A,
+// so a warp takes 4 rows with its lanes along c (coalesced), then reduces by shuffles.
+constexpr int kTrUpRows = 32;  // rows per 256-thread CTA (8 warps x 4)
+template <typename R, bool EFF_LOWER>
+__global__ void __launch_bounds__(256) k_trsv_big_update_h(const MatInst* __restrict__ insts,
+                                                           int64_t r0) {
+  const MatInst& M = insts[blockIdx.z];
+  const int rhs = blockIdx.y;
+  const int64_t n = M.n;
+  if (!M.active || rhs >= M.nrhs || r0 >= n) return;
+  const int nbs = (int)min((int64_t)kBigB, n - r0);
+  const int64_t lda = M.lda, off = (int64_t)rhs * M.ldx;
+  __shared__ cx<R> sx[kBigB];
+  for (int i = threadIdx.x; i < nbs; i += blockDim.x) sx[i] = ld<R>(M.x, off + r0 + i);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int64_t row0 = (int64_t)blockIdx.x * kTrUpRows + warp * 4;
+  if (EFF_LOWER) row0 += r0 + nbs;
+  const int64_t lim = EFF_LOWER ? n : r0;
+  if (row0 >= lim) return;
+  cx<R> acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+  for (int c = lane; c < nbs; c += 32) {
+    const cx<R> xv = sx[c];
+    cx<R> v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      v[u] = (row0 + u < lim) ? ld<R>(M.a, (r0 + c) + (row0 + u) * lda) : cx<R>{0, 0};
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u] += cconj(v[u]) * xv;
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      acc[u].x += __shfl_xor_sync(0xffffffffu, acc[u].x, o);
+      acc[u].y += __shfl_xor_sync(0xffffffffu, acc[u].y, o);
+    }
+    if (lane == 0 && row0 + u < lim) st<R>(M.x, off + row0 + u, ld<R>(M.x, off + row0 + u) - acc[u]);
+  }
 }
 
 // x[i] = y[perm[i]] (forward interchanges as one gather; y holds a copy of x)
@@ -847,18 +939,30 @@ static void trsv_t(const Launch& L, const MatInst* d, int ninst, int64_t nmax, i
 template <typename R, bool EL, bool TR, bool UN>
 static void trsv_big_t(const Launch& L, const MatInst* d, int ninst, int64_t nmax,
                        int32_t max_rhs) {
+  constexpr size_t smem = diag_smem_bytes<R>();
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_trsv_diag<R, EL, TR, UN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    attr = true;
+  }
   const int64_t nblk = (nmax + kBigB - 1) / kBigB;
   for (int64_t b = 0; b < nblk; ++b) {
     const int64_t blk = EL ? b : nblk - 1 - b;
     const int64_t r0 = blk * kBigB;
-    k_trsv_diag<R, EL, TR, UN><<<dim3((unsigned)max_rhs, (unsigned)ninst), kDiagThreads, 0,
+    k_trsv_diag<R, EL, TR, UN><<<dim3((unsigned)max_rhs, (unsigned)ninst), kDiagThreads, smem,
                                  L.stream>>>(d, r0);
     count_launch(1);
     const int64_t rows = EL ? (nmax - r0 - kBigB) : r0;
     if (rows > 0) {
-      k_trsv_big_update<R, EL, TR><<<dim3((unsigned)((rows + 255) / 256), (unsigned)max_rhs,
-                                          (unsigned)ninst),
+      if (TR)
+        k_trsv_big_update_h<R, EL><<<dim3((unsigned)((rows + kTrUpRows - 1) / kTrUpRows),
+                                          (unsigned)max_rhs, (unsigned)ninst),
                                      256, 0, L.stream>>>(d, r0);
+      else
+        k_trsv_big_update<R, EL, TR><<<dim3((unsigned)((rows + 255) / 256), (unsigned)max_rhs,
+                                            (unsigned)ninst),
+                                       256, 0, L.stream>>>(d, r0);
       count_launch(1);
     }
   }

@@ -166,6 +166,78 @@ __device__ __forceinline__ void rem_point(double k, const double* u, const doubl
   o.H += (w * kInv4Pi * ir3) * (nn * E1 - c * E3);
 }
 
+// ---- FP32 remainders (near pairs of the mixed-precision assembly).  The Laplace parts
+// stay FP64; only the bounded remainders are summed in FP32, from source-to-target
+// offsets formed in FP64, so their relative error is that of the FP32 regular pairs.
+// The series branch is taken below z = 1, where the closed forms would lose up to a
+// factor 5 to cancellation; 7 even/odd pairs leave z^14/14! < 1.2e-11 at z = 1.
+constexpr float kSeriesZf = 1.0f;
+constexpr int kSeriesPairsF = 7;
+struct SeriesTabF {
+  float re[4][kSeriesPairsF];
+  float im[4][kSeriesPairsF];
+};
+__host__ __device__ constexpr SeriesTabF make_series_f() {
+  SeriesTabF t{};
+  const SeriesTab d = make_series();
+  for (int e = 0; e < 4; ++e)
+    for (int j = 0; j < kSeriesPairsF; ++j) {
+      t.re[e][j] = (float)d.re[e][j];
+      t.im[e][j] = (float)d.im[e][j];
+    }
+  return t;
+}
+static __constant__ SeriesTabF dSeriesF = make_series_f();
+
+__device__ __forceinline__ cf series_eval_f(int e, float z, float z2) {
+  float re = dSeriesF.re[e][kSeriesPairsF - 1], im = dSeriesF.im[e][kSeriesPairsF - 1];
+#pragma unroll
+  for (int j = kSeriesPairsF - 2; j >= 0; --j) {
+    re = fmaf(re, z2, dSeriesF.re[e][j]);
+    im = fmaf(im, z2, dSeriesF.im[e][j]);
+  }
+  return cf{re, im * z};
+}
+
+__device__ __forceinline__ void remainder_funcs_f(float z, cf& E0, cf& E1, cf& E2, cf& E3) {
+  if (z < kSeriesZf) {
+    const float z2 = z * z;
+    E0 = series_eval_f(0, z, z2);
+    E1 = series_eval_f(1, z, z2);
+    E2 = series_eval_f(2, z, z2);
+    E3 = series_eval_f(3, z, z2);
+  } else {
+    float sn, cs;
+    sincosf(z, &sn, &cs);
+    const cf e = {cs, sn};
+    E0 = cf{cs - 1.0f, sn};
+    E1 = e * cf{1.0f, -z} - cf{1.0f + 0.5f * z * z, 0.0f};
+    E2 = e * cf{-1.0f, z} + cf{1.0f, 0.0f};
+    E3 = e * cf{3.0f - z * z, -3.0f * z} - cf{3.0f, 0.0f};
+  }
+}
+
+struct OpsF {
+  cf S, D, K, H;
+};
+
+// w already carries 1/(4 pi).
+__device__ __forceinline__ void rem_point_f(float k, const float* u, const float* nx,
+                                            const float* ny, float w, OpsF& o) {
+  const float r2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+  const float r = sqrtf(r2), ir = 1.0f / r;
+  cf E0, E1, E2, E3;
+  remainder_funcs_f(k * r, E0, E1, E2, E3);
+  const float uny = u[0] * ny[0] + u[1] * ny[1] + u[2] * ny[2];
+  const float unx = u[0] * nx[0] + u[1] * nx[1] + u[2] * nx[2];
+  const float nn = nx[0] * ny[0] + nx[1] * ny[1] + nx[2] * ny[2];
+  const float ir3 = ir * ir * ir, c = unx * uny * ir * ir;
+  o.S += (w * ir) * E0;
+  o.D += (w * ir3 * uny) * E2;
+  o.K -= (w * ir3 * unx) * E2;
+  o.H += (w * ir3) * (nn * E1 - c * E3);
+}
+
 // Closed-form Laplace parts of a flat triangle (v: 9 doubles, nT: unit normal) at x
 // with target normal nx.  self: x is the triangle's own centroid (principal values).
 __device__ __forceinline__ void laplace_parts(const double* v, const double* nT,
@@ -269,6 +341,52 @@ __device__ __forceinline__ Ops near_ops(const double* v, const double* recj, con
   o.K += cd{K0, 0.0};
   o.H += cd{H0 + 0.5 * k * k * nn * S0, 0.0};
   return o;
+}
+
+// near_ops with the remainders in FP32 (same points and weights).
+__device__ __forceinline__ Ops near_ops_f(const double* v, const double* recj, const double* x,
+                                          const double* nx, bool self, double k, double S0,
+                                          double D0, double K0, double H0) {
+  OpsF o;
+  o.S = o.D = o.K = o.H = cf{0.0f, 0.0f};
+  const double* nT = recj + 3;
+  const float nxf[3] = {(float)nx[0], (float)nx[1], (float)nx[2]};
+  const float nTf[3] = {(float)nT[0], (float)nT[1], (float)nT[2]};
+  const float kf = (float)k;
+  const double area = recj[6];
+  if (self) {
+    const double* c = recj;
+    const float sa = (float)(area / 3.0 * kInv4Pi);
+#pragma unroll 1
+    for (int a = 0; a < 3; ++a) {
+      const double* Pa = v + 3 * a;
+      const double* Pb = v + 3 * ((a + 1) % 3);
+#pragma unroll 1
+      for (int q = 0; q < 7; ++q) {
+        float u[3];
+#pragma unroll
+        for (int t = 0; t < 3; ++t)
+          u[t] = (float)(dRuleB[q][0] * c[t] + dRuleB[q][1] * Pa[t] + dRuleB[q][2] * Pb[t] -
+                         x[t]);
+        rem_point_f(kf, u, nxf, nTf, (float)dRuleW[q] * sa, o);
+      }
+    }
+  } else {
+    const float sa = (float)(area * kInv4Pi);
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+      const float u[3] = {(float)(recj[8 + 3 * q] - x[0]), (float)(recj[9 + 3 * q] - x[1]),
+                          (float)(recj[10 + 3 * q] - x[2])};
+      rem_point_f(kf, u, nxf, nTf, (float)dRuleW[q] * sa, o);
+    }
+  }
+  const double nn = dot3(nx, nT);
+  Ops r;
+  r.S = cd{S0 + (double)o.S.x, (double)o.S.y};
+  r.D = cd{D0 + (double)o.D.x, (double)o.D.y};
+  r.K = cd{K0 + (double)o.K.x, (double)o.K.y};
+  r.H = cd{H0 + 0.5 * k * k * nn * S0 + (double)o.H.x, (double)o.H.y};
+  return r;
 }
 
 }  // namespace bemgpu

@@ -38,30 +38,54 @@ __device__ __forceinline__ void chunk_range(int64_t n, int ch, int nch, int64_t*
   *j1 = min(n, *j0 + w);
 }
 
+// Element access of the system: complex128, or complex64 for compact instances (a32).
+__device__ __forceinline__ float2 ldf(const void* base, int64_t idx) {
+  return reinterpret_cast<const float2*>(base)[idx];
+}
+template <bool A32>
+__device__ __forceinline__ float mag_at(const VecInst& V, int64_t idx) {
+  if (A32) {
+    const float2 a = ldf(V.A, idx);
+    return sqrtf(fmaf(a.x, a.x, a.y * a.y));
+  }
+  return fabs_c(ldc(V.A, idx));
+}
+
 // ---------------------------------------------------------------- equilibration
-__global__ void k_rowstats(const VecInst* __restrict__ insts) {
-  const VecInst& V = insts[blockIdx.z];
+template <bool A32>
+__device__ __forceinline__ void rowstats_body(const VecInst& V) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.n) return;
   int64_t j0, j1;
   chunk_range(V.n, blockIdx.y, kChunks, &j0, &j1);
   float mx = 0.f;
   double sm = 0.0;
-  float sm32 = 0.f;
-  int cnt = 0;
-  for (int64_t j = j0; j < j1; ++j) {
-    float a = fabs_c(ldc(V.A, i + j * V.lda));
-    mx = fmaxf(mx, a);
-    sm32 += a;
-    if (++cnt == 256) {  // fold into FP64 every 256 terms
-      sm += sm32;
-      sm32 = 0.f;
-      cnt = 0;
+  constexpr int kB = 16;
+  for (int64_t jf = j0; jf < j1; jf += 256) {  // fold into FP64 every 256 terms
+    float sm32 = 0.f;
+    const int64_t jf1 = min(j1, jf + 256);
+    for (int64_t jb = jf; jb < jf1; jb += kB) {
+      const int cnt = (int)min((int64_t)kB, jf1 - jb);
+      float a[kB];
+#pragma unroll
+      for (int q = 0; q < kB; ++q) a[q] = q < cnt ? mag_at<A32>(V, i + (jb + q) * V.lda) : 0.f;
+#pragma unroll
+      for (int q = 0; q < kB; ++q) {
+        mx = fmaxf(mx, a[q]);
+        sm32 += a[q];
+      }
     }
+    sm += sm32;
   }
-  sm += sm32;
   V.part[2 * (blockIdx.y * V.n + i)] = mx;
   V.part[2 * (blockIdx.y * V.n + i) + 1] = sm;
+}
+__global__ void k_rowstats(const VecInst* __restrict__ insts) {
+  const VecInst& V = insts[blockIdx.z];
+  if (V.a32)
+    rowstats_body<true>(V);
+  else
+    rowstats_body<false>(V);
 }
 
 __global__ void k_rowstats_finish(const VecInst* __restrict__ insts) {
@@ -79,47 +103,106 @@ __global__ void k_rowstats_finish(const VecInst* __restrict__ insts) {
 }
 
 // columns[j] = max_i |A_ij / rows_i|, one warp per column
-__global__ void k_colmax(const VecInst* __restrict__ insts) {
-  const VecInst& V = insts[blockIdx.y];
+template <bool A32>
+__device__ __forceinline__ void colmax_body(const VecInst& V) {
   const int64_t j = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (j >= V.n) return;
   float mx = 0.f;
-  for (int64_t i = lane; i < V.n; i += 32) {
-    cd a = ldc(V.A, i + j * V.lda);
-    mx = fmaxf(mx, fabs_c(a) * V.rows_inv[i]);
+  const int64_t n = V.n, base = j * V.lda;
+  int64_t i = lane;
+  for (; i + 96 < n; i += 128) {
+    float a[4], w[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      a[q] = mag_at<A32>(V, base + i + 32 * q);
+      w[q] = V.rows_inv[i + 32 * q];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) mx = fmaxf(mx, a[q] * w[q]);
   }
+  for (; i < n; i += 32) mx = fmaxf(mx, mag_at<A32>(V, base + i) * V.rows_inv[i]);
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
   if (lane == 0) V.cols[j] = (mx == 0.f) ? 1.0 : (double)mx;
+}
+__global__ void k_colmax(const VecInst* __restrict__ insts) {
+  const VecInst& V = insts[blockIdx.y];
+  if (V.a32)
+    colmax_body<true>(V);
+  else
+    colmax_body<false>(V);
 }
 
 __global__ void k_cols_inv(const VecInst* __restrict__ insts) {
   const VecInst& V = insts[blockIdx.y];
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j < V.n) V.cols_inv[j] = 1.0 / V.cols[j];
+  if (j < V.n) {
+    V.cols_inv[j] = 1.0 / V.cols[j];
+    if (V.cols_inv32) V.cols_inv32[j] = (float)V.cols_inv[j];
+    if (V.rows_inv) V.rows_inv[j] = (float)(1.0 / V.rows[j]);  // rows may have been reset
+  }
 }
 
-// out_ij = A_ij / rows_i / cols_j (complex64 or complex128); partial row sums of |out|
-__global__ void k_scale_copy(const VecInst* __restrict__ insts) {
-  const VecInst& V = insts[blockIdx.z];
+// out_ij = A_ij / rows_i / cols_j (complex64 or complex128); partial row sums of |out|.
+// The complex64 copy scales in FP32 by the FP32 reciprocals (a rounding-level change of
+// the scaling that the refinement, which uses the FP64 scales, absorbs).
+template <bool A32>
+__device__ __forceinline__ void scale_copy_body(const VecInst& V) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.n) return;
   int64_t j0, j1;
   chunk_range(V.n, blockIdx.y, kChunks, &j0, &j1);
-  const double ri = 1.0 / V.rows[i];
   double sm = 0.0;
+  float sm32 = 0.f;
+  int cnt = 0;
   bool bad = false;
-  for (int64_t j = j0; j < j1; ++j) {
-    cd a = ldc(V.A, i + j * V.lda);
-    const double sc = ri * V.cols_inv[j];
-    if (V.out_single) {
-      const float fs = (float)sc;
-      float2 f = make_float2((float)a.x * fs, (float)a.y * fs);
-      reinterpret_cast<float2*>(V.out)[i + j * V.n] = f;
-      bad |= !(isfinite(f.x) && isfinite(f.y));
-      sm += sqrtf(fmaf(f.x, f.x, f.y * f.y));
-    } else {
+  if (V.out_single) {
+    const float ri = V.rows_inv[i];
+    constexpr int kB = 8;
+    for (int64_t jb = j0; jb < j1; jb += kB) {
+      const int nb = (int)min((int64_t)kB, j1 - jb);
+      float2 a[kB];
+#pragma unroll
+      for (int q = 0; q < kB; ++q) {
+        if (q < nb) {
+          if (A32) {
+            a[q] = ldf(V.A, i + (jb + q) * V.lda);
+          } else {
+            const cd d = ldc(V.A, i + (jb + q) * V.lda);
+            a[q] = make_float2((float)d.x, (float)d.y);
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < kB; ++q) {
+        if (q < nb) {
+          const float fs = ri * V.cols_inv32[jb + q];
+          const float2 f = make_float2(a[q].x * fs, a[q].y * fs);
+          reinterpret_cast<float2*>(V.out)[i + (jb + q) * V.n] = f;
+          bad |= !(isfinite(f.x) && isfinite(f.y));
+          sm32 += sqrtf(fmaf(f.x, f.x, f.y * f.y));
+        }
+      }
+      cnt += nb;
+      if (cnt >= 256) {  // fold into FP64 every 256 terms
+        sm += sm32;
+        sm32 = 0.f;
+        cnt = 0;
+      }
+    }
+    sm += sm32;
+  } else {
+    const double ri = 1.0 / V.rows[i];
+    for (int64_t j = j0; j < j1; ++j) {
+      cd a;
+      if (A32) {
+        const float2 f = ldf(V.A, i + j * V.lda);
+        a = cd{(double)f.x, (double)f.y};
+      } else {
+        a = ldc(V.A, i + j * V.lda);
+      }
+      const double sc = ri * V.cols_inv[j];
       cd v = {a.x * sc, a.y * sc};
       stc(V.out, i + j * V.n, v);
       bad |= !(isfinite(v.x) && isfinite(v.y));
@@ -128,6 +211,13 @@ __global__ void k_scale_copy(const VecInst* __restrict__ insts) {
   }
   V.part[blockIdx.y * V.n + i] = sm;
   if (bad) atomicExch(V.flag, 1);
+}
+__global__ void k_scale_copy(const VecInst* __restrict__ insts) {
+  const VecInst& V = insts[blockIdx.z];
+  if (V.a32)
+    scale_copy_body<true>(V);
+  else
+    scale_copy_body<false>(V);
 }
 
 // stats[0] = max_i rowsum_i (||A||_inf), stats[1] = max_i sum_c part (||scaled||_inf)
@@ -157,11 +247,70 @@ __global__ void k_norms_finish(const VecInst* __restrict__ insts) {
   }
 }
 
-// ---------------------------------------------------------------- products
-// partial y = A x (and |A||x|) over a column chunk, up to kGemvR right-hand sides
-// per pass (rhs group = blockIdx.y / kChunks).
-__global__ void __launch_bounds__(256) k_gemv_part(const VecInst* __restrict__ insts, int with_abs) {
+// ---------------------------------------------------------------- compact storage helpers
+// out += near corrections (scaled unless unit); one thread per (near pair, block)
+__global__ void k_near_add(const VecInst* __restrict__ insts, int unit) {
   const VecInst& V = insts[blockIdx.z];
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (!V.a32 || p >= V.n_near || b >= V.nbc * V.nbc) return;
+  const int br = b / V.nbc, bc = b % V.nbc;
+  const int64_t row = br * V.n_mesh + V.near_i[p], col = bc * V.n_mesh + V.near_j[p];
+  const cd d = ldc(V.dnear, (int64_t)b * V.n_near + p);
+  const double sc = unit ? 1.0 : (1.0 / V.rows[row]) * V.cols_inv[col];
+  const int64_t o = row + col * V.n;
+  cd v = ldc(V.out, o);
+  stc(V.out, o, cd{v.x + d.x * sc, v.y + d.y * sc});
+}
+
+__global__ void k_expand_a32(const VecInst* __restrict__ insts) {
+  const VecInst& V = insts[blockIdx.z];
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!V.a32 || i >= V.n) return;
+  for (int64_t j = blockIdx.y; j < V.n; j += gridDim.y) {
+    const float2 f = ldf(V.A, i + j * V.lda);
+    stc(V.out, i + j * V.n, cd{(double)f.x, (double)f.y});
+  }
+}
+
+// x split for the compact products: hi = fl32(x), lo = fl32(x - hi)
+__global__ void k_split_x(const VecInst* __restrict__ insts) {
+  const VecInst& V = insts[blockIdx.z];
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y;
+  if (!V.a32 || i >= V.n || r >= V.nrhs) return;
+  const cd x = ldc(V.x, i + (int64_t)r * V.ldx);
+  const float hr = (float)x.x, hi = (float)x.y;
+  const float lr = (float)(x.x - (double)hr), li = (float)(x.y - (double)hi);
+  V.xs[i + (int64_t)r * V.n] = make_float4(hr, hi, lr, li);
+  V.xa[i + (int64_t)r * V.n] = sqrtf(fmaf(hr, hr, hi * hi));
+}
+
+// ---------------------------------------------------------------- products
+// Compact products in FP32 pair arithmetic.  A complex64 entry times the split x
+// (hi + lo): each product a * hi is exact as p + e (round-to-nearest product and its FMA
+// error), p enters a (s, t) pair by TwoSum (s + t carries the sum exactly up to the FP32
+// rounding of t), and e and a * lo go into t.  Every 16 columns the pair is folded into
+// FP64, so t never holds more than 16 terms' errors: the partial sums carry about 46
+// bits, the accuracy of the FP64 products of the complex128 path at a small fraction of
+// its FP64 instruction count.  The intrinsics keep the compiler from contracting or
+// reassociating the error-free steps.
+struct FPair {
+  float s, t;
+};
+__device__ __forceinline__ void pair_add_prod(FPair& a, float u, float v) {
+  const float p = __fmul_rn(u, v);
+  const float e = __fmaf_rn(u, v, -p);
+  const float s = __fadd_rn(a.s, p);
+  const float bb = __fsub_rn(s, a.s);
+  const float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  a.s = s;
+  a.t = __fadd_rn(a.t, __fadd_rn(err, e));
+}
+
+template <bool A32, int NR>
+__device__ __forceinline__ void gemv_body(const VecInst& V, int with_abs) {
+  constexpr int kGemvR = NR;  // right-hand sides per pass of this instantiation
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int ch = blockIdx.y % kChunks, grp = blockIdx.y / kChunks;
   const int r0 = grp * kGemvR;
@@ -176,29 +325,89 @@ __global__ void __launch_bounds__(256) k_gemv_part(const VecInst* __restrict__ i
     acc[r] = cd{0.0, 0.0};
     aacc[r] = 0.f;
   }
-  for (int64_t j = j0; j < j1; ++j) {
-    cd a = ldc(V.A, i + j * V.lda);
-    const float aa = with_abs ? fabs_c(a) : 0.f;
+  if (A32) {
+    // fold into FP64 every kFold columns; columns loaded kBatch at a time so each
+    // thread keeps kBatch independent requests in flight
+    constexpr int kFold = 32, kBatch = NR == 1 ? 16 : 8;
+    const float2* Acol = reinterpret_cast<const float2*>(V.A) + i;
+    const int64_t lda = V.lda, ldxs = V.n;
+    for (int64_t jf = j0; jf < j1; jf += kFold) {
+      FPair re[kGemvR], im[kGemvR];
 #pragma unroll
-    for (int r = 0; r < kGemvR; ++r) {
-      if (r < nr) {
-        cd x = ldc(V.x, j + (int64_t)(r0 + r) * V.ldx);
-        acc[r].x = fma(a.x, x.x, fma(-a.y, x.y, acc[r].x));
-        acc[r].y = fma(a.x, x.y, fma(a.y, x.x, acc[r].y));
-        if (with_abs) aacc[r] = fmaf(aa, fabs_c(x), aacc[r]);
+      for (int r = 0; r < kGemvR; ++r) re[r] = im[r] = FPair{0.f, 0.f};
+      const int64_t jf1 = min(j1, jf + kFold);
+      for (int64_t jb = jf; jb < jf1; jb += kBatch) {
+        const int cnt = (int)min((int64_t)kBatch, jf1 - jb);
+        float2 a[kBatch];
+#pragma unroll
+        for (int q = 0; q < kBatch; ++q)
+          a[q] = q < cnt ? Acol[(jb + q) * lda] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < kBatch; ++q) {
+          if (q < cnt) {
+            const float aa = with_abs ? sqrtf(fmaf(a[q].x, a[q].x, a[q].y * a[q].y)) : 0.f;
+#pragma unroll
+            for (int r = 0; r < kGemvR; ++r) {
+              if (r < nr) {
+                const int64_t xo = jb + q + (int64_t)(r0 + r) * ldxs;
+                const float4 x = V.xs[xo];
+                // re += a.x x.re - a.y x.im ; im += a.x x.im + a.y x.re
+                pair_add_prod(re[r], a[q].x, x.x);
+                pair_add_prod(re[r], -a[q].y, x.y);
+                pair_add_prod(im[r], a[q].x, x.y);
+                pair_add_prod(im[r], a[q].y, x.x);
+                re[r].t = __fmaf_rn(a[q].x, x.z, __fmaf_rn(-a[q].y, x.w, re[r].t));
+                im[r].t = __fmaf_rn(a[q].x, x.w, __fmaf_rn(a[q].y, x.z, im[r].t));
+                if (with_abs) aacc[r] = fmaf(aa, V.xa[xo], aacc[r]);
+              }
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kGemvR; ++r) {
+        acc[r].x += (double)re[r].s + (double)re[r].t;
+        acc[r].y += (double)im[r].s + (double)im[r].t;
+      }
+    }
+  } else {
+    for (int64_t j = j0; j < j1; ++j) {
+      cd a = ldc(V.A, i + j * V.lda);
+      const float aa = with_abs ? fabs_c(a) : 0.f;
+#pragma unroll
+      for (int r = 0; r < kGemvR; ++r) {
+        if (r < nr) {
+          cd x = ldc(V.x, j + (int64_t)(r0 + r) * V.ldx);
+          acc[r].x = fma(a.x, x.x, fma(-a.y, x.y, acc[r].x));
+          acc[r].y = fma(a.x, x.y, fma(a.y, x.x, acc[r].y));
+          if (with_abs) aacc[r] = fmaf(aa, fabs_c(x), aacc[r]);
+        }
       }
     }
   }
   // part layout: [chunk][rhs][row] x (re, im, abs)
-  for (int r = 0; r < nr; ++r) {
-    int64_t o = 3 * (((int64_t)ch * V.nrhs + r0 + r) * V.n + i);
-    V.part[o] = acc[r].x;
-    V.part[o + 1] = acc[r].y;
-    V.part[o + 2] = (double)aacc[r];
+#pragma unroll
+  for (int r = 0; r < kGemvR; ++r) {
+    if (r < nr) {
+      int64_t o = 3 * (((int64_t)ch * V.nrhs + r0 + r) * V.n + i);
+      V.part[o] = acc[r].x;
+      V.part[o + 1] = acc[r].y;
+      V.part[o + 2] = (double)aacc[r];
+    }
   }
 }
 
-// mode 0: y = A x.  mode 1: y = b - A x, den = |b| + |A||x|.
+// partial y = A x (and |A||x|) over a column chunk, up to kGemvR right-hand sides
+// per pass (rhs group = blockIdx.y / kChunks).
+template <bool A32, int NR>
+__global__ void __launch_bounds__(256) k_gemv_part(const VecInst* __restrict__ insts, int with_abs) {
+  const VecInst& V = insts[blockIdx.z];
+  if ((V.a32 != 0) != A32) return;
+  gemv_body<A32, NR>(V, with_abs);
+}
+
+// mode 0: y = A x.  mode 1: y = b - A x, den = |b| + |A||x|.  Compact instances add the
+// near corrections of the row (FP64, fixed CSR order).
 __global__ void k_gemv_finish(const VecInst* __restrict__ insts, int mode) {
   const VecInst& V = insts[blockIdx.z];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -210,6 +419,19 @@ __global__ void k_gemv_finish(const VecInst* __restrict__ insts, int mode) {
     re += V.part[o];
     im += V.part[o + 1];
     ab += V.part[o + 2];
+  }
+  if (V.a32) {
+    const int br = i >= V.n_mesh ? 1 : 0;
+    const int64_t im_ = i - br * V.n_mesh;
+    for (int32_t p = V.near_ptr[im_]; p < V.near_ptr[im_ + 1]; ++p) {
+      const int64_t j = V.near_j[p];
+      for (int bc = 0; bc < V.nbc; ++bc) {
+        const cd d = ldc(V.dnear, (int64_t)(br * V.nbc + bc) * V.n_near + p);
+        const cd x = ldc(V.x, j + bc * V.n_mesh + (int64_t)r * V.ldx);
+        re = fma(d.x, x.x, fma(-d.y, x.y, re));
+        im = fma(d.x, x.y, fma(d.y, x.x, im));
+      }
+    }
   }
   const int64_t yo = i + (int64_t)r * V.ldy;
   if (mode == 0) {
@@ -370,11 +592,37 @@ void launch_scale_copy(const Launch& L, const VecInst* d, int ninst, int64_t nma
 
 void launch_gemv(const Launch& L, const VecInst* d, int ninst, int64_t nmax, int32_t max_rhs,
                  int mode) {
-  const int groups = (max_rhs + kGemvR - 1) / kGemvR;
+  // compact and complex128 instances by their own instantiations (each skips the others);
+  // one right-hand side gets a single-rhs instantiation
+  const int nr = max_rhs == 1 ? 1 : kGemvR;
+  const int groups = (max_rhs + nr - 1) / nr;
+  dim3 g0((unsigned)((nmax + 255) / 256), (unsigned)max_rhs, (unsigned)ninst);
+  k_split_x<<<g0, 256, 0, L.stream>>>(d); count_launch(1);
   dim3 g1((unsigned)((nmax + 255) / 256), (unsigned)(kChunks * groups), (unsigned)ninst);
-  k_gemv_part<<<g1, 256, 0, L.stream>>>(d, mode == 1); count_launch(1);
+  if (nr == 1) {
+    k_gemv_part<true, 1><<<g1, 256, 0, L.stream>>>(d, mode == 1);
+    k_gemv_part<false, 1><<<g1, 256, 0, L.stream>>>(d, mode == 1);
+  } else {
+    k_gemv_part<true, kGemvR><<<g1, 256, 0, L.stream>>>(d, mode == 1);
+    k_gemv_part<false, kGemvR><<<g1, 256, 0, L.stream>>>(d, mode == 1);
+  }
+  count_launch(2);
   dim3 g2((unsigned)((nmax + 255) / 256), (unsigned)max_rhs, (unsigned)ninst);
   k_gemv_finish<<<g2, 256, 0, L.stream>>>(d, mode); count_launch(1);
+}
+
+void launch_near_add(const Launch& L, const VecInst* d, int ninst, int64_t max_near,
+                     int unit_scales) {
+  if (max_near <= 0 || ninst <= 0) return;
+  k_near_add<<<dim3((unsigned)((max_near + 255) / 256), 4, (unsigned)ninst), 256, 0, L.stream>>>(
+      d, unit_scales);
+  count_launch(1);
+}
+
+void launch_expand_a32(const Launch& L, const VecInst* d, int ninst, int64_t nmax) {
+  if (nmax <= 0 || ninst <= 0) return;
+  k_expand_a32<<<dim3((unsigned)((nmax + 255) / 256), 256, (unsigned)ninst), 256, 0, L.stream>>>(d);
+  count_launch(1);
 }
 
 void launch_resid_stats(const Launch& L, const VecInst* d, int ninst, int32_t max_rhs) {

@@ -33,6 +33,19 @@ struct VecInst {
   double* stats;     // kStats doubles per right-hand side
   int32_t* active;   // per rhs: still refining (null = all)
   int32_t* changed;  // per rhs: last correction changed x
+  // Compact system storage (mixed precision with FP32 regular pairs): A is complex64,
+  // exact for every regular pair, and the near pairs carry an FP64 correction
+  // dnear = a64 - (complex128)(complex64)a64, so A64 = A + the sparse corrections.
+  int32_t a32;
+  int32_t nbc;               // block columns of the near pattern: 1 (n x n) or 2 (2n x 2n)
+  int64_t n_mesh, n_near;
+  const int32_t* near_ptr;   // CSR row pointers over the mesh's near pairs (n_mesh + 1)
+  const int32_t* near_i;
+  const int32_t* near_j;
+  const double* dnear;       // corrections, complex128 [block][n_near], block = nbc br + bc
+  float4* xs;                // x split as FP32 (hi.re, hi.im, lo.re, lo.im), n x nrhs
+  float* xa;                 // |x| in FP32, n x nrhs
+  float* cols_inv32;         // 1 / cols in FP32 (n)
 };
 
 #ifdef __CUDACC__
@@ -41,6 +54,12 @@ void launch_scale_copy(const Launch& L, const VecInst* d, int ninst, int64_t nma
 // mode 0: y = A x; mode 1: y = b - A x and den = |b| + |A||x|
 void launch_gemv(const Launch& L, const VecInst* d, int ninst, int64_t nmax, int32_t max_rhs,
                  int mode);
+// compact instances: out (complex128, ld n) += the near corrections, each scaled by
+// 1 / (rows_i cols_j) (unit_scales = 0) or unscaled (unit_scales = 1)
+void launch_near_add(const Launch& L, const VecInst* d, int ninst, int64_t max_near,
+                     int unit_scales);
+// compact instances: out (complex128, ld n) = complex128(A)
+void launch_expand_a32(const Launch& L, const VecInst* d, int ninst, int64_t nmax);
 void launch_resid_stats(const Launch& L, const VecInst* d, int ninst, int32_t max_rhs);
 void launch_corr_prep(const Launch& L, const VecInst* d, int ninst, int64_t nmax,
                       int32_t max_rhs);
