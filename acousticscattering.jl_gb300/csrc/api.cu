@@ -845,6 +845,27 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
       if (m > 0) tiles1[(size_t)st] += (m + 127) / 128;
     }
   }
+  // tensor maps of the factors for the reduction epilogue (all instances or none)
+  Buf dmaps;
+  bool red = true;
+  {
+    std::vector<uint8_t> maps((size_t)ni * kTcMapBytes + 64);
+    uint8_t* hm = reinterpret_cast<uint8_t*>(
+        (reinterpret_cast<uintptr_t>(maps.data()) + 63) & ~uintptr_t(63));
+    for (int t = 0; t < ni && red; ++t)
+      red = tc_encode_cmap(hm + (size_t)t * kTcMapBytes, mi[t].a, mi[t].lda, mi[t].n, mi[t].n);
+    if (red) {
+      TRY(alloc(c, (size_t)ni * kTcMapBytes, &dmaps));
+      CUDA_TRY(c, cudaMemcpyAsync(dmaps.p, hm, (size_t)ni * kTcMapBytes, cudaMemcpyHostToDevice,
+                                  c->stream));
+      for (int64_t st = 0; st < steps; ++st)
+        for (int t = 0; t < ni; ++t) {
+          const void* mp = dmaps.as<uint8_t>() + (size_t)t * kTcMapBytes;
+          gems[(size_t)(st * ni + t)].cmap = mp;
+          gems1[(size_t)(st * ni + t)].cmap = mp;
+        }
+    }
+  }
   Buf dpack, dgem, dpack1, dgem1;
   TRY(to_device(c, packs, &dpack));
   TRY(to_device(c, gems, &dgem));
@@ -881,7 +902,7 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
       Prof pr(c, "trsm");
       launch_linv_neg(L, dm, ni, K0, d_negn.as<float2* const>());
       launch_tc_pack(L, dpack1.as<TcPackInst>() + st * 2 * ni, 2 * ni, max_rows, NB);
-      launch_tc_cgemm(L, dgem1.as<TcGemmInst>() + st * ni, ni, tiles1[(size_t)st]);
+      launch_tc_cgemm(L, dgem1.as<TcGemmInst>() + st * ni, ni, tiles1[(size_t)st], red);
     }
     max_rows = 0;
     for (int t = 0; t < ni; ++t) max_rows = std::max(max_rows, mi[t].n - K0 - NB);
@@ -891,7 +912,7 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
     }
     {
       Prof pr(c, "gemm_tc");
-      launch_tc_cgemm(L, dgem.as<TcGemmInst>() + st * ni, ni, tiles[(size_t)st]);
+      launch_tc_cgemm(L, dgem.as<TcGemmInst>() + st * ni, ni, tiles[(size_t)st], red);
     }
   }
   CUDA_TRY(c, cudaGetLastError());
@@ -2772,13 +2793,22 @@ int bemgpu_debug_cgemm(bemgpu_ctx* c, int64_t m, int64_t n, int32_t k, const flo
   g[0].n = n;
   g[0].kk = k;
   g[0].active = 1;
+  // even m: the reduction epilogue (as in the LU); odd m: the load / store epilogue
+  alignas(64) uint8_t hmap[kTcMapBytes];
+  Buf dmap;
+  const bool red = tc_encode_cmap(hmap, dC.p, m, m, n);
+  if (red) {
+    TRY(alloc(c, kTcMapBytes, &dmap));
+    CUDA_TRY(c, cudaMemcpyAsync(dmap.p, hmap, kTcMapBytes, cudaMemcpyHostToDevice, c->stream));
+    g[0].cmap = dmap.p;
+  }
   TRY(to_device(c, pk, &dpi));
   TRY(to_device(c, g, &dgi));
   const Launch L = c->launch();
   launch_tc_pack(L, dpi.as<TcPackInst>(), 2, std::max(m, n), k);
   {
     Prof pr(c, "gemm_tc");
-    launch_tc_cgemm(L, dgi.as<TcGemmInst>(), 1, ((m + 127) / 128) * ((n + 127) / 128));
+    launch_tc_cgemm(L, dgi.as<TcGemmInst>(), 1, ((m + 127) / 128) * ((n + 127) / 128), red);
   }
   CUDA_TRY(c, cudaGetLastError());
   CUDA_TRY(c, cudaMemcpyAsync(C, dC.p, (size_t)m * n * 8, cudaMemcpyDeviceToHost, c->stream));

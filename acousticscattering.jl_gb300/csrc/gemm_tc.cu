@@ -15,16 +15,21 @@
 // descriptors read.  The GEMM kernel then moves each block with a single bulk
 // asynchronous copy (TMA engine) - no tensor map, no coordinate arithmetic.
 //
-// Kernel: persistent, one CTA per SM, 6 warps, warp-specialised:
+// Kernel: persistent, one CTA per SM, 10 warps, warp-specialised:
 //   warp 0      producer: 4 bulk copies (64 KB) per stage, 3-stage ring;
 //   warp 1      TMEM allocation (512 columns) and the single-thread MMA issuer;
-//   warps 2..5  epilogue: tcgen05.ld of the FP32 accumulators (thread = tile row),
-//               complex64 read-modify-write of C with coalesced column accesses.
+//   warps 2..9  epilogue: tcgen05.ld of the FP32 accumulators (thread = tile row).
+//               With a tensor map of C, -acc is staged in shared memory 16 columns at
+//               a time (two 16 KB buffers) and added into C by bulk tensor reductions
+//               (cp.reduce.async.bulk.tensor .add.f32, performed at L2), so the SMs
+//               never wait on C; without one, C is read, updated and written back.
 // Two accumulator buffers (Cr | Ci, 128 + 128 columns each) let the epilogue of one
 // tile overlap the MMAs of the next.  Every mbarrier wait is bounded: a timeout
 // records BEMGPU_ETIMEOUT, stops all roles, drains the copies in flight and frees TMEM.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <cstdint>
 #include <cstdio>
@@ -44,6 +49,9 @@ constexpr int kTcStageBytes = 4 * kTcBlock;  // Ar, Ai, Br, Bi
 constexpr int kTcThreads = 320;   // producer, MMA, 8 epilogue warps
 constexpr int kTcEpiThreads = 256;
 constexpr uint32_t kTmemCols = 512;
+constexpr int kTcRedCols = 16;                      // columns per reduction chunk
+constexpr int kTcRedBytes = kTcRedCols * kTcM * 8;  // 16 KB staging buffer
+constexpr int kTcNamedBar = 1;                      // epilogue-only barrier id
 
 // ------------------------------------------------------------------ descriptors
 // UMMA shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
@@ -197,8 +205,43 @@ struct TcShared {
   uint32_t tmem_base;
   int abort_flag;
   int ninst;
-  int64_t prefix[kTcMaxInst + 1];
+  int epi_go;
+  int32_t prefix[kTcMaxInst + 1];
 };
+
+__device__ __forceinline__ void epi_bar() {
+  asm volatile("bar.sync %0, %1;" ::"n"(kTcNamedBar), "n"(kTcEpiThreads) : "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void red_add_tile(const void* map, int32_t x, int32_t y, uint32_t src) {
+  asm volatile(
+      "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2}], "
+      "[%3];" ::"l"(map),
+      "r"(x), "r"(y), "r"(src)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_read1() {
+  asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+// 32 lanes x 8 consecutive 32-bit TMEM columns
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
 
 __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, int* err,
                                         volatile int* abort_flag) {
@@ -223,7 +266,7 @@ __device__ __forceinline__ void tile_coords(const TcShared& S, const TcGemmInst*
     else
       hi = mid - 1;
   }
-  const int64_t local = t - S.prefix[lo];
+  const int64_t local = t - (int64_t)S.prefix[lo];
   const int64_t mtiles = (insts[lo].m + kTcM - 1) / kTcM;
   *inst = lo;
   *mt = local % mtiles;
@@ -231,12 +274,13 @@ __device__ __forceinline__ void tile_coords(const TcShared& S, const TcGemmInst*
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_tc_cgemm(const TcGemmInst* __restrict__ insts, int ninst, int* err) {
+    k_tc_cgemm(const TcGemmInst* __restrict__ insts, int ninst, int* err, int red) {
   extern __shared__ uint8_t smem_raw[];
   // 1024-byte aligned stage buffers (swizzle atoms), barriers after them
   uint8_t* base = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  TcShared& S = *reinterpret_cast<TcShared*>(base + kTcStages * kTcStageBytes);
+  uint8_t* red_smem = base + kTcStages * kTcStageBytes;  // 2 reduction staging buffers
+  TcShared& S = *reinterpret_cast<TcShared*>(red_smem + 2 * kTcRedBytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
@@ -250,14 +294,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     S.abort_flag = 0;
     S.ninst = ninst;
-    int64_t acc = 0;
+    int32_t acc = 0;
     S.prefix[0] = 0;
     for (int i = 0; i < ninst; ++i) {
       const TcGemmInst& G = insts[i];
       const int64_t t = (G.active && G.m > 0 && G.n > 0 && G.kk > 0)
                             ? ((G.m + kTcM - 1) / kTcM) * ((G.n + kTcN - 1) / kTcN)
                             : 0;
-      acc += t;
+      acc += (int32_t)t;
       S.prefix[i + 1] = acc;
     }
     mbar_fence_init();
@@ -387,9 +431,60 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int quad = warp & 3;
     const int half = (warp - 2) >> 2;
     const int row = quad * 32 + lane;
+    const bool leader = threadIdx.x == 64;  // warp 2, lane 0: issues the reductions
     int buf = 0;
     uint32_t bphase = 0;
-    for (int64_t t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x) {
+    if (red) {
+      // ---- reduction epilogue: C += (-acc) through the TMA unit.  Every control
+      // decision is taken by the leader and published through shared memory behind the
+      // epilogue barrier, so the eight warps always pass the same barriers.
+      int rchunk = 0;  // reduction chunks issued (selects the staging buffer)
+      for (int64_t t = blockIdx.x; t < total; t += gridDim.x) {
+        if (leader) S.epi_go = (!*abort_flag && tc_wait(&S.tfull[buf], bphase, err, abort_flag)) ? 1 : 0;
+        epi_bar();
+        if (!S.epi_go) break;
+        tc_fence_after();
+        int inst;
+        int64_t mt, nt;
+        tile_coords(S, insts, t, &inst, &mt, &nt);
+        const TcGemmInst& G = insts[inst];
+        const uint32_t tl = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * 256);
+        const int32_t x0 = (int32_t)(2 * (G.c_r0 + mt * kTcM));
+        const int64_t ncols = G.n - nt * kTcN;
+        const int nchunks =
+            (int)min((int64_t)(kTcN / kTcRedCols), (ncols + kTcRedCols - 1) / kTcRedCols);
+#pragma unroll 1
+        for (int cc = 0; cc < nchunks; ++cc, ++rchunk) {
+          uint8_t* sb = red_smem + (rchunk & 1) * kTcRedBytes;
+          if (leader) bulk_wait_read1();  // the reduction that used this buffer has read it
+          epi_bar();
+          const int j0 = cc * kTcRedCols + half * 8;
+          float vr[8], vi[8];
+          tmem_ld8(tl + (uint32_t)j0, vr);
+          tmem_ld8(tl + 128u + (uint32_t)j0, vi);
+          tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            *reinterpret_cast<float2*>(sb + ((half * 8 + j) * kTcM + row) * 8) =
+                make_float2(-vr[j], -vi[j]);
+          fence_async_smem();
+          epi_bar();
+          if (leader) {
+            red_add_tile(G.cmap, x0, (int32_t)(G.c_c0 + nt * kTcN + cc * kTcRedCols),
+                         smem_addr(sb));
+            bulk_commit();
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(&S.tempty[buf]);
+        if (++buf == 2) {
+          buf = 0;
+          bphase ^= 1;
+        }
+      }
+      if (leader) bulk_wait_all();  // every reduction performed before the CTA exits
+    }
+    for (int64_t t = blockIdx.x; !red && t < total && !*abort_flag; t += gridDim.x) {
       int inst;
       int64_t mt, nt;
       tile_coords(S, insts, t, &inst, &mt, &nt);
@@ -474,9 +569,36 @@ void launch_tc_pack(const Launch& L, const TcPackInst* d, int ninst, int64_t max
 
 static int g_sms = 0;
 
-void launch_tc_cgemm(const Launch& L, const TcGemmInst* d, int ninst, int64_t total_tiles) {
+bool tc_encode_cmap(void* map, const void* c, int64_t ldc, int64_t rows, int64_t cols) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    looked = true;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  if (!encode || (ldc & 1) || rows <= 0 || cols <= 0 ||
+      (reinterpret_cast<uintptr_t>(c) & 15) != 0)
+    return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)(2 * rows), (cuuint64_t)cols};
+  const cuuint64_t strides[1] = {(cuuint64_t)ldc * 8};
+  const cuuint32_t box[2] = {2 * kTcM, kTcRedCols};
+  const cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode(reinterpret_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                      const_cast<void*>(c), dims, strides, box, estr,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+void launch_tc_cgemm(const Launch& L, const TcGemmInst* d, int ninst, int64_t total_tiles,
+                     bool red) {
   if (ninst <= 0 || total_tiles <= 0) return;
-  const size_t smem = 1024 + kTcStages * kTcStageBytes + sizeof(TcShared);
+  const size_t smem = 1024 + kTcStages * kTcStageBytes + 2 * kTcRedBytes + sizeof(TcShared);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_tc_cgemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -486,7 +608,7 @@ void launch_tc_cgemm(const Launch& L, const TcGemmInst* d, int ninst, int64_t to
     attr = true;
   }
   const int64_t grid = total_tiles < g_sms ? total_tiles : g_sms;
-  k_tc_cgemm<<<(unsigned)grid, kTcThreads, smem, L.stream>>>(d, ninst, L.err_flag);
+  k_tc_cgemm<<<(unsigned)grid, kTcThreads, smem, L.stream>>>(d, ninst, L.err_flag, red ? 1 : 0);
   count_launch(1);
 }
 

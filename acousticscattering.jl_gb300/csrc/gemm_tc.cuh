@@ -31,13 +31,26 @@ struct TcGemmInst {
   int64_t m, n;
   int32_t kk;
   int32_t active;
+  // Tensor map (device address, 64-byte aligned) of C viewed as FP32 pairs, used by
+  // the reduction epilogue (launch_tc_cgemm with red = true; c_r0 must be even): -A B
+  // is added into C by asynchronous bulk tensor reductions instead of reading C.
+  const void* cmap;
 };
 
+constexpr size_t kTcMapBytes = 128;  // sizeof(CUtensorMap)
+
 size_t tc_pack_bytes(int64_t rows, int kk);
+// Encodes into map (kTcMapBytes, host memory) the tensor map of a column-major complex64
+// matrix c with `rows` x `cols` addressable entries and leading dimension ldc, as used
+// by the reduction epilogue.  False when the layout does not allow it (odd ldc,
+// misaligned base) or the driver entry point is unavailable.
+bool tc_encode_cmap(void* map, const void* c, int64_t ldc, int64_t rows, int64_t cols);
 
 #ifdef __CUDACC__
 void launch_tc_pack(const Launch& L, const TcPackInst* d, int ninst, int64_t max_rows, int max_kk);
-void launch_tc_cgemm(const Launch& L, const TcGemmInst* d, int ninst, int64_t total_tiles);
+// red: every instance carries cmap (reduction epilogue); otherwise C is read and written
+void launch_tc_cgemm(const Launch& L, const TcGemmInst* d, int ninst, int64_t total_tiles,
+                     bool red = false);
 #endif
 
 }  // namespace bemgpu
