@@ -61,6 +61,8 @@ struct bemgpu_ctx {
   bool tensor_lu = true;  // complex64 trailing updates on the tensor cores
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
+  float* pinned = nullptr;  // page-locked staging of host <-> device vector exchanges
+  size_t pinned_bytes = 0;
   std::recursive_mutex mu;
   Launch launch() const { return Launch{stream, d_err}; }
 };
@@ -675,49 +677,68 @@ struct Lacn2 {
 
 // Infinity-norm reciprocal condition of the complex64 factors (LAPACK cgecon('I'):
 // kase 2 applies (LU)^{-1}, kase 1 applies (LU)^{-H}; rcond = 1 / (anorm ||A^-1||)).
+// Page-locked host staging of at least `bytes`, kept by the context.
+float* pinned_buffer(bemgpu_ctx* c, size_t bytes) {
+  if (c->pinned_bytes >= bytes) return c->pinned;
+  if (c->pinned) cudaFreeHost(c->pinned);
+  c->pinned = nullptr;
+  c->pinned_bytes = 0;
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+  c->pinned = static_cast<float*>(p);
+  c->pinned_bytes = bytes;
+  return c->pinned;
+}
+
+// LAPACK's 1-norm estimate (zlacn2 reverse communication) for every factor of the batch:
+// each round packs the vectors of all instances that ask for the same product into one
+// page-locked buffer, runs one batched triangular solve and reads them back with one copy.
 int estimate_rcond(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
   if (fs.empty()) return BEMGPU_OK;
   const Launch L = c->launch();
   const size_t F = fs.size();
   std::vector<Lacn2> st(F);
-  std::vector<Buf> work(F), work2(F);
   std::vector<std::vector<std::complex<double>>> xs(F);
+  std::vector<size_t> off(F + 1, 0);
   int64_t nmax = 0;
   for (size_t t = 0; t < F; ++t) {
     st[t].n = (int)fs[t]->N;
     xs[t].assign((size_t)fs[t]->N, 0.0);
-    TRY(alloc(c, (size_t)fs[t]->N * 8, &work[t]));
-    TRY(alloc(c, (size_t)fs[t]->N * 8, &work2[t]));
+    off[t + 1] = off[t] + (size_t)fs[t]->N;
     nmax = std::max(nmax, fs[t]->N);
   }
+  Buf work, work2;
+  TRY(alloc(c, off[F] * 8, &work));
+  TRY(alloc(c, off[F] * 8, &work2));
+  float* host = pinned_buffer(c, off[F] * 8);
+  if (!host) return fail(c, BEMGPU_ECUDA, "page-locked staging allocation failed");
   TrsvWork tw{1};
   std::vector<int> kase(F);
   for (size_t t = 0; t < F; ++t) kase[t] = st[t].step(xs[t]);
   Buf d_mi;
-  std::vector<float> tmp;
   for (int round = 0; round < 64; ++round) {
     bool any = false;
     for (int want : {1, 2}) {
       std::vector<MatInst> mi;
       std::vector<size_t> who;
+      size_t lo = off[F], hi = 0;
       for (size_t t = 0; t < F; ++t) {
         if (kase[t] != want) continue;
-        tmp.resize(2 * xs[t].size());
+        float* h = host + 2 * off[t];
         for (size_t i = 0; i < xs[t].size(); ++i) {
-          tmp[2 * i] = (float)xs[t][i].real();
-          tmp[2 * i + 1] = (float)xs[t][i].imag();
+          h[2 * i] = (float)xs[t][i].real();
+          h[2 * i + 1] = (float)xs[t][i].imag();
         }
-        CUDA_TRY(c, cudaMemcpyAsync(work[t].p, tmp.data(), tmp.size() * 4, cudaMemcpyHostToDevice,
-                                    c->stream));
-        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        lo = std::min(lo, off[t]);
+        hi = std::max(hi, off[t + 1]);
         MatInst m{};
         m.a = fs[t]->LU.p;
         m.n = fs[t]->N;
         m.lda = fs[t]->N;
         m.ipiv = fs[t]->ipiv.as<int32_t>();
         m.info = fs[t]->info.as<int32_t>();
-        m.x = work[t].p;
-        m.y = work2[t].p;
+        m.x = work.as<float2>() + off[t];
+        m.y = work2.as<float2>() + off[t];
         m.ldx = fs[t]->N;
         m.nrhs = 1;
         m.active = 1;
@@ -726,19 +747,21 @@ int estimate_rcond(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
       }
       if (mi.empty()) continue;
       any = true;
+      CUDA_TRY(c, cudaMemcpyAsync(work.as<float2>() + lo, host + 2 * lo, (hi - lo) * 8,
+                                  cudaMemcpyHostToDevice, c->stream));
       TRY(to_device(c, mi, &d_mi));
       {
         Prof pr(c, "getrs");
         launch_getrs(L, d_mi.as<MatInst>(), (int)mi.size(), nmax, 1, want == 1 ? 1 : 0, 1, 0,
                      &tw);
       }
+      CUDA_TRY(c, cudaMemcpyAsync(host + 2 * lo, work.as<float2>() + lo, (hi - lo) * 8,
+                                  cudaMemcpyDeviceToHost, c->stream));
+      CUDA_TRY(c, cudaStreamSynchronize(c->stream));
       for (size_t w : who) {
-        tmp.resize(2 * xs[w].size());
-        CUDA_TRY(c, cudaMemcpyAsync(tmp.data(), work[w].p, tmp.size() * 4, cudaMemcpyDeviceToHost,
-                                    c->stream));
-        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        const float* h = host + 2 * off[w];
         for (size_t i = 0; i < xs[w].size(); ++i)
-          xs[w][i] = std::complex<double>(tmp[2 * i], tmp[2 * i + 1]);
+          xs[w][i] = std::complex<double>(h[2 * i], h[2 * i + 1]);
         kase[w] = st[w].step(xs[w]);
       }
     }
@@ -2071,6 +2094,7 @@ int bemgpu_ctx_destroy(bemgpu_ctx* c) {
       cudaEventDestroy(pr.second);
     }
   drop_cache(c);
+  if (c->pinned) cudaFreeHost(c->pinned);
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
   cudaFree(c->d_err);

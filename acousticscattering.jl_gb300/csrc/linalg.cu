@@ -602,7 +602,7 @@ void launch_linv_neg(const Launch& L, const MatInst* d, int ninst, int64_t k0, f
 // the current one from shared memory with shuffles), then all warps update the rest of
 // the block.  op(A) = A^H reads A along its columns in both phases (a warp per row,
 // lanes along the column), so every global access is coalesced.
-constexpr int kBigB = 1024;
+constexpr int kBigB = 512;
 constexpr int kDiagThreads = 512;
 constexpr int kTilePad = 33;
 
