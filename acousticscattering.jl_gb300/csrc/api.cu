@@ -774,103 +774,49 @@ int estimate_rcond(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
   return BEMGPU_OK;
 }
 
-// Complex64 LU with 128-column outer panels: the panel is factored by the SIMT kernels
-// in 32-column steps, the trailing matrix is updated on the tensor cores (split-BF16
-// tcgen05 GEMM, gemm_tc.cu) from packed operand images of L21 and U12.
+// Complex64 LU with 256-column outer steps made of two 128-column halves.  Each half is
+// factored by the SIMT panel kernels in 32-column steps; the left half's update of the
+// right half, the 256-row U12 solve (through -(L11^{-1} - I) products) and the trailing
+// update are tcgen05 split-BF16 GEMMs (gemm_tc.cu) on packed operand images.  The
+// trailing update runs once per 256 columns with K = 256, so the matrix streams through
+// HBM half as often as with 128-column steps.
+//
+// Per outer step (K0, halves H0 = K0 and H1 = K0 + 128, kk0 / kk1 their widths):
+//   factor half 0 (columns [H0, H0 + kk0))
+//   half-0 interchanges on the right half; P1: U12r = L11a^{-1} A[H0.., H1..H1 + kk1)
+//   P2: A[H1.., H1..H1 + kk1) -= L21a U12r
+//   factor half 1; interchanges of both halves on the columns outside [K0, K0 + 256)
+//   P3: U12top = L11a^{-1} A12top            P4: A12bot -= Lmid U12top
+//   P5: U12bot = L11b^{-1} A12bot            P6: A22 -= L21 U12 (K = kk0 + kk1)
 int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatInst>& mi,
              Buf& d, int64_t nmax) {
   const Launch L = c->launch();
   const MatInst* dm = d.as<MatInst>();
   const int ni = (int)fs.size();
-  const int NB = kTcPanel;
-  // packed operand buffers per instance (sized for the first step, the largest)
-  std::vector<Buf> apack(fs.size()), bpack(fs.size());
-  for (size_t t = 0; t < fs.size(); ++t) {
-    const size_t bytes = tc_pack_bytes(fs[t]->N, NB);
+  constexpr int HB = kTcPanel;       // half width (128)
+  constexpr int SB = 2 * kTcPanel;   // outer step (256)
+  std::vector<Buf> apack(ni), bpack(ni), mpack(ni);
+  std::vector<Buf> negn0(ni), negn1(ni), npack0(ni), npack1(ni);
+  std::vector<float2*> p0(ni), p1(ni);
+  for (int t = 0; t < ni; ++t) {
+    const size_t bytes = tc_pack_bytes(fs[t]->N, SB);
     TRY(alloc(c, bytes, &apack[t]));
     TRY(alloc(c, bytes, &bpack[t]));
+    TRY(alloc(c, tc_pack_bytes(HB, HB), &mpack[t]));
+    TRY(alloc(c, (size_t)HB * HB * 8, &negn0[t]));
+    TRY(alloc(c, (size_t)HB * HB * 8, &negn1[t]));
+    TRY(alloc(c, tc_pack_bytes(HB, HB), &npack0[t]));
+    TRY(alloc(c, tc_pack_bytes(HB, HB), &npack1[t]));
+    p0[t] = negn0[t].as<float2>();
+    p1[t] = negn1[t].as<float2>();
   }
-  // -(L11^{-1} - I) per instance and its packed image (the U12 solve on tensor cores)
-  std::vector<Buf> negn(fs.size()), npack(fs.size());
-  std::vector<float2*> negn_ptrs(fs.size());
-  for (size_t t = 0; t < fs.size(); ++t) {
-    TRY(alloc(c, (size_t)NB * NB * 8, &negn[t]));
-    TRY(alloc(c, tc_pack_bytes(NB, NB), &npack[t]));
-    negn_ptrs[t] = negn[t].as<float2>();
-  }
-  Buf d_negn;
-  TRY(to_device(c, negn_ptrs, &d_negn));
-  // descriptors of every outer step, uploaded once
-  const int64_t steps = (nmax + NB - 1) / NB;
-  std::vector<TcPackInst> packs((size_t)steps * 2 * ni);
-  std::vector<TcGemmInst> gems((size_t)steps * ni);
-  std::vector<int64_t> tiles((size_t)steps, 0);
-  std::vector<TcPackInst> packs1((size_t)steps * 2 * ni);  // (-N, A12)
-  std::vector<TcGemmInst> gems1((size_t)steps * ni);       // A12 -= (-N) A12
-  std::vector<int64_t> tiles1((size_t)steps, 0);
-  for (int64_t st = 0; st < steps; ++st) {
-    const int64_t K0 = st * NB;
-    for (int t = 0; t < ni; ++t) {
-      const int64_t n = mi[t].n;
-      const int64_t m = n - K0 - NB;
-      const int kk = (int)std::max<int64_t>(0, std::min<int64_t>(NB, n - K0));
-      TcPackInst& pa = packs[(size_t)(st * 2 * ni + t)];
-      TcPackInst& pb = packs[(size_t)(st * 2 * ni + ni + t)];
-      std::memset(&pa, 0, sizeof pa);
-      std::memset(&pb, 0, sizeof pb);
-      pa.a = pb.a = mi[t].a;
-      pa.lda = pb.lda = mi[t].lda;
-      pa.r0 = pb.r0 = K0 + NB;
-      pa.k0 = pb.k0 = K0;
-      pa.rows = pb.rows = std::max<int64_t>(0, m);
-      pa.kk = pb.kk = kk;
-      pa.trans = 0;
-      pb.trans = 1;
-      pa.out = apack[t].p;
-      pb.out = bpack[t].p;
-      pa.active = pb.active = m > 0 ? 1 : 0;
-      TcGemmInst& g = gems[(size_t)(st * ni + t)];
-      std::memset(&g, 0, sizeof g);
-      g.apack = apack[t].p;
-      g.bpack = bpack[t].p;
-      g.c = mi[t].a;
-      g.ldc = mi[t].lda;
-      g.c_r0 = g.c_c0 = K0 + NB;
-      g.m = g.n = std::max<int64_t>(0, m);
-      g.kk = kk;
-      g.active = m > 0 ? 1 : 0;
-      if (m > 0) tiles[(size_t)st] += ((m + 127) / 128) * ((m + 127) / 128);
-      // U12 solve: C = A12 (rows K0.., kk rows; columns K0 + NB..), A = -N (kk x kk)
-      TcPackInst& qa = packs1[(size_t)(st * 2 * ni + t)];
-      TcPackInst& qb = packs1[(size_t)(st * 2 * ni + ni + t)];
-      std::memset(&qa, 0, sizeof qa);
-      std::memset(&qb, 0, sizeof qb);
-      qa.a = negn[t].p;
-      qa.lda = NB;
-      qa.rows = kk;
-      qa.kk = kk;
-      qa.trans = 0;
-      qa.out = npack[t].p;
-      qa.active = m > 0 ? 1 : 0;
-      qb = pb;  // A12 packed exactly like U12 of the trailing update
-      TcGemmInst& g1 = gems1[(size_t)(st * ni + t)];
-      std::memset(&g1, 0, sizeof g1);
-      g1.apack = npack[t].p;
-      g1.bpack = bpack[t].p;
-      g1.c = mi[t].a;
-      g1.ldc = mi[t].lda;
-      g1.c_r0 = K0;
-      g1.c_c0 = K0 + NB;
-      g1.m = kk;
-      g1.n = std::max<int64_t>(0, m);
-      g1.kk = kk;
-      g1.active = m > 0 ? 1 : 0;
-      if (m > 0) tiles1[(size_t)st] += (m + 127) / 128;
-    }
-  }
+  Buf d_p0, d_p1;
+  TRY(to_device(c, p0, &d_p0));
+  TRY(to_device(c, p1, &d_p1));
   // tensor maps of the factors for the reduction epilogue (all instances or none)
   Buf dmaps;
   bool red = true;
+  std::vector<const void*> cmaps(ni, nullptr);
   {
     std::vector<uint8_t> maps((size_t)ni * kTcMapBytes + 64);
     uint8_t* hm = reinterpret_cast<uint8_t*>(
@@ -881,61 +827,182 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
       TRY(alloc(c, (size_t)ni * kTcMapBytes, &dmaps));
       CUDA_TRY(c, cudaMemcpyAsync(dmaps.p, hm, (size_t)ni * kTcMapBytes, cudaMemcpyHostToDevice,
                                   c->stream));
-      for (int64_t st = 0; st < steps; ++st)
-        for (int t = 0; t < ni; ++t) {
-          const void* mp = dmaps.as<uint8_t>() + (size_t)t * kTcMapBytes;
-          gems[(size_t)(st * ni + t)].cmap = mp;
-          gems1[(size_t)(st * ni + t)].cmap = mp;
-        }
+      for (int t = 0; t < ni; ++t) cmaps[t] = dmaps.as<uint8_t>() + (size_t)t * kTcMapBytes;
     }
   }
-  Buf dpack, dgem, dpack1, dgem1;
+  // descriptors of every outer step and phase, uploaded once
+  const int64_t steps = (nmax + SB - 1) / SB;
+  enum { kNeg0, kNeg1, kP1b, kP2a, kP2b, kP3b, kP4a, kP4b, kP5b, kP6a, kP6b, kNPack };
+  enum { kG1, kG2, kG3, kG4, kG5, kG6, kNGem };
+  std::vector<TcPackInst> packs((size_t)steps * kNPack * ni);
+  std::vector<TcGemmInst> gems((size_t)steps * kNGem * ni);
+  std::vector<int64_t> tiles((size_t)steps * kNGem, 0), prow((size_t)steps * kNPack, 0);
+  std::vector<int> pkk((size_t)steps * kNPack, 0);
+  auto PK = [&](int64_t st, int ph, int t) -> TcPackInst& {
+    return packs[((size_t)st * kNPack + ph) * ni + t];
+  };
+  auto GM = [&](int64_t st, int ph, int t) -> TcGemmInst& {
+    return gems[((size_t)st * kNGem + ph) * ni + t];
+  };
+  // operand image of rows [r0, r0 + rows) x K [k0, k0 + kk) of `a` (trans: (r, k) at k + r lda)
+  auto set_pack = [&](int64_t st, int ph, int t, const void* a, int64_t lda, int64_t r0,
+                      int64_t k0, int64_t rows, int kk, int trans, void* out) {
+    TcPackInst& p = PK(st, ph, t);
+    std::memset(&p, 0, sizeof p);
+    const bool on = rows > 0 && kk > 0;
+    p.a = a;
+    p.lda = lda;
+    p.r0 = r0;
+    p.k0 = k0;
+    p.rows = on ? rows : 0;
+    p.kk = on ? kk : 0;
+    p.trans = trans;
+    p.out = out;
+    p.active = on ? 1 : 0;
+    const size_t q = (size_t)st * kNPack + ph;
+    if (on) {
+      prow[q] = std::max(prow[q], rows);
+      pkk[q] = std::max(pkk[q], kk);
+    }
+  };
+  auto set_gemm = [&](int64_t st, int ph, int t, const void* ap, const void* bp, int64_t c_r0,
+                      int64_t c_c0, int64_t m, int64_t n, int kk) {
+    TcGemmInst& g = GM(st, ph, t);
+    std::memset(&g, 0, sizeof g);
+    const bool on = m > 0 && n > 0 && kk > 0;
+    g.apack = ap;
+    g.bpack = bp;
+    g.c = mi[t].a;
+    g.ldc = mi[t].lda;
+    g.c_r0 = c_r0;
+    g.c_c0 = c_c0;
+    g.m = on ? m : 0;
+    g.n = on ? n : 0;
+    g.kk = on ? kk : 0;
+    g.active = on ? 1 : 0;
+    g.cmap = cmaps[t];
+    if (on) tiles[(size_t)st * kNGem + ph] += ((m + 127) / 128) * ((n + 127) / 128);
+  };
+  for (int64_t st = 0; st < steps; ++st) {
+    const int64_t K0 = st * SB, H1 = K0 + HB;
+    for (int t = 0; t < ni; ++t) {
+      const int64_t n = mi[t].n, lda = mi[t].lda;
+      const void* A = mi[t].a;
+      const int kk0 = (int)std::max<int64_t>(0, std::min<int64_t>(HB, n - K0));
+      const int kk1 = (int)std::max<int64_t>(0, std::min<int64_t>(HB, n - H1));
+      const int64_t m2 = std::max<int64_t>(0, n - H1);       // rows below half 0's block
+      const int64_t m3 = std::max<int64_t>(0, n - K0 - SB);  // trailing extent
+      void *ap = apack[t].p, *bp = bpack[t].p;
+      set_pack(st, kNeg0, t, negn0[t].p, HB, 0, 0, kk1 > 0 ? kk0 : 0, kk0, 0, npack0[t].p);
+      set_pack(st, kNeg1, t, negn1[t].p, HB, 0, 0, m3 > 0 ? kk1 : 0, kk1, 0, npack1[t].p);
+      // P1: U12r (rows H0.., columns H1..H1 + kk1)
+      set_pack(st, kP1b, t, A, lda, H1, K0, kk1, kk0, 1, bp);
+      set_gemm(st, kG1, t, npack0[t].p, bp, K0, H1, kk0, kk1, kk0);
+      // P2: rows [H1, n) x columns [H1, H1 + kk1) -= L21a U12r
+      set_pack(st, kP2a, t, A, lda, H1, K0, kk1 > 0 ? m2 : 0, kk0, 0, ap);
+      set_pack(st, kP2b, t, A, lda, H1, K0, kk1, kk0, 1, bp);
+      set_gemm(st, kG2, t, ap, bp, H1, H1, m2, kk1, kk0);
+      // P3: U12top (rows K0.., columns K0 + SB..)
+      set_pack(st, kP3b, t, A, lda, K0 + SB, K0, m3, kk0, 1, bp);
+      set_gemm(st, kG3, t, npack0[t].p, bp, K0, K0 + SB, kk0, m3, kk0);
+      // P4: A12bot -= Lmid U12top
+      set_pack(st, kP4a, t, A, lda, H1, K0, m3 > 0 ? kk1 : 0, kk0, 0, mpack[t].p);
+      set_pack(st, kP4b, t, A, lda, K0 + SB, K0, m3, kk0, 1, bp);
+      set_gemm(st, kG4, t, mpack[t].p, bp, H1, K0 + SB, kk1, m3, kk0);
+      // P5: U12bot = L11b^{-1} A12bot
+      set_pack(st, kP5b, t, A, lda, K0 + SB, H1, m3, kk1, 1, bp);
+      set_gemm(st, kG5, t, npack1[t].p, bp, H1, K0 + SB, kk1, m3, kk1);
+      // P6: trailing update with K = kk0 + kk1
+      set_pack(st, kP6a, t, A, lda, K0 + SB, K0, m3, kk0 + kk1, 0, ap);
+      set_pack(st, kP6b, t, A, lda, K0 + SB, K0, m3, kk0 + kk1, 1, bp);
+      set_gemm(st, kG6, t, ap, bp, K0 + SB, K0 + SB, m3, m3, kk0 + kk1);
+    }
+  }
+  Buf dpack, dgem;
   TRY(to_device(c, packs, &dpack));
   TRY(to_device(c, gems, &dgem));
-  TRY(to_device(c, packs1, &dpack1));
-  TRY(to_device(c, gems1, &dgem1));
-  for (int64_t st = 0; st < steps; ++st) {
-    const int64_t K0 = st * NB;
-    for (int64_t k0 = K0; k0 < K0 + NB && k0 < nmax; k0 += kPanelNB) {
+  auto pack = [&](int64_t st, int ph) {
+    const size_t q = (size_t)st * kNPack + ph;
+    if (prow[q] > 0)
+      launch_tc_pack(L, dpack.as<TcPackInst>() + q * ni, ni, prow[q], pkk[q]);
+  };
+  auto gemm = [&](int64_t st, int ph) {
+    const size_t q = (size_t)st * kNGem + ph;
+    if (tiles[q] > 0) launch_tc_cgemm(L, dgem.as<TcGemmInst>() + q * ni, ni, tiles[q], red);
+  };
+  auto any = [&](int64_t st, int ph) { return tiles[(size_t)st * kNGem + ph] > 0; };
+  auto factor_half = [&](int64_t H) {
+    for (int64_t k0 = H; k0 < H + HB && k0 < nmax; k0 += kPanelNB) {
       {
         Prof pr(c, "getf2");
         launch_getf2(L, dm, ni, k0, kPanelNB, 1);
       }
       {
         Prof pr(c, "laswp");
-        launch_laswp(L, dm, ni, k0, kPanelNB, K0, K0 + NB, k0, k0 + kPanelNB, 1);
+        launch_laswp(L, dm, ni, k0, kPanelNB, H, H + HB, k0, k0 + kPanelNB, 1);
       }
       {
         Prof pr(c, "trsm");
-        launch_trsm_panel(L, dm, ni, k0, kPanelNB, k0 + kPanelNB, K0 + NB, 1);
+        launch_trsm_panel(L, dm, ni, k0, kPanelNB, k0 + kPanelNB, H + HB, 1);
       }
       {
         Prof pr(c, "gemm_panel");
-        launch_gemm_update(L, dm, ni, k0, kPanelNB, nmax, k0 + kPanelNB, K0 + NB, 1);
+        launch_gemm_update(L, dm, ni, k0, kPanelNB, nmax, k0 + kPanelNB, H + HB, 1);
       }
     }
-    if (K0 + NB >= nmax) break;
+  };
+  for (int64_t st = 0; st < steps; ++st) {
+    const int64_t K0 = st * SB, H1 = K0 + HB;
+    factor_half(K0);
+    if (H1 < nmax) {
+      {
+        Prof pr(c, "laswp");
+        launch_laswp(L, dm, ni, K0, HB, H1, H1 + HB, H1, H1, 1);
+      }
+      {
+        Prof pr(c, "trsm");
+        launch_linv_neg(L, dm, ni, K0, d_p0.as<float2* const>());
+        pack(st, kNeg0);
+        pack(st, kP1b);
+        gemm(st, kG1);
+      }
+      {
+        Prof pr(c, "tc_pack");
+        pack(st, kP2a);
+        pack(st, kP2b);
+      }
+      {
+        Prof pr(c, "gemm_tc");
+        gemm(st, kG2);
+      }
+      factor_half(H1);
+    }
     {
       Prof pr(c, "laswp");
-      launch_laswp(L, dm, ni, K0, NB, 0, nmax, K0, K0 + NB, 1);
+      launch_laswp(L, dm, ni, K0, HB, 0, nmax, K0, K0 + SB, 1);
+      if (H1 < nmax) launch_laswp(L, dm, ni, H1, HB, 0, nmax, H1, K0 + SB, 1);
     }
-    int64_t max_rows = 0;
-    for (int t = 0; t < ni; ++t) max_rows = std::max(max_rows, mi[t].n - K0 - NB);
+    if (!any(st, kG6)) continue;
     {
       Prof pr(c, "trsm");
-      launch_linv_neg(L, dm, ni, K0, d_negn.as<float2* const>());
-      launch_tc_pack(L, dpack1.as<TcPackInst>() + st * 2 * ni, 2 * ni, max_rows, NB);
-      launch_tc_cgemm(L, dgem1.as<TcGemmInst>() + st * ni, ni, tiles1[(size_t)st], red);
+      pack(st, kP3b);
+      gemm(st, kG3);
+      pack(st, kP4a);
+      pack(st, kP4b);
+      gemm(st, kG4);
+      launch_linv_neg(L, dm, ni, H1, d_p1.as<float2* const>());
+      pack(st, kNeg1);
+      pack(st, kP5b);
+      gemm(st, kG5);
     }
-    max_rows = 0;
-    for (int t = 0; t < ni; ++t) max_rows = std::max(max_rows, mi[t].n - K0 - NB);
     {
       Prof pr(c, "tc_pack");
-      launch_tc_pack(L, dpack.as<TcPackInst>() + st * 2 * ni, 2 * ni, max_rows, NB);
+      pack(st, kP6a);
+      pack(st, kP6b);
     }
     {
       Prof pr(c, "gemm_tc");
-      launch_tc_cgemm(L, dgem.as<TcGemmInst>() + st * ni, ni, tiles[(size_t)st], red);
+      gemm(st, kG6);
     }
   }
   CUDA_TRY(c, cudaGetLastError());
