@@ -169,6 +169,198 @@ __global__ void __launch_bounds__(Getf2Cfg<R>::kThreads) k_getf2(const MatInst* 
   }
 }
 
+// ------------------------------------------------------------------ getf2, left-looking
+// Complex64 panel factorisation for the LU driver: column c is brought up to date only
+// when it is reached (U[0:c, c] by one warp from the finished L11 rows cached in shared
+// memory, then a[r, c] -= sum_j L[r, j] u_j for the rows below), and the pivot search is
+// fused into that pass, as is the scaling of column c - 1 by its pivot's reciprocal.
+// Each row of the panel is read about c + 2 times at column c instead of the
+// right-looking 2 (31 - c) + 1, and a cluster of kGetf2CS CTAs shares an instance's rows
+// (fixed ownership: row k0 + g + t kGetf2CS T belongs to cluster thread g), exchanging
+// the pivot candidates through distributed shared memory.  Two cluster barriers per
+// column order the global writes of one CTA before the reads of the other.  Pivoting
+// rule, interchanges and the singular marker are those of the right-looking kernel.
+constexpr int kGetf2CS = 2;
+constexpr int kGetf2T = 1024;
+
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
+                   : "memory");
+}
+__device__ __forceinline__ uint32_t peer_smem(const void* p, unsigned rank) {
+  uint32_t a = (uint32_t)__cvta_generic_to_shared(p), r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ float ld_peer_f32(uint32_t a) {
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ long long ld_peer_s64(uint32_t a) {
+  long long v;
+  asm volatile("ld.shared::cluster.s64 %0, [%1];" : "=l"(v) : "r"(a) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void better(float& bv, int64_t& bi, float ov, int64_t oi) {
+  if (ov > bv || (ov == bv && oi < bi)) {
+    bv = ov;
+    bi = oi;
+  }
+}
+
+template <int CS>
+__global__ void __launch_bounds__(kGetf2T) k_getf2_ll(const MatInst* __restrict__ insts,
+                                                      int64_t k0, int nb) {
+  constexpr int T = kGetf2T;
+  const unsigned rank = CS > 1 ? cluster_rank() : 0u;
+  const MatInst& M = insts[blockIdx.x / CS];
+  const int64_t n = M.n;
+  if (!M.active || k0 >= n) return;  // the whole cluster (one instance) leaves together
+  const int nbe = (int)min((int64_t)nb, n - k0);
+  const int64_t lda = M.lda;
+  float2* A = static_cast<float2*>(M.a);
+  __shared__ cf sL[kPanelNB][kPanelNB + 1];  // finished L11 rows
+  __shared__ cf su[kPanelNB];                // U[0:c, c]
+  __shared__ float w_val[T / 32];
+  __shared__ int64_t w_idx[T / 32];
+  __shared__ float c_val;                    // this CTA's pivot candidate
+  __shared__ int64_t c_idx;
+  __shared__ cf s_inv;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int64_t g = (int64_t)rank * T + tid;
+  constexpr int64_t stride = (int64_t)CS * T;
+  cf inv_prev = {1.f, 0.f};
+  for (int c = 0; c < nbe; ++c) {
+    const int64_t col = k0 + c;
+    // (1) u = L11[0:c, 0:c]^{-1} a[k0:k0+c, col] (identical in every CTA)
+    if (wid == 0) {
+      cf x = {0.f, 0.f};
+      if (lane < c) {
+        const float2 v = A[(k0 + lane) + col * lda];
+        x = cf{v.x, v.y};
+      }
+      for (int i = 0; i + 1 < c; ++i) {
+        cf ui;
+        ui.x = __shfl_sync(0xffffffffu, x.x, i);
+        ui.y = __shfl_sync(0xffffffffu, x.y, i);
+        if (lane > i && lane < c) x -= sL[lane][i] * ui;
+      }
+      if (lane < c) su[lane] = x;  // stored after the first cluster barrier (peers read
+                                   // the original values of these rows first)
+    }
+    __syncthreads();
+    // (2) rows >= col: finish L[., c - 1], update column c, pivot candidate
+    float best = -1.f;
+    int64_t bidx = INT64_MAX;
+    int64_t r = k0 + g;
+    if (r < col) r += ((col - r + stride - 1) / stride) * stride;
+    for (; r < n; r += stride) {
+      const float2 av = A[r + col * lda];
+      cf acc = {av.x, av.y};
+      for (int j0 = 0; j0 < c; j0 += 8) {
+        cf lv[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          lv[e] = cf{0.f, 0.f};
+          if (j0 + e < c) {
+            const float2 v = A[r + (k0 + j0 + e) * lda];
+            lv[e] = cf{v.x, v.y};
+          }
+        }
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          if (j0 + e < c) {
+            if (j0 + e == c - 1) {
+              lv[e] = lv[e] * inv_prev;
+              A[r + (k0 + j0 + e) * lda] = make_float2(lv[e].x, lv[e].y);
+            }
+            acc -= lv[e] * su[j0 + e];
+          }
+        }
+      }
+      A[r + col * lda] = make_float2(acc.x, acc.y);
+      better(best, bidx, cabs1(acc), r);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const float ov = __shfl_down_sync(0xffffffffu, best, off);
+      const int64_t oi = __shfl_down_sync(0xffffffffu, bidx, off);
+      better(best, bidx, ov, oi);
+    }
+    if (lane == 0) {
+      w_val[wid] = best;
+      w_idx[wid] = bidx;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      float bv = w_val[0];
+      int64_t bi = w_idx[0];
+      for (int w = 1; w < T / 32; ++w) better(bv, bi, w_val[w], w_idx[w]);
+      c_val = bv;
+      c_idx = bi;
+    }
+    // (3) pivot of the cluster
+    if (CS > 1)
+      cluster_sync_all();
+    else
+      __syncthreads();
+    float pv = c_val;
+    int64_t piv = c_idx;
+    if (CS > 1) {
+      for (unsigned q = 0; q < (unsigned)CS; ++q) {
+        if (q == rank) continue;
+        better(pv, piv, ld_peer_f32(peer_smem(&c_val, q)), (int64_t)ld_peer_s64(peer_smem(&c_idx, q)));
+      }
+    }
+    if (piv >= n) piv = col;  // no candidate rows (cannot happen for col < n)
+    const bool nonzero = pv > 0.f;
+    if (rank == 0) {
+      if (tid < c) A[(k0 + tid) + col * lda] = make_float2(su[tid].x, su[tid].y);
+      if (tid == 0) {
+        M.ipiv[col] = (int32_t)piv;
+        if (!nonzero && *M.info == 0) *M.info = (int32_t)(col + 1);
+      }
+      if (piv != col && tid < nbe) {  // interchange over the panel's columns
+        const int64_t cc = k0 + tid;
+        const float2 a = A[col + cc * lda], b = A[piv + cc * lda];
+        A[col + cc * lda] = b;
+        A[piv + cc * lda] = a;
+      }
+    }
+    if (CS > 1)
+      cluster_sync_all();
+    else
+      __syncthreads();
+    // (4) reciprocal of the pivot; cache the finished row of L11
+    if (tid < c) {
+      const float2 v = A[col + (k0 + tid) * lda];
+      sL[c][tid] = cf{v.x, v.y};
+    }
+    if (tid == 0) {
+      const float2 p = A[col + col * lda];
+      s_inv = nonzero ? cinv(cf{p.x, p.y}) : cf{1.f, 0.f};
+    }
+    __syncthreads();
+    inv_prev = s_inv;
+  }
+  // scale the last column below its pivot
+  const int64_t colL = k0 + nbe - 1;
+  int64_t r = k0 + g;
+  if (r <= colL) r += ((colL + 1 - r + stride - 1) / stride) * stride;
+  for (; r < n; r += stride) {
+    const float2 v = A[r + colL * lda];
+    const cf l = cf{v.x, v.y} * inv_prev;
+    A[r + colL * lda] = make_float2(l.x, l.y);
+  }
+}
+
 // ------------------------------------------------------------------ laswp
 // Interchanges of rows k0 .. k0 + nbe - 1 applied to the columns j in
 // [c_lo, min(c_hi, n)) that lie outside [s_lo, s_hi).
@@ -843,10 +1035,24 @@ __global__ void __launch_bounds__(256) k_make_perm(const MatInst* __restrict__ i
 static int prec_is_single(int prec) { return prec == 1; }
 
 void launch_getf2(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb, int prec) {
-  if (prec_is_single(prec))
-    k_getf2<float><<<ninst, Getf2Cfg<float>::kThreads, 0, L.stream>>>(d, k0, nb);
-  else
+  if (prec_is_single(prec)) {
+    // left-looking, kGetf2CS CTAs (one cluster) per instance
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(ninst * kGetf2CS));
+    cfg.blockDim = dim3(kGetf2T);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = L.stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kGetf2CS;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_getf2_ll<kGetf2CS>, d, k0, nb);
+  } else {
     k_getf2<double><<<ninst, Getf2Cfg<double>::kThreads, 0, L.stream>>>(d, k0, nb);
+  }
   count_launch(1);
 }
 
