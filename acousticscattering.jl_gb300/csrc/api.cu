@@ -832,7 +832,8 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
   }
   // descriptors of every outer step and phase, uploaded once
   const int64_t steps = (nmax + SB - 1) / SB;
-  enum { kNeg0, kNeg1, kP1b, kP2a, kP2b, kP3b, kP4a, kP4b, kP5b, kP6a, kP6b, kNPack };
+  // pack phases; pairs launched together are adjacent
+  enum { kNeg0, kP1b, kP2a, kP2b, kP3b, kP4a, kP4b, kNeg1, kP5b, kP6a, kP6b, kNPack };
   enum { kG1, kG2, kG3, kG4, kG5, kG6, kNGem };
   std::vector<TcPackInst> packs((size_t)steps * kNPack * ni);
   std::vector<TcGemmInst> gems((size_t)steps * kNGem * ni);
@@ -926,6 +927,13 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
     if (prow[q] > 0)
       launch_tc_pack(L, dpack.as<TcPackInst>() + q * ni, ni, prow[q], pkk[q]);
   };
+  // phases ph and ph + 1 in one launch (2 ni instances)
+  auto pack2 = [&](int64_t st, int ph) {
+    const size_t q = (size_t)st * kNPack + ph;
+    const int64_t rows = std::max(prow[q], prow[q + 1]);
+    const int kk = std::max(pkk[q], pkk[q + 1]);
+    if (rows > 0) launch_tc_pack(L, dpack.as<TcPackInst>() + q * ni, 2 * ni, rows, kk);
+  };
   auto gemm = [&](int64_t st, int ph) {
     const size_t q = (size_t)st * kNGem + ph;
     if (tiles[q] > 0) launch_tc_cgemm(L, dgem.as<TcGemmInst>() + q * ni, ni, tiles[q], red);
@@ -962,14 +970,12 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
       {
         Prof pr(c, "trsm");
         launch_linv_neg(L, dm, ni, K0, d_p0.as<float2* const>());
-        pack(st, kNeg0);
-        pack(st, kP1b);
+        pack2(st, kNeg0);  // -N and A12r
         gemm(st, kG1);
       }
       {
         Prof pr(c, "tc_pack");
-        pack(st, kP2a);
-        pack(st, kP2b);
+        pack2(st, kP2a);   // L21a and U12r
       }
       {
         Prof pr(c, "gemm_tc");
@@ -987,18 +993,15 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
       Prof pr(c, "trsm");
       pack(st, kP3b);
       gemm(st, kG3);
-      pack(st, kP4a);
-      pack(st, kP4b);
+      pack2(st, kP4a);   // Lmid and U12top
       gemm(st, kG4);
       launch_linv_neg(L, dm, ni, H1, d_p1.as<float2* const>());
-      pack(st, kNeg1);
-      pack(st, kP5b);
+      pack2(st, kNeg1);  // -N (second half) and A12bot
       gemm(st, kG5);
     }
     {
       Prof pr(c, "tc_pack");
-      pack(st, kP6a);
-      pack(st, kP6b);
+      pack2(st, kP6a);   // L21 and U12
     }
     {
       Prof pr(c, "gemm_tc");
@@ -1887,8 +1890,9 @@ int run_batch(bemgpu_server* S, std::vector<Item>& items,
   TRY(solve_batch(c, sf, nr, inc, outs));
   // backscatter of every (item, angle) in one far-field launch
   std::vector<WaveInst> wi(items.size());
-  std::vector<Buf> dirs(items.size()), amps(items.size());
+  std::vector<Buf> dirs(items.size()), amps(items.size()), parts(items.size());
   int32_t rmax = 0;
+  int64_t nmx = 0;
   for (size_t t = 0; t < items.size(); ++t) {
     SolutionData* sd = outs[t];
     std::vector<double> d(3 * (size_t)sd->nrhs);
@@ -1907,13 +1911,16 @@ int run_batch(bemgpu_server* S, std::vector<Item>& items,
     w.q = sd->qs.as<double>();
     w.out = amps[t].as<double>();
     w.ldp = sd->mesh->n;
+    TRY(alloc(c, far_field_scratch(w.n, 1, w.nrhs), &parts[t]));
+    w.part = parts[t].as<double>();
     rmax = std::max(rmax, sd->nrhs);
+    nmx = std::max(nmx, w.n);
   }
   Buf dw;
   TRY(upload(c, wi, &dw));
   {
     Prof p(c, "far_field");
-    launch_far_field(c->launch(), dw.as<WaveInst>(), (int)wi.size(), rmax, 1);
+    launch_far_field(c->launch(), dw.as<WaveInst>(), (int)wi.size(), rmax, 1, nmx);
   }
   CUDA_TRY(c, cudaGetLastError());
   for (size_t t = 0; t < items.size(); ++t) {
@@ -2363,11 +2370,14 @@ int bemgpu_far_field(bemgpu_solution* sol, int32_t rhs, int64_t ndir, const doub
   w.q = s->qs.as<double>() + 2 * (size_t)s->mesh->n * rhs;
   w.out = dout.as<double>();
   w.ldp = s->mesh->n;
+  Buf dpart;
+  TRY(alloc(c, far_field_scratch(w.n, (int32_t)ndir, 1), &dpart));
+  w.part = dpart.as<double>();
   std::vector<WaveInst> wv{w};
   TRY(upload(c, wv, &dw));
   {
     Prof p(c, "far_field");
-    launch_far_field(c->launch(), dw.as<WaveInst>(), 1, 1, (int32_t)ndir);
+    launch_far_field(c->launch(), dw.as<WaveInst>(), 1, 1, (int32_t)ndir, w.n);
   }
   CUDA_TRY(c, cudaGetLastError());
   CUDA_TRY(c, cudaMemcpyAsync(out, dout.p, (size_t)ndir * 16, cudaMemcpyDeviceToHost, c->stream));

@@ -356,20 +356,31 @@ void launch_incident(const Launch& L, const WaveInst* d_inst, int ninst, int64_t
 
 // ------------------------------------------------------------------ far field
 // f(xh) = -(1/4pi) sum_j area_j (ik xh.n_j p_j + q_j) sum_g W_g e^{-ik xh.y_jg}
-// (solvers/bem/full.jl:509-519).  One CTA per (direction, rhs, instance); fixed-order
-// per-thread sums, warp shuffles and a shared-memory pass make the result independent
-// of what else runs on the GPU.
-constexpr int kFarThreads = 256;
+// (solvers/bem/full.jl:509-519).  The panels are split into chunks of kFarChunk, one CTA
+// (one panel per thread) per (chunk, direction, rhs, instance), so the FP64 phase work
+// of one direction is spread over the GPU; a second kernel sums the chunk partials in
+// chunk order.  Every sum has a fixed order, so the result does not depend on what else
+// runs on the GPU.
+constexpr int kFarChunk = 128;
 
-__global__ void __launch_bounds__(kFarThreads) k_far_field(const WaveInst* __restrict__ insts) {
+size_t far_field_scratch(int64_t n, int32_t ndir, int32_t nrhs) {
+  const int64_t chunks = (n + kFarChunk - 1) / kFarChunk;
+  return (size_t)chunks * (size_t)ndir * (size_t)nrhs * 2 * sizeof(double);
+}
+
+__global__ void __launch_bounds__(kFarChunk) k_far_field(const WaveInst* __restrict__ insts) {
   const WaveInst& W = insts[blockIdx.z];
-  const int d = blockIdx.x, r = blockIdx.y;
-  if (d >= W.ndir || r >= W.nrhs) return;
+  const int64_t dr = blockIdx.x;
+  const int64_t chunk = blockIdx.y;
+  const int64_t nchunks = (W.n + kFarChunk - 1) / kFarChunk;
+  if (dr >= (int64_t)W.ndir * W.nrhs || chunk >= nchunks) return;
+  const int r = (int)(dr / W.ndir), d = (int)(dr % W.ndir);
   const double* xh = W.dirs + 3 * ((int64_t)r * W.ndir + d);
   const double k = W.k;
   const double x0 = xh[0], x1 = xh[1], x2 = xh[2];
   double ar = 0.0, ai = 0.0;
-  for (int64_t j = threadIdx.x; j < W.n; j += kFarThreads) {
+  const int64_t j = chunk * kFarChunk + threadIdx.x;
+  if (j < W.n) {
     const double* rec = W.panels + j * kPanelDoubles;
     const int64_t o = 2 * (j + r * W.ldp);
     const double pr = W.p[o], pi = W.p[o + 1];
@@ -387,15 +398,15 @@ __global__ void __launch_bounds__(kFarThreads) k_far_field(const WaveInst* __res
       si += dRuleW[g] * sn;
     }
     const double area = rec[6];
-    ar += area * (a_r * sr - a_i * si);
-    ai += area * (a_r * si + a_i * sr);
+    ar = area * (a_r * sr - a_i * si);
+    ai = area * (a_r * si + a_i * sr);
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
     ar += __shfl_down_sync(0xffffffffu, ar, off);
     ai += __shfl_down_sync(0xffffffffu, ai, off);
   }
-  __shared__ double red[2][kFarThreads / 32];
+  __shared__ double red[2][kFarChunk / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) {
     red[0][wid] = ar;
@@ -404,21 +415,39 @@ __global__ void __launch_bounds__(kFarThreads) k_far_field(const WaveInst* __res
   __syncthreads();
   if (threadIdx.x == 0) {
     double tr = 0.0, ti = 0.0;
-    for (int w = 0; w < kFarThreads / 32; ++w) {
+    for (int w = 0; w < kFarChunk / 32; ++w) {
       tr += red[0][w];
       ti += red[1][w];
     }
-    const int64_t o = 2 * ((int64_t)r * W.ndir + d);
-    W.out[o] = -tr * kInv4Pi;
-    W.out[o + 1] = -ti * kInv4Pi;
+    double* o = W.part + 2 * (dr * nchunks + chunk);
+    o[0] = tr;
+    o[1] = ti;
   }
 }
 
+__global__ void k_far_field_finish(const WaveInst* __restrict__ insts) {
+  const WaveInst& W = insts[blockIdx.z];
+  const int64_t dr = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (dr >= (int64_t)W.ndir * W.nrhs) return;
+  const int64_t nchunks = (W.n + kFarChunk - 1) / kFarChunk;
+  double tr = 0.0, ti = 0.0;
+  for (int64_t c = 0; c < nchunks; ++c) {
+    tr += W.part[2 * (dr * nchunks + c)];
+    ti += W.part[2 * (dr * nchunks + c) + 1];
+  }
+  W.out[2 * dr] = -tr * kInv4Pi;
+  W.out[2 * dr + 1] = -ti * kInv4Pi;
+}
+
 void launch_far_field(const Launch& L, const WaveInst* d_inst, int ninst, int32_t max_rhs,
-                      int32_t max_dirs) {
-  if (ninst <= 0 || max_dirs <= 0 || max_rhs <= 0) return;
-  dim3 grid((unsigned)max_dirs, (unsigned)max_rhs, (unsigned)ninst);
-  k_far_field<<<grid, kFarThreads, 0, L.stream>>>(d_inst); count_launch(1);
+                      int32_t max_dirs, int64_t max_n) {
+  if (ninst <= 0 || max_dirs <= 0 || max_rhs <= 0 || max_n <= 0) return;
+  const int64_t dr = (int64_t)max_dirs * max_rhs;
+  dim3 grid((unsigned)dr, (unsigned)((max_n + kFarChunk - 1) / kFarChunk), (unsigned)ninst);
+  k_far_field<<<grid, kFarChunk, 0, L.stream>>>(d_inst);
+  k_far_field_finish<<<dim3((unsigned)((dr + 127) / 128), 1, (unsigned)ninst), 128, 0, L.stream>>>(
+      d_inst);
+  count_launch(2);
 }
 
 }  // namespace bemgpu

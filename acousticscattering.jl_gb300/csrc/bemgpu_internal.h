@@ -93,7 +93,11 @@ struct WaveInst {
   double* q;
   double* out;             // complex128 results
   int64_t ldp;             // leading dimension of p / q
+  double* part;            // far field: per-chunk partial sums (far_field_scratch bytes)
 };
+
+// bytes of WaveInst.part for a far-field launch over n panels, ndir directions, nrhs
+size_t far_field_scratch(int64_t n, int32_t ndir, int32_t nrhs);
 
 // Dense-matrix instance for the batched factor / solve kernels.
 struct MatInst {
@@ -133,7 +137,7 @@ void launch_near_laplace(const Launch& L, const double* panels, const double* ve
 void launch_incident(const Launch& L, const WaveInst* d_inst, int ninst, int64_t nmax,
                      int32_t max_rhs);
 void launch_far_field(const Launch& L, const WaveInst* d_inst, int ninst, int32_t max_rhs,
-                      int32_t max_dirs);
+                      int32_t max_dirs, int64_t max_n);
 #endif
 
 }  // namespace bemgpu

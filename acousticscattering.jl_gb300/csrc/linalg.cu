@@ -182,6 +182,7 @@ __global__ void __launch_bounds__(Getf2Cfg<R>::kThreads) k_getf2(const MatInst* 
 // rule, interchanges and the singular marker are those of the right-looking kernel.
 constexpr int kGetf2CS = 2;
 constexpr int kGetf2T = 1024;
+constexpr int kLLBatch = 16;  // L values per row in flight
 
 __device__ __forceinline__ unsigned cluster_rank() {
   unsigned r;
@@ -264,10 +265,10 @@ __global__ void __launch_bounds__(kGetf2T) k_getf2_ll(const MatInst* __restrict_
     for (; r < n; r += stride) {
       const float2 av = A[r + col * lda];
       cf acc = {av.x, av.y};
-      for (int j0 = 0; j0 < c; j0 += 8) {
-        cf lv[8];
+      for (int j0 = 0; j0 < c; j0 += kLLBatch) {
+        cf lv[kLLBatch];
 #pragma unroll
-        for (int e = 0; e < 8; ++e) {
+        for (int e = 0; e < kLLBatch; ++e) {
           lv[e] = cf{0.f, 0.f};
           if (j0 + e < c) {
             const float2 v = A[r + (k0 + j0 + e) * lda];
@@ -275,7 +276,7 @@ __global__ void __launch_bounds__(kGetf2T) k_getf2_ll(const MatInst* __restrict_
           }
         }
 #pragma unroll
-        for (int e = 0; e < 8; ++e) {
+        for (int e = 0; e < kLLBatch; ++e) {
           if (j0 + e < c) {
             if (j0 + e == c - 1) {
               lv[e] = lv[e] * inv_prev;
@@ -797,10 +798,14 @@ void launch_linv_neg(const Launch& L, const MatInst* d, int ninst, int64_t k0, f
 constexpr int kBigB = 512;
 constexpr int kDiagThreads = 512;
 constexpr int kTilePad = 33;
+constexpr int kPre = 32;  // prefetched update operands per thread
+static_assert(kBigB - 32 <= kDiagThreads, "one update row per thread");
+static_assert((kBigB - 32 + (kDiagThreads / 32) * 4 - 1) / ((kDiagThreads / 32) * 4) * 4 <= kPre,
+              "transposed update rows per lane");
 
 template <typename R>
 constexpr size_t diag_smem_bytes() {
-  return sizeof(cx<R>) * (kBigB + 2 * 32 * kTilePad);
+  return sizeof(cx<R>) * (kBigB + 2 * 32 * kTilePad + 2 * 32);
 }
 
 template <typename R, bool EFF_LOWER, bool TRANS, bool UNIT>
@@ -814,6 +819,7 @@ __global__ void __launch_bounds__(kDiagThreads) k_trsv_diag(const MatInst* __res
   extern __shared__ __align__(16) unsigned char diag_smem[];
   cx<R>* sx = reinterpret_cast<cx<R>*>(diag_smem);
   cx<R>* tiles = sx + kBigB;  // [2][32][kTilePad], tile[i][j] = op(A)[s0 + i, s0 + j]
+  cx<R>* dinv = tiles + 2 * 32 * kTilePad;  // [2][32] reciprocals of the tiles' diagonals
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nsub = (nbs + 31) / 32;
   auto sub_of = [&](int bb) { return EFF_LOWER ? bb : nsub - 1 - bb; };
@@ -829,6 +835,7 @@ __global__ void __launch_bounds__(kDiagThreads) k_trsv_diag(const MatInst* __res
         T[q * kTilePad + p] = cconj(v);
       else
         T[p * kTilePad + q] = v;
+      if (!UNIT && p == q && p < nb) dinv[buf * 32 + p] = cinv(TRANS ? cconj(v) : v);
     }
   };
   for (int i = tid; i < nbs; i += kDiagThreads) sx[i] = ld<R>(M.x, off + r0 + i);
@@ -839,11 +846,33 @@ __global__ void __launch_bounds__(kDiagThreads) k_trsv_diag(const MatInst* __res
     const int s0 = b * 32;
     const int nb = min(32, nbs - s0);
     const cx<R>* T = tiles + (bb & 1) * 32 * kTilePad;
+    const cx<R>* DI = dinv + (bb & 1) * 32;
+    // this sub-block's update operands, loaded before the solve so that their memory
+    // latency overlaps it (one row of 32 values per thread, or 32 column values per
+    // lane for op(A) = A^H)
+    constexpr int kP = sizeof(R) == 4 ? kPre : kPre / 2;  // FP64: half, rest on demand
+    cx<R> pre[kP];
+    {
+      const int lo = EFF_LOWER ? s0 + nb : 0, hi = EFF_LOWER ? nbs : s0;
+      if (!TRANS) {
+        const int r = lo + tid;
+#pragma unroll
+        for (int c = 0; c < kP; ++c)
+          pre[c] = (r < hi && c < nb) ? ld<R>(M.a, (r0 + r) + (r0 + s0 + c) * lda) : cx<R>{0, 0};
+      } else {
+#pragma unroll
+        for (int q = 0; q < kP; ++q) {
+          const int r = lo + warp * 4 + (q & 3) + (q >> 2) * (kDiagThreads / 32) * 4;
+          pre[q] = (r < hi && lane < nb) ? ld<R>(M.a, (r0 + s0 + lane) + (r0 + r) * lda)
+                                         : cx<R>{0, 0};
+        }
+      }
+    }
     if (warp == 0) {
       cx<R> x = lane < nb ? sx[s0 + lane] : cx<R>{0, 0};
       if (EFF_LOWER) {
         for (int c = 0; c < nb; ++c) {
-          if (!UNIT && lane == c) x = x * cinv(T[c * kTilePad + c]);
+          if (!UNIT && lane == c) x = x * DI[c];
           cx<R> xc;
           xc.x = __shfl_sync(0xffffffffu, x.x, c);
           xc.y = __shfl_sync(0xffffffffu, x.y, c);
@@ -851,7 +880,7 @@ __global__ void __launch_bounds__(kDiagThreads) k_trsv_diag(const MatInst* __res
         }
       } else {
         for (int c = nb - 1; c >= 0; --c) {
-          if (!UNIT && lane == c) x = x * cinv(T[c * kTilePad + c]);
+          if (!UNIT && lane == c) x = x * DI[c];
           cx<R> xc;
           xc.x = __shfl_sync(0xffffffffu, x.x, c);
           xc.y = __shfl_sync(0xffffffffu, x.y, c);
@@ -865,39 +894,38 @@ __global__ void __launch_bounds__(kDiagThreads) k_trsv_diag(const MatInst* __res
     __syncthreads();
     const int lo = EFF_LOWER ? s0 + nb : 0, hi = EFF_LOWER ? nbs : s0;
     if (!TRANS) {
-      for (int r = lo + tid; r < hi; r += kDiagThreads) {
+      // one row per thread (the block's rows outside the sub-block fit in kDiagThreads)
+      const int r = lo + tid;
+      if (r < hi) {
         cx<R> acc = {0, 0};
-        cx<R> lv[16];
 #pragma unroll
-        for (int h = 0; h < 32; h += 16) {
+        for (int c = 0; c < kP; ++c)
+          if (c < nb) acc += pre[c] * sx[s0 + c];
 #pragma unroll
-          for (int c = 0; c < 16; ++c)
-            lv[c] = (h + c < nb) ? ld<R>(M.a, (r0 + r) + (r0 + s0 + h + c) * lda) : cx<R>{0, 0};
-#pragma unroll
-          for (int c = 0; c < 16; ++c)
-            if (h + c < nb) acc += lv[c] * sx[s0 + h + c];
-        }
+        for (int c = kP; c < 32; ++c)
+          if (c < nb) acc += ld<R>(M.a, (r0 + r) + (r0 + s0 + c) * lda) * sx[s0 + c];
         sx[r] -= acc;
       }
     } else {
       // op(A)[r, s0 + c] = conj(A[s0 + c, r]): lanes along c, 4 rows per warp pass
       const cx<R> xv = lane < nb ? sx[s0 + lane] : cx<R>{0, 0};
-      for (int r = lo + warp * 4; r < hi; r += (kDiagThreads / 32) * 4) {
-        cx<R> v[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-          v[u] = (r + u < hi && lane < nb) ? ld<R>(M.a, (r0 + s0 + lane) + (r0 + r + u) * lda)
-                                           : cx<R>{0, 0};
+      for (int q = 0; q < kPre; ++q) {
+        const cx<R> av =
+            q < kP ? pre[q < kP ? q : 0]
+                   : [&] {
+                       const int rr = lo + warp * 4 + (q & 3) + (q >> 2) * (kDiagThreads / 32) * 4;
+                       return (rr < hi && lane < nb) ? ld<R>(M.a, (r0 + s0 + lane) + (r0 + rr) * lda)
+                                                     : cx<R>{0, 0};
+                     }();
+        cx<R> t = cconj(av) * xv;
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          cx<R> t = cconj(v[u]) * xv;
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) {
-            t.x += __shfl_xor_sync(0xffffffffu, t.x, o);
-            t.y += __shfl_xor_sync(0xffffffffu, t.y, o);
-          }
-          if (lane == 0 && r + u < hi) sx[r + u] -= t;
+        for (int o = 16; o > 0; o >>= 1) {
+          t.x += __shfl_xor_sync(0xffffffffu, t.x, o);
+          t.y += __shfl_xor_sync(0xffffffffu, t.y, o);
         }
+        const int r = lo + warp * 4 + (q & 3) + (q >> 2) * (kDiagThreads / 32) * 4;
+        if (lane == 0 && r < hi) sx[r] -= t;
       }
     }
     __syncthreads();
