@@ -390,6 +390,7 @@ struct FactorData {
   Buf A, Mrhs;             // system (complex128, or complex64 when a32), rhs operator
   bool a32 = false;        // system stored compact: complex64 + FP64 near corrections
   Buf dnear;               // near corrections of the compact system
+  Buf dnear_rhs;           // near corrections of the compact rhs operator (a32, rigid/soft)
   Buf LU, ipiv, info, perm;        // working factor (complex64 when single)
   Buf LU64, ipiv64, info64, perm64;  // complex128 factor after promotion
   Buf rows, cols, rowsum, cols_inv, rows_inv, cols_inv32;
@@ -406,7 +407,7 @@ struct FactorData {
   int32_t* info_ptr() const { return single ? info.as<int32_t>() : (mixed ? info64.as<int32_t>() : info.as<int32_t>()); }
   int32_t* perm_ptr() const { return single ? perm.as<int32_t>() : (mixed ? perm64.as<int32_t>() : perm.as<int32_t>()); }
   size_t bytes() const {
-    return A.bytes + dnear.bytes + Mrhs.bytes + LU.bytes + LU64.bytes + ipiv.bytes +
+    return A.bytes + dnear.bytes + dnear_rhs.bytes + Mrhs.bytes + LU.bytes + LU64.bytes + ipiv.bytes +
            ipiv64.bytes + rows.bytes + cols.bytes + rowsum.bytes;
   }
 };
@@ -497,9 +498,11 @@ int assemble_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
     f->N = fluid ? 2 * m->n : m->n;
     f->a32 = f->fp32_regular;
     TRY(alloc(c, (size_t)f->N * f->N * (f->a32 ? 8 : 16), &f->A));
-    if (!fluid) TRY(alloc(c, (size_t)f->n * f->n * 16, &f->Mrhs));
-    if (f->a32)
+    if (!fluid) TRY(alloc(c, (size_t)f->n * f->n * (f->a32 ? 8 : 16), &f->Mrhs));
+    if (f->a32) {
       TRY(alloc(c, (size_t)std::max<int64_t>(1, m->n_near) * (fluid ? 4 : 1) * 16, &f->dnear));
+      if (!fluid) TRY(alloc(c, (size_t)std::max<int64_t>(1, m->n_near) * 16, &f->dnear_rhs));
+    }
     AsmInst& I = ai[t];
     std::memset(&I, 0, sizeof I);
     I.panels = m->panels.as<double>();
@@ -526,9 +529,14 @@ int assemble_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
       f->rhs_is_m2 = f->prob.boundary == BEMGPU_RIGID;
       I.out1 = f->rhs_is_m2 ? f->A.p : f->Mrhs.p;
       I.out2 = f->rhs_is_m2 ? f->Mrhs.p : f->A.p;
-      I.c64 = f->a32 ? (f->rhs_is_m2 ? 1 : 2) : 0;
+      I.c64 = f->a32 ? 3 : 0;
     }
-    I.dnear = f->a32 ? f->dnear.as<double>() : nullptr;
+    if (f->a32) {
+      double* sysd = f->dnear.as<double>();
+      double* rhsd = fluid ? nullptr : f->dnear_rhs.as<double>();
+      I.dnear = (fluid || f->rhs_is_m2) ? sysd : rhsd;   // corrections of out1
+      I.dnear2 = (fluid || f->rhs_is_m2) ? rhsd : sysd;  // corrections of out2
+    }
   }
   // group by (kind, regular precision) so each group is one launch
   std::vector<size_t> order(fs.size());
@@ -1307,8 +1315,12 @@ void fill_vec(VecInst& v, SolveInst& s, const void* A, int64_t N) {
   v.changed = s.changed.as<int32_t>();
   v.out = s.work.p;
   v.out_single = s.f->single ? 1 : 0;
-  if (A == s.f->A.p && s.f->a32) {
+  if (s.f->a32 && (A == s.f->A.p || A == s.f->Mrhs.p)) {
     set_compact(v, s.f);
+    if (A == s.f->Mrhs.p) {  // the rhs operator: n x n, its own corrections
+      v.nbc = 1;
+      v.dnear = s.f->dnear_rhs.as<double>();
+    }
     v.xs = s.xs.as<float4>();
     v.xa = s.xa.as<float>();
   }
@@ -1803,8 +1815,8 @@ size_t item_bytes(const ServerReq& r) {
   const bool mixed = r.prob.precision == BEMGPU_MIXED;
   const bool a32 = r.prob.assembly == BEMGPU_ASSEMBLY_SINGLE ||
                    (r.prob.assembly == BEMGPU_ASSEMBLY_DEFAULT && mixed);
-  size_t b = N * N * (a32 ? 8 : 16) + N * N * (mixed ? 8 : 16) + (fl ? 0 : n * n * 16);
-  b += a32 ? (size_t)r.mesh->n_near * (fl ? 4 : 1) * 16 : 0;
+  size_t b = N * N * (a32 ? 8 : 16) + N * N * (mixed ? 8 : 16) + (fl ? 0 : n * n * (a32 ? 8 : 16));
+  b += a32 ? (size_t)r.mesh->n_near * (fl ? 4 : 2) * 16 : 0;
   b += 2 * tc_pack_bytes((int64_t)N, 128) + N * 64;
   const size_t R = (size_t)r.nangles;
   b += N * R * (16 * 6 + 8) + (size_t)kChunks * R * N * 3 * 8;
@@ -2776,33 +2788,46 @@ int bemgpu_assemble_dense(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_p
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   TRY(check_device_error(c));
   const bool fluid = kind == kAsmMuller || kind == kAsmFluidCBIE;
-  // the compact system expanded to complex128 (value + near correction)
-  Buf full;
+  // compact operators expanded to complex128 (value + near correction)
+  Buf full, full_rhs;
   const void* sys = f->A.p;
+  const void* rhs = f->Mrhs.p;
   if (f->a32) {
-    TRY(alloc(c, (size_t)f->N * f->N * 16, &full));
+    std::vector<VecInst> vi;
     VecInst v;
     std::memset(&v, 0, sizeof v);
     v.A = f->A.p;
     v.n = f->N;
     v.lda = f->N;
+    TRY(alloc(c, (size_t)f->N * f->N * 16, &full));
     v.out = full.p;
     set_compact(v, f.get());
-    std::vector<VecInst> vi{v};
+    vi.push_back(v);
+    if (!fluid) {
+      TRY(alloc(c, (size_t)f->n * f->n * 16, &full_rhs));
+      VecInst w = v;
+      w.A = f->Mrhs.p;
+      w.n = w.lda = f->n;
+      w.out = full_rhs.p;
+      w.nbc = 1;
+      w.dnear = f->dnear_rhs.as<double>();
+      vi.push_back(w);
+    }
     Buf d;
     TRY(to_device(c, vi, &d));
     const Launch L = c->launch();
-    launch_expand_a32(L, d.as<VecInst>(), 1, f->N);
-    launch_near_add(L, d.as<VecInst>(), 1, v.n_near, 1);
+    launch_expand_a32(L, d.as<VecInst>(), (int)vi.size(), f->N);
+    launch_near_add(L, d.as<VecInst>(), (int)vi.size(), v.n_near, 1);
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     sys = full.p;
+    if (!fluid) rhs = full_rhs.p;
   }
   // M1 / M2 in the reference's naming: rigid system is M1, pressure release system is M2
   if (fluid) {
     CUDA_TRY(c, cudaMemcpy(M1, sys, (size_t)f->N * f->N * 16, cudaMemcpyDeviceToHost));
   } else {
-    const void* m1 = f->rhs_is_m2 ? sys : f->Mrhs.p;
-    const void* m2 = f->rhs_is_m2 ? f->Mrhs.p : sys;
+    const void* m1 = f->rhs_is_m2 ? sys : rhs;
+    const void* m2 = f->rhs_is_m2 ? rhs : sys;
     CUDA_TRY(c, cudaMemcpy(M1, m1, (size_t)f->n * f->n * 16, cudaMemcpyDeviceToHost));
     if (M2) CUDA_TRY(c, cudaMemcpy(M2, m2, (size_t)f->n * f->n * 16, cudaMemcpyDeviceToHost));
   }

@@ -159,8 +159,8 @@ __global__ void __launch_bounds__(kAsmRows) k_assemble_regular(const AsmInst* __
         m1 -= al * a.H;
         m2 += al * a.K;
       }
-      store_r(I.out1, I.c64 == 1, i + j * lda, m1);
-      store_r(I.out2, I.c64 == 2, i + j * lda, m2);
+      store_r(I.out1, (I.c64 & 1) != 0, i + j * lda, m1);
+      store_r(I.out2, (I.c64 & 2) != 0, i + j * lda, m2);
     } else {
       Acc<R> e, t;
       e.S = e.D = e.K = e.H = cx<R>{0, 0};
@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(kAsmRows) k_assemble_regular(const AsmInst* __
         a21 = t.D;
         a22 = cx<R>{-g * t.S.x, -g * t.S.y};
       }
-      const bool c64 = I.c64 == 1;
+      const bool c64 = (I.c64 & 1) != 0;
       store_r(I.out1, c64, i + j * lda, a11);
       store_r(I.out1, c64, i + (n + j) * lda, a12);
       store_r(I.out1, c64, (n + i) + j * lda, a21);
@@ -227,8 +227,8 @@ __global__ void __launch_bounds__(128) k_assemble_near(const AsmInst* __restrict
       m1 -= al * o.H;
       m2 += al * (o.K + cd{0.5 * delta, 0.0});
     }
-    store_n(I.out1, I.c64 == 1, I.dnear, p, i + j * lda, m1);
-    store_n(I.out2, I.c64 == 2, I.dnear, p, i + j * lda, m2);
+    store_n(I.out1, (I.c64 & 1) != 0, I.dnear, p, i + j * lda, m1);
+    store_n(I.out2, (I.c64 & 2) != 0, I.dnear2, p, i + j * lda, m2);
   } else {
     Ops e = near_pair<KIND, F32>(v, rj, x, nx, self, I.k_e, S0, D0, K0, H0);
     Ops t = near_pair<KIND, F32>(v, rj, x, nx, self, I.k_i, S0, D0, K0, H0);
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(128) k_assemble_near(const AsmInst* __restrict
       a21 = cd{0.5 * delta + t.D.x, t.D.y};
       a22 = cd{-g * t.S.x, -g * t.S.y};
     }
-    const bool c64 = I.c64 == 1;
+    const bool c64 = (I.c64 & 1) != 0;
     const int64_t nn = I.n_near;
     store_n(I.out1, c64, I.dnear, p, i + j * lda, a11);
     store_n(I.out1, c64, I.dnear, nn + p, i + (n + j) * lda, a12);

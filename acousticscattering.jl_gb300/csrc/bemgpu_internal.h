@@ -75,10 +75,11 @@ struct AsmInst {
   double k_e, k_i, g;      // exterior/interior wavenumber, density contrast
   double a_re, a_im;       // Burton-Miller coupling (0 for CBIE)
   int32_t kind;            // AsmKind
-  int32_t c64;             // 0: both outputs complex128; 1 / 2: out1 / out2 is complex64
+  int32_t c64;             // bit 0 / bit 1: out1 / out2 stored complex64 (else complex128)
   void* out1;              // M1 (or A for fluid)
   void* out2;              // M2 (rigid/soft), null for fluid
-  double* dnear;           // complex64 output: FP64 near corrections [block][n_near]
+  double* dnear;           // complex64 out1: FP64 near corrections [block][n_near]
+  double* dnear2;          // complex64 out2: FP64 near corrections [n_near]
 };
 
 // Incident field / far-field instance.

@@ -175,12 +175,11 @@ __global__ void __launch_bounds__(Getf2Cfg<R>::kThreads) k_getf2(const MatInst* 
 // memory, then a[r, c] -= sum_j L[r, j] u_j for the rows below), and the pivot search is
 // fused into that pass, as is the scaling of column c - 1 by its pivot's reciprocal.
 // Each row of the panel is read about c + 2 times at column c instead of the
-// right-looking 2 (31 - c) + 1, and a cluster of kGetf2CS CTAs shares an instance's rows
-// (fixed ownership: row k0 + g + t kGetf2CS T belongs to cluster thread g), exchanging
+// right-looking 2 (31 - c) + 1, and a cluster of CS CTAs shares an instance's rows
+// (fixed ownership: row k0 + g + t CS T belongs to cluster thread g), exchanging
 // the pivot candidates through distributed shared memory.  Two cluster barriers per
 // column order the global writes of one CTA before the reads of the other.  Pivoting
 // rule, interchanges and the singular marker are those of the right-looking kernel.
-constexpr int kGetf2CS = 2;
 constexpr int kGetf2T = 1024;
 constexpr int kLLBatch = 16;  // L values per row in flight
 
@@ -1062,22 +1061,44 @@ __global__ void __launch_bounds__(256) k_make_perm(const MatInst* __restrict__ i
 // ------------------------------------------------------------------ launch wrappers
 static int prec_is_single(int prec) { return prec == 1; }
 
+// CTAs per instance of the left-looking panel kernel: as many as keep the batch on the
+// SMs in one wave (a power of two, 2..8: the portable cluster limit).
+static int getf2_cluster(int ninst) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  int cs = 2;
+  while (cs < 8 && (int64_t)ninst * cs * 2 <= sms) cs *= 2;
+  return cs;
+}
+
+template <int CS>
+static void getf2_ll_t(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(ninst * CS));
+  cfg.blockDim = dim3(kGetf2T);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = L.stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CS;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_getf2_ll<CS>, d, k0, nb);
+}
+
 void launch_getf2(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb, int prec) {
   if (prec_is_single(prec)) {
-    // left-looking, kGetf2CS CTAs (one cluster) per instance
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(ninst * kGetf2CS));
-    cfg.blockDim = dim3(kGetf2T);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = L.stream;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = kGetf2CS;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, k_getf2_ll<kGetf2CS>, d, k0, nb);
+    switch (getf2_cluster(ninst)) {  // left-looking, one cluster per instance
+      case 8: getf2_ll_t<8>(L, d, ninst, k0, nb); break;
+      case 4: getf2_ll_t<4>(L, d, ninst, k0, nb); break;
+      default: getf2_ll_t<2>(L, d, ninst, k0, nb); break;
+    }
   } else {
     k_getf2<double><<<ninst, Getf2Cfg<double>::kThreads, 0, L.stream>>>(d, k0, nb);
   }

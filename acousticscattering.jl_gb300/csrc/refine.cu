@@ -397,6 +397,117 @@ __device__ __forceinline__ void gemv_body(const VecInst& V, int with_abs) {
   }
 }
 
+// Compact instances: two rows per thread (i and i + 256, both coalesced), so every x
+// value loaded serves two rows and each thread carries four independent pair-sum chains
+// per right-hand side.  Columns are loaded kBatch at a time, folded into FP64 every
+// kFold columns.
+constexpr int kA32Rows = 2;
+template <int NR>
+__device__ __forceinline__ void gemv_a32_body(const VecInst& V, int with_abs) {
+  constexpr int kFold = 32, kBatch = NR == 1 ? 8 : 4;
+  const int64_t n = V.n;
+  const int64_t i0 = (int64_t)blockIdx.x * (256 * kA32Rows) + threadIdx.x;
+  const int ch = blockIdx.y % kChunks, grp = blockIdx.y / kChunks;
+  const int r0 = grp * NR;
+  if (i0 >= n || r0 >= V.nrhs) return;
+  const int nr = min(NR, V.nrhs - r0);
+  const bool ok1 = i0 + 256 < n;
+  int64_t j0, j1;
+  chunk_range(n, ch, kChunks, &j0, &j1);
+  const float2* A0 = reinterpret_cast<const float2*>(V.A) + i0;
+  const float2* A1 = ok1 ? A0 + 256 : A0;
+  const int64_t lda = V.lda;
+  const float4* xs[NR];
+  const float* xa[NR];
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    const int64_t rr = (int64_t)(r0 + (r < nr ? r : 0)) * n;
+    xs[r] = V.xs + rr;
+    xa[r] = V.xa + rr;
+  }
+  cd acc[kA32Rows][NR];
+  float aacc[kA32Rows][NR];
+#pragma unroll
+  for (int h = 0; h < kA32Rows; ++h)
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+      acc[h][r] = cd{0.0, 0.0};
+      aacc[h][r] = 0.f;
+    }
+  for (int64_t jf = j0; jf < j1; jf += kFold) {
+    FPair re[kA32Rows][NR], im[kA32Rows][NR];
+#pragma unroll
+    for (int h = 0; h < kA32Rows; ++h)
+#pragma unroll
+      for (int r = 0; r < NR; ++r) re[h][r] = im[h][r] = FPair{0.f, 0.f};
+    const int64_t jf1 = min(j1, jf + kFold);
+    for (int64_t jb = jf; jb < jf1; jb += kBatch) {
+      const int cnt = (int)min((int64_t)kBatch, jf1 - jb);
+      float2 a[kA32Rows][kBatch];
+#pragma unroll
+      for (int q = 0; q < kBatch; ++q) {
+        a[0][q] = q < cnt ? A0[(jb + q) * lda] : make_float2(0.f, 0.f);
+        a[1][q] = q < cnt ? A1[(jb + q) * lda] : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int q = 0; q < kBatch; ++q) {
+        if (q < cnt) {
+          float aa[kA32Rows];
+#pragma unroll
+          for (int h = 0; h < kA32Rows; ++h)
+            aa[h] = with_abs ? sqrtf(fmaf(a[h][q].x, a[h][q].x, a[h][q].y * a[h][q].y)) : 0.f;
+#pragma unroll
+          for (int r = 0; r < NR; ++r) {
+            const float4 x = xs[r][jb + q];
+            const float xm = with_abs ? xa[r][jb + q] : 0.f;
+#pragma unroll
+            for (int h = 0; h < kA32Rows; ++h) {
+              const float2 av = a[h][q];
+              // re += a.x x.re - a.y x.im ; im += a.x x.im + a.y x.re
+              pair_add_prod(re[h][r], av.x, x.x);
+              pair_add_prod(re[h][r], -av.y, x.y);
+              pair_add_prod(im[h][r], av.x, x.y);
+              pair_add_prod(im[h][r], av.y, x.x);
+              re[h][r].t = __fmaf_rn(av.x, x.z, __fmaf_rn(-av.y, x.w, re[h][r].t));
+              im[h][r].t = __fmaf_rn(av.x, x.w, __fmaf_rn(av.y, x.z, im[h][r].t));
+              aacc[h][r] = fmaf(aa[h], xm, aacc[h][r]);
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < kA32Rows; ++h)
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        acc[h][r].x += (double)re[h][r].s + (double)re[h][r].t;
+        acc[h][r].y += (double)im[h][r].s + (double)im[h][r].t;
+      }
+  }
+  // part layout: [chunk][rhs][row] x (re, im, abs)
+#pragma unroll
+  for (int h = 0; h < kA32Rows; ++h) {
+    const int64_t i = i0 + 256 * h;
+    if (h == 1 && !ok1) break;
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+      if (r < nr) {
+        const int64_t o = 3 * (((int64_t)ch * V.nrhs + r0 + r) * n + i);
+        V.part[o] = acc[h][r].x;
+        V.part[o + 1] = acc[h][r].y;
+        V.part[o + 2] = (double)aacc[h][r];
+      }
+    }
+  }
+}
+
+template <int NR>
+__global__ void __launch_bounds__(256, 2) k_gemv_a32(const VecInst* __restrict__ insts, int with_abs) {
+  const VecInst& V = insts[blockIdx.z];
+  if (!V.a32) return;
+  gemv_a32_body<NR>(V, with_abs);
+}
+
 // partial y = A x (and |A||x|) over a column chunk, up to kGemvR right-hand sides
 // per pass (rhs group = blockIdx.y / kChunks).
 template <bool A32, int NR>
@@ -599,11 +710,13 @@ void launch_gemv(const Launch& L, const VecInst* d, int ninst, int64_t nmax, int
   dim3 g0((unsigned)((nmax + 255) / 256), (unsigned)max_rhs, (unsigned)ninst);
   k_split_x<<<g0, 256, 0, L.stream>>>(d); count_launch(1);
   dim3 g1((unsigned)((nmax + 255) / 256), (unsigned)(kChunks * groups), (unsigned)ninst);
+  dim3 ga((unsigned)((nmax + 256 * kA32Rows - 1) / (256 * kA32Rows)), (unsigned)(kChunks * groups),
+          (unsigned)ninst);
   if (nr == 1) {
-    k_gemv_part<true, 1><<<g1, 256, 0, L.stream>>>(d, mode == 1);
+    k_gemv_a32<1><<<ga, 256, 0, L.stream>>>(d, mode == 1);
     k_gemv_part<false, 1><<<g1, 256, 0, L.stream>>>(d, mode == 1);
   } else {
-    k_gemv_part<true, kGemvR><<<g1, 256, 0, L.stream>>>(d, mode == 1);
+    k_gemv_a32<kGemvR><<<ga, 256, 0, L.stream>>>(d, mode == 1);
     k_gemv_part<false, kGemvR><<<g1, 256, 0, L.stream>>>(d, mode == 1);
   }
   count_launch(2);

@@ -301,6 +301,324 @@ def run_ours(args):
     return line
 
 
+# ------------------------------------------------------------------ other workloads
+# The remaining named workloads, selected with --config; each prints its own JSON line
+# (the default line above is the headline workload).
+def _base_line(metric, value, unit, ms, args, config, **kw):
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "data": "synthetic", "config": config}
+    line.update(kw)
+    return line
+
+
+def run_config0(args):
+    """Rigid sphere a = 0.01 m, icosphere 1280 panels, c = 1477.4 m/s, f = 38 kHz, plane
+    wave along +z (polar pi/2, azimuth pi/2), Burton-Miller alpha = i/k: one solve per step
+    (assembly + factor + solve + backscatter), mixed and FP64."""
+    import bemgpu
+    from bemgpu import meshes
+    ctx = bemgpu.Context(0)
+    nodes, tris = meshes.icosphere(0.01, 3)
+    surf = bemgpu.mesh(nodes, tris)
+    k = 2 * math.pi * 38e3 / 1477.4
+    beta, alpha = math.pi / 2, math.pi / 2
+
+    def one(precision):
+        sol = bemgpu.bem(surf, bemgpu.Rigid(), k, incidence_angle=beta, incidence_azimuth=alpha,
+                         precision=precision, ctx=ctx)
+        f = bemgpu.scattering_amplitude(sol)
+        sol.close()
+        return f
+
+    steps = max(args.steps, 20)
+    out = {}
+    for prec in ("mixed", "double"):
+        for _ in range(max(args.warmup, 3)):
+            one(prec)
+        clocks = Clocks(0)
+        clocks.start()
+        l0 = bemgpu.Context.launch_count()
+        ts = []
+        for _ in range(steps):
+            ctx.timer_start()
+            f = one(prec)
+            ts.append(ctx.timer_stop())
+        out[prec] = (f, float(np.mean(ts)), float(np.percentile(ts, 50)),
+                     float(np.percentile(ts, 99)), clocks.stop(),
+                     (bemgpu.Context.launch_count() - l0) // steps)
+    fm, fd = out["mixed"][0], out["double"][0]
+    ms = out["mixed"][1]
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+        t0 = time.perf_counter()
+        O.solve(nodes, tris, "rigid", k, incidence_angle=beta, incidence_azimuth=alpha)
+        dt = time.perf_counter() - t0
+        cpu = {"value": 1.0 / dt, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"one FP64 solve of the same sphere by the oracle, {dt:.2f} s"}
+    line = _base_line(
+        "BEM solves/s, rigid sphere 1280 panels (plain FP64 case)", 1e3 / ms, "solves/s", ms,
+        args, {"workload": "rigid sphere a=0.01 m, icosphere 1280 panels, f=38 kHz, "
+                           "c=1477.4 m/s, +z incidence, Burton-Miller", "panels": 1280},
+        steps=steps, dtype="c64 factor + fp64 refinement",
+        latency_ms={"p50": out["mixed"][2], "p99": out["mixed"][3]},
+        fp64={"solves_per_s": 1e3 / out["double"][1], "p50_ms": out["double"][2],
+              "p99_ms": out["double"][3], "ts_db": 20 * math.log10(abs(fd))},
+        ts_db=20 * math.log10(abs(fm)),
+        ts_error_db_vs_fp64=abs(20 * math.log10(abs(fm)) - 20 * math.log10(abs(fd))),
+        amplitude_rel_error_vs_fp64=abs(fm - fd) / abs(fd),
+        clocks=out["mixed"][4], gpu_launches=out["mixed"][5], cpu_baseline=cpu)
+    print(json.dumps(line))
+    return line
+
+
+def run_config2(args):
+    """Rigid prolate spheroid 0.05 x 0.0125 m, 128 x 80 UV mesh (20480 panels), f = 60 kHz,
+    c = 1500 m/s: one factor, 181 incidence angles 0..180 deg (monostatic backscatter),
+    refined to a relative backward error of 1e-10; FP64 on the same factor path for the
+    per-angle error."""
+    import bemgpu
+    from bemgpu import meshes
+    ctx = bemgpu.Context(0)
+    nodes, tris = meshes.uv_spheroid(0.05, 0.0125, 128, 80)
+    surf = bemgpu.mesh(nodes, tris)
+    k = 2 * math.pi * 60e3 / 1500.0
+    angles = np.linspace(0.0, math.pi, 181)
+
+    def sweep(precision, **kw):
+        return bemgpu.incidence_angle_sweep(surf, bemgpu.Rigid(), k, angles,
+                                            precision=precision, ctx=ctx, **kw)
+
+    ref = dict(refinement=dict(tolerance=1e-10))
+    for _ in range(max(1, args.warmup)):
+        sweep("mixed", **ref)
+    clocks = Clocks(0)
+    clocks.start()
+    ctx.profile(True)
+    ctx.profile_reset()
+    l0 = bemgpu.Context.launch_count()
+    ts = []
+    for _ in range(args.steps):
+        ctx.timer_start()
+        sw = sweep("mixed", **ref)
+        ts.append(ctx.timer_stop())
+    launches = (bemgpu.Context.launch_count() - l0) // args.steps
+    prof = {fam: ctx.profile_read(fam)[1] / args.steps for fam in
+            ("assemble", "near", "getf2", "gemm_tc", "trsm", "gecon", "getrs", "residual",
+             "forcing", "far_field")}
+    ctx.profile(False)
+    clk = clocks.stop()
+    ctx.timer_start()
+    sw64 = sweep("double")
+    fp64_ms = ctx.timer_stop()
+    err = np.abs(sw.target_strength - sw64.target_strength)
+    ms = float(np.mean(ts))
+    line = _base_line(
+        "BEM solves/s, rigid spheroid 20480 panels x 181 angles (precision study)",
+        181 * 1e3 / ms, "solves/s", ms, args,
+        {"workload": "rigid prolate spheroid 0.05x0.0125 m, 20480 panels, f=60 kHz, "
+                     "181 incidence angles, refinement tolerance 1e-10", "panels": 20480,
+         "angles": 181},
+        dtype="c64 factor + fp64 refinement", phase_ms_per_step=prof,
+        fp64={"solves_per_s": 181 * 1e3 / fp64_ms, "ms": fp64_ms},
+        ts_error_db={"max": float(err.max()), "median": float(np.median(err))},
+        diagnostics={k2: (v if isinstance(v, (int, float, str)) else str(v))
+                     for k2, v in sw.diagnostics.items()},
+        target_strength_db=[round(float(v), 4) for v in sw.target_strength],
+        fp64_error_db_per_angle=[float(v) for v in err],
+        clocks=clk, gpu_launches=launches)
+    print(json.dumps(line))
+    return line
+
+
+def _uneven_batch(master, count, panel_range):
+    from bemgpu import meshes
+    bodies = []
+    for i in range(count):
+        b = meshes.random_body(master, i, panel_range)
+        nodes, tris = meshes.body_of_revolution(b["b"], b["aspect"], b["coeffs"], b["nlon"],
+                                                b["nrings"])
+        bodies.append((b, nodes, tris))
+    return bodies
+
+
+def _memory_groups(sizes, budget_bytes, per_unknown2):
+    """Consecutive groups whose summed n^2 * per_unknown2 stays within the budget."""
+    groups, cur, acc = [], [], 0.0
+    for i, n in enumerate(sizes):
+        b = n * n * per_unknown2
+        if cur and acc + b > budget_bytes:
+            groups.append(cur)
+            cur, acc = [], 0.0
+        cur.append(i)
+        acc += b
+    if cur:
+        groups.append(cur)
+    return groups
+
+
+def run_config3(args):
+    """256 seeded bodies of revolution (panels log-uniform 500..12000, f ~ U(10, 200) kHz,
+    incidence uniform on the sphere, rigid / pressure release 50/50, Burton-Miller),
+    assembled, factored and solved as uneven batches (grouped to a device-memory budget)."""
+    import bemgpu
+    ctx = bemgpu.Context(0)
+    count = args.bodies
+    bodies = _uneven_batch(SEED + 3, count, (500, 12000))
+    surfs = [bemgpu.mesh(nodes, tris) for _, nodes, tris in bodies]
+    for s_ in surfs:
+        s_.handle(ctx)
+    sizes = [s_.n_panels for s_ in surfs]
+    groups = _memory_groups(sizes, 90e9, 24.0 + 40.0 / 1e3)
+
+    def step(precision, idx):
+        amps = {}
+        for g in _memory_groups([sizes[i] for i in idx], 90e9, 24.0 if precision == "mixed"
+                                else 48.0):
+            ids = [idx[q] for q in g]
+            items = []
+            for i in ids:
+                b = bodies[i][0]
+                bc = bemgpu.Rigid() if b["boundary"] == "rigid" else bemgpu.PressureRelease()
+                items.append((surfs[i], bc, 2 * math.pi * b["frequency"] / 1500.0,
+                              dict(precision=precision)))
+            fs = bemgpu.factor_batch(items, ctx)
+            sols = bemgpu.solve_batch(fs, [[bodies[i][0]["incidence_angle"]] for i in ids],
+                                      [[bodies[i][0]["incidence_azimuth"]] for i in ids])
+            for i, s_ in zip(ids, sols):
+                amps[i] = bemgpu.scattering_amplitude(s_)
+                s_.close()
+            for f in fs:
+                f.close()
+        return amps
+
+    allidx = list(range(count))
+    for _ in range(max(1, args.warmup)):
+        step("mixed", allidx)
+    clocks = Clocks(0)
+    clocks.start()
+    l0 = bemgpu.Context.launch_count()
+    ts = []
+    for _ in range(args.steps):
+        ctx.timer_start()
+        am = step("mixed", allidx)
+        ts.append(ctx.timer_stop())
+    launches = (bemgpu.Context.launch_count() - l0) // args.steps
+    clk = clocks.stop()
+    order = np.argsort(sizes)
+    sub = [int(i) for i in order[:: max(1, count // 8)]][:8]
+    ctx.timer_start()
+    a64 = step("double", sub)
+    fp64_ms = ctx.timer_stop()
+    err = [abs(20 * math.log10(abs(am[i])) - 20 * math.log10(abs(a64[i]))) for i in sub]
+    ms = float(np.mean(ts))
+    line = _base_line(
+        "BEM solves/s, uneven batch of 256 bodies of revolution", count * 1e3 / ms, "solves/s",
+        ms, args,
+        {"workload": f"{count} seeded bodies of revolution, panels log-uniform 500-12000, "
+                     "f 10-200 kHz, rigid/soft 50/50, Burton-Miller", "bodies": count,
+         "panels_total": int(sum(sizes)), "panels_max": int(max(sizes)),
+         "memory_groups": len(groups), "seed": SEED + 3},
+        dtype="c64 factor + fp64 refinement",
+        fp64={"solves_per_s": len(sub) * 1e3 / fp64_ms, "bodies": len(sub),
+              "panels": [sizes[i] for i in sub]},
+        ts_error_db={"max": float(max(err)), "per_body": [float(e) for e in err]},
+        clocks=clk, gpu_launches=launches)
+    print(json.dumps(line))
+    return line
+
+
+def run_config4(args):
+    """Open-loop Poisson request stream into the continuous-batching server: bodies from
+    the uneven distribution (panels 500..16000), 1-32 frequencies and 1-64 incidence
+    angles per request; latency = completion - arrival."""
+    import bemgpu
+    from bemgpu import meshes
+    ctx = bemgpu.Context(0, hbm_budget_bytes=int(150e9))
+    nreq = args.requests
+    rng = np.random.default_rng(SEED + 4)
+    reqs = []
+    for i in range(nreq):
+        b = meshes.random_body(SEED + 4, i, (500, 16000))
+        nodes, tris = meshes.body_of_revolution(b["b"], b["aspect"], b["coeffs"], b["nlon"],
+                                                b["nrings"])
+        nf = int(rng.integers(1, 33))
+        na = int(rng.integers(1, 65))
+        f0 = b["frequency"]
+        freqs = f0 * (1.0 + 0.05 * np.arange(nf))
+        ang = rng.uniform(0.0, math.pi, size=na)
+        surf = bemgpu.mesh(nodes, tris)
+        surf.handle(ctx)  # meshes resident before the stream starts
+        reqs.append((b, surf, None, 2 * math.pi * freqs / 1500.0, ang))
+
+    def serve(precision, rate, subset):
+        srv = bemgpu.Server(ctx, max_batch=64, cache_bytes=int(40e9))
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(subset)))
+        tickets = []
+        t0 = time.perf_counter()
+        import threading as th
+        lat = {}
+
+        def waiter():
+            for tk, i in tickets_q:
+                out, ms = srv.wait(tk, timeout_ms=-1)
+                lat[i] = (ms, out)
+        tickets_q = []
+        for j, i in enumerate(subset):
+            now = time.perf_counter() - t0
+            if arrivals[j] > now:
+                time.sleep(arrivals[j] - now)
+            b, surf, _, ks, ang = reqs[i]
+            bc = bemgpu.Rigid() if b["boundary"] == "rigid" else bemgpu.PressureRelease()
+            tk = srv.submit(surf, bc, ks, ang, precision=precision)
+            tickets_q.append((tk, i))
+        wt = th.Thread(target=waiter)
+        wt.start()
+        wt.join()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        lats = np.array([lat[i][0] for i in subset])
+        solves = sum(len(reqs[i][3]) * len(reqs[i][4]) for i in subset)
+        return dict(wall_s=wall, solves=solves, solves_per_s=solves / wall,
+                    p50_ms=float(np.percentile(lats, 50)), p99_ms=float(np.percentile(lats, 99)),
+                    stats=st), {i: lat[i][1] for i in subset}
+
+    # calibrate the rate to ~70% of the closed-loop throughput on a warm-up subset
+    warm = list(range(min(8, nreq)))
+    res_w, _ = serve("mixed", 1e6, warm)
+    per_req = res_w["wall_s"] / len(warm)
+    rate = args.rate or 0.7 / max(per_req, 1e-3)
+    clocks = Clocks(0)
+    clocks.start()
+    res_m, out_m = serve("mixed", rate, list(range(nreq)))
+    clk = clocks.stop()
+    # FP64 arm on the six smallest requests (panels x frequencies): the FP64 LU runs at
+    # the GB300's FP64 rate, far below its tensor-core throughput
+    cost = [reqs[i][1].n_panels ** 3 * len(reqs[i][3]) for i in range(nreq)]
+    sub = [int(i) for i in np.argsort(cost)[:6]]
+    res_d, out_d = serve("double", 1e6, sub)
+    err = []
+    for i in sub:
+        a, b2 = out_m[i], out_d[i]
+        err.append(float(np.max(np.abs(20 * np.log10(np.abs(a)) - 20 * np.log10(np.abs(b2))))))
+    line = _base_line(
+        "BEM solves/s & p99 latency, served Poisson stream", res_m["solves_per_s"], "solves/s",
+        res_m["wall_s"] * 1e3, args,
+        {"workload": f"{nreq} Poisson requests, bodies of revolution 500-16000 panels, 1-32 "
+                     "frequencies, 1-64 angles, continuous batching with a factor cache",
+         "requests": nreq, "rate_per_s": rate, "seed": SEED + 4},
+        dtype="c64 factor + fp64 refinement",
+        latency_ms={"p50": res_m["p50_ms"], "p99": res_m["p99_ms"]},
+        server=res_m["stats"],
+        fp64_closed_loop={"requests": len(sub), "solves_per_s": res_d["solves_per_s"],
+                          "p50_ms": res_d["p50_ms"], "p99_ms": res_d["p99_ms"]},
+        ts_error_db={"max": max(err), "requests": len(sub)}, clocks=clk)
+    print(json.dumps(line))
+    return line
+
+
 # ------------------------------------------------------------------ CPU baseline
 def _oracle_one(k, nodes, tris, precision):
     from oracle import oracle as O
@@ -365,11 +683,19 @@ def main():
     ap.add_argument("--nlon", type=int, default=W["nlon"])
     ap.add_argument("--nrings", type=int, default=W["nrings"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3, 4],
+                    help="workload: 1 = headline batched frequency sweep (default); 0 rigid "
+                         "sphere; 2 large single solve x 181 angles; 3 uneven batch; 4 serving")
+    ap.add_argument("--bodies", type=int, default=256, help="config 3: bodies")
+    ap.add_argument("--requests", type=int, default=200, help="config 4: requests")
+    ap.add_argument("--rate", type=float, default=0.0, help="config 4: arrivals/s (0: 70%% load)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
-    else:
+    elif args.config == 1:
         run_ours(args)
+    else:
+        {0: run_config0, 2: run_config2, 3: run_config3, 4: run_config4}[args.config](args)
 
 
 if __name__ == "__main__":
