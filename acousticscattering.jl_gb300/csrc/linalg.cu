@@ -934,72 +934,118 @@ __global__ void __launch_bounds__(kDiagThreads) k_trsv_diag(const MatInst* __res
 
 // Rows outside the solved block [r0, r0 + kBigB): x_r -= sum_c op(A)[r, c] x_c, one
 // thread per row, the block's solution in shared memory (op(A) = A, coalesced along r).
-template <typename R, bool EFF_LOWER, bool TRANS>
+// RG right-hand sides per CTA share every matrix element a thread loads, so a sweep's
+// many right-hand sides read the factor once per group instead of once each.
+template <typename R, int RG>
+constexpr size_t upd_smem_bytes() {
+  return sizeof(cx<R>) * (size_t)RG * kBigB;
+}
+
+template <typename R, bool EFF_LOWER, bool TRANS, int RG>
 __global__ void __launch_bounds__(256) k_trsv_big_update(const MatInst* __restrict__ insts,
                                                          int64_t r0) {
   const MatInst& M = insts[blockIdx.z];
-  const int rhs = blockIdx.y;
+  const int rg0 = blockIdx.y * RG;
   const int64_t n = M.n;
-  if (!M.active || rhs >= M.nrhs || r0 >= n) return;
+  if (!M.active || rg0 >= M.nrhs || r0 >= n) return;
+  const int nr = min(RG, M.nrhs - rg0);
   const int nbs = (int)min((int64_t)kBigB, n - r0);
-  const int64_t lda = M.lda, off = (int64_t)rhs * M.ldx;
-  __shared__ cx<R> sx[kBigB];
-  for (int i = threadIdx.x; i < nbs; i += blockDim.x) sx[i] = ld<R>(M.x, off + r0 + i);
+  const int64_t lda = M.lda, ldx = M.ldx;
+  extern __shared__ __align__(16) unsigned char upd_smem[];
+  cx<R>* sx = reinterpret_cast<cx<R>*>(upd_smem);  // [RG][kBigB]
+  for (int r = 0; r < nr; ++r)
+    for (int i = threadIdx.x; i < nbs; i += blockDim.x)
+      sx[r * kBigB + i] = ld<R>(M.x, (int64_t)(rg0 + r) * ldx + r0 + i);
   __syncthreads();
   int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (EFF_LOWER) row += r0 + nbs;
   if (EFF_LOWER ? row >= n : row >= r0) return;
-  cx<R> acc = {0, 0};
+  cx<R> acc[RG];
+#pragma unroll
+  for (int r = 0; r < RG; ++r) acc[r] = cx<R>{0, 0};
   for (int c0 = 0; c0 < nbs; c0 += 8) {
     cx<R> lv[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c)
       lv[c] = (c0 + c < nbs) ? opel<R, TRANS>(M.a, lda, row, r0 + c0 + c) : cx<R>{0, 0};
 #pragma unroll
-    for (int c = 0; c < 8; ++c)
-      if (c0 + c < nbs) acc += lv[c] * sx[c0 + c];
+    for (int c = 0; c < 8; ++c) {
+      if (c0 + c < nbs) {
+#pragma unroll
+        for (int r = 0; r < RG; ++r)
+          if (r < nr) acc[r] += lv[c] * sx[r * kBigB + c0 + c];
+      }
+    }
   }
-  st<R>(M.x, off + row, ld<R>(M.x, off + row) - acc);
+#pragma unroll
+  for (int r = 0; r < RG; ++r) {
+    if (r < nr) {
+      const int64_t o = (int64_t)(rg0 + r) * ldx + row;
+      st<R>(M.x, o, ld<R>(M.x, o) - acc[r]);
+    }
+  }
 }
 
 // The same update for op(A) = A^H: x_r -= sum_c conj(A[c, r]) x_c reads column r of A,
 // so a warp takes 4 rows with its lanes along c (coalesced), then reduces by shuffles.
 constexpr int kTrUpRows = 32;  // rows per 256-thread CTA (8 warps x 4)
-template <typename R, bool EFF_LOWER>
+template <typename R, bool EFF_LOWER, int RG>
 __global__ void __launch_bounds__(256) k_trsv_big_update_h(const MatInst* __restrict__ insts,
                                                            int64_t r0) {
   const MatInst& M = insts[blockIdx.z];
-  const int rhs = blockIdx.y;
+  const int rg0 = blockIdx.y * RG;
   const int64_t n = M.n;
-  if (!M.active || rhs >= M.nrhs || r0 >= n) return;
+  if (!M.active || rg0 >= M.nrhs || r0 >= n) return;
+  const int nr = min(RG, M.nrhs - rg0);
   const int nbs = (int)min((int64_t)kBigB, n - r0);
-  const int64_t lda = M.lda, off = (int64_t)rhs * M.ldx;
-  __shared__ cx<R> sx[kBigB];
-  for (int i = threadIdx.x; i < nbs; i += blockDim.x) sx[i] = ld<R>(M.x, off + r0 + i);
+  const int64_t lda = M.lda, ldx = M.ldx;
+  extern __shared__ __align__(16) unsigned char upd_smem[];
+  cx<R>* sx = reinterpret_cast<cx<R>*>(upd_smem);  // [RG][kBigB]
+  for (int r = 0; r < nr; ++r)
+    for (int i = threadIdx.x; i < nbs; i += blockDim.x)
+      sx[r * kBigB + i] = ld<R>(M.x, (int64_t)(rg0 + r) * ldx + r0 + i);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int64_t row0 = (int64_t)blockIdx.x * kTrUpRows + warp * 4;
   if (EFF_LOWER) row0 += r0 + nbs;
   const int64_t lim = EFF_LOWER ? n : r0;
   if (row0 >= lim) return;
-  cx<R> acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+  cx<R> acc[4][RG];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int r = 0; r < RG; ++r) acc[u][r] = cx<R>{0, 0};
   for (int c = lane; c < nbs; c += 32) {
-    const cx<R> xv = sx[c];
     cx<R> v[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u)
-      v[u] = (row0 + u < lim) ? ld<R>(M.a, (r0 + c) + (row0 + u) * lda) : cx<R>{0, 0};
+      v[u] = (row0 + u < lim) ? cconj(ld<R>(M.a, (r0 + c) + (row0 + u) * lda)) : cx<R>{0, 0};
 #pragma unroll
-    for (int u = 0; u < 4; ++u) acc[u] += cconj(v[u]) * xv;
+    for (int r = 0; r < RG; ++r) {
+      if (r < nr) {
+        const cx<R> xv = sx[r * kBigB + c];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc[u][r] += v[u] * xv;
+      }
+    }
   }
 #pragma unroll
   for (int u = 0; u < 4; ++u) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      acc[u].x += __shfl_xor_sync(0xffffffffu, acc[u].x, o);
-      acc[u].y += __shfl_xor_sync(0xffffffffu, acc[u].y, o);
+    for (int r = 0; r < RG; ++r) {
+      if (r < nr) {
+        cx<R> t = acc[u][r];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          t.x += __shfl_xor_sync(0xffffffffu, t.x, o);
+          t.y += __shfl_xor_sync(0xffffffffu, t.y, o);
+        }
+        if (lane == 0 && row0 + u < lim) {
+          const int64_t o2 = (int64_t)(rg0 + r) * ldx + row0 + u;
+          st<R>(M.x, o2, ld<R>(M.x, o2) - t);
+        }
+      }
     }
-    if (lane == 0 && row0 + u < lim) st<R>(M.x, off + row0 + u, ld<R>(M.x, off + row0 + u) - acc[u]);
   }
 }
 
@@ -1201,6 +1247,17 @@ static void trsv_big_t(const Launch& L, const MatInst* d, int ninst, int64_t nma
                          (int)smem);
     attr = true;
   }
+  // right-hand sides per update CTA: one, or a group sharing the matrix loads
+  constexpr int RG = sizeof(R) == 4 ? 8 : 4;
+  const bool grouped = max_rhs >= 4;
+  static bool uattr = false;
+  if (!uattr) {
+    cudaFuncSetAttribute(k_trsv_big_update<R, EL, TR, RG>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem_bytes<R, RG>());
+    cudaFuncSetAttribute(k_trsv_big_update_h<R, EL, RG>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem_bytes<R, RG>());
+    uattr = true;
+  }
   const int64_t nblk = (nmax + kBigB - 1) / kBigB;
   for (int64_t b = 0; b < nblk; ++b) {
     const int64_t blk = EL ? b : nblk - 1 - b;
@@ -1210,14 +1267,20 @@ static void trsv_big_t(const Launch& L, const MatInst* d, int ninst, int64_t nma
     count_launch(1);
     const int64_t rows = EL ? (nmax - r0 - kBigB) : r0;
     if (rows > 0) {
-      if (TR)
-        k_trsv_big_update_h<R, EL><<<dim3((unsigned)((rows + kTrUpRows - 1) / kTrUpRows),
-                                          (unsigned)max_rhs, (unsigned)ninst),
-                                     256, 0, L.stream>>>(d, r0);
-      else
-        k_trsv_big_update<R, EL, TR><<<dim3((unsigned)((rows + 255) / 256), (unsigned)max_rhs,
-                                            (unsigned)ninst),
-                                       256, 0, L.stream>>>(d, r0);
+      const unsigned gy = grouped ? (unsigned)((max_rhs + RG - 1) / RG) : (unsigned)max_rhs;
+      if (TR) {
+        const dim3 g((unsigned)((rows + kTrUpRows - 1) / kTrUpRows), gy, (unsigned)ninst);
+        if (grouped)
+          k_trsv_big_update_h<R, EL, RG><<<g, 256, upd_smem_bytes<R, RG>(), L.stream>>>(d, r0);
+        else
+          k_trsv_big_update_h<R, EL, 1><<<g, 256, upd_smem_bytes<R, 1>(), L.stream>>>(d, r0);
+      } else {
+        const dim3 g((unsigned)((rows + 255) / 256), gy, (unsigned)ninst);
+        if (grouped)
+          k_trsv_big_update<R, EL, TR, RG><<<g, 256, upd_smem_bytes<R, RG>(), L.stream>>>(d, r0);
+        else
+          k_trsv_big_update<R, EL, TR, 1><<<g, 256, upd_smem_bytes<R, 1>(), L.stream>>>(d, r0);
+      }
       count_launch(1);
     }
   }

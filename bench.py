@@ -585,8 +585,9 @@ def run_config4(args):
                     p50_ms=float(np.percentile(lats, 50)), p99_ms=float(np.percentile(lats, 99)),
                     stats=st), {i: lat[i][1] for i in subset}
 
-    # calibrate the rate to ~70% of the closed-loop throughput on a warm-up subset
-    warm = list(range(min(8, nreq)))
+    # offered load: 70% of the closed-loop capacity measured on a random quarter of the
+    # requests (all submitted at once)
+    warm = sorted(int(i) for i in rng.choice(nreq, size=max(1, nreq // 4), replace=False))
     res_w, _ = serve("mixed", 1e6, warm)
     per_req = res_w["wall_s"] / len(warm)
     rate = args.rate or 0.7 / max(per_req, 1e-3)
