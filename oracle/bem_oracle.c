@@ -359,6 +359,29 @@ int oracle_assemble_bm(const or_panel *P, int64_t n, double eta, double k, int b
 }
 
 /*
+ * The four raw operators S, D, K', H of every panel pair (target i, source j) at one
+ * wavenumber, column-major n x n interleaved complex each.  The multi-region restatement
+ * combines blocks of these (solvers/bem/regions.jl:189-236).
+ */
+int oracle_assemble_ops(const or_panel *P, int64_t n, double eta, double k, double *S,
+                        double *D, double *K, double *H) {
+  double eta2 = eta * eta;
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t j = 0; j < n; ++j) {
+    for (int64_t i = 0; i < n; ++i) {
+      or_ops o;
+      pair_ops(P, i, j, is_near(P, i, j, eta2), k, &o);
+      int64_t idx = 2 * (i + j * n);
+      S[idx] = creal(o.S); S[idx + 1] = cimag(o.S);
+      D[idx] = creal(o.D); D[idx + 1] = cimag(o.D);
+      K[idx] = creal(o.K); K[idx + 1] = cimag(o.K);
+      H[idx] = creal(o.H); H[idx + 1] = cimag(o.H);
+    }
+  }
+  return 0;
+}
+
+/*
  * Fluid system, column-major 2n x 2n interleaved complex.
  * formulation 0: Mueller, 1: CBIE.  k_int = k / h.
  */

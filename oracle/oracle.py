@@ -57,6 +57,8 @@ def lib():
         L.oracle_assemble_fluid.argtypes = [vp, i64, ctypes.c_double, ctypes.c_double,
                                             ctypes.c_double, ctypes.c_double,
                                             ctypes.c_int, dp]
+        L.oracle_assemble_ops.argtypes = [vp, i64, ctypes.c_double, ctypes.c_double,
+                                          dp, dp, dp, dp]
         L.oracle_incident.argtypes = [vp, i64, ctypes.c_double, dp, dp, dp]
         L.oracle_far_field.argtypes = [vp, i64, ctypes.c_double, dp, dp, dp, dp]
         L.oracle_pair_ops.argtypes = [vp, i64, i64, ctypes.c_int, ctypes.c_double, dp]
@@ -151,6 +153,96 @@ def assemble_fluid(P: Panels, k, g, h, formulation="muller", eta=NEAR_ETA):
                                 0 if formulation == "muller" else 1,
                                 _dp(A))
     return A
+
+
+def assemble_ops(P: Panels, k, eta=NEAR_ETA):
+    """Raw S, D, K', H (n x n each) of all panel pairs at wavenumber k."""
+    n = P.n
+    out = [np.zeros((n, n), dtype=np.complex128, order="F") for _ in range(4)]
+    lib().oracle_assemble_ops(P.ptr, n, eta, float(k), *[_dp(m) for m in out])
+    return out
+
+
+def combined_panels(surfaces):
+    """One panel set over several closed surfaces (each (nodes, triangles), 1-based),
+    panels in surface order; returns (Panels, panel offsets)."""
+    nodes, tris, offs, base = [], [], [0], 0
+    for nd, tr in surfaces:
+        nodes.append(np.asarray(nd, dtype=np.float64))
+        tris.append(np.asarray(tr, dtype=np.int64) + base)
+        base += nd.shape[1]
+        offs.append(offs[-1] + tr.shape[1])
+    return Panels(np.concatenate(nodes, axis=1), np.concatenate(tris, axis=1)), offs
+
+
+def assemble_regions(surfaces, materials, parents, k, formulation="muller", eta=NEAR_ETA):
+    """Coupled fluid regions (solvers/bem/regions.jl:189-236): surface i (1-based) encloses
+    region i, parents[i-1] is the region outside it (0 = exterior); materials[i-1] =
+    (density, sound speed) contrasts of region i relative to the exterior.  Returns the
+    2n x 2n system, the combined panels and the panel offsets."""
+    P, offs = combined_panels(surfaces)
+    n = P.n
+    count = len(surfaces)
+    dens = [1.0] + [float(m[0]) for m in materials]
+    speeds = [1.0] + [float(m[1]) for m in materials]
+    ops = {}
+
+    def region_ops(r):
+        if r not in ops:
+            ops[r] = assemble_ops(P, k / speeds[r], eta)
+        return ops[r]
+
+    A = np.eye(2 * n, dtype=np.complex128) if formulation == "muller" else \
+        np.zeros((2 * n, 2 * n), dtype=np.complex128)
+    for i in range(1, count + 1):
+        rows = np.arange(offs[i - 1], offs[i])
+        for region in (i, parents[i - 1]):
+            rho = dens[region]
+            S, D, K, H = region_ops(region)
+            eqs = rows + n if region == i else rows
+            if formulation == "cbie":
+                A[np.ix_(eqs, rows)] += 0.5 * np.eye(len(rows))
+            for j in range(1, count + 1):
+                if not (j == region or parents[j - 1] == region):
+                    continue
+                sign = 1.0 if j == region else -1.0
+                cols = np.arange(offs[j - 1], offs[j])
+                blk = np.ix_(rows, cols)
+                if formulation == "cbie":
+                    A[np.ix_(eqs, cols)] += sign * D[blk]
+                    A[np.ix_(eqs, cols + n)] -= sign * rho * S[blk]
+                    continue
+                A[np.ix_(rows, cols)] += sign * D[blk]
+                A[np.ix_(rows, cols + n)] -= sign * rho * S[blk]
+                A[np.ix_(rows + n, cols)] += (sign / rho) * H[blk]
+                A[np.ix_(rows + n, cols + n)] -= sign * K[blk]
+    return A, P, offs
+
+
+def solve_regions(surfaces, materials, parents, k, incidence_angle=math.pi / 2,
+                  incidence_azimuth=0.0, formulation="muller", eta=NEAR_ETA):
+    """FP64 dense solve of the coupled-region system with the exterior plane wave on the
+    surfaces that border the exterior (regions.jl:240-253), and the backscatter amplitude
+    summed over those surfaces (solvers/bem/postprocessing.jl:15-31)."""
+    A, P, offs = assemble_regions(surfaces, materials, parents, k, formulation, eta)
+    n = P.n
+    d = incidence_direction(incidence_angle, incidence_azimuth)
+    pinc, qinc = incident(P, k, d)
+    b = np.zeros(2 * n, dtype=np.complex128)
+    outer = np.zeros(n, dtype=bool)
+    for i in range(1, len(surfaces) + 1):
+        if parents[i - 1] == 0:
+            sl = slice(offs[i - 1], offs[i])
+            outer[sl] = True
+            b[sl] = pinc[sl]
+            if formulation == "muller":
+                b[n + offs[i - 1]:n + offs[i]] = qinc[sl]
+    x = np.linalg.solve(A, b)
+    p_tot, v = x[:n], x[n:]
+    ps = np.where(outer, p_tot - pinc, 0.0)
+    qs = np.where(outer, v - qinc, 0.0)  # exterior density is 1
+    amp = far_field(P, k, -d, ps, qs)
+    return dict(A=A, b=b, x=x, amplitude=amp, p_scat=ps, dpdn_scat=qs, panels=P, offsets=offs)
 
 
 def incident(P: Panels, k, direction):

@@ -216,3 +216,27 @@ def test_rotation_invariance():
     b = O.solve(R @ nodes, tris, "rigid", 2.0, incidence_angle=beta, incidence_azimuth=alpha,
                 directions=[R @ obs])["amplitudes"][0]
     assert abs(a - b) / abs(a) < 1e-9
+
+
+def test_region_assembly_single_surface_equals_fluid():
+    """One interface through the coupled-region assembly (regions.jl:189-236) is the
+    single-interface fluid system (full.jl:289-346), for both formulations."""
+    nodes, tris = meshes.icosphere(1.0, 1)
+    P = O.Panels(nodes, tris)
+    for form in ("muller", "cbie"):
+        A, _, _ = O.assemble_regions([(nodes, tris)], [(1.07, 1.04)], [0], 1.3, form)
+        B = O.assemble_fluid(P, 1.3, 1.07, 1.04, form)
+        assert np.max(np.abs(A - B)) <= 1e-13 * np.max(np.abs(B))
+
+
+def test_region_transparent_inner_interface():
+    """A nested interface whose region has its parent's material is invisible in the
+    continuum: the coupled result matches the single interface to discretisation level."""
+    outer = meshes.icosphere(1.0, 2)
+    inner = meshes.icosphere(0.5, 2)
+    k = 1.2
+    one = O.solve_regions([outer], [(1.05, 1.03)], [0], k, incidence_angle=0.3)
+    two = O.solve_regions([outer, inner], [(1.05, 1.03), (1.05, 1.03)], [0, 1], k,
+                          incidence_angle=0.3)
+    rel = abs(two["amplitude"] - one["amplitude"]) / abs(one["amplitude"])
+    assert rel < 1e-3, rel
