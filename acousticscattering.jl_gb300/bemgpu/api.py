@@ -413,8 +413,24 @@ class BEMSolution:
                self.ctx.handle)
         return out
 
+    @property
+    def n_panels(self) -> int:
+        if isinstance(self.body, (list, tuple)):
+            return sum(s.n_panels for s in self.body)
+        return self.body.n_panels
+
+    def region_traces(self, rhs: int = 0):
+        """Coupled regions: total pressure p and flux unknown v on every panel, surfaces in
+        order (the interior normal derivative is density_i v)."""
+        n = self.n_panels
+        p = np.zeros(n, dtype=np.complex128)
+        v = np.zeros(n, dtype=np.complex128)
+        _check(C.lib().bemgpu_region_traces(self.handle, rhs, C.dptr(p), C.dptr(v)),
+               self.ctx.handle)
+        return p, v
+
     def traces(self, rhs: int = 0):
-        n = self.body.n_panels
+        n = self.n_panels
         p = np.zeros(n, dtype=np.complex128)
         q = np.zeros(n, dtype=np.complex128)
         _check(C.lib().bemgpu_traces(self.handle, rhs, C.dptr(p), C.dptr(q)), self.ctx.handle)
@@ -441,6 +457,10 @@ class BEMSolution:
     def diagnostics(self) -> dict:
         d = C.Diagnostics()
         _check(C.lib().bemgpu_solution_diagnostics(self.handle, ctypes.byref(d)))
+        if isinstance(self.body, (list, tuple)):  # coupled regions
+            return _diag_dict(d, {"meshsize": max(s_.resolution for s_ in self.body),
+                                  "illumination": "plane_wave", "interface_count": len(self.body),
+                                  "mesh_hash": [s_.hash for s_ in self.body]})
         return _diag_dict(d, {"meshsize": self.body.resolution,
                               "illumination": "plane_wave", "mesh_hash": self.body.hash})
 
@@ -459,10 +479,21 @@ class BEMSolution:
 # ------------------------------------------------------------------ reference-named API
 def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_azimuth=0.0,
         formulation=None, precision="double", equilibrate=True, refinement=None,
-        assembly=None, ctx: Context | None = None, **unsupported) -> BEMSolution:
-    """Full-3D BEM on a supplied surface (solvers/bem/surface.jl:10-23)."""
+        assembly=None, ctx: Context | None = None, parents=None,
+        **unsupported) -> BEMSolution:
+    """Full-3D BEM on a supplied surface (solvers/bem/surface.jl:10-23), or, given lists of
+    surfaces and FluidFilled materials, the coupled fluid regions of
+    bem(surfaces, materials, k; parents) (solvers/bem/regions.jl:132-150)."""
     if unsupported:
         raise ArgumentError(f"unsupported option(s): {sorted(unsupported)}")
+    if isinstance(surface, (list, tuple)):
+        return _bem_regions(list(surface), boundary, k, parents=parents,
+                            incidence_angle=incidence_angle,
+                            incidence_azimuth=incidence_azimuth, formulation=formulation,
+                            precision=precision, equilibrate=equilibrate,
+                            refinement=refinement, assembly=assembly, ctx=ctx)
+    if parents is not None:
+        raise ArgumentError("parents applies to lists of surfaces and materials")
     if not isinstance(surface, Mesh):
         raise ArgumentError("surface must be a Mesh from mesh(nodes, triangles)")
     if not (math.isfinite(incidence_angle) and math.isfinite(incidence_azimuth)):
@@ -476,6 +507,45 @@ def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_az
         return f.solve([incidence_angle], [incidence_azimuth])
     finally:
         f.close()
+
+
+def _bem_regions(surfaces, materials, k, *, parents, incidence_angle, incidence_azimuth,
+                 formulation, precision, equilibrate, refinement, assembly, ctx):
+    ctx = ctx or context()
+    count = len(surfaces)
+    if count == 0:
+        raise ArgumentError("at least one interface is required")
+    materials = list(materials) if isinstance(materials, (list, tuple)) else None
+    if materials is None or len(materials) != count:
+        raise ArgumentError("supply one material and parent per interface")
+    if not all(isinstance(s_, Mesh) for s_ in surfaces):
+        raise ArgumentError("each interface must be a Mesh from mesh(nodes, triangles)")
+    if not all(isinstance(m, FluidFilled) for m in materials):
+        raise ArgumentError("materials must be FluidFilled")
+    parents = list(range(count)) if parents is None else [int(p) for p in parents]
+    if len(parents) != count:
+        raise ArgumentError("supply one material and parent per interface")
+    if not all(0 <= parents[i] <= i for i in range(count)):
+        raise ArgumentError("each parent must be zero or an earlier region index")
+    if formulation not in (None, "muller", "cbie"):
+        raise ArgumentError("formulation must be :muller or :cbie")
+    if not (math.isfinite(incidence_angle) and math.isfinite(incidence_azimuth)):
+        raise ArgumentError("incidence angles must be finite")
+    # the problem fields that apply (boundary and contrasts are per region)
+    p = _problem(FluidFilled(1.0, 1.0), float(k), formulation=formulation,
+                 precision=precision, equilibrate=equilibrate, refinement=refinement,
+                 assembly=assembly)
+    handles = (ctypes.c_void_p * count)(*[s_.handle(ctx) for s_ in surfaces])
+    dens = np.array([m.density_contrast for m in materials], dtype=np.float64)
+    speeds = np.array([m.soundspeed_contrast for m in materials], dtype=np.float64)
+    par = (ctypes.c_int32 * count)(*parents)
+    inc = np.array([incidence_angle, incidence_azimuth], dtype=np.float64)
+    out = ctypes.c_void_p()
+    _check(C.lib().bemgpu_region_solve(ctx.handle, count, handles, C.dptr(dens), C.dptr(speeds),
+                                       par, ctypes.byref(p), 1, C.dptr(inc), ctypes.byref(out)),
+           ctx.handle)
+    return BEMSolution(ctx, out, list(surfaces), list(materials), float(k), [incidence_angle],
+                       [incidence_azimuth])
 
 
 def factor_batch(items, ctx: Context | None = None):

@@ -266,6 +266,10 @@ struct MeshData {
   Buf panels, panelsf, verts, near_i, near_j, near_ptr, near_lap;
   int64_t n_near = 0;
   double eta = 2.0;
+  std::vector<double> nodes_h;   // the surface as supplied (3 x nn, 1-based triangles)
+  std::vector<int64_t> tris_h;
+  Buf surf;                      // union of several surfaces: surface of every panel
+  std::vector<int64_t> offsets;  // union: first panel of every surface (+ total)
 };
 }  // namespace
 
@@ -346,6 +350,8 @@ int make_mesh(bemgpu_ctx* c, const double* nodes, int64_t N, const int64_t* tris
   m->resolution = res;
   m->eta = eta;
   mesh_hash(nodes, N, tris, M, m->hash);
+  m->nodes_h.assign(nodes, nodes + 3 * N);
+  m->tris_h.assign(tris, tris + 3 * M);
   std::vector<float> recf;
   std::vector<double> verts;
   build_panels(nodes, tris, M, &m->panels_h, &recf, &verts, m->center);
@@ -378,6 +384,89 @@ int make_mesh(bemgpu_ctx* c, const double* nodes, int64_t N, const int64_t* tris
 }
 }  // namespace
 
+// The union of several validated surfaces as one panel set (each surface was validated
+// on its own upload; the union is not one closed surface): panels in surface order, FP32
+// records relative to the union's centre, near pairs over all surfaces (a close pair of
+// surfaces gets its cross near pairs), the surface of every panel.
+int make_union_mesh(bemgpu_ctx* c, const std::vector<const MeshData*>& parts, double eta,
+                    std::shared_ptr<MeshData>* out) {
+  std::vector<double> nodes;
+  std::vector<int64_t> tris;
+  std::vector<int32_t> surf;
+  auto m = std::make_shared<MeshData>();
+  int64_t base = 0;
+  m->offsets.push_back(0);
+  for (size_t s = 0; s < parts.size(); ++s) {
+    const MeshData* p = parts[s];
+    nodes.insert(nodes.end(), p->nodes_h.begin(), p->nodes_h.end());
+    for (int64_t t : p->tris_h) tris.push_back(t + base);
+    base += p->nn;
+    for (int64_t q = 0; q < p->n; ++q) surf.push_back((int32_t)s);
+    m->offsets.push_back(m->offsets.back() + p->n);
+    m->resolution = std::max(m->resolution, p->resolution);
+  }
+  const int64_t N = base, M = (int64_t)tris.size() / 3;
+  m->c = c;
+  m->n = M;
+  m->nn = N;
+  m->eta = eta;
+  mesh_hash(nodes.data(), N, tris.data(), M, m->hash);
+  m->nodes_h = nodes;
+  m->tris_h = tris;
+  std::vector<float> recf;
+  std::vector<double> verts;
+  build_panels(nodes.data(), tris.data(), M, &m->panels_h, &recf, &verts, m->center);
+  std::vector<double> cent, diam;
+  panel_centroids(nodes.data(), tris.data(), M, &cent, &diam);
+  std::vector<int64_t> rowptr, cols;
+  near_pairs(cent, diam, eta, &rowptr, &cols);
+  std::vector<int32_t> ni(cols.size()), nj(cols.size());
+  for (int64_t i = 0; i < M; ++i)
+    for (int64_t p = rowptr[i]; p < rowptr[i + 1]; ++p) {
+      ni[p] = (int32_t)i;
+      nj[p] = (int32_t)cols[p];
+    }
+  m->n_near = (int64_t)cols.size();
+  std::vector<int32_t> np(rowptr.begin(), rowptr.end());
+  TRY(upload(c, m->panels_h, &m->panels));
+  TRY(upload(c, recf, &m->panelsf));
+  TRY(upload(c, verts, &m->verts));
+  TRY(upload(c, ni, &m->near_i));
+  TRY(upload(c, nj, &m->near_j));
+  TRY(upload(c, np, &m->near_ptr));
+  TRY(upload(c, surf, &m->surf));
+  TRY(alloc(c, (size_t)std::max<int64_t>(1, m->n_near) * 32, &m->near_lap));
+  launch_near_laplace(c->launch(), m->panels.as<double>(), m->verts.as<double>(),
+                      m->near_i.as<int32_t>(), m->near_j.as<int32_t>(), m->n_near,
+                      m->near_lap.as<double>());
+  CUDA_TRY(c, cudaGetLastError());
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  *out = m;
+  return BEMGPU_OK;
+}
+
+// Solid angle of a closed surface (host, FP64) seen from x: 4 pi inside, 0 outside.
+double host_solid_angle(const MeshData* m, const double* x) {
+  double om = 0.0;
+  for (int64_t t = 0; t < m->n; ++t) {
+    const double* v[3];
+    for (int a = 0; a < 3; ++a) v[a] = &m->nodes_h[3 * (m->tris_h[3 * t + a] - 1)];
+    double R[3][3], r[3];
+    for (int a = 0; a < 3; ++a) {
+      for (int d = 0; d < 3; ++d) R[a][d] = v[a][d] - x[d];
+      r[a] = std::sqrt(R[a][0] * R[a][0] + R[a][1] * R[a][1] + R[a][2] * R[a][2]);
+    }
+    const double cx = R[1][1] * R[2][2] - R[1][2] * R[2][1];
+    const double cy = R[1][2] * R[2][0] - R[1][0] * R[2][2];
+    const double cz = R[1][0] * R[2][1] - R[1][1] * R[2][0];
+    const double num = R[0][0] * cx + R[0][1] * cy + R[0][2] * cz;
+    auto dot = [&](int a, int b) { return R[a][0] * R[b][0] + R[a][1] * R[b][1] + R[a][2] * R[b][2]; };
+    const double den = r[0] * r[1] * r[2] + dot(0, 1) * r[2] + dot(0, 2) * r[1] + dot(1, 2) * r[0];
+    om += 2.0 * std::atan2(num, den);
+  }
+  return om;
+}
+
 // ===================================================================== factors
 namespace {
 struct FactorData {
@@ -391,6 +480,9 @@ struct FactorData {
   bool a32 = false;        // system stored compact: complex64 + FP64 near corrections
   Buf dnear;               // near corrections of the compact system
   Buf dnear_rhs;           // near corrections of the compact rhs operator (a32, rigid/soft)
+  Buf region_tab;          // kAsmRegion: RegionTable
+  Buf outer;               // kAsmRegion: panel borders the exterior (int8)
+  bool region_cbie = false;
   Buf LU, ipiv, info, perm;        // working factor (complex64 when single)
   Buf LU64, ipiv64, info64, perm64;  // complex128 factor after promotion
   Buf rows, cols, rowsum, cols_inv, rows_inv, cols_inv32;
@@ -426,6 +518,8 @@ struct SolutionData {
   int32_t nrhs = 0;
   std::vector<double> dirs;  // incidence direction vectors, 3 per rhs
   Buf ps, qs;                // scattered traces, complex128 n x nrhs
+  Buf xsol;                  // coupled regions: the solved unknowns [p; v], 2n x nrhs
+  bool region = false;
   bemgpu_diagnostics diag{};
 };
 }  // namespace
@@ -493,7 +587,7 @@ int assemble_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
   for (size_t t = 0; t < fs.size(); ++t) {
     FactorData* f = fs[t];
     MeshData* m = f->mesh.get();
-    const bool fluid = f->kind == kAsmMuller || f->kind == kAsmFluidCBIE;
+    const bool fluid = f->kind == kAsmMuller || f->kind == kAsmFluidCBIE || f->kind == kAsmRegion;
     f->n = m->n;
     f->N = fluid ? 2 * m->n : m->n;
     f->a32 = f->fp32_regular;
@@ -530,6 +624,10 @@ int assemble_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
       I.out1 = f->rhs_is_m2 ? f->A.p : f->Mrhs.p;
       I.out2 = f->rhs_is_m2 ? f->Mrhs.p : f->A.p;
       I.c64 = f->a32 ? 3 : 0;
+    }
+    if (f->kind == kAsmRegion) {
+      I.surf = m->surf.as<int32_t>();
+      I.region = f->region_tab.as<RegionTable>();
     }
     if (f->a32) {
       double* sysd = f->dnear.as<double>();
@@ -1519,7 +1617,12 @@ int solve_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<i
         tr.qinc = s.qinc.as<double>();
         tr.n = f->n;
         tr.nrhs = s.R;
-        tr.ps = f->kind == kAsmMuller ? s.b.as<double>() : s.x.as<double>();
+        tr.ps = (f->kind == kAsmMuller || f->kind == kAsmRegion) ? s.b.as<double>()
+                                                                 : s.x.as<double>();
+        if (f->kind == kAsmRegion) {  // plane wave on the surfaces bordering the exterior
+          tr.outer = f->outer.as<int8_t>();
+          tr.stack_q = f->region_cbie ? 0 : 1;
+        }
         stack.push_back(tr);
         if (f->kind == kAsmFluidCBIE) {
           VecInst v;
@@ -1685,7 +1788,9 @@ int solve_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<i
       tr.nrhs = s.R;
       tr.kind = s.f->kind == kAsmMuller ? 2
                 : s.f->kind == kAsmFluidCBIE ? 3
+                : s.f->kind == kAsmRegion ? 4
                 : (s.f->prob.boundary == BEMGPU_RIGID ? 0 : 1);
+      if (s.f->kind == kAsmRegion) tr.outer = s.f->outer.as<int8_t>();
       n_max = std::max(n_max, s.f->n);
     }
     Buf d;
@@ -1727,7 +1832,8 @@ int solve_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<i
     dg.unknown_count = f->N;
     dg.quadrature_nodes = f->n;
     dg.near_pairs = f->mesh ? f->mesh->n_near : 0;
-    dg.formulation = formulation_of(f->kind);
+    dg.formulation = f->kind == kAsmRegion ? (f->region_cbie ? BEMGPU_CBIE : BEMGPU_MULLER)
+                                           : formulation_of(f->kind);
     dg.precision = f->prob.precision;
     dg.factor_precision = f->single ? 0 : 1;
     dg.refinement_reason = f->reason;
@@ -1764,6 +1870,12 @@ int solve_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<i
     out[t]->boundary = f->prob.boundary;
     out[t]->g = f->prob.density_contrast;
     out[t]->h = f->prob.soundspeed_contrast;
+    if (f->kind == kAsmRegion) {  // keep the unknowns [p; v] of every interface
+      out[t]->region = true;
+      TRY(alloc(c, (size_t)f->N * s.R * 16, &out[t]->xsol));
+      CUDA_TRY(c, cudaMemcpyAsync(out[t]->xsol.p, s.x.p, (size_t)f->N * s.R * 16,
+                                  cudaMemcpyDeviceToDevice, c->stream));
+    }
   }
   return BEMGPU_OK;
 }
@@ -2322,7 +2434,8 @@ int bemgpu_factor_diagnostics(const bemgpu_factor* f, bemgpu_diagnostics* out) {
   out->unknown_count = d->N;
   out->quadrature_nodes = d->n;
   out->near_pairs = d->mesh ? d->mesh->n_near : 0;
-  out->formulation = formulation_of(d->kind);
+  out->formulation = d->kind == kAsmRegion ? (d->region_cbie ? BEMGPU_CBIE : BEMGPU_MULLER)
+                                           : formulation_of(d->kind);
   out->precision = d->prob.precision;
   out->factor_precision = d->single ? 0 : 1;
   out->refinement_reason = d->reason;
@@ -2424,6 +2537,129 @@ int bemgpu_traces(const bemgpu_solution* sol, int32_t rhs, double* p, double* q)
   return BEMGPU_OK;
 }
 
+int bemgpu_region_solve(bemgpu_ctx* c, int32_t count, const bemgpu_mesh* const* surfaces,
+                        const double* density, const double* soundspeed, const int32_t* parents,
+                        const bemgpu_problem* problem, int32_t nrhs, const double* incidence,
+                        bemgpu_solution** solution) {
+  if (!c) return fail(nullptr, BEMGPU_EINVAL, "null context");
+  if (!surfaces || !density || !soundspeed || !parents || !problem || !incidence || !solution)
+    return fail(c, BEMGPU_EINVAL, "null argument");
+  if (count < 1) return fail(c, BEMGPU_EINVAL, "at least one interface is required");
+  if (count > kMaxRegions) return fail(c, BEMGPU_EINVAL, "too many interfaces");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  for (int32_t i = 0; i < count; ++i) {
+    if (!surfaces[i]) return fail(c, BEMGPU_EINVAL, "null surface");
+    if (!(parents[i] >= 0 && parents[i] <= i))
+      return fail(c, BEMGPU_EINVAL, "each parent must be zero or an earlier region index");
+    if (!(std::isfinite(density[i]) && density[i] > 0 && std::isfinite(soundspeed[i]) &&
+          soundspeed[i] > 0))
+      return fail(c, BEMGPU_EINVAL, "fluid contrasts must be finite and positive");
+    if (std::fabs(problem->near_eta - surfaces[i]->d->eta) > 0)
+      return fail(c, BEMGPU_EINVAL, "near_eta differs from the mesh's (upload with that eta)");
+  }
+  bemgpu_problem q = *problem;
+  q.boundary = BEMGPU_FLUID;
+  q.density_contrast = q.soundspeed_contrast = 1.0;  // per region below
+  int kind = 0;
+  TRY(check_problem(c, q, &kind));
+  // containment must match the parents (regions.jl:302-307): surface i contains surface
+  // j exactly when region i + 1 is an ancestor of region j + 1
+  auto ancestor = [&](int32_t region, int32_t j) {
+    int32_t r = parents[j];
+    while (r != 0) {
+      if (r == region) return true;
+      r = parents[r - 1];
+    }
+    return false;
+  };
+  for (int32_t i = 0; i < count; ++i)
+    for (int32_t j = 0; j < count; ++j) {
+      if (i == j) continue;
+      const MeshData* mi = surfaces[i]->d.get();
+      const MeshData* mj = surfaces[j]->d.get();
+      const bool inside = host_solid_angle(mi, mj->nodes_h.data()) > 2.0 * M_PI;
+      if (inside != ancestor(i + 1, j))
+        return fail(c, BEMGPU_EINVAL, "interfaces " + std::to_string(i + 1) + " and " +
+                                          std::to_string(j + 1) +
+                                          " do not match the specified parents");
+    }
+  std::vector<const MeshData*> parts;
+  for (int32_t i = 0; i < count; ++i) parts.push_back(surfaces[i]->d.get());
+  std::shared_ptr<MeshData> un;
+  TRY(make_union_mesh(c, parts, problem->near_eta, &un));
+  // coupling table
+  RegionTable tab;
+  std::memset(&tab, 0, sizeof tab);
+  tab.count = count;
+  tab.cbie = kind == kAsmFluidCBIE ? 1 : 0;
+  std::vector<double> rho(count + 1, 1.0);
+  tab.kr[0] = q.k;
+  for (int32_t i = 0; i < count; ++i) {
+    tab.kr[i + 1] = q.k / soundspeed[i];
+    rho[i + 1] = density[i];
+  }
+  for (int32_t si = 0; si < count; ++si)
+    for (int32_t sj = 0; sj < count; ++sj) {
+      RegionCoef& C = tab.c[si * kMaxRegions + sj];
+      for (int32_t region : {si + 1, parents[si]}) {
+        double sign;
+        if (sj + 1 == region)
+          sign = 1.0;
+        else if (parents[sj] == region)
+          sign = -1.0;
+        else
+          continue;
+        C.kidx[C.count] = region;
+        C.eq[C.count] = region == si + 1 ? 1 : 0;
+        C.sign[C.count] = sign;
+        C.rho[C.count] = rho[region];
+        ++C.count;
+      }
+    }
+  std::vector<int8_t> outer((size_t)un->n, 0);
+  for (int32_t i = 0; i < count; ++i)
+    if (parents[i] == 0)
+      for (int64_t p = un->offsets[i]; p < un->offsets[i + 1]; ++p) outer[(size_t)p] = 1;
+  auto f = std::make_shared<FactorData>();
+  f->c = c;
+  f->mesh = un;
+  f->prob = q;
+  f->kind = kAsmRegion;
+  f->region_cbie = tab.cbie != 0;
+  f->mixed = q.precision == BEMGPU_MIXED;
+  f->fp32_regular = q.assembly == BEMGPU_ASSEMBLY_SINGLE ||
+                    (q.assembly == BEMGPU_ASSEMBLY_DEFAULT && f->mixed);
+  std::vector<RegionTable> tv{tab};
+  TRY(upload(c, tv, &f->region_tab));
+  TRY(upload(c, outer, &f->outer));
+  std::vector<FactorData*> fs{f.get()};
+  TRY(factor_batch(c, fs, true));
+  auto sd = std::make_shared<SolutionData>();
+  sd->c = c;
+  std::vector<SolutionData*> outs{sd.get()};
+  std::vector<int32_t> nr{nrhs};
+  std::vector<const double*> inc{incidence};
+  TRY(solve_batch(c, fs, nr, inc, outs));
+  *solution = new bemgpu_solution{sd};
+  return BEMGPU_OK;
+}
+
+int bemgpu_region_traces(const bemgpu_solution* sol, int32_t rhs, double* p, double* v) {
+  if (!sol) return fail(nullptr, BEMGPU_EINVAL, "null solution");
+  SolutionData* s = sol->d.get();
+  bemgpu_ctx* c = s->c;
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  if (!s->region) return fail(c, BEMGPU_EINVAL, "not a coupled-region solution");
+  if (rhs < 0 || rhs >= s->nrhs) return fail(c, BEMGPU_EINVAL, "rhs index out of range");
+  const size_t n = (size_t)s->mesh->n;
+  const double* x = s->xsol.as<double>() + 4 * n * rhs;
+  if (p) CUDA_TRY(c, cudaMemcpyAsync(p, x, n * 16, cudaMemcpyDeviceToHost, c->stream));
+  if (v) CUDA_TRY(c, cudaMemcpyAsync(v, x + 2 * n, n * 16, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return BEMGPU_OK;
+}
+
 int bemgpu_solution_diagnostics(const bemgpu_solution* sol, bemgpu_diagnostics* out) {
   if (!sol || !out) return fail(nullptr, BEMGPU_EINVAL, "null argument");
   *out = sol->d->diag;
@@ -2448,6 +2684,8 @@ int bemgpu_pressure(bemgpu_solution* sol, int32_t rhs, int64_t npts, const doubl
   if (rhs < 0 || rhs >= s->nrhs) return fail(c, BEMGPU_EINVAL, "rhs index out of range");
   if (field < BEMGPU_FIELD_TOTAL || field > BEMGPU_FIELD_INTERIOR)
     return fail(c, BEMGPU_EINVAL, "field must be :total, :scattered, :incident or :interior");
+  if (s->region)
+    return fail(c, BEMGPU_EINVAL, "pressure of a coupled-region solution is not supported");
   if (npts < 0 || (npts > 0 && (!points || !out)))
     return fail(c, BEMGPU_EINVAL, "invalid points");
   if (npts == 0) return BEMGPU_OK;

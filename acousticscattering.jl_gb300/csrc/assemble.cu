@@ -145,6 +145,7 @@ __global__ void __launch_bounds__(kAsmRows) k_assemble_regular(const AsmInst* __
   if (!ok || !row_ok) return;
   const R ke = (R)I.k_e, ki = (R)I.k_i;
   const int64_t lda = I.lda;
+  const int si = KIND == kAsmRegion ? I.surf[i] : 0;
   for (int jj = 0; jj < cnt; ++jj) {
     const int64_t j = j0 + jj;
     if (j == i) continue;  // self pair: near kernel
@@ -161,6 +162,37 @@ __global__ void __launch_bounds__(kAsmRows) k_assemble_regular(const AsmInst* __
       }
       store_r(I.out1, (I.c64 & 1) != 0, i + j * lda, m1);
       store_r(I.out2, (I.c64 & 2) != 0, i + j * lda, m2);
+    } else if (KIND == kAsmRegion) {
+      const RegionTable& RT = *I.region;
+      const RegionCoef& C = RT.c[si * kMaxRegions + I.surf[j]];
+      cx<R> a11 = {0, 0}, a12 = {0, 0}, a21 = {0, 0}, a22 = {0, 0};
+      for (int q = 0; q < C.count; ++q) {
+        Acc<R> t;
+        t.S = t.D = t.K = t.H = cx<R>{0, 0};
+        const R kq = (R)RT.kr[C.kidx[q]];
+        if (RT.cbie)
+          regular_panel<R, false>(rec, x, nx, kq, t);
+        else
+          regular_panel<R, true>(rec, x, nx, kq, t);
+        const R sg = (R)C.sign[q], rho = (R)C.rho[q];
+        if (!RT.cbie) {
+          a11 += sg * t.D;
+          a12 -= (sg * rho) * t.S;
+          a21 += (sg / rho) * t.H;
+          a22 -= sg * t.K;
+        } else if (C.eq[q] == 0) {
+          a11 += sg * t.D;
+          a12 -= (sg * rho) * t.S;
+        } else {
+          a21 += sg * t.D;
+          a22 -= (sg * rho) * t.S;
+        }
+      }
+      const bool c64 = (I.c64 & 1) != 0;
+      store_r(I.out1, c64, i + j * lda, a11);
+      store_r(I.out1, c64, i + (n + j) * lda, a12);
+      store_r(I.out1, c64, (n + i) + j * lda, a21);
+      store_r(I.out1, c64, (n + i) + (n + j) * lda, a22);
     } else {
       Acc<R> e, t;
       e.S = e.D = e.K = e.H = cx<R>{0, 0};
@@ -229,6 +261,40 @@ __global__ void __launch_bounds__(128) k_assemble_near(const AsmInst* __restrict
     }
     store_n(I.out1, (I.c64 & 1) != 0, I.dnear, p, i + j * lda, m1);
     store_n(I.out2, (I.c64 & 2) != 0, I.dnear2, p, i + j * lda, m2);
+  } else if (KIND == kAsmRegion) {
+    const RegionTable& RT = *I.region;
+    const RegionCoef& C = RT.c[I.surf[i] * kMaxRegions + I.surf[j]];
+    cd a11, a12 = {0.0, 0.0}, a21, a22 = {0.0, 0.0};
+    if (RT.cbie) {  // 1/2 I in both equation rows (one per region of the interface)
+      a11 = cd{0.5 * delta, 0.0};
+      a21 = cd{0.5 * delta, 0.0};
+    } else {
+      a11 = cd{delta, 0.0};
+      a22 = cd{delta, 0.0};
+      a21 = cd{0.0, 0.0};
+    }
+    for (int q = 0; q < C.count; ++q) {
+      const Ops o = near_pair<KIND, F32>(v, rj, x, nx, self, RT.kr[C.kidx[q]], S0, D0, K0, H0);
+      const double sg = C.sign[q], rho = C.rho[q];
+      if (!RT.cbie) {
+        a11 += sg * o.D;
+        a12 -= (sg * rho) * o.S;
+        a21 += (sg / rho) * o.H;
+        a22 -= sg * o.K;
+      } else if (C.eq[q] == 0) {
+        a11 += sg * o.D;
+        a12 -= (sg * rho) * o.S;
+      } else {
+        a21 += sg * o.D;
+        a22 -= (sg * rho) * o.S;
+      }
+    }
+    const bool c64 = (I.c64 & 1) != 0;
+    const int64_t nn = I.n_near;
+    store_n(I.out1, c64, I.dnear, p, i + j * lda, a11);
+    store_n(I.out1, c64, I.dnear, nn + p, i + (n + j) * lda, a12);
+    store_n(I.out1, c64, I.dnear, 2 * nn + p, (n + i) + j * lda, a21);
+    store_n(I.out1, c64, I.dnear, 3 * nn + p, (n + i) + (n + j) * lda, a22);
   } else {
     Ops e = near_pair<KIND, F32>(v, rj, x, nx, self, I.k_e, S0, D0, K0, H0);
     Ops t = near_pair<KIND, F32>(v, rj, x, nx, self, I.k_i, S0, D0, K0, H0);
@@ -292,6 +358,7 @@ static void launch_regular_t(const Launch& L, const AsmInst* d, int ninst, int64
     case kAsmBM: k_assemble_regular<R, kAsmBM><<<grid, kAsmRows, 0, L.stream>>>(d, L.err_flag); count_launch(1); break;
     case kAsmCBIE: k_assemble_regular<R, kAsmCBIE><<<grid, kAsmRows, 0, L.stream>>>(d, L.err_flag); count_launch(1); break;
     case kAsmMuller: k_assemble_regular<R, kAsmMuller><<<grid, kAsmRows, 0, L.stream>>>(d, L.err_flag); count_launch(1); break;
+    case kAsmRegion: k_assemble_regular<R, kAsmRegion><<<grid, kAsmRows, 0, L.stream>>>(d, L.err_flag); count_launch(1); break;
     default: k_assemble_regular<R, kAsmFluidCBIE><<<grid, kAsmRows, 0, L.stream>>>(d, L.err_flag); count_launch(1); break;
   }
 }
@@ -313,6 +380,7 @@ static void launch_near_t(const Launch& L, const AsmInst* d_inst, int ninst, int
     case kAsmBM: k_assemble_near<kAsmBM, F32><<<grid, 128, 0, L.stream>>>(d_inst); break;
     case kAsmCBIE: k_assemble_near<kAsmCBIE, F32><<<grid, 128, 0, L.stream>>>(d_inst); break;
     case kAsmMuller: k_assemble_near<kAsmMuller, F32><<<grid, 128, 0, L.stream>>>(d_inst); break;
+    case kAsmRegion: k_assemble_near<kAsmRegion, F32><<<grid, 128, 0, L.stream>>>(d_inst); break;
     default: k_assemble_near<kAsmFluidCBIE, F32><<<grid, 128, 0, L.stream>>>(d_inst); break;
   }
   count_launch(1);

@@ -58,7 +58,32 @@ enum AsmKind : int32_t {
   kAsmBM = 0,        // rigid/soft Burton-Miller: M1 = 1/2 I - D - a H, M2 = S + a(1/2 I + K')
   kAsmCBIE = 1,      // rigid/soft CBIE:           M1 = 1/2 I - D,        M2 = S
   kAsmMuller = 2,    // fluid Mueller 2n x 2n
-  kAsmFluidCBIE = 3  // fluid CBIE 2n x 2n
+  kAsmFluidCBIE = 3, // fluid CBIE 2n x 2n
+  kAsmRegion = 4     // coupled fluid regions over several surfaces, 2n x 2n (RegionTable)
+};
+
+// Coupled fluid regions (solvers/bem/regions.jl:189-236).  Surface s (0-based) encloses
+// region s + 1; region 0 is the unbounded exterior.  The operators from source surface
+// sj to target surface si enter the system through at most two regions, each with a
+// sign (+1 when sj is the region's outer boundary, -1 when it is an inner one), the
+// region's density contrast and wavenumber k / speed; Mueller adds
+// [sign D, -sign rho S; sign / rho H, -sign K] to the 2 x 2 panel block, CBIE adds
+// [sign D, -sign rho S] to the equation row block of the region (0: the side outside
+// si, 1: inside) plus 1/2 I on the diagonal for each region.
+constexpr int kMaxRegions = 16;  // interfaces per coupled problem
+struct RegionCoef {
+  int32_t count;    // contributing regions (0..2)
+  int32_t kidx[2];  // region index of each contribution
+  int32_t eq[2];    // CBIE equation row block
+  int32_t pad;
+  double sign[2];
+  double rho[2];
+};
+struct RegionTable {
+  int32_t count;                            // interfaces
+  int32_t cbie;                             // 0 Mueller, 1 CBIE
+  double kr[kMaxRegions + 1];               // wavenumber of every region
+  RegionCoef c[kMaxRegions * kMaxRegions];  // [target surface * kMaxRegions + source]
 };
 
 // One assembly instance (device-resident array of these drives a batched launch).
@@ -80,6 +105,8 @@ struct AsmInst {
   void* out2;              // M2 (rigid/soft), null for fluid
   double* dnear;           // complex64 out1: FP64 near corrections [block][n_near]
   double* dnear2;          // complex64 out2: FP64 near corrections [n_near]
+  const int32_t* surf;     // kAsmRegion: surface of every panel
+  const RegionTable* region;  // kAsmRegion: coupling table
 };
 
 // Incident field / far-field instance.

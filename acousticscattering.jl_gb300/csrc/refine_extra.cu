@@ -14,7 +14,9 @@ __device__ __forceinline__ void st2(double* p, int64_t i, double2 v) {
 }
 
 // kind: 0 rigid (p = x, q = -q_inc), 1 pressure release (p = -p_inc, q = x),
-// 2 Mueller (p = x_top - p_inc, q = x_bot - q_inc), 3 fluid CBIE (p = x_top, q = x_bot)
+// 2 Mueller (p = x_top - p_inc, q = x_bot - q_inc), 3 fluid CBIE (p = x_top, q = x_bot),
+// 4 coupled regions (as Mueller on the surfaces bordering the exterior, 0 elsewhere: the
+// far field sums only those, solvers/bem/postprocessing.jl:15-31)
 // (solvers/bem/full.jl:160-161, 472-477).
 __global__ void k_traces(const TraceInst* __restrict__ insts) {
   const TraceInst& T = insts[blockIdx.z];
@@ -34,6 +36,12 @@ __global__ void k_traces(const TraceInst* __restrict__ insts) {
       p = make_double2(-pi.x, -pi.y);
       q = xt;
       break;
+    case 4:  // regions: scattered traces on the surfaces bordering the exterior, 0 inside
+      if (!T.outer[i]) {
+        p = q = make_double2(0.0, 0.0);
+        break;
+      }
+      [[fallthrough]];  // total traces minus incident, as Mueller
     case 2: {
       const double2 xb = ld2(T.x, T.n + i + (int64_t)r * T.ldx);
       p = make_double2(xt.x - pi.x, xt.y - pi.y);
@@ -70,8 +78,11 @@ __global__ void k_stack(const TraceInst* __restrict__ insts) {
   const int r = blockIdx.y;
   if (i >= T.n || r >= T.nrhs) return;
   const int64_t ld = 2 * T.n;
-  st2(T.ps, i + (int64_t)r * ld, ld2(T.pinc, i + (int64_t)r * T.n));
-  st2(T.ps, T.n + i + (int64_t)r * ld, ld2(T.qinc, i + (int64_t)r * T.n));
+  const bool on = T.outer ? T.outer[i] != 0 : true;  // regions: exterior surfaces only
+  const bool q = T.outer ? (on && T.stack_q) : true;
+  const double2 z = make_double2(0.0, 0.0);
+  st2(T.ps, i + (int64_t)r * ld, on ? ld2(T.pinc, i + (int64_t)r * T.n) : z);
+  st2(T.ps, T.n + i + (int64_t)r * ld, q ? ld2(T.qinc, i + (int64_t)r * T.n) : z);
 }
 
 __global__ void k_fill(double* p, int64_t count, double v) {

@@ -14,7 +14,10 @@ struct TraceInst {
   double* ps;          // scattered traces out (n x nrhs) / forcing out (2n x nrhs)
   double* qs;
   int32_t nrhs;
-  int32_t kind;
+  int32_t kind;            // traces: 0 rigid, 1 soft, 2 Mueller, 3 fluid CBIE, 4 regions
+  const int8_t* outer;     // regions: panel borders the exterior (forcing and far field)
+  int32_t stack_q;         // regions forcing: the second block gets q_inc (Mueller)
+  int32_t pad;
 };
 
 #ifdef __CUDACC__

@@ -162,6 +162,47 @@ function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
         Float64(k), :full, data)
 end
 
+"""
+    bem(gpu_meshes::Vector{GPUMesh}, materials::Vector{FluidFilled}, k;
+        parents=collect(0:length(gpu_meshes)-1), incidence_angle=π/2, incidence_azimuth=0,
+        formulation=:muller, precision=:double, equilibrate=true, refinement=(;))
+
+The reference's coupled-region `bem(surfaces, materials, k; parents, ...)`
+(solvers/bem/regions.jl:132-150) on the GPU.  The returned solution answers
+`scattering_amplitude` / `target_strength` (summed over the surfaces bordering the
+exterior, solvers/bem/postprocessing.jl:15-31) and `diagnostics`.
+"""
+function bem(ms::AbstractVector{GPUMesh}, materials::AbstractVector{<:FluidFilled}, k::Real;
+        parents::AbstractVector{<:Integer} = collect(0:(length(ms) - 1)),
+        incidence_angle::Real = π / 2, incidence_azimuth::Real = 0.0,
+        formulation::Symbol = :muller, precision::Symbol = :double, equilibrate::Bool = true,
+        refinement::NamedTuple = (;), assembly::Symbol = :default, ctx::Context = context())
+    count = length(ms)
+    length(materials) == length(parents) == count ||
+        throw(ArgumentError("supply one material and parent per interface"))
+    p = Problem(Int32(2), FORMULATIONS[formulation],
+        precision === :mixed ? Int32(1) : Int32(0), Int32(equilibrate), Float64(k), 1.0, 1.0,
+        get(refinement, :tolerance, 1e-13), Int32(get(refinement, :maxiter, 8)),
+        assembly === :double ? Int32(1) : assembly === :single ? Int32(2) : Int32(0),
+        get(refinement, :condition_guard, 10eps(Float32)), 2.0)
+    handles = Ptr{Cvoid}[m.ptr for m in ms]
+    dens = Float64[m.density_contrast for m in materials]
+    speeds = Float64[m.soundspeed_contrast for m in materials]
+    par = Int32.(parents)
+    inc = Float64[incidence_angle, incidence_azimuth]
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:bemgpu_region_solve, libbemgpu), Cint,
+        (Ptr{Cvoid}, Int32, Ptr{Ptr{Cvoid}}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32},
+            Ref{Problem}, Int32, Ptr{Float64}, Ptr{Ptr{Cvoid}}),
+        ctx.ptr, count, handles, dens, speeds, par, p, 1, inc, r), ctx.ptr)
+    d = Ref{Diagnostics}()
+    ccall((:bemgpu_solution_diagnostics, libbemgpu), Cint, (Ptr{Cvoid}, Ref{Diagnostics}), r[], d)
+    data = _GPUBEMData(r[], ms[1].nodes, ms[1].triangles, incidence_angle, incidence_azimuth,
+        d[])
+    return BEMSolution(AcousticScattering._SurfaceGeometry(ms[1].nodes, ms[1].triangles),
+        materials[1], Float64(k), :full, data)
+end
+
 function scattering_amplitude(sol::BEMSolution{_GPUBEMData};
         direction::Union{Nothing, AbstractVector} = nothing)
     out = zeros(Float64, 2)

@@ -241,6 +241,31 @@ int bemgpu_factor_diagnostics(const bemgpu_factor *factor, bemgpu_diagnostics *o
 int bemgpu_solve(bemgpu_ctx *ctx, const bemgpu_mesh *mesh, const bemgpu_problem *problem,
                  int32_t nrhs, const double *incidence, bemgpu_solution **solution);
 
+/*
+ * Coupled fluid regions: the reference's bem(surfaces, materials, k; parents, ...)
+ * (solvers/bem/regions.jl:132-253).  surfaces[i] (i = 0..count-1, count <= 16) encloses
+ * region i + 1; parents[i] is the region outside it: 0 for the unbounded exterior or the
+ * 1-based index of an earlier surface (a nested chain is {0, 1, 2, ...}).  density[i] and
+ * soundspeed[i] are region i + 1's contrasts relative to the exterior.  The surfaces must
+ * not intersect; their containment is checked against the parents (BEMGPU_EINVAL
+ * otherwise).  `problem` supplies k, the formulation (DEFAULT/MULLER or CBIE), precision,
+ * refinement, assembly and near_eta (each surface uploaded with it); its boundary and
+ * contrast fields are ignored.  The plane wave lights the surfaces that border the
+ * exterior.  The solution answers far_field / target_strength (summed over those
+ * surfaces, solvers/bem/postprocessing.jl:15-31), traces (scattered traces there, zero
+ * on inner surfaces), region_traces and diagnostics; pressure returns BEMGPU_EINVAL.
+ */
+int bemgpu_region_solve(bemgpu_ctx *ctx, int32_t count, const bemgpu_mesh *const *surfaces,
+                        const double *density, const double *soundspeed, const int32_t *parents,
+                        const bemgpu_problem *problem, int32_t nrhs, const double *incidence,
+                        bemgpu_solution **solution);
+/*
+ * Unknowns of a coupled-region solution for right-hand side `rhs`, every panel in surface
+ * order (2 * n doubles each): p = total pressure, v = the flux unknown (the interior normal
+ * derivative is density_i * v, the exterior one density_parent * v).
+ */
+int bemgpu_region_traces(const bemgpu_solution *sol, int32_t rhs, double *p, double *v);
+
 /* ------------------------------------------------------------------ queries */
 /*
  * Far-field amplitude f(x_hat) of right-hand side `rhs` at ndir unit directions
