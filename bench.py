@@ -150,10 +150,10 @@ def lu_update_flops(N, nb):
 
 
 # DRAM traffic of one k_tc_cgemm launch over its algorithmic bytes, from one ncu capture
-# (--set full) of `bench.py --freqs 2 --nlon 48 --nrings 30`: 4th launch = trailing
-# update of outer step 1 of 2 x 5760 unknowns (m = n = 5504, k = 128),
-# dram__bytes_read.sum + dram__bytes_write.sum = 507.54 + 423.62 MB.
-NCU_GEMM_TRAFFIC = (507.543808e6 + 423.618560e6) / (2 * (16.0 * 5504 ** 2 + 8.0 * 128 * 2 * 5504))
+# (--set full) of `bench.py --freqs 8 --nlon 48 --nrings 30`: 6th launch = K = 256
+# trailing update of the first step of 8 x 5760 unknowns (m = n = 5504),
+# dram__bytes_read.sum + dram__bytes_write.sum = 2.119512 + 1.876776 GB.
+NCU_GEMM_TRAFFIC = (2.119512e9 + 1.876776e9) / (8 * (16.0 * 5504 ** 2 + 8.0 * 256 * 2 * 5504))
 
 
 def aggregate_replicas(ms, units, world):
