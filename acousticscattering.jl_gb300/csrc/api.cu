@@ -1025,9 +1025,63 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
       set_gemm(st, kG6, t, ap, bp, K0 + SB, K0 + SB, m3, m3, kk0 + kk1);
     }
   }
-  Buf dpack, dgem;
+  // in-half updates after each 32-column panel (K = 32): rows [k0 + 32, n) x columns
+  // [k0 + 32, H + 128) -= L21 U12, on the tensor cores as well
+  constexpr int kInner = HB / kPanelNB - 1;  // panels with columns to their right
+  const size_t nis = (size_t)steps * 2 * kInner;
+  std::vector<TcPackInst> ipacks(nis * 2 * ni);
+  std::vector<TcGemmInst> igems(nis * ni);
+  std::vector<int64_t> itiles(nis, 0), irows(nis, 0);
+  for (int64_t st = 0; st < steps; ++st)
+    for (int h = 0; h < 2; ++h)
+      for (int q = 0; q < kInner; ++q) {
+        const size_t idx = ((size_t)st * 2 + h) * kInner + q;
+        const int64_t H = st * SB + h * HB, k0 = H + (int64_t)q * kPanelNB;
+        for (int t = 0; t < ni; ++t) {
+          const int64_t n = mi[t].n, lda = mi[t].lda;
+          const int64_t m = std::max<int64_t>(0, n - k0 - kPanelNB);
+          const int64_t nc = std::max<int64_t>(0, std::min<int64_t>(H + HB, n) - k0 - kPanelNB);
+          const bool on = m > 0 && nc > 0;
+          TcPackInst& a = ipacks[idx * 2 * ni + t];
+          TcPackInst& b = ipacks[idx * 2 * ni + ni + t];
+          std::memset(&a, 0, sizeof a);
+          std::memset(&b, 0, sizeof b);
+          a.a = b.a = mi[t].a;
+          a.lda = b.lda = lda;
+          a.r0 = k0 + kPanelNB;  // rows of L21
+          b.r0 = k0 + kPanelNB;  // columns of U12
+          a.k0 = b.k0 = k0;
+          a.rows = on ? m : 0;
+          b.rows = on ? nc : 0;
+          a.kk = b.kk = on ? kPanelNB : 0;
+          a.trans = 0;
+          b.trans = 1;
+          a.out = apack[t].p;
+          b.out = bpack[t].p;
+          a.active = b.active = on ? 1 : 0;
+          TcGemmInst& g = igems[idx * ni + t];
+          std::memset(&g, 0, sizeof g);
+          g.apack = apack[t].p;
+          g.bpack = bpack[t].p;
+          g.c = mi[t].a;
+          g.ldc = lda;
+          g.c_r0 = g.c_c0 = k0 + kPanelNB;
+          g.m = on ? m : 0;
+          g.n = on ? nc : 0;
+          g.kk = on ? kPanelNB : 0;
+          g.active = on ? 1 : 0;
+          g.cmap = cmaps[t];
+          if (on) {
+            itiles[idx] += ((m + 127) / 128) * ((nc + 127) / 128);
+            irows[idx] = std::max(irows[idx], std::max(m, nc));
+          }
+        }
+      }
+  Buf dpack, dgem, dipack, digem;
   TRY(to_device(c, packs, &dpack));
   TRY(to_device(c, gems, &dgem));
+  TRY(to_device(c, ipacks, &dipack));
+  TRY(to_device(c, igems, &digem));
   auto pack = [&](int64_t st, int ph) {
     const size_t q = (size_t)st * kNPack + ph;
     if (prow[q] > 0)
@@ -1046,6 +1100,8 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
   };
   auto any = [&](int64_t st, int ph) { return tiles[(size_t)st * kNGem + ph] > 0; };
   auto factor_half = [&](int64_t H) {
+    const int64_t st = H / SB;
+    const int h = (int)((H % SB) / HB);
     for (int64_t k0 = H; k0 < H + HB && k0 < nmax; k0 += kPanelNB) {
       {
         Prof pr(c, "getf2");
@@ -1059,9 +1115,19 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
         Prof pr(c, "trsm");
         launch_trsm_panel(L, dm, ni, k0, kPanelNB, k0 + kPanelNB, H + HB, 1);
       }
-      {
-        Prof pr(c, "gemm_panel");
-        launch_gemm_update(L, dm, ni, k0, kPanelNB, nmax, k0 + kPanelNB, H + HB, 1);
+      const int q = (int)((k0 - H) / kPanelNB);
+      if (q < kInner) {
+        const size_t idx = ((size_t)st * 2 + h) * kInner + q;
+        if (itiles[idx] > 0) {
+          Prof pr(c, "gemm_panel");
+          if (red) {  // tensor cores, reduction epilogue
+            launch_tc_pack(L, dipack.as<TcPackInst>() + idx * 2 * ni, 2 * ni, irows[idx],
+                           kPanelNB);
+            launch_tc_cgemm(L, digem.as<TcGemmInst>() + idx * ni, ni, itiles[idx], true);
+          } else {
+            launch_gemm_update(L, dm, ni, k0, kPanelNB, nmax, k0 + kPanelNB, H + HB, 1);
+          }
+        }
       }
     }
   };
