@@ -107,6 +107,7 @@ SIGNATURES = {
                                            ctypes.POINTER(_i32), ctypes.POINTER(Problem), _i32,
                                            _dp, ctypes.POINTER(_vp)]),
     "bemgpu_region_traces": (ctypes.c_int, [_vp, _i32, _dp, _dp]),
+    "bemgpu_ctx_set_autotune": (ctypes.c_int, [_vp, _i32]),
     "bemgpu_solution_diagnostics": (ctypes.c_int, [_vp, ctypes.POINTER(Diagnostics)]),
     "bemgpu_pressure": (ctypes.c_int, [_vp, _i32, _i64, _dp, _i32, _dp]),
     "bemgpu_solution_destroy": (ctypes.c_int, [_vp]),

@@ -118,6 +118,11 @@ class Context:
     def synchronize(self):
         _check(C.lib().bemgpu_ctx_synchronize(self.handle), self.handle)
 
+    def set_autotune(self, enable: bool = True):
+        """Measured launch shapes (panel cluster size, residual rows per thread); every
+        choice gives bit-identical results."""
+        _check(C.lib().bemgpu_ctx_set_autotune(self.handle, int(enable)), self.handle)
+
     def profile(self, enable: bool = True):
         _check(C.lib().bemgpu_profile_enable(self.handle, int(enable)), self.handle)
 

@@ -63,6 +63,9 @@ struct bemgpu_ctx {
   std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
   float* pinned = nullptr;  // page-locked staging of host <-> device vector exchanges
   size_t pinned_bytes = 0;
+  // launch-shape autotuner: the fastest measured choice per (kernel family, shape class)
+  std::map<std::string, int> tuned;
+  bool autotune = true;
   std::recursive_mutex mu;
   Launch launch() const { return Launch{stream, d_err}; }
 };
@@ -796,6 +799,98 @@ float* pinned_buffer(bemgpu_ctx* c, size_t bytes) {
   return c->pinned;
 }
 
+// ------------------------------------------------------------------ autotuner
+// Launch shapes whose choice leaves every result bit-for-bit unchanged (the rows each
+// thread or CTA takes, not the order of any sum) are picked by measurement: the first
+// time a (family, shape class) is met, every candidate runs on the live data (or on a
+// scratch copy when the kernel works in place), timed with CUDA events on the context's
+// stream, and the fastest is kept for the context's lifetime.
+int log2_bucket(int64_t v) {
+  int b = 0;
+  while (v > 1) {
+    v >>= 1;
+    ++b;
+  }
+  return b;
+}
+
+template <class Run, class Prepare>
+int tune_pick(bemgpu_ctx* c, const std::string& key, const std::vector<int>& cands, Run run,
+              Prepare prepare) {
+  auto it = c->tuned.find(key);
+  if (it != c->tuned.end()) return it->second;
+  if (!c->autotune || cands.size() < 2) return cands.front();
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best_ms = INFINITY;
+  int best = cands.front();
+  for (int v : cands) {
+    prepare();
+    cudaEventRecord(e0, c->stream);
+    run(v);
+    cudaEventRecord(e1, c->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->tuned[key] = best;
+  return best;
+}
+
+// Cluster size of the complex64 panel kernel for this batch and panel height, measured
+// on scratch copies of the panels (the kernel factors in place).
+int tuned_getf2_cluster(bemgpu_ctx* c, const std::vector<MatInst>& mi, int64_t k0) {
+  const int ni = (int)mi.size();
+  int64_t mmax = 0;
+  for (const MatInst& m : mi) mmax = std::max<int64_t>(mmax, m.n - k0);
+  if (mmax <= 0) return 0;
+  const std::string key = "getf2/" + std::to_string(ni) + "/" + std::to_string(log2_bucket(mmax));
+  auto it = c->tuned.find(key);
+  if (it != c->tuned.end()) return it->second;
+  if (!c->autotune) return 0;
+  const int64_t lds = (mmax + 31) / 32 * 32;
+  Buf scratch, piv, info, dsm;
+  if (alloc(c, (size_t)ni * lds * kPanelNB * 8, &scratch) != BEMGPU_OK ||
+      alloc(c, (size_t)ni * kPanelNB * 4, &piv) != BEMGPU_OK ||
+      alloc(c, (size_t)ni * 4, &info) != BEMGPU_OK)
+    return 0;  // no room to measure: the batch-size rule
+  std::vector<MatInst> sm(mi.size());
+  for (int t = 0; t < ni; ++t) {
+    MatInst& m = sm[(size_t)t];
+    std::memset(&m, 0, sizeof m);
+    m.a = scratch.as<float2>() + (size_t)t * lds * kPanelNB;
+    m.n = std::max<int64_t>(0, mi[(size_t)t].n - k0);
+    m.lda = lds;
+    m.ipiv = piv.as<int32_t>() + (size_t)t * kPanelNB;
+    m.info = info.as<int32_t>() + t;
+    m.active = m.n > 0 ? 1 : 0;
+  }
+  if (to_device(c, sm, &dsm) != BEMGPU_OK) return 0;
+  auto prepare = [&]() {
+    cudaMemsetAsync(info.p, 0, (size_t)ni * 4, c->stream);
+    for (int t = 0; t < ni; ++t) {
+      if (!sm[(size_t)t].active) continue;
+      const MatInst& m = mi[(size_t)t];
+      const int64_t cols = std::min<int64_t>(kPanelNB, m.n - k0);  // the panel's columns
+      cudaMemcpy2DAsync(sm[(size_t)t].a, (size_t)lds * 8,
+                        static_cast<const float2*>(m.a) + k0 + k0 * m.lda, (size_t)m.lda * 8,
+                        (size_t)sm[(size_t)t].n * 8, (size_t)cols, cudaMemcpyDeviceToDevice,
+                        c->stream);
+    }
+  };
+  const Launch L = c->launch();
+  return tune_pick(c, key, {2, 4, 8},
+                   [&](int cs) { launch_getf2(L, dsm.as<MatInst>(), ni, 0, kPanelNB, 1, cs); },
+                   prepare);
+}
+
 // LAPACK's 1-norm estimate (zlacn2 reverse communication) for every factor of the batch:
 // each round packs the vectors of all instances that ask for the same product into one
 // page-locked buffer, runs one batched triangular solve and reads them back with one copy.
@@ -1103,9 +1198,10 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
     const int64_t st = H / SB;
     const int h = (int)((H % SB) / HB);
     for (int64_t k0 = H; k0 < H + HB && k0 < nmax; k0 += kPanelNB) {
+      const int cs = tuned_getf2_cluster(c, mi, k0);
       {
         Prof pr(c, "getf2");
-        launch_getf2(L, dm, ni, k0, kPanelNB, 1);
+        launch_getf2(L, dm, ni, k0, kPanelNB, 1, cs);
       }
       {
         Prof pr(c, "laswp");
@@ -1572,7 +1668,20 @@ int residual_pass(bemgpu_ctx* c, std::vector<SolveInst*>& ss,
   TRY(to_device(c, vi, &d));
   {
     Prof p(c, "residual");
-    launch_gemv(L, d.as<VecInst>(), (int)vi.size(), nmax, rmax, 1);
+    // rows per thread of the compact products, measured on the live pass (idempotent: the
+    // last candidate's outputs are the pass's outputs)
+    bool any32 = false;
+    for (auto* s : ss) any32 |= s->f->a32;
+    const std::string key = "gemv/" + std::to_string(vi.size()) + "/" +
+                            std::to_string(log2_bucket(nmax)) + "/" + std::to_string(rmax > 1);
+    const int rows = any32 ? tune_pick(c, key, {2, 1},
+                                       [&](int r) {
+                                         launch_gemv(L, d.as<VecInst>(), (int)vi.size(), nmax,
+                                                     rmax, 1, r);
+                                       },
+                                       [] {})
+                           : 2;
+    launch_gemv(L, d.as<VecInst>(), (int)vi.size(), nmax, rmax, 1, rows);
     launch_resid_stats(L, d.as<VecInst>(), (int)vi.size(), rmax);
   }
   stats->resize(ss.size());
@@ -3173,6 +3282,14 @@ int bemgpu_profile_read(bemgpu_ctx* c, const char* family, int64_t* launches, do
     }
   if (launches) *launches = cnt;
   if (total_ms) *total_ms = ms;
+  return BEMGPU_OK;
+}
+
+int bemgpu_ctx_set_autotune(bemgpu_ctx* c, int32_t enable) {
+  if (!c) return fail(nullptr, BEMGPU_EINVAL, "null context");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  c->autotune = enable != 0;
+  if (!c->autotune) c->tuned.clear();
   return BEMGPU_OK;
 }
 

@@ -1138,9 +1138,10 @@ static void getf2_ll_t(const Launch& L, const MatInst* d, int ninst, int64_t k0,
   cudaLaunchKernelEx(&cfg, k_getf2_ll<CS>, d, k0, nb);
 }
 
-void launch_getf2(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb, int prec) {
+void launch_getf2(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb, int prec,
+                  int cs) {
   if (prec_is_single(prec)) {
-    switch (getf2_cluster(ninst)) {  // left-looking, one cluster per instance
+    switch (cs > 0 ? cs : getf2_cluster(ninst)) {  // left-looking, one cluster per instance
       case 8: getf2_ll_t<8>(L, d, ninst, k0, nb); break;
       case 4: getf2_ll_t<4>(L, d, ninst, k0, nb); break;
       default: getf2_ll_t<2>(L, d, ninst, k0, nb); break;

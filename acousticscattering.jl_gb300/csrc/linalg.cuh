@@ -9,7 +9,10 @@ namespace bemgpu {
 constexpr int kPanelNB = 32;  // LU panel width (columns factored per getf2 launch)
 constexpr int kTrsvNB = 64;   // triangular-solve block (rows per diagonal block)
 
-void launch_getf2(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb, int prec);
+// cs: CTAs per instance of the complex64 panel kernel (2, 4 or 8; 0 = the batch-size
+// rule); the factor is identical for every choice
+void launch_getf2(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb, int prec,
+                  int cs = 0);
 // row interchanges k0 .. k0 + nb - 1 on columns [c_lo, c_hi) \ [s_lo, s_hi)
 void launch_laswp(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb, int64_t c_lo,
                   int64_t c_hi, int64_t s_lo, int64_t s_hi, int prec);

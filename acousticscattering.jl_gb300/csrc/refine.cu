@@ -397,13 +397,14 @@ __device__ __forceinline__ void gemv_body(const VecInst& V, int with_abs) {
   }
 }
 
-// Compact instances: two rows per thread (i and i + 256, both coalesced), so every x
-// value loaded serves two rows and each thread carries four independent pair-sum chains
+// Compact instances: ROWS rows per thread (i, i + 256, ..., all coalesced), so every x
+// value loaded serves ROWS rows and each thread carries 2 ROWS independent pair-sum chains
 // per right-hand side.  Columns are loaded kBatch at a time, folded into FP64 every
-// kFold columns.
-constexpr int kA32Rows = 2;
-template <int NR>
+// kFold columns.  ROWS (1 or 2) is a launch shape of the autotuner; it does not change
+// any row's arithmetic.
+template <int NR, int ROWS>
 __device__ __forceinline__ void gemv_a32_body(const VecInst& V, int with_abs) {
+  constexpr int kA32Rows = ROWS;
   constexpr int kFold = 32, kBatch = NR == 1 ? 8 : 4;
   const int64_t n = V.n;
   const int64_t i0 = (int64_t)blockIdx.x * (256 * kA32Rows) + threadIdx.x;
@@ -415,7 +416,7 @@ __device__ __forceinline__ void gemv_a32_body(const VecInst& V, int with_abs) {
   int64_t j0, j1;
   chunk_range(n, ch, kChunks, &j0, &j1);
   const float2* A0 = reinterpret_cast<const float2*>(V.A) + i0;
-  const float2* A1 = ok1 ? A0 + 256 : A0;
+  const float2* A1 = (ROWS > 1 && ok1) ? A0 + 256 : A0;
   const int64_t lda = V.lda;
   const float4* xs[NR];
   const float* xa[NR];
@@ -447,7 +448,7 @@ __device__ __forceinline__ void gemv_a32_body(const VecInst& V, int with_abs) {
 #pragma unroll
       for (int q = 0; q < kBatch; ++q) {
         a[0][q] = q < cnt ? A0[(jb + q) * lda] : make_float2(0.f, 0.f);
-        a[1][q] = q < cnt ? A1[(jb + q) * lda] : make_float2(0.f, 0.f);
+        if (ROWS > 1) a[ROWS - 1][q] = q < cnt ? A1[(jb + q) * lda] : make_float2(0.f, 0.f);
       }
 #pragma unroll
       for (int q = 0; q < kBatch; ++q) {
@@ -501,11 +502,11 @@ __device__ __forceinline__ void gemv_a32_body(const VecInst& V, int with_abs) {
   }
 }
 
-template <int NR>
+template <int NR, int ROWS>
 __global__ void __launch_bounds__(256, 2) k_gemv_a32(const VecInst* __restrict__ insts, int with_abs) {
   const VecInst& V = insts[blockIdx.z];
   if (!V.a32) return;
-  gemv_a32_body<NR>(V, with_abs);
+  gemv_a32_body<NR, ROWS>(V, with_abs);
 }
 
 // partial y = A x (and |A||x|) over a column chunk, up to kGemvR right-hand sides
@@ -702,7 +703,7 @@ void launch_scale_copy(const Launch& L, const VecInst* d, int ninst, int64_t nma
 }
 
 void launch_gemv(const Launch& L, const VecInst* d, int ninst, int64_t nmax, int32_t max_rhs,
-                 int mode) {
+                 int mode, int rows) {
   // compact and complex128 instances by their own instantiations (each skips the others);
   // one right-hand side gets a single-rhs instantiation
   const int nr = max_rhs == 1 ? 1 : kGemvR;
@@ -710,13 +711,20 @@ void launch_gemv(const Launch& L, const VecInst* d, int ninst, int64_t nmax, int
   dim3 g0((unsigned)((nmax + 255) / 256), (unsigned)max_rhs, (unsigned)ninst);
   k_split_x<<<g0, 256, 0, L.stream>>>(d); count_launch(1);
   dim3 g1((unsigned)((nmax + 255) / 256), (unsigned)(kChunks * groups), (unsigned)ninst);
-  dim3 ga((unsigned)((nmax + 256 * kA32Rows - 1) / (256 * kA32Rows)), (unsigned)(kChunks * groups),
+  const int rw = rows == 1 ? 1 : 2;
+  dim3 ga((unsigned)((nmax + 256 * rw - 1) / (256 * rw)), (unsigned)(kChunks * groups),
           (unsigned)ninst);
   if (nr == 1) {
-    k_gemv_a32<1><<<ga, 256, 0, L.stream>>>(d, mode == 1);
+    if (rw == 1)
+      k_gemv_a32<1, 1><<<ga, 256, 0, L.stream>>>(d, mode == 1);
+    else
+      k_gemv_a32<1, 2><<<ga, 256, 0, L.stream>>>(d, mode == 1);
     k_gemv_part<false, 1><<<g1, 256, 0, L.stream>>>(d, mode == 1);
   } else {
-    k_gemv_a32<kGemvR><<<ga, 256, 0, L.stream>>>(d, mode == 1);
+    if (rw == 1)
+      k_gemv_a32<kGemvR, 1><<<ga, 256, 0, L.stream>>>(d, mode == 1);
+    else
+      k_gemv_a32<kGemvR, 2><<<ga, 256, 0, L.stream>>>(d, mode == 1);
     k_gemv_part<false, kGemvR><<<g1, 256, 0, L.stream>>>(d, mode == 1);
   }
   count_launch(2);

@@ -51,9 +51,10 @@ struct VecInst {
 #ifdef __CUDACC__
 void launch_equilibrate(const Launch& L, const VecInst* d, int ninst, int64_t nmax);
 void launch_scale_copy(const Launch& L, const VecInst* d, int ninst, int64_t nmax);
-// mode 0: y = A x; mode 1: y = b - A x and den = |b| + |A||x|
+// mode 0: y = A x; mode 1: y = b - A x and den = |b| + |A||x|.  rows: rows per thread of
+// the compact-storage product (1 or 2; results identical)
 void launch_gemv(const Launch& L, const VecInst* d, int ninst, int64_t nmax, int32_t max_rhs,
-                 int mode);
+                 int mode, int rows = 2);
 // compact instances: out (complex128, ld n) += the near corrections, each scaled by
 // 1 / (rows_i cols_j) (unit_scales = 0) or unscaled (unit_scales = 1)
 void launch_near_add(const Launch& L, const VecInst* d, int ninst, int64_t max_near,

@@ -355,6 +355,14 @@ int bemgpu_assemble_dense(bemgpu_ctx *ctx, const bemgpu_mesh *mesh,
                           const bemgpu_problem *problem, double *M1, double *M2);
 
 /*
+ * Launch-shape autotuner (default on): the first time a batch shape is met, the panel
+ * factorisation's CTAs per instance and the compact residual's rows per thread are chosen
+ * by timing the candidates (on scratch copies where the kernel works in place).  Every
+ * candidate computes bit-identical results.  enable = 0 switches it off and forgets the
+ * measured choices (fixed rules are used).  No reference counterpart.
+ */
+int bemgpu_ctx_set_autotune(bemgpu_ctx *ctx, int32_t enable);
+/*
  * Complex64 trailing updates of the mixed-precision LU on the tensor cores (split-BF16
  * tcgen05 GEMM, default 1) or on the CUDA cores (0).  No reference counterpart: a
  * switch for the precision study and for tests.
