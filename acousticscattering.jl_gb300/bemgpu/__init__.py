@@ -11,7 +11,7 @@ from .api import (ArgumentError, BEMGPUError, BEMSolution, Context, Factor, Flui
                   FrequencySweep, GasFilled, Mesh, PressureRelease, Rigid, Server,
                   SweepResult,
                   assemble, bem, context, dense_solve, diagnostics, factor_batch,
-                  frequency_sweep, solve_batch,
+                  frequency_sweep, hmatrix_apply, solve_batch,
                   incidence_angle_sweep, mesh, pressure, scattering_amplitude,
                   target_strength)
 
@@ -19,6 +19,6 @@ __all__ = ["ArgumentError", "BEMGPUError", "BEMSolution", "Context", "Factor", "
            "FrequencySweep", "GasFilled", "Mesh", "PressureRelease", "Rigid", "Server",
            "SweepResult",
            "assemble", "bem", "context", "dense_solve", "diagnostics", "factor_batch",
-           "frequency_sweep", "solve_batch",
+           "frequency_sweep", "hmatrix_apply", "solve_batch",
            "incidence_angle_sweep", "mesh", "meshes", "pressure", "scattering_amplitude",
            "target_strength", "lib", "LIB_PATH"]

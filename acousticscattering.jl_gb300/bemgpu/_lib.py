@@ -63,6 +63,23 @@ class Diagnostics(ctypes.Structure):
                 ("info", ctypes.c_int32)]
 
 
+class HmatrixOptions(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("eta", ctypes.c_double),
+                ("leaf_size", ctypes.c_int32), ("restart", ctypes.c_int32),
+                ("reltol", ctypes.c_double), ("abstol", ctypes.c_double),
+                ("maxiter", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+class HmatrixStats(ctypes.Structure):
+    _fields_ = [("lowrank_blocks", ctypes.c_int64), ("dense_blocks", ctypes.c_int64),
+                ("densified_blocks", ctypes.c_int64), ("lowrank_entries", ctypes.c_int64),
+                ("dense_entries", ctypes.c_int64), ("max_rank", ctypes.c_int32),
+                ("depth", ctypes.c_int32), ("leaves", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("compression", ctypes.c_double), ("gmres_iterations", ctypes.c_int32),
+                ("gmres_converged", ctypes.c_int32), ("build_ms", ctypes.c_double),
+                ("gmres_ms", ctypes.c_double)]
+
+
 _vp = ctypes.c_void_p
 _dp = ctypes.POINTER(ctypes.c_double)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -107,6 +124,18 @@ SIGNATURES = {
                                            ctypes.POINTER(_i32), ctypes.POINTER(Problem), _i32,
                                            _dp, ctypes.POINTER(_vp)]),
     "bemgpu_region_traces": (ctypes.c_int, [_vp, _i32, _dp, _dp]),
+    "bemgpu_hmatrix_options_init": (None, [ctypes.POINTER(HmatrixOptions)]),
+    "bemgpu_hmatrix_plan": (ctypes.c_int, [_dp, _i64, _i64p, _i64, ctypes.c_double,
+                                           ctypes.POINTER(HmatrixOptions), _i64p,
+                                           ctypes.POINTER(_i32), _i64, ctypes.POINTER(_i32)]),
+    "bemgpu_hmatrix_solve": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(Problem),
+                                            ctypes.POINTER(HmatrixOptions), _i32, _dp,
+                                            ctypes.POINTER(_vp)]),
+    "bemgpu_hmatrix_stats_get": (ctypes.c_int, [_vp, ctypes.POINTER(HmatrixStats)]),
+    "bemgpu_gmres_history": (ctypes.c_int, [_vp, _i32, _dp, _i32, ctypes.POINTER(_i32)]),
+    "bemgpu_hmatrix_apply": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(Problem),
+                                            ctypes.POINTER(HmatrixOptions), _i32, _i32, _dp,
+                                            _dp, ctypes.POINTER(HmatrixStats)]),
     "bemgpu_ctx_set_autotune": (ctypes.c_int, [_vp, _i32]),
     "bemgpu_solution_diagnostics": (ctypes.c_int, [_vp, ctypes.POINTER(Diagnostics)]),
     "bemgpu_pressure": (ctypes.c_int, [_vp, _i32, _i64, _dp, _i32, _dp]),

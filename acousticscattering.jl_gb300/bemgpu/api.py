@@ -22,6 +22,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import warnings
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -459,9 +460,32 @@ class BEMSolution:
                                            C.FIELDS[field], C.dptr(out)), self.ctx.handle)
         return out
 
+    def hmatrix_stats(self) -> dict:
+        """Compression and GMRES statistics (compressed-operator solutions)."""
+        st = C.HmatrixStats()
+        _check(C.lib().bemgpu_hmatrix_stats_get(self.handle, ctypes.byref(st)), self.ctx.handle)
+        return {f: getattr(st, f) for f, _ in C.HmatrixStats._fields_ if f != "pad"}
+
+    def residual_history(self, rhs: int = 0) -> np.ndarray:
+        """GMRES residual estimates, one per Arnoldi step (compressed-operator solutions)."""
+        cnt = ctypes.c_int32()
+        _check(C.lib().bemgpu_gmres_history(self.handle, rhs, None, 0, ctypes.byref(cnt)),
+               self.ctx.handle)
+        out = np.zeros(max(1, cnt.value))
+        _check(C.lib().bemgpu_gmres_history(self.handle, rhs, C.dptr(out), cnt.value,
+                                            ctypes.byref(cnt)), self.ctx.handle)
+        return out[:cnt.value]
+
     def diagnostics(self) -> dict:
         d = C.Diagnostics()
         _check(C.lib().bemgpu_solution_diagnostics(self.handle, ctypes.byref(d)))
+        if self.method == "hmatrix":  # the reference's GMRES diagnostics (full.jl:160-176)
+            st = self.hmatrix_stats()
+            return _diag_dict(d, {"method": "gmres", "converged": bool(st["gmres_converged"]),
+                                  "iterations": st["gmres_iterations"],
+                                  "residual_history": self.residual_history(0),
+                                  "compression": st, "meshsize": self.body.resolution,
+                                  "illumination": "plane_wave", "mesh_hash": self.body.hash})
         if isinstance(self.body, (list, tuple)):  # coupled regions
             return _diag_dict(d, {"meshsize": max(s_.resolution for s_ in self.body),
                                   "illumination": "plane_wave", "interface_count": len(self.body),
@@ -481,16 +505,109 @@ class BEMSolution:
             pass
 
 
+# ------------------------------------------------------------------ compressed operators
+_GMRES_KEYS = {"reltol", "abstol", "restart", "maxiter"}
+
+
+def _hmatrix_options(compression, gmres_kwargs):
+    """HmatrixOptions for compression=(method=:hmatrix, tol[, eta, leaf_size]) with
+    gmres_kwargs, or None for the dense path (full.jl:52-58 defaults)."""
+    comp = dict(compression or {"method": "none"})
+    method = comp.pop("method", "none")
+    gm = dict(gmres_kwargs or {})
+    if set(gm) - _GMRES_KEYS:
+        raise ArgumentError(f"unknown gmres option(s): {sorted(set(gm) - _GMRES_KEYS)}")
+    if method == "none":
+        if comp:
+            raise ArgumentError("compression=(method=:none,) takes no other options")
+        return None
+    if method != "hmatrix":
+        raise ArgumentError("compression method must be :none or :hmatrix")
+    if set(comp) - {"tol", "eta", "leaf_size"}:
+        raise ArgumentError(f"unknown compression option(s): "
+                            f"{sorted(set(comp) - {'tol', 'eta', 'leaf_size'})}")
+    o = C.HmatrixOptions()
+    C.lib().bemgpu_hmatrix_options_init(ctypes.byref(o))
+    o.tol = float(comp.get("tol", o.tol))
+    o.eta = float(comp.get("eta", o.eta))
+    o.leaf_size = int(comp.get("leaf_size", o.leaf_size))
+    o.reltol = float(gm.get("reltol", o.reltol))
+    o.abstol = float(gm.get("abstol", o.abstol))
+    o.restart = int(gm.get("restart", o.restart))
+    o.maxiter = int(gm.get("maxiter", o.maxiter))
+    return o
+
+
+def _bem_hmatrix(surface, boundary, k, angles, azimuths, opts, *, formulation, precision, ctx):
+    if isinstance(boundary, FluidFilled):
+        raise ArgumentError(
+            "hierarchical compression applies to Rigid and PressureRelease boundaries")
+    if precision != "double":
+        raise ArgumentError("hierarchical compression computes in double precision")
+    ctx = ctx or context()
+    p = _problem(boundary, k, formulation=formulation, precision="double")
+    angles = np.atleast_1d(np.asarray(angles, dtype=np.float64))
+    az = np.broadcast_to(np.asarray(azimuths, dtype=np.float64), angles.shape)
+    inc = np.ascontiguousarray(np.stack([angles, az], axis=1).reshape(-1))
+    h = ctypes.c_void_p()
+    _check(C.lib().bemgpu_hmatrix_solve(ctx.handle, surface.handle(ctx), ctypes.byref(p),
+                                        ctypes.byref(opts), len(angles), C.dptr(inc),
+                                        ctypes.byref(h)), ctx.handle)
+    sol = BEMSolution(ctx, h, surface, boundary, k, angles, az)
+    sol.method = "hmatrix"
+    st = sol.hmatrix_stats()
+    if not st["gmres_converged"]:
+        warnings.warn("solve_full_bem: GMRES did not converge to the requested tolerance, "
+                      f"result may be inaccurate (boundary={boundary}, "
+                      f"iters={st['gmres_iterations']})", RuntimeWarning, stacklevel=3)
+    return sol
+
+
+def hmatrix_apply(surface: Mesh, boundary, k, X, *, op=0, formulation=None, tol=1e-5,
+                  eta=3.0, leaf_size=64, ctx=None):
+    """Products M X of the compressed rigid/soft operators (op 0: M1 = 1/2 I - D - a H,
+    op 1: M2 = S + a (1/2 I + K')) and their statistics, for inspecting the compression."""
+    ctx = ctx or context()
+    p = _problem(boundary, k, formulation=formulation, precision="double")
+    o = _hmatrix_options(dict(method="hmatrix", tol=tol, eta=eta, leaf_size=leaf_size), None)
+    X = np.asarray(X, dtype=np.complex128)
+    if X.ndim == 1:
+        X = X[:, None]
+    X = np.asfortranarray(X)
+    Y = np.zeros_like(X, order="F")
+    st = C.HmatrixStats()
+    _check(C.lib().bemgpu_hmatrix_apply(ctx.handle, surface.handle(ctx), ctypes.byref(p),
+                                        ctypes.byref(o), int(op), X.shape[1], C.dptr(X),
+                                        C.dptr(Y), ctypes.byref(st)), ctx.handle)
+    return Y, {f: getattr(st, f) for f, _ in C.HmatrixStats._fields_ if f != "pad"}
+
+
 # ------------------------------------------------------------------ reference-named API
 def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_azimuth=0.0,
         formulation=None, precision="double", equilibrate=True, refinement=None,
-        assembly=None, ctx: Context | None = None, parents=None,
-        **unsupported) -> BEMSolution:
+        assembly=None, ctx: Context | None = None, parents=None, compression=None,
+        gmres_kwargs=None, **unsupported) -> BEMSolution:
     """Full-3D BEM on a supplied surface (solvers/bem/surface.jl:10-23), or, given lists of
     surfaces and FluidFilled materials, the coupled fluid regions of
-    bem(surfaces, materials, k; parents) (solvers/bem/regions.jl:132-150)."""
+    bem(surfaces, materials, k; parents) (solvers/bem/regions.jl:132-150).
+
+    compression=dict(method="hmatrix", tol=1e-5) selects the reference's compressed
+    operators with GMRES (solve_full_bem, full.jl:52-58; gmres_kwargs reltol, abstol,
+    restart, maxiter as there) for Rigid and PressureRelease bodies.  Without it (or with
+    method="none") the system is factored densely; gmres_kwargs then have no effect, as the
+    direct solve meets any GMRES tolerance."""
     if unsupported:
         raise ArgumentError(f"unsupported option(s): {sorted(unsupported)}")
+    hm = _hmatrix_options(compression, gmres_kwargs)
+    if hm is not None:
+        if isinstance(surface, (list, tuple)) or parents is not None:
+            raise ArgumentError("hierarchical compression applies to a single surface")
+        if not isinstance(surface, Mesh):
+            raise ArgumentError("surface must be a Mesh from mesh(nodes, triangles)")
+        if not (math.isfinite(incidence_angle) and math.isfinite(incidence_azimuth)):
+            raise ArgumentError("incidence angles must be finite")
+        return _bem_hmatrix(surface, boundary, k, [incidence_angle], [incidence_azimuth], hm,
+                            formulation=formulation, precision=precision, ctx=ctx)
     if isinstance(surface, (list, tuple)):
         return _bem_regions(list(surface), boundary, k, parents=parents,
                             incidence_angle=incidence_angle,
@@ -713,15 +830,27 @@ class SweepResult:
 
 def incidence_angle_sweep(surface: Mesh, boundary, k, angles, *, incidence_azimuth=0.0,
                           formulation=None, precision="double", equilibrate=True,
-                          refinement=None, assembly=None, ctx=None) -> SweepResult:
+                          refinement=None, assembly=None, ctx=None, compression=None,
+                          gmres_kwargs=None) -> SweepResult:
     """Backscatter at many polar incidence angles from one factorisation
     (postprocessing/sweeps.jl:626-701): assembled and factored once, all angles
-    solved as one multi-right-hand-side batch."""
+    solved as one multi-right-hand-side batch.  With compression=(method=:hmatrix, ...)
+    the operators are compressed once and every angle runs its own GMRES (batched)."""
     angles = np.asarray(angles, dtype=np.float64)
     if angles.ndim != 1 or angles.size == 0 or not np.all(np.isfinite(angles)):
         raise ArgumentError("angles must be a nonempty vector of finite values")
     if not math.isfinite(incidence_azimuth):
         raise ArgumentError("incidence_azimuth must be finite")
+    hm = _hmatrix_options(compression, gmres_kwargs)
+    if hm is not None:
+        sol = _bem_hmatrix(surface, boundary, k, angles, incidence_azimuth, hm,
+                           formulation=formulation, precision=precision, ctx=ctx)
+        try:
+            amps = np.array([scattering_amplitude(sol, rhs=r) for r in range(len(angles))])
+            diag = sol.diagnostics()
+        finally:
+            sol.close()
+        return SweepResult(angles, amps, 20 * np.log10(np.abs(amps)), diag)
     f = Factor(surface, boundary, k, ctx=ctx, formulation=formulation, precision=precision,
                equilibrate=equilibrate, refinement=refinement, assembly=assembly)
     try:

@@ -27,6 +27,8 @@
 #include "linalg.cuh"
 #include "refine.cuh"
 #include "gemm_tc.cuh"
+#include "hmatrix.cuh"
+#include "hmatrix_plan.h"
 #include "pressure.cuh"
 #include "solve_kernels.cuh"
 
@@ -524,6 +526,11 @@ struct SolutionData {
   Buf xsol;                  // coupled regions: the solved unknowns [p; v], 2n x nrhs
   bool region = false;
   bemgpu_diagnostics diag{};
+  bool hmatrix = false;                 // from bemgpu_hmatrix_solve
+  bemgpu_hmatrix_stats hm{};
+  std::vector<double> gm_hist;          // residual estimates, gm_stride per rhs
+  std::vector<int32_t> gm_iters;
+  int32_t gm_stride = 0;
 };
 }  // namespace
 
@@ -2710,6 +2717,587 @@ int bemgpu_traces(const bemgpu_solution* sol, int32_t rhs, double* p, double* q)
                                 c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return BEMGPU_OK;
+}
+
+// ===================================================================== hierarchical matrices
+namespace {
+
+// Compressed M1 / M2 of one rigid/soft problem on one mesh.
+struct HmData {
+  HmPlan plan;
+  Buf perm, iperm, leaf_lo, leaf_ptr, leaf_ent, dn, D1, D2;
+  Buf lr[2], U[2], V[2];
+  int32_t n_lr = 0, n_dense = 0, n_leaf = 0;
+  int64_t tstride = 0;
+  bemgpu_hmatrix_stats st{};
+  size_t bytes() const {
+    size_t b = perm.bytes + iperm.bytes + leaf_lo.bytes + leaf_ptr.bytes + leaf_ent.bytes +
+               dn.bytes + D1.bytes + D2.bytes;
+    for (int o = 0; o < 2; ++o) b += lr[o].bytes + U[o].bytes + V[o].bytes;
+    return b;
+  }
+  HmOp op(int o, double* T) const {
+    HmOp A{};
+    A.lr = lr[o].as<HmLR>();
+    A.dn = dn.as<HmDense>();
+    A.U = U[o].as<double>();
+    A.V = V[o].as<double>();
+    A.D = (o == 0 ? D1 : D2).as<double>();
+    A.leaf_lo = leaf_lo.as<int32_t>();
+    A.leaf_ptr = leaf_ptr.as<int32_t>();
+    A.leaf_ent = leaf_ent.as<int32_t>();
+    A.n_lr = n_lr;
+    A.n_dense = n_dense;
+    A.n_leaf = n_leaf;
+    A.T = T;
+    A.tstride = tstride;
+    return A;
+  }
+};
+
+int check_hm_options(bemgpu_ctx* c, const bemgpu_hmatrix_options& o) {
+  if (!(std::isfinite(o.tol) && o.tol > 0 && o.tol < 1))
+    return fail(c, BEMGPU_EINVAL, "compression tolerance must lie in (0, 1)");
+  if (!(std::isfinite(o.eta) && o.eta > 0))
+    return fail(c, BEMGPU_EINVAL, "admissibility eta must be finite and positive");
+  if (o.leaf_size < 8 || o.leaf_size > 64)
+    return fail(c, BEMGPU_EINVAL, "leaf_size must lie in [8, 64]");
+  if (o.restart < 1 || o.restart > 500)
+    return fail(c, BEMGPU_EINVAL, "restart must lie in [1, 500]");
+  if (!(std::isfinite(o.reltol) && o.reltol >= 0 && std::isfinite(o.abstol) && o.abstol >= 0))
+    return fail(c, BEMGPU_EINVAL, "GMRES tolerances must be finite and nonnegative");
+  if (o.maxiter < 0) return fail(c, BEMGPU_EINVAL, "maxiter must be a nonnegative integer");
+  return BEMGPU_OK;
+}
+
+// Cluster tree and blocks on the host, cross approximation of both operators, full
+// blocks (regular kernel + near kernel into block storage), product lists.
+int hm_build(bemgpu_ctx* c, const MeshData* m, const bemgpu_problem& p, int kind,
+             const bemgpu_hmatrix_options& o, HmData* H) {
+  const Launch L = c->launch();
+  Timer tb(c->stream);
+  const int64_t n = m->n;
+  std::vector<double> cent, diam;
+  panel_centroids(m->nodes_h.data(), m->tris_h.data(), n, &cent, &diam);
+  std::string err;
+  if (hm_build_plan(cent.data(), diam.data(), n, o.leaf_size, o.eta, m->eta, &H->plan, &err))
+    return fail(c, BEMGPU_EINVAL, err);
+  const HmPlan& P = H->plan;
+  const double k = p.k;
+  const double a_re = 0.0, a_im = kind == kAsmBM ? 1.0 / k : 0.0;  // alpha = i / k
+  // admissible blocks: rank capacity below the size where a full block is cheaper
+  std::vector<HmLR> lr(P.lowrank.size());
+  int64_t uo = 0, vo = 0, to = 0;
+  int32_t max_m = 1;
+  for (size_t b = 0; b < lr.size(); ++b) {
+    const HmBlock& B = P.lowrank[b];
+    const int64_t cap = (int64_t)B.m * B.n / ((int64_t)B.m + B.n);
+    const int32_t kmax = (int32_t)std::max<int64_t>(1, std::min<int64_t>(kHmMaxRank, cap));
+    lr[b] = HmLR{B.rlo, B.m, B.clo, B.n, uo, vo, to, kmax, 0, 0, 0};
+    uo += (int64_t)B.m * kmax;
+    vo += (int64_t)B.n * kmax;
+    to += kmax;
+    max_m = std::max(max_m, B.m);
+  }
+  TRY(upload(c, P.perm, &H->perm));
+  TRY(upload(c, P.iperm, &H->iperm));
+  std::vector<HmLR> lrh[2];
+  for (int op = 0; op < 2; ++op) {
+    TRY(upload(c, lr, &H->lr[op]));
+    TRY(alloc(c, (size_t)std::max<int64_t>(1, uo) * 16, &H->U[op]));
+    TRY(alloc(c, (size_t)std::max<int64_t>(1, vo) * 16, &H->V[op]));
+    {
+      Prof pr(c, "hm_aca");
+      launch_hm_aca(L, H->lr[op].as<HmLR>(), (int32_t)lr.size(), max_m, H->U[op].as<double>(),
+                    H->V[op].as<double>(), m->panels.as<double>(), H->perm.as<int32_t>(), kind,
+                    op, k, a_re, a_im, o.tol);
+    }
+    CUDA_TRY(c, cudaGetLastError());
+  }
+  for (int op = 0; op < 2; ++op) TRY(download(c, H->lr[op], &lrh[op], lr.size()));
+  // blocks whose approximation did not converge within the cap are stored in full
+  std::vector<HmDense> dn;
+  std::vector<HmBlock> dblk = P.dense, lblk;
+  std::vector<HmLR> keep[2];
+  int64_t off = 0;
+  for (const HmBlock& B : P.dense) {
+    dn.push_back(HmDense{B.rlo, B.m, B.clo, B.n, off});
+    off += (int64_t)B.m * B.n;
+  }
+  int64_t densified = 0, lr_entries = 0;
+  int32_t max_rank = 0;
+  for (size_t b = 0; b < lr.size(); ++b) {
+    if (!lrh[0][b].conv || !lrh[1][b].conv) {
+      const HmBlock& B = P.lowrank[b];
+      dn.push_back(HmDense{B.rlo, B.m, B.clo, B.n, off});
+      dblk.push_back(B);
+      off += (int64_t)B.m * B.n;
+      ++densified;
+      continue;
+    }
+    lblk.push_back(P.lowrank[b]);
+    for (int op = 0; op < 2; ++op) {
+      keep[op].push_back(lrh[op][b]);
+      lr_entries += (int64_t)lrh[op][b].rank * (lrh[op][b].m + lrh[op][b].n);
+      max_rank = std::max(max_rank, lrh[op][b].rank);
+    }
+  }
+  H->n_dense = (int32_t)dn.size();
+  H->n_lr = (int32_t)lblk.size();
+  H->tstride = std::max<int64_t>(1, to);
+  TRY(upload(c, dn, &H->dn));
+  TRY(alloc(c, (size_t)std::max<int64_t>(1, off) * 16, &H->D1));
+  TRY(alloc(c, (size_t)std::max<int64_t>(1, off) * 16, &H->D2));
+  for (int op = 0; op < 2; ++op) TRY(upload(c, keep[op], &H->lr[op]));
+  {
+    Prof pr(c, "hm_dense");
+    launch_hm_dense(L, H->dn.as<HmDense>(), H->n_dense, H->D1.as<double>(), H->D2.as<double>(),
+                    m->panels.as<double>(), H->perm.as<int32_t>(), kind, k, a_re, a_im);
+  }
+  // near pairs (the mesh's list, same order) into their full leaf blocks
+  if (m->n_near > 0) {
+    std::vector<int64_t> rowptr, cols;
+    near_pairs(cent, diam, m->eta, &rowptr, &cols);
+    if ((int64_t)cols.size() != m->n_near)
+      return fail(c, BEMGPU_EINVAL, "internal: near-pair list differs from the mesh's");
+    const int64_t nl = (int64_t)P.leaf_lo.size() - 1;
+    auto leaf_of = [&](int32_t pos) {
+      return (int64_t)(std::upper_bound(P.leaf_lo.begin(), P.leaf_lo.end(), pos) -
+                       P.leaf_lo.begin() - 1);
+    };
+    std::map<int64_t, int32_t> blk;
+    for (size_t b = 0; b < P.dense.size(); ++b)
+      blk[(int64_t)leaf_of(P.dense[b].rlo) * nl + leaf_of(P.dense[b].clo)] = (int32_t)b;
+    std::vector<int64_t> dst((size_t)m->n_near);
+    for (int64_t i = 0; i < n; ++i)
+      for (int64_t q = rowptr[i]; q < rowptr[i + 1]; ++q) {
+        const int32_t pi = P.iperm[(size_t)i], pj = P.iperm[(size_t)cols[q]];
+        auto it = blk.find(leaf_of(pi) * nl + leaf_of(pj));
+        if (it == blk.end())
+          return fail(c, BEMGPU_EINVAL, "internal: near pair outside the full blocks");
+        const HmDense& D = dn[(size_t)it->second];
+        dst[(size_t)q] = D.off + (pi - D.rlo) + (int64_t)(pj - D.clo) * D.m;
+      }
+    Buf d_dst, d_ai;
+    TRY(upload(c, dst, &d_dst));
+    AsmInst I{};
+    I.panels = m->panels.as<double>();
+    I.panelsf = m->panelsf.as<float>();
+    I.verts = m->verts.as<double>();
+    I.near_i = m->near_i.as<int32_t>();
+    I.near_j = m->near_j.as<int32_t>();
+    I.near_lap = m->near_lap.as<double>();
+    I.n = n;
+    I.n_near = m->n_near;
+    I.lda = n;
+    I.k_e = I.k_i = k;
+    I.g = 1.0;
+    I.a_re = a_re;
+    I.a_im = a_im;
+    I.kind = kind;
+    I.out1 = H->D1.p;
+    I.out2 = H->D2.p;
+    I.near_dst = d_dst.as<int64_t>();
+    std::vector<AsmInst> ai{I};
+    TRY(upload(c, ai, &d_ai));
+    {
+      Prof pr(c, "near");
+      launch_assemble_near(L, d_ai.as<AsmInst>(), 1, m->n_near, kind, false);
+    }
+    CUDA_TRY(c, cudaGetLastError());
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // d_dst / d_ai are released below
+  }
+  std::vector<int32_t> ptr, ent;
+  hm_leaf_lists(P, dblk, lblk, &ptr, &ent);
+  H->n_leaf = (int32_t)ptr.size() - 1;
+  TRY(upload(c, P.leaf_lo, &H->leaf_lo));
+  TRY(upload(c, ptr, &H->leaf_ptr));
+  TRY(upload(c, ent, &H->leaf_ent));
+  CUDA_TRY(c, cudaGetLastError());
+  bemgpu_hmatrix_stats& S = H->st;
+  std::memset(&S, 0, sizeof S);
+  S.lowrank_blocks = H->n_lr;
+  S.dense_blocks = H->n_dense;
+  S.densified_blocks = densified;
+  S.lowrank_entries = lr_entries;
+  S.dense_entries = 2 * off;
+  S.max_rank = max_rank;
+  S.depth = P.depth;
+  S.leaves = H->n_leaf;
+  S.compression = (double)(lr_entries + 2 * off) / (2.0 * (double)n * (double)n);
+  S.build_ms = tb.stop();
+  return BEMGPU_OK;
+}
+
+// GMRES on A x = b for nr right-hand sides (permuted order, n x nr each), grouped so
+// that the Krylov bases fit the context budget.  x receives the solutions; hist, iters,
+// conv, resid receive per right-hand side the residual estimates (maxiter per rhs), the
+// Arnoldi steps, the convergence flag and |b - A x| / |b|.
+int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x, int64_t n,
+             int32_t nr, const bemgpu_hmatrix_options& o, std::vector<double>* hist,
+             std::vector<int32_t>* iters, std::vector<int32_t>* conv, std::vector<double>* resid,
+             std::vector<double>* absres) {
+  const Launch L = c->launch();
+  const int32_t R = o.restart, mi = std::max(1, o.maxiter);
+  const int32_t chunks = (int32_t)((n + 4095) / 4096);
+  const size_t per = ((size_t)(R + 1) * n + 2 * (size_t)n) * 16 + (size_t)(R + 1) * R * 16 +
+                     (size_t)chunks * (R + 1) * 16 + (size_t)mi * 8 + (size_t)H.tstride * 16 +
+                     (size_t)(4 * R + 8) * 16;
+  const uint64_t avail = c->budget > c->live ? (c->budget - c->live) : 0;
+  const int32_t G = (int32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)nr, avail / 2 / per));
+  hist->assign((size_t)nr * mi, 0.0);
+  iters->assign((size_t)nr, 0);
+  conv->assign((size_t)nr, 0);
+  resid->assign((size_t)nr, 0.0);
+  absres->assign((size_t)nr, 0.0);
+  for (int32_t r0 = 0; r0 < nr; r0 += G) {
+    const int32_t g = std::min(G, nr - r0);
+    Buf st, Vb, Hh, cs, sn, gg, hc, part, hb, w, T, nact;
+    TRY(alloc(c, sizeof(GmState) * g, &st));
+    TRY(alloc(c, (size_t)g * (R + 1) * n * 16, &Vb));
+    TRY(alloc(c, (size_t)g * (R + 1) * R * 16, &Hh));
+    TRY(alloc(c, (size_t)g * R * 8, &cs));
+    TRY(alloc(c, (size_t)g * R * 16, &sn));
+    TRY(alloc(c, (size_t)g * (R + 1) * 16, &gg));
+    TRY(alloc(c, (size_t)g * (R + 1) * 16, &hc));
+    TRY(alloc(c, (size_t)g * chunks * (R + 1) * 16, &part));
+    TRY(alloc(c, (size_t)g * mi * 8, &hb));
+    TRY(alloc(c, (size_t)g * n * 16, &w));
+    TRY(alloc(c, (size_t)g * H.tstride * 16, &T));
+    TRY(alloc(c, sizeof(int32_t), &nact));
+    CUDA_TRY(c, cudaMemsetAsync(st.p, 0, st.bytes, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(Hh.p, 0, Hh.bytes, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(gg.p, 0, gg.bytes, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(hb.p, 0, hb.bytes, c->stream));
+    double* xg = x + 2 * (size_t)r0 * n;
+    const double* bg = b + 2 * (size_t)r0 * n;
+    CUDA_TRY(c, cudaMemsetAsync(xg, 0, (size_t)g * n * 16, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(w.p, bg, (size_t)g * n * 16, cudaMemcpyDeviceToDevice, c->stream));
+    GmWork W{};
+    W.st = st.as<GmState>();
+    W.Vb = Vb.as<double>();
+    W.H = Hh.as<double>();
+    W.cs = cs.as<double>();
+    W.sn = sn.as<double>();
+    W.g = gg.as<double>();
+    W.hc = hc.as<double>();
+    W.part = part.as<double>();
+    W.hist = hb.as<double>();
+    W.x = xg;
+    W.b = bg;
+    W.w = w.as<double>();
+    W.n = n;
+    W.nr = g;
+    W.restart = R;
+    W.maxiter = mi;
+    W.chunks = chunks;
+    W.nact = nact.as<int32_t>();
+    const HmOp A = H.op(op, T.as<double>());
+    auto active = [&](int32_t* out) -> int {
+      CUDA_TRY(c, cudaMemcpyAsync(out, W.nact, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+      CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+      return BEMGPU_OK;
+    };
+    {
+      Prof pr(c, "gmres");
+      if (o.maxiter == 0) W.maxiter = 0;  // the start step marks every rhs done
+      launch_gm_start(L, W, o.reltol, o.abstol, 1);
+      W.maxiter = mi;
+    }
+    int32_t na = 0;
+    TRY(active(&na));
+    if (o.maxiter == 0) na = 0;
+    while (na > 0) {
+      {
+        Prof pr(c, "gmres");
+        for (int32_t j = 0; j < R; ++j) {
+          launch_hm_matvec(L, A, W.Vb + 2 * (size_t)j * n, (int64_t)(R + 1) * n, W.w, n, nullptr,
+                           0, 0.0, 1.0, g, W.st, 1);
+          launch_gm_arnoldi(L, W, j);
+          launch_gm_rotate(L, W, j);
+          if ((j + 1) % 4 == 0 && j + 1 < R) {
+            TRY(active(&na));
+            if (na == 0) break;
+          }
+        }
+        launch_gm_update_x(L, W);
+        launch_hm_matvec(L, A, xg, n, W.w, n, bg, n, 1.0, -1.0, g, W.st, 2);
+        launch_gm_start(L, W, o.reltol, o.abstol, 0);
+      }
+      CUDA_TRY(c, cudaGetLastError());
+      TRY(active(&na));
+    }
+    // explicit residuals b - A x
+    {
+      Prof pr(c, "gmres");
+      launch_hm_matvec(L, A, xg, n, W.w, n, bg, n, 1.0, -1.0, g, nullptr, 0);
+    }
+    std::vector<double> wh;
+    TRY(download(c, w, &wh, (size_t)g * n * 2));
+    std::vector<GmState> sh;
+    TRY(download(c, st, &sh, (size_t)g));
+    std::vector<double> hh;
+    TRY(download(c, hb, &hh, (size_t)g * mi));
+    for (int32_t r = 0; r < g; ++r) {
+      double s = 0.0;
+      for (int64_t i = 0; i < 2 * n; ++i) s += wh[(size_t)r * 2 * n + i] * wh[(size_t)r * 2 * n + i];
+      const GmState& S = sh[(size_t)r];
+      (*absres)[(size_t)(r0 + r)] = std::sqrt(s);
+      (*resid)[(size_t)(r0 + r)] = S.bnorm > 0 ? std::sqrt(s) / S.bnorm : 0.0;
+      (*iters)[(size_t)(r0 + r)] = S.iters;
+      (*conv)[(size_t)(r0 + r)] = S.converged;
+      std::copy(hh.begin() + (size_t)r * mi, hh.begin() + (size_t)(r + 1) * mi,
+                hist->begin() + (size_t)(r0 + r) * mi);
+    }
+  }
+  return BEMGPU_OK;
+}
+
+int hm_problem(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_problem* problem,
+               const bemgpu_hmatrix_options* opt, int* kind) {
+  if (!mesh || !problem || !opt) return fail(c, BEMGPU_EINVAL, "null argument");
+  TRY(check_problem(c, *problem, kind));
+  if (*kind != kAsmBM && *kind != kAsmCBIE)
+    return fail(c, BEMGPU_EINVAL,
+                "hierarchical compression applies to Rigid and PressureRelease boundaries");
+  if (problem->precision != BEMGPU_DOUBLE)
+    return fail(c, BEMGPU_EINVAL, "hierarchical compression computes in double precision");
+  if (std::fabs(problem->near_eta - mesh->d->eta) > 0)
+    return fail(c, BEMGPU_EINVAL, "near_eta differs from the mesh's (upload with that eta)");
+  return check_hm_options(c, *opt);
+}
+
+}  // namespace
+
+void bemgpu_hmatrix_options_init(bemgpu_hmatrix_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof *o);
+  o->tol = 1e-5;
+  o->eta = 3.0;
+  o->leaf_size = 64;
+  o->restart = 150;
+  o->reltol = 1e-4;
+  o->abstol = 0.0;
+  o->maxiter = 1200;
+}
+
+int bemgpu_hmatrix_plan(const double* nodes, int64_t n_nodes, const int64_t* triangles,
+                        int64_t n_triangles, double near_eta, const bemgpu_hmatrix_options* opt,
+                        int64_t counts[4], int32_t* blocks, int64_t cap, int32_t* perm) {
+  if (!opt || !counts) return fail(nullptr, BEMGPU_EINVAL, "null argument");
+  TRY(check_hm_options(nullptr, *opt));
+  if (!(std::isfinite(near_eta) && near_eta > 0))
+    return fail(nullptr, BEMGPU_EINVAL, "near_eta must be finite and positive");
+  std::string e;
+  double res;
+  int s = validate_surface(nodes, n_nodes, triangles, n_triangles, &res, &e);
+  if (s != BEMGPU_OK) return fail(nullptr, s, e);
+  std::vector<double> cent, diam;
+  panel_centroids(nodes, triangles, n_triangles, &cent, &diam);
+  HmPlan P;
+  if (hm_build_plan(cent.data(), diam.data(), n_triangles, opt->leaf_size, opt->eta, near_eta,
+                    &P, &e))
+    return fail(nullptr, BEMGPU_EINVAL, e);
+  counts[0] = (int64_t)P.lowrank.size();
+  counts[1] = (int64_t)P.dense.size();
+  counts[2] = (int64_t)P.leaf_lo.size() - 1;
+  counts[3] = P.depth;
+  if (blocks) {
+    if (counts[0] + counts[1] > cap) return fail(nullptr, BEMGPU_EINVAL, "capacity too small");
+    int32_t* o = blocks;
+    for (const HmBlock& B : P.dense) {
+      o[0] = 0; o[1] = B.rlo; o[2] = B.m; o[3] = B.clo; o[4] = B.n;
+      o += 5;
+    }
+    for (const HmBlock& B : P.lowrank) {
+      o[0] = 1; o[1] = B.rlo; o[2] = B.m; o[3] = B.clo; o[4] = B.n;
+      o += 5;
+    }
+  }
+  if (perm) std::copy(P.perm.begin(), P.perm.end(), perm);
+  return BEMGPU_OK;
+}
+
+int bemgpu_hmatrix_solve(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_problem* problem,
+                         const bemgpu_hmatrix_options* opt, int32_t nrhs, const double* incidence,
+                         bemgpu_solution** solution) {
+  if (!c) return fail(nullptr, BEMGPU_EINVAL, "null context");
+  if (!incidence || !solution) return fail(c, BEMGPU_EINVAL, "null argument");
+  if (nrhs <= 0) return fail(c, BEMGPU_EINVAL, "nrhs must be positive");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  int kind = 0;
+  TRY(hm_problem(c, mesh, problem, opt, &kind));
+  const bemgpu_problem& p = *problem;
+  MeshData* m = mesh->d.get();
+  const int64_t n = m->n;
+  std::vector<double> dirs(3 * (size_t)nrhs);
+  for (int32_t r = 0; r < nrhs; ++r) {
+    const double be = incidence[2 * r], al = incidence[2 * r + 1];
+    if (!(std::isfinite(be) && std::isfinite(al)))
+      return fail(c, BEMGPU_EINVAL, "incidence angles must be finite");
+    dirs[3 * r] = std::cos(be);
+    dirs[3 * r + 1] = std::sin(be) * std::cos(al);
+    dirs[3 * r + 2] = std::sin(be) * std::sin(al);
+  }
+  Timer ttot(c->stream);
+  HmData H;
+  TRY(hm_build(c, m, p, kind, *opt, &H));
+  const Launch L = c->launch();
+  Timer tsol(c->stream);
+  auto sd = std::make_shared<SolutionData>();
+  sd->c = c;
+  sd->mesh = mesh->d;
+  sd->boundary = p.boundary;
+  sd->k = p.k;
+  sd->nrhs = nrhs;
+  sd->dirs = dirs;
+  Buf d_dirs, pinc, qinc, tp, bb, xp, xs, T, d_wi, d_ti;
+  TRY(upload(c, dirs, &d_dirs));
+  TRY(alloc(c, (size_t)n * nrhs * 16, &pinc));
+  TRY(alloc(c, (size_t)n * nrhs * 16, &qinc));
+  TRY(alloc(c, (size_t)n * nrhs * 16, &tp));
+  TRY(alloc(c, (size_t)n * nrhs * 16, &bb));
+  TRY(alloc(c, (size_t)n * nrhs * 16, &xp));
+  TRY(alloc(c, (size_t)n * nrhs * 16, &xs));
+  TRY(alloc(c, (size_t)H.tstride * nrhs * 16, &T));
+  TRY(alloc(c, (size_t)n * nrhs * 16, &sd->ps));
+  TRY(alloc(c, (size_t)n * nrhs * 16, &sd->qs));
+  WaveInst wv{};
+  wv.panels = m->panels.as<double>();
+  wv.n = n;
+  wv.k = p.k;
+  wv.nrhs = nrhs;
+  wv.dirs = d_dirs.as<double>();
+  wv.p = pinc.as<double>();
+  wv.q = qinc.as<double>();
+  wv.ldp = n;
+  std::vector<WaveInst> wi{wv};
+  TRY(upload(c, wi, &d_wi));
+  {
+    Prof pr(c, "incident");
+    launch_incident(L, d_wi.as<WaveInst>(), 1, n, nrhs);
+  }
+  // rigid: A = M1, b = M2 q_inc; soft: A = M2, b = M1 p_inc (full.jl:98-128, 144-152)
+  const bool rigid = p.boundary == BEMGPU_RIGID;
+  const int sys = rigid ? 0 : 1;
+  launch_hm_permute(L, (rigid ? qinc : pinc).as<double>(), n, tp.as<double>(), n,
+                    H.perm.as<int32_t>(), n, nrhs);
+  {
+    Prof pr(c, "hm_matvec");
+    launch_hm_matvec(L, H.op(1 - sys, T.as<double>()), tp.as<double>(), n, bb.as<double>(), n,
+                     nullptr, 0, 0.0, 1.0, nrhs, nullptr, 0);
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  std::vector<double> resid, absres;
+  std::vector<int32_t> conv;
+  TRY(hm_gmres(c, H, sys, bb.as<double>(), xp.as<double>(), n, nrhs, *opt, &sd->gm_hist,
+               &sd->gm_iters, &conv, &resid, &absres));
+  sd->gm_stride = std::max(1, opt->maxiter);
+  launch_hm_permute(L, xp.as<double>(), n, xs.as<double>(), n, H.iperm.as<int32_t>(), n, nrhs);
+  TraceInst tr{};
+  tr.x = xs.as<double>();
+  tr.ldx = n;
+  tr.pinc = pinc.as<double>();
+  tr.qinc = qinc.as<double>();
+  tr.n = n;
+  tr.ps = sd->ps.as<double>();
+  tr.qs = sd->qs.as<double>();
+  tr.nrhs = nrhs;
+  tr.kind = rigid ? 0 : 1;
+  std::vector<TraceInst> ti{tr};
+  TRY(upload(c, ti, &d_ti));
+  launch_traces(L, d_ti.as<TraceInst>(), 1, n, nrhs);
+  CUDA_TRY(c, cudaGetLastError());
+  const double sol_ms = tsol.stop();
+  TRY(check_device_error(c));
+  bemgpu_hmatrix_stats& S = sd->hm;
+  S = H.st;
+  S.gmres_converged = 1;
+  for (int32_t r = 0; r < nrhs; ++r) {
+    S.gmres_iterations = std::max(S.gmres_iterations, sd->gm_iters[(size_t)r]);
+    S.gmres_converged &= conv[(size_t)r];
+  }
+  S.gmres_ms = sol_ms;
+  sd->hmatrix = true;
+  bemgpu_diagnostics& dg = sd->diag;
+  std::memset(&dg, 0, sizeof dg);
+  dg.unknown_count = n;
+  dg.quadrature_nodes = n;
+  dg.near_pairs = m->n_near;
+  dg.formulation = kind == kAsmBM ? BEMGPU_BURTON_MILLER : BEMGPU_CBIE;
+  dg.precision = BEMGPU_DOUBLE;
+  dg.factor_precision = 1;
+  dg.refinement_iterations = S.gmres_iterations;
+  dg.coupling_im = kind == kAsmBM ? 1.0 / p.k : 0.0;
+  for (int32_t r = 0; r < nrhs; ++r) {
+    dg.absolute_residual = std::max(dg.absolute_residual, absres[(size_t)r]);
+    dg.relative_residual = std::max(dg.relative_residual, resid[(size_t)r]);
+  }
+  dg.scaled_absolute_residual = dg.absolute_residual;
+  dg.scaled_relative_residual = dg.relative_residual;
+  dg.assemble_ms = H.st.build_ms;
+  dg.solve_ms = sol_ms;
+  dg.total_ms = ttot.stop();
+  dg.device_bytes = (int64_t)H.bytes();
+  dg.nrhs = nrhs;
+  *solution = new bemgpu_solution{sd};
+  return BEMGPU_OK;
+}
+
+int bemgpu_hmatrix_stats_get(const bemgpu_solution* sol, bemgpu_hmatrix_stats* stats) {
+  if (!sol || !stats) return fail(nullptr, BEMGPU_EINVAL, "null argument");
+  if (!sol->d->hmatrix) return fail(sol->d->c, BEMGPU_EINVAL, "not a hierarchical-matrix solution");
+  *stats = sol->d->hm;
+  return BEMGPU_OK;
+}
+
+int bemgpu_gmres_history(const bemgpu_solution* sol, int32_t rhs, double* out, int32_t cap,
+                         int32_t* count) {
+  if (!sol || !count) return fail(nullptr, BEMGPU_EINVAL, "null argument");
+  const SolutionData* s = sol->d.get();
+  if (!s->hmatrix) return fail(s->c, BEMGPU_EINVAL, "not a hierarchical-matrix solution");
+  if (rhs < 0 || rhs >= s->nrhs) return fail(s->c, BEMGPU_EINVAL, "rhs index out of range");
+  const int32_t it = std::min(s->gm_iters[(size_t)rhs], s->gm_stride);
+  *count = it;
+  if (out)
+    for (int32_t i = 0; i < std::min(it, cap); ++i)
+      out[i] = s->gm_hist[(size_t)rhs * s->gm_stride + i];
+  return BEMGPU_OK;
+}
+
+int bemgpu_hmatrix_apply(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_problem* problem,
+                         const bemgpu_hmatrix_options* opt, int32_t op, int32_t nr,
+                         const double* X, double* Y, bemgpu_hmatrix_stats* stats) {
+  if (!c) return fail(nullptr, BEMGPU_EINVAL, "null context");
+  if (op != 0 && op != 1) return fail(c, BEMGPU_EINVAL, "op must be 0 (M1) or 1 (M2)");
+  if (nr < 0 || (nr > 0 && (!X || !Y))) return fail(c, BEMGPU_EINVAL, "invalid vectors");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  int kind = 0;
+  TRY(hm_problem(c, mesh, problem, opt, &kind));
+  MeshData* m = mesh->d.get();
+  const int64_t n = m->n;
+  HmData H;
+  TRY(hm_build(c, m, *problem, kind, *opt, &H));
+  if (stats) *stats = H.st;
+  if (nr == 0) return BEMGPU_OK;
+  const Launch L = c->launch();
+  Buf xh, xp, yp, yh, T;
+  TRY(alloc(c, (size_t)n * nr * 16, &xh));
+  TRY(alloc(c, (size_t)n * nr * 16, &xp));
+  TRY(alloc(c, (size_t)n * nr * 16, &yp));
+  TRY(alloc(c, (size_t)n * nr * 16, &yh));
+  TRY(alloc(c, (size_t)H.tstride * nr * 16, &T));
+  CUDA_TRY(c, cudaMemcpyAsync(xh.p, X, (size_t)n * nr * 16, cudaMemcpyHostToDevice, c->stream));
+  launch_hm_permute(L, xh.as<double>(), n, xp.as<double>(), n, H.perm.as<int32_t>(), n, nr);
+  launch_hm_matvec(L, H.op(op, T.as<double>()), xp.as<double>(), n, yp.as<double>(), n, nullptr, 0,
+                   0.0, 1.0, nr, nullptr, 0);
+  launch_hm_permute(L, yp.as<double>(), n, yh.as<double>(), n, H.iperm.as<int32_t>(), n, nr);
+  CUDA_TRY(c, cudaMemcpyAsync(Y, yh.p, (size_t)n * nr * 16, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  CUDA_TRY(c, cudaGetLastError());
+  return check_device_error(c);
 }
 
 int bemgpu_region_solve(bemgpu_ctx* c, int32_t count, const bemgpu_mesh* const* surfaces,

@@ -107,6 +107,8 @@ struct AsmInst {
   double* dnear2;          // complex64 out2: FP64 near corrections [n_near]
   const int32_t* surf;     // kAsmRegion: surface of every panel
   const RegionTable* region;  // kAsmRegion: coupling table
+  const int64_t* near_dst;  // kAsmBM / kAsmCBIE: when set, index of near pair p in
+                            // out1 / out2 (blocked storage) instead of i + j lda
 };
 
 // Incident field / far-field instance.

@@ -1,0 +1,661 @@
+// Hierarchical-matrix operators and batched restarted GMRES on the device.
+//
+// Compressed operators (the reference's compression=(method=:hmatrix, tol) of
+// solvers/bem/full.jl:89-97, which builds Inti operators compressed by HMatrices.jl):
+//  * admissible blocks: adaptive cross approximation with partial pivoting, one CTA per
+//    block, the matrix entries evaluated on demand by the same regular 7-point rule as
+//    the dense assembly (admissible blocks hold no near pair, so the regular rule is the
+//    entry), stopped when |u_r| |v_r| <= tol |S_r|_F with the Frobenius norm of the
+//    running approximation updated exactly from the projections of the new cross;
+//  * full leaf blocks: the regular kernel here, then the near-pair kernel of the dense
+//    assembly writing into block storage (AsmInst.near_dst);
+//  * products: coefficients V^T x of every admissible block (one warp per rank column),
+//    then one CTA per row leaf that sums, in the fixed order of its block list, the full
+//    blocks and the U (V^T x) terms covering its rows.  No atomics: every output element
+//    has one writer and a fixed summation order.
+// GMRES (IterativeSolvers.gmres as called by solvers/bem/full.jl:153-154: x0 = 0,
+// stopping when the residual estimate <= max(reltol |b|, abstol), restart and maxiter in
+// Arnoldi steps): classical Gram-Schmidt with one reorthogonalisation (CGS2: the same
+// Krylov basis as modified Gram-Schmidt up to rounding, with the projections as
+// parallel dot products), complex Givens rotations, an explicit residual at each restart.
+// Right-hand sides iterate in lock step; one that converges is frozen by its state word,
+// so its iterates do not depend on the others.
+#include "hmatrix.cuh"
+#include "quad_math.cuh"
+#include "quad_regular.cuh"
+
+namespace bemgpu {
+
+namespace {
+
+__device__ __forceinline__ cd ldc(const double* p, int64_t i) {
+  const double2 v = reinterpret_cast<const double2*>(p)[i];
+  return cd{v.x, v.y};
+}
+__device__ __forceinline__ void stc(double* p, int64_t i, cd v) {
+  reinterpret_cast<double2*>(p)[i] = make_double2(v.x, v.y);
+}
+// conj(a) b
+__device__ __forceinline__ cd conjmul(cd a, cd b) {
+  return cd{a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ double abs2(cd a) { return a.x * a.x + a.y * a.y; }
+__device__ __forceinline__ cd cdiv_real(cd a, double s) { return cd{a.x / s, a.y / s}; }
+__device__ __forceinline__ cd crecip(cd a) {
+  const double d = a.x * a.x + a.y * a.y;
+  return cd{a.x / d, -a.y / d};
+}
+__device__ __forceinline__ cd warp_sum(cd v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, off);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, off);
+  }
+  return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+__device__ __forceinline__ void amax(double& v, int32_t& i, double ov, int32_t oi) {
+  if (ov > v || (ov == v && oi < i)) {
+    v = ov;
+    i = oi;
+  }
+}
+
+// Entry (i, j) of M1 (op 0) or M2 (op 1) of a rigid/soft assembly kind at panels pi != pj
+// by the regular rule, combined as in the dense FP64 regular kernel.
+template <int KIND, int OP>
+__device__ __forceinline__ cd hm_entry(const double* __restrict__ panels, int32_t pi, int32_t pj,
+                                       double k, cd al) {
+  const double* ri = panels + (int64_t)pi * kPanelDoubles;
+  const double x[3] = {ri[0], ri[1], ri[2]}, nx[3] = {ri[3], ri[4], ri[5]};
+  Acc<double> a;
+  a.S = a.D = a.K = a.H = cd{0.0, 0.0};
+  regular_panel<double, KIND == kAsmBM>(panels + (int64_t)pj * kPanelDoubles, x, nx, k, a);
+  if (OP == 0) {
+    cd m1 = cd{-a.D.x, -a.D.y};
+    if (KIND == kAsmBM) m1 -= al * a.H;
+    return m1;
+  }
+  cd m2 = a.S;
+  if (KIND == kAsmBM) m2 += al * a.K;
+  return m2;
+}
+
+constexpr int kAcaT = 256;
+constexpr int kAcaW = kAcaT / 32;
+
+// block-wide argmax (largest value, then smallest index); every thread gets the result
+__device__ __forceinline__ void block_argmax(double& v, int32_t& i, double* rv, int32_t* ri) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const double ov = __shfl_xor_sync(0xffffffffu, v, off);
+    const int32_t oi = __shfl_xor_sync(0xffffffffu, i, off);
+    amax(v, i, ov, oi);
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) {
+    rv[w] = v;
+    ri[w] = i;
+  }
+  __syncthreads();
+  v = rv[0];
+  i = ri[0];
+  for (int q = 1; q < kAcaW; ++q) amax(v, i, rv[q], ri[q]);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ cross approximation
+template <int KIND, int OP>
+__global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, double* Up, double* Vp,
+                                                  const double* __restrict__ panels,
+                                                  const int32_t* __restrict__ perm, double k,
+                                                  double a_re, double a_im, double tol) {
+  HmLR& B = lrs[blockIdx.x];
+  const int m = B.m, n = B.n, kmax = B.kmax;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  double* U = Up + 2 * B.uoff;
+  double* V = Vp + 2 * B.voff;
+  const int32_t* prow = perm + B.rlo;
+  const int32_t* pcol = perm + B.clo;
+  const cd al = {a_re, a_im};
+  extern __shared__ uint32_t used[];  // pivot rows taken, (m + 31) / 32 words
+  __shared__ double rv[kAcaW];
+  __shared__ int32_t ri[kAcaW];
+  __shared__ cd su[kHmMaxRank], sv[kHmMaxRank];    // U[i*, l], V[j*, l]
+  __shared__ cd cu[kHmMaxRank], cv[kHmMaxRank];    // projections of the new cross
+  __shared__ cd s_piv;
+  __shared__ double s_s2;
+  __shared__ int s_stop;
+  const int words = (m + 31) >> 5;
+  for (int w = tid; w < words; w += kAcaT) used[w] = 0u;
+  if (tid == 0) s_s2 = 0.0;
+  int rank = 0, conv = 0;
+  int32_t istar = 0;
+  __syncthreads();
+  for (int it = 0; rank < kmax && it < m; ++it) {
+    if (tid < rank) su[tid] = ldc(U, istar + (int64_t)tid * m);
+    if (tid == 0) used[istar >> 5] |= 1u << (istar & 31);
+    __syncthreads();
+    // residual row i*: A[i*, :] - sum_l U[i*, l] V[:, l]
+    double bv = -1.0;
+    int32_t bj = INT32_MAX;
+    const int32_t pi = prow[istar];
+    for (int j = tid; j < n; j += kAcaT) {
+      cd v = hm_entry<KIND, OP>(panels, pi, pcol[j], k, al);
+      for (int l = 0; l < rank; ++l) v -= su[l] * ldc(V, j + (int64_t)l * n);
+      stc(V, j + (int64_t)rank * n, v);
+      amax(bv, bj, abs2(v), j);
+    }
+    block_argmax(bv, bj, rv, ri);
+    if (!(bv > 0.0)) {  // the residual row vanishes: continue from the next unused row
+      double fv = -1.0;
+      int32_t fi = INT32_MAX;
+      for (int i = tid; i < m; i += kAcaT)
+        if (!((used[i >> 5] >> (i & 31)) & 1u)) {
+          amax(fv, fi, 1.0, i);
+          break;
+        }
+      block_argmax(fv, fi, rv, ri);
+      if (fv < 0.0) {  // every row was a pivot row: the approximation is exact
+        conv = 1;
+        break;
+      }
+      istar = fi;
+      continue;
+    }
+    const int32_t jstar = bj;
+    if (tid == 0) s_piv = ldc(V, jstar + (int64_t)rank * n);
+    if (tid < rank) sv[tid] = ldc(V, jstar + (int64_t)tid * n);
+    __syncthreads();
+    const cd inv = crecip(s_piv);
+    // residual column j*: A[:, j*] - sum_l U[:, l] V[j*, l]; next pivot row
+    double cb = -1.0;
+    int32_t ci = INT32_MAX;
+    const int32_t pj = pcol[jstar];
+    for (int i = tid; i < m; i += kAcaT) {
+      cd u = hm_entry<KIND, OP>(panels, prow[i], pj, k, al);
+      for (int l = 0; l < rank; ++l) u -= ldc(U, i + (int64_t)l * m) * sv[l];
+      stc(U, i + (int64_t)rank * m, u);
+      if (!((used[i >> 5] >> (i & 31)) & 1u)) amax(cb, ci, abs2(u), i);
+    }
+    for (int j = tid; j < n; j += kAcaT)
+      stc(V, j + (int64_t)rank * n, ldc(V, j + (int64_t)rank * n) * inv);
+    __syncthreads();
+    // projections U_l^H U_r and V_l^H V_r, l = 0..rank (one warp per l, fixed order)
+    for (int l = wid; l <= rank; l += kAcaW) {
+      cd a = {0.0, 0.0}, b = {0.0, 0.0};
+      for (int i = lane; i < m; i += 32)
+        a += conjmul(ldc(U, i + (int64_t)l * m), ldc(U, i + (int64_t)rank * m));
+      for (int j = lane; j < n; j += 32)
+        b += conjmul(ldc(V, j + (int64_t)l * n), ldc(V, j + (int64_t)rank * n));
+      a = warp_sum(a);
+      b = warp_sum(b);
+      if (lane == 0) {
+        cu[l] = a;
+        cv[l] = b;
+      }
+    }
+    block_argmax(cb, ci, rv, ri);
+    if (tid == 0) {
+      // |S_r|^2 = |S_{r-1}|^2 + |u_r|^2 |v_r|^2 + 2 Re sum_{l<r} (U_l^H u_r)(V_l^H v_r)
+      const double uv2 = cu[rank].x * cv[rank].x;
+      double s = s_s2 + uv2;
+      for (int l = 0; l < rank; ++l) s += 2.0 * (cu[l].x * cv[l].x - cu[l].y * cv[l].y);
+      s_s2 = s;
+      s_stop = uv2 <= tol * tol * s ? 1 : 0;
+    }
+    __syncthreads();
+    ++rank;
+    if (s_stop || cb < 0.0) {  // converged, or every row was a pivot row (exact)
+      conv = 1;
+      break;
+    }
+    istar = ci;
+  }
+  if (tid == 0) {
+    B.rank = rank;
+    B.conv = conv;
+  }
+}
+
+void launch_hm_aca(const Launch& L, HmLR* lr, int32_t n_lr, int32_t max_m, double* U, double* V,
+                   const double* panels, const int32_t* perm, int kind, int op, double k,
+                   double a_re, double a_im, double tol) {
+  if (n_lr <= 0) return;
+  const size_t smem = (size_t)((max_m + 31) / 32) * 4;
+  auto go = [&](auto kern) {
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<(unsigned)n_lr, kAcaT, smem, L.stream>>>(lr, U, V, panels, perm, k, a_re, a_im, tol);
+  };
+  if (kind == kAsmBM)
+    op == 0 ? go(k_hm_aca<kAsmBM, 0>) : go(k_hm_aca<kAsmBM, 1>);
+  else
+    op == 0 ? go(k_hm_aca<kAsmCBIE, 0>) : go(k_hm_aca<kAsmCBIE, 1>);
+  count_launch(1);
+}
+
+// ------------------------------------------------------------------ full blocks
+template <int KIND>
+__global__ void __launch_bounds__(256) k_hm_dense(const HmDense* __restrict__ dn, double* D1,
+                                                  double* D2, const double* __restrict__ panels,
+                                                  const int32_t* __restrict__ perm, double k,
+                                                  double a_re, double a_im) {
+  const HmDense B = dn[blockIdx.x];
+  const int64_t cnt = (int64_t)B.m * B.n;
+  const cd al = {a_re, a_im};
+  for (int64_t e = (int64_t)blockIdx.y * blockDim.x + threadIdx.x; e < cnt;
+       e += (int64_t)blockDim.x * gridDim.y) {
+    const int i = (int)(e % B.m), j = (int)(e / B.m);
+    const int32_t pi = perm[B.rlo + i], pj = perm[B.clo + j];
+    if (pi == pj) continue;  // self pair: near kernel
+    const double* ri = panels + (int64_t)pi * kPanelDoubles;
+    const double x[3] = {ri[0], ri[1], ri[2]}, nx[3] = {ri[3], ri[4], ri[5]};
+    Acc<double> a;
+    a.S = a.D = a.K = a.H = cd{0.0, 0.0};
+    regular_panel<double, KIND == kAsmBM>(panels + (int64_t)pj * kPanelDoubles, x, nx, k, a);
+    cd m1 = cd{-a.D.x, -a.D.y}, m2 = a.S;
+    if (KIND == kAsmBM) {
+      m1 -= al * a.H;
+      m2 += al * a.K;
+    }
+    stc(D1, B.off + e, m1);
+    stc(D2, B.off + e, m2);
+  }
+}
+
+void launch_hm_dense(const Launch& L, const HmDense* dn, int32_t n_dense, double* D1, double* D2,
+                     const double* panels, const int32_t* perm, int kind, double k, double a_re,
+                     double a_im) {
+  if (n_dense <= 0) return;
+  dim3 g((unsigned)n_dense, 4);
+  if (kind == kAsmBM)
+    k_hm_dense<kAsmBM><<<g, 256, 0, L.stream>>>(dn, D1, D2, panels, perm, k, a_re, a_im);
+  else
+    k_hm_dense<kAsmCBIE><<<g, 256, 0, L.stream>>>(dn, D1, D2, panels, perm, k, a_re, a_im);
+  count_launch(1);
+}
+
+// ------------------------------------------------------------------ products
+__device__ __forceinline__ bool rhs_on(const GmState* st, int r, int mode) {
+  if (mode == 0 || !st) return true;
+  return mode == 1 ? st[r].active != 0 : st[r].done == 0;
+}
+
+__global__ void __launch_bounds__(256) k_hm_vt(HmOp A, const double* __restrict__ X, int64_t ldx,
+                                               const GmState* st, int mode) {
+  const int r = blockIdx.y;
+  if (!rhs_on(st, r, mode)) return;
+  const HmLR& B = A.lr[blockIdx.x];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const double* V = A.V + 2 * B.voff;
+  const double* x = X + 2 * ((int64_t)r * ldx + B.clo);
+  for (int l = wid; l < B.rank; l += 8) {
+    cd s = {0.0, 0.0};
+    for (int j = lane; j < B.n; j += 32) s += ldc(V, j + (int64_t)l * B.n) * ldc(x, j);
+    s = warp_sum(s);
+    if (lane == 0) stc(A.T, (int64_t)r * A.tstride + B.toff + l, s);
+  }
+}
+
+constexpr int kLeafRows = 64;
+constexpr int kLeafSlices = 4;
+
+__global__ void __launch_bounds__(kLeafRows * kLeafSlices) k_hm_leaf(
+    HmOp A, const double* __restrict__ X, int64_t ldx, double* __restrict__ Y, int64_t ldy,
+    const double* __restrict__ Bv, int64_t ldb, double sb, double sa, const GmState* st,
+    int mode) {
+  const int r = blockIdx.y;
+  if (!rhs_on(st, r, mode)) return;
+  const int leaf = blockIdx.x;
+  const int32_t lo = A.leaf_lo[leaf], rows = A.leaf_lo[leaf + 1] - lo;
+  const int row = threadIdx.x % kLeafRows, s = threadIdx.x / kLeafRows;
+  __shared__ cd part[kLeafSlices][kLeafRows];
+  cd acc = {0.0, 0.0};
+  const double* x = X + 2 * (int64_t)r * ldx;
+  const double* T = A.T + 2 * (int64_t)r * A.tstride;
+  if (row < rows) {
+    for (int e = A.leaf_ptr[leaf]; e < A.leaf_ptr[leaf + 1]; ++e) {
+      const int32_t b = A.leaf_ent[e];
+      if (b >= 0) {
+        const HmDense& B = A.dn[b];
+        const double* D = A.D + 2 * B.off;
+        const int il = lo + row - B.rlo;
+        for (int j = s; j < B.n; j += kLeafSlices)
+          acc += ldc(D, il + (int64_t)j * B.m) * ldc(x, B.clo + j);
+      } else {
+        const HmLR& B = A.lr[-b - 1];
+        const double* U = A.U + 2 * B.uoff;
+        const int il = lo + row - B.rlo;
+        for (int l = s; l < B.rank; l += kLeafSlices)
+          acc += ldc(U, il + (int64_t)l * B.m) * ldc(T, B.toff + l);
+      }
+    }
+  }
+  part[s][row] = acc;
+  __syncthreads();
+  if (s == 0 && row < rows) {
+    const cd y = ((part[0][row] + part[1][row]) + part[2][row]) + part[3][row];
+    const int64_t i = lo + row;
+    cd out = sa * y;
+    if (Bv) out += sb * ldc(Bv, (int64_t)r * ldb + i);
+    stc(Y, (int64_t)r * ldy + i, out);
+  }
+}
+
+void launch_hm_matvec(const Launch& L, const HmOp& A, const double* X, int64_t ldx, double* Y,
+                      int64_t ldy, const double* B, int64_t ldb, double sb, double sa, int32_t nr,
+                      const GmState* act, int mode) {
+  if (nr <= 0) return;
+  if (A.n_lr > 0) {
+    k_hm_vt<<<dim3((unsigned)A.n_lr, (unsigned)nr), 256, 0, L.stream>>>(A, X, ldx, act, mode);
+    count_launch(1);
+  }
+  k_hm_leaf<<<dim3((unsigned)A.n_leaf, (unsigned)nr), kLeafRows * kLeafSlices, 0, L.stream>>>(
+      A, X, ldx, Y, ldy, B, ldb, sb, sa, act, mode);
+  count_launch(1);
+}
+
+__global__ void k_hm_permute(const double* __restrict__ src, int64_t lds, double* __restrict__ dst,
+                             int64_t ldd, const int32_t* __restrict__ idx, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y;
+  if (i >= n) return;
+  stc(dst, (int64_t)r * ldd + i, ldc(src, (int64_t)r * lds + idx[i]));
+}
+
+void launch_hm_permute(const Launch& L, const double* src, int64_t lds, double* dst, int64_t ldd,
+                       const int32_t* idx, int64_t n, int32_t nr) {
+  if (n <= 0 || nr <= 0) return;
+  k_hm_permute<<<dim3((unsigned)((n + 255) / 256), (unsigned)nr), 256, 0, L.stream>>>(src, lds, dst,
+                                                                                     ldd, idx, n);
+  count_launch(1);
+}
+
+// ------------------------------------------------------------------ GMRES
+constexpr int kGmChunk = 4096;  // rows per partial sum
+constexpr int kGmT = 256;
+
+namespace {
+__device__ __forceinline__ double* vcol(const GmWork& w, int r, int l) {
+  return w.Vb + 2 * (((int64_t)r * (w.restart + 1) + l) * w.n);
+}
+__device__ __forceinline__ int64_t hidx(const GmWork& w, int r, int i, int j) {
+  return (int64_t)r * (w.restart + 1) * w.restart + i + (int64_t)j * (w.restart + 1);
+}
+__device__ __forceinline__ double* partp(const GmWork& w, int r, int chunk) {
+  return w.part + 2 * (((int64_t)r * w.chunks + chunk) * (w.restart + 1));
+}
+}  // namespace
+
+// part[r][chunk][l] = sum over the chunk of conj(V_l) w, l = 0..j (warp per l)
+__global__ void __launch_bounds__(kGmT) k_gm_dot(GmWork w, int32_t j) {
+  const int r = blockIdx.y, chunk = blockIdx.x;
+  if (!w.st[r].active) return;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t i0 = (int64_t)chunk * kGmChunk, i1 = min(w.n, i0 + kGmChunk);
+  const double* wr = w.w + 2 * (int64_t)r * w.n;
+  double* pp = partp(w, r, chunk);
+  for (int l = wid; l <= j; l += kGmT / 32) {
+    const double* v = vcol(w, r, l);
+    cd s = {0.0, 0.0};
+    for (int64_t i = i0 + lane; i < i1; i += 32) s += conjmul(ldc(v, i), ldc(wr, i));
+    s = warp_sum(s);
+    if (lane == 0) stc(pp, l, s);
+  }
+}
+
+// hc[r][l] = sum over chunks (in order); pass 0 stores H[l, j], pass 1 adds to it
+__global__ void k_gm_dot_finish(GmWork w, int32_t j, int pass) {
+  const int r = blockIdx.x;
+  if (!w.st[r].active) return;
+  for (int l = threadIdx.x; l <= j; l += blockDim.x) {
+    cd s = {0.0, 0.0};
+    for (int c = 0; c < w.chunks; ++c) s += ldc(partp(w, r, c), l);
+    stc(w.hc, (int64_t)r * (w.restart + 1) + l, s);
+    const int64_t h = hidx(w, r, l, j);
+    stc(w.H, h, pass == 0 ? s : ldc(w.H, h) + s);
+  }
+}
+
+// w -= sum_{l <= j} V_l hc_l
+__global__ void __launch_bounds__(kGmT) k_gm_orth(GmWork w, int32_t j) {
+  const int r = blockIdx.y;
+  if (!w.st[r].active) return;
+  __shared__ cd h[512];
+  const cd* hc = reinterpret_cast<const cd*>(w.hc) + (int64_t)r * (w.restart + 1);
+  for (int l = threadIdx.x; l <= j; l += blockDim.x) h[l] = hc[l];
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= w.n) return;
+  double* wr = w.w + 2 * (int64_t)r * w.n;
+  cd s = ldc(wr, i);
+  for (int l = 0; l <= j; ++l) s -= ldc(vcol(w, r, l), i) * h[l];
+  stc(wr, i, s);
+}
+
+// part[r][chunk][0].x = sum over the chunk of |w_i|^2 (mode 1: active, 2: not done)
+__global__ void __launch_bounds__(kGmT) k_gm_norm(GmWork w, int mode) {
+  const int r = blockIdx.y, chunk = blockIdx.x;
+  if (!rhs_on(w.st, r, mode)) return;
+  __shared__ double red[kGmT / 32];
+  const int64_t i0 = (int64_t)chunk * kGmChunk, i1 = min(w.n, i0 + kGmChunk);
+  const double* wr = w.w + 2 * (int64_t)r * w.n;
+  double s = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += kGmT) s += abs2(ldc(wr, i));
+  s = warp_sum_d(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < kGmT / 32; ++q) t += red[q];
+    stc(partp(w, r, chunk), 0, cd{t, 0.0});
+  }
+}
+
+__device__ __forceinline__ double chunk_norm(const GmWork& w, int r) {
+  double t = 0.0;
+  for (int c = 0; c < w.chunks; ++c) t += partp(w, r, c)[0];
+  return sqrt(t);
+}
+
+// V_{j+1} = w / |w|, H[j + 1, j] = |w|
+__global__ void __launch_bounds__(kGmT) k_gm_normalize(GmWork w, int32_t j) {
+  const int r = blockIdx.y;
+  if (!w.st[r].active) return;
+  const double hn = chunk_norm(w, r);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.x == 0 && threadIdx.x == 0) stc(w.H, hidx(w, r, j + 1, j), cd{hn, 0.0});
+  if (i >= w.n) return;
+  const cd v = ldc(w.w + 2 * (int64_t)r * w.n, i);
+  stc(vcol(w, r, j + 1), i, hn > 0.0 ? cdiv_real(v, hn) : cd{0.0, 0.0});
+}
+
+void launch_gm_arnoldi(const Launch& L, const GmWork& w, int32_t j) {
+  const dim3 gc((unsigned)w.chunks, (unsigned)w.nr);
+  const dim3 gv((unsigned)((w.n + kGmT - 1) / kGmT), (unsigned)w.nr);
+  for (int pass = 0; pass < 2; ++pass) {
+    k_gm_dot<<<gc, kGmT, 0, L.stream>>>(w, j);
+    k_gm_dot_finish<<<(unsigned)w.nr, 128, 0, L.stream>>>(w, j, pass);
+    k_gm_orth<<<gv, kGmT, 0, L.stream>>>(w, j);
+  }
+  k_gm_norm<<<gc, kGmT, 0, L.stream>>>(w, 1);
+  k_gm_normalize<<<gv, kGmT, 0, L.stream>>>(w, j);
+  count_launch(8);
+}
+
+// Givens rotations of column j, residual estimate, stopping tests; nact = active count.
+__global__ void __launch_bounds__(1024) k_gm_rotate(GmWork w, int32_t j) {
+  int total = 0;
+  for (int base = 0; base < w.nr; base += blockDim.x) {
+    const int r = base + threadIdx.x;
+    bool act = false;
+    if (r < w.nr && w.st[r].active) {
+      GmState& S = w.st[r];
+      cd* H = reinterpret_cast<cd*>(w.H);
+      cd* g = reinterpret_cast<cd*>(w.g) + (int64_t)r * (w.restart + 1);
+      double* cs = w.cs + (int64_t)r * w.restart;
+      cd* sn = reinterpret_cast<cd*>(w.sn) + (int64_t)r * w.restart;
+      for (int i = 0; i < j; ++i) {
+        const cd a = H[hidx(w, r, i, j)], b = H[hidx(w, r, i + 1, j)];
+        const cd s = sn[i];
+        H[hidx(w, r, i, j)] = cs[i] * a + s * b;
+        H[hidx(w, r, i + 1, j)] = cs[i] * b - conjmul(s, a);
+      }
+      const cd a = H[hidx(w, r, j, j)], b = H[hidx(w, r, j + 1, j)];
+      const double aa = hypot(a.x, a.y), bb = hypot(b.x, b.y);
+      double c;
+      cd s, rr;
+      if (aa == 0.0) {
+        c = 0.0;
+        s = cd{1.0, 0.0};
+        rr = b;
+      } else {
+        const double t = hypot(aa, bb);
+        const cd ph = cd{a.x / aa, a.y / aa};
+        c = aa / t;
+        s = ph * cd{b.x / t, -b.y / t};
+        rr = cd{ph.x * t, ph.y * t};
+      }
+      cs[j] = c;
+      sn[j] = s;
+      H[hidx(w, r, j, j)] = rr;
+      H[hidx(w, r, j + 1, j)] = cd{0.0, 0.0};
+      const cd gj = g[j];
+      g[j + 1] = cd{0.0, 0.0} - conjmul(s, gj);
+      g[j] = c * gj;
+      const double res = hypot(g[j + 1].x, g[j + 1].y);
+      S.res = res;
+      S.kdim = j + 1;
+      if (S.iters < w.maxiter) w.hist[(int64_t)r * w.maxiter + S.iters] = res;
+      S.iters += 1;
+      if (res <= S.tol) {
+        S.converged = 1;
+        S.done = 1;
+        S.active = 0;
+      } else if (S.iters >= w.maxiter) {
+        S.done = 1;
+        S.active = 0;
+      } else if (j + 1 == w.restart) {
+        S.active = 0;
+      }
+      act = S.active != 0;
+    }
+    total += __syncthreads_count(act);
+  }
+  if (threadIdx.x == 0) *w.nact = total;
+}
+
+void launch_gm_rotate(const Launch& L, const GmWork& w, int32_t j) {
+  k_gm_rotate<<<1, 1024, 0, L.stream>>>(w, j);
+  count_launch(1);
+}
+
+// y = H[0:kdim, 0:kdim]^{-1} g (back substitution, one warp per right-hand side) into hc
+__global__ void k_gm_solve_y(GmWork w) {
+  const int r = blockIdx.x;
+  const int kd = w.st[r].kdim;
+  if (kd <= 0) return;
+  const int lane = threadIdx.x;
+  const cd* H = reinterpret_cast<const cd*>(w.H);
+  const cd* g = reinterpret_cast<const cd*>(w.g) + (int64_t)r * (w.restart + 1);
+  cd* y = reinterpret_cast<cd*>(w.hc) + (int64_t)r * (w.restart + 1);
+  for (int i = kd - 1; i >= 0; --i) {
+    cd s = {0.0, 0.0};
+    for (int l = i + 1 + lane; l < kd; l += 32) s += H[hidx(w, r, i, l)] * y[l];
+    s = warp_sum(s);
+    if (lane == 0) {
+      const cd d = H[hidx(w, r, i, i)];
+      y[i] = (d.x == 0.0 && d.y == 0.0) ? cd{0.0, 0.0} : (g[i] - s) * crecip(d);
+    }
+    __syncwarp();
+  }
+}
+
+// x += V y for every right-hand side that iterated in this cycle
+__global__ void __launch_bounds__(kGmT) k_gm_xupd(GmWork w) {
+  const int r = blockIdx.y;
+  const int kd = w.st[r].kdim;
+  if (kd <= 0) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= w.n) return;
+  const cd* y = reinterpret_cast<const cd*>(w.hc) + (int64_t)r * (w.restart + 1);
+  double* x = w.x + 2 * (int64_t)r * w.n;
+  cd s = ldc(x, i);
+  for (int l = 0; l < kd; ++l) s += ldc(vcol(w, r, l), i) * y[l];
+  stc(x, i, s);
+}
+
+void launch_gm_update_x(const Launch& L, const GmWork& w) {
+  k_gm_solve_y<<<(unsigned)w.nr, 32, 0, L.stream>>>(w);
+  k_gm_xupd<<<dim3((unsigned)((w.n + kGmT - 1) / kGmT), (unsigned)w.nr), kGmT, 0, L.stream>>>(w);
+  count_launch(2);
+}
+
+// New cycle from the residual in w (its chunk norms already in part): state, then V_0.
+__global__ void k_gm_start_state(GmWork w, double reltol, double abstol, int first) {
+  int total = 0;
+  for (int base = 0; base < w.nr; base += blockDim.x) {
+    const int r = base + threadIdx.x;
+    bool act = false;
+    if (r < w.nr) {
+      GmState& S = w.st[r];
+      S.kdim = 0;
+      if (first) {
+        const double beta = chunk_norm(w, r);
+        S.bnorm = beta;
+        S.tol = fmax(reltol * beta, abstol);
+        S.iters = 0;
+        S.converged = 0;
+        S.done = 0;
+      }
+      if (!S.done) {
+        const double beta = chunk_norm(w, r);
+        S.res = beta;
+        if (beta <= S.tol) {
+          S.converged = 1;
+          S.done = 1;
+          S.active = 0;
+        } else if (S.iters >= w.maxiter) {
+          S.done = 1;
+          S.active = 0;
+        } else {
+          S.active = 1;
+          cd* g = reinterpret_cast<cd*>(w.g) + (int64_t)r * (w.restart + 1);
+          g[0] = cd{beta, 0.0};
+        }
+      } else {
+        S.active = 0;
+      }
+      act = S.active != 0;
+    }
+    total += __syncthreads_count(act);
+  }
+  if (threadIdx.x == 0) *w.nact = total;
+}
+
+__global__ void __launch_bounds__(kGmT) k_gm_start_vec(GmWork w) {
+  const int r = blockIdx.y;
+  if (!w.st[r].active) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= w.n) return;
+  const double beta = w.st[r].res;
+  stc(vcol(w, r, 0), i, cdiv_real(ldc(w.w + 2 * (int64_t)r * w.n, i), beta));
+}
+
+void launch_gm_start(const Launch& L, const GmWork& w, double reltol, double abstol, int first) {
+  const dim3 gc((unsigned)w.chunks, (unsigned)w.nr);
+  k_gm_norm<<<gc, kGmT, 0, L.stream>>>(w, first ? 0 : 2);
+  k_gm_start_state<<<1, 1024, 0, L.stream>>>(w, reltol, abstol, first);
+  k_gm_start_vec<<<dim3((unsigned)((w.n + kGmT - 1) / kGmT), (unsigned)w.nr), kGmT, 0, L.stream>>>(
+      w);
+  count_launch(3);
+}
+
+}  // namespace bemgpu

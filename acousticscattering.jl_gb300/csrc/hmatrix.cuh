@@ -1,0 +1,104 @@
+// Device descriptors and launchers of the hierarchical-matrix operators and the batched
+// restarted GMRES (hmatrix.cu).  All vectors are complex128 in the permuted panel order
+// of the cluster tree; every reduction runs in a fixed order, so results do not depend on
+// scheduling or on how many right-hand sides share a launch.
+#pragma once
+
+#include "bemgpu_internal.h"
+
+namespace bemgpu {
+
+constexpr int kHmMaxRank = 64;  // rank capacity of a compressed block
+
+// Admissible block: rows [rlo, rlo + m), columns [clo, clo + n) of the permuted order,
+// approximated by U V^T with U (m x rank) and V (n x rank) column-major.
+struct HmLR {
+  int32_t rlo, m, clo, n;
+  int64_t uoff, voff;  // complex offsets of U (m x kmax) and V (n x kmax) in the pools
+  int64_t toff;        // offset of the block's coefficients V^T x in the product scratch
+  int32_t kmax;        // rank capacity
+  int32_t rank;        // rank reached by the cross approximation
+  int32_t conv;        // 1: converged to the tolerance within kmax
+  int32_t pad;
+};
+
+// Full block (column-major m x n at complex offset off of the dense pool).
+struct HmDense {
+  int32_t rlo, m, clo, n;
+  int64_t off;
+};
+
+// One compressed operator.
+struct HmOp {
+  const HmLR* lr;
+  const HmDense* dn;
+  const double* U;
+  const double* V;
+  const double* D;
+  const int32_t* leaf_lo;   // n_leaf + 1 row boundaries
+  const int32_t* leaf_ptr;  // n_leaf + 1
+  const int32_t* leaf_ent;  // dense block b as b, low-rank block b as -(b + 1)
+  int32_t n_lr, n_dense, n_leaf, pad;
+  double* T;                // product scratch: per right-hand side tstride complex
+  int64_t tstride;
+};
+
+// Batched GMRES state of one right-hand side.
+struct GmState {
+  int32_t active;     // iterating in the current restart cycle
+  int32_t done;       // converged or out of iterations
+  int32_t converged;
+  int32_t kdim;       // Krylov vectors of the current cycle
+  int32_t iters;      // Arnoldi steps so far
+  int32_t pad;
+  double tol;         // max(reltol ||b||, abstol)
+  double res;         // current residual estimate
+  double bnorm;
+};
+
+// GMRES work arrays of a group of right-hand sides (device pointers).
+struct GmWork {
+  GmState* st;
+  double* Vb;     // basis: [r][restart + 1][n] complex
+  double* H;      // Hessenberg: [r][(restart + 1) x restart] complex, column-major
+  double* cs;     // rotation cosines [r][restart]
+  double* sn;     // rotation sines [r][restart] complex
+  double* g;      // least-squares right side [r][restart + 1] complex
+  double* hc;     // current projection coefficients [r][restart + 1] complex
+  double* part;   // chunk partial sums [r][chunks][restart + 1] complex
+  double* hist;   // residual estimates [r][maxiter]
+  double* x;      // solutions [r][n] complex
+  const double* b;  // right-hand sides [r][n] complex
+  double* w;      // work vector [r][n] complex
+  int64_t n;
+  int32_t nr, restart, maxiter, chunks;
+  int32_t* nact;  // active right-hand sides after the last rotation step
+};
+
+#ifdef __CUDACC__
+// Cross approximation of every admissible block of op (0: M1, 1: M2 of the assembly kind).
+void launch_hm_aca(const Launch& L, HmLR* lr, int32_t n_lr, int32_t max_m, double* U,
+                   double* V, const double* panels, const int32_t* perm, int kind, int op,
+                   double k, double a_re, double a_im, double tol);
+// Regular-rule entries of the full blocks of both operators (self pairs left to the near
+// kernel, which writes them through AsmInst.near_dst).
+void launch_hm_dense(const Launch& L, const HmDense* dn, int32_t n_dense, double* D1,
+                     double* D2, const double* panels, const int32_t* perm, int kind, double k,
+                     double a_re, double a_im);
+// Y[:, r] = sb B[:, r] + sa (A X)[:, r] for every right-hand side r < nr with
+// (act == null or act[r].active), the operands in permuted order.
+void launch_hm_matvec(const Launch& L, const HmOp& A, const double* X, int64_t ldx, double* Y,
+                      int64_t ldy, const double* B, int64_t ldb, double sb, double sa, int32_t nr,
+                      const GmState* act, int mode);
+
+// GMRES steps (hmatrix.cu describes each).
+void launch_gm_start(const Launch& L, const GmWork& w, double reltol, double abstol, int first);
+void launch_gm_arnoldi(const Launch& L, const GmWork& w, int32_t j);
+void launch_gm_rotate(const Launch& L, const GmWork& w, int32_t j);
+void launch_gm_update_x(const Launch& L, const GmWork& w);
+// permuted <-> panel order of nr complex vectors of length n
+void launch_hm_permute(const Launch& L, const double* src, int64_t lds, double* dst,
+                       int64_t ldd, const int32_t* idx, int64_t n, int32_t nr);
+#endif
+
+}  // namespace bemgpu

@@ -266,6 +266,66 @@ int bemgpu_region_solve(bemgpu_ctx *ctx, int32_t count, const bemgpu_mesh *const
  */
 int bemgpu_region_traces(const bemgpu_solution *sol, int32_t rhs, double *p, double *v);
 
+/* ------------------------------------------------------------------ hierarchical matrices */
+/*
+ * Compressed operators and GMRES: the reference's default rigid/soft path,
+ * solve_full_bem(...; compression=(method=:hmatrix, tol), gmres_kwargs=(reltol, restart,
+ * maxiter)) (full.jl:52-58, 68-184).  Complex128 throughout.
+ */
+typedef struct {
+  double tol;         /* cross-approximation tolerance (compression tol, default 1e-5) */
+  double eta;         /* admissibility min(diam s, diam t) < eta dist(s, t) (default 3) */
+  int32_t leaf_size;  /* panels per leaf cluster, 8..64 (default 64) */
+  int32_t restart;    /* GMRES restart length, 1..500 (default 150) */
+  double reltol;      /* GMRES: stop when the residual <= max(reltol |b|, abstol) (1e-4) */
+  double abstol;      /* (default 0) */
+  int32_t maxiter;    /* GMRES Arnoldi steps (default 1200) */
+  int32_t pad;
+} bemgpu_hmatrix_options;
+
+typedef struct {
+  int64_t lowrank_blocks;    /* admissible blocks kept compressed */
+  int64_t dense_blocks;      /* full blocks (leaf pairs + densified admissible blocks) */
+  int64_t densified_blocks;  /* admissible blocks whose cross approximation hit the rank cap */
+  int64_t lowrank_entries;   /* complex entries of U and V, both operators */
+  int64_t dense_entries;     /* complex entries of the full blocks, both operators */
+  int32_t max_rank, depth, leaves, pad;
+  double compression;        /* stored entries / (2 n^2) */
+  int32_t gmres_iterations;  /* Arnoldi steps, max over right-hand sides */
+  int32_t gmres_converged;   /* 1 when every right-hand side met the tolerance */
+  double build_ms, gmres_ms;
+} bemgpu_hmatrix_stats;
+
+/* [host] Fill options with the reference's defaults. */
+void bemgpu_hmatrix_options_init(bemgpu_hmatrix_options *opt);
+/*
+ * [host] Block partition of the compressed operators of a surface (no device work):
+ * counts = {admissible blocks, full blocks, leaves, tree depth}; blocks (optional, room
+ * for cap blocks of 5 int32: kind 0 full / 1 admissible, first row, rows, first column,
+ * columns, in permuted positions); perm (optional, n_triangles int32: permuted position
+ * -> panel).  near_eta as for bemgpu_near_pairs.
+ */
+int bemgpu_hmatrix_plan(const double *nodes, int64_t n_nodes, const int64_t *triangles,
+                        int64_t n_triangles, double near_eta, const bemgpu_hmatrix_options *opt,
+                        int64_t counts[4], int32_t *blocks, int64_t cap, int32_t *perm);
+/*
+ * Rigid / pressure-release solve with compressed operators and GMRES for nrhs plane waves
+ * (incidence as for bemgpu_factor_solve).  The returned solution answers every query.
+ * GMRES that stops without meeting the tolerance returns BEMGPU_OK with gmres_converged =
+ * 0, as the reference warns and returns (full.jl:157-159).
+ */
+int bemgpu_hmatrix_solve(bemgpu_ctx *ctx, const bemgpu_mesh *mesh, const bemgpu_problem *problem,
+                         const bemgpu_hmatrix_options *opt, int32_t nrhs,
+                         const double *incidence, bemgpu_solution **solution);
+/* Compression and GMRES statistics of a solution from bemgpu_hmatrix_solve. */
+int bemgpu_hmatrix_stats_get(const bemgpu_solution *sol, bemgpu_hmatrix_stats *stats);
+/*
+ * GMRES residual estimates of right-hand side rhs, one per Arnoldi step (the reference's
+ * residual_history); writes min(cap, steps) values and the step count.
+ */
+int bemgpu_gmres_history(const bemgpu_solution *sol, int32_t rhs, double *out, int32_t cap,
+                         int32_t *count);
+
 /* ------------------------------------------------------------------ queries */
 /*
  * Far-field amplitude f(x_hat) of right-hand side `rhs` at ndir unit directions
@@ -353,6 +413,15 @@ int bemgpu_dense_solve(bemgpu_ctx *ctx, int64_t n, const double *A, int32_t nrhs
  * A 2n x 2n in M1, M2 unused).  Column-major interleaved complex128. */
 int bemgpu_assemble_dense(bemgpu_ctx *ctx, const bemgpu_mesh *mesh,
                           const bemgpu_problem *problem, double *M1, double *M2);
+
+/*
+ * Products Y = M X of the compressed rigid/soft operators (op 0: M1, op 1: M2 as in
+ * bemgpu_assemble_dense) with nr columns (n x nr column-major interleaved complex128),
+ * for inspecting the compression; stats (optional) receives the operators' statistics.
+ */
+int bemgpu_hmatrix_apply(bemgpu_ctx *ctx, const bemgpu_mesh *mesh, const bemgpu_problem *problem,
+                         const bemgpu_hmatrix_options *opt, int32_t op, int32_t nr,
+                         const double *X, double *Y, bemgpu_hmatrix_stats *stats);
 
 /*
  * Launch-shape autotuner (default on): the first time a batch shape is met, the panel

@@ -13,7 +13,10 @@ Layers:
                            promotion state machine (solvers/bem/fluid_system.jl:172-309);
   * ``solve``           -- the ``bem`` call chain for one mesh, boundary and k
                            (full.jl:52-184, :273-495), returning scattered traces;
-  * ``far_field``       -- full.jl:509-519;  ``target_strength`` -- target_strength.jl:8.
+  * ``far_field``       -- full.jl:509-519;  ``target_strength`` -- target_strength.jl:8;
+  * ``gmres`` / ``solve_gmres`` -- the reference's GMRES path for rigid/soft bodies
+                           (full.jl:130-184) on dense operators: the checker of the
+                           compressed-operator GPU path.
 """
 from __future__ import annotations
 
@@ -303,6 +306,102 @@ def pressure(P: Panels, k, points, p_scat, q_scat, direction, field="scattered",
 def target_strength(f):
     """20 log10 |f| (postprocessing/target_strength.jl:8)."""
     return 20.0 * math.log10(abs(f))
+
+
+# ---------------------------------------------------------------- GMRES
+def gmres(A, b, reltol=1e-4, abstol=0.0, restart=150, maxiter=1200):
+    """Restarted GMRES with the semantics of IterativeSolvers.gmres as the reference calls
+    it for rigid/soft bodies (solvers/bem/full.jl:153-154, defaults full.jl:57): x0 = 0;
+    stop when the residual estimate |g[j+1]| <= max(reltol |b|, abstol) or after maxiter
+    Arnoldi steps; an explicit residual b - A x starts every restart cycle.  The Arnoldi
+    vectors are orthogonalised by classical Gram-Schmidt with one reorthogonalisation and
+    the Hessenberg matrix reduced by complex Givens rotations [c s; -conj(s) c].
+    Returns x and dict(iterations, converged, history)."""
+    b = np.asarray(b, dtype=np.complex128)
+    n = b.size
+    x = np.zeros(n, dtype=np.complex128)
+    beta = float(np.linalg.norm(b))
+    tol = max(reltol * beta, abstol)
+    hist, iters, converged = [], 0, False
+    r = b.copy()
+    while True:
+        if beta <= tol:
+            converged = True
+            break
+        if iters >= maxiter:
+            break
+        V = np.zeros((n, restart + 1), dtype=np.complex128)
+        H = np.zeros((restart + 1, restart), dtype=np.complex128)
+        g = np.zeros(restart + 1, dtype=np.complex128)
+        cs = np.zeros(restart)
+        sn = np.zeros(restart, dtype=np.complex128)
+        V[:, 0] = r / beta
+        g[0] = beta
+        kd = 0
+        for j in range(restart):
+            w = A @ V[:, j]
+            for _ in range(2):
+                h = V[:, :j + 1].conj().T @ w
+                w = w - V[:, :j + 1] @ h
+                H[:j + 1, j] += h
+            hn = float(np.linalg.norm(w))
+            H[j + 1, j] = hn
+            V[:, j + 1] = w / hn if hn > 0 else 0.0
+            for i in range(j):
+                a, c2 = H[i, j], H[i + 1, j]
+                H[i, j] = cs[i] * a + sn[i] * c2
+                H[i + 1, j] = cs[i] * c2 - np.conj(sn[i]) * a
+            a, c2 = H[j, j], H[j + 1, j]
+            aa, bb = abs(a), abs(c2)
+            if aa == 0.0:
+                c, s, rr = 0.0, 1.0 + 0.0j, c2
+            else:
+                t = math.hypot(aa, bb)
+                ph = a / aa
+                c, s, rr = aa / t, ph * np.conj(c2) / t, ph * t
+            cs[j], sn[j] = c, s
+            H[j, j], H[j + 1, j] = rr, 0.0
+            g[j + 1] = -np.conj(s) * g[j]
+            g[j] = c * g[j]
+            res = abs(g[j + 1])
+            iters += 1
+            hist.append(res)
+            kd = j + 1
+            if res <= tol:
+                converged = True
+                break
+            if iters >= maxiter:
+                break
+        y = sla.solve_triangular(H[:kd, :kd], g[:kd], lower=False)
+        x = x + V[:, :kd] @ y
+        if converged or iters >= maxiter:
+            break
+        r = b - A @ x
+        beta = float(np.linalg.norm(r))
+    return x, dict(iterations=iters, converged=converged, history=np.array(hist))
+
+
+def solve_gmres(nodes, triangles, boundary, k, incidence_angle=math.pi / 2,
+                incidence_azimuth=0.0, formulation="burton_miller", eta=NEAR_ETA, panels=None,
+                **gmres_kwargs):
+    """The reference's rigid/soft path solve_full_bem (full.jl:52-184) with GMRES on the
+    dense operators (compression=(method=:none,)): traces, backscatter and the GMRES
+    report."""
+    P = panels if panels is not None else Panels(nodes, triangles)
+    d = incidence_direction(incidence_angle, incidence_azimuth)
+    p_inc, q_inc = incident(P, k, d)
+    M1, M2 = assemble_bm(P, k, formulation == "burton_miller", eta)
+    if boundary == "rigid":
+        A, b = M1, M2 @ q_inc
+    elif boundary == "pressure_release":
+        A, b = M2, M1 @ p_inc
+    else:
+        raise ValueError(f"unknown boundary {boundary!r}")
+    x, rep = gmres(A, b, **gmres_kwargs)
+    p_s, q_s = (x, -q_inc) if boundary == "rigid" else (-p_inc, x)
+    amp = far_field(P, k, -d, p_s, q_s)
+    rep.update(p_scat=p_s, dpdn_scat=q_s, amplitude=amp, A=A, b=b, x=x, panels=P)
+    return rep
 
 
 # ---------------------------------------------------------------- dense factor/solve

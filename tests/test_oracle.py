@@ -240,3 +240,40 @@ def test_region_transparent_inner_interface():
                           incidence_angle=0.3)
     rel = abs(two["amplitude"] - one["amplitude"]) / abs(one["amplitude"])
     assert rel < 1e-3, rel
+
+
+def test_oracle_gmres_contract():
+    """The GMRES restatement (IterativeSolvers semantics): reaches max(reltol |b|, abstol),
+    honours maxiter and restart, returns x = 0 for b = 0, and its per-cycle residual
+    estimates never increase."""
+    rng = np.random.default_rng(5)
+    n = 80
+    A = 4 * np.eye(n) + 0.15 * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    x, rep = O.gmres(A, b, reltol=1e-10, restart=150)
+    assert rep["converged"]
+    assert np.linalg.norm(A @ x - b) <= 2e-10 * np.linalg.norm(b)
+    assert np.all(np.diff(rep["history"]) <= 1e-12 * np.linalg.norm(b))
+    x5, rep5 = O.gmres(A, b, reltol=1e-10, restart=5, maxiter=5000)
+    assert rep5["converged"] and rep5["iterations"] > rep["iterations"]
+    assert np.linalg.norm(A @ x5 - b) <= 2e-10 * np.linalg.norm(b)
+    _, rep3 = O.gmres(A, b, reltol=1e-14, restart=5, maxiter=3)
+    assert rep3["iterations"] == 3 and not rep3["converged"]
+    x0, rep0 = O.gmres(A, np.zeros(n, complex))
+    assert rep0["converged"] and rep0["iterations"] == 0 and not np.any(x0)
+    _, repa = O.gmres(A, b, reltol=0.0, abstol=1e-3 * np.linalg.norm(b))
+    assert repa["converged"] and repa["history"][-1] <= 1e-3 * np.linalg.norm(b)
+
+
+def test_oracle_gmres_path_matches_direct_solve():
+    """solve_full_bem's GMRES path on the dense operators agrees with the direct solve."""
+    nodes, tris = meshes.icosphere(0.01, 2)
+    k = 2 * math.pi * 38e3 / 1477.4
+    for boundary in ("rigid", "pressure_release"):
+        direct = O.solve(nodes, tris, boundary, k, incidence_angle=math.pi / 2,
+                         incidence_azimuth=math.pi / 2)
+        it = O.solve_gmres(nodes, tris, boundary, k, incidence_angle=math.pi / 2,
+                           incidence_azimuth=math.pi / 2, reltol=1e-12)
+        assert it["converged"]
+        f0 = direct["amplitudes"][0]
+        assert abs(it["amplitude"] - f0) <= 1e-9 * abs(f0)
