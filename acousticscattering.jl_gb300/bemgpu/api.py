@@ -542,10 +542,8 @@ def _bem_hmatrix(surface, boundary, k, angles, azimuths, opts, *, formulation, p
     if isinstance(boundary, FluidFilled):
         raise ArgumentError(
             "hierarchical compression applies to Rigid and PressureRelease boundaries")
-    if precision != "double":
-        raise ArgumentError("hierarchical compression computes in double precision")
     ctx = ctx or context()
-    p = _problem(boundary, k, formulation=formulation, precision="double")
+    p = _problem(boundary, k, formulation=formulation, precision=precision)
     angles = np.atleast_1d(np.asarray(angles, dtype=np.float64))
     az = np.broadcast_to(np.asarray(azimuths, dtype=np.float64), angles.shape)
     inc = np.ascontiguousarray(np.stack([angles, az], axis=1).reshape(-1))
@@ -564,11 +562,12 @@ def _bem_hmatrix(surface, boundary, k, angles, azimuths, opts, *, formulation, p
 
 
 def hmatrix_apply(surface: Mesh, boundary, k, X, *, op=0, formulation=None, tol=1e-5,
-                  eta=3.0, leaf_size=64, ctx=None):
+                  eta=3.0, leaf_size=64, precision="double", ctx=None):
     """Products M X of the compressed rigid/soft operators (op 0: M1 = 1/2 I - D - a H,
-    op 1: M2 = S + a (1/2 I + K')) and their statistics, for inspecting the compression."""
+    op 1: M2 = S + a (1/2 I + K')) and their statistics, for inspecting the compression.
+    precision="mixed": complex64 operators with FP32 entries and products."""
     ctx = ctx or context()
-    p = _problem(boundary, k, formulation=formulation, precision="double")
+    p = _problem(boundary, k, formulation=formulation, precision=precision)
     o = _hmatrix_options(dict(method="hmatrix", tol=tol, eta=eta, leaf_size=leaf_size), None)
     X = np.asarray(X, dtype=np.complex128)
     if X.ndim == 1:
@@ -593,9 +592,11 @@ def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_az
 
     compression=dict(method="hmatrix", tol=1e-5) selects the reference's compressed
     operators with GMRES (solve_full_bem, full.jl:52-58; gmres_kwargs reltol, abstol,
-    restart, maxiter as there) for Rigid and PressureRelease bodies.  Without it (or with
-    method="none") the system is factored densely; gmres_kwargs then have no effect, as the
-    direct solve meets any GMRES tolerance."""
+    restart, maxiter as there) for Rigid and PressureRelease bodies; precision="mixed"
+    then stores the operators as complex64 with FP32 entries and products (GMRES itself
+    stays FP64), which limits the attainable relative residual to about 1e-6.  Without it
+    (or with method="none") the system is factored densely; gmres_kwargs then have no
+    effect, as the direct solve meets any GMRES tolerance."""
     if unsupported:
         raise ArgumentError(f"unsupported option(s): {sorted(unsupported)}")
     hm = _hmatrix_options(compression, gmres_kwargs)

@@ -275,6 +275,13 @@ struct MeshData {
   std::vector<int64_t> tris_h;
   Buf surf;                      // union of several surfaces: surface of every panel
   std::vector<int64_t> offsets;  // union: first panel of every surface (+ total)
+  // compressed operators: cluster tree, block partition and near-pair destinations of
+  // each (leaf size, admissibility eta), built on first use
+  struct HmPlanCache {
+    HmPlan plan;
+    Buf perm, iperm, near_dst;
+  };
+  std::map<std::pair<int32_t, double>, std::shared_ptr<HmPlanCache>> hm_plans;
 };
 }  // namespace
 
@@ -2725,32 +2732,47 @@ namespace {
 // Compressed M1 / M2 of one rigid/soft problem on one mesh.
 struct HmData {
   HmPlan plan;
-  Buf perm, iperm, leaf_lo, leaf_ptr, leaf_ent, dn, D1, D2;
+  std::shared_ptr<MeshData::HmPlanCache> pc;  // the mesh's plan (perm, iperm on the device)
+  Buf leaf_lo, leaf_ptr, leaf_ent, dn, D1, D2, vt_items, lb_items;
+  int32_t n_vt = 0, n_lb = 0;
   Buf lr[2], U[2], V[2];
   int32_t n_lr = 0, n_dense = 0, n_leaf = 0;
-  int64_t tstride = 0;
+  int64_t tstride = 0, pstride = 0;
+  bool f32 = false;  // complex64 operators, FP32 entries and products (precision mixed)
   bemgpu_hmatrix_stats st{};
   size_t bytes() const {
-    size_t b = perm.bytes + iperm.bytes + leaf_lo.bytes + leaf_ptr.bytes + leaf_ent.bytes +
-               dn.bytes + D1.bytes + D2.bytes;
+    size_t b = leaf_lo.bytes + leaf_ptr.bytes + leaf_ent.bytes + dn.bytes + D1.bytes +
+               D2.bytes + vt_items.bytes + lb_items.bytes;
     for (int o = 0; o < 2; ++o) b += lr[o].bytes + U[o].bytes + V[o].bytes;
     return b;
   }
-  HmOp op(int o, double* T) const {
+  size_t scratch_bytes(int32_t nr) const {  // T and P of a product over nr vectors
+    return (size_t)nr * ((size_t)tstride * 16 + (size_t)pstride * (f32 ? 8 : 16));
+  }
+  // s: scratch_bytes(nr) bytes for products over at most nr vectors
+  HmOp op(int o, void* s, int32_t nr) const {
+    double* T = static_cast<double*>(s);
     HmOp A{};
     A.lr = lr[o].as<HmLR>();
     A.dn = dn.as<HmDense>();
-    A.U = U[o].as<double>();
-    A.V = V[o].as<double>();
-    A.D = (o == 0 ? D1 : D2).as<double>();
+    A.U = U[o].p;
+    A.V = V[o].p;
+    A.D = (o == 0 ? D1 : D2).p;
+    A.f32 = f32 ? 1 : 0;
     A.leaf_lo = leaf_lo.as<int32_t>();
     A.leaf_ptr = leaf_ptr.as<int32_t>();
     A.leaf_ent = leaf_ent.as<int32_t>();
     A.n_lr = n_lr;
     A.n_dense = n_dense;
     A.n_leaf = n_leaf;
+    A.vt_items = vt_items.as<HmItem>();
+    A.lb_items = lb_items.as<HmItem>();
+    A.n_vt = n_vt;
+    A.n_lb = n_lb;
     A.T = T;
     A.tstride = tstride;
+    A.P = static_cast<char*>(s) + (size_t)nr * tstride * 16;
+    A.pstride = pstride;
     return A;
   }
 };
@@ -2772,18 +2794,72 @@ int check_hm_options(bemgpu_ctx* c, const bemgpu_hmatrix_options& o) {
 
 // Cluster tree and blocks on the host, cross approximation of both operators, full
 // blocks (regular kernel + near kernel into block storage), product lists.
-int hm_build(bemgpu_ctx* c, const MeshData* m, const bemgpu_problem& p, int kind,
+int hm_build(bemgpu_ctx* c, MeshData* m, const bemgpu_problem& p, int kind,
              const bemgpu_hmatrix_options& o, HmData* H) {
   const Launch L = c->launch();
   Timer tb(c->stream);
   const int64_t n = m->n;
-  std::vector<double> cent, diam;
-  panel_centroids(m->nodes_h.data(), m->tris_h.data(), n, &cent, &diam);
-  std::string err;
-  if (hm_build_plan(cent.data(), diam.data(), n, o.leaf_size, o.eta, m->eta, &H->plan, &err))
-    return fail(c, BEMGPU_EINVAL, err);
+  std::shared_ptr<MeshData::HmPlanCache>& pc = m->hm_plans[{o.leaf_size, o.eta}];
+  if (!pc) {  // cluster tree, partition and near-pair destinations of this mesh
+    auto fresh = std::make_shared<MeshData::HmPlanCache>();
+    std::vector<double> cent, diam;
+    panel_centroids(m->nodes_h.data(), m->tris_h.data(), n, &cent, &diam);
+    std::string err;
+    if (hm_build_plan(cent.data(), diam.data(), n, o.leaf_size, o.eta, m->eta, &fresh->plan,
+                      &err)) {
+      m->hm_plans.erase({o.leaf_size, o.eta});
+      return fail(c, BEMGPU_EINVAL, err);
+    }
+    const HmPlan& P = fresh->plan;
+    std::vector<int64_t> dst((size_t)std::max<int64_t>(1, m->n_near), 0);
+    if (m->n_near > 0) {
+      std::vector<int64_t> rowptr, cols;
+      near_pairs(cent, diam, m->eta, &rowptr, &cols);
+      if ((int64_t)cols.size() != m->n_near) {
+        m->hm_plans.erase({o.leaf_size, o.eta});
+        return fail(c, BEMGPU_EINVAL, "internal: near-pair list differs from the mesh's");
+      }
+      // destination of every near pair inside its full leaf block: the leaf pairs of the
+      // full blocks, looked up per row leaf (blocks of a row leaf sorted by column leaf)
+      const int64_t nl = (int64_t)P.leaf_lo.size() - 1;
+      std::vector<int32_t> leaf((size_t)n);
+      for (int64_t l = 0; l < nl; ++l)
+        for (int32_t t = P.leaf_lo[(size_t)l]; t < P.leaf_lo[(size_t)l + 1]; ++t) leaf[(size_t)t] = (int32_t)l;
+      std::vector<std::vector<std::pair<int32_t, int64_t>>> row_blocks((size_t)nl);
+      int64_t off = 0;
+      for (const HmBlock& B : P.dense) {  // full-block offsets as hm_build lays them out
+        row_blocks[(size_t)leaf[(size_t)B.rlo]].push_back({leaf[(size_t)B.clo], off});
+        off += (int64_t)B.m * B.n;
+      }
+      for (auto& v : row_blocks) std::sort(v.begin(), v.end());
+      for (int64_t i = 0; i < n; ++i)
+        for (int64_t q = rowptr[i]; q < rowptr[i + 1]; ++q) {
+          const int32_t pi = P.iperm[(size_t)i], pj = P.iperm[(size_t)cols[q]];
+          const auto& v = row_blocks[(size_t)leaf[(size_t)pi]];
+          auto it = std::lower_bound(v.begin(), v.end(),
+                                     std::pair<int32_t, int64_t>{leaf[(size_t)pj], INT64_MIN});
+          if (it == v.end() || it->first != leaf[(size_t)pj]) {
+            m->hm_plans.erase({o.leaf_size, o.eta});
+            return fail(c, BEMGPU_EINVAL, "internal: near pair outside the full blocks");
+          }
+          const int32_t rlo = P.leaf_lo[(size_t)leaf[(size_t)pi]];
+          const int32_t clo = P.leaf_lo[(size_t)leaf[(size_t)pj]];
+          const int32_t mrows = P.leaf_lo[(size_t)leaf[(size_t)pi] + 1] - rlo;
+          dst[(size_t)q] = it->second + (pi - rlo) + (int64_t)(pj - clo) * mrows;
+        }
+    }
+    TRY(upload(c, P.perm, &fresh->perm));
+    TRY(upload(c, P.iperm, &fresh->iperm));
+    TRY(upload(c, dst, &fresh->near_dst));
+    pc = fresh;
+  }
+  H->plan = pc->plan;
+  H->pc = pc;
   const HmPlan& P = H->plan;
   const double k = p.k;
+  H->f32 = p.precision == BEMGPU_MIXED;
+  const size_t es = H->f32 ? 8 : 16;  // bytes per stored complex entry
+  const void* recs = H->f32 ? m->panelsf.p : m->panels.p;
   const double a_re = 0.0, a_im = kind == kAsmBM ? 1.0 / k : 0.0;  // alpha = i / k
   // admissible blocks: rank capacity below the size where a full block is cheaper
   std::vector<HmLR> lr(P.lowrank.size());
@@ -2793,24 +2869,21 @@ int hm_build(bemgpu_ctx* c, const MeshData* m, const bemgpu_problem& p, int kind
     const HmBlock& B = P.lowrank[b];
     const int64_t cap = (int64_t)B.m * B.n / ((int64_t)B.m + B.n);
     const int32_t kmax = (int32_t)std::max<int64_t>(1, std::min<int64_t>(kHmMaxRank, cap));
-    lr[b] = HmLR{B.rlo, B.m, B.clo, B.n, uo, vo, to, kmax, 0, 0, 0};
+    lr[b] = HmLR{B.rlo, B.m, B.clo, B.n, uo, vo, to, kmax, 0, 0, 0, 0};
     uo += (int64_t)B.m * kmax;
     vo += (int64_t)B.n * kmax;
     to += kmax;
     max_m = std::max(max_m, B.m);
   }
-  TRY(upload(c, P.perm, &H->perm));
-  TRY(upload(c, P.iperm, &H->iperm));
   std::vector<HmLR> lrh[2];
   for (int op = 0; op < 2; ++op) {
     TRY(upload(c, lr, &H->lr[op]));
-    TRY(alloc(c, (size_t)std::max<int64_t>(1, uo) * 16, &H->U[op]));
-    TRY(alloc(c, (size_t)std::max<int64_t>(1, vo) * 16, &H->V[op]));
+    TRY(alloc(c, (size_t)std::max<int64_t>(1, uo) * es, &H->U[op]));
+    TRY(alloc(c, (size_t)std::max<int64_t>(1, vo) * es, &H->V[op]));
     {
       Prof pr(c, "hm_aca");
-      launch_hm_aca(L, H->lr[op].as<HmLR>(), (int32_t)lr.size(), max_m, H->U[op].as<double>(),
-                    H->V[op].as<double>(), m->panels.as<double>(), H->perm.as<int32_t>(), kind,
-                    op, k, a_re, a_im, o.tol);
+      launch_hm_aca(L, H->lr[op].as<HmLR>(), (int32_t)lr.size(), max_m, H->U[op].p, H->V[op].p,
+                    recs, H->f32, H->pc->perm.as<int32_t>(), kind, op, k, a_re, a_im, o.tol);
     }
     CUDA_TRY(c, cudaGetLastError());
   }
@@ -2820,66 +2893,71 @@ int hm_build(bemgpu_ctx* c, const MeshData* m, const bemgpu_problem& p, int kind
   std::vector<HmBlock> dblk = P.dense, lblk;
   std::vector<HmLR> keep[2];
   int64_t off = 0;
+  int64_t poff = 0;
   for (const HmBlock& B : P.dense) {
-    dn.push_back(HmDense{B.rlo, B.m, B.clo, B.n, off});
+    dn.push_back(HmDense{B.rlo, B.m, B.clo, B.n, off, poff});
     off += (int64_t)B.m * B.n;
+    poff += B.m;
   }
   int64_t densified = 0, lr_entries = 0;
   int32_t max_rank = 0;
   for (size_t b = 0; b < lr.size(); ++b) {
     if (!lrh[0][b].conv || !lrh[1][b].conv) {
       const HmBlock& B = P.lowrank[b];
-      dn.push_back(HmDense{B.rlo, B.m, B.clo, B.n, off});
+      dn.push_back(HmDense{B.rlo, B.m, B.clo, B.n, off, poff});
       dblk.push_back(B);
       off += (int64_t)B.m * B.n;
+      poff += B.m;
       ++densified;
       continue;
     }
     lblk.push_back(P.lowrank[b]);
     for (int op = 0; op < 2; ++op) {
       keep[op].push_back(lrh[op][b]);
+      keep[op].back().poff = poff;
       lr_entries += (int64_t)lrh[op][b].rank * (lrh[op][b].m + lrh[op][b].n);
       max_rank = std::max(max_rank, lrh[op][b].rank);
     }
+    poff += P.lowrank[b].m;
   }
+  H->pstride = std::max<int64_t>(1, poff);
+  // work items of the compressed products and the coefficient offsets of the kept blocks
+  std::vector<HmItem> vti, lbi;
+  int64_t tof = 0;
+  for (size_t b = 0; b < lblk.size(); ++b) {
+    const int32_t m_ = lblk[b].m, n_ = lblk[b].n;
+    const int32_t nvc = (n_ + kHmColChunk - 1) / kHmColChunk;
+    for (int op = 0; op < 2; ++op) {
+      keep[op][b].toff = tof;
+      keep[op][b].nvc = nvc;
+    }
+    tof += (int64_t)nvc * keep[0][b].kmax;
+    for (int32_t c = 0; c < nvc; ++c)
+      vti.push_back(HmItem{(int32_t)b, c * kHmColChunk, std::min(kHmColChunk, n_ - c * kHmColChunk), c});
+    for (int32_t r0 = 0; r0 < m_; r0 += kHmRowChunk)
+      lbi.push_back(HmItem{(int32_t)b, r0, std::min(kHmRowChunk, m_ - r0), 0});
+  }
+  H->tstride = std::max<int64_t>(1, tof);
+  H->n_vt = (int32_t)vti.size();
+  H->n_lb = (int32_t)lbi.size();
+  TRY(upload(c, vti, &H->vt_items));
+  TRY(upload(c, lbi, &H->lb_items));
   H->n_dense = (int32_t)dn.size();
   H->n_lr = (int32_t)lblk.size();
-  H->tstride = std::max<int64_t>(1, to);
   TRY(upload(c, dn, &H->dn));
-  TRY(alloc(c, (size_t)std::max<int64_t>(1, off) * 16, &H->D1));
-  TRY(alloc(c, (size_t)std::max<int64_t>(1, off) * 16, &H->D2));
+  TRY(alloc(c, (size_t)std::max<int64_t>(1, off) * es, &H->D1));
+  TRY(alloc(c, (size_t)std::max<int64_t>(1, off) * es, &H->D2));
   for (int op = 0; op < 2; ++op) TRY(upload(c, keep[op], &H->lr[op]));
   {
     Prof pr(c, "hm_dense");
-    launch_hm_dense(L, H->dn.as<HmDense>(), H->n_dense, H->D1.as<double>(), H->D2.as<double>(),
-                    m->panels.as<double>(), H->perm.as<int32_t>(), kind, k, a_re, a_im);
+    launch_hm_dense(L, H->dn.as<HmDense>(), H->n_dense, H->D1.p, H->D2.p, recs, H->f32,
+                    H->pc->perm.as<int32_t>(), kind, k, a_re, a_im);
   }
   // near pairs (the mesh's list, same order) into their full leaf blocks
   if (m->n_near > 0) {
-    std::vector<int64_t> rowptr, cols;
-    near_pairs(cent, diam, m->eta, &rowptr, &cols);
-    if ((int64_t)cols.size() != m->n_near)
-      return fail(c, BEMGPU_EINVAL, "internal: near-pair list differs from the mesh's");
-    const int64_t nl = (int64_t)P.leaf_lo.size() - 1;
-    auto leaf_of = [&](int32_t pos) {
-      return (int64_t)(std::upper_bound(P.leaf_lo.begin(), P.leaf_lo.end(), pos) -
-                       P.leaf_lo.begin() - 1);
-    };
-    std::map<int64_t, int32_t> blk;
-    for (size_t b = 0; b < P.dense.size(); ++b)
-      blk[(int64_t)leaf_of(P.dense[b].rlo) * nl + leaf_of(P.dense[b].clo)] = (int32_t)b;
-    std::vector<int64_t> dst((size_t)m->n_near);
-    for (int64_t i = 0; i < n; ++i)
-      for (int64_t q = rowptr[i]; q < rowptr[i + 1]; ++q) {
-        const int32_t pi = P.iperm[(size_t)i], pj = P.iperm[(size_t)cols[q]];
-        auto it = blk.find(leaf_of(pi) * nl + leaf_of(pj));
-        if (it == blk.end())
-          return fail(c, BEMGPU_EINVAL, "internal: near pair outside the full blocks");
-        const HmDense& D = dn[(size_t)it->second];
-        dst[(size_t)q] = D.off + (pi - D.rlo) + (int64_t)(pj - D.clo) * D.m;
-      }
-    Buf d_dst, d_ai;
-    TRY(upload(c, dst, &d_dst));
+    Buf d_ai, d_corr;
+    if (H->f32)  // complex64 full blocks: the near values' rounding errors are not kept
+      TRY(alloc(c, (size_t)m->n_near * 16, &d_corr));
     AsmInst I{};
     I.panels = m->panels.as<double>();
     I.panelsf = m->panelsf.as<float>();
@@ -2897,15 +2975,17 @@ int hm_build(bemgpu_ctx* c, const MeshData* m, const bemgpu_problem& p, int kind
     I.kind = kind;
     I.out1 = H->D1.p;
     I.out2 = H->D2.p;
-    I.near_dst = d_dst.as<int64_t>();
+    I.c64 = H->f32 ? 3 : 0;
+    I.dnear = I.dnear2 = H->f32 ? d_corr.as<double>() : nullptr;
+    I.near_dst = pc->near_dst.as<int64_t>();
     std::vector<AsmInst> ai{I};
     TRY(upload(c, ai, &d_ai));
     {
       Prof pr(c, "near");
-      launch_assemble_near(L, d_ai.as<AsmInst>(), 1, m->n_near, kind, false);
+      launch_assemble_near(L, d_ai.as<AsmInst>(), 1, m->n_near, kind, H->f32);
     }
     CUDA_TRY(c, cudaGetLastError());
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // d_dst / d_ai are released below
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // d_ai / d_corr are released below
   }
   std::vector<int32_t> ptr, ent;
   hm_leaf_lists(P, dblk, lblk, &ptr, &ent);
@@ -2939,9 +3019,9 @@ int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x,
              std::vector<double>* absres) {
   const Launch L = c->launch();
   const int32_t R = o.restart, mi = std::max(1, o.maxiter);
-  const int32_t chunks = (int32_t)((n + 4095) / 4096);
+  const int32_t chunks = (int32_t)((n + kGmChunk - 1) / kGmChunk);
   const size_t per = ((size_t)(R + 1) * n + 2 * (size_t)n) * 16 + (size_t)(R + 1) * R * 16 +
-                     (size_t)chunks * (R + 1) * 16 + (size_t)mi * 8 + (size_t)H.tstride * 16 +
+                     (size_t)chunks * (R + 1) * 16 + (size_t)mi * 8 + H.scratch_bytes(1) +
                      (size_t)(4 * R + 8) * 16;
   const uint64_t avail = c->budget > c->live ? (c->budget - c->live) : 0;
   const int32_t G = (int32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)nr, avail / 2 / per));
@@ -2963,8 +3043,8 @@ int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x,
     TRY(alloc(c, (size_t)g * chunks * (R + 1) * 16, &part));
     TRY(alloc(c, (size_t)g * mi * 8, &hb));
     TRY(alloc(c, (size_t)g * n * 16, &w));
-    TRY(alloc(c, (size_t)g * H.tstride * 16, &T));
-    TRY(alloc(c, sizeof(int32_t), &nact));
+    TRY(alloc(c, H.scratch_bytes(g), &T));
+    TRY(alloc(c, sizeof(int32_t) * (size_t)(2 + g), &nact));  // count + one per CTA
     CUDA_TRY(c, cudaMemsetAsync(st.p, 0, st.bytes, c->stream));
     CUDA_TRY(c, cudaMemsetAsync(Hh.p, 0, Hh.bytes, c->stream));
     CUDA_TRY(c, cudaMemsetAsync(gg.p, 0, gg.bytes, c->stream));
@@ -2992,7 +3072,7 @@ int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x,
     W.maxiter = mi;
     W.chunks = chunks;
     W.nact = nact.as<int32_t>();
-    const HmOp A = H.op(op, T.as<double>());
+    const HmOp A = H.op(op, T.p, g);
     auto active = [&](int32_t* out) -> int {
       CUDA_TRY(c, cudaMemcpyAsync(out, W.nact, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
       CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -3060,8 +3140,6 @@ int hm_problem(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_problem* pro
   if (*kind != kAsmBM && *kind != kAsmCBIE)
     return fail(c, BEMGPU_EINVAL,
                 "hierarchical compression applies to Rigid and PressureRelease boundaries");
-  if (problem->precision != BEMGPU_DOUBLE)
-    return fail(c, BEMGPU_EINVAL, "hierarchical compression computes in double precision");
   if (std::fabs(problem->near_eta - mesh->d->eta) > 0)
     return fail(c, BEMGPU_EINVAL, "near_eta differs from the mesh's (upload with that eta)");
   return check_hm_options(c, *opt);
@@ -3160,7 +3238,7 @@ int bemgpu_hmatrix_solve(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_pr
   TRY(alloc(c, (size_t)n * nrhs * 16, &bb));
   TRY(alloc(c, (size_t)n * nrhs * 16, &xp));
   TRY(alloc(c, (size_t)n * nrhs * 16, &xs));
-  TRY(alloc(c, (size_t)H.tstride * nrhs * 16, &T));
+  TRY(alloc(c, H.scratch_bytes(nrhs), &T));
   TRY(alloc(c, (size_t)n * nrhs * 16, &sd->ps));
   TRY(alloc(c, (size_t)n * nrhs * 16, &sd->qs));
   WaveInst wv{};
@@ -3182,10 +3260,10 @@ int bemgpu_hmatrix_solve(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_pr
   const bool rigid = p.boundary == BEMGPU_RIGID;
   const int sys = rigid ? 0 : 1;
   launch_hm_permute(L, (rigid ? qinc : pinc).as<double>(), n, tp.as<double>(), n,
-                    H.perm.as<int32_t>(), n, nrhs);
+                    H.pc->perm.as<int32_t>(), n, nrhs);
   {
     Prof pr(c, "hm_matvec");
-    launch_hm_matvec(L, H.op(1 - sys, T.as<double>()), tp.as<double>(), n, bb.as<double>(), n,
+    launch_hm_matvec(L, H.op(1 - sys, T.p, nrhs), tp.as<double>(), n, bb.as<double>(), n,
                      nullptr, 0, 0.0, 1.0, nrhs, nullptr, 0);
   }
   CUDA_TRY(c, cudaGetLastError());
@@ -3194,7 +3272,7 @@ int bemgpu_hmatrix_solve(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_pr
   TRY(hm_gmres(c, H, sys, bb.as<double>(), xp.as<double>(), n, nrhs, *opt, &sd->gm_hist,
                &sd->gm_iters, &conv, &resid, &absres));
   sd->gm_stride = std::max(1, opt->maxiter);
-  launch_hm_permute(L, xp.as<double>(), n, xs.as<double>(), n, H.iperm.as<int32_t>(), n, nrhs);
+  launch_hm_permute(L, xp.as<double>(), n, xs.as<double>(), n, H.pc->iperm.as<int32_t>(), n, nrhs);
   TraceInst tr{};
   tr.x = xs.as<double>();
   tr.ldx = n;
@@ -3226,8 +3304,8 @@ int bemgpu_hmatrix_solve(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_pr
   dg.quadrature_nodes = n;
   dg.near_pairs = m->n_near;
   dg.formulation = kind == kAsmBM ? BEMGPU_BURTON_MILLER : BEMGPU_CBIE;
-  dg.precision = BEMGPU_DOUBLE;
-  dg.factor_precision = 1;
+  dg.precision = p.precision;
+  dg.factor_precision = H.f32 ? 0 : 1;
   dg.refinement_iterations = S.gmres_iterations;
   dg.coupling_im = kind == kAsmBM ? 1.0 / p.k : 0.0;
   for (int32_t r = 0; r < nrhs; ++r) {
@@ -3288,12 +3366,12 @@ int bemgpu_hmatrix_apply(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_pr
   TRY(alloc(c, (size_t)n * nr * 16, &xp));
   TRY(alloc(c, (size_t)n * nr * 16, &yp));
   TRY(alloc(c, (size_t)n * nr * 16, &yh));
-  TRY(alloc(c, (size_t)H.tstride * nr * 16, &T));
+  TRY(alloc(c, H.scratch_bytes(nr), &T));
   CUDA_TRY(c, cudaMemcpyAsync(xh.p, X, (size_t)n * nr * 16, cudaMemcpyHostToDevice, c->stream));
-  launch_hm_permute(L, xh.as<double>(), n, xp.as<double>(), n, H.perm.as<int32_t>(), n, nr);
-  launch_hm_matvec(L, H.op(op, T.as<double>()), xp.as<double>(), n, yp.as<double>(), n, nullptr, 0,
+  launch_hm_permute(L, xh.as<double>(), n, xp.as<double>(), n, H.pc->perm.as<int32_t>(), n, nr);
+  launch_hm_matvec(L, H.op(op, T.p, nr), xp.as<double>(), n, yp.as<double>(), n, nullptr, 0,
                    0.0, 1.0, nr, nullptr, 0);
-  launch_hm_permute(L, yp.as<double>(), n, yh.as<double>(), n, H.iperm.as<int32_t>(), n, nr);
+  launch_hm_permute(L, yp.as<double>(), n, yh.as<double>(), n, H.pc->iperm.as<int32_t>(), n, nr);
   CUDA_TRY(c, cudaMemcpyAsync(Y, yh.p, (size_t)n * nr * 16, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   CUDA_TRY(c, cudaGetLastError());

@@ -66,23 +66,43 @@ __device__ __forceinline__ void amax(double& v, int32_t& i, double ov, int32_t o
 }
 
 // Entry (i, j) of M1 (op 0) or M2 (op 1) of a rigid/soft assembly kind at panels pi != pj
-// by the regular rule, combined as in the dense FP64 regular kernel.
-template <int KIND, int OP>
-__device__ __forceinline__ cd hm_entry(const double* __restrict__ panels, int32_t pi, int32_t pj,
-                                       double k, cd al) {
-  const double* ri = panels + (int64_t)pi * kPanelDoubles;
-  const double x[3] = {ri[0], ri[1], ri[2]}, nx[3] = {ri[3], ri[4], ri[5]};
-  Acc<double> a;
-  a.S = a.D = a.K = a.H = cd{0.0, 0.0};
-  regular_panel<double, KIND == kAsmBM>(panels + (int64_t)pj * kPanelDoubles, x, nx, k, a);
+// by the regular rule in precision R (FP32 on the records relative to the mesh centre, as
+// the dense mixed-precision assembly), combined as in the dense regular kernel.
+template <typename R, int KIND, int OP>
+__device__ __forceinline__ cx<R> hm_entry(const R* __restrict__ recs, int32_t pi, int32_t pj,
+                                          R k, cx<R> al) {
+  constexpr int kRec = Prec<R>::kRec;
+  const R* ri = recs + (int64_t)pi * kRec;
+  const R x[3] = {ri[0], ri[1], ri[2]}, nx[3] = {ri[3], ri[4], ri[5]};
+  Acc<R> a;
+  a.S = a.D = a.K = a.H = cx<R>{0, 0};
+  regular_panel<R, KIND == kAsmBM>(recs + (int64_t)pj * kRec, x, nx, k, a);
   if (OP == 0) {
-    cd m1 = cd{-a.D.x, -a.D.y};
+    cx<R> m1 = cx<R>{-a.D.x, -a.D.y};
     if (KIND == kAsmBM) m1 -= al * a.H;
     return m1;
   }
-  cd m2 = a.S;
+  cx<R> m2 = a.S;
   if (KIND == kAsmBM) m2 += al * a.K;
   return m2;
+}
+
+template <typename R>
+__device__ __forceinline__ cx<R> cconjmul(cx<R> a, cx<R> b) {  // conj(a) b
+  return cx<R>{a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x};
+}
+template <typename R>
+__device__ __forceinline__ cx<R> cwarp_sum(cx<R> v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, off);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, off);
+  }
+  return v;
+}
+template <typename R>
+__device__ __forceinline__ cx<R> to(cd v) {
+  return cx<R>{(R)v.x, (R)v.y};
 }
 
 constexpr int kAcaT = 256;
@@ -111,25 +131,27 @@ __device__ __forceinline__ void block_argmax(double& v, int32_t& i, double* rv, 
 }  // namespace
 
 // ------------------------------------------------------------------ cross approximation
-template <int KIND, int OP>
-__global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, double* Up, double* Vp,
-                                                  const double* __restrict__ panels,
-                                                  const int32_t* __restrict__ perm, double k,
+template <typename R, int KIND, int OP>
+__global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, void* Up, void* Vp,
+                                                  const R* __restrict__ recs,
+                                                  const int32_t* __restrict__ perm, double k_,
                                                   double a_re, double a_im, double tol) {
+  using C = cx<R>;
   HmLR& B = lrs[blockIdx.x];
   const int m = B.m, n = B.n, kmax = B.kmax;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  double* U = Up + 2 * B.uoff;
-  double* V = Vp + 2 * B.voff;
+  C* U = static_cast<C*>(Up) + B.uoff;
+  C* V = static_cast<C*>(Vp) + B.voff;
   const int32_t* prow = perm + B.rlo;
   const int32_t* pcol = perm + B.clo;
-  const cd al = {a_re, a_im};
+  const C al = {(R)a_re, (R)a_im};
+  const R k = (R)k_;
   extern __shared__ uint32_t used[];  // pivot rows taken, (m + 31) / 32 words
   __shared__ double rv[kAcaW];
   __shared__ int32_t ri[kAcaW];
-  __shared__ cd su[kHmMaxRank], sv[kHmMaxRank];    // U[i*, l], V[j*, l]
-  __shared__ cd cu[kHmMaxRank], cv[kHmMaxRank];    // projections of the new cross
-  __shared__ cd s_piv;
+  __shared__ C su[kHmMaxRank], sv[kHmMaxRank];    // U[i*, l], V[j*, l]
+  __shared__ C cu[kHmMaxRank], cv[kHmMaxRank];    // projections of the new cross
+  __shared__ C s_piv;
   __shared__ double s_s2;
   __shared__ int s_stop;
   const int words = (m + 31) >> 5;
@@ -139,7 +161,7 @@ __global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, double
   int32_t istar = 0;
   __syncthreads();
   for (int it = 0; rank < kmax && it < m; ++it) {
-    if (tid < rank) su[tid] = ldc(U, istar + (int64_t)tid * m);
+    if (tid < rank) su[tid] = U[istar + (int64_t)tid * m];
     if (tid == 0) used[istar >> 5] |= 1u << (istar & 31);
     __syncthreads();
     // residual row i*: A[i*, :] - sum_l U[i*, l] V[:, l]
@@ -147,10 +169,10 @@ __global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, double
     int32_t bj = INT32_MAX;
     const int32_t pi = prow[istar];
     for (int j = tid; j < n; j += kAcaT) {
-      cd v = hm_entry<KIND, OP>(panels, pi, pcol[j], k, al);
-      for (int l = 0; l < rank; ++l) v -= su[l] * ldc(V, j + (int64_t)l * n);
-      stc(V, j + (int64_t)rank * n, v);
-      amax(bv, bj, abs2(v), j);
+      C v = hm_entry<R, KIND, OP>(recs, pi, pcol[j], k, al);
+      for (int l = 0; l < rank; ++l) v -= su[l] * V[j + (int64_t)l * n];
+      V[j + (int64_t)rank * n] = v;
+      amax(bv, bj, (double)(v.x * v.x + v.y * v.y), j);
     }
     block_argmax(bv, bj, rv, ri);
     if (!(bv > 0.0)) {  // the residual row vanishes: continue from the next unused row
@@ -170,32 +192,32 @@ __global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, double
       continue;
     }
     const int32_t jstar = bj;
-    if (tid == 0) s_piv = ldc(V, jstar + (int64_t)rank * n);
-    if (tid < rank) sv[tid] = ldc(V, jstar + (int64_t)tid * n);
+    if (tid == 0) s_piv = V[jstar + (int64_t)rank * n];
+    if (tid < rank) sv[tid] = V[jstar + (int64_t)tid * n];
     __syncthreads();
-    const cd inv = crecip(s_piv);
+    const R pd = s_piv.x * s_piv.x + s_piv.y * s_piv.y;
+    const C inv = {s_piv.x / pd, -s_piv.y / pd};
     // residual column j*: A[:, j*] - sum_l U[:, l] V[j*, l]; next pivot row
     double cb = -1.0;
     int32_t ci = INT32_MAX;
     const int32_t pj = pcol[jstar];
     for (int i = tid; i < m; i += kAcaT) {
-      cd u = hm_entry<KIND, OP>(panels, prow[i], pj, k, al);
-      for (int l = 0; l < rank; ++l) u -= ldc(U, i + (int64_t)l * m) * sv[l];
-      stc(U, i + (int64_t)rank * m, u);
-      if (!((used[i >> 5] >> (i & 31)) & 1u)) amax(cb, ci, abs2(u), i);
+      C u = hm_entry<R, KIND, OP>(recs, prow[i], pj, k, al);
+      for (int l = 0; l < rank; ++l) u -= U[i + (int64_t)l * m] * sv[l];
+      U[i + (int64_t)rank * m] = u;
+      if (!((used[i >> 5] >> (i & 31)) & 1u)) amax(cb, ci, (double)(u.x * u.x + u.y * u.y), i);
     }
-    for (int j = tid; j < n; j += kAcaT)
-      stc(V, j + (int64_t)rank * n, ldc(V, j + (int64_t)rank * n) * inv);
+    for (int j = tid; j < n; j += kAcaT) V[j + (int64_t)rank * n] = V[j + (int64_t)rank * n] * inv;
     __syncthreads();
     // projections U_l^H U_r and V_l^H V_r, l = 0..rank (one warp per l, fixed order)
     for (int l = wid; l <= rank; l += kAcaW) {
-      cd a = {0.0, 0.0}, b = {0.0, 0.0};
+      C a = {0, 0}, b = {0, 0};
       for (int i = lane; i < m; i += 32)
-        a += conjmul(ldc(U, i + (int64_t)l * m), ldc(U, i + (int64_t)rank * m));
+        a += cconjmul(U[i + (int64_t)l * m], U[i + (int64_t)rank * m]);
       for (int j = lane; j < n; j += 32)
-        b += conjmul(ldc(V, j + (int64_t)l * n), ldc(V, j + (int64_t)rank * n));
-      a = warp_sum(a);
-      b = warp_sum(b);
+        b += cconjmul(V[j + (int64_t)l * n], V[j + (int64_t)rank * n]);
+      a = cwarp_sum(a);
+      b = cwarp_sum(b);
       if (lane == 0) {
         cu[l] = a;
         cv[l] = b;
@@ -204,9 +226,10 @@ __global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, double
     block_argmax(cb, ci, rv, ri);
     if (tid == 0) {
       // |S_r|^2 = |S_{r-1}|^2 + |u_r|^2 |v_r|^2 + 2 Re sum_{l<r} (U_l^H u_r)(V_l^H v_r)
-      const double uv2 = cu[rank].x * cv[rank].x;
+      const double uv2 = (double)cu[rank].x * (double)cv[rank].x;
       double s = s_s2 + uv2;
-      for (int l = 0; l < rank; ++l) s += 2.0 * (cu[l].x * cv[l].x - cu[l].y * cv[l].y);
+      for (int l = 0; l < rank; ++l)
+        s += 2.0 * ((double)cu[l].x * cv[l].x - (double)cu[l].y * cv[l].y);
       s_s2 = s;
       s_stop = uv2 <= tol * tol * s ? 1 : 0;
     }
@@ -224,126 +247,245 @@ __global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, double
   }
 }
 
-void launch_hm_aca(const Launch& L, HmLR* lr, int32_t n_lr, int32_t max_m, double* U, double* V,
-                   const double* panels, const int32_t* perm, int kind, int op, double k,
+void launch_hm_aca(const Launch& L, HmLR* lr, int32_t n_lr, int32_t max_m, void* U, void* V,
+                   const void* recs, bool f32, const int32_t* perm, int kind, int op, double k,
                    double a_re, double a_im, double tol) {
   if (n_lr <= 0) return;
   const size_t smem = (size_t)((max_m + 31) / 32) * 4;
-  auto go = [&](auto kern) {
+  auto go = [&](auto kern, auto rec) {
     if (smem > 48 * 1024)
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<(unsigned)n_lr, kAcaT, smem, L.stream>>>(lr, U, V, panels, perm, k, a_re, a_im, tol);
+    kern<<<(unsigned)n_lr, kAcaT, smem, L.stream>>>(lr, U, V, rec, perm, k, a_re, a_im, tol);
   };
-  if (kind == kAsmBM)
-    op == 0 ? go(k_hm_aca<kAsmBM, 0>) : go(k_hm_aca<kAsmBM, 1>);
-  else
-    op == 0 ? go(k_hm_aca<kAsmCBIE, 0>) : go(k_hm_aca<kAsmCBIE, 1>);
+  const float* rf = static_cast<const float*>(recs);
+  const double* rd = static_cast<const double*>(recs);
+  const int sel = (f32 ? 4 : 0) + (kind == kAsmBM ? 2 : 0) + op;
+  switch (sel) {
+    case 0: go(k_hm_aca<double, kAsmCBIE, 0>, rd); break;
+    case 1: go(k_hm_aca<double, kAsmCBIE, 1>, rd); break;
+    case 2: go(k_hm_aca<double, kAsmBM, 0>, rd); break;
+    case 3: go(k_hm_aca<double, kAsmBM, 1>, rd); break;
+    case 4: go(k_hm_aca<float, kAsmCBIE, 0>, rf); break;
+    case 5: go(k_hm_aca<float, kAsmCBIE, 1>, rf); break;
+    case 6: go(k_hm_aca<float, kAsmBM, 0>, rf); break;
+    default: go(k_hm_aca<float, kAsmBM, 1>, rf); break;
+  }
   count_launch(1);
 }
 
 // ------------------------------------------------------------------ full blocks
-template <int KIND>
-__global__ void __launch_bounds__(256) k_hm_dense(const HmDense* __restrict__ dn, double* D1,
-                                                  double* D2, const double* __restrict__ panels,
-                                                  const int32_t* __restrict__ perm, double k,
+template <typename R, int KIND>
+__global__ void __launch_bounds__(256) k_hm_dense(const HmDense* __restrict__ dn, void* D1,
+                                                  void* D2, const R* __restrict__ recs,
+                                                  const int32_t* __restrict__ perm, double k_,
                                                   double a_re, double a_im) {
+  constexpr int kRec = Prec<R>::kRec;
   const HmDense B = dn[blockIdx.x];
   const int64_t cnt = (int64_t)B.m * B.n;
-  const cd al = {a_re, a_im};
+  const cx<R> al = {(R)a_re, (R)a_im};
+  const R k = (R)k_;
+  cx<R>* o1 = static_cast<cx<R>*>(D1) + B.off;
+  cx<R>* o2 = static_cast<cx<R>*>(D2) + B.off;
   for (int64_t e = (int64_t)blockIdx.y * blockDim.x + threadIdx.x; e < cnt;
        e += (int64_t)blockDim.x * gridDim.y) {
     const int i = (int)(e % B.m), j = (int)(e / B.m);
     const int32_t pi = perm[B.rlo + i], pj = perm[B.clo + j];
     if (pi == pj) continue;  // self pair: near kernel
-    const double* ri = panels + (int64_t)pi * kPanelDoubles;
-    const double x[3] = {ri[0], ri[1], ri[2]}, nx[3] = {ri[3], ri[4], ri[5]};
-    Acc<double> a;
-    a.S = a.D = a.K = a.H = cd{0.0, 0.0};
-    regular_panel<double, KIND == kAsmBM>(panels + (int64_t)pj * kPanelDoubles, x, nx, k, a);
-    cd m1 = cd{-a.D.x, -a.D.y}, m2 = a.S;
+    const R* ri = recs + (int64_t)pi * kRec;
+    const R x[3] = {ri[0], ri[1], ri[2]}, nx[3] = {ri[3], ri[4], ri[5]};
+    Acc<R> a;
+    a.S = a.D = a.K = a.H = cx<R>{0, 0};
+    regular_panel<R, KIND == kAsmBM>(recs + (int64_t)pj * kRec, x, nx, k, a);
+    cx<R> m1 = cx<R>{-a.D.x, -a.D.y}, m2 = a.S;
     if (KIND == kAsmBM) {
       m1 -= al * a.H;
       m2 += al * a.K;
     }
-    stc(D1, B.off + e, m1);
-    stc(D2, B.off + e, m2);
+    o1[e] = m1;
+    o2[e] = m2;
   }
 }
 
-void launch_hm_dense(const Launch& L, const HmDense* dn, int32_t n_dense, double* D1, double* D2,
-                     const double* panels, const int32_t* perm, int kind, double k, double a_re,
-                     double a_im) {
+void launch_hm_dense(const Launch& L, const HmDense* dn, int32_t n_dense, void* D1, void* D2,
+                     const void* recs, bool f32, const int32_t* perm, int kind, double k,
+                     double a_re, double a_im) {
   if (n_dense <= 0) return;
   dim3 g((unsigned)n_dense, 4);
-  if (kind == kAsmBM)
-    k_hm_dense<kAsmBM><<<g, 256, 0, L.stream>>>(dn, D1, D2, panels, perm, k, a_re, a_im);
-  else
-    k_hm_dense<kAsmCBIE><<<g, 256, 0, L.stream>>>(dn, D1, D2, panels, perm, k, a_re, a_im);
+  const float* rf = static_cast<const float*>(recs);
+  const double* rd = static_cast<const double*>(recs);
+  if (f32) {
+    if (kind == kAsmBM)
+      k_hm_dense<float, kAsmBM><<<g, 256, 0, L.stream>>>(dn, D1, D2, rf, perm, k, a_re, a_im);
+    else
+      k_hm_dense<float, kAsmCBIE><<<g, 256, 0, L.stream>>>(dn, D1, D2, rf, perm, k, a_re, a_im);
+  } else {
+    if (kind == kAsmBM)
+      k_hm_dense<double, kAsmBM><<<g, 256, 0, L.stream>>>(dn, D1, D2, rd, perm, k, a_re, a_im);
+    else
+      k_hm_dense<double, kAsmCBIE><<<g, 256, 0, L.stream>>>(dn, D1, D2, rd, perm, k, a_re, a_im);
+  }
   count_launch(1);
 }
 
 // ------------------------------------------------------------------ products
+// Operators stored in precision R (complex128 / complex64) are applied in that precision;
+// the vectors stay complex128.
 __device__ __forceinline__ bool rhs_on(const GmState* st, int r, int mode) {
   if (mode == 0 || !st) return true;
   return mode == 1 ? st[r].active != 0 : st[r].done == 0;
 }
 
+// Coefficients of one column chunk of a compressed block: T[toff + c kmax + l] =
+// sum over the chunk of V[j, l] x[clo + j]; one warp per l, four independent accumulators
+// per lane (added in a fixed order) to keep several loads in flight.
+template <typename R>
 __global__ void __launch_bounds__(256) k_hm_vt(HmOp A, const double* __restrict__ X, int64_t ldx,
                                                const GmState* st, int mode) {
+  using C = cx<R>;
   const int r = blockIdx.y;
   if (!rhs_on(st, r, mode)) return;
-  const HmLR& B = A.lr[blockIdx.x];
+  const HmItem it = A.vt_items[blockIdx.x];
+  const HmLR B = A.lr[it.blk];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const double* V = A.V + 2 * B.voff;
+  const C* V = static_cast<const C*>(A.V) + B.voff;
   const double* x = X + 2 * ((int64_t)r * ldx + B.clo);
+  double* T = A.T + 2 * ((int64_t)r * A.tstride + B.toff + (int64_t)it.c * B.kmax);
+  const int j0 = it.lo, j1 = it.lo + it.cnt;
   for (int l = wid; l < B.rank; l += 8) {
-    cd s = {0.0, 0.0};
-    for (int j = lane; j < B.n; j += 32) s += ldc(V, j + (int64_t)l * B.n) * ldc(x, j);
-    s = warp_sum(s);
-    if (lane == 0) stc(A.T, (int64_t)r * A.tstride + B.toff + l, s);
+    const C* v = V + (int64_t)l * B.n;
+    C s0 = {0, 0}, s1 = {0, 0}, s2 = {0, 0}, s3 = {0, 0};
+    int j = j0 + lane;
+    for (; j + 96 < j1; j += 128) {
+      s0 += v[j] * to<R>(ldc(x, j));
+      s1 += v[j + 32] * to<R>(ldc(x, j + 32));
+      s2 += v[j + 64] * to<R>(ldc(x, j + 64));
+      s3 += v[j + 96] * to<R>(ldc(x, j + 96));
+    }
+    for (; j < j1; j += 32) s0 += v[j] * to<R>(ldc(x, j));
+    C s = cwarp_sum(((s0 + s1) + s2) + s3);
+    if (lane == 0) stc(T, l, cd{(double)s.x, (double)s.y});
   }
 }
 
 constexpr int kLeafRows = 64;
 constexpr int kLeafSlices = 4;
 
-__global__ void __launch_bounds__(kLeafRows * kLeafSlices) k_hm_leaf(
-    HmOp A, const double* __restrict__ X, int64_t ldx, double* __restrict__ Y, int64_t ldy,
-    const double* __restrict__ Bv, int64_t ldb, double sb, double sa, const GmState* st,
-    int mode) {
+// Partial rows of every full block: P[poff + i] = sum_j D[i, j] x[clo + j] (64 rows x 4
+// column slices per pass, slices added in a fixed order).
+template <typename R>
+__global__ void __launch_bounds__(kLeafRows * kLeafSlices) k_hm_dblk(
+    HmOp A, const double* __restrict__ X, int64_t ldx, const GmState* st, int mode) {
+  using C = cx<R>;
+  const int r = blockIdx.y;
+  if (!rhs_on(st, r, mode)) return;
+  const HmDense& B = A.dn[blockIdx.x];
+  const int row = threadIdx.x % kLeafRows, s = threadIdx.x / kLeafRows;
+  __shared__ C part[kLeafSlices][kLeafRows];
+  const C* D = static_cast<const C*>(A.D) + B.off;
+  const double* x = X + 2 * ((int64_t)r * ldx + B.clo);
+  C* P = static_cast<C*>(A.P) + (int64_t)r * A.pstride + B.poff;
+  if (B.m == kLeafRows && B.n == kLeafRows) {  // leaf x leaf block: all loads in flight
+    constexpr int kPer = kLeafRows / kLeafSlices;
+    C v[kPer];
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+      const int j = s + q * kLeafSlices;
+      v[q] = D[row + (int64_t)j * kLeafRows] * to<R>(ldc(x, j));
+    }
+    C a = v[0];
+#pragma unroll
+    for (int q = 1; q < kPer; ++q) a += v[q];
+    part[s][row] = a;
+    __syncthreads();
+    if (s == 0) P[row] = ((part[0][row] + part[1][row]) + part[2][row]) + part[3][row];
+    return;
+  }
+  for (int r0 = 0; r0 < B.m; r0 += kLeafRows) {
+    const int i = r0 + row;
+    C a0 = {0, 0}, a1 = {0, 0};
+    if (i < B.m) {
+      int j = s;
+      for (; j + kLeafSlices < B.n; j += 2 * kLeafSlices) {
+        a0 += D[i + (int64_t)j * B.m] * to<R>(ldc(x, j));
+        a1 += D[i + (int64_t)(j + kLeafSlices) * B.m] * to<R>(ldc(x, j + kLeafSlices));
+      }
+      for (; j < B.n; j += kLeafSlices) a0 += D[i + (int64_t)j * B.m] * to<R>(ldc(x, j));
+    }
+    part[s][row] = a0 + a1;
+    __syncthreads();
+    if (s == 0 && i < B.m) P[i] = ((part[0][row] + part[1][row]) + part[2][row]) + part[3][row];
+    __syncthreads();
+  }
+}
+
+// Partial rows of one row chunk of a compressed block: P[poff + i] = sum_l U[i, l] t[l],
+// t = the block's coefficient chunks added in order.
+template <typename R>
+__global__ void __launch_bounds__(kHmRowChunk) k_hm_lblk(HmOp A, const GmState* st, int mode) {
+  using C = cx<R>;
+  const int r = blockIdx.y;
+  if (!rhs_on(st, r, mode)) return;
+  const HmItem it = A.lb_items[blockIdx.x];
+  const HmLR B = A.lr[it.blk];
+  __shared__ C t[kHmMaxRank];
+  const double* T = A.T + 2 * ((int64_t)r * A.tstride + B.toff);
+  if (threadIdx.x < B.rank) {
+    cd v = ldc(T, threadIdx.x);
+    for (int c = 1; c < B.nvc; ++c) v += ldc(T, (int64_t)c * B.kmax + threadIdx.x);
+    t[threadIdx.x] = to<R>(v);
+  }
+  __syncthreads();
+  const int i = it.lo + threadIdx.x;
+  if (threadIdx.x >= it.cnt) return;
+  const C* U = static_cast<const C*>(A.U) + B.uoff + i;
+  C a0 = {0, 0}, a1 = {0, 0}, a2 = {0, 0}, a3 = {0, 0};
+  int l = 0;
+  for (; l + 3 < B.rank; l += 4) {
+    a0 += U[(int64_t)l * B.m] * t[l];
+    a1 += U[(int64_t)(l + 1) * B.m] * t[l + 1];
+    a2 += U[(int64_t)(l + 2) * B.m] * t[l + 2];
+    a3 += U[(int64_t)(l + 3) * B.m] * t[l + 3];
+  }
+  for (; l < B.rank; ++l) a0 += U[(int64_t)l * B.m] * t[l];
+  static_cast<C*>(A.P)[(int64_t)r * A.pstride + B.poff + i] = ((a0 + a1) + a2) + a3;
+}
+
+// Y = sb B + sa (sum of the partial rows covering each row, in the leaf's list order, the
+// list split over 4 slices added in a fixed order)
+template <typename R>
+__global__ void __launch_bounds__(kLeafRows * kLeafSlices) k_hm_gather(
+    HmOp A, double* __restrict__ Y, int64_t ldy, const double* __restrict__ Bv, int64_t ldb,
+    double sb, double sa, const GmState* st, int mode) {
+  using C = cx<R>;
   const int r = blockIdx.y;
   if (!rhs_on(st, r, mode)) return;
   const int leaf = blockIdx.x;
   const int32_t lo = A.leaf_lo[leaf], rows = A.leaf_lo[leaf + 1] - lo;
   const int row = threadIdx.x % kLeafRows, s = threadIdx.x / kLeafRows;
-  __shared__ cd part[kLeafSlices][kLeafRows];
-  cd acc = {0.0, 0.0};
-  const double* x = X + 2 * (int64_t)r * ldx;
-  const double* T = A.T + 2 * (int64_t)r * A.tstride;
+  __shared__ C part[kLeafSlices][kLeafRows];
+  const C* P = static_cast<const C*>(A.P) + (int64_t)r * A.pstride;
+  C acc = {0, 0};
   if (row < rows) {
-    for (int e = A.leaf_ptr[leaf]; e < A.leaf_ptr[leaf + 1]; ++e) {
+    const int32_t e1 = A.leaf_ptr[leaf + 1];
+    for (int e = A.leaf_ptr[leaf] + s; e < e1; e += kLeafSlices) {
       const int32_t b = A.leaf_ent[e];
+      int64_t q;
       if (b >= 0) {
         const HmDense& B = A.dn[b];
-        const double* D = A.D + 2 * B.off;
-        const int il = lo + row - B.rlo;
-        for (int j = s; j < B.n; j += kLeafSlices)
-          acc += ldc(D, il + (int64_t)j * B.m) * ldc(x, B.clo + j);
+        q = B.poff + (lo + row - B.rlo);
       } else {
         const HmLR& B = A.lr[-b - 1];
-        const double* U = A.U + 2 * B.uoff;
-        const int il = lo + row - B.rlo;
-        for (int l = s; l < B.rank; l += kLeafSlices)
-          acc += ldc(U, il + (int64_t)l * B.m) * ldc(T, B.toff + l);
+        q = B.poff + (lo + row - B.rlo);
       }
+      acc += P[q];
     }
   }
   part[s][row] = acc;
   __syncthreads();
   if (s == 0 && row < rows) {
-    const cd y = ((part[0][row] + part[1][row]) + part[2][row]) + part[3][row];
+    const C y = ((part[0][row] + part[1][row]) + part[2][row]) + part[3][row];
     const int64_t i = lo + row;
-    cd out = sa * y;
+    cd out = sa * cd{(double)y.x, (double)y.y};
     if (Bv) out += sb * ldc(Bv, (int64_t)r * ldb + i);
     stc(Y, (int64_t)r * ldy + i, out);
   }
@@ -353,13 +495,28 @@ void launch_hm_matvec(const Launch& L, const HmOp& A, const double* X, int64_t l
                       int64_t ldy, const double* B, int64_t ldb, double sb, double sa, int32_t nr,
                       const GmState* act, int mode) {
   if (nr <= 0) return;
-  if (A.n_lr > 0) {
-    k_hm_vt<<<dim3((unsigned)A.n_lr, (unsigned)nr), 256, 0, L.stream>>>(A, X, ldx, act, mode);
-    count_launch(1);
-  }
-  k_hm_leaf<<<dim3((unsigned)A.n_leaf, (unsigned)nr), kLeafRows * kLeafSlices, 0, L.stream>>>(
-      A, X, ldx, Y, ldy, B, ldb, sb, sa, act, mode);
-  count_launch(1);
+  const dim3 gv((unsigned)A.n_vt, (unsigned)nr), gb((unsigned)A.n_lb, (unsigned)nr),
+      gd((unsigned)A.n_dense, (unsigned)nr), gl((unsigned)A.n_leaf, (unsigned)nr);
+  constexpr int TL = kLeafRows * kLeafSlices;
+  int launches = 1;
+  auto run = [&](auto tag) {
+    using R = decltype(tag);
+    if (A.n_lr > 0) {
+      k_hm_vt<R><<<gv, 256, 0, L.stream>>>(A, X, ldx, act, mode);
+      k_hm_lblk<R><<<gb, kHmRowChunk, 0, L.stream>>>(A, act, mode);
+      launches += 2;
+    }
+    if (A.n_dense > 0) {
+      k_hm_dblk<R><<<gd, TL, 0, L.stream>>>(A, X, ldx, act, mode);
+      ++launches;
+    }
+    k_hm_gather<R><<<gl, TL, 0, L.stream>>>(A, Y, ldy, B, ldb, sb, sa, act, mode);
+  };
+  if (A.f32)
+    run(float{});
+  else
+    run(double{});
+  count_launch(launches);
 }
 
 __global__ void k_hm_permute(const double* __restrict__ src, int64_t lds, double* __restrict__ dst,
@@ -379,7 +536,6 @@ void launch_hm_permute(const Launch& L, const double* src, int64_t lds, double* 
 }
 
 // ------------------------------------------------------------------ GMRES
-constexpr int kGmChunk = 4096;  // rows per partial sum
 constexpr int kGmT = 256;
 
 namespace {
@@ -394,21 +550,28 @@ __device__ __forceinline__ double* partp(const GmWork& w, int r, int chunk) {
 }
 }  // namespace
 
-// part[r][chunk][l] = sum over the chunk of conj(V_l) w, l = 0..j (warp per l)
+// part[r][chunk][l] = sum over the chunk of conj(V_l) w; one warp per basis vector l
+// (blockIdx.y selects 8 of them), lanes over the chunk's rows
 __global__ void __launch_bounds__(kGmT) k_gm_dot(GmWork w, int32_t j) {
-  const int r = blockIdx.y, chunk = blockIdx.x;
+  const int r = blockIdx.z, chunk = blockIdx.x;
   if (!w.st[r].active) return;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int l = blockIdx.y * (kGmT / 32) + (threadIdx.x >> 5);
+  if (l > j) return;
   const int64_t i0 = (int64_t)chunk * kGmChunk, i1 = min(w.n, i0 + kGmChunk);
   const double* wr = w.w + 2 * (int64_t)r * w.n;
-  double* pp = partp(w, r, chunk);
-  for (int l = wid; l <= j; l += kGmT / 32) {
-    const double* v = vcol(w, r, l);
-    cd s = {0.0, 0.0};
-    for (int64_t i = i0 + lane; i < i1; i += 32) s += conjmul(ldc(v, i), ldc(wr, i));
-    s = warp_sum(s);
-    if (lane == 0) stc(pp, l, s);
+  const double* v = vcol(w, r, l);
+  cd s0 = {0.0, 0.0}, s1 = s0, s2 = s0, s3 = s0;
+  int64_t i = i0 + lane;
+  for (; i + 96 < i1; i += 128) {
+    s0 += conjmul(ldc(v, i), ldc(wr, i));
+    s1 += conjmul(ldc(v, i + 32), ldc(wr, i + 32));
+    s2 += conjmul(ldc(v, i + 64), ldc(wr, i + 64));
+    s3 += conjmul(ldc(v, i + 96), ldc(wr, i + 96));
   }
+  for (; i < i1; i += 32) s0 += conjmul(ldc(v, i), ldc(wr, i));
+  const cd s = warp_sum(((s0 + s1) + s2) + s3);
+  if (lane == 0) stc(partp(w, r, chunk), l, s);
 }
 
 // hc[r][l] = sum over chunks (in order); pass 0 stores H[l, j], pass 1 adds to it
@@ -416,28 +579,53 @@ __global__ void k_gm_dot_finish(GmWork w, int32_t j, int pass) {
   const int r = blockIdx.x;
   if (!w.st[r].active) return;
   for (int l = threadIdx.x; l <= j; l += blockDim.x) {
-    cd s = {0.0, 0.0};
-    for (int c = 0; c < w.chunks; ++c) s += ldc(partp(w, r, c), l);
+    cd s0 = {0.0, 0.0}, s1 = s0;
+    int c = 0;
+    for (; c + 1 < w.chunks; c += 2) {
+      s0 += ldc(partp(w, r, c), l);
+      s1 += ldc(partp(w, r, c + 1), l);
+    }
+    if (c < w.chunks) s0 += ldc(partp(w, r, c), l);
+    const cd s = s0 + s1;
     stc(w.hc, (int64_t)r * (w.restart + 1) + l, s);
     const int64_t h = hidx(w, r, l, j);
     stc(w.H, h, pass == 0 ? s : ldc(w.H, h) + s);
   }
 }
 
-// w -= sum_{l <= j} V_l hc_l
+// w -= sum_{l <= j} V_l hc_l: 64 rows per CTA, the basis vectors split over 4 slices
+// of threads whose partial sums are added in a fixed order
+constexpr int kOrthRows = 64;
+constexpr int kOrthSlices = kGmT / kOrthRows;
+
 __global__ void __launch_bounds__(kGmT) k_gm_orth(GmWork w, int32_t j) {
   const int r = blockIdx.y;
   if (!w.st[r].active) return;
   __shared__ cd h[512];
+  __shared__ cd part[kOrthSlices][kOrthRows];
   const cd* hc = reinterpret_cast<const cd*>(w.hc) + (int64_t)r * (w.restart + 1);
   for (int l = threadIdx.x; l <= j; l += blockDim.x) h[l] = hc[l];
   __syncthreads();
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= w.n) return;
-  double* wr = w.w + 2 * (int64_t)r * w.n;
-  cd s = ldc(wr, i);
-  for (int l = 0; l <= j; ++l) s -= ldc(vcol(w, r, l), i) * h[l];
-  stc(wr, i, s);
+  const int row = threadIdx.x % kOrthRows, sl = threadIdx.x / kOrthRows;
+  const int64_t i = (int64_t)blockIdx.x * kOrthRows + row;
+  cd s0 = {0.0, 0.0}, s1 = s0, s2 = s0, s3 = s0;
+  if (i < w.n) {
+    int l = sl;
+    for (; l + 3 * kOrthSlices <= j; l += 4 * kOrthSlices) {
+      s0 += ldc(vcol(w, r, l), i) * h[l];
+      s1 += ldc(vcol(w, r, l + kOrthSlices), i) * h[l + kOrthSlices];
+      s2 += ldc(vcol(w, r, l + 2 * kOrthSlices), i) * h[l + 2 * kOrthSlices];
+      s3 += ldc(vcol(w, r, l + 3 * kOrthSlices), i) * h[l + 3 * kOrthSlices];
+    }
+    for (; l <= j; l += kOrthSlices) s0 += ldc(vcol(w, r, l), i) * h[l];
+  }
+  part[sl][row] = ((s0 + s1) + s2) + s3;
+  __syncthreads();
+  if (sl == 0 && i < w.n) {
+    double* wr = w.w + 2 * (int64_t)r * w.n;
+    const cd t = ((part[0][row] + part[1][row]) + part[2][row]) + part[3][row];
+    stc(wr, i, ldc(wr, i) - t);
+  }
 }
 
 // part[r][chunk][0].x = sum over the chunk of |w_i|^2 (mode 1: active, 2: not done)
@@ -479,36 +667,52 @@ __global__ void __launch_bounds__(kGmT) k_gm_normalize(GmWork w, int32_t j) {
 
 void launch_gm_arnoldi(const Launch& L, const GmWork& w, int32_t j) {
   const dim3 gc((unsigned)w.chunks, (unsigned)w.nr);
+  const dim3 gd((unsigned)w.chunks, (unsigned)((j + 1 + kGmT / 32 - 1) / (kGmT / 32)),
+                (unsigned)w.nr);
+  const dim3 go((unsigned)((w.n + kOrthRows - 1) / kOrthRows), (unsigned)w.nr);
   const dim3 gv((unsigned)((w.n + kGmT - 1) / kGmT), (unsigned)w.nr);
   for (int pass = 0; pass < 2; ++pass) {
-    k_gm_dot<<<gc, kGmT, 0, L.stream>>>(w, j);
+    k_gm_dot<<<gd, kGmT, 0, L.stream>>>(w, j);
     k_gm_dot_finish<<<(unsigned)w.nr, 128, 0, L.stream>>>(w, j, pass);
-    k_gm_orth<<<gv, kGmT, 0, L.stream>>>(w, j);
+    k_gm_orth<<<go, kGmT, 0, L.stream>>>(w, j);
   }
   k_gm_norm<<<gc, kGmT, 0, L.stream>>>(w, 1);
   k_gm_normalize<<<gv, kGmT, 0, L.stream>>>(w, j);
   count_launch(8);
 }
 
-// Givens rotations of column j, residual estimate, stopping tests; nact = active count.
-__global__ void __launch_bounds__(1024) k_gm_rotate(GmWork w, int32_t j) {
-  int total = 0;
-  for (int base = 0; base < w.nr; base += blockDim.x) {
-    const int r = base + threadIdx.x;
-    bool act = false;
-    if (r < w.nr && w.st[r].active) {
+// Givens rotations of column j, residual estimate, stopping tests (one warp per
+// right-hand side: the column and the rotations are staged in shared memory, lane 0 applies
+// them in order); nact = active right-hand sides afterwards.
+constexpr int kRotWarps = 2;  // 40 KB of static shared memory per CTA
+
+__global__ void __launch_bounds__(kRotWarps * 32) k_gm_rotate(GmWork w, int32_t j, int32_t* cnt) {
+  __shared__ cd col[kRotWarps][512];
+  __shared__ cd ssn[kRotWarps][512];
+  __shared__ double scs[kRotWarps][512];
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  const int r = blockIdx.x * kRotWarps + wq;
+  bool act = false;
+  if (r < w.nr && w.st[r].active) {
+    cd* H = reinterpret_cast<cd*>(w.H);
+    cd* g = reinterpret_cast<cd*>(w.g) + (int64_t)r * (w.restart + 1);
+    double* cs = w.cs + (int64_t)r * w.restart;
+    cd* sn = reinterpret_cast<cd*>(w.sn) + (int64_t)r * w.restart;
+    for (int i = lane; i <= j + 1; i += 32) col[wq][i] = H[hidx(w, r, i, j)];
+    for (int i = lane; i < j; i += 32) {
+      ssn[wq][i] = sn[i];
+      scs[wq][i] = cs[i];
+    }
+    __syncwarp();
+    if (lane == 0) {
       GmState& S = w.st[r];
-      cd* H = reinterpret_cast<cd*>(w.H);
-      cd* g = reinterpret_cast<cd*>(w.g) + (int64_t)r * (w.restart + 1);
-      double* cs = w.cs + (int64_t)r * w.restart;
-      cd* sn = reinterpret_cast<cd*>(w.sn) + (int64_t)r * w.restart;
+      cd* cc = col[wq];
       for (int i = 0; i < j; ++i) {
-        const cd a = H[hidx(w, r, i, j)], b = H[hidx(w, r, i + 1, j)];
-        const cd s = sn[i];
-        H[hidx(w, r, i, j)] = cs[i] * a + s * b;
-        H[hidx(w, r, i + 1, j)] = cs[i] * b - conjmul(s, a);
+        const cd a = cc[i], b = cc[i + 1], s = ssn[wq][i];
+        cc[i] = scs[wq][i] * a + s * b;
+        cc[i + 1] = scs[wq][i] * b - conjmul(s, a);
       }
-      const cd a = H[hidx(w, r, j, j)], b = H[hidx(w, r, j + 1, j)];
+      const cd a = cc[j], b = cc[j + 1];
       const double aa = hypot(a.x, a.y), bb = hypot(b.x, b.y);
       double c;
       cd s, rr;
@@ -525,8 +729,8 @@ __global__ void __launch_bounds__(1024) k_gm_rotate(GmWork w, int32_t j) {
       }
       cs[j] = c;
       sn[j] = s;
-      H[hidx(w, r, j, j)] = rr;
-      H[hidx(w, r, j + 1, j)] = cd{0.0, 0.0};
+      cc[j] = rr;
+      cc[j + 1] = cd{0.0, 0.0};
       const cd gj = g[j];
       g[j + 1] = cd{0.0, 0.0} - conjmul(s, gj);
       g[j] = c * gj;
@@ -545,16 +749,29 @@ __global__ void __launch_bounds__(1024) k_gm_rotate(GmWork w, int32_t j) {
       } else if (j + 1 == w.restart) {
         S.active = 0;
       }
-      act = S.active != 0;
     }
-    total += __syncthreads_count(act);
+    __syncwarp();
+    for (int i = lane; i <= j + 1; i += 32) H[hidx(w, r, i, j)] = col[wq][i];
+    act = w.st[r].active != 0;
   }
-  if (threadIdx.x == 0) *w.nact = total;
+  const int c = __syncthreads_count(act && lane == 0);
+  if (threadIdx.x == 0) cnt[blockIdx.x] = c;
+}
+
+// nact = sum of the per-CTA counts (fixed order)
+__global__ void k_gm_count(GmWork w, const int32_t* cnt, int nb) {
+  if (threadIdx.x != 0) return;
+  int t = 0;
+  for (int b = 0; b < nb; ++b) t += cnt[b];
+  *w.nact = t;
 }
 
 void launch_gm_rotate(const Launch& L, const GmWork& w, int32_t j) {
-  k_gm_rotate<<<1, 1024, 0, L.stream>>>(w, j);
-  count_launch(1);
+  const int nb = (w.nr + kRotWarps - 1) / kRotWarps;
+  int32_t* cnt = w.nact + 1;  // nact is followed by room for one count per CTA
+  k_gm_rotate<<<(unsigned)nb, kRotWarps * 32, 0, L.stream>>>(w, j, cnt);
+  k_gm_count<<<1, 32, 0, L.stream>>>(w, cnt, nb);
+  count_launch(2);
 }
 
 // y = H[0:kdim, 0:kdim]^{-1} g (back substitution, one warp per right-hand side) into hc

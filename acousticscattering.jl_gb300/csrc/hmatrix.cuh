@@ -9,38 +9,55 @@
 namespace bemgpu {
 
 constexpr int kHmMaxRank = 64;  // rank capacity of a compressed block
+constexpr int kGmChunk = 1024;  // rows per GMRES partial sum
 
 // Admissible block: rows [rlo, rlo + m), columns [clo, clo + n) of the permuted order,
 // approximated by U V^T with U (m x rank) and V (n x rank) column-major.
 struct HmLR {
   int32_t rlo, m, clo, n;
   int64_t uoff, voff;  // complex offsets of U (m x kmax) and V (n x kmax) in the pools
-  int64_t toff;        // offset of the block's coefficients V^T x in the product scratch
+  int64_t toff;        // offset of the block's coefficients in the coefficient scratch:
+                       // nvc partial sums of V^T x over column chunks, kmax each
   int32_t kmax;        // rank capacity
   int32_t rank;        // rank reached by the cross approximation
   int32_t conv;        // 1: converged to the tolerance within kmax
-  int32_t pad;
+  int32_t nvc;         // column chunks of the coefficient products
+  int64_t poff;        // offset of the block's m partial rows in the row scratch
+};
+
+// Work items of the compressed-block products: a column chunk of V^T x (c: chunk index)
+// or a row chunk of U t.
+constexpr int kHmColChunk = 256;
+constexpr int kHmRowChunk = 256;
+struct HmItem {
+  int32_t blk, lo, cnt, c;
 };
 
 // Full block (column-major m x n at complex offset off of the dense pool).
 struct HmDense {
   int32_t rlo, m, clo, n;
   int64_t off;
+  int64_t poff;        // offset of the block's m partial rows in the row scratch
 };
 
-// One compressed operator.
+// One compressed operator (U, V and the full blocks complex128, or complex64 when f32).
 struct HmOp {
   const HmLR* lr;
   const HmDense* dn;
-  const double* U;
-  const double* V;
-  const double* D;
+  const void* U;
+  const void* V;
+  const void* D;
   const int32_t* leaf_lo;   // n_leaf + 1 row boundaries
   const int32_t* leaf_ptr;  // n_leaf + 1
   const int32_t* leaf_ent;  // dense block b as b, low-rank block b as -(b + 1)
-  int32_t n_lr, n_dense, n_leaf, pad;
-  double* T;                // product scratch: per right-hand side tstride complex
+  int32_t n_lr, n_dense, n_leaf, f32;
+  const HmItem* vt_items;   // column chunks of every compressed block
+  const HmItem* lb_items;   // row chunks of every compressed block
+  int32_t n_vt, n_lb;
+  double* T;                // coefficient scratch: per right-hand side tstride complex128
   int64_t tstride;
+  void* P;                  // partial-row scratch: per right-hand side pstride complex
+  int64_t pstride;          // (complex64 when f32)
 };
 
 // Batched GMRES state of one right-hand side.
@@ -76,14 +93,15 @@ struct GmWork {
 };
 
 #ifdef __CUDACC__
-// Cross approximation of every admissible block of op (0: M1, 1: M2 of the assembly kind).
-void launch_hm_aca(const Launch& L, HmLR* lr, int32_t n_lr, int32_t max_m, double* U,
-                   double* V, const double* panels, const int32_t* perm, int kind, int op,
-                   double k, double a_re, double a_im, double tol);
+// Cross approximation of every admissible block of op (0: M1, 1: M2 of the assembly
+// kind); f32: FP32 entries (records: FP32 panel records) into complex64 U, V, else FP64.
+void launch_hm_aca(const Launch& L, HmLR* lr, int32_t n_lr, int32_t max_m, void* U, void* V,
+                   const void* recs, bool f32, const int32_t* perm, int kind, int op, double k,
+                   double a_re, double a_im, double tol);
 // Regular-rule entries of the full blocks of both operators (self pairs left to the near
-// kernel, which writes them through AsmInst.near_dst).
-void launch_hm_dense(const Launch& L, const HmDense* dn, int32_t n_dense, double* D1,
-                     double* D2, const double* panels, const int32_t* perm, int kind, double k,
+// kernel, which writes them through AsmInst.near_dst), precision as launch_hm_aca.
+void launch_hm_dense(const Launch& L, const HmDense* dn, int32_t n_dense, void* D1, void* D2,
+                     const void* recs, bool f32, const int32_t* perm, int kind, double k,
                      double a_re, double a_im);
 // Y[:, r] = sb B[:, r] + sa (A X)[:, r] for every right-hand side r < nr with
 // (act == null or act[r].active), the operands in permuted order.
