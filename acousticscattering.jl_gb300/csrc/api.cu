@@ -2746,8 +2746,9 @@ struct HmData {
     for (int o = 0; o < 2; ++o) b += lr[o].bytes + U[o].bytes + V[o].bytes;
     return b;
   }
-  size_t scratch_bytes(int32_t nr) const {  // T and P of a product over nr vectors
-    return (size_t)nr * ((size_t)tstride * 16 + (size_t)pstride * (f32 ? 8 : 16));
+  size_t scratch_bytes(int32_t nr) const {  // T, P (and Xf) of a product over nr vectors
+    return (size_t)nr * ((size_t)tstride * 16 + (size_t)pstride * (f32 ? 8 : 16) +
+                         (f32 ? (size_t)plan.n * 8 : 0));
   }
   // s: scratch_bytes(nr) bytes for products over at most nr vectors
   HmOp op(int o, void* s, int32_t nr) const {
@@ -2773,6 +2774,8 @@ struct HmData {
     A.tstride = tstride;
     A.P = static_cast<char*>(s) + (size_t)nr * tstride * 16;
     A.pstride = pstride;
+    A.Xf = f32 ? static_cast<char*>(A.P) + (size_t)nr * pstride * 8 : nullptr;
+    A.n = plan.n;
     return A;
   }
 };

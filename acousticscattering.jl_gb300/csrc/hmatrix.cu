@@ -58,7 +58,8 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
   return v;
 }
-__device__ __forceinline__ void amax(double& v, int32_t& i, double ov, int32_t oi) {
+template <typename V>
+__device__ __forceinline__ void amax(V& v, int32_t& i, V ov, int32_t oi) {
   if (ov > v || (ov == v && oi < i)) {
     v = ov;
     i = oi;
@@ -104,15 +105,21 @@ template <typename R>
 __device__ __forceinline__ cx<R> to(cd v) {
   return cx<R>{(R)v.x, (R)v.y};
 }
+// element i of a vector held in the operator's precision (complex128 or complex64)
+template <typename R>
+__device__ __forceinline__ cx<R> ldv(const void* p, int64_t i) {
+  return static_cast<const cx<R>*>(p)[i];
+}
 
 constexpr int kAcaT = 256;
 constexpr int kAcaW = kAcaT / 32;
 
 // block-wide argmax (largest value, then smallest index); every thread gets the result
-__device__ __forceinline__ void block_argmax(double& v, int32_t& i, double* rv, int32_t* ri) {
+template <typename V>
+__device__ __forceinline__ void block_argmax(V& v, int32_t& i, V* rv, int32_t* ri) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
-    const double ov = __shfl_xor_sync(0xffffffffu, v, off);
+    const V ov = __shfl_xor_sync(0xffffffffu, v, off);
     const int32_t oi = __shfl_xor_sync(0xffffffffu, i, off);
     amax(v, i, ov, oi);
   }
@@ -147,7 +154,7 @@ __global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, void* 
   const C al = {(R)a_re, (R)a_im};
   const R k = (R)k_;
   extern __shared__ uint32_t used[];  // pivot rows taken, (m + 31) / 32 words
-  __shared__ double rv[kAcaW];
+  __shared__ R rv[kAcaW];
   __shared__ int32_t ri[kAcaW];
   __shared__ C su[kHmMaxRank], sv[kHmMaxRank];    // U[i*, l], V[j*, l]
   __shared__ C cu[kHmMaxRank], cv[kHmMaxRank];    // projections of the new cross
@@ -165,26 +172,26 @@ __global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, void* 
     if (tid == 0) used[istar >> 5] |= 1u << (istar & 31);
     __syncthreads();
     // residual row i*: A[i*, :] - sum_l U[i*, l] V[:, l]
-    double bv = -1.0;
+    R bv = -1;
     int32_t bj = INT32_MAX;
     const int32_t pi = prow[istar];
     for (int j = tid; j < n; j += kAcaT) {
       C v = hm_entry<R, KIND, OP>(recs, pi, pcol[j], k, al);
       for (int l = 0; l < rank; ++l) v -= su[l] * V[j + (int64_t)l * n];
       V[j + (int64_t)rank * n] = v;
-      amax(bv, bj, (double)(v.x * v.x + v.y * v.y), j);
+      amax(bv, bj, v.x * v.x + v.y * v.y, j);
     }
     block_argmax(bv, bj, rv, ri);
-    if (!(bv > 0.0)) {  // the residual row vanishes: continue from the next unused row
-      double fv = -1.0;
+    if (!(bv > 0)) {  // the residual row vanishes: continue from the next unused row
+      R fv = -1;
       int32_t fi = INT32_MAX;
       for (int i = tid; i < m; i += kAcaT)
         if (!((used[i >> 5] >> (i & 31)) & 1u)) {
-          amax(fv, fi, 1.0, i);
+          amax(fv, fi, (R)1, i);
           break;
         }
       block_argmax(fv, fi, rv, ri);
-      if (fv < 0.0) {  // every row was a pivot row: the approximation is exact
+      if (fv < 0) {  // every row was a pivot row: the approximation is exact
         conv = 1;
         break;
       }
@@ -198,14 +205,14 @@ __global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, void* 
     const R pd = s_piv.x * s_piv.x + s_piv.y * s_piv.y;
     const C inv = {s_piv.x / pd, -s_piv.y / pd};
     // residual column j*: A[:, j*] - sum_l U[:, l] V[j*, l]; next pivot row
-    double cb = -1.0;
+    R cb = -1;
     int32_t ci = INT32_MAX;
     const int32_t pj = pcol[jstar];
     for (int i = tid; i < m; i += kAcaT) {
       C u = hm_entry<R, KIND, OP>(recs, prow[i], pj, k, al);
       for (int l = 0; l < rank; ++l) u -= U[i + (int64_t)l * m] * sv[l];
       U[i + (int64_t)rank * m] = u;
-      if (!((used[i >> 5] >> (i & 31)) & 1u)) amax(cb, ci, (double)(u.x * u.x + u.y * u.y), i);
+      if (!((used[i >> 5] >> (i & 31)) & 1u)) amax(cb, ci, u.x * u.x + u.y * u.y, i);
     }
     for (int j = tid; j < n; j += kAcaT) V[j + (int64_t)rank * n] = V[j + (int64_t)rank * n] * inv;
     __syncthreads();
@@ -235,7 +242,7 @@ __global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, void* 
     }
     __syncthreads();
     ++rank;
-    if (s_stop || cb < 0.0) {  // converged, or every row was a pivot row (exact)
+    if (s_stop || cb < 0) {  // converged, or every row was a pivot row (exact)
       conv = 1;
       break;
     }
@@ -339,7 +346,7 @@ __device__ __forceinline__ bool rhs_on(const GmState* st, int r, int mode) {
 // sum over the chunk of V[j, l] x[clo + j]; one warp per l, four independent accumulators
 // per lane (added in a fixed order) to keep several loads in flight.
 template <typename R>
-__global__ void __launch_bounds__(256) k_hm_vt(HmOp A, const double* __restrict__ X, int64_t ldx,
+__global__ void __launch_bounds__(256) k_hm_vt(HmOp A, const void* __restrict__ X, int64_t ldx,
                                                const GmState* st, int mode) {
   using C = cx<R>;
   const int r = blockIdx.y;
@@ -348,7 +355,7 @@ __global__ void __launch_bounds__(256) k_hm_vt(HmOp A, const double* __restrict_
   const HmLR B = A.lr[it.blk];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const C* V = static_cast<const C*>(A.V) + B.voff;
-  const double* x = X + 2 * ((int64_t)r * ldx + B.clo);
+  const C* x = static_cast<const C*>(X) + (int64_t)r * ldx + B.clo;
   double* T = A.T + 2 * ((int64_t)r * A.tstride + B.toff + (int64_t)it.c * B.kmax);
   const int j0 = it.lo, j1 = it.lo + it.cnt;
   for (int l = wid; l < B.rank; l += 8) {
@@ -356,12 +363,12 @@ __global__ void __launch_bounds__(256) k_hm_vt(HmOp A, const double* __restrict_
     C s0 = {0, 0}, s1 = {0, 0}, s2 = {0, 0}, s3 = {0, 0};
     int j = j0 + lane;
     for (; j + 96 < j1; j += 128) {
-      s0 += v[j] * to<R>(ldc(x, j));
-      s1 += v[j + 32] * to<R>(ldc(x, j + 32));
-      s2 += v[j + 64] * to<R>(ldc(x, j + 64));
-      s3 += v[j + 96] * to<R>(ldc(x, j + 96));
+      s0 += v[j] * x[j];
+      s1 += v[j + 32] * x[j + 32];
+      s2 += v[j + 64] * x[j + 64];
+      s3 += v[j + 96] * x[j + 96];
     }
-    for (; j < j1; j += 32) s0 += v[j] * to<R>(ldc(x, j));
+    for (; j < j1; j += 32) s0 += v[j] * x[j];
     C s = cwarp_sum(((s0 + s1) + s2) + s3);
     if (lane == 0) stc(T, l, cd{(double)s.x, (double)s.y});
   }
@@ -374,7 +381,7 @@ constexpr int kLeafSlices = 4;
 // column slices per pass, slices added in a fixed order).
 template <typename R>
 __global__ void __launch_bounds__(kLeafRows * kLeafSlices) k_hm_dblk(
-    HmOp A, const double* __restrict__ X, int64_t ldx, const GmState* st, int mode) {
+    HmOp A, const void* __restrict__ X, int64_t ldx, const GmState* st, int mode) {
   using C = cx<R>;
   const int r = blockIdx.y;
   if (!rhs_on(st, r, mode)) return;
@@ -382,7 +389,7 @@ __global__ void __launch_bounds__(kLeafRows * kLeafSlices) k_hm_dblk(
   const int row = threadIdx.x % kLeafRows, s = threadIdx.x / kLeafRows;
   __shared__ C part[kLeafSlices][kLeafRows];
   const C* D = static_cast<const C*>(A.D) + B.off;
-  const double* x = X + 2 * ((int64_t)r * ldx + B.clo);
+  const C* x = static_cast<const C*>(X) + (int64_t)r * ldx + B.clo;
   C* P = static_cast<C*>(A.P) + (int64_t)r * A.pstride + B.poff;
   if (B.m == kLeafRows && B.n == kLeafRows) {  // leaf x leaf block: all loads in flight
     constexpr int kPer = kLeafRows / kLeafSlices;
@@ -390,7 +397,7 @@ __global__ void __launch_bounds__(kLeafRows * kLeafSlices) k_hm_dblk(
 #pragma unroll
     for (int q = 0; q < kPer; ++q) {
       const int j = s + q * kLeafSlices;
-      v[q] = D[row + (int64_t)j * kLeafRows] * to<R>(ldc(x, j));
+      v[q] = D[row + (int64_t)j * kLeafRows] * x[j];
     }
     C a = v[0];
 #pragma unroll
@@ -406,10 +413,10 @@ __global__ void __launch_bounds__(kLeafRows * kLeafSlices) k_hm_dblk(
     if (i < B.m) {
       int j = s;
       for (; j + kLeafSlices < B.n; j += 2 * kLeafSlices) {
-        a0 += D[i + (int64_t)j * B.m] * to<R>(ldc(x, j));
-        a1 += D[i + (int64_t)(j + kLeafSlices) * B.m] * to<R>(ldc(x, j + kLeafSlices));
+        a0 += D[i + (int64_t)j * B.m] * x[j];
+        a1 += D[i + (int64_t)(j + kLeafSlices) * B.m] * x[j + kLeafSlices];
       }
-      for (; j < B.n; j += kLeafSlices) a0 += D[i + (int64_t)j * B.m] * to<R>(ldc(x, j));
+      for (; j < B.n; j += kLeafSlices) a0 += D[i + (int64_t)j * B.m] * x[j];
     }
     part[s][row] = a0 + a1;
     __syncthreads();
@@ -491,6 +498,15 @@ __global__ void __launch_bounds__(kLeafRows * kLeafSlices) k_hm_gather(
   }
 }
 
+// complex128 -> complex64 copy of the input vectors (one rounding per element)
+__global__ void k_hm_to_f32(const double* __restrict__ X, int64_t ldx, cf* __restrict__ Xf,
+                            int64_t n, const GmState* st, int mode) {
+  const int r = blockIdx.y;
+  if (!rhs_on(st, r, mode)) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) Xf[(int64_t)r * n + i] = to<float>(ldc(X, (int64_t)r * ldx + i));
+}
+
 void launch_hm_matvec(const Launch& L, const HmOp& A, const double* X, int64_t ldx, double* Y,
                       int64_t ldy, const double* B, int64_t ldb, double sb, double sa, int32_t nr,
                       const GmState* act, int mode) {
@@ -499,15 +515,24 @@ void launch_hm_matvec(const Launch& L, const HmOp& A, const double* X, int64_t l
       gd((unsigned)A.n_dense, (unsigned)nr), gl((unsigned)A.n_leaf, (unsigned)nr);
   constexpr int TL = kLeafRows * kLeafSlices;
   int launches = 1;
+  const void* Xr = X;  // the input in the operator's precision
+  int64_t ldr = ldx;
+  if (A.f32) {
+    k_hm_to_f32<<<dim3((unsigned)((A.n + 255) / 256), (unsigned)nr), 256, 0, L.stream>>>(
+        X, ldx, static_cast<cf*>(A.Xf), A.n, act, mode);
+    ++launches;
+    Xr = A.Xf;
+    ldr = A.n;
+  }
   auto run = [&](auto tag) {
     using R = decltype(tag);
     if (A.n_lr > 0) {
-      k_hm_vt<R><<<gv, 256, 0, L.stream>>>(A, X, ldx, act, mode);
+      k_hm_vt<R><<<gv, 256, 0, L.stream>>>(A, Xr, ldr, act, mode);
       k_hm_lblk<R><<<gb, kHmRowChunk, 0, L.stream>>>(A, act, mode);
       launches += 2;
     }
     if (A.n_dense > 0) {
-      k_hm_dblk<R><<<gd, TL, 0, L.stream>>>(A, X, ldx, act, mode);
+      k_hm_dblk<R><<<gd, TL, 0, L.stream>>>(A, Xr, ldr, act, mode);
       ++launches;
     }
     k_hm_gather<R><<<gl, TL, 0, L.stream>>>(A, Y, ldy, B, ldb, sb, sa, act, mode);

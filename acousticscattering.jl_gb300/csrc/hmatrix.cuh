@@ -58,6 +58,8 @@ struct HmOp {
   int64_t tstride;
   void* P;                  // partial-row scratch: per right-hand side pstride complex
   int64_t pstride;          // (complex64 when f32)
+  void* Xf;                 // f32: the input vectors rounded once to complex64 (n x nr)
+  int64_t n;                // order
 };
 
 // Batched GMRES state of one right-hand side.

@@ -690,6 +690,134 @@ def run_reference(args):
     return line
 
 
+NCU_HM_TRAFFIC = 362.57e6 / 360.526e6
+
+
+def run_config5(args):
+    """The reference's default rigid path, compressed operators + GMRES
+    (solve_full_bem(...; compression=(method=:hmatrix, tol=1e-5), gmres_kwargs=(reltol=1e-4,
+    restart=150, maxiter=1200)), full.jl:52-184) on the 20480-panel rigid prolate spheroid
+    0.05 x 0.0125 m at 60 kHz: one bem() call per step (cluster tree cached on the mesh;
+    cross approximation, full blocks, GMRES and far field every step), complex64/FP32
+    operators (precision=:mixed) and complex128 (precision=:double); TS against the dense
+    refined solve of the same incidence; an 81920-panel body as the size the dense path
+    cannot reach in comparable time."""
+    import bemgpu
+    from bemgpu import meshes
+    ctx = bemgpu.Context(0)
+    nodes, tris = meshes.uv_spheroid(0.05, 0.0125, 128, 80)
+    surf = bemgpu.mesh(nodes, tris)
+    k = 2 * math.pi * 60e3 / 1500.0
+    beta, alpha = 1.0, 0.3
+    hm = dict(method="hmatrix", tol=1e-5)
+    gk = dict(reltol=1e-4, restart=150, maxiter=1200)
+
+    def one(prec):
+        sol = bemgpu.bem(surf, bemgpu.Rigid(), k, incidence_angle=beta, incidence_azimuth=alpha,
+                         compression=hm, gmres_kwargs=gk, precision=prec, ctx=ctx)
+        f = bemgpu.scattering_amplitude(sol)
+        st = sol.hmatrix_stats()
+        sol.close()
+        return f, st
+
+    out = {}
+    for prec in ("mixed", "double"):
+        for _ in range(max(args.warmup, 3)):
+            one(prec)
+        steps = args.steps if prec == "mixed" else max(1, min(args.steps, 3))
+        clocks = Clocks(0)
+        clocks.start()
+        ctx.profile(True)
+        ctx.profile_reset()
+        l0 = bemgpu.Context.launch_count()
+        ts = []
+        for _ in range(steps):
+            ctx.timer_start()
+            f, st = one(prec)
+            ts.append(ctx.timer_stop())
+        launches = (bemgpu.Context.launch_count() - l0) // steps
+        prof = {fam: ctx.profile_read(fam)[1] / steps for fam in
+                ("hm_aca", "hm_dense", "near", "hm_matvec", "gmres", "incident", "far_field")}
+        ctx.profile(False)
+        out[prec] = dict(f=f, ms=float(np.mean(ts)), clocks=clocks.stop(), launches=launches,
+                         prof=prof, stats=st)
+    # accurate reference: the dense refined solve of the same incidence
+    ref = bemgpu.bem(surf, bemgpu.Rigid(), k, incidence_angle=beta, incidence_azimuth=alpha,
+                     precision="mixed", refinement=dict(tolerance=1e-12), ctx=ctx)
+    f_ref = bemgpu.scattering_amplitude(ref)
+    ref.close()
+    ctx.timer_start()
+    ref = bemgpu.bem(surf, bemgpu.Rigid(), k, incidence_angle=beta, incidence_azimuth=alpha,
+                     precision="mixed", ctx=ctx)
+    dense_ms = ctx.timer_stop()
+    ref.close()
+    ts_ref = 20 * math.log10(abs(f_ref))
+    # 81920 panels, mixed
+    n2, t2 = meshes.uv_spheroid(0.1, 0.025, 256, 160)
+    big = bemgpu.mesh(n2, t2)
+    bemgpu.bem(big, bemgpu.Rigid(), k, compression=hm, gmres_kwargs=gk, precision="mixed",
+               ctx=ctx).close()
+    ctx.timer_start()
+    sb = bemgpu.bem(big, bemgpu.Rigid(), k, compression=hm, gmres_kwargs=gk, precision="mixed",
+                    ctx=ctx)
+    big_ms = ctx.timer_stop()
+    big_st = sb.hmatrix_stats()
+    sb.close()
+    m = out["mixed"]
+    st = m["stats"]
+    hbm, _, which = measured_peaks()
+    n = int(np.asarray(tris).shape[1])
+    # one product of the system operator: its stored entries (complex64) once, the vector in
+    # and out (complex128)
+    mv_bytes = (st["lowrank_entries"] + st["dense_entries"]) / 2 * 8 + 2 * 16 * n
+    mv_ms = m["prof"]["hm_matvec"]
+    achieved = mv_bytes / (mv_ms * 1e-3) / 1e9 if mv_ms else None
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+        ns, tsm = meshes.uv_spheroid(0.05, 0.0125, 48, 30)
+        t0 = time.perf_counter()
+        rep = O.solve_gmres(ns, tsm, "rigid", k, incidence_angle=beta, incidence_azimuth=alpha,
+                            reltol=1e-4, restart=150, maxiter=1200)
+        dt = time.perf_counter() - t0
+        cpu = {"value": 1.0 / dt, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"the oracle's GMRES path (dense operators, compression=:none) on the "
+                         f"same spheroid meshed with {int(np.asarray(tsm).shape[1])} panels "
+                         f"(a smaller body: the dense CPU path at 20480 panels takes minutes), "
+                         f"{rep['iterations']} iterations, {dt:.2f} s"}
+    line = _base_line(
+        "BEM solves/s, rigid spheroid 20480 panels, compressed operators + GMRES",
+        1e3 / m["ms"], "solves/s", m["ms"], args,
+        {"workload": "rigid prolate spheroid 0.05x0.0125 m, 20480 panels, f=60 kHz, one "
+                     "incidence per solve, compression=(hmatrix, tol 1e-5), GMRES reltol 1e-4 "
+                     "restart 150", "panels": n, "leaf_size": 64, "eta": 3.0},
+        dtype="c64 operators (FP32 entries and products) + fp64 GMRES",
+        e2e={"value": 1e3 / m["ms"], "unit": "solves/s", "h2d_bytes_per_step": 16,
+             "d2h_bytes_per_step": 16,
+             "note": "each step is the public bem() call: angles in, amplitude out"},
+        phase_ms_per_step=m["prof"],
+        compression=st,
+        fp64={"solves_per_s": 1e3 / out["double"]["ms"], "phase_ms_per_step": out["double"]["prof"],
+              "ts_db": 20 * math.log10(abs(out["double"]["f"]))},
+        ts_db=20 * math.log10(abs(m["f"])), ts_dense_refined_db=ts_ref,
+        ts_error_db_vs_dense=abs(20 * math.log10(abs(m["f"])) - ts_ref),
+        ts_error_db_fp64_vs_dense=abs(20 * math.log10(abs(out["double"]["f"])) - ts_ref),
+        dense_mixed_ms=dense_ms,
+        large={"panels": int(np.asarray(t2).shape[1]), "ms": big_ms,
+               "compression": big_st["compression"], "gmres_iterations": big_st["gmres_iterations"],
+               "dense_complex64_bytes": int(np.asarray(t2).shape[1]) ** 2 * 8},
+        roofline={"bound": "hbm", "kernel": "hierarchical product (k_hm_vt, k_hm_lblk, "
+                                            "k_hm_dblk, k_hm_gather)",
+                  "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                  "frac": achieved / hbm if achieved else None, "peak_source": f"{which} HBM",
+                  # ncu DRAM bytes of the four product kernels over the algorithmic bytes,
+                  # same workload (profiles/hmatrix_aca_products_rigid_spheroid_20480_mixed.md)
+                  "traffic": NCU_HM_TRAFFIC * mv_bytes, "algorithmic_bytes_per_launch": mv_bytes},
+        clocks=m["clocks"], gpu_launches=m["launches"], cpu_baseline=cpu)
+    print(json.dumps(line))
+    return line
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -701,9 +829,10 @@ def main():
     ap.add_argument("--nlon", type=int, default=W["nlon"])
     ap.add_argument("--nrings", type=int, default=W["nrings"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3, 4],
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3, 4, 5],
                     help="workload: 1 = headline batched frequency sweep (default); 0 rigid "
-                         "sphere; 2 large single solve x 181 angles; 3 uneven batch; 4 serving")
+                         "sphere; 2 large single solve x 181 angles; 3 uneven batch; 4 serving; "
+                         "5 compressed operators + GMRES (the reference's default rigid path)")
     ap.add_argument("--bodies", type=int, default=256, help="config 3: bodies")
     ap.add_argument("--requests", type=int, default=200, help="config 4: requests")
     ap.add_argument("--rate", type=float, default=0.0, help="config 4: arrivals/s (0: 70%% load)")
@@ -713,7 +842,8 @@ def main():
     elif args.config == 1:
         run_ours(args)
     else:
-        {0: run_config0, 2: run_config2, 3: run_config3, 4: run_config4}[args.config](args)
+        {0: run_config0, 2: run_config2, 3: run_config3, 4: run_config4,
+         5: run_config5}[args.config](args)
 
 
 if __name__ == "__main__":
