@@ -131,17 +131,83 @@ _boundary_code(::PressureRelease) = Int32(1)
 _boundary_code(::FluidFilled) = Int32(2)
 const FORMULATIONS = Dict(:burton_miller => Int32(0), :cbie => Int32(1), :muller => Int32(2))
 
+struct HmatrixOptions
+    tol::Float64
+    eta::Float64
+    leaf_size::Int32
+    restart::Int32
+    reltol::Float64
+    abstol::Float64
+    maxiter::Int32
+    pad::Int32
+end
+
+struct HmatrixStats
+    lowrank_blocks::Int64
+    dense_blocks::Int64
+    densified_blocks::Int64
+    lowrank_entries::Int64
+    dense_entries::Int64
+    max_rank::Int32
+    depth::Int32
+    leaves::Int32
+    pad::Int32
+    compression::Float64
+    gmres_iterations::Int32
+    gmres_converged::Int32
+    build_ms::Float64
+    gmres_ms::Float64
+end
+
 """
     bem(gpu_mesh, boundary, k; incidence_angle=π/2, incidence_azimuth=0, formulation,
-        precision=:double, equilibrate=true, refinement=(;), assembly=:default)
+        precision=:double, equilibrate=true, refinement=(;), assembly=:default,
+        compression=(method=:none,), gmres_kwargs=(;))
 
-The reference's `bem(surface::Mesh, boundary, k; ...)` on the GPU.
+The reference's `bem(surface::Mesh, boundary, k; ...)` on the GPU.  With
+`compression=(method=:hmatrix, tol=1e-5)` a Rigid or PressureRelease body is solved as the
+reference's `solve_full_bem` does by default: compressed operators and GMRES with
+`gmres_kwargs` (reltol, abstol, restart, maxiter); non-convergence warns as there.
 """
 function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
         incidence_azimuth::Real = 0.0, formulation::Union{Nothing, Symbol} = nothing,
         precision::Symbol = :double, equilibrate::Bool = true,
-        refinement::NamedTuple = (;), assembly::Symbol = :default, ctx::Context = context())
+        refinement::NamedTuple = (;), assembly::Symbol = :default,
+        compression::NamedTuple = (method = :none,), gmres_kwargs::NamedTuple = (;),
+        ctx::Context = context())
     isfinite(k) && k > 0 || throw(ArgumentError("k must be finite and positive"))
+    method = get(compression, :method, :none)
+    method in (:none, :hmatrix) ||
+        throw(ArgumentError("compression method must be :none or :hmatrix"))
+    if method === :hmatrix
+        boundary isa FluidFilled && throw(ArgumentError(
+            "hierarchical compression applies to Rigid and PressureRelease boundaries"))
+        p = Problem(_boundary_code(boundary),
+            formulation === nothing ? Int32(-1) : FORMULATIONS[formulation],
+            precision === :mixed ? Int32(1) : Int32(0), Int32(1), Float64(k), 1.0, 1.0,
+            1e-13, Int32(8), Int32(0), 10eps(Float32), 2.0)
+        o = HmatrixOptions(get(compression, :tol, 1e-5), get(compression, :eta, 3.0),
+            Int32(get(compression, :leaf_size, 64)), Int32(get(gmres_kwargs, :restart, 150)),
+            get(gmres_kwargs, :reltol, 1e-4), get(gmres_kwargs, :abstol, 0.0),
+            Int32(get(gmres_kwargs, :maxiter, 1200)), Int32(0))
+        inc = Float64[incidence_angle, incidence_azimuth]
+        r = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:bemgpu_hmatrix_solve, libbemgpu), Cint,
+            (Ptr{Cvoid}, Ptr{Cvoid}, Ref{Problem}, Ref{HmatrixOptions}, Int32, Ptr{Float64},
+                Ptr{Ptr{Cvoid}}),
+            ctx.ptr, m.ptr, p, o, 1, inc, r), ctx.ptr)
+        st = Ref{HmatrixStats}()
+        ccall((:bemgpu_hmatrix_stats_get, libbemgpu), Cint, (Ptr{Cvoid}, Ref{HmatrixStats}),
+            r[], st)
+        st[].gmres_converged == 1 ||
+            @warn "solve_full_bem: GMRES did not converge to the requested tolerance, result may be inaccurate" boundary iters = st[].gmres_iterations
+        d = Ref{Diagnostics}()
+        ccall((:bemgpu_solution_diagnostics, libbemgpu), Cint, (Ptr{Cvoid}, Ref{Diagnostics}),
+            r[], d)
+        data = _GPUBEMData(r[], m.nodes, m.triangles, incidence_angle, incidence_azimuth, d[])
+        return BEMSolution(AcousticScattering._SurfaceGeometry(m.nodes, m.triangles), boundary,
+            Float64(k), :full, data)
+    end
     g, h = boundary isa FluidFilled ?
            (boundary.density_contrast, boundary.soundspeed_contrast) : (1.0, 1.0)
     p = Problem(_boundary_code(boundary),
