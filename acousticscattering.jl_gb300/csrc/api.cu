@@ -68,6 +68,7 @@ struct bemgpu_ctx {
   // launch-shape autotuner: the fastest measured choice per (kernel family, shape class)
   std::map<std::string, int> tuned;
   bool autotune = true;
+
   std::recursive_mutex mu;
   Launch launch() const { return Launch{stream, d_err}; }
 };
@@ -860,51 +861,6 @@ int tune_pick(bemgpu_ctx* c, const std::string& key, const std::vector<int>& can
 
 // Cluster size of the complex64 panel kernel for this batch and panel height, measured
 // on scratch copies of the panels (the kernel factors in place).
-int tuned_getf2_cluster(bemgpu_ctx* c, const std::vector<MatInst>& mi, int64_t k0) {
-  const int ni = (int)mi.size();
-  int64_t mmax = 0;
-  for (const MatInst& m : mi) mmax = std::max<int64_t>(mmax, m.n - k0);
-  if (mmax <= 0) return 0;
-  const std::string key = "getf2/" + std::to_string(ni) + "/" + std::to_string(log2_bucket(mmax));
-  auto it = c->tuned.find(key);
-  if (it != c->tuned.end()) return it->second;
-  if (!c->autotune) return 0;
-  const int64_t lds = (mmax + 31) / 32 * 32;
-  Buf scratch, piv, info, dsm;
-  if (alloc(c, (size_t)ni * lds * kPanelNB * 8, &scratch) != BEMGPU_OK ||
-      alloc(c, (size_t)ni * kPanelNB * 4, &piv) != BEMGPU_OK ||
-      alloc(c, (size_t)ni * 4, &info) != BEMGPU_OK)
-    return 0;  // no room to measure: the batch-size rule
-  std::vector<MatInst> sm(mi.size());
-  for (int t = 0; t < ni; ++t) {
-    MatInst& m = sm[(size_t)t];
-    std::memset(&m, 0, sizeof m);
-    m.a = scratch.as<float2>() + (size_t)t * lds * kPanelNB;
-    m.n = std::max<int64_t>(0, mi[(size_t)t].n - k0);
-    m.lda = lds;
-    m.ipiv = piv.as<int32_t>() + (size_t)t * kPanelNB;
-    m.info = info.as<int32_t>() + t;
-    m.active = m.n > 0 ? 1 : 0;
-  }
-  if (to_device(c, sm, &dsm) != BEMGPU_OK) return 0;
-  auto prepare = [&]() {
-    cudaMemsetAsync(info.p, 0, (size_t)ni * 4, c->stream);
-    for (int t = 0; t < ni; ++t) {
-      if (!sm[(size_t)t].active) continue;
-      const MatInst& m = mi[(size_t)t];
-      const int64_t cols = std::min<int64_t>(kPanelNB, m.n - k0);  // the panel's columns
-      cudaMemcpy2DAsync(sm[(size_t)t].a, (size_t)lds * 8,
-                        static_cast<const float2*>(m.a) + k0 + k0 * m.lda, (size_t)m.lda * 8,
-                        (size_t)sm[(size_t)t].n * 8, (size_t)cols, cudaMemcpyDeviceToDevice,
-                        c->stream);
-    }
-  };
-  const Launch L = c->launch();
-  return tune_pick(c, key, {2, 4, 8},
-                   [&](int cs) { launch_getf2(L, dsm.as<MatInst>(), ni, 0, kPanelNB, 1, cs); },
-                   prepare);
-}
-
 // LAPACK's 1-norm estimate (zlacn2 reverse communication) for every factor of the batch:
 // each round packs the vectors of all instances that ask for the same product into one
 // page-locked buffer, runs one batched triangular solve and reads them back with one copy.
@@ -1212,10 +1168,12 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
     const int64_t st = H / SB;
     const int h = (int)((H % SB) / HB);
     for (int64_t k0 = H; k0 < H + HB && k0 < nmax; k0 += kPanelNB) {
-      const int cs = tuned_getf2_cluster(c, mi, k0);
       {
+        // cluster size by the batch-size rule: timing the candidates (on scratch copies
+        // or in place on successive panels) chose sizes that were slower over a whole
+        // batch (152 vs 139 ms per 64 x 10240 factorisation)
         Prof pr(c, "getf2");
-        launch_getf2(L, dm, ni, k0, kPanelNB, 1, cs);
+        launch_getf2(L, dm, ni, k0, kPanelNB, 1, 0);
       }
       {
         Prof pr(c, "laswp");

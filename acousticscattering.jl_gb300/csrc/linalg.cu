@@ -19,6 +19,8 @@
 #include <cstdio>
 
 #include "bemgpu_internal.h"
+#include <algorithm>
+
 #include "linalg.cuh"
 
 namespace bemgpu {
@@ -362,25 +364,97 @@ __global__ void __launch_bounds__(kGetf2T) k_getf2_ll(const MatInst* __restrict_
 }
 
 // ------------------------------------------------------------------ laswp
-// Interchanges of rows k0 .. k0 + nbe - 1 applied to the columns j in
-// [c_lo, min(c_hi, n)) that lie outside [s_lo, s_hi).
+// Interchanges of rows k0 .. k0 + nbe - 1 (LAPACK's sequential order: row k0 + c with
+// ipiv[k0 + c] for c = 0, 1, ...) applied to the columns j in [c_lo, min(c_hi, n)) that
+// lie outside [s_lo, s_hi).  The sequence is first resolved, once per CTA, into the
+// permutation of the rows it touches (destination row <- source row); then one warp per
+// column loads every moved element (one per lane and slot, all loads in flight), meets at a
+// warp barrier and stores them at their destinations.
+constexpr int kSwpMaxNb = 128;   // interchanges per launch
+constexpr int kSwpWarps = 8;
+constexpr int kSwpCols = 128;    // columns per CTA
+constexpr int kSwpHash = 512;    // open-addressing table of touched rows beyond the block
+
 template <typename R>
-__global__ void k_laswp(const MatInst* __restrict__ insts, int64_t k0, int nb, int64_t c_lo,
-                        int64_t c_hi, int64_t s_lo, int64_t s_hi) {
+__global__ void __launch_bounds__(kSwpWarps * 32) k_laswp(const MatInst* __restrict__ insts,
+                                                         int64_t k0, int nb, int64_t c_lo,
+                                                         int64_t c_hi, int64_t s_lo,
+                                                         int64_t s_hi) {
   const MatInst& M = insts[blockIdx.y];
   const int64_t n = M.n;
   if (!M.active || k0 >= n) return;
   const int nbe = (int)min((int64_t)nb, n - k0);
-  int64_t j = c_lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= s_lo) j += (s_hi - s_lo);
-  if (j >= n || j >= c_hi) return;
+  const int64_t skip = s_hi - s_lo;
+  auto column = [&](int64_t q) {  // compacted column index -> matrix column (or -1)
+    int64_t j = c_lo + q;
+    if (j >= s_lo) j += skip;
+    return (j >= n || j >= c_hi) ? (int64_t)-1 : j;
+  };
+  const int64_t q0 = (int64_t)blockIdx.x * kSwpCols;
+  if (column(q0) < 0) return;  // uniform per CTA
+  __shared__ int32_t piv[kSwpMaxNb];
+  __shared__ int32_t pos[2 * kSwpMaxNb], src[2 * kSwpMaxNb];  // slot: row, its source row
+  __shared__ int32_t hkey[kSwpHash];
+  __shared__ int16_t hslot[kSwpHash];
+  __shared__ int32_t mpos[2 * kSwpMaxNb], msrc[2 * kSwpMaxNb];
+  __shared__ int nmove;
+  const int tid = threadIdx.x;
+  for (int c = tid; c < nbe; c += blockDim.x) piv[c] = M.ipiv[k0 + c];
+  for (int h = tid; h < kSwpHash; h += blockDim.x) hkey[h] = -1;
+  __syncthreads();
+  if (tid == 0) {
+    int ns = nbe;
+    for (int c = 0; c < nbe; ++c) pos[c] = src[c] = (int32_t)(k0 + c);
+    for (int c = 0; c < nbe; ++c) {
+      const int32_t p = piv[c];
+      if (p == (int32_t)(k0 + c)) continue;
+      int sp;
+      if (p < (int32_t)(k0 + nbe)) {
+        sp = p - (int32_t)k0;
+      } else {
+        int h = (int)(((uint32_t)p * 2654435761u) >> 23) & (kSwpHash - 1);
+        while (hkey[h] != -1 && hkey[h] != p) h = (h + 1) & (kSwpHash - 1);
+        if (hkey[h] == -1) {
+          hkey[h] = p;
+          hslot[h] = (int16_t)ns;
+          pos[ns] = src[ns] = p;
+          ++ns;
+        }
+        sp = hslot[h];
+      }
+      const int32_t t = src[c];
+      src[c] = src[sp];
+      src[sp] = t;
+    }
+    int nm = 0;
+    for (int t = 0; t < ns; ++t)
+      if (src[t] != pos[t]) {
+        mpos[nm] = pos[t];
+        msrc[nm] = src[t];
+        ++nm;
+      }
+    nmove = nm;
+  }
+  __syncthreads();
+  const int nm = nmove;
+  if (nm == 0) return;
+  const int lane = tid & 31, wid = tid >> 5;
   const int64_t lda = M.lda;
-  for (int c = 0; c < nbe; ++c) {
-    const int64_t row = k0 + c, p = M.ipiv[row];
-    if (p != row) {
-      cx<R> a = ld<R>(M.a, row + j * lda), b = ld<R>(M.a, p + j * lda);
-      st<R>(M.a, row + j * lda, b);
-      st<R>(M.a, p + j * lda, a);
+  constexpr int kPer = 2 * kSwpMaxNb / 32;
+  for (int q = wid; q < kSwpCols; q += kSwpWarps) {
+    const int64_t j = column(q0 + q);
+    if (j < 0) break;
+    cx<R> v[kPer];
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int t = lane + 32 * u;
+      if (t < nm) v[u] = ld<R>(M.a, msrc[t] + j * lda);
+    }
+    __syncwarp();  // every load of this column is performed before any store
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int t = lane + 32 * u;
+      if (t < nm) st<R>(M.a, mpos[t] + j * lda, v[u]);
     }
   }
 }
@@ -1156,12 +1230,17 @@ void launch_laswp(const Launch& L, const MatInst* d, int ninst, int64_t k0, int 
                   int64_t c_hi, int64_t s_lo, int64_t s_hi, int prec) {
   const int64_t cols = (c_hi - c_lo) - (s_hi - s_lo);
   if (cols <= 0) return;
-  dim3 grid((unsigned)((cols + 255) / 256), (unsigned)ninst);
-  if (prec_is_single(prec))
-    k_laswp<float><<<grid, 256, 0, L.stream>>>(d, k0, nb, c_lo, c_hi, s_lo, s_hi);
-  else
-    k_laswp<double><<<grid, 256, 0, L.stream>>>(d, k0, nb, c_lo, c_hi, s_lo, s_hi);
-  count_launch(1);
+  dim3 grid((unsigned)((cols + kSwpCols - 1) / kSwpCols), (unsigned)ninst);
+  for (int b0 = 0; b0 < nb; b0 += kSwpMaxNb) {  // sequential chunks of interchanges
+    const int nbc = std::min(kSwpMaxNb, nb - b0);
+    if (prec_is_single(prec))
+      k_laswp<float><<<grid, kSwpWarps * 32, 0, L.stream>>>(d, k0 + b0, nbc, c_lo, c_hi, s_lo,
+                                                              s_hi);
+    else
+      k_laswp<double><<<grid, kSwpWarps * 32, 0, L.stream>>>(d, k0 + b0, nbc, c_lo, c_hi, s_lo,
+                                                               s_hi);
+    count_launch(1);
+  }
 }
 
 template <typename R, int NB>

@@ -5,7 +5,8 @@
  * AcousticScattering.jl, the reference's solve and its result queries:
  *
  *   bem(surface::Mesh, boundary, k; ...)         solvers/bem/surface.jl:10-23
- *   solve_full_bem(::Rigid|::PressureRelease)    solvers/bem/full.jl:52-184
+ *   solve_full_bem(::Rigid|::PressureRelease)    solvers/bem/full.jl:52-184 (dense factor,
+ *     or compression=(method=:hmatrix) + GMRES: bemgpu_hmatrix_solve)
  *   solve_full_bem(::FluidFilled)                solvers/bem/full.jl:273-495
  *   MixedRefinement (precision=:mixed)           solvers/bem/fluid_system.jl:172-309
  *   scattering_amplitude / far_field             solvers/bem/postprocessing.jl:1-13,
@@ -424,11 +425,10 @@ int bemgpu_hmatrix_apply(bemgpu_ctx *ctx, const bemgpu_mesh *mesh, const bemgpu_
                          const double *X, double *Y, bemgpu_hmatrix_stats *stats);
 
 /*
- * Launch-shape autotuner (default on): the first time a batch shape is met, the panel
- * factorisation's CTAs per instance and the compact residual's rows per thread are chosen
- * by timing the candidates (on scratch copies where the kernel works in place).  Every
- * candidate computes bit-identical results.  enable = 0 switches it off and forgets the
- * measured choices (fixed rules are used).  No reference counterpart.
+ * Launch-shape autotuner (default on): the first time a batch shape is met, the compact
+ * residual's rows per thread are chosen by timing the candidates.  Every candidate
+ * computes bit-identical results.  enable = 0 switches it off and forgets the measured
+ * choices (fixed rules are used).  No reference counterpart.
  */
 int bemgpu_ctx_set_autotune(bemgpu_ctx *ctx, int32_t enable);
 /*
