@@ -20,6 +20,8 @@
 // parallel dot products), complex Givens rotations, an explicit residual at each restart.
 // Right-hand sides iterate in lock step; one that converges is frozen by its state word,
 // so its iterates do not depend on the others.
+#include <type_traits>
+
 #include "hmatrix.cuh"
 #include "quad_math.cuh"
 #include "quad_regular.cuh"
@@ -342,35 +344,62 @@ __device__ __forceinline__ bool rhs_on(const GmState* st, int r, int mode) {
   return mode == 1 ? st[r].active != 0 : st[r].done == 0;
 }
 
+// Products over RB right-hand sides per CTA (each stored block element is read once for
+// all of them); every right-hand side keeps the same summation order whatever RB is, so
+// results do not depend on how many right-hand sides share a launch.
+__device__ __forceinline__ bool group_on(const GmState* st, int r0, int rb, int nr, int mode) {
+  for (int q = 0; q < rb && r0 + q < nr; ++q)
+    if (rhs_on(st, r0 + q, mode)) return true;
+  return false;
+}
+
 // Coefficients of one column chunk of a compressed block: T[toff + c kmax + l] =
 // sum over the chunk of V[j, l] x[clo + j]; one warp per l, four independent accumulators
-// per lane (added in a fixed order) to keep several loads in flight.
-template <typename R>
+// per lane and right-hand side (added in a fixed order).
+template <typename R, int RB>
 __global__ void __launch_bounds__(256) k_hm_vt(HmOp A, const void* __restrict__ X, int64_t ldx,
-                                               const GmState* st, int mode) {
+                                               int32_t nr, const GmState* st, int mode) {
   using C = cx<R>;
-  const int r = blockIdx.y;
-  if (!rhs_on(st, r, mode)) return;
+  const int r0 = blockIdx.y * RB;
+  if (!group_on(st, r0, RB, nr, mode)) return;
   const HmItem it = A.vt_items[blockIdx.x];
   const HmLR B = A.lr[it.blk];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const C* V = static_cast<const C*>(A.V) + B.voff;
-  const C* x = static_cast<const C*>(X) + (int64_t)r * ldx + B.clo;
-  double* T = A.T + 2 * ((int64_t)r * A.tstride + B.toff + (int64_t)it.c * B.kmax);
+  const C* x[RB];
+#pragma unroll
+  for (int q = 0; q < RB; ++q)
+    x[q] = static_cast<const C*>(X) + (int64_t)min(r0 + q, nr - 1) * ldx + B.clo;
   const int j0 = it.lo, j1 = it.lo + it.cnt;
   for (int l = wid; l < B.rank; l += 8) {
     const C* v = V + (int64_t)l * B.n;
-    C s0 = {0, 0}, s1 = {0, 0}, s2 = {0, 0}, s3 = {0, 0};
+    C s[RB][4];
+#pragma unroll
+    for (int q = 0; q < RB; ++q) s[q][0] = s[q][1] = s[q][2] = s[q][3] = C{0, 0};
     int j = j0 + lane;
     for (; j + 96 < j1; j += 128) {
-      s0 += v[j] * x[j];
-      s1 += v[j + 32] * x[j + 32];
-      s2 += v[j + 64] * x[j + 64];
-      s3 += v[j + 96] * x[j + 96];
+      const C v0 = v[j], v1 = v[j + 32], v2 = v[j + 64], v3 = v[j + 96];
+#pragma unroll
+      for (int q = 0; q < RB; ++q) {
+        s[q][0] += v0 * x[q][j];
+        s[q][1] += v1 * x[q][j + 32];
+        s[q][2] += v2 * x[q][j + 64];
+        s[q][3] += v3 * x[q][j + 96];
+      }
     }
-    for (; j < j1; j += 32) s0 += v[j] * x[j];
-    C s = cwarp_sum(((s0 + s1) + s2) + s3);
-    if (lane == 0) stc(T, l, cd{(double)s.x, (double)s.y});
+    for (; j < j1; j += 32) {
+      const C v0 = v[j];
+#pragma unroll
+      for (int q = 0; q < RB; ++q) s[q][0] += v0 * x[q][j];
+    }
+#pragma unroll
+    for (int q = 0; q < RB; ++q) {
+      const C t = cwarp_sum(((s[q][0] + s[q][1]) + s[q][2]) + s[q][3]);
+      if (lane == 0 && r0 + q < nr) {
+        double* T = A.T + 2 * ((int64_t)(r0 + q) * A.tstride + B.toff + (int64_t)it.c * B.kmax);
+        stc(T, l, cd{(double)t.x, (double)t.y});
+      }
+    }
   }
 }
 
@@ -378,83 +407,114 @@ constexpr int kLeafRows = 64;
 constexpr int kLeafSlices = 4;
 
 // Partial rows of every full block: P[poff + i] = sum_j D[i, j] x[clo + j] (64 rows x 4
-// column slices per pass, slices added in a fixed order).
-template <typename R>
+// column slices per pass, slices added in a fixed order), RB right-hand sides per CTA.
+template <typename R, int RB>
 __global__ void __launch_bounds__(kLeafRows * kLeafSlices) k_hm_dblk(
-    HmOp A, const void* __restrict__ X, int64_t ldx, const GmState* st, int mode) {
+    HmOp A, const void* __restrict__ X, int64_t ldx, int32_t nr, const GmState* st, int mode) {
   using C = cx<R>;
-  const int r = blockIdx.y;
-  if (!rhs_on(st, r, mode)) return;
+  const int r0 = blockIdx.y * RB;
+  if (!group_on(st, r0, RB, nr, mode)) return;
   const HmDense& B = A.dn[blockIdx.x];
   const int row = threadIdx.x % kLeafRows, s = threadIdx.x / kLeafRows;
-  __shared__ C part[kLeafSlices][kLeafRows];
+  __shared__ C part[RB][kLeafSlices][kLeafRows];
   const C* D = static_cast<const C*>(A.D) + B.off;
-  const C* x = static_cast<const C*>(X) + (int64_t)r * ldx + B.clo;
-  C* P = static_cast<C*>(A.P) + (int64_t)r * A.pstride + B.poff;
+  const C* x[RB];
+#pragma unroll
+  for (int q = 0; q < RB; ++q)
+    x[q] = static_cast<const C*>(X) + (int64_t)min(r0 + q, nr - 1) * ldx + B.clo;
+  auto store = [&](int i) {
+#pragma unroll
+    for (int q = 0; q < RB; ++q)
+      if (r0 + q < nr)
+        static_cast<C*>(A.P)[(int64_t)(r0 + q) * A.pstride + B.poff + i] =
+            ((part[q][0][row] + part[q][1][row]) + part[q][2][row]) + part[q][3][row];
+  };
   if (B.m == kLeafRows && B.n == kLeafRows) {  // leaf x leaf block: all loads in flight
     constexpr int kPer = kLeafRows / kLeafSlices;
-    C v[kPer];
+    C d[kPer];
 #pragma unroll
-    for (int q = 0; q < kPer; ++q) {
-      const int j = s + q * kLeafSlices;
-      v[q] = D[row + (int64_t)j * kLeafRows] * x[j];
+    for (int u = 0; u < kPer; ++u) d[u] = D[row + (int64_t)(s + u * kLeafSlices) * kLeafRows];
+#pragma unroll
+    for (int q = 0; q < RB; ++q) {
+      C a = d[0] * x[q][s];
+#pragma unroll
+      for (int u = 1; u < kPer; ++u) a += d[u] * x[q][s + u * kLeafSlices];
+      part[q][s][row] = a;
     }
-    C a = v[0];
-#pragma unroll
-    for (int q = 1; q < kPer; ++q) a += v[q];
-    part[s][row] = a;
     __syncthreads();
-    if (s == 0) P[row] = ((part[0][row] + part[1][row]) + part[2][row]) + part[3][row];
+    if (s == 0) store(row);
     return;
   }
-  for (int r0 = 0; r0 < B.m; r0 += kLeafRows) {
-    const int i = r0 + row;
-    C a0 = {0, 0}, a1 = {0, 0};
-    if (i < B.m) {
-      int j = s;
-      for (; j + kLeafSlices < B.n; j += 2 * kLeafSlices) {
-        a0 += D[i + (int64_t)j * B.m] * x[j];
-        a1 += D[i + (int64_t)(j + kLeafSlices) * B.m] * x[j + kLeafSlices];
+  for (int rr = 0; rr < B.m; rr += kLeafRows) {
+    const int i = rr + row;
+#pragma unroll
+    for (int q = 0; q < RB; ++q) {
+      C a0 = {0, 0}, a1 = {0, 0};
+      if (i < B.m) {
+        int j = s;
+        for (; j + kLeafSlices < B.n; j += 2 * kLeafSlices) {
+          a0 += D[i + (int64_t)j * B.m] * x[q][j];
+          a1 += D[i + (int64_t)(j + kLeafSlices) * B.m] * x[q][j + kLeafSlices];
+        }
+        for (; j < B.n; j += kLeafSlices) a0 += D[i + (int64_t)j * B.m] * x[q][j];
       }
-      for (; j < B.n; j += kLeafSlices) a0 += D[i + (int64_t)j * B.m] * x[j];
+      part[q][s][row] = a0 + a1;
     }
-    part[s][row] = a0 + a1;
     __syncthreads();
-    if (s == 0 && i < B.m) P[i] = ((part[0][row] + part[1][row]) + part[2][row]) + part[3][row];
+    if (s == 0 && i < B.m) store(i);
     __syncthreads();
   }
 }
 
 // Partial rows of one row chunk of a compressed block: P[poff + i] = sum_l U[i, l] t[l],
-// t = the block's coefficient chunks added in order.
-template <typename R>
-__global__ void __launch_bounds__(kHmRowChunk) k_hm_lblk(HmOp A, const GmState* st, int mode) {
+// t = the block's coefficient chunks added in order; RB right-hand sides per CTA.
+template <typename R, int RB>
+__global__ void __launch_bounds__(kHmRowChunk) k_hm_lblk(HmOp A, int32_t nr, const GmState* st,
+                                                        int mode) {
   using C = cx<R>;
-  const int r = blockIdx.y;
-  if (!rhs_on(st, r, mode)) return;
+  const int r0 = blockIdx.y * RB;
+  if (!group_on(st, r0, RB, nr, mode)) return;
   const HmItem it = A.lb_items[blockIdx.x];
   const HmLR B = A.lr[it.blk];
-  __shared__ C t[kHmMaxRank];
-  const double* T = A.T + 2 * ((int64_t)r * A.tstride + B.toff);
+  __shared__ C t[RB][kHmMaxRank];
   if (threadIdx.x < B.rank) {
-    cd v = ldc(T, threadIdx.x);
-    for (int c = 1; c < B.nvc; ++c) v += ldc(T, (int64_t)c * B.kmax + threadIdx.x);
-    t[threadIdx.x] = to<R>(v);
+#pragma unroll
+    for (int q = 0; q < RB; ++q) {
+      const double* T = A.T + 2 * ((int64_t)min(r0 + q, nr - 1) * A.tstride + B.toff);
+      cd v = ldc(T, threadIdx.x);
+      for (int c = 1; c < B.nvc; ++c) v += ldc(T, (int64_t)c * B.kmax + threadIdx.x);
+      t[q][threadIdx.x] = to<R>(v);
+    }
   }
   __syncthreads();
   const int i = it.lo + threadIdx.x;
   if (threadIdx.x >= it.cnt) return;
   const C* U = static_cast<const C*>(A.U) + B.uoff + i;
-  C a0 = {0, 0}, a1 = {0, 0}, a2 = {0, 0}, a3 = {0, 0};
+  C a[RB][4];
+#pragma unroll
+  for (int q = 0; q < RB; ++q) a[q][0] = a[q][1] = a[q][2] = a[q][3] = C{0, 0};
   int l = 0;
   for (; l + 3 < B.rank; l += 4) {
-    a0 += U[(int64_t)l * B.m] * t[l];
-    a1 += U[(int64_t)(l + 1) * B.m] * t[l + 1];
-    a2 += U[(int64_t)(l + 2) * B.m] * t[l + 2];
-    a3 += U[(int64_t)(l + 3) * B.m] * t[l + 3];
+    const C u0 = U[(int64_t)l * B.m], u1 = U[(int64_t)(l + 1) * B.m],
+            u2 = U[(int64_t)(l + 2) * B.m], u3 = U[(int64_t)(l + 3) * B.m];
+#pragma unroll
+    for (int q = 0; q < RB; ++q) {
+      a[q][0] += u0 * t[q][l];
+      a[q][1] += u1 * t[q][l + 1];
+      a[q][2] += u2 * t[q][l + 2];
+      a[q][3] += u3 * t[q][l + 3];
+    }
   }
-  for (; l < B.rank; ++l) a0 += U[(int64_t)l * B.m] * t[l];
-  static_cast<C*>(A.P)[(int64_t)r * A.pstride + B.poff + i] = ((a0 + a1) + a2) + a3;
+  for (; l < B.rank; ++l) {
+    const C u0 = U[(int64_t)l * B.m];
+#pragma unroll
+    for (int q = 0; q < RB; ++q) a[q][0] += u0 * t[q][l];
+  }
+#pragma unroll
+  for (int q = 0; q < RB; ++q)
+    if (r0 + q < nr)
+      static_cast<C*>(A.P)[(int64_t)(r0 + q) * A.pstride + B.poff + i] =
+          ((a[q][0] + a[q][1]) + a[q][2]) + a[q][3];
 }
 
 // Y = sb B + sa (sum of the partial rows covering each row, in the leaf's list order, the
@@ -511,8 +571,11 @@ void launch_hm_matvec(const Launch& L, const HmOp& A, const double* X, int64_t l
                       int64_t ldy, const double* B, int64_t ldb, double sb, double sa, int32_t nr,
                       const GmState* act, int mode) {
   if (nr <= 0) return;
-  const dim3 gv((unsigned)A.n_vt, (unsigned)nr), gb((unsigned)A.n_lb, (unsigned)nr),
-      gd((unsigned)A.n_dense, (unsigned)nr), gl((unsigned)A.n_leaf, (unsigned)nr);
+  constexpr int kRB = 4;  // right-hand sides per CTA of the block products
+  const int rb = nr >= kRB ? kRB : 1;
+  const unsigned ng = (unsigned)((nr + rb - 1) / rb);
+  const dim3 gv((unsigned)A.n_vt, ng), gb((unsigned)A.n_lb, ng), gd((unsigned)A.n_dense, ng),
+      gl((unsigned)A.n_leaf, (unsigned)nr);
   constexpr int TL = kLeafRows * kLeafSlices;
   int launches = 1;
   const void* Xr = X;  // the input in the operator's precision
@@ -524,17 +587,25 @@ void launch_hm_matvec(const Launch& L, const HmOp& A, const double* X, int64_t l
     Xr = A.Xf;
     ldr = A.n;
   }
-  auto run = [&](auto tag) {
+  auto blocks = [&](auto tag, auto rbt) {
     using R = decltype(tag);
+    constexpr int RB = decltype(rbt)::value;
     if (A.n_lr > 0) {
-      k_hm_vt<R><<<gv, 256, 0, L.stream>>>(A, Xr, ldr, act, mode);
-      k_hm_lblk<R><<<gb, kHmRowChunk, 0, L.stream>>>(A, act, mode);
+      k_hm_vt<R, RB><<<gv, 256, 0, L.stream>>>(A, Xr, ldr, nr, act, mode);
+      k_hm_lblk<R, RB><<<gb, kHmRowChunk, 0, L.stream>>>(A, nr, act, mode);
       launches += 2;
     }
     if (A.n_dense > 0) {
-      k_hm_dblk<R><<<gd, TL, 0, L.stream>>>(A, Xr, ldr, act, mode);
+      k_hm_dblk<R, RB><<<gd, TL, 0, L.stream>>>(A, Xr, ldr, nr, act, mode);
       ++launches;
     }
+  };
+  auto run = [&](auto tag) {
+    using R = decltype(tag);
+    if (rb == kRB)
+      blocks(tag, std::integral_constant<int, kRB>{});
+    else
+      blocks(tag, std::integral_constant<int, 1>{});
     k_hm_gather<R><<<gl, TL, 0, L.stream>>>(A, Y, ldy, B, ldb, sb, sa, act, mode);
   };
   if (A.f32)

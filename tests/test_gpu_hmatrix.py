@@ -120,17 +120,19 @@ def test_gmres_stops_at_maxiter_and_warns(ctx, sphere):
     sol.close()
 
 
-def test_batched_right_hand_sides_equal_single_solves(ctx, sphere):
-    """Right-hand sides iterate in lock step but independently: a sweep returns exactly the
-    amplitudes of separate solves."""
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_batched_right_hand_sides_equal_single_solves(ctx, sphere, precision):
+    """Right-hand sides iterate in lock step but independently, and the block products
+    keep each one's summation order: a sweep returns exactly the amplitudes of separate
+    solves."""
     nodes, tris, surf, P = sphere
-    angles = [0.3, 1.2, 2.5]
+    angles = [0.3, 1.2, 2.5, 0.7, 1.9]  # a group of 4 products per CTA plus a tail
     sw = bemgpu.incidence_angle_sweep(surf, bemgpu.Rigid(), K0, angles, compression=HM,
-                                      ctx=ctx)
+                                      precision=precision, ctx=ctx)
     single = []
     for a in angles:
         sol = bemgpu.bem(surf, bemgpu.Rigid(), K0, incidence_angle=a, incidence_azimuth=0.0,
-                         compression=HM, ctx=ctx)
+                         compression=HM, precision=precision, ctx=ctx)
         single.append(bemgpu.scattering_amplitude(sol))
         sol.close()
     assert np.array_equal(sw.amplitudes, np.array(single))
@@ -183,3 +185,26 @@ def test_mixed_precision_operators(ctx, spheroid, boundary):
     assert d["converged"] and d["factor_precision"] == "single"
     assert abs(bemgpu.target_strength(sol) - O.target_strength(ref["amplitudes"][0])) <= 0.01
     sol.close()
+
+
+def test_queries_of_a_compressed_solution(ctx, sphere):
+    """pressure() and far fields at many directions of a compressed-operator solution
+    equal the dense solution's (tight tolerances)."""
+    nodes, tris, surf, P = sphere
+    kw = dict(incidence_angle=0.8, incidence_azimuth=0.4)
+    dense = bemgpu.bem(surf, bemgpu.Rigid(), K0, ctx=ctx, **kw)
+    comp = bemgpu.bem(surf, bemgpu.Rigid(), K0, compression=dict(HM, tol=1e-11),
+                      gmres_kwargs=dict(reltol=1e-11), ctx=ctx, **kw)
+    rng = np.random.default_rng(9)
+    pts = rng.standard_normal((20, 3))
+    pts *= (0.015 + 0.02 * rng.random(20))[:, None] / np.linalg.norm(pts, axis=1)[:, None]
+    for field in ("total", "scattered"):
+        a = dense.pressure(pts, field=field)
+        b = comp.pressure(pts, field=field)
+        assert np.linalg.norm(a - b) <= 1e-8 * np.linalg.norm(a)
+    dirs = rng.standard_normal((7, 3))
+    dirs /= np.linalg.norm(dirs, axis=1)[:, None]
+    fa, fb = dense.far_field(dirs), comp.far_field(dirs)
+    assert np.linalg.norm(fa - fb) <= 1e-8 * np.linalg.norm(fa)
+    dense.close()
+    comp.close()
