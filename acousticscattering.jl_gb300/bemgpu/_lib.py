@@ -139,6 +139,7 @@ SIGNATURES = {
     "bemgpu_ctx_set_autotune": (ctypes.c_int, [_vp, _i32]),
     "bemgpu_solution_diagnostics": (ctypes.c_int, [_vp, ctypes.POINTER(Diagnostics)]),
     "bemgpu_pressure": (ctypes.c_int, [_vp, _i32, _i64, _dp, _i32, _dp]),
+    "bemgpu_pressure_region": (ctypes.c_int, [_vp, _i32, _i64, _dp, _i32, _i32, _dp]),
     "bemgpu_solution_destroy": (ctypes.c_int, [_vp]),
     "bemgpu_dense_solve": (ctypes.c_int, [_vp, _i64, _dp, _i32, _dp, _i32, _i32,
                                           ctypes.c_double, _i32, ctypes.c_double,

@@ -450,14 +450,19 @@ class BEMSolution:
     def dpdn_scat(self):
         return self.traces(0)[1]
 
-    def pressure(self, points, field: str = "total", rhs: int = 0) -> np.ndarray:
+    def pressure(self, points, field: str = "total", rhs: int = 0, region=None) -> np.ndarray:
+        """Field at points; region (coupled-region solutions only, fields/pressure.jl:42-53):
+        None = each point's own region, else 0 (unbounded) or an interface index."""
         if field not in C.FIELDS:
             raise ArgumentError("field must be :total, :scattered, :incident or :interior")
+        if region is not None and not (isinstance(region, (int, np.integer)) and region >= 0):
+            raise ArgumentError("region must be zero or an interface index")
         pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
         out = np.zeros(pts.shape[0], dtype=np.complex128)
         if pts.shape[0]:
-            _check(C.lib().bemgpu_pressure(self.handle, rhs, pts.shape[0], C.dptr(pts),
-                                           C.FIELDS[field], C.dptr(out)), self.ctx.handle)
+            _check(C.lib().bemgpu_pressure_region(
+                self.handle, rhs, pts.shape[0], C.dptr(pts), C.FIELDS[field],
+                -1 if region is None else int(region), C.dptr(out)), self.ctx.handle)
         return out
 
     def hmatrix_stats(self) -> dict:
@@ -739,12 +744,14 @@ def diagnostics(sol) -> dict:
     return sol.diagnostics()
 
 
-def pressure(sol: BEMSolution, points, *, field: str = "total", rhs: int = 0):
+def pressure(sol: BEMSolution, points, *, field: str = "total", rhs: int = 0, region=None):
     """Pressure at points (fields/pressure.jl:42-53, full-BEM branch :404-471).
 
     ``points``: one point (3 numbers) -> complex; a sequence of points or a 3 x N / N x 3
     array -> complex array.  field: "total" (incident + scattered outside, interior field
-    inside a fluid body), "scattered", "incident" or "interior"."""
+    inside a fluid body), "scattered", "incident" or "interior".  region (coupled-region
+    solutions, fields/regions.jl:1-65): None = each point's own region, else 0 (the
+    unbounded region) or an interface index whose interior the point belongs to."""
     arr = np.asarray(points, dtype=np.float64)
     if arr.size == 0:
         return np.zeros(0, dtype=np.complex128)
@@ -755,7 +762,7 @@ def pressure(sol: BEMSolution, points, *, field: str = "total", rhs: int = 0):
         arr = arr.T
     if not np.all(np.isfinite(arr)):
         raise ArgumentError("point coordinates must be finite")
-    out = sol.pressure(arr.reshape(-1, 3), field=field, rhs=rhs)
+    out = sol.pressure(arr.reshape(-1, 3), field=field, rhs=rhs, region=region)
     return complex(out[0]) if single else out
 
 

@@ -534,6 +534,8 @@ struct SolutionData {
   Buf xsol;                  // coupled regions: the solved unknowns [p; v], 2n x nrhs
   bool region = false;
   bemgpu_diagnostics diag{};
+  std::vector<int32_t> parents;         // coupled regions: parent region of each surface,
+  std::vector<double> region_k, region_rho;  // wavenumber and density of every region
   bool hmatrix = false;                 // from bemgpu_hmatrix_solve
   bemgpu_hmatrix_stats hm{};
   std::vector<double> gm_hist;          // residual estimates, gm_stride per rhs
@@ -3443,6 +3445,9 @@ int bemgpu_region_solve(bemgpu_ctx* c, int32_t count, const bemgpu_mesh* const* 
   std::vector<int32_t> nr{nrhs};
   std::vector<const double*> inc{incidence};
   TRY(solve_batch(c, fs, nr, inc, outs));
+  sd->parents.assign(parents, parents + count);
+  sd->region_k.assign(tab.kr, tab.kr + count + 1);
+  sd->region_rho = rho;
   *solution = new bemgpu_solution{sd};
   return BEMGPU_OK;
 }
@@ -3478,6 +3483,11 @@ int bemgpu_solution_destroy(bemgpu_solution* sol) {
 
 int bemgpu_pressure(bemgpu_solution* sol, int32_t rhs, int64_t npts, const double* points,
                     int32_t field, double* out) {
+  return bemgpu_pressure_region(sol, rhs, npts, points, field, -1, out);
+}
+
+int bemgpu_pressure_region(bemgpu_solution* sol, int32_t rhs, int64_t npts, const double* points,
+                           int32_t field, int32_t region, double* out) {
   if (!sol) return fail(nullptr, BEMGPU_EINVAL, "null solution");
   SolutionData* s = sol->d.get();
   bemgpu_ctx* c = s->c;
@@ -3486,14 +3496,16 @@ int bemgpu_pressure(bemgpu_solution* sol, int32_t rhs, int64_t npts, const doubl
   if (rhs < 0 || rhs >= s->nrhs) return fail(c, BEMGPU_EINVAL, "rhs index out of range");
   if (field < BEMGPU_FIELD_TOTAL || field > BEMGPU_FIELD_INTERIOR)
     return fail(c, BEMGPU_EINVAL, "field must be :total, :scattered, :incident or :interior");
-  if (s->region)
-    return fail(c, BEMGPU_EINVAL, "pressure of a coupled-region solution is not supported");
+  if (region >= 0 && !s->region)
+    return fail(c, BEMGPU_EINVAL, "region selection requires a coupled fluid BEM solution");
+  if (s->region && region > (int32_t)s->parents.size())
+    return fail(c, BEMGPU_EINVAL, "region must be zero or an interface index");
   if (npts < 0 || (npts > 0 && (!points || !out)))
     return fail(c, BEMGPU_EINVAL, "invalid points");
   if (npts == 0) return BEMGPU_OK;
   for (int64_t i = 0; i < 3 * npts; ++i)
     if (!std::isfinite(points[i])) return fail(c, BEMGPU_EINVAL, "point coordinates must be finite");
-  const bool fluid = s->boundary == BEMGPU_FLUID;
+  const bool fluid = s->boundary == BEMGPU_FLUID || s->region;
   if (field == BEMGPU_FIELD_INTERIOR && !fluid)
     return fail(c, BEMGPU_EINVAL, "interior field requires a fluid-filled body");
   std::vector<double> pts(points, points + 3 * npts);
@@ -3520,6 +3532,18 @@ int bemgpu_pressure(bemgpu_solution* sol, int32_t rhs, int64_t npts, const doubl
   P.eta = s->mesh->eta;
   P.field = field;
   P.fluid = fluid ? 1 : 0;
+  if (s->region) {  // coupled regions: the union's surfaces and the solved unknowns
+    const int32_t count = (int32_t)s->parents.size();
+    P.nsurf = count;
+    P.requested = region;
+    P.xr = s->xsol.as<double>() + 4 * (size_t)s->mesh->n * rhs;
+    for (int32_t i = 0; i <= count; ++i) {
+      P.offsets[i] = s->mesh->offsets[(size_t)i];
+      P.kr[i] = s->region_k[(size_t)i];
+      P.rho[i] = s->region_rho[(size_t)i];
+    }
+    for (int32_t i = 0; i < count; ++i) P.parents[i] = s->parents[(size_t)i];
+  }
   {
     Prof pr(c, "pressure");
     launch_pressure(c->launch(), P);
@@ -3528,6 +3552,20 @@ int bemgpu_pressure(bemgpu_solution* sol, int32_t rhs, int64_t npts, const doubl
   std::vector<int32_t> reg;
   CUDA_TRY(c, cudaMemcpyAsync(out, dout.p, (size_t)npts * 16, cudaMemcpyDeviceToHost, c->stream));
   TRY(download(c, dreg, &reg, (size_t)npts));
+  if (s->region) {  // the reference's errors (fields/regions.jl:17-26)
+    for (int64_t i = 0; i < npts; ++i)
+      switch (-reg[(size_t)i]) {
+        case kPrBadRegion:
+          return fail(c, BEMGPU_EINVAL, "the point does not belong to the selected region");
+        case kPrNeedExterior:
+          return fail(c, BEMGPU_EINVAL,
+                      "field=:scattered requires the unbounded exterior region");
+        case kPrNeedFluid:
+          return fail(c, BEMGPU_EINVAL, "field=:interior requires a bounded fluid region");
+        default: break;
+      }
+    return BEMGPU_OK;
+  }
   for (int64_t i = 0; i < npts; ++i)
     if (std::isnan(out[2 * i]) && field != BEMGPU_FIELD_INCIDENT) {
       if (field == BEMGPU_FIELD_INTERIOR)

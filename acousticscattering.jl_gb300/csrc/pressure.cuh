@@ -19,10 +19,24 @@ struct PressureInst {
   double k, k_int, g, eta;
   int32_t field;         // bemgpu_field
   int32_t fluid;         // interior field exists
+  // coupled regions (nsurf > 0; p, q, k_int, g, fluid unused): surface s encloses region
+  // s + 1 and borders region parents[s]; xr holds the solved [p; v] (complex128, 2n)
+  int32_t nsurf;
+  int32_t requested;                 // region asked for, -1: the point's own
+  const double* xr;
+  int64_t offsets[kMaxRegions + 1];  // first panel of every surface, then n
+  int32_t parents[kMaxRegions];
+  double kr[kMaxRegions + 1];        // wavenumber of every region
+  double rho[kMaxRegions + 1];       // density contrast of every region (region 0: 1)
 };
 
+// Region pressure status per point (PressureInst.region in region mode, as -code):
+constexpr int kPrBadRegion = 1;      // the point does not belong to the requested region
+constexpr int kPrNeedExterior = 2;   // field scattered outside the unbounded region
+constexpr int kPrNeedFluid = 3;      // field interior in the unbounded region
+
 #ifdef __CUDACC__
-void launch_pressure(const Launch& L, const PressureInst& P);
+void launch_pressure(const Launch& L, const PressureInst& P);  // either mode
 #endif
 
 }  // namespace bemgpu

@@ -12,7 +12,7 @@
 module BEMGPU
 
 using LinearAlgebra
-import AcousticScattering: bem, scattering_amplitude, target_strength, diagnostics,
+import AcousticScattering: bem, scattering_amplitude, target_strength, diagnostics, pressure,
     BEMSolution, Rigid, PressureRelease, FluidFilled
 
 const libbemgpu = joinpath(@__DIR__, "..", "bemgpu", "libbemgpu.so")
@@ -283,6 +283,33 @@ function scattering_amplitude(sol::BEMSolution{_GPUBEMData};
             sol.data.solution, 0, 1, d, out))
     end
     return complex(out[1], out[2])
+end
+
+const FIELDS = Dict(:total => Int32(0), :scattered => Int32(1), :incident => Int32(2),
+    :interior => Int32(3))
+
+"""
+    pressure(sol::BEMSolution{_GPUBEMData}, points; field=:total, region=nothing)
+
+The reference's `pressure(solution, points; field, region)` (fields/pressure.jl:42-53;
+coupled regions fields/regions.jl:1-65): one point (3 numbers) gives a complex value, a
+vector of points a vector.
+"""
+function pressure(sol::BEMSolution{_GPUBEMData}, points; field::Symbol = :total,
+        region::Union{Nothing, Integer} = nothing)
+    haskey(FIELDS, field) ||
+        throw(ArgumentError("field must be :total, :scattered, :incident or :interior"))
+    single = points isa AbstractVector{<:Real}
+    pts = single ? [points] : collect(points)
+    flat = Float64[c for p in pts for c in p]
+    length(flat) == 3 * length(pts) || throw(ArgumentError("a point has three coordinates"))
+    out = zeros(Float64, 2 * length(pts))
+    check(ccall((:bemgpu_pressure_region, libbemgpu), Cint,
+        (Ptr{Cvoid}, Int32, Int64, Ptr{Float64}, Int32, Int32, Ptr{Float64}),
+        sol.data.solution, 0, length(pts), flat, FIELDS[field],
+        region === nothing ? Int32(-1) : Int32(region), out))
+    values = [complex(out[2i - 1], out[2i]) for i in 1:length(pts)]
+    return single ? values[1] : values
 end
 
 target_strength(sol::BEMSolution{_GPUBEMData}; kwargs...) =

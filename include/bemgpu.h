@@ -348,6 +348,17 @@ int bemgpu_solution_diagnostics(const bemgpu_solution *sol, bemgpu_diagnostics *
  */
 int bemgpu_pressure(bemgpu_solution *sol, int32_t rhs, int64_t npts, const double *points,
                     int32_t field, double *out);
+/*
+ * pressure(sol, points; field, region) of a coupled-region solution
+ * (fields/regions.jl:30-65): region = -1 evaluates each point in the region that contains
+ * it (on an interface: the outer region, or the inner one for the interior field);
+ * region >= 0 selects a region the point belongs to.  The total field in the unbounded
+ * region adds the incident wave; field=:scattered needs the unbounded region and
+ * field=:interior a bounded one (BEMGPU_EINVAL otherwise, as the reference's ArgumentError).
+ * bemgpu_pressure on a coupled-region solution is this call with region = -1.
+ */
+int bemgpu_pressure_region(bemgpu_solution *sol, int32_t rhs, int64_t npts,
+                           const double *points, int32_t field, int32_t region, double *out);
 int bemgpu_solution_destroy(bemgpu_solution *sol);
 
 /* ------------------------------------------------------------------ serving */

@@ -248,6 +248,77 @@ def solve_regions(surfaces, materials, parents, k, incidence_angle=math.pi / 2,
     return dict(A=A, b=b, x=x, amplitude=amp, p_scat=ps, dpdn_scat=qs, panels=P, offsets=offs)
 
 
+def pressure_regions(surfaces, materials, parents, k, points, x, direction, field="total",
+                     region=None, eta=NEAR_ETA):
+    """Pressure of a coupled-region solution (fields/regions.jl:1-65): each point's region by
+    the walk over the interfaces (an interface is tested when its parent is the region
+    found so far: inside, on, or outside by its solid angle), then the interfaces bordering
+    that region contribute S dp - D p (region inside them) or D p - S dp (outside), with the
+    region's wavenumber, p the solved pressure and dp = density * v of the region's side;
+    in the unbounded region the traces are the scattered ones and the total field adds
+    the incident wave.  x = the solved [p; v] over the surfaces in order."""
+    L = lib()
+    count = len(surfaces)
+    dens = [1.0] + [float(m[0]) for m in materials]
+    speeds = [1.0] + [float(m[1]) for m in materials]
+    Ps = [Panels(nd, tr) for nd, tr in surfaces]
+    offs = np.cumsum([0] + [P_.n for P_ in Ps])
+    n = int(offs[-1])
+    d = np.asarray(direction, dtype=np.float64)
+    out = []
+    for xp in np.atleast_2d(np.asarray(points, dtype=np.float64)):
+        xp = np.ascontiguousarray(xp)
+        containing, adjacent = 0, None
+        for i in range(1, count + 1):
+            if parents[i - 1] != containing:
+                continue
+            om = L.oracle_solid_angle(Ps[i - 1].ptr, Ps[i - 1].n, _dp(xp))
+            if abs(om - 2 * math.pi) < 1e-6 * 4 * math.pi:
+                adjacent = (parents[i - 1], i)
+                break
+            if om > 2 * math.pi:
+                containing = i
+        if region is not None:
+            ok = region == containing if adjacent is None else region in adjacent
+            if not ok:
+                raise ValueError("the point does not belong to the selected region")
+            reg = region
+        elif adjacent is not None:
+            reg = adjacent[1] if field == "interior" else adjacent[0]
+        else:
+            reg = containing
+        if field == "scattered" and reg != 0:
+            raise ValueError("field=:scattered requires the unbounded exterior region")
+        if field == "interior" and reg == 0:
+            raise ValueError("field=:interior requires a bounded fluid region")
+        inc = np.exp(1j * k * d @ xp)
+        if field == "incident":
+            out.append(inc)
+            continue
+        kr = k / speeds[reg]
+        val = 0.0 + 0.0j
+        for i in range(1, count + 1):
+            inside = i == reg
+            if not (inside or parents[i - 1] == reg):
+                continue
+            sl = slice(offs[i - 1], offs[i])
+            p = np.array(x[sl], dtype=np.complex128)
+            dp = (dens[i] if inside else dens[parents[i - 1]]) * np.array(x[n + offs[i - 1]:n + offs[i]])
+            if reg == 0:
+                pinc, qinc = incident(Ps[i - 1], k, d)
+                p, dp = p - pinc, dp - qinc
+            p, dp = np.ascontiguousarray(p), np.ascontiguousarray(dp)
+            r = np.zeros(2)
+            # oracle_layer_potentials: interior flag 1 -> S dp - D p, 0 -> D p - S dp
+            L.oracle_layer_potentials(Ps[i - 1].ptr, Ps[i - 1].n, kr, _dp(xp), eta, _dp(p),
+                                      _dp(dp), 1 if inside else 0, _dp(r))
+            val += complex(r[0], r[1])
+        if field == "total" and reg == 0:
+            val += inc
+        out.append(val)
+    return np.array(out)
+
+
 def incident(P: Panels, k, direction):
     d = np.ascontiguousarray(direction, dtype=np.float64)
     p = np.zeros(P.n, dtype=np.complex128)

@@ -81,3 +81,38 @@ def test_parents_must_match_containment(ctx):
         bemgpu.bem([outer, inner], fl, 1.0, parents=[0, 0], ctx=ctx)  # inner is inside
     with pytest.raises(bemgpu.ArgumentError):
         bemgpu.bem([outer, inner], fl, 1.0, parents=[0, 2], ctx=ctx)  # not an earlier region
+
+
+@pytest.mark.parametrize("formulation", ["muller", "cbie"])
+def test_region_pressure_matches_oracle(ctx, formulation):
+    """pressure(sol, points; field, region) of a coupled-region solution
+    (fields/regions.jl:1-65): points outside, between the shells and inside the core, every
+    field, region selection; against the oracle's restatement on the oracle's solution."""
+    surfs = [meshes.icosphere(1.0, 2), meshes.icosphere(0.5, 1)]
+    mats = [(1.05, 1.03), (1.3, 1.2)]
+    k, beta = 1.2, 0.3
+    sol, ref = _solve_both(ctx, surfs, mats, [0, 1], k, beta, formulation)
+    d = O.incidence_direction(beta, 0.0)
+    rng = np.random.default_rng(3)
+
+    def shell(r0, r1, m):
+        v = rng.standard_normal((m, 3))
+        return v / np.linalg.norm(v, axis=1)[:, None] * rng.uniform(r0, r1, m)[:, None]
+
+    outside, between, core = shell(1.3, 2.5, 6), shell(0.7, 0.85, 6), shell(0.05, 0.3, 6)
+    cases = [(outside, "total", None), (outside, "scattered", None), (outside, "incident", None),
+             (between, "total", None), (between, "interior", None), (core, "total", None),
+             (core, "interior", 2), (between, "total", 1)]
+    for pts, field, region in cases:
+        got = sol.pressure(pts, field=field, region=region)
+        want = O.pressure_regions(surfs, mats, [0, 1], k, pts, ref["x"], d, field=field,
+                                  region=region)
+        assert np.max(np.abs(got - want)) <= 1e-8 * np.max(np.abs(want)), (field, region)
+    with pytest.raises(bemgpu.ArgumentError):
+        sol.pressure(between, field="scattered")
+    with pytest.raises(bemgpu.ArgumentError):
+        sol.pressure(outside, field="interior")
+    with pytest.raises(bemgpu.ArgumentError):
+        sol.pressure(core, field="total", region=1)
+    with pytest.raises(bemgpu.ArgumentError):
+        sol.pressure(core, field="total", region=5)

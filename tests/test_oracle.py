@@ -277,3 +277,20 @@ def test_oracle_gmres_path_matches_direct_solve():
         assert it["converged"]
         f0 = direct["amplitudes"][0]
         assert abs(it["amplitude"] - f0) <= 1e-9 * abs(f0)
+
+
+def test_region_pressure_single_interface_is_the_fluid_pressure():
+    """The coupled-region field restatement with one interface equals the single-body
+    fluid field (fields/pressure.jl:404-471) outside and inside."""
+    s = meshes.icosphere(1.0, 2)
+    g, h, k, beta = 1.07, 1.04, 1.4, 0.5
+    reg = O.solve_regions([s], [(g, h)], [0], k, incidence_angle=beta)
+    one = O.solve(s[0], s[1], "fluid", k, incidence_angle=beta, g=g, h=h)
+    d = O.incidence_direction(beta, 0.0)
+    pts = np.array([[1.6, 0.2, -0.3], [0.1, -2.0, 0.4], [0.2, 0.1, -0.3], [-0.4, 0.3, 0.2]])
+    for field in ("total", "scattered", "interior"):
+        sel = pts[:2] if field == "scattered" else (pts[2:] if field == "interior" else pts)
+        a = O.pressure_regions([s], [(g, h)], [0], k, sel, reg["x"], d, field=field)
+        b = O.pressure(one["panels"], k, sel, one["p_scat"], one["dpdn_scat"], d, field=field,
+                       g=g, h=h, fluid=True)
+        assert np.max(np.abs(a - b)) <= 1e-9 * np.max(np.abs(b)), field
