@@ -204,6 +204,17 @@ __device__ __forceinline__ float ld_peer_f32(uint32_t a) {
   asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(a) : "memory");
   return v;
 }
+__device__ __forceinline__ int32_t ld_peer_s32(uint32_t a) {
+  int32_t v;
+  asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ void better32(float& bv, int32_t& bi, float ov, int32_t oi) {
+  if (ov > bv || (ov == bv && oi < bi)) {
+    bv = ov;
+    bi = oi;
+  }
+}
 __device__ __forceinline__ long long ld_peer_s64(uint32_t a) {
   long long v;
   asm volatile("ld.shared::cluster.s64 %0, [%1];" : "=l"(v) : "r"(a) : "memory");
@@ -231,9 +242,9 @@ __global__ void __launch_bounds__(kGetf2T) k_getf2_ll(const MatInst* __restrict_
   __shared__ cf sL[kPanelNB][kPanelNB + 1];  // finished L11 rows
   __shared__ cf su[kPanelNB];                // U[0:c, c]
   __shared__ float w_val[T / 32];
-  __shared__ int64_t w_idx[T / 32];
+  __shared__ int32_t w_idx[T / 32];          // rows as int32 (orders below 2^31)
   __shared__ float c_val;                    // this CTA's pivot candidate
-  __shared__ int64_t c_idx;
+  __shared__ int32_t c_idx;
   __shared__ cf s_inv;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int64_t g = (int64_t)rank * T + tid;
@@ -260,7 +271,7 @@ __global__ void __launch_bounds__(kGetf2T) k_getf2_ll(const MatInst* __restrict_
     __syncthreads();
     // (2) rows >= col: finish L[., c - 1], update column c, pivot candidate
     float best = -1.f;
-    int64_t bidx = INT64_MAX;
+    int32_t bidx = INT32_MAX;
     int64_t r = k0 + g;
     if (r < col) r += ((col - r + stride - 1) / stride) * stride;
     for (; r < n; r += stride) {
@@ -288,39 +299,59 @@ __global__ void __launch_bounds__(kGetf2T) k_getf2_ll(const MatInst* __restrict_
         }
       }
       A[r + col * lda] = make_float2(acc.x, acc.y);
-      better(best, bidx, cabs1(acc), r);
+      better32(best, bidx, cabs1(acc), (int32_t)r);
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       const float ov = __shfl_down_sync(0xffffffffu, best, off);
-      const int64_t oi = __shfl_down_sync(0xffffffffu, bidx, off);
-      better(best, bidx, ov, oi);
+      const int32_t oi = __shfl_down_sync(0xffffffffu, bidx, off);
+      better32(best, bidx, ov, oi);
     }
     if (lane == 0) {
       w_val[wid] = best;
       w_idx[wid] = bidx;
     }
     __syncthreads();
-    if (tid == 0) {
-      float bv = w_val[0];
-      int64_t bi = w_idx[0];
-      for (int w = 1; w < T / 32; ++w) better(bv, bi, w_val[w], w_idx[w]);
-      c_val = bv;
-      c_idx = bi;
+    if (wid == 0) {  // the CTA's candidate: a shuffle tree over the 32 warps' candidates
+      float bv = w_val[lane];
+      int32_t bi = w_idx[lane];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, bv, off);
+        const int32_t oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        better32(bv, bi, ov, oi);
+      }
+      if (lane == 0) {
+        c_val = bv;
+        c_idx = bi;
+      }
     }
-    // (3) pivot of the cluster
+    // (3) pivot of the cluster: only warp 0 needs it (the U row, the interchange over the
+    // panel's <= 32 columns, the singular marker and the pivot's reciprocal are its work)
     if (CS > 1)
       cluster_sync_all();
     else
       __syncthreads();
-    float pv = c_val;
-    int64_t piv = c_idx;
-    if (CS > 1) {
-      for (unsigned q = 0; q < (unsigned)CS; ++q) {
-        if (q == rank) continue;
-        better(pv, piv, ld_peer_f32(peer_smem(&c_val, q)), (int64_t)ld_peer_s64(peer_smem(&c_idx, q)));
+    float pv = -1.f;
+    int32_t piv32 = INT32_MAX;
+    if (wid == 0) {  // one lane per CTA of the cluster, all peer loads in flight
+      if (lane < CS) {
+        if (CS > 1 && (unsigned)lane != rank) {
+          pv = ld_peer_f32(peer_smem(&c_val, (unsigned)lane));
+          piv32 = ld_peer_s32(peer_smem(&c_idx, (unsigned)lane));
+        } else {
+          pv = c_val;
+          piv32 = c_idx;
+        }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {  // every lane gets the cluster's pivot
+        const float ov = __shfl_xor_sync(0xffffffffu, pv, off);
+        const int32_t oi = __shfl_xor_sync(0xffffffffu, piv32, off);
+        better32(pv, piv32, ov, oi);
       }
     }
+    int64_t piv = piv32;
     if (piv >= n) piv = col;  // no candidate rows (cannot happen for col < n)
     const bool nonzero = pv > 0.f;
     if (rank == 0) {

@@ -208,3 +208,32 @@ def test_queries_of_a_compressed_solution(ctx, sphere):
     assert np.linalg.norm(fa - fb) <= 1e-8 * np.linalg.norm(fa)
     dense.close()
     comp.close()
+
+
+def test_tiny_mesh_without_admissible_blocks(ctx):
+    """A surface of one leaf: no compressed block, the full block and GMRES alone."""
+    nodes, tris = meshes.icosphere(0.01, 0)
+    surf = bemgpu.mesh(nodes, tris)
+    ref = O.solve(nodes, tris, "rigid", K0, incidence_angle=0.9, incidence_azimuth=0.1)
+    sol = bemgpu.bem(surf, bemgpu.Rigid(), K0, incidence_angle=0.9, incidence_azimuth=0.1,
+                     compression=dict(HM, tol=1e-10), gmres_kwargs=dict(reltol=1e-12), ctx=ctx)
+    st = sol.hmatrix_stats()
+    assert st["lowrank_blocks"] == 0 and st["dense_blocks"] == 1
+    f0 = ref["amplitudes"][0]
+    assert abs(bemgpu.scattering_amplitude(sol) - f0) <= 1e-9 * abs(f0)
+    sol.close()
+
+
+def test_gmres_groups_under_a_small_budget(sphere):
+    """With an HBM budget that holds the Krylov bases of only a few right-hand sides, GMRES
+    runs them in groups; the results are those of one group."""
+    nodes, tris, surf, P = sphere
+    angles = np.linspace(0.1, 3.0, 12)
+    kw = dict(compression=HM, gmres_kwargs=dict(restart=500, reltol=1e-8))
+    big = bemgpu.Context(0)
+    small = bemgpu.Context(0, 200 << 20)
+    a = bemgpu.incidence_angle_sweep(bemgpu.mesh(nodes, tris), bemgpu.Rigid(), K0, angles,
+                                     ctx=big, **kw)
+    b = bemgpu.incidence_angle_sweep(bemgpu.mesh(nodes, tris), bemgpu.Rigid(), K0, angles,
+                                     ctx=small, **kw)
+    assert np.array_equal(a.amplitudes, b.amplitudes)
