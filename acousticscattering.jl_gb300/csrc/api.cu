@@ -63,8 +63,6 @@ struct bemgpu_ctx {
   bool tensor_lu = true;  // complex64 trailing updates on the tensor cores
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   std::map<std::string, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>> events;
-  float* pinned = nullptr;  // page-locked staging of host <-> device vector exchanges
-  size_t pinned_bytes = 0;
   // launch-shape autotuner: the fastest measured choice per (kernel family, shape class)
   std::map<std::string, int> tuned;
   bool autotune = true;
@@ -700,121 +698,6 @@ int assemble_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
 }
 
 // ------------------------------------------------------------------ factorisation
-// zlacn2 (Higham 1988, LAPACK) reverse-communication state for one instance.
-struct Lacn2 {
-  int n = 0, kase = 0, isave1 = 0, isave2 = 0, isave3 = 0;
-  double est = 0.0;
-  std::vector<std::complex<double>> v;
-  static double sum1(const std::vector<std::complex<double>>& x) {
-    double s = 0.0;
-    for (auto& z : x) s += std::abs(z);
-    return s;
-  }
-  static int imax(const std::vector<std::complex<double>>& x) {
-    int b = 0;
-    double bv = -1.0;
-    for (int i = 0; i < (int)x.size(); ++i)
-      if (std::abs(x[i]) > bv) {
-        bv = std::abs(x[i]);
-        b = i;
-      }
-    return b;
-  }
-  static void normalise(std::vector<std::complex<double>>& x) {
-    const double safmin = 2.2250738585072014e-308;
-    for (auto& z : x) {
-      double a = std::abs(z);
-      z = a > safmin ? z / a : std::complex<double>(1.0, 0.0);
-    }
-  }
-  // One reverse-communication step: x in/out.  Returns kase (0 = done).
-  int step(std::vector<std::complex<double>>& x) {
-    const int itmax = 5;
-    if (kase == 0) {
-      for (auto& z : x) z = std::complex<double>(1.0 / n, 0.0);
-      kase = 1;
-      isave1 = 1;
-      return kase;
-    }
-    switch (isave1) {
-      case 1:
-        if (n == 1) {
-          v = x;
-          est = std::abs(v[0]);
-          kase = 0;
-          return 0;
-        }
-        est = sum1(x);
-        normalise(x);
-        kase = 2;
-        isave1 = 2;
-        return kase;
-      case 2:
-        isave2 = imax(x);
-        isave3 = 2;
-        goto main_loop;
-      case 3: {
-        v = x;
-        double estold = est;
-        est = sum1(v);
-        if (est <= estold) goto final_stage;
-        normalise(x);
-        kase = 2;
-        isave1 = 4;
-        return kase;
-      }
-      case 4: {
-        int jlast = isave2;
-        isave2 = imax(x);
-        if (std::abs(x[jlast]) != std::abs(x[isave2]) && isave3 < itmax) {
-          ++isave3;
-          goto main_loop;
-        }
-        goto final_stage;
-      }
-      case 5: {
-        double temp = 2.0 * (sum1(x) / (3.0 * n));
-        if (temp > est) {
-          v = x;
-          est = temp;
-        }
-        kase = 0;
-        return 0;
-      }
-    }
-  main_loop:
-    for (auto& z : x) z = 0.0;
-    x[isave2] = 1.0;
-    kase = 1;
-    isave1 = 3;
-    return kase;
-  final_stage : {
-    double alt = 1.0;
-    for (int i = 0; i < n; ++i) {
-      x[i] = std::complex<double>(alt * (1.0 + (double)i / (double)(n - 1)), 0.0);
-      alt = -alt;
-    }
-  }
-    kase = 1;
-    isave1 = 5;
-    return kase;
-  }
-};
-
-// Infinity-norm reciprocal condition of the complex64 factors (LAPACK cgecon('I'):
-// kase 2 applies (LU)^{-1}, kase 1 applies (LU)^{-H}; rcond = 1 / (anorm ||A^-1||)).
-// Page-locked host staging of at least `bytes`, kept by the context.
-float* pinned_buffer(bemgpu_ctx* c, size_t bytes) {
-  if (c->pinned_bytes >= bytes) return c->pinned;
-  if (c->pinned) cudaFreeHost(c->pinned);
-  c->pinned = nullptr;
-  c->pinned_bytes = 0;
-  void* p = nullptr;
-  if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
-  c->pinned = static_cast<float*>(p);
-  c->pinned_bytes = bytes;
-  return c->pinned;
-}
 
 // ------------------------------------------------------------------ autotuner
 // Launch shapes whose choice leaves every result bit-for-bit unchanged (the rows each
@@ -863,85 +746,82 @@ int tune_pick(bemgpu_ctx* c, const std::string& key, const std::vector<int>& can
 
 // Cluster size of the complex64 panel kernel for this batch and panel height, measured
 // on scratch copies of the panels (the kernel factors in place).
-// LAPACK's 1-norm estimate (zlacn2 reverse communication) for every factor of the batch:
-// each round packs the vectors of all instances that ask for the same product into one
-// page-locked buffer, runs one batched triangular solve and reads them back with one copy.
+// Infinity-norm reciprocal condition of the complex64 factors (LAPACK cgecon('I'):
+// zlacn2's kase 2 applies (LU)^{-1}, kase 1 applies (LU)^{-H}; rcond = 1 / (anorm
+// ||A^-1||)).  Every factor's zlacn2 state lives on the device (k_lacn2); each round runs
+// the batched products the states ask for and reads back only the states.
 int estimate_rcond(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
   if (fs.empty()) return BEMGPU_OK;
   const Launch L = c->launch();
   const size_t F = fs.size();
-  std::vector<Lacn2> st(F);
-  std::vector<std::vector<std::complex<double>>> xs(F);
+  std::vector<Lacn2Dev> st(F);
   std::vector<size_t> off(F + 1, 0);
   int64_t nmax = 0;
   for (size_t t = 0; t < F; ++t) {
-    st[t].n = (int)fs[t]->N;
-    xs[t].assign((size_t)fs[t]->N, 0.0);
+    std::memset(&st[t], 0, sizeof st[t]);
+    st[t].n = (int32_t)fs[t]->N;
+    st[t].off = (int64_t)off[t];
     off[t + 1] = off[t] + (size_t)fs[t]->N;
     nmax = std::max(nmax, fs[t]->N);
   }
-  Buf work, work2;
+  Buf work, work2, d_st, d_m1, d_m2;
   TRY(alloc(c, off[F] * 8, &work));
   TRY(alloc(c, off[F] * 8, &work2));
-  float* host = pinned_buffer(c, off[F] * 8);
-  if (!host) return fail(c, BEMGPU_ECUDA, "page-locked staging allocation failed");
+  // one descriptor array per product: kase 1 applies (LU)^{-H}, kase 2 (LU)^{-1}; the
+  // device step switches each instance's active flag
+  std::vector<MatInst> mi(F);
+  for (size_t t = 0; t < F; ++t) {
+    MatInst& m = mi[t];
+    std::memset(&m, 0, sizeof m);
+    m.a = fs[t]->LU.p;
+    m.n = fs[t]->N;
+    m.lda = fs[t]->N;
+    m.ipiv = fs[t]->ipiv.as<int32_t>();
+    m.info = fs[t]->info.as<int32_t>();
+    m.x = work.as<float2>() + off[t];
+    m.y = work2.as<float2>() + off[t];
+    m.ldx = fs[t]->N;
+    m.nrhs = 1;
+    m.active = 0;
+  }
+  TRY(upload(c, st, &d_st));
+  TRY(upload(c, mi, &d_m1));
+  TRY(upload(c, mi, &d_m2));
   TrsvWork tw{1};
-  std::vector<int> kase(F);
-  for (size_t t = 0; t < F; ++t) kase[t] = st[t].step(xs[t]);
-  Buf d_mi;
+  Lacn2Dev* ds = d_st.as<Lacn2Dev>();
+  MatInst* m1 = d_m1.as<MatInst>();
+  MatInst* m2 = d_m2.as<MatInst>();
+  launch_lacn2(L, ds, (int)F, work.as<float2>(), m1, m2, 0);
+  std::vector<int32_t> kase(F, 1);
   for (int round = 0; round < 64; ++round) {
-    bool any = false;
-    for (int want : {1, 2}) {
-      std::vector<MatInst> mi;
-      std::vector<size_t> who;
-      size_t lo = off[F], hi = 0;
-      for (size_t t = 0; t < F; ++t) {
-        if (kase[t] != want) continue;
-        float* h = host + 2 * off[t];
-        for (size_t i = 0; i < xs[t].size(); ++i) {
-          h[2 * i] = (float)xs[t][i].real();
-          h[2 * i + 1] = (float)xs[t][i].imag();
-        }
-        lo = std::min(lo, off[t]);
-        hi = std::max(hi, off[t + 1]);
-        MatInst m{};
-        m.a = fs[t]->LU.p;
-        m.n = fs[t]->N;
-        m.lda = fs[t]->N;
-        m.ipiv = fs[t]->ipiv.as<int32_t>();
-        m.info = fs[t]->info.as<int32_t>();
-        m.x = work.as<float2>() + off[t];
-        m.y = work2.as<float2>() + off[t];
-        m.ldx = fs[t]->N;
-        m.nrhs = 1;
-        m.active = 1;
-        mi.push_back(m);
-        who.push_back(t);
-      }
-      if (mi.empty()) continue;
-      any = true;
-      CUDA_TRY(c, cudaMemcpyAsync(work.as<float2>() + lo, host + 2 * lo, (hi - lo) * 8,
-                                  cudaMemcpyHostToDevice, c->stream));
-      TRY(to_device(c, mi, &d_mi));
+    bool any1 = false, any2 = false;
+    for (int32_t k : kase) {
+      any1 |= k == 1;
+      any2 |= k == 2;
+    }
+    if (!any1 && !any2) break;
+    if (any1) {
       {
         Prof pr(c, "getrs");
-        launch_getrs(L, d_mi.as<MatInst>(), (int)mi.size(), nmax, 1, want == 1 ? 1 : 0, 1, 0,
-                     &tw);
+        launch_getrs(L, m1, (int)F, nmax, 1, 1, 1, 0, &tw);
       }
-      CUDA_TRY(c, cudaMemcpyAsync(host + 2 * lo, work.as<float2>() + lo, (hi - lo) * 8,
-                                  cudaMemcpyDeviceToHost, c->stream));
-      CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-      for (size_t w : who) {
-        const float* h = host + 2 * off[w];
-        for (size_t i = 0; i < xs[w].size(); ++i)
-          xs[w][i] = std::complex<double>(h[2 * i], h[2 * i + 1]);
-        kase[w] = st[w].step(xs[w]);
-      }
+      launch_lacn2(L, ds, (int)F, work.as<float2>(), m1, m2, 1);
+      any2 = true;  // those instances usually ask for the other product next
     }
-    if (!any) break;
+    if (any2) {
+      {
+        Prof pr(c, "getrs");
+        launch_getrs(L, m2, (int)F, nmax, 1, 0, 1, 0, &tw);
+      }
+      launch_lacn2(L, ds, (int)F, work.as<float2>(), m1, m2, 2);
+    }
+    CUDA_TRY(c, cudaGetLastError());
+    TRY(download(c, d_st, &st, F));
+    for (size_t t = 0; t < F; ++t) kase[t] = st[t].kase;
   }
   for (size_t t = 0; t < F; ++t) {
-    double ainv = st[t].est;
+    if (st[t].kase != 0) return fail(c, BEMGPU_ENOTCONVERGED, "condition estimate did not end");
+    const double ainv = st[t].est;
     fs[t]->rcond = (ainv != 0.0) ? (1.0 / ainv) / fs[t]->anorm : 0.0;
   }
   return BEMGPU_OK;
@@ -2441,7 +2321,6 @@ int bemgpu_ctx_destroy(bemgpu_ctx* c) {
       cudaEventDestroy(pr.second);
     }
   drop_cache(c);
-  if (c->pinned) cudaFreeHost(c->pinned);
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
   cudaFree(c->d_err);

@@ -90,6 +90,170 @@ __global__ void k_fill(double* p, int64_t count, double v) {
   if (i < count) p[i] = v;
 }
 
+// ------------------------------------------------------------------ zlacn2 on the device
+// LAPACK's zlacn2 (1-norm estimate by reverse communication, the estimator inside gecon),
+// one CTA per factor: the same states and tests as LAPACK (sum of moduli, first index of
+// the largest modulus, x_i / |x_i| with 1 below safmin, at most 5 iterations, the
+// alternating-sign final vector), moduli and sums in FP64 from the complex64 vector, sums
+// in a fixed order.
+constexpr int kLacT = 256;
+
+__device__ double lac_sum(double v, double* sh) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < kLacT / 32; ++w) t += sh[w];
+  return t;
+}
+
+__device__ int lac_imax(const float2* x, int n, double* sv, int* si) {
+  double bv = -1.0;
+  int bi = INT32_MAX;
+  for (int i = threadIdx.x; i < n; i += kLacT) {
+    const double a = hypot((double)x[i].x, (double)x[i].y);
+    if (a > bv) {  // increasing i per thread: the first index of each thread's maximum
+      bv = a;
+      bi = i;
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const double ov = __shfl_xor_sync(0xffffffffu, bv, off);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+    if (ov > bv || (ov == bv && oi < bi)) {
+      bv = ov;
+      bi = oi;
+    }
+  }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) {
+    sv[threadIdx.x >> 5] = bv;
+    si[threadIdx.x >> 5] = bi;
+  }
+  __syncthreads();
+  bv = sv[0];
+  bi = si[0];
+  for (int w = 1; w < kLacT / 32; ++w)
+    if (sv[w] > bv || (sv[w] == bv && si[w] < bi)) {
+      bv = sv[w];
+      bi = si[w];
+    }
+  return bi;
+}
+
+__global__ void __launch_bounds__(kLacT) k_lacn2(Lacn2Dev* __restrict__ st, float2* __restrict__ work,
+                                                MatInst* __restrict__ mi1,
+                                                MatInst* __restrict__ mi2, int want) {
+  Lacn2Dev& S = st[blockIdx.x];
+  const int kase0 = S.kase;
+  if (want == 0 ? (kase0 != 0 || S.isave1 != 0) : kase0 != want) return;  // uniform
+  __shared__ double sh[kLacT / 32];
+  __shared__ int shi[kLacT / 32];
+  float2* x = work + S.off;
+  const int n = S.n;
+  int kase = 0, isave1 = S.isave1, isave2 = S.isave2, isave3 = S.isave3;
+  double est = S.est;
+  auto sum1 = [&]() {
+    double t = 0.0;
+    for (int i = threadIdx.x; i < n; i += kLacT) t += hypot((double)x[i].x, (double)x[i].y);
+    return lac_sum(t, sh);
+  };
+  auto normalise = [&]() {
+    const double safmin = 2.2250738585072014e-308;
+    for (int i = threadIdx.x; i < n; i += kLacT) {
+      const double re = x[i].x, im = x[i].y, a = hypot(re, im);
+      x[i] = a > safmin ? make_float2((float)(re / a), (float)(im / a)) : make_float2(1.f, 0.f);
+    }
+  };
+  int go = 0;  // 1: the main loop's unit vector, 2: the final alternating vector
+  if (want == 0) {
+    for (int i = threadIdx.x; i < n; i += kLacT) x[i] = make_float2((float)(1.0 / n), 0.f);
+    kase = 1;
+    isave1 = 1;
+  } else {
+    switch (isave1) {
+      case 1:
+        if (n == 1) {
+          est = hypot((double)x[0].x, (double)x[0].y);
+          kase = 0;
+          break;
+        }
+        est = sum1();
+        normalise();
+        kase = 2;
+        isave1 = 2;
+        break;
+      case 2:
+        isave2 = lac_imax(x, n, sh, shi);
+        isave3 = 2;
+        go = 1;
+        break;
+      case 3: {
+        const double estold = est;
+        est = sum1();
+        if (est <= estold) {
+          go = 2;
+          break;
+        }
+        normalise();
+        kase = 2;
+        isave1 = 4;
+        break;
+      }
+      case 4: {
+        const int jlast = isave2;
+        isave2 = lac_imax(x, n, sh, shi);
+        const double a = hypot((double)x[jlast].x, (double)x[jlast].y);
+        const double b = hypot((double)x[isave2].x, (double)x[isave2].y);
+        if (a != b && isave3 < 5) {
+          ++isave3;
+          go = 1;
+        } else {
+          go = 2;
+        }
+        break;
+      }
+      default: {  // 5
+        const double temp = 2.0 * (sum1() / (3.0 * n));
+        if (temp > est) est = temp;
+        kase = 0;
+        break;
+      }
+    }
+  }
+  __syncthreads();  // every read of x above precedes the writes below
+  if (go == 1) {
+    for (int i = threadIdx.x; i < n; i += kLacT) x[i] = make_float2(i == isave2 ? 1.f : 0.f, 0.f);
+    kase = 1;
+    isave1 = 3;
+  } else if (go == 2) {
+    for (int i = threadIdx.x; i < n; i += kLacT) {
+      const double v = (1.0 + (double)i / (double)(n - 1)) * ((i & 1) ? -1.0 : 1.0);
+      x[i] = make_float2((float)v, 0.f);
+    }
+    kase = 1;
+    isave1 = 5;
+  }
+  if (threadIdx.x == 0) {
+    S.kase = kase;
+    S.isave1 = isave1;
+    S.isave2 = isave2;
+    S.isave3 = isave3;
+    S.est = est;
+    mi1[blockIdx.x].active = kase == 1;
+    mi2[blockIdx.x].active = kase == 2;
+  }
+}
+
+void launch_lacn2(const Launch& L, Lacn2Dev* st, int ninst, float2* work, MatInst* mi1,
+                  MatInst* mi2, int want) {
+  k_lacn2<<<(unsigned)ninst, kLacT, 0, L.stream>>>(st, work, mi1, mi2, want);
+  count_launch(1);
+}
+
 void launch_traces(const Launch& L, const TraceInst* d, int ninst, int64_t nmax, int32_t max_rhs) {
   dim3 g((unsigned)((nmax + 255) / 256), (unsigned)max_rhs, (unsigned)ninst);
   k_traces<<<g, 256, 0, L.stream>>>(d);

@@ -20,7 +20,19 @@ struct TraceInst {
   int32_t pad;
 };
 
+// Device state of LAPACK's zlacn2 reverse communication for one factor (the 1-norm
+// estimate of gecon); its vector is complex64 at work + off.
+struct Lacn2Dev {
+  int64_t off;
+  int32_t n, kase, isave1, isave2, isave3, pad;
+  double est;
+};
+
 #ifdef __CUDACC__
+// One zlacn2 step for every instance whose kase == want (want = 0: the first call); the
+// next product is flagged active in mi1 (kase 1) or mi2 (kase 2).
+void launch_lacn2(const Launch& L, Lacn2Dev* st, int ninst, float2* work, MatInst* mi1,
+                  MatInst* mi2, int want);
 void launch_traces(const Launch& L, const TraceInst* d, int ninst, int64_t nmax, int32_t max_rhs);
 void launch_cbie_forcing(const Launch& L, const TraceInst* d, int ninst, int64_t nmax,
                          int32_t max_rhs);
