@@ -2886,7 +2886,7 @@ int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x,
     TRY(alloc(c, (size_t)g * mi * 8, &hb));
     TRY(alloc(c, (size_t)g * n * 16, &w));
     TRY(alloc(c, H.scratch_bytes(g), &T));
-    TRY(alloc(c, sizeof(int32_t) * (size_t)(2 + g), &nact));  // count + one per CTA
+    TRY(alloc(c, sizeof(int32_t) * (size_t)(3 + g), &nact));  // count, step, one per CTA
     CUDA_TRY(c, cudaMemsetAsync(st.p, 0, st.bytes, c->stream));
     CUDA_TRY(c, cudaMemsetAsync(Hh.p, 0, Hh.bytes, c->stream));
     CUDA_TRY(c, cudaMemsetAsync(gg.p, 0, gg.bytes, c->stream));
@@ -2914,6 +2914,7 @@ int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x,
     W.maxiter = mi;
     W.chunks = chunks;
     W.nact = nact.as<int32_t>();
+    W.jcur = nact.as<int32_t>() + 2 + g;
     const HmOp A = H.op(op, T.p, g);
     auto active = [&](int32_t* out) -> int {
       CUDA_TRY(c, cudaMemcpyAsync(out, W.nact, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
@@ -2929,15 +2930,50 @@ int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x,
     int32_t na = 0;
     TRY(active(&na));
     if (o.maxiter == 0) na = 0;
+    // one Arnoldi step with the step index on the device, so that a CUDA graph of kSteps
+    // steps captured once replays any kSteps consecutive steps of any cycle
+    constexpr int32_t kSteps = 4;
+    auto step = [&]() {
+      launch_hm_matvec(L, A, W.Vb, (int64_t)(R + 1) * n, W.w, n, nullptr, 0, 0.0, 1.0, g, W.st,
+                       1, W.jcur, n);
+      launch_gm_arnoldi(L, W, -1);
+      launch_gm_rotate(L, W, -1);
+    };
+    cudaGraphExec_t steps = nullptr;
+    long long graph_launches = 0;
+    if (R >= kSteps) {
+      cudaGraph_t graph = nullptr;
+      const long long before = launch_total();
+      if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        for (int32_t q = 0; q < kSteps; ++q) step();
+        if (cudaStreamEndCapture(c->stream, &graph) == cudaSuccess && graph) {
+          if (cudaGraphInstantiate(&steps, graph, 0) != cudaSuccess) steps = nullptr;
+          cudaGraphDestroy(graph);
+        }
+      }
+      cudaGetLastError();
+      graph_launches = launch_total() - before;
+      count_launch(-(int)graph_launches);  // captured, not run
+    }
+    struct GraphGuard {
+      cudaGraphExec_t& e;
+      ~GraphGuard() {
+        if (e) cudaGraphExecDestroy(e);
+      }
+    } guard{steps};
     while (na > 0) {
       {
         Prof pr(c, "gmres");
-        for (int32_t j = 0; j < R; ++j) {
-          launch_hm_matvec(L, A, W.Vb + 2 * (size_t)j * n, (int64_t)(R + 1) * n, W.w, n, nullptr,
-                           0, 0.0, 1.0, g, W.st, 1);
-          launch_gm_arnoldi(L, W, j);
-          launch_gm_rotate(L, W, j);
-          if ((j + 1) % 4 == 0 && j + 1 < R) {
+        for (int32_t j = 0; j < R;) {
+          if (steps && j + kSteps <= R) {
+            CUDA_TRY(c, cudaGraphLaunch(steps, c->stream));
+            count_launch((int)graph_launches);
+            j += kSteps;
+          } else {
+            step();
+            ++j;
+          }
+          if (j % kSteps == 0 && j < R) {
             TRY(active(&na));
             if (na == 0) break;
           }

@@ -358,10 +358,12 @@ __device__ __forceinline__ bool group_on(const GmState* st, int r0, int rb, int 
 // per lane and right-hand side (added in a fixed order).
 template <typename R, int RB>
 __global__ void __launch_bounds__(256) k_hm_vt(HmOp A, const void* __restrict__ X, int64_t ldx,
-                                               int32_t nr, const GmState* st, int mode) {
+                                               int32_t nr, const GmState* st, int mode,
+                                               const int32_t* jptr, int64_t jstride) {
   using C = cx<R>;
   const int r0 = blockIdx.y * RB;
   if (!group_on(st, r0, RB, nr, mode)) return;
+  if (jptr) X = static_cast<const C*>(X) + (int64_t)*jptr * jstride;
   const HmItem it = A.vt_items[blockIdx.x];
   const HmLR B = A.lr[it.blk];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -410,10 +412,12 @@ constexpr int kLeafSlices = 4;
 // column slices per pass, slices added in a fixed order), RB right-hand sides per CTA.
 template <typename R, int RB>
 __global__ void __launch_bounds__(kLeafRows * kLeafSlices) k_hm_dblk(
-    HmOp A, const void* __restrict__ X, int64_t ldx, int32_t nr, const GmState* st, int mode) {
+    HmOp A, const void* __restrict__ X, int64_t ldx, int32_t nr, const GmState* st, int mode,
+    const int32_t* jptr, int64_t jstride) {
   using C = cx<R>;
   const int r0 = blockIdx.y * RB;
   if (!group_on(st, r0, RB, nr, mode)) return;
+  if (jptr) X = static_cast<const C*>(X) + (int64_t)*jptr * jstride;
   const HmDense& B = A.dn[blockIdx.x];
   const int row = threadIdx.x % kLeafRows, s = threadIdx.x / kLeafRows;
   __shared__ C part[RB][kLeafSlices][kLeafRows];
@@ -560,16 +564,18 @@ __global__ void __launch_bounds__(kLeafRows * kLeafSlices) k_hm_gather(
 
 // complex128 -> complex64 copy of the input vectors (one rounding per element)
 __global__ void k_hm_to_f32(const double* __restrict__ X, int64_t ldx, cf* __restrict__ Xf,
-                            int64_t n, const GmState* st, int mode) {
+                            int64_t n, const GmState* st, int mode, const int32_t* jptr,
+                            int64_t jstride) {
   const int r = blockIdx.y;
   if (!rhs_on(st, r, mode)) return;
+  if (jptr) X += 2 * (int64_t)*jptr * jstride;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) Xf[(int64_t)r * n + i] = to<float>(ldc(X, (int64_t)r * ldx + i));
 }
 
 void launch_hm_matvec(const Launch& L, const HmOp& A, const double* X, int64_t ldx, double* Y,
                       int64_t ldy, const double* B, int64_t ldb, double sb, double sa, int32_t nr,
-                      const GmState* act, int mode) {
+                      const GmState* act, int mode, const int32_t* jptr, int64_t jstride) {
   if (nr <= 0) return;
   constexpr int kRB = 4;  // right-hand sides per CTA of the block products
   const int rb = nr >= kRB ? kRB : 1;
@@ -582,21 +588,22 @@ void launch_hm_matvec(const Launch& L, const HmOp& A, const double* X, int64_t l
   int64_t ldr = ldx;
   if (A.f32) {
     k_hm_to_f32<<<dim3((unsigned)((A.n + 255) / 256), (unsigned)nr), 256, 0, L.stream>>>(
-        X, ldx, static_cast<cf*>(A.Xf), A.n, act, mode);
+        X, ldx, static_cast<cf*>(A.Xf), A.n, act, mode, jptr, jstride);
     ++launches;
     Xr = A.Xf;
     ldr = A.n;
+    jptr = nullptr;  // the copy is already the step's vector
   }
   auto blocks = [&](auto tag, auto rbt) {
     using R = decltype(tag);
     constexpr int RB = decltype(rbt)::value;
     if (A.n_lr > 0) {
-      k_hm_vt<R, RB><<<gv, 256, 0, L.stream>>>(A, Xr, ldr, nr, act, mode);
+      k_hm_vt<R, RB><<<gv, 256, 0, L.stream>>>(A, Xr, ldr, nr, act, mode, jptr, jstride);
       k_hm_lblk<R, RB><<<gb, kHmRowChunk, 0, L.stream>>>(A, nr, act, mode);
       launches += 2;
     }
     if (A.n_dense > 0) {
-      k_hm_dblk<R, RB><<<gd, TL, 0, L.stream>>>(A, Xr, ldr, nr, act, mode);
+      k_hm_dblk<R, RB><<<gd, TL, 0, L.stream>>>(A, Xr, ldr, nr, act, mode, jptr, jstride);
       ++launches;
     }
   };
@@ -635,6 +642,7 @@ void launch_hm_permute(const Launch& L, const double* src, int64_t lds, double* 
 constexpr int kGmT = 256;
 
 namespace {
+__device__ __forceinline__ int32_t jval(const GmWork& w, int32_t j) { return j >= 0 ? j : *w.jcur; }
 __device__ __forceinline__ double* vcol(const GmWork& w, int r, int l) {
   return w.Vb + 2 * (((int64_t)r * (w.restart + 1) + l) * w.n);
 }
@@ -651,6 +659,7 @@ __device__ __forceinline__ double* partp(const GmWork& w, int r, int chunk) {
 __global__ void __launch_bounds__(kGmT) k_gm_dot(GmWork w, int32_t j) {
   const int r = blockIdx.z, chunk = blockIdx.x;
   if (!w.st[r].active) return;
+  j = jval(w, j);
   const int lane = threadIdx.x & 31;
   const int l = blockIdx.y * (kGmT / 32) + (threadIdx.x >> 5);
   if (l > j) return;
@@ -674,6 +683,7 @@ __global__ void __launch_bounds__(kGmT) k_gm_dot(GmWork w, int32_t j) {
 __global__ void k_gm_dot_finish(GmWork w, int32_t j, int pass) {
   const int r = blockIdx.x;
   if (!w.st[r].active) return;
+  j = jval(w, j);
   for (int l = threadIdx.x; l <= j; l += blockDim.x) {
     cd s0 = {0.0, 0.0}, s1 = s0;
     int c = 0;
@@ -697,6 +707,7 @@ constexpr int kOrthSlices = kGmT / kOrthRows;
 __global__ void __launch_bounds__(kGmT) k_gm_orth(GmWork w, int32_t j) {
   const int r = blockIdx.y;
   if (!w.st[r].active) return;
+  j = jval(w, j);
   __shared__ cd h[512];
   __shared__ cd part[kOrthSlices][kOrthRows];
   const cd* hc = reinterpret_cast<const cd*>(w.hc) + (int64_t)r * (w.restart + 1);
@@ -753,6 +764,7 @@ __device__ __forceinline__ double chunk_norm(const GmWork& w, int r) {
 __global__ void __launch_bounds__(kGmT) k_gm_normalize(GmWork w, int32_t j) {
   const int r = blockIdx.y;
   if (!w.st[r].active) return;
+  j = jval(w, j);
   const double hn = chunk_norm(w, r);
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (blockIdx.x == 0 && threadIdx.x == 0) stc(w.H, hidx(w, r, j + 1, j), cd{hn, 0.0});
@@ -763,7 +775,8 @@ __global__ void __launch_bounds__(kGmT) k_gm_normalize(GmWork w, int32_t j) {
 
 void launch_gm_arnoldi(const Launch& L, const GmWork& w, int32_t j) {
   const dim3 gc((unsigned)w.chunks, (unsigned)w.nr);
-  const dim3 gd((unsigned)w.chunks, (unsigned)((j + 1 + kGmT / 32 - 1) / (kGmT / 32)),
+  const int32_t jg = j >= 0 ? j : w.restart - 1;  // device step: the largest grid
+  const dim3 gd((unsigned)w.chunks, (unsigned)((jg + 1 + kGmT / 32 - 1) / (kGmT / 32)),
                 (unsigned)w.nr);
   const dim3 go((unsigned)((w.n + kOrthRows - 1) / kOrthRows), (unsigned)w.nr);
   const dim3 gv((unsigned)((w.n + kGmT - 1) / kGmT), (unsigned)w.nr);
@@ -783,6 +796,7 @@ void launch_gm_arnoldi(const Launch& L, const GmWork& w, int32_t j) {
 constexpr int kRotWarps = 2;  // 40 KB of static shared memory per CTA
 
 __global__ void __launch_bounds__(kRotWarps * 32) k_gm_rotate(GmWork w, int32_t j, int32_t* cnt) {
+  j = jval(w, j);
   __shared__ cd col[kRotWarps][512];
   __shared__ cd ssn[kRotWarps][512];
   __shared__ double scs[kRotWarps][512];
@@ -854,19 +868,20 @@ __global__ void __launch_bounds__(kRotWarps * 32) k_gm_rotate(GmWork w, int32_t 
   if (threadIdx.x == 0) cnt[blockIdx.x] = c;
 }
 
-// nact = sum of the per-CTA counts (fixed order)
-__global__ void k_gm_count(GmWork w, const int32_t* cnt, int nb) {
+// nact = sum of the per-CTA counts (fixed order); a device step index advances
+__global__ void k_gm_count(GmWork w, const int32_t* cnt, int nb, int advance) {
   if (threadIdx.x != 0) return;
   int t = 0;
   for (int b = 0; b < nb; ++b) t += cnt[b];
   *w.nact = t;
+  if (advance) *w.jcur += 1;
 }
 
 void launch_gm_rotate(const Launch& L, const GmWork& w, int32_t j) {
   const int nb = (w.nr + kRotWarps - 1) / kRotWarps;
   int32_t* cnt = w.nact + 1;  // nact is followed by room for one count per CTA
   k_gm_rotate<<<(unsigned)nb, kRotWarps * 32, 0, L.stream>>>(w, j, cnt);
-  k_gm_count<<<1, 32, 0, L.stream>>>(w, cnt, nb);
+  k_gm_count<<<1, 32, 0, L.stream>>>(w, cnt, nb, j < 0 ? 1 : 0);
   count_launch(2);
 }
 
@@ -950,7 +965,10 @@ __global__ void k_gm_start_state(GmWork w, double reltol, double abstol, int fir
     }
     total += __syncthreads_count(act);
   }
-  if (threadIdx.x == 0) *w.nact = total;
+  if (threadIdx.x == 0) {
+    *w.nact = total;
+    if (w.jcur) *w.jcur = 0;
+  }
 }
 
 __global__ void __launch_bounds__(kGmT) k_gm_start_vec(GmWork w) {

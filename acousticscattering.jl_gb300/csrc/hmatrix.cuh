@@ -92,6 +92,8 @@ struct GmWork {
   int64_t n;
   int32_t nr, restart, maxiter, chunks;
   int32_t* nact;  // active right-hand sides after the last rotation step
+  int32_t* jcur;  // the current Arnoldi step on the device (kernels given j < 0 read it;
+                  // the rotation step advances it, a new cycle resets it)
 };
 
 #ifdef __CUDACC__
@@ -107,11 +109,14 @@ void launch_hm_dense(const Launch& L, const HmDense* dn, int32_t n_dense, void* 
                      double a_re, double a_im);
 // Y[:, r] = sb B[:, r] + sa (A X)[:, r] for every right-hand side r < nr with
 // (act == null or act[r].active), the operands in permuted order.
+// jptr (optional): X is offset by (*jptr) * jstride complex entries, read on the device
+// (the Arnoldi vector of the current step, so that a captured graph replays any step).
 void launch_hm_matvec(const Launch& L, const HmOp& A, const double* X, int64_t ldx, double* Y,
                       int64_t ldy, const double* B, int64_t ldb, double sb, double sa, int32_t nr,
-                      const GmState* act, int mode);
+                      const GmState* act, int mode, const int32_t* jptr = nullptr,
+                      int64_t jstride = 0);
 
-// GMRES steps (hmatrix.cu describes each).
+// GMRES steps (hmatrix.cu describes each); j < 0: the step index is read from w.jcur.
 void launch_gm_start(const Launch& L, const GmWork& w, double reltol, double abstol, int first);
 void launch_gm_arnoldi(const Launch& L, const GmWork& w, int32_t j);
 void launch_gm_rotate(const Launch& L, const GmWork& w, int32_t j);
