@@ -50,6 +50,8 @@ void bemgpu_set_process_error(const char* msg) { g_err = msg ? msg : ""; }
 }  // namespace bemgpu
 
 // ===================================================================== context + memory
+constexpr int kEventPool = 512;  // ordering events of the two-stream triangular solves
+
 struct bemgpu_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -68,7 +70,12 @@ struct bemgpu_ctx {
   bool autotune = true;
 
   std::recursive_mutex mu;
-  Launch launch() const { return Launch{stream, d_err}; }
+  cudaStream_t side = nullptr;           // look-ahead stream of the triangular solves
+  std::vector<cudaEvent_t> evpool;       // their ordering events
+  Launch launch() const {
+    return Launch{stream, d_err, side, const_cast<cudaEvent_t*>(evpool.data()),
+                  (int)evpool.size()};
+  }
 };
 
 namespace {
@@ -2306,6 +2313,23 @@ int bemgpu_ctx_create(int device, uint64_t hbm_budget_bytes, bemgpu_ctx** out) {
     return cuda_fail(nullptr, e, "cudaMalloc");
   }
   cudaMemset(c->d_err, 0, sizeof(int));
+  // look-ahead stream and events of the blocked triangular solves (optional: without them
+  // the solves run on the main stream alone)
+  if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) == cudaSuccess) {
+    c->evpool.resize(kEventPool, nullptr);
+    for (auto& ev : c->evpool)
+      if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) ev = nullptr;
+    if (std::any_of(c->evpool.begin(), c->evpool.end(), [](cudaEvent_t ev) { return !ev; })) {
+      for (auto& ev : c->evpool)
+        if (ev) cudaEventDestroy(ev);
+      c->evpool.clear();
+      cudaStreamDestroy(c->side);
+      c->side = nullptr;
+    }
+  } else {
+    c->side = nullptr;
+  }
+  cudaGetLastError();
   cudaDeviceSynchronize();
   *out = c;
   return BEMGPU_OK;
@@ -2321,6 +2345,11 @@ int bemgpu_ctx_destroy(bemgpu_ctx* c) {
       cudaEventDestroy(pr.second);
     }
   drop_cache(c);
+  for (auto& ev : c->evpool) cudaEventDestroy(ev);
+  if (c->side) {
+    cudaStreamSynchronize(c->side);
+    cudaStreamDestroy(c->side);
+  }
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
   cudaFree(c->d_err);

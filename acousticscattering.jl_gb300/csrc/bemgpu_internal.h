@@ -153,7 +153,10 @@ struct TrsvWork {
 #ifdef __CUDACC__
 struct Launch {
   cudaStream_t stream;
-  int* err_flag;  // device word set by bounded waits that give up
+  int* err_flag;                  // device word set by bounded waits that give up
+  cudaStream_t side = nullptr;    // second stream for overlapped work (joined before return)
+  cudaEvent_t* events = nullptr;  // event pool for the two streams' ordering
+  int n_events = 0;
 };
 
 void launch_assemble_regular(const Launch& L, const AsmInst* d_inst, int ninst, int64_t nmax,

@@ -1046,9 +1046,11 @@ constexpr size_t upd_smem_bytes() {
   return sizeof(cx<R>) * (size_t)RG * kBigB;
 }
 
+// Rows [lo, hi) (absolute, clamped to the instance: beyond its block for the lower solve,
+// before it for the upper one) are updated from the solution of block [r0, r0 + kBigB).
 template <typename R, bool EFF_LOWER, bool TRANS, int RG>
 __global__ void __launch_bounds__(256) k_trsv_big_update(const MatInst* __restrict__ insts,
-                                                         int64_t r0) {
+                                                         int64_t r0, int64_t lo, int64_t hi) {
   const MatInst& M = insts[blockIdx.z];
   const int rg0 = blockIdx.y * RG;
   const int64_t n = M.n;
@@ -1062,9 +1064,8 @@ __global__ void __launch_bounds__(256) k_trsv_big_update(const MatInst* __restri
     for (int i = threadIdx.x; i < nbs; i += blockDim.x)
       sx[r * kBigB + i] = ld<R>(M.x, (int64_t)(rg0 + r) * ldx + r0 + i);
   __syncthreads();
-  int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (EFF_LOWER) row += r0 + nbs;
-  if (EFF_LOWER ? row >= n : row >= r0) return;
+  const int64_t row = lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= hi || (EFF_LOWER ? (row < r0 + nbs || row >= n) : row >= r0)) return;
   cx<R> acc[RG];
 #pragma unroll
   for (int r = 0; r < RG; ++r) acc[r] = cx<R>{0, 0};
@@ -1096,7 +1097,7 @@ __global__ void __launch_bounds__(256) k_trsv_big_update(const MatInst* __restri
 constexpr int kTrUpRows = 32;  // rows per 256-thread CTA (8 warps x 4)
 template <typename R, bool EFF_LOWER, int RG>
 __global__ void __launch_bounds__(256) k_trsv_big_update_h(const MatInst* __restrict__ insts,
-                                                           int64_t r0) {
+                                                           int64_t r0, int64_t lo, int64_t hi) {
   const MatInst& M = insts[blockIdx.z];
   const int rg0 = blockIdx.y * RG;
   const int64_t n = M.n;
@@ -1111,10 +1112,9 @@ __global__ void __launch_bounds__(256) k_trsv_big_update_h(const MatInst* __rest
       sx[r * kBigB + i] = ld<R>(M.x, (int64_t)(rg0 + r) * ldx + r0 + i);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int64_t row0 = (int64_t)blockIdx.x * kTrUpRows + warp * 4;
-  if (EFF_LOWER) row0 += r0 + nbs;
-  const int64_t lim = EFF_LOWER ? n : r0;
-  if (row0 >= lim) return;
+  const int64_t row0 = lo + (int64_t)blockIdx.x * kTrUpRows + warp * 4;
+  const int64_t lim = min(hi, EFF_LOWER ? n : r0);
+  if (row0 >= lim || (EFF_LOWER && row0 < r0 + nbs)) return;  // lo is a multiple of 4 rows
   cx<R> acc[4][RG];
 #pragma unroll
   for (int u = 0; u < 4; ++u)
@@ -1360,7 +1360,6 @@ static void trsv_big_t(const Launch& L, const MatInst* d, int ninst, int64_t nma
   }
   // right-hand sides per update CTA: one, or a group sharing the matrix loads
   constexpr int RG = sizeof(R) == 4 ? 8 : 4;
-  const bool grouped = max_rhs >= 4;
   static bool uattr = false;
   if (!uattr) {
     cudaFuncSetAttribute(k_trsv_big_update<R, EL, TR, RG>,
@@ -1370,31 +1369,69 @@ static void trsv_big_t(const Launch& L, const MatInst* d, int ninst, int64_t nma
     uattr = true;
   }
   const int64_t nblk = (nmax + kBigB - 1) / kBigB;
-  for (int64_t b = 0; b < nblk; ++b) {
-    const int64_t blk = EL ? b : nblk - 1 - b;
-    const int64_t r0 = blk * kBigB;
-    k_trsv_diag<R, EL, TR, UN><<<dim3((unsigned)max_rhs, (unsigned)ninst), kDiagThreads, smem,
-                                 L.stream>>>(d, r0);
+  const unsigned gy = max_rhs >= 4 ? (unsigned)((max_rhs + RG - 1) / RG) : (unsigned)max_rhs;
+  auto diag = [&](cudaStream_t s, int64_t r0) {
+    k_trsv_diag<R, EL, TR, UN><<<dim3((unsigned)max_rhs, (unsigned)ninst), kDiagThreads, smem, s>>>(
+        d, r0);
     count_launch(1);
-    const int64_t rows = EL ? (nmax - r0 - kBigB) : r0;
-    if (rows > 0) {
-      const unsigned gy = grouped ? (unsigned)((max_rhs + RG - 1) / RG) : (unsigned)max_rhs;
-      if (TR) {
-        const dim3 g((unsigned)((rows + kTrUpRows - 1) / kTrUpRows), gy, (unsigned)ninst);
-        if (grouped)
-          k_trsv_big_update_h<R, EL, RG><<<g, 256, upd_smem_bytes<R, RG>(), L.stream>>>(d, r0);
-        else
-          k_trsv_big_update_h<R, EL, 1><<<g, 256, upd_smem_bytes<R, 1>(), L.stream>>>(d, r0);
-      } else {
-        const dim3 g((unsigned)((rows + 255) / 256), gy, (unsigned)ninst);
-        if (grouped)
-          k_trsv_big_update<R, EL, TR, RG><<<g, 256, upd_smem_bytes<R, RG>(), L.stream>>>(d, r0);
-        else
-          k_trsv_big_update<R, EL, TR, 1><<<g, 256, upd_smem_bytes<R, 1>(), L.stream>>>(d, r0);
-      }
-      count_launch(1);
+  };
+  auto update = [&](cudaStream_t s, int64_t r0, int64_t lo, int64_t hi) {  // rows [lo, hi)
+    if (hi <= lo) return;
+    const int64_t rows = hi - lo;
+    if (TR) {
+      const dim3 g((unsigned)((rows + kTrUpRows - 1) / kTrUpRows), gy, (unsigned)ninst);
+      if (max_rhs >= 4)
+        k_trsv_big_update_h<R, EL, RG><<<g, 256, upd_smem_bytes<R, RG>(), s>>>(d, r0, lo, hi);
+      else
+        k_trsv_big_update_h<R, EL, 1><<<g, 256, upd_smem_bytes<R, 1>(), s>>>(d, r0, lo, hi);
+    } else {
+      const dim3 g((unsigned)((rows + 255) / 256), gy, (unsigned)ninst);
+      if (max_rhs >= 4)
+        k_trsv_big_update<R, EL, TR, RG><<<g, 256, upd_smem_bytes<R, RG>(), s>>>(d, r0, lo, hi);
+      else
+        k_trsv_big_update<R, EL, TR, 1><<<g, 256, upd_smem_bytes<R, 1>(), s>>>(d, r0, lo, hi);
     }
+    count_launch(1);
+  };
+  auto block_row = [&](int64_t b) { return (EL ? b : nblk - 1 - b) * kBigB; };
+  if (!L.side || nblk < 3 || L.n_events < 2 * (int)nblk + 1) {
+    for (int64_t b = 0; b < nblk; ++b) {
+      const int64_t r0 = block_row(b);
+      diag(L.stream, r0);
+      if (EL)
+        update(L.stream, r0, r0 + kBigB, nmax);
+      else
+        update(L.stream, r0, 0, r0);
+    }
+    return;
   }
+  // Look-ahead: the main stream updates only the next block's rows and solves that block
+  // while the side stream updates every later row from the same solved block.  Both write
+  // x by read-modify-write, so the main stream's next-block update waits for the side
+  // stream's previous update (which also covered those rows), and the side stream's update
+  // waits for the block it reads.
+  cudaEvent_t* ev = L.events;
+  cudaEventRecord(ev[0], L.stream);  // the side stream starts after the main stream's work
+  cudaStreamWaitEvent(L.side, ev[0], 0);
+  diag(L.stream, block_row(0));
+  for (int64_t b = 0; b < nblk; ++b) {
+    const int64_t r0 = block_row(b);
+    cudaEvent_t e_diag = ev[1 + 2 * b], e_big = ev[2 + 2 * b];
+    cudaEventRecord(e_diag, L.stream);
+    if (b + 1 < nblk) {
+      const int64_t rn = block_row(b + 1);  // the next block in solve order
+      if (b > 0) cudaStreamWaitEvent(L.stream, ev[2 + 2 * (b - 1)], 0);
+      update(L.stream, r0, rn, rn + kBigB);
+      diag(L.stream, rn);
+    }
+    cudaStreamWaitEvent(L.side, e_diag, 0);
+    if (EL)
+      update(L.side, r0, r0 + 2 * kBigB, nmax);
+    else
+      update(L.side, r0, 0, r0 - kBigB);
+    cudaEventRecord(e_big, L.side);
+  }
+  cudaStreamWaitEvent(L.stream, ev[2 + 2 * (nblk - 1)], 0);  // join before returning
 }
 
 template <typename R>
