@@ -2818,6 +2818,31 @@ int hm_build(bemgpu_ctx* c, MeshData* m, const bemgpu_problem& p, int kind,
   TRY(upload(c, dn, &H->dn));
   TRY(alloc(c, (size_t)std::max<int64_t>(1, off) * es, &H->D1));
   TRY(alloc(c, (size_t)std::max<int64_t>(1, off) * es, &H->D2));
+  // U and V were allocated at the rank cap: move the ranks reached into tight pools
+  for (int op = 0; op < 2; ++op) {
+    std::vector<HmCopy> cu, cv;
+    int64_t tu = 0, tv = 0;
+    const int64_t w = (int64_t)es / 8;  // 8-byte words per complex entry
+    for (HmLR& B : keep[op]) {
+      const int64_t mu = (int64_t)B.m * B.rank, nv = (int64_t)B.n * B.rank;
+      if (mu > 0) cu.push_back(HmCopy{B.uoff * w, tu * w, mu * w});
+      if (nv > 0) cv.push_back(HmCopy{B.voff * w, tv * w, nv * w});
+      B.uoff = tu;
+      B.voff = tv;
+      tu += mu;
+      tv += nv;
+    }
+    Buf ut, vt, dcu, dcv;
+    TRY(alloc(c, (size_t)std::max<int64_t>(1, tu) * es, &ut));
+    TRY(alloc(c, (size_t)std::max<int64_t>(1, tv) * es, &vt));
+    TRY(upload(c, cu, &dcu));
+    TRY(upload(c, cv, &dcv));
+    launch_hm_compact(L, dcu.as<HmCopy>(), (int32_t)cu.size(), H->U[op].p, ut.p);
+    launch_hm_compact(L, dcv.as<HmCopy>(), (int32_t)cv.size(), H->V[op].p, vt.p);
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // the capacity pools are released next
+    H->U[op] = std::move(ut);
+    H->V[op] = std::move(vt);
+  }
   for (int op = 0; op < 2; ++op) TRY(upload(c, keep[op], &H->lr[op]));
   {
     Prof pr(c, "hm_dense");

@@ -282,6 +282,22 @@ void launch_hm_aca(const Launch& L, HmLR* lr, int32_t n_lr, int32_t max_m, void*
   count_launch(1);
 }
 
+// ------------------------------------------------------------------ pool compaction
+__global__ void __launch_bounds__(256) k_hm_compact(const HmCopy* __restrict__ cp,
+                                                    const uint2* __restrict__ src,
+                                                    uint2* __restrict__ dst) {
+  const HmCopy c = cp[blockIdx.x];
+  for (int64_t w = threadIdx.x; w < c.words; w += blockDim.x) dst[c.dst + w] = src[c.src + w];
+}
+
+void launch_hm_compact(const Launch& L, const HmCopy* d, int32_t count, const void* src,
+                       void* dst) {
+  if (count <= 0) return;
+  k_hm_compact<<<(unsigned)count, 256, 0, L.stream>>>(d, static_cast<const uint2*>(src),
+                                                        static_cast<uint2*>(dst));
+  count_launch(1);
+}
+
 // ------------------------------------------------------------------ full blocks
 template <typename R, int KIND>
 __global__ void __launch_bounds__(256) k_hm_dense(const HmDense* __restrict__ dn, void* D1,

@@ -102,6 +102,13 @@ struct GmWork {
 void launch_hm_aca(const Launch& L, HmLR* lr, int32_t n_lr, int32_t max_m, void* U, void* V,
                    const void* recs, bool f32, const int32_t* perm, int kind, int op, double k,
                    double a_re, double a_im, double tol);
+// One contiguous copy per descriptor (the first rank columns of a block's U or V moved into
+// pools sized by the ranks reached); sizes and offsets in 8-byte words.
+struct HmCopy {
+  int64_t src, dst, words;
+};
+void launch_hm_compact(const Launch& L, const HmCopy* d, int32_t count, const void* src,
+                       void* dst);
 // Regular-rule entries of the full blocks of both operators (self pairs left to the near
 // kernel, which writes them through AsmInst.near_dst), precision as launch_hm_aca.
 void launch_hm_dense(const Launch& L, const HmDense* dn, int32_t n_dense, void* D1, void* D2,
