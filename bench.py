@@ -701,7 +701,8 @@ def run_config5(args):
     cross approximation, full blocks, GMRES and far field every step), complex64/FP32
     operators (precision=:mixed) and complex128 (precision=:double); TS against the dense
     refined solve of the same incidence; an 81920-panel body as the size the dense path
-    cannot reach in comparable time."""
+    cannot reach in comparable time, and a 327680-panel one whose dense system (860 GB)
+    does not fit one GPU."""
     import bemgpu
     from bemgpu import meshes
     ctx = bemgpu.Context(0)
@@ -763,6 +764,18 @@ def run_config5(args):
     big_ms = ctx.timer_stop()
     big_st = sb.hmatrix_stats()
     sb.close()
+    # 327680 panels, the same body: beyond one GPU's memory as a dense system (860 GB)
+    n3, t3 = meshes.uv_spheroid(0.1, 0.025, 512, 320)
+    huge = bemgpu.mesh(n3, t3)
+    bemgpu.bem(huge, bemgpu.Rigid(), k, compression=hm, gmres_kwargs=gk, precision="mixed",
+               ctx=ctx).close()
+    ctx.timer_start()
+    sh = bemgpu.bem(huge, bemgpu.Rigid(), k, compression=hm, gmres_kwargs=gk, precision="mixed",
+                    ctx=ctx)
+    huge_ms = ctx.timer_stop()
+    huge_st, huge_d = sh.hmatrix_stats(), sh.diagnostics()
+    huge_ts = 20 * math.log10(abs(bemgpu.scattering_amplitude(sh)))
+    sh.close()
     m = out["mixed"]
     st = m["stats"]
     hbm, _, which = measured_peaks()
@@ -806,6 +819,11 @@ def run_config5(args):
         large={"panels": int(np.asarray(t2).shape[1]), "ms": big_ms,
                "compression": big_st["compression"], "gmres_iterations": big_st["gmres_iterations"],
                "dense_complex64_bytes": int(np.asarray(t2).shape[1]) ** 2 * 8},
+        huge={"panels": int(np.asarray(t3).shape[1]), "ms": huge_ms,
+              "device_bytes": huge_d["device_bytes"], "compression": huge_st["compression"],
+              "gmres_iterations": huge_st["gmres_iterations"],
+              "gmres_converged": bool(huge_st["gmres_converged"]), "ts_db": huge_ts,
+              "dense_complex64_bytes": int(np.asarray(t3).shape[1]) ** 2 * 8},
         roofline={"bound": "hbm", "kernel": "hierarchical product (k_hm_vt, k_hm_lblk, "
                                             "k_hm_dblk, k_hm_gather)",
                   "achieved": achieved, "peak": hbm, "unit": "GB/s",
