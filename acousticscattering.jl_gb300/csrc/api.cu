@@ -2734,8 +2734,9 @@ int hm_build(bemgpu_ctx* c, MeshData* m, const bemgpu_problem& p, int kind,
   const double a_re = 0.0, a_im = kind == kAsmBM ? 1.0 / k : 0.0;  // alpha = i / k
   // admissible blocks: rank capacity below the size where a full block is cheaper
   std::vector<HmLR> lr(P.lowrank.size());
+  std::vector<int32_t> normal, large;  // 256- or 512-thread CTAs
   int64_t uo = 0, vo = 0, to = 0;
-  int32_t max_m = 1;
+  int32_t max_m = 1, max_m_large = 1;
   for (size_t b = 0; b < lr.size(); ++b) {
     const HmBlock& B = P.lowrank[b];
     const int64_t cap = (int64_t)B.m * B.n / ((int64_t)B.m + B.n);
@@ -2744,8 +2745,17 @@ int hm_build(bemgpu_ctx* c, MeshData* m, const bemgpu_problem& p, int kind,
     uo += (int64_t)B.m * kmax;
     vo += (int64_t)B.n * kmax;
     to += kmax;
-    max_m = std::max(max_m, B.m);
+    if (B.m + B.n >= kHmAcaLarge) {
+      large.push_back((int32_t)b);
+      max_m_large = std::max(max_m_large, B.m);
+    } else {
+      normal.push_back((int32_t)b);
+      max_m = std::max(max_m, B.m);
+    }
   }
+  Buf d_normal, d_large;
+  TRY(upload(c, normal, &d_normal));
+  TRY(upload(c, large, &d_large));
   std::vector<HmLR> lrh[2];
   for (int op = 0; op < 2; ++op) {
     TRY(upload(c, lr, &H->lr[op]));
@@ -2753,8 +2763,10 @@ int hm_build(bemgpu_ctx* c, MeshData* m, const bemgpu_problem& p, int kind,
     TRY(alloc(c, (size_t)std::max<int64_t>(1, vo) * es, &H->V[op]));
     {
       Prof pr(c, "hm_aca");
-      launch_hm_aca(L, H->lr[op].as<HmLR>(), (int32_t)lr.size(), max_m, H->U[op].p, H->V[op].p,
-                    recs, H->f32, H->pc->perm.as<int32_t>(), kind, op, k, a_re, a_im, o.tol);
+      launch_hm_aca(L, H->lr[op].as<HmLR>(), d_normal.as<int32_t>(), (int32_t)normal.size(),
+                    max_m, d_large.as<int32_t>(), (int32_t)large.size(), max_m_large,
+                    H->U[op].p, H->V[op].p, recs, H->f32, H->pc->perm.as<int32_t>(), kind, op, k,
+                    a_re, a_im, o.tol);
     }
     CUDA_TRY(c, cudaGetLastError());
   }

@@ -116,8 +116,9 @@ __device__ __forceinline__ cx<R> ldv(const void* p, int64_t i) {
 constexpr int kAcaT = 256;
 constexpr int kAcaW = kAcaT / 32;
 
-// block-wide argmax (largest value, then smallest index); every thread gets the result
-template <typename V>
+// block-wide argmax over NW warps (largest value, then smallest index); every thread gets
+// the result
+template <int NW, typename V>
 __device__ __forceinline__ void block_argmax(V& v, int32_t& i, V* rv, int32_t* ri) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -134,19 +135,23 @@ __device__ __forceinline__ void block_argmax(V& v, int32_t& i, V* rv, int32_t* r
   __syncthreads();
   v = rv[0];
   i = ri[0];
-  for (int q = 1; q < kAcaW; ++q) amax(v, i, rv[q], ri[q]);
+  for (int q = 1; q < NW; ++q) amax(v, i, rv[q], ri[q]);
 }
 
 }  // namespace
 
 // ------------------------------------------------------------------ cross approximation
-template <typename R, int KIND, int OP>
-__global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, void* Up, void* Vp,
-                                                  const R* __restrict__ recs,
-                                                  const int32_t* __restrict__ perm, double k_,
-                                                  double a_re, double a_im, double tol) {
+// NT threads per CTA (512 for the largest blocks, whose serial rank steps set the
+// kernel's duration; 256 otherwise); list: the blocks of this launch.
+template <typename R, int KIND, int OP, int NT>
+__global__ void __launch_bounds__(NT) k_hm_aca(HmLR* __restrict__ lrs,
+                                              const int32_t* __restrict__ list, void* Up,
+                                              void* Vp, const R* __restrict__ recs,
+                                              const int32_t* __restrict__ perm, double k_,
+                                              double a_re, double a_im, double tol) {
   using C = cx<R>;
-  HmLR& B = lrs[blockIdx.x];
+  constexpr int NW = NT / 32;
+  HmLR& B = lrs[list[blockIdx.x]];
   const int m = B.m, n = B.n, kmax = B.kmax;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   C* U = static_cast<C*>(Up) + B.uoff;
@@ -156,15 +161,15 @@ __global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, void* 
   const C al = {(R)a_re, (R)a_im};
   const R k = (R)k_;
   extern __shared__ uint32_t used[];  // pivot rows taken, (m + 31) / 32 words
-  __shared__ R rv[kAcaW];
-  __shared__ int32_t ri[kAcaW];
+  __shared__ R rv[NW];
+  __shared__ int32_t ri[NW];
   __shared__ C su[kHmMaxRank], sv[kHmMaxRank];    // U[i*, l], V[j*, l]
   __shared__ C cu[kHmMaxRank], cv[kHmMaxRank];    // projections of the new cross
   __shared__ C s_piv;
   __shared__ double s_s2;
   __shared__ int s_stop;
   const int words = (m + 31) >> 5;
-  for (int w = tid; w < words; w += kAcaT) used[w] = 0u;
+  for (int w = tid; w < words; w += NT) used[w] = 0u;
   if (tid == 0) s_s2 = 0.0;
   int rank = 0, conv = 0;
   int32_t istar = 0;
@@ -177,22 +182,22 @@ __global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, void* 
     R bv = -1;
     int32_t bj = INT32_MAX;
     const int32_t pi = prow[istar];
-    for (int j = tid; j < n; j += kAcaT) {
+    for (int j = tid; j < n; j += NT) {
       C v = hm_entry<R, KIND, OP>(recs, pi, pcol[j], k, al);
       for (int l = 0; l < rank; ++l) v -= su[l] * V[j + (int64_t)l * n];
       V[j + (int64_t)rank * n] = v;
       amax(bv, bj, v.x * v.x + v.y * v.y, j);
     }
-    block_argmax(bv, bj, rv, ri);
+    block_argmax<NW>(bv, bj, rv, ri);
     if (!(bv > 0)) {  // the residual row vanishes: continue from the next unused row
       R fv = -1;
       int32_t fi = INT32_MAX;
-      for (int i = tid; i < m; i += kAcaT)
+      for (int i = tid; i < m; i += NT)
         if (!((used[i >> 5] >> (i & 31)) & 1u)) {
           amax(fv, fi, (R)1, i);
           break;
         }
-      block_argmax(fv, fi, rv, ri);
+      block_argmax<NW>(fv, fi, rv, ri);
       if (fv < 0) {  // every row was a pivot row: the approximation is exact
         conv = 1;
         break;
@@ -210,16 +215,16 @@ __global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, void* 
     R cb = -1;
     int32_t ci = INT32_MAX;
     const int32_t pj = pcol[jstar];
-    for (int i = tid; i < m; i += kAcaT) {
+    for (int i = tid; i < m; i += NT) {
       C u = hm_entry<R, KIND, OP>(recs, prow[i], pj, k, al);
       for (int l = 0; l < rank; ++l) u -= U[i + (int64_t)l * m] * sv[l];
       U[i + (int64_t)rank * m] = u;
       if (!((used[i >> 5] >> (i & 31)) & 1u)) amax(cb, ci, u.x * u.x + u.y * u.y, i);
     }
-    for (int j = tid; j < n; j += kAcaT) V[j + (int64_t)rank * n] = V[j + (int64_t)rank * n] * inv;
+    for (int j = tid; j < n; j += NT) V[j + (int64_t)rank * n] = V[j + (int64_t)rank * n] * inv;
     __syncthreads();
     // projections U_l^H U_r and V_l^H V_r, l = 0..rank (one warp per l, fixed order)
-    for (int l = wid; l <= rank; l += kAcaW) {
+    for (int l = wid; l <= rank; l += NW) {
       C a = {0, 0}, b = {0, 0};
       for (int i = lane; i < m; i += 32)
         a += cconjmul(U[i + (int64_t)l * m], U[i + (int64_t)rank * m]);
@@ -232,7 +237,7 @@ __global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, void* 
         cv[l] = b;
       }
     }
-    block_argmax(cb, ci, rv, ri);
+    block_argmax<NW>(cb, ci, rv, ri);
     if (tid == 0) {
       // |S_r|^2 = |S_{r-1}|^2 + |u_r|^2 |v_r|^2 + 2 Re sum_{l<r} (U_l^H u_r)(V_l^H v_r)
       const double uv2 = (double)cu[rank].x * (double)cv[rank].x;
@@ -256,30 +261,54 @@ __global__ void __launch_bounds__(kAcaT) k_hm_aca(HmLR* __restrict__ lrs, void* 
   }
 }
 
-void launch_hm_aca(const Launch& L, HmLR* lr, int32_t n_lr, int32_t max_m, void* U, void* V,
-                   const void* recs, bool f32, const int32_t* perm, int kind, int op, double k,
-                   double a_re, double a_im, double tol) {
-  if (n_lr <= 0) return;
-  const size_t smem = (size_t)((max_m + 31) / 32) * 4;
-  auto go = [&](auto kern, auto rec) {
-    if (smem > 48 * 1024)
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<(unsigned)n_lr, kAcaT, smem, L.stream>>>(lr, U, V, rec, perm, k, a_re, a_im, tol);
+void launch_hm_aca(const Launch& L, HmLR* lr, const int32_t* normal, int32_t n_normal,
+                   int32_t max_m, const int32_t* large, int32_t n_large, int32_t max_m_large,
+                   void* U, void* V, const void* recs, bool f32, const int32_t* perm, int kind,
+                   int op, double k, double a_re, double a_im, double tol) {
+  // the large blocks' launch runs beside the others (on the side stream when there is one):
+  // its few long CTAs are the critical path, the many short ones fill the GPU around them
+  const bool two = L.side && L.n_events >= 2 && n_large > 0 && n_normal > 0;
+  const cudaStream_t sl = two ? L.side : L.stream;
+  if (two) {
+    cudaEventRecord(L.events[0], L.stream);
+    cudaStreamWaitEvent(L.side, L.events[0], 0);
+  }
+  auto go = [&](auto kern, auto kern_l, auto rec) {
+    const size_t smem = (size_t)((max_m + 31) / 32) * 4;
+    const size_t smem_l = (size_t)((max_m_large + 31) / 32) * 4;
+    if (n_large > 0) {
+      if (smem_l > 48 * 1024)
+        cudaFuncSetAttribute(kern_l, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_l);
+      kern_l<<<(unsigned)n_large, 2 * kAcaT, smem_l, sl>>>(lr, large, U, V, rec, perm, k, a_re,
+                                                           a_im, tol);
+      count_launch(1);
+    }
+    if (n_normal > 0) {
+      if (smem > 48 * 1024)
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      kern<<<(unsigned)n_normal, kAcaT, smem, L.stream>>>(lr, normal, U, V, rec, perm, k, a_re,
+                                                         a_im, tol);
+      count_launch(1);
+    }
   };
   const float* rf = static_cast<const float*>(recs);
   const double* rd = static_cast<const double*>(recs);
+  constexpr int T1 = kAcaT, T2 = 2 * kAcaT;
   const int sel = (f32 ? 4 : 0) + (kind == kAsmBM ? 2 : 0) + op;
   switch (sel) {
-    case 0: go(k_hm_aca<double, kAsmCBIE, 0>, rd); break;
-    case 1: go(k_hm_aca<double, kAsmCBIE, 1>, rd); break;
-    case 2: go(k_hm_aca<double, kAsmBM, 0>, rd); break;
-    case 3: go(k_hm_aca<double, kAsmBM, 1>, rd); break;
-    case 4: go(k_hm_aca<float, kAsmCBIE, 0>, rf); break;
-    case 5: go(k_hm_aca<float, kAsmCBIE, 1>, rf); break;
-    case 6: go(k_hm_aca<float, kAsmBM, 0>, rf); break;
-    default: go(k_hm_aca<float, kAsmBM, 1>, rf); break;
+    case 0: go(k_hm_aca<double, kAsmCBIE, 0, T1>, k_hm_aca<double, kAsmCBIE, 0, T2>, rd); break;
+    case 1: go(k_hm_aca<double, kAsmCBIE, 1, T1>, k_hm_aca<double, kAsmCBIE, 1, T2>, rd); break;
+    case 2: go(k_hm_aca<double, kAsmBM, 0, T1>, k_hm_aca<double, kAsmBM, 0, T2>, rd); break;
+    case 3: go(k_hm_aca<double, kAsmBM, 1, T1>, k_hm_aca<double, kAsmBM, 1, T2>, rd); break;
+    case 4: go(k_hm_aca<float, kAsmCBIE, 0, T1>, k_hm_aca<float, kAsmCBIE, 0, T2>, rf); break;
+    case 5: go(k_hm_aca<float, kAsmCBIE, 1, T1>, k_hm_aca<float, kAsmCBIE, 1, T2>, rf); break;
+    case 6: go(k_hm_aca<float, kAsmBM, 0, T1>, k_hm_aca<float, kAsmBM, 0, T2>, rf); break;
+    default: go(k_hm_aca<float, kAsmBM, 1, T1>, k_hm_aca<float, kAsmBM, 1, T2>, rf); break;
   }
-  count_launch(1);
+  if (two) {  // join
+    cudaEventRecord(L.events[1], L.side);
+    cudaStreamWaitEvent(L.stream, L.events[1], 0);
+  }
 }
 
 // ------------------------------------------------------------------ pool compaction

@@ -99,9 +99,13 @@ struct GmWork {
 #ifdef __CUDACC__
 // Cross approximation of every admissible block of op (0: M1, 1: M2 of the assembly
 // kind); f32: FP32 entries (records: FP32 panel records) into complex64 U, V, else FP64.
-void launch_hm_aca(const Launch& L, HmLR* lr, int32_t n_lr, int32_t max_m, void* U, void* V,
-                   const void* recs, bool f32, const int32_t* perm, int kind, int op, double k,
-                   double a_re, double a_im, double tol);
+// normal / large: the blocks for 256- and 512-thread CTAs (large: m + n >= kHmAcaLarge),
+// max_m / max_m_large their largest row counts.
+constexpr int kHmAcaLarge = 1024;
+void launch_hm_aca(const Launch& L, HmLR* lr, const int32_t* normal, int32_t n_normal,
+                   int32_t max_m, const int32_t* large, int32_t n_large, int32_t max_m_large,
+                   void* U, void* V, const void* recs, bool f32, const int32_t* perm, int kind,
+                   int op, double k, double a_re, double a_im, double tol);
 // One contiguous copy per descriptor (the first rank columns of a block's U or V moved into
 // pools sized by the ranks reached); sizes and offsets in 8-byte words.
 struct HmCopy {
