@@ -209,11 +209,24 @@ __device__ __forceinline__ int32_t ld_peer_s32(uint32_t a) {
   asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
   return v;
 }
-__device__ __forceinline__ void better32(float& bv, int32_t& bi, float ov, int32_t oi) {
+template <typename V>
+__device__ __forceinline__ void better32(V& bv, int32_t& bi, V ov, int32_t oi) {
   if (ov > bv || (ov == bv && oi < bi)) {
     bv = ov;
     bi = oi;
   }
+}
+__device__ __forceinline__ double ld_peer_f64(uint32_t a) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(a) : "memory");
+  return v;
+}
+template <typename R>
+__device__ __forceinline__ R ld_peer_real(uint32_t a) {
+  if constexpr (sizeof(R) == 8)
+    return ld_peer_f64(a);
+  else
+    return ld_peer_f32(a);
 }
 __device__ __forceinline__ long long ld_peer_s64(uint32_t a) {
   long long v;
@@ -228,39 +241,36 @@ __device__ __forceinline__ void better(float& bv, int64_t& bi, float ov, int64_t
   }
 }
 
-template <int CS>
-__global__ void __launch_bounds__(kGetf2T) k_getf2_ll(const MatInst* __restrict__ insts,
-                                                      int64_t k0, int nb) {
-  constexpr int T = kGetf2T;
+template <typename R, int CS, int T, int BATCH>
+__global__ void __launch_bounds__(T) k_getf2_ll(const MatInst* __restrict__ insts, int64_t k0,
+                                                int nb) {
+  using C = cx<R>;
   const unsigned rank = CS > 1 ? cluster_rank() : 0u;
   const MatInst& M = insts[blockIdx.x / CS];
   const int64_t n = M.n;
   if (!M.active || k0 >= n) return;  // the whole cluster (one instance) leaves together
   const int nbe = (int)min((int64_t)nb, n - k0);
   const int64_t lda = M.lda;
-  float2* A = static_cast<float2*>(M.a);
-  __shared__ cf sL[kPanelNB][kPanelNB + 1];  // finished L11 rows
-  __shared__ cf su[kPanelNB];                // U[0:c, c]
-  __shared__ float w_val[T / 32];
-  __shared__ int32_t w_idx[T / 32];          // rows as int32 (orders below 2^31)
-  __shared__ float c_val;                    // this CTA's pivot candidate
+  void* A = M.a;
+  __shared__ C sL[kPanelNB][kPanelNB + 1];  // finished L11 rows
+  __shared__ C su[kPanelNB];                // U[0:c, c]
+  __shared__ R w_val[T / 32];
+  __shared__ int32_t w_idx[T / 32];         // rows as int32 (orders below 2^31)
+  __shared__ R c_val;                       // this CTA's pivot candidate
   __shared__ int32_t c_idx;
-  __shared__ cf s_inv;
+  __shared__ C s_inv;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int64_t g = (int64_t)rank * T + tid;
   constexpr int64_t stride = (int64_t)CS * T;
-  cf inv_prev = {1.f, 0.f};
+  C inv_prev = {(R)1, (R)0};
   for (int c = 0; c < nbe; ++c) {
     const int64_t col = k0 + c;
     // (1) u = L11[0:c, 0:c]^{-1} a[k0:k0+c, col] (identical in every CTA)
     if (wid == 0) {
-      cf x = {0.f, 0.f};
-      if (lane < c) {
-        const float2 v = A[(k0 + lane) + col * lda];
-        x = cf{v.x, v.y};
-      }
+      C x = {(R)0, (R)0};
+      if (lane < c) x = ld<R>(A, (k0 + lane) + col * lda);
       for (int i = 0; i + 1 < c; ++i) {
-        cf ui;
+        C ui;
         ui.x = __shfl_sync(0xffffffffu, x.x, i);
         ui.y = __shfl_sync(0xffffffffu, x.y, i);
         if (lane > i && lane < c) x -= sL[lane][i] * ui;
@@ -270,40 +280,36 @@ __global__ void __launch_bounds__(kGetf2T) k_getf2_ll(const MatInst* __restrict_
     }
     __syncthreads();
     // (2) rows >= col: finish L[., c - 1], update column c, pivot candidate
-    float best = -1.f;
+    R best = (R)-1;
     int32_t bidx = INT32_MAX;
     int64_t r = k0 + g;
     if (r < col) r += ((col - r + stride - 1) / stride) * stride;
     for (; r < n; r += stride) {
-      const float2 av = A[r + col * lda];
-      cf acc = {av.x, av.y};
-      for (int j0 = 0; j0 < c; j0 += kLLBatch) {
-        cf lv[kLLBatch];
+      C acc = ld<R>(A, r + col * lda);
+      for (int j0 = 0; j0 < c; j0 += BATCH) {
+        C lv[BATCH];
 #pragma unroll
-        for (int e = 0; e < kLLBatch; ++e) {
-          lv[e] = cf{0.f, 0.f};
-          if (j0 + e < c) {
-            const float2 v = A[r + (k0 + j0 + e) * lda];
-            lv[e] = cf{v.x, v.y};
-          }
+        for (int e = 0; e < BATCH; ++e) {
+          lv[e] = C{(R)0, (R)0};
+          if (j0 + e < c) lv[e] = ld<R>(A, r + (k0 + j0 + e) * lda);
         }
 #pragma unroll
-        for (int e = 0; e < kLLBatch; ++e) {
+        for (int e = 0; e < BATCH; ++e) {
           if (j0 + e < c) {
             if (j0 + e == c - 1) {
               lv[e] = lv[e] * inv_prev;
-              A[r + (k0 + j0 + e) * lda] = make_float2(lv[e].x, lv[e].y);
+              st<R>(A, r + (k0 + j0 + e) * lda, lv[e]);
             }
             acc -= lv[e] * su[j0 + e];
           }
         }
       }
-      A[r + col * lda] = make_float2(acc.x, acc.y);
+      st<R>(A, r + col * lda, acc);
       better32(best, bidx, cabs1(acc), (int32_t)r);
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-      const float ov = __shfl_down_sync(0xffffffffu, best, off);
+      const R ov = __shfl_down_sync(0xffffffffu, best, off);
       const int32_t oi = __shfl_down_sync(0xffffffffu, bidx, off);
       better32(best, bidx, ov, oi);
     }
@@ -313,11 +319,11 @@ __global__ void __launch_bounds__(kGetf2T) k_getf2_ll(const MatInst* __restrict_
     }
     __syncthreads();
     if (wid == 0) {  // the CTA's candidate: a shuffle tree over the 32 warps' candidates
-      float bv = w_val[lane];
-      int32_t bi = w_idx[lane];
+      R bv = lane < T / 32 ? w_val[lane] : (R)-1;
+      int32_t bi = lane < T / 32 ? w_idx[lane] : INT32_MAX;
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {
-        const float ov = __shfl_xor_sync(0xffffffffu, bv, off);
+        const R ov = __shfl_xor_sync(0xffffffffu, bv, off);
         const int32_t oi = __shfl_xor_sync(0xffffffffu, bi, off);
         better32(bv, bi, ov, oi);
       }
@@ -332,12 +338,12 @@ __global__ void __launch_bounds__(kGetf2T) k_getf2_ll(const MatInst* __restrict_
       cluster_sync_all();
     else
       __syncthreads();
-    float pv = -1.f;
+    R pv = (R)-1;
     int32_t piv32 = INT32_MAX;
     if (wid == 0) {  // one lane per CTA of the cluster, all peer loads in flight
       if (lane < CS) {
         if (CS > 1 && (unsigned)lane != rank) {
-          pv = ld_peer_f32(peer_smem(&c_val, (unsigned)lane));
+          pv = ld_peer_real<R>(peer_smem(&c_val, (unsigned)lane));
           piv32 = ld_peer_s32(peer_smem(&c_idx, (unsigned)lane));
         } else {
           pv = c_val;
@@ -346,25 +352,25 @@ __global__ void __launch_bounds__(kGetf2T) k_getf2_ll(const MatInst* __restrict_
       }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {  // every lane gets the cluster's pivot
-        const float ov = __shfl_xor_sync(0xffffffffu, pv, off);
+        const R ov = __shfl_xor_sync(0xffffffffu, pv, off);
         const int32_t oi = __shfl_xor_sync(0xffffffffu, piv32, off);
         better32(pv, piv32, ov, oi);
       }
     }
     int64_t piv = piv32;
     if (piv >= n) piv = col;  // no candidate rows (cannot happen for col < n)
-    const bool nonzero = pv > 0.f;
+    const bool nonzero = pv > (R)0;
     if (rank == 0) {
-      if (tid < c) A[(k0 + tid) + col * lda] = make_float2(su[tid].x, su[tid].y);
+      if (tid < c) st<R>(A, (k0 + tid) + col * lda, su[tid]);
       if (tid == 0) {
         M.ipiv[col] = (int32_t)piv;
         if (!nonzero && *M.info == 0) *M.info = (int32_t)(col + 1);
       }
       if (piv != col && tid < nbe) {  // interchange over the panel's columns
         const int64_t cc = k0 + tid;
-        const float2 a = A[col + cc * lda], b = A[piv + cc * lda];
-        A[col + cc * lda] = b;
-        A[piv + cc * lda] = a;
+        const C a = ld<R>(A, col + cc * lda), b = ld<R>(A, piv + cc * lda);
+        st<R>(A, col + cc * lda, b);
+        st<R>(A, piv + cc * lda, a);
       }
     }
     if (CS > 1)
@@ -372,14 +378,8 @@ __global__ void __launch_bounds__(kGetf2T) k_getf2_ll(const MatInst* __restrict_
     else
       __syncthreads();
     // (4) reciprocal of the pivot; cache the finished row of L11
-    if (tid < c) {
-      const float2 v = A[col + (k0 + tid) * lda];
-      sL[c][tid] = cf{v.x, v.y};
-    }
-    if (tid == 0) {
-      const float2 p = A[col + col * lda];
-      s_inv = nonzero ? cinv(cf{p.x, p.y}) : cf{1.f, 0.f};
-    }
+    if (tid < c) sL[c][tid] = ld<R>(A, col + (k0 + tid) * lda);
+    if (tid == 0) s_inv = nonzero ? cinv(ld<R>(A, col + col * lda)) : C{(R)1, (R)0};
     __syncthreads();
     inv_prev = s_inv;
   }
@@ -387,11 +387,7 @@ __global__ void __launch_bounds__(kGetf2T) k_getf2_ll(const MatInst* __restrict_
   const int64_t colL = k0 + nbe - 1;
   int64_t r = k0 + g;
   if (r <= colL) r += ((colL + 1 - r + stride - 1) / stride) * stride;
-  for (; r < n; r += stride) {
-    const float2 v = A[r + colL * lda];
-    const cf l = cf{v.x, v.y} * inv_prev;
-    A[r + colL * lda] = make_float2(l.x, l.y);
-  }
+  for (; r < n; r += stride) st<R>(A, r + colL * lda, ld<R>(A, r + colL * lda) * inv_prev);
 }
 
 // ------------------------------------------------------------------ laswp
@@ -492,15 +488,21 @@ __global__ void __launch_bounds__(kSwpWarps * 32) k_laswp(const MatInst* __restr
 
 // ------------------------------------------------------------------ trsm (U12)
 // U12 = L11^{-1} A12 for the columns [c_lo, min(c_hi, n)); L11 = unit lower nbe x nbe
-// block at (k0, k0), staged once per CTA in shared memory; each warp solves kTrsmCols
+// block at (k0, k0), staged once per CTA in shared memory; each warp solves TrsmCols<R>
 // columns (column = warp + kTrsmWarps * t), lane r holding rows r, r + 32, ...
+// complex128 takes fewer columns per warp: its FP64 solve is about 8x slower per column,
+// and more CTAs spread the few trailing columns of small orders over the SMs.
 constexpr int kTrsmWarps = 8;
-constexpr int kTrsmCols = 16;
+template <typename R>
+struct TrsmCols {
+  static constexpr int value = sizeof(R) == 4 ? 16 : 2;
+};
 
 template <typename R, int NB>
 __global__ void __launch_bounds__(kTrsmWarps * 32) k_trsm_panel(const MatInst* __restrict__ insts,
                                                                int64_t k0, int64_t c_lo,
                                                                int64_t c_hi) {
+  constexpr int kTrsmCols = TrsmCols<R>::value;
   const MatInst& M = insts[blockIdx.y];
   const int64_t n = M.n;
   if (!M.active || k0 >= n) return;
@@ -1226,11 +1228,19 @@ static int getf2_cluster(int ninst) {
   return cs;
 }
 
-template <int CS>
+// complex64: 1024 threads, 16 L values in flight per row; complex128: 512 threads and 8
+// (the 64-register budget of 1024 threads would spill the FP64 values)
+template <typename R>
+struct LLCfg {
+  static constexpr int kT = sizeof(R) == 4 ? kGetf2T : kGetf2T / 2;
+  static constexpr int kBatch = sizeof(R) == 4 ? kLLBatch : kLLBatch / 2;
+};
+
+template <typename R, int CS>
 static void getf2_ll_t(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(ninst * CS));
-  cfg.blockDim = dim3(kGetf2T);
+  cfg.blockDim = dim3(LLCfg<R>::kT);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = L.stream;
   cudaLaunchAttribute at[1];
@@ -1240,19 +1250,25 @@ static void getf2_ll_t(const Launch& L, const MatInst* d, int ninst, int64_t k0,
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k_getf2_ll<CS>, d, k0, nb);
+  cudaLaunchKernelEx(&cfg, k_getf2_ll<R, CS, LLCfg<R>::kT, LLCfg<R>::kBatch>, d, k0, nb);
 }
 
 void launch_getf2(const Launch& L, const MatInst* d, int ninst, int64_t k0, int nb, int prec,
                   int cs) {
+  // left-looking, one thread-block cluster per instance
+  const int csel = cs > 0 ? cs : getf2_cluster(ninst);
   if (prec_is_single(prec)) {
-    switch (cs > 0 ? cs : getf2_cluster(ninst)) {  // left-looking, one cluster per instance
-      case 8: getf2_ll_t<8>(L, d, ninst, k0, nb); break;
-      case 4: getf2_ll_t<4>(L, d, ninst, k0, nb); break;
-      default: getf2_ll_t<2>(L, d, ninst, k0, nb); break;
+    switch (csel) {
+      case 8: getf2_ll_t<float, 8>(L, d, ninst, k0, nb); break;
+      case 4: getf2_ll_t<float, 4>(L, d, ninst, k0, nb); break;
+      default: getf2_ll_t<float, 2>(L, d, ninst, k0, nb); break;
     }
   } else {
-    k_getf2<double><<<ninst, Getf2Cfg<double>::kThreads, 0, L.stream>>>(d, k0, nb);
+    switch (csel) {
+      case 8: getf2_ll_t<double, 8>(L, d, ninst, k0, nb); break;
+      case 4: getf2_ll_t<double, 4>(L, d, ninst, k0, nb); break;
+      default: getf2_ll_t<double, 2>(L, d, ninst, k0, nb); break;
+    }
   }
   count_launch(1);
 }
@@ -1284,7 +1300,7 @@ static void trsm_t(const Launch& L, const MatInst* d, int ninst, int64_t k0, int
                          (int)smem);
     attr = true;
   }
-  const int64_t per = (int64_t)kTrsmWarps * kTrsmCols;
+  const int64_t per = (int64_t)kTrsmWarps * TrsmCols<R>::value;
   dim3 grid((unsigned)((c_hi - c_lo + per - 1) / per), (unsigned)ninst);
   k_trsm_panel<R, NB><<<grid, kTrsmWarps * 32, smem, L.stream>>>(d, k0, c_lo, c_hi);
   count_launch(1);
