@@ -16,6 +16,8 @@ RIGID, PRESSURE_RELEASE, FLUID = 0, 1, 2
 FORMULATION_DEFAULT, BURTON_MILLER, CBIE, MULLER = -1, 0, 1, 2
 DOUBLE, MIXED = 0, 1
 ASSEMBLY = {None: 0, "default": 0, "double": 1, "single": 2}
+DISCRETIZATION = {"collocation": 0, "nystrom": 1}
+NODES_PER_PANEL = {"collocation": 1, "nystrom": 7}
 REASONS = ("none", "conversion", "single_singular", "condition", "nonfinite",
            "iteration_limit", "stagnation")
 FIELDS = {"total": 0, "scattered": 1, "incident": 2, "interior": 3}
@@ -28,7 +30,8 @@ class Problem(ctypes.Structure):
                 ("soundspeed_contrast", ctypes.c_double),
                 ("refine_tolerance", ctypes.c_double), ("refine_maxiter", ctypes.c_int32),
                 ("assembly", ctypes.c_int32), ("condition_guard", ctypes.c_double),
-                ("near_eta", ctypes.c_double)]
+                ("near_eta", ctypes.c_double), ("discretization", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class ServerOptions(ctypes.Structure):

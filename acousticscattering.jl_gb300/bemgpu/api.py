@@ -257,9 +257,14 @@ def mesh(nodes, triangles, *, units: str = "m") -> Mesh:
 
 # ------------------------------------------------------------------ problems
 def _problem(boundary, k, formulation=None, precision="double", equilibrate=True,
-             refinement=None, near_eta=2.0, assembly=None) -> C.Problem:
+             refinement=None, near_eta=2.0, assembly=None,
+             discretization="collocation") -> C.Problem:
     if not isinstance(boundary, AbstractBoundaryCondition):
         raise ArgumentError("boundary must be Rigid(), PressureRelease() or FluidFilled(g, h)")
+    if discretization not in C.DISCRETIZATION:
+        raise ArgumentError("discretization must be :collocation or :nystrom")
+    if discretization == "nystrom" and isinstance(boundary, FluidFilled):
+        raise ArgumentError("the Nyström discretisation covers rigid and pressure-release bodies")
     if formulation not in _FORMULATIONS:
         raise ArgumentError("formulation must be :burton_miller, :cbie or :muller")
     if precision not in ("double", "mixed"):
@@ -310,7 +315,12 @@ def _problem(boundary, k, formulation=None, precision="double", equilibrate=True
     p.condition_guard = float(refinement.get("condition_guard", 10 * np.finfo(np.float32).eps))
     p.near_eta = float(near_eta)
     p.assembly = C.ASSEMBLY[assembly]
+    p.discretization = C.DISCRETIZATION[discretization]
     return p
+
+
+def _discretization(problem) -> str:
+    return "nystrom" if problem.discretization == C.DISCRETIZATION["nystrom"] else "collocation"
 
 
 def _direction(beta, alpha):
@@ -362,7 +372,8 @@ class Factor:
         h = ctypes.c_void_p()
         _check(C.lib().bemgpu_factor_solve(self.handle, len(angles), C.dptr(inc),
                                            ctypes.byref(h)), self.ctx.handle)
-        return BEMSolution(self.ctx, h, self.surface, self.boundary, self.k, angles, az)
+        return BEMSolution(self.ctx, h, self.surface, self.boundary, self.k, angles, az,
+                           discretization=_discretization(self.problem))
 
     def diagnostics(self) -> dict:
         d = C.Diagnostics()
@@ -387,8 +398,10 @@ class BEMSolution:
 
     method = "full"
 
-    def __init__(self, ctx, handle, surface, boundary, k, angles, azimuths):
+    def __init__(self, ctx, handle, surface, boundary, k, angles, azimuths,
+                 discretization="collocation"):
         self.ctx, self.handle = ctx, handle
+        self.discretization = discretization
         self.body = surface
         self.boundary = boundary
         self.k = float(k)
@@ -435,8 +448,15 @@ class BEMSolution:
                self.ctx.handle)
         return p, v
 
+    @property
+    def n_nodes(self) -> int:
+        """Unknown locations: panel centroids (collocation) or quadrature nodes (Nyström,
+        node q of panel t at index 7 t + q)."""
+        return self.n_panels * C.NODES_PER_PANEL[self.discretization]
+
     def traces(self, rhs: int = 0):
-        n = self.n_panels
+        """Scattered pressure and normal derivative at every unknown location (n_nodes)."""
+        n = self.n_nodes
         p = np.zeros(n, dtype=np.complex128)
         q = np.zeros(n, dtype=np.complex128)
         _check(C.lib().bemgpu_traces(self.handle, rhs, C.dptr(p), C.dptr(q)), self.ctx.handle)
@@ -495,8 +515,11 @@ class BEMSolution:
             return _diag_dict(d, {"meshsize": max(s_.resolution for s_ in self.body),
                                   "illumination": "plane_wave", "interface_count": len(self.body),
                                   "mesh_hash": [s_.hash for s_ in self.body]})
-        return _diag_dict(d, {"meshsize": self.body.resolution,
-                              "illumination": "plane_wave", "mesh_hash": self.body.hash})
+        extra = {"meshsize": self.body.resolution, "illumination": "plane_wave",
+                 "mesh_hash": self.body.hash, "discretization": self.discretization}
+        if self.discretization == "nystrom":
+            extra["correction"] = {"method": "dim", "basis": "plane_waves"}
+        return _diag_dict(d, extra)
 
     def close(self):
         if getattr(self, "handle", None):
@@ -590,7 +613,7 @@ def hmatrix_apply(surface: Mesh, boundary, k, X, *, op=0, formulation=None, tol=
 def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_azimuth=0.0,
         formulation=None, precision="double", equilibrate=True, refinement=None,
         assembly=None, ctx: Context | None = None, parents=None, compression=None,
-        gmres_kwargs=None, **unsupported) -> BEMSolution:
+        gmres_kwargs=None, discretization="collocation", **unsupported) -> BEMSolution:
     """Full-3D BEM on a supplied surface (solvers/bem/surface.jl:10-23), or, given lists of
     surfaces and FluidFilled materials, the coupled fluid regions of
     bem(surfaces, materials, k; parents) (solvers/bem/regions.jl:132-150).
@@ -601,10 +624,20 @@ def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_az
     then stores the operators as complex64 with FP32 entries and products (GMRES itself
     stays FP64), which limits the attainable relative residual to about 1e-6.  Without it
     (or with method="none") the system is factored densely; gmres_kwargs then have no
-    effect, as the direct solve meets any GMRES tolerance."""
+    effect, as the direct solve meets any GMRES tolerance.
+
+    discretization="nystrom" (Rigid and PressureRelease, dense factor) puts the unknowns on
+    the seven quadrature nodes of every panel with the density-interpolation correction of
+    the reference's Nyström operators (full.jl:68-128, correction=(method=:dim,)); traces
+    then hold one value per node and point evaluation (pressure) is not available."""
     if unsupported:
         raise ArgumentError(f"unsupported option(s): {sorted(unsupported)}")
+    if discretization not in C.DISCRETIZATION:
+        raise ArgumentError("discretization must be :collocation or :nystrom")
     hm = _hmatrix_options(compression, gmres_kwargs)
+    if discretization != "collocation" and (hm is not None or
+                                            isinstance(surface, (list, tuple))):
+        raise ArgumentError("the Nyström discretisation takes one surface and a dense factor")
     if hm is not None:
         if isinstance(surface, (list, tuple)) or parents is not None:
             raise ArgumentError("hierarchical compression applies to a single surface")
@@ -630,7 +663,8 @@ def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_az
     if not (math.isfinite(k) and k > 0):
         raise ArgumentError("k must be finite and positive")
     f = Factor(surface, boundary, k, ctx=ctx, formulation=formulation, precision=precision,
-               equilibrate=equilibrate, refinement=refinement, assembly=assembly)
+               equilibrate=equilibrate, refinement=refinement, assembly=assembly,
+               discretization=discretization)
     try:
         return f.solve([incidence_angle], [incidence_azimuth])
     finally:
@@ -839,7 +873,7 @@ class SweepResult:
 def incidence_angle_sweep(surface: Mesh, boundary, k, angles, *, incidence_azimuth=0.0,
                           formulation=None, precision="double", equilibrate=True,
                           refinement=None, assembly=None, ctx=None, compression=None,
-                          gmres_kwargs=None) -> SweepResult:
+                          gmres_kwargs=None, discretization="collocation") -> SweepResult:
     """Backscatter at many polar incidence angles from one factorisation
     (postprocessing/sweeps.jl:626-701): assembled and factored once, all angles
     solved as one multi-right-hand-side batch.  With compression=(method=:hmatrix, ...)
@@ -850,6 +884,8 @@ def incidence_angle_sweep(surface: Mesh, boundary, k, angles, *, incidence_azimu
     if not math.isfinite(incidence_azimuth):
         raise ArgumentError("incidence_azimuth must be finite")
     hm = _hmatrix_options(compression, gmres_kwargs)
+    if hm is not None and discretization != "collocation":
+        raise ArgumentError("the Nyström discretisation takes a dense factor")
     if hm is not None:
         sol = _bem_hmatrix(surface, boundary, k, angles, incidence_azimuth, hm,
                            formulation=formulation, precision=precision, ctx=ctx)
@@ -860,7 +896,8 @@ def incidence_angle_sweep(surface: Mesh, boundary, k, angles, *, incidence_azimu
             sol.close()
         return SweepResult(angles, amps, 20 * np.log10(np.abs(amps)), diag)
     f = Factor(surface, boundary, k, ctx=ctx, formulation=formulation, precision=precision,
-               equilibrate=equilibrate, refinement=refinement, assembly=assembly)
+               equilibrate=equilibrate, refinement=refinement, assembly=assembly,
+               discretization=discretization)
     try:
         sol = f.solve(angles, incidence_azimuth)
         amps = np.array([scattering_amplitude(sol, rhs=r) for r in range(len(angles))])
@@ -919,12 +956,14 @@ def dense_solve(A, B, *, precision="double", equilibrate=True, refinement=None, 
 
 
 def assemble(surface: Mesh, boundary, k, *, formulation=None, precision="double",
-             assembly=None, ctx=None):
+             assembly=None, ctx=None, discretization="collocation"):
     """The assembled operators (rigid/soft: M1 = 1/2 I - D - a H and
-    M2 = S + a (1/2 I + K'); fluid: the 2n x 2n system) as complex128 arrays."""
+    M2 = S + a (1/2 I + K'); fluid: the 2n x 2n system) as complex128 arrays; Nyström:
+    the node operators (7 n x 7 n) with the element corrections applied."""
     ctx = ctx or context()
-    p = _problem(boundary, k, formulation=formulation, precision=precision, assembly=assembly)
-    n = surface.n_panels
+    p = _problem(boundary, k, formulation=formulation, precision=precision, assembly=assembly,
+                 discretization=discretization)
+    n = surface.n_panels * C.NODES_PER_PANEL[discretization]
     if isinstance(boundary, FluidFilled):
         M1 = np.zeros((2 * n, 2 * n), dtype=np.complex128, order="F")
         _check(C.lib().bemgpu_assemble_dense(ctx.handle, surface.handle(ctx), ctypes.byref(p),

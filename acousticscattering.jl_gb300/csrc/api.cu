@@ -25,6 +25,7 @@
 
 #include "bemgpu_internal.h"
 #include "linalg.cuh"
+#include "nystrom.cuh"
 #include "refine.cuh"
 #include "gemm_tc.cuh"
 #include "hmatrix.cuh"
@@ -288,6 +289,10 @@ struct MeshData {
     Buf perm, iperm, near_dst;
   };
   std::map<std::pair<int32_t, double>, std::shared_ptr<HmPlanCache>> hm_plans;
+  // Nyström node set: one record per quadrature node (the panel-record layout with the
+  // node as centroid and all seven Gauss points, its weight as area), built on first use
+  bool nystrom = false;
+  std::shared_ptr<MeshData> node_mesh;
 };
 }  // namespace
 
@@ -400,6 +405,43 @@ int make_mesh(bemgpu_ctx* c, const double* nodes, int64_t N, const int64_t* tris
   *out = m;
   return BEMGPU_OK;
 }
+
+// Nyström node set of a panel mesh: node q of panel t is record 7 t + q, at the panel's
+// Gauss point q with the panel normal and weight area * w_q (MeshData::node_mesh).
+int nystrom_mesh(bemgpu_ctx* c, MeshData* m, std::shared_ptr<MeshData>* out) {
+  if (m->node_mesh) {
+    *out = m->node_mesh;
+    return BEMGPU_OK;
+  }
+  if (m->surf.p) return fail(c, BEMGPU_EINVAL, "the Nyström discretisation takes one surface");
+  auto d = std::make_shared<MeshData>();
+  d->c = c;
+  d->n = (int64_t)kNyNodes * m->n;
+  d->resolution = m->resolution;
+  d->eta = m->eta;
+  std::memcpy(d->hash, m->hash, sizeof d->hash);
+  for (int a = 0; a < 3; ++a) d->center[a] = m->center[a];
+  d->nystrom = true;
+  d->panels_h.assign((size_t)d->n * kPanelDoubles, 0.0);
+  for (int64_t t = 0; t < m->n; ++t) {
+    const double* r = m->panels_h.data() + t * kPanelDoubles;
+    for (int q = 0; q < kNyNodes; ++q) {
+      double* o = d->panels_h.data() + (t * kNyNodes + q) * kPanelDoubles;
+      for (int a = 0; a < 3; ++a) {
+        o[a] = r[8 + 3 * q + a];
+        o[3 + a] = r[3 + a];
+      }
+      o[6] = r[6] * kRuleW[q];
+      o[7] = r[7];
+      for (int g = 0; g < 7; ++g)
+        for (int a = 0; a < 3; ++a) o[8 + 3 * g + a] = o[a];
+    }
+  }
+  TRY(upload(c, d->panels_h, &d->panels));
+  m->node_mesh = d;
+  *out = d;
+  return BEMGPU_OK;
+}
 }  // namespace
 
 // The union of several validated surfaces as one panel set (each surface was validated
@@ -507,6 +549,7 @@ struct FactorData {
   bool single = false;     // current factor precision
   bool mixed = false;      // requested precision
   bool fp32_regular = false;  // regular pairs assembled in FP32
+  bool nystrom = false;       // Nyström operators on the node set (mesh = node mesh)
   int reason = BEMGPU_REASON_NONE;
   double rcond = NAN;
   double matrix_norm = 0.0, anorm = 0.0;
@@ -571,6 +614,11 @@ int check_problem(bemgpu_ctx* c, const bemgpu_problem& p, int* kind) {
     return fail(c, BEMGPU_EINVAL, "assembly must be :default, :double or :single");
   if (!(std::isfinite(p.near_eta) && p.near_eta > 0))
     return fail(c, BEMGPU_EINVAL, "near_eta must be finite and positive");
+  if (p.discretization != BEMGPU_COLLOCATION && p.discretization != BEMGPU_NYSTROM)
+    return fail(c, BEMGPU_EINVAL, "discretization must be :collocation or :nystrom");
+  if (p.discretization == BEMGPU_NYSTROM && p.boundary == BEMGPU_FLUID)
+    return fail(c, BEMGPU_EINVAL,
+                "the Nyström discretisation covers rigid and pressure-release bodies");
   if (p.boundary == BEMGPU_RIGID || p.boundary == BEMGPU_PRESSURE_RELEASE) {
     int f = p.formulation == BEMGPU_FORMULATION_DEFAULT ? BEMGPU_BURTON_MILLER : p.formulation;
     if (f != BEMGPU_BURTON_MILLER && f != BEMGPU_CBIE)
@@ -600,13 +648,106 @@ int formulation_of(int kind) {
   }
 }
 
+// Mesh and assembly precision of a factor (f->prob set): the Nyström node set for that
+// discretisation (FP64 node operators; mixed precision reduces the factor only), else the
+// panel mesh with FP32 regular pairs where the problem asks for them.
+int bind_mesh(bemgpu_ctx* c, FactorData* f, const std::shared_ptr<MeshData>& m) {
+  f->mixed = f->prob.precision == BEMGPU_MIXED;
+  f->nystrom = f->prob.discretization == BEMGPU_NYSTROM;
+  if (f->nystrom) {
+    f->fp32_regular = false;
+    return nystrom_mesh(c, m.get(), &f->mesh);
+  }
+  f->mesh = m;
+  f->fp32_regular = f->prob.assembly == BEMGPU_ASSEMBLY_SINGLE ||
+                    (f->prob.assembly == BEMGPU_ASSEMBLY_DEFAULT && f->mixed);
+  return BEMGPU_OK;
+}
+
+// The nine plane-wave directions of the Nyström correction: integer vectors normalised
+// by a correctly rounded square root (reproducible on any host).
+void nystrom_directions(double* dirs) {
+  static const int v[kNyBasis][3] = {{3, 1, -1}, {-3, -2, 2}, {-3, 1, -1}, {1, 2, -3}, {2, 2, 3},
+                                     {0, 1, 2},  {0, -1, -1}, {-1, -3, 1}, {-3, -3, -1}};
+  for (int s = 0; s < kNyBasis; ++s) {
+    const double a = v[s][0], b = v[s][1], e = v[s][2];
+    const double nr = std::sqrt(a * a + b * b + e * e);
+    dirs[3 * s] = a / nr;
+    dirs[3 * s + 1] = b / nr;
+    dirs[3 * s + 2] = e / nr;
+  }
+}
+
 template <class T>
 int to_device(bemgpu_ctx* c, const std::vector<T>& h, Buf* out) {
   return upload(c, h, out);
 }
 
 // ------------------------------------------------------------------ assembly
+// M1 and M2 of one Nyström instance (complex128, node order), corrected on every element.
+int assemble_nystrom(bemgpu_ctx* c, FactorData* f) {
+  const Launch L = c->launch();
+  MeshData* m = f->mesh.get();
+  const int64_t N = m->n;
+  f->n = f->N = N;
+  f->a32 = false;
+  f->rhs_is_m2 = f->prob.boundary == BEMGPU_RIGID;
+  TRY(alloc(c, (size_t)N * N * 16, &f->A));
+  TRY(alloc(c, (size_t)N * N * 16, &f->Mrhs));
+  const int32_t chunks = nystrom_chunks(N);
+  const int64_t ne = N / kNyNodes;
+  Buf scratch, status;
+  TRY(alloc(c, (size_t)nystrom_scratch_doubles(N, chunks) * 8, &scratch));
+  TRY(alloc(c, (size_t)ne * 4, &status));
+  CUDA_TRY(c, cudaMemsetAsync(status.p, 0, (size_t)ne * 4, c->stream));
+  NyInst I{};
+  I.nodes = m->panels.as<double>();
+  I.n = N;
+  I.k = f->prob.k;
+  I.a_re = 0.0;
+  I.a_im = f->kind == kAsmBM ? 1.0 / f->prob.k : 0.0;
+  // rigid: system M1, rhs M2; pressure release: system M2, rhs M1
+  I.M1 = (f->rhs_is_m2 ? f->A : f->Mrhs).as<double>();
+  I.M2 = (f->rhs_is_m2 ? f->Mrhs : f->A).as<double>();
+  nystrom_directions(I.dirs);
+  I.trace = scratch.as<double>();
+  I.part = scratch.as<double>() + 2 * (2 * (int64_t)kNyBasis * N);
+  I.n_chunks = chunks;
+  I.status = status.as<int32_t>();
+  {
+    Prof pr(c, "assemble");
+    launch_nystrom(L, I);
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  std::vector<int32_t> st;
+  TRY(download(c, status, &st, (size_t)ne));
+  int64_t bad = 0;
+  for (int32_t v : st) bad += v != 0;
+  if (bad) {
+    char msg[200];
+    std::snprintf(msg, sizeof msg,
+                  "density-interpolation fit is rank-deficient on %lld elements (k times the "
+                  "panel size far below the plane-wave basis' resolution)",
+                  (long long)bad);
+    return fail(c, BEMGPU_EINVAL, msg);
+  }
+  return BEMGPU_OK;
+}
+
+int assemble_panels(bemgpu_ctx* c, std::vector<FactorData*>& fs);
+
 int assemble_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
+  std::vector<FactorData*> panels;
+  for (FactorData* f : fs) {
+    if (f->nystrom)
+      TRY(assemble_nystrom(c, f));
+    else
+      panels.push_back(f);
+  }
+  return panels.empty() ? BEMGPU_OK : assemble_panels(c, panels);
+}
+
+int assemble_panels(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
   const Launch L = c->launch();
   std::vector<AsmInst> ai(fs.size());
   for (size_t t = 0; t < fs.size(); ++t) {
@@ -2019,15 +2160,12 @@ int run_batch(bemgpu_server* S, std::vector<Item>& items,
                             })->req;
       auto f = std::make_shared<FactorData>();
       f->c = c;
-      f->mesh = r.mesh;
       f->prob = r.prob;
       f->prob.k = kv.first.k;
       int kind = 0;
       TRY(check_problem(c, f->prob, &kind));
       f->kind = kind;
-      f->mixed = f->prob.precision == BEMGPU_MIXED;
-      f->fp32_regular = f->prob.assembly == BEMGPU_ASSEMBLY_SINGLE ||
-                        (f->prob.assembly == BEMGPU_ASSEMBLY_DEFAULT && f->mixed);
+      TRY(bind_mesh(c, f.get(), r.mesh));
       kv.second = f;
       fresh.push_back(f);
       fs.push_back(f.get());
@@ -2419,14 +2557,11 @@ int bemgpu_factor_create_batch(bemgpu_ctx* c, int32_t count, const bemgpu_mesh* 
     TRY(check_problem(c, problems[t], &kind));
     auto f = std::make_shared<FactorData>();
     f->c = c;
-    f->mesh = meshes[t]->d;
     f->prob = problems[t];
     f->kind = kind;
-    f->mixed = problems[t].precision == BEMGPU_MIXED;
-    f->fp32_regular = problems[t].assembly == BEMGPU_ASSEMBLY_SINGLE ||
-                      (problems[t].assembly == BEMGPU_ASSEMBLY_DEFAULT && f->mixed);
+    TRY(bind_mesh(c, f.get(), meshes[t]->d));
     // near pairs are a mesh property; a different eta rebuilds them once
-    if (std::fabs(f->prob.near_eta - f->mesh->eta) > 0) {
+    if (!f->nystrom && std::fabs(f->prob.near_eta - f->mesh->eta) > 0) {
       return fail(c, BEMGPU_EINVAL, "near_eta differs from the mesh's (upload with that eta)");
     }
     own.push_back(f);
@@ -3084,6 +3219,9 @@ int hm_problem(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_problem* pro
   if (*kind != kAsmBM && *kind != kAsmCBIE)
     return fail(c, BEMGPU_EINVAL,
                 "hierarchical compression applies to Rigid and PressureRelease boundaries");
+  if (problem->discretization != BEMGPU_COLLOCATION)
+    return fail(c, BEMGPU_EINVAL,
+                "hierarchical compression applies to the collocation discretisation");
   if (std::fabs(problem->near_eta - mesh->d->eta) > 0)
     return fail(c, BEMGPU_EINVAL, "near_eta differs from the mesh's (upload with that eta)");
   return check_hm_options(c, *opt);
@@ -3475,6 +3613,8 @@ int bemgpu_pressure_region(bemgpu_solution* sol, int32_t rhs, int64_t npts, cons
   std::lock_guard<std::recursive_mutex> lk(c->mu);
   cudaSetDevice(c->device);
   if (rhs < 0 || rhs >= s->nrhs) return fail(c, BEMGPU_EINVAL, "rhs index out of range");
+  if (s->mesh && s->mesh->nystrom)
+    return fail(c, BEMGPU_EINVAL, "pressure at points needs the collocation discretisation");
   if (field < BEMGPU_FIELD_TOTAL || field > BEMGPU_FIELD_INTERIOR)
     return fail(c, BEMGPU_EINVAL, "field must be :total, :scattered, :incident or :interior");
   if (region >= 0 && !s->region)
@@ -3591,6 +3731,8 @@ int bemgpu_server_submit(bemgpu_server* S, const bemgpu_mesh* mesh, const bemgpu
     p.k = ks[i];
     TRY(check_problem(S->c, p, &kind));
   }
+  if (problem->discretization != BEMGPU_COLLOCATION)  // not part of the factor-cache key
+    return fail(S->c, BEMGPU_EINVAL, "the server solves collocation problems");
   for (int32_t i = 0; i < 2 * nangles; ++i)
     if (!std::isfinite(incidence[i])) return fail(S->c, BEMGPU_EINVAL, "incidence angles must be finite");
   auto r = std::make_shared<ServerReq>();
@@ -3836,12 +3978,9 @@ int bemgpu_assemble_dense(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_p
   TRY(check_problem(c, *problem, &kind));
   auto f = std::make_shared<FactorData>();
   f->c = c;
-  f->mesh = mesh->d;
   f->prob = *problem;
   f->kind = kind;
-  f->mixed = problem->precision == BEMGPU_MIXED;
-  f->fp32_regular = problem->assembly == BEMGPU_ASSEMBLY_SINGLE ||
-                    (problem->assembly == BEMGPU_ASSEMBLY_DEFAULT && f->mixed);
+  TRY(bind_mesh(c, f.get(), mesh->d));
   std::vector<FactorData*> fs{f.get()};
   TRY(assemble_batch(c, fs));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));

@@ -1,0 +1,333 @@
+// Nyström operators on quadrature nodes with a density-interpolation correction.
+//
+// The reference assembles its rigid/soft system from Inti's Nyström operators on the
+// surface quadrature nodes (solvers/bem/full.jl:68-128, Inti.single_double_layer and
+// Inti.adj_double_layer_hypersingular with correction=(method=:dim,)), and corrects the
+// singular and nearly singular quadrature with a Green-identity fit over each target's
+// nearest element (the structure of solvers/bem/quadrature/fluid.jl:104-163: defect of
+// the discrete identity on a basis of Helmholtz solutions, scaled minimum-norm fit of the
+// element's node weights).  The basis here is kNyBasis plane waves (Faria, Perez-Arancibia
+// and Bonnet 2021, doi:10.1016/j.cma.2021.113703, for the general-purpose kernel
+// regularisation; plane-wave interpolants after Perez-Arancibia, Faria and Turc 2019,
+// SIAM J. Sci. Comput. 41(4)).
+//
+// For on-surface targets every node's nearest element is its own, so the correction is a
+// 7x7 block on the diagonal of each operator.  With u a plane wave (regular inside the
+// body, outward normals) the identities are
+//   1/2 u(x)     = S[du/dn](x)  - D[u](x)
+//   1/2 du/dn(x) = K'[du/dn](x) - H[u](x)
+// and the defect of the uncorrected node rule, row by row and basis function by basis
+// function, is fitted by weights on the seven nodes of the row's element.
+//
+// Work split: k_ny_traces (basis traces at the nodes), k_ny_assemble (every pair once:
+// the two system matrices and the defect sums, FP64-issue-bound), k_ny_correct (one
+// thread per element: Householder QR of the 14 x 9 trace matrix, the 14 fits, the
+// corrections).
+#include <cmath>
+
+#include "nystrom.cuh"
+
+namespace bemgpu {
+
+namespace {
+
+struct z2 {
+  double x, y;
+};
+__device__ __forceinline__ z2 zmul(z2 a, z2 b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+__device__ __forceinline__ z2 zconj(z2 a) { return {a.x, -a.y}; }
+// acc += a * b
+__device__ __forceinline__ void zfma(z2& acc, z2 a, z2 b) {
+  acc.x += a.x * b.x - a.y * b.y;
+  acc.y += a.x * b.y + a.y * b.x;
+}
+// acc -= a * b
+__device__ __forceinline__ void zfms(z2& acc, z2 a, z2 b) {
+  acc.x -= a.x * b.x - a.y * b.y;
+  acc.y -= a.x * b.y + a.y * b.x;
+}
+__device__ __forceinline__ z2 zdiv(z2 a, z2 b) {
+  const double d = b.x * b.x + b.y * b.y;
+  return {(a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d};
+}
+
+constexpr double kInv4Pi = 0.07957747154594766788;  // 1 / (4 pi)
+
+// ------------------------------------------------------------------ interpolant traces
+// u_s(y) = exp(i k d_s . y), du_s/dn = i k (d_s . n) u_s at every node.
+__global__ void k_ny_traces(NyInst I) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= I.n) return;
+  const double* r = I.nodes + j * kPanelDoubles;
+  z2* tr = reinterpret_cast<z2*>(I.trace);
+  for (int s = 0; s < kNyBasis; ++s) {
+    const double* d = I.dirs + 3 * s;
+    const double ph = I.k * (d[0] * r[0] + d[1] * r[1] + d[2] * r[2]);
+    const double kdn = I.k * (d[0] * r[3] + d[1] * r[4] + d[2] * r[5]);
+    double sn, cs;
+    sincos(ph, &sn, &cs);
+    tr[(int64_t)s * I.n + j] = {cs, sn};
+    tr[(int64_t)(kNyBasis + s) * I.n + j] = {-kdn * sn, kdn * cs};
+  }
+}
+
+// ------------------------------------------------------------------ pair assembly
+// Thread = row i (coalesced column-major stores), CTA = kNyRows rows x one column range;
+// columns staged kNyTile at a time.  Per pair (i != j), with d = x_i - y_j, r = |d|,
+// G = e^{ikr} / (4 pi r), G' = G (ik - 1/r), G'' = G ((ik - 1/r)^2 + 1/r^2), weight w_j:
+//   S = G w,  D = -G' (d.n_j)/r w,  K' = G' (d.n_i)/r w,
+//   H = -[(G'' - G'/r) (d.n_i)(d.n_j)/r^2 + G' (n_i.n_j)/r] w;
+// the coincident pair (i == j) contributes zero to every operator.
+__global__ void __launch_bounds__(kNyRows) k_ny_assemble(NyInst I) {
+  const int64_t n = I.n;
+  const int64_t i = (int64_t)blockIdx.x * kNyRows + threadIdx.x;
+  const int64_t c0 = (int64_t)blockIdx.y * I.chunk_cols;
+  const int64_t c1 = min(n, c0 + I.chunk_cols);
+  __shared__ double s_node[kNyTile][7];           // position, normal, weight
+  __shared__ z2 s_tr[2 * kNyBasis][kNyTile];      // u_s, du_s/dn
+  const bool row = i < n;
+  double xi[3] = {0, 0, 0}, ni[3] = {0, 0, 0};
+  if (row) {
+    const double* r = I.nodes + i * kPanelDoubles;
+    for (int d = 0; d < 3; ++d) {
+      xi[d] = r[d];
+      ni[d] = r[3 + d];
+    }
+  }
+  const double k = I.k;
+  const z2 al = {I.a_re, I.a_im};
+  z2 acc[2 * kNyBasis];
+#pragma unroll
+  for (int t = 0; t < 2 * kNyBasis; ++t) acc[t] = {0.0, 0.0};
+  const z2* tr = reinterpret_cast<const z2*>(I.trace);
+  z2* M1 = reinterpret_cast<z2*>(I.M1);
+  z2* M2 = reinterpret_cast<z2*>(I.M2);
+  for (int64_t t0 = c0; t0 < c1; t0 += kNyTile) {
+    const int cnt = (int)min((int64_t)kNyTile, c1 - t0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < kNyTile * 7; e += kNyRows) {
+      const int jj = e / 7, f = e % 7;
+      s_node[jj][f] = jj < cnt ? I.nodes[(t0 + jj) * kPanelDoubles + f] : 0.0;
+    }
+    for (int e = threadIdx.x; e < kNyTile * 2 * kNyBasis; e += kNyRows) {
+      const int jj = e % kNyTile, t = e / kNyTile;
+      s_tr[t][jj] = jj < cnt ? tr[(int64_t)t * n + t0 + jj] : z2{0.0, 0.0};
+    }
+    __syncthreads();
+    if (!row) continue;
+    for (int jj = 0; jj < cnt; ++jj) {
+      const int64_t j = t0 + jj;
+      z2 S = {0, 0}, D = {0, 0}, K = {0, 0}, H = {0, 0};
+      z2 m1, m2;
+      if (j == i) {
+        m1 = {0.5, 0.0};
+        m2 = {0.5 * al.x, 0.5 * al.y};
+      } else {
+        const double dx = xi[0] - s_node[jj][0], dy = xi[1] - s_node[jj][1],
+                     dz = xi[2] - s_node[jj][2];
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        const double r = sqrt(r2);
+        const double ir = 1.0 / r;
+        double sn, cs;
+        sincos(k * r, &sn, &cs);
+        const double w = s_node[jj][6];
+        const double gs = kInv4Pi * ir;
+        const z2 G = {cs * gs, sn * gs};
+        const z2 G1 = zmul(G, z2{-ir, k});
+        const z2 G2 = zmul(G, z2{2.0 * ir * ir - k * k, -2.0 * k * ir});
+        const double dny = dx * s_node[jj][3] + dy * s_node[jj][4] + dz * s_node[jj][5];
+        const double dnx = dx * ni[0] + dy * ni[1] + dz * ni[2];
+        const double nn = ni[0] * s_node[jj][3] + ni[1] * s_node[jj][4] + ni[2] * s_node[jj][5];
+        S = {G.x * w, G.y * w};
+        const double fd = -dny * ir * w, fk = dnx * ir * w;
+        D = {G1.x * fd, G1.y * fd};
+        K = {G1.x * fk, G1.y * fk};
+        const double f2 = dnx * dny * ir * ir, f1 = nn * ir;
+        H = {-((G2.x - G1.x * ir) * f2 + G1.x * f1) * w, -((G2.y - G1.y * ir) * f2 + G1.y * f1) * w};
+        const z2 aH = zmul(al, H), aK = zmul(al, K);
+        m1 = {-D.x - aH.x, -D.y - aH.y};
+        m2 = {S.x + aK.x, S.y + aK.y};
+      }
+      M1[i + j * n] = m1;
+      M2[i + j * n] = m2;
+#pragma unroll
+      for (int s = 0; s < kNyBasis; ++s) {
+        const z2 u = s_tr[s][jj], f = s_tr[kNyBasis + s][jj];
+        zfma(acc[s], S, f);
+        zfms(acc[s], D, u);
+        zfma(acc[kNyBasis + s], K, f);
+        zfms(acc[kNyBasis + s], H, u);
+      }
+    }
+  }
+  if (!row) return;
+  z2* part = reinterpret_cast<z2*>(I.part);
+#pragma unroll
+  for (int t = 0; t < 2 * kNyBasis; ++t)
+    part[((int64_t)blockIdx.y * 2 * kNyBasis + t) * n + i] = acc[t];
+}
+
+// ------------------------------------------------------------------ element corrections
+// Element e, nodes 7e..7e+6.  Trace matrix M (14 x kNyBasis): rows u_s and du_s/dn at the
+// nodes, each row scaled to unit norm (scale sc).  A = (M / sc)^T; the weights of a row's
+// defect d are the minimum-norm solution of A w~ = d, w = w~ / sc, computed from the
+// Householder QR A^H = Qf R: w~ = Qf R^{-H} d (equal to the pseudo-inverse solution for
+// A of full row rank).  Weights split into pressure (first 7) and flux (last 7) parts:
+//   D += w_p, S -= w_f (pressure identity); H += w_p, K' -= w_f (flux identity),
+// applied to M1 = 1/2 I - D - alpha H and M2 = S + alpha (1/2 I + K').
+constexpr int kNyFit = 2 * kNyNodes;  // unknown weights per element
+constexpr int kNyCorrT = 64;
+
+__global__ void __launch_bounds__(kNyCorrT) k_ny_correct(NyInst I) {
+  const int64_t e = (int64_t)blockIdx.x * kNyCorrT + threadIdx.x;
+  const int64_t n = I.n;
+  if (e >= n / kNyNodes) return;
+  const z2* tr = reinterpret_cast<const z2*>(I.trace);
+  const z2* part = reinterpret_cast<const z2*>(I.part);
+  z2* M1 = reinterpret_cast<z2*>(I.M1);
+  z2* M2 = reinterpret_cast<z2*>(I.M2);
+  const int64_t b = e * kNyNodes;
+  z2 B[kNyFit][kNyBasis];  // A^H, reduced in place to R
+  z2 V[kNyFit][kNyBasis];  // Householder vectors (unit norm), column c from row c on
+  double sc[kNyFit];
+  for (int j = 0; j < kNyFit; ++j) {
+    const int64_t node = b + (j % kNyNodes);
+    const int t = j < kNyNodes ? 0 : 1;
+    double s2 = 0.0;
+    for (int s = 0; s < kNyBasis; ++s) {
+      const z2 v = tr[(int64_t)(t * kNyBasis + s) * n + node];
+      B[j][s] = v;
+      s2 += v.x * v.x + v.y * v.y;
+    }
+    sc[j] = fmax(sqrt(s2), 1e-300);
+    for (int s = 0; s < kNyBasis; ++s) B[j][s] = {B[j][s].x / sc[j], -B[j][s].y / sc[j]};
+  }
+  int singular = 0;
+  for (int c = 0; c < kNyBasis; ++c) {
+    double nx = 0.0;
+    for (int j = c; j < kNyFit; ++j) nx += B[j][c].x * B[j][c].x + B[j][c].y * B[j][c].y;
+    nx = sqrt(nx);
+    const z2 x0 = B[c][c];
+    const double ax0 = hypot(x0.x, x0.y);
+    const z2 ph = ax0 > 0.0 ? z2{x0.x / ax0, x0.y / ax0} : z2{1.0, 0.0};
+    const z2 alpha = {-ph.x * nx, -ph.y * nx};
+    for (int j = 0; j < kNyFit; ++j) V[j][c] = {0.0, 0.0};
+    double vn = 0.0;
+    for (int j = c; j < kNyFit; ++j) {
+      V[j][c] = j == c ? z2{x0.x - alpha.x, x0.y - alpha.y} : B[j][c];
+      vn += V[j][c].x * V[j][c].x + V[j][c].y * V[j][c].y;
+    }
+    vn = sqrt(vn);
+    if (!(vn > 0.0)) {
+      singular = 1;
+      break;
+    }
+    for (int j = c; j < kNyFit; ++j) V[j][c] = {V[j][c].x / vn, V[j][c].y / vn};
+    for (int q = c; q < kNyBasis; ++q) {
+      z2 dot = {0.0, 0.0};
+      for (int j = c; j < kNyFit; ++j) zfma(dot, zconj(V[j][c]), B[j][q]);
+      for (int j = c; j < kNyFit; ++j) {
+        const z2 v2 = {2.0 * V[j][c].x, 2.0 * V[j][c].y};
+        zfms(B[j][q], v2, dot);
+      }
+    }
+  }
+  if (!singular) {
+    const double r00 = hypot(B[0][0].x, B[0][0].y);
+    for (int c = 0; c < kNyBasis; ++c)
+      if (!(hypot(B[c][c].x, B[c][c].y) > 1e-13 * r00)) singular = 1;
+  }
+  if (singular) {  // rank-deficient fit: the element keeps its uncorrected rule
+    I.status[e] = 1;
+    return;
+  }
+  const z2 al = {I.a_re, I.a_im};
+  for (int t = 0; t < kNyNodes; ++t) {
+    const int64_t row = b + t;
+    z2 dP[kNyNodes], dF[kNyNodes], hP[kNyNodes], hF[kNyNodes];
+    for (int id = 0; id < 2; ++id) {  // 0: pressure identity (S, D); 1: flux identity (K', H)
+      z2 d[kNyBasis];
+      for (int s = 0; s < kNyBasis; ++s) {
+        const int slot = id * kNyBasis + s;
+        z2 acc = {0.0, 0.0};
+        for (int c = 0; c < I.n_chunks; ++c) {
+          const z2 p = part[((int64_t)c * 2 * kNyBasis + slot) * n + row];
+          acc.x += p.x;
+          acc.y += p.y;
+        }
+        const z2 own = tr[(int64_t)(id * kNyBasis + s) * n + row];  // u or du/dn at the row
+        d[s] = {acc.x - 0.5 * own.x, acc.y - 0.5 * own.y};
+      }
+      // z = R^{-H} d (R^H lower triangular)
+      z2 z[kNyBasis];
+      for (int q = 0; q < kNyBasis; ++q) {
+        z2 v = d[q];
+        for (int p = 0; p < q; ++p) zfms(v, zconj(B[p][q]), z[p]);
+        z[q] = zdiv(v, zconj(B[q][q]));
+      }
+      // w~ = H_0 ... H_8 [z; 0]
+      z2 wv[kNyFit];
+      for (int j = 0; j < kNyFit; ++j) wv[j] = j < kNyBasis ? z[j] : z2{0.0, 0.0};
+      for (int c = kNyBasis - 1; c >= 0; --c) {
+        z2 dot = {0.0, 0.0};
+        for (int j = c; j < kNyFit; ++j) zfma(dot, zconj(V[j][c]), wv[j]);
+        for (int j = c; j < kNyFit; ++j) {
+          const z2 v2 = {2.0 * V[j][c].x, 2.0 * V[j][c].y};
+          zfms(wv[j], v2, dot);
+        }
+      }
+      for (int j = 0; j < kNyNodes; ++j) {
+        const z2 wp = {wv[j].x / sc[j], wv[j].y / sc[j]};
+        const z2 wf = {wv[kNyNodes + j].x / sc[kNyNodes + j], wv[kNyNodes + j].y / sc[kNyNodes + j]};
+        if (id == 0) {
+          dP[j] = wp;
+          dF[j] = wf;
+        } else {
+          hP[j] = wp;
+          hF[j] = wf;
+        }
+      }
+    }
+    for (int j = 0; j < kNyNodes; ++j) {
+      const int64_t o = row + (b + j) * n;
+      // M1 += -dD - alpha dH = -w_p(pressure) - alpha w_p(flux identity)
+      const z2 aH = zmul(al, hP[j]);
+      M1[o] = {M1[o].x - dP[j].x - aH.x, M1[o].y - dP[j].y - aH.y};
+      // M2 += dS + alpha dK' = -w_f(pressure) - alpha w_f(flux identity)
+      const z2 aK = zmul(al, hF[j]);
+      M2[o] = {M2[o].x - dF[j].x - aK.x, M2[o].y - dF[j].y - aK.y};
+    }
+  }
+}
+
+}  // namespace
+
+int64_t nystrom_scratch_doubles(int64_t n, int32_t n_chunks) {
+  return 2 * (2 * (int64_t)kNyBasis * n) + 2 * ((int64_t)n_chunks * 2 * kNyBasis * n);
+}
+
+int32_t nystrom_chunks(int64_t n) {
+  const int64_t rb = (n + kNyRows - 1) / kNyRows;
+  const int64_t want = 152 * 4;
+  int64_t c = (want + rb - 1) / rb;
+  c = std::max<int64_t>(1, std::min<int64_t>(c, 64));
+  // every range holds at least one tile
+  c = std::min<int64_t>(c, (n + kNyTile - 1) / kNyTile);
+  return (int32_t)std::max<int64_t>(1, c);
+}
+
+void launch_nystrom(const Launch& L, const NyInst& I0) {
+  NyInst I = I0;
+  const int64_t per = (I.n + I.n_chunks - 1) / I.n_chunks;
+  I.chunk_cols = (per + kNyTile - 1) / kNyTile * kNyTile;
+  k_ny_traces<<<(unsigned)((I.n + 127) / 128), 128, 0, L.stream>>>(I);
+  count_launch(1);
+  dim3 grid((unsigned)((I.n + kNyRows - 1) / kNyRows), (unsigned)I.n_chunks);
+  k_ny_assemble<<<grid, kNyRows, 0, L.stream>>>(I);
+  count_launch(1);
+  const int64_t ne = I.n / kNyNodes;
+  k_ny_correct<<<(unsigned)((ne + kNyCorrT - 1) / kNyCorrT), kNyCorrT, 0, L.stream>>>(I);
+  count_launch(1);
+}
+
+}  // namespace bemgpu

@@ -1,0 +1,44 @@
+// Nyström discretisation on the quadrature nodes (nystrom.cu): the rigid/soft operators of
+// the reference's solve_full_bem (solvers/bem/full.jl:68-128) with unknowns at the seven
+// Radon nodes of every panel, kernel values times node weights, the coincident-node entry
+// zero, and a density-interpolation correction of every node's own element.
+#pragma once
+
+#include "bemgpu_internal.h"
+
+namespace bemgpu {
+
+constexpr int kNyNodes = 7;   // nodes per element (the panel's Radon rule)
+constexpr int kNyBasis = 9;   // plane-wave interpolants of the correction
+constexpr int kNyRows = 128;  // rows (threads) per assembly CTA
+constexpr int kNyTile = 64;   // columns staged per shared-memory tile
+
+// Node records use the panel-record layout (kPanelDoubles): [0..2] position, [3..5] unit
+// normal of the element, [6] quadrature weight, [8..28] the position seven times, so that
+// the incident-trace and far-field kernels of the panel path evaluate node sums.
+struct NyInst {
+  const double* nodes;  // node records, n of them (7 per element, element-major)
+  int64_t n;
+  double k;             // wavenumber
+  double a_re, a_im;    // Burton-Miller coupling alpha (0 for CBIE)
+  double* M1;           // 1/2 I - D - alpha H   (complex128, column-major, leading dim n)
+  double* M2;           // S + alpha (1/2 I + K') (complex128, column-major, leading dim n)
+  double dirs[3 * kNyBasis];  // unit plane-wave directions of the interpolants
+  double* trace;        // interpolant traces [2][kNyBasis][n] complex: u, du/dn at the nodes
+  double* part;         // defect partial sums [n_chunks][2 kNyBasis][n] complex
+  int32_t n_chunks;     // column ranges of the assembly (partial sums per range)
+  int64_t chunk_cols;   // columns per range (a multiple of kNyTile)
+  int32_t* status;      // per element: 0, or 1 when its correction fit met a zero pivot
+};
+
+// Scratch of launch_nystrom in doubles: traces and defect partials.
+int64_t nystrom_scratch_doubles(int64_t n, int32_t n_chunks);
+// Column ranges for n nodes (enough CTAs to fill the SMs a few times over).
+int32_t nystrom_chunks(int64_t n);
+
+#ifdef __CUDACC__
+// Assembles M1 and M2 of one instance with the correction applied.
+void launch_nystrom(const Launch& L, const NyInst& I);
+#endif
+
+}  // namespace bemgpu

@@ -33,6 +33,8 @@ struct Problem
     assembly::Int32
     condition_guard::Float64
     near_eta::Float64
+    discretization::Int32   # 0 collocation, 1 Nyström (the reference's correction=(method=:dim,))
+    reserved::Int32
 end
 
 struct Diagnostics
@@ -168,14 +170,19 @@ The reference's `bem(surface::Mesh, boundary, k; ...)` on the GPU.  With
 `compression=(method=:hmatrix, tol=1e-5)` a Rigid or PressureRelease body is solved as the
 reference's `solve_full_bem` does by default: compressed operators and GMRES with
 `gmres_kwargs` (reltol, abstol, restart, maxiter); non-convergence warns as there.
+`discretization=:nystrom` (Rigid/PressureRelease, dense factor) solves on the quadrature
+nodes with the density-interpolation correction, as the reference's default
+`correction=(method=:dim,)` does.
 """
 function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
         incidence_azimuth::Real = 0.0, formulation::Union{Nothing, Symbol} = nothing,
         precision::Symbol = :double, equilibrate::Bool = true,
         refinement::NamedTuple = (;), assembly::Symbol = :default,
         compression::NamedTuple = (method = :none,), gmres_kwargs::NamedTuple = (;),
-        ctx::Context = context())
+        discretization::Symbol = :collocation, ctx::Context = context())
     isfinite(k) && k > 0 || throw(ArgumentError("k must be finite and positive"))
+    discretization in (:collocation, :nystrom) ||
+        throw(ArgumentError("discretization must be :collocation or :nystrom"))
     method = get(compression, :method, :none)
     method in (:none, :hmatrix) ||
         throw(ArgumentError("compression method must be :none or :hmatrix"))
@@ -185,7 +192,7 @@ function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
         p = Problem(_boundary_code(boundary),
             formulation === nothing ? Int32(-1) : FORMULATIONS[formulation],
             precision === :mixed ? Int32(1) : Int32(0), Int32(1), Float64(k), 1.0, 1.0,
-            1e-13, Int32(8), Int32(0), 10eps(Float32), 2.0)
+            1e-13, Int32(8), Int32(0), 10eps(Float32), 2.0, Int32(0), Int32(0))
         o = HmatrixOptions(get(compression, :tol, 1e-5), get(compression, :eta, 3.0),
             Int32(get(compression, :leaf_size, 64)), Int32(get(gmres_kwargs, :restart, 150)),
             get(gmres_kwargs, :reltol, 1e-4), get(gmres_kwargs, :abstol, 0.0),
@@ -215,7 +222,8 @@ function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
         precision === :mixed ? Int32(1) : Int32(0), Int32(equilibrate), Float64(k), g, h,
         get(refinement, :tolerance, 1e-13), Int32(get(refinement, :maxiter, 8)),
         assembly === :double ? Int32(1) : assembly === :single ? Int32(2) : Int32(0),
-        get(refinement, :condition_guard, 10eps(Float32)), 2.0)
+        get(refinement, :condition_guard, 10eps(Float32)), 2.0,
+        discretization === :nystrom ? Int32(1) : Int32(0), Int32(0))
     inc = Float64[incidence_angle, incidence_azimuth]
     r = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:bemgpu_solve, libbemgpu), Cint,
@@ -250,7 +258,7 @@ function bem(ms::AbstractVector{GPUMesh}, materials::AbstractVector{<:FluidFille
         precision === :mixed ? Int32(1) : Int32(0), Int32(equilibrate), Float64(k), 1.0, 1.0,
         get(refinement, :tolerance, 1e-13), Int32(get(refinement, :maxiter, 8)),
         assembly === :double ? Int32(1) : assembly === :single ? Int32(2) : Int32(0),
-        get(refinement, :condition_guard, 10eps(Float32)), 2.0)
+        get(refinement, :condition_guard, 10eps(Float32)), 2.0, Int32(0), Int32(0))
     handles = Ptr{Cvoid}[m.ptr for m in ms]
     dens = Float64[m.density_contrast for m in materials]
     speeds = Float64[m.soundspeed_contrast for m in materials]

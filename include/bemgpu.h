@@ -100,6 +100,16 @@ typedef enum {
   BEMGPU_FIELD_INTERIOR = 3
 } bemgpu_field;
 
+/*
+ * Discretisation of the rigid/soft equations.  COLLOCATION: constant panel values at the
+ * centroids with analytic singular rules (this library's default).  NYSTROM: unknowns at
+ * the seven quadrature nodes of every panel, kernel values times node weights, with a
+ * density-interpolation correction of every node's own element, the discretisation of the
+ * reference's solve_full_bem (full.jl:68-128 with correction=(method=:dim,)); dense
+ * factor only, rigid and pressure-release bodies, no point evaluation (pressure).
+ */
+typedef enum { BEMGPU_COLLOCATION = 0, BEMGPU_NYSTROM = 1 } bemgpu_discretization;
+
 typedef struct bemgpu_ctx bemgpu_ctx;
 typedef struct bemgpu_mesh bemgpu_mesh;
 typedef struct bemgpu_factor bemgpu_factor;
@@ -122,6 +132,8 @@ typedef struct {
   int32_t assembly;            /* bemgpu_assembly: precision of the regular-pair quadrature */
   double condition_guard;      /* single rcond guard (default 10 eps(float32)) */
   double near_eta;             /* near-pair radius in source diameters (default 2) */
+  int32_t discretization;      /* bemgpu_discretization (default COLLOCATION) */
+  int32_t reserved;
 } bemgpu_problem;
 
 /* Diagnostics of one solution; names follow the reference's diagnostics() fields. */
@@ -421,8 +433,9 @@ int bemgpu_dense_solve(bemgpu_ctx *ctx, int64_t n, const double *A, int32_t nrhs
                        int32_t refine_maxiter, double condition_guard,
                        bemgpu_diagnostics *diag);
 
-/* Assembled operators of a problem for inspection (rigid/soft: M1 and M2 n x n; fluid:
- * A 2n x 2n in M1, M2 unused).  Column-major interleaved complex128. */
+/* Assembled operators of a problem for inspection (rigid/soft: M1 and M2 n x n, or 7n x 7n
+ * on the quadrature nodes for the Nyström discretisation, corrections applied; fluid: A
+ * 2n x 2n in M1, M2 unused).  Column-major interleaved complex128. */
 int bemgpu_assemble_dense(bemgpu_ctx *ctx, const bemgpu_mesh *mesh,
                           const bemgpu_problem *problem, double *M1, double *M2);
 

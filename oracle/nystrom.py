@@ -1,0 +1,152 @@
+"""CPU FP64 oracle of the Nyström discretisation: test infrastructure.  Only tests/ and
+bench.py's CPU-baseline leg import it, as the checker; the library never calls it.
+
+Restates the reference's rigid/soft Nyström system on the surface quadrature nodes:
+
+* operators S, D, K', H at the nodes with node weights and zero coincident entries, the
+  Burton-Miller / CBIE combinations and right-hand sides of ``_assemble_full_boundary`` and
+  ``_solve_full_boundary`` (solvers/bem/full.jl:68-128, 130-184);
+* the density-interpolation correction in the structure of ``_fluid_layer_operators``
+  (solvers/bem/quadrature/fluid.jl:104-163): the defect of the discrete Green identity
+  ``mult * u + S du/dn - D u`` (and its normal-derivative form ``mult * du/dn + K' du/dn -
+  H u``, ``mult = -1/2`` on the surface) on a basis of Helmholtz solutions, fitted per
+  target on its nearest element (for on-surface targets, the target's own element) by a
+  scaled minimum-norm solve through an SVD with the 1e-13 relative cutoff
+  (fluid.jl:145-152); corrections ``S -= w_flux``, ``D += w_pressure`` (fluid.jl:153-155).
+
+The basis is nine plane waves exp(i k d . y) with fixed integer directions (the general
+correction of the reference lives in Inti.jl, a third-party package not present here; the
+plane-wave basis is this build's choice, after the plane-wave density interpolation of
+Perez-Arancibia, Faria and Turc 2019).  The far field is the node sum of full.jl:509-519.
+"""
+import math
+
+import numpy as np
+
+from . import oracle as O
+
+# Radon 7-point rule weights (barycentric rule of the panel records)
+RULE_W = np.array([0.225] + [0.13239415278850618] * 3 + [0.12593918054482715] * 3)
+NODES = 7
+_DIRS = np.array([(3, 1, -1), (-3, -2, 2), (-3, 1, -1), (1, 2, -3), (2, 2, 3), (0, 1, 2),
+                  (0, -1, -1), (-1, -3, 1), (-3, -3, -1)], dtype=np.float64)
+
+
+def directions():
+    """The nine unit plane-wave directions (integer vectors over a rounded square root)."""
+    a, b, c = _DIRS[:, 0], _DIRS[:, 1], _DIRS[:, 2]
+    nr = np.sqrt(a * a + b * b + c * c)
+    return np.stack([a / nr, b / nr, c / nr], axis=1)
+
+
+def nodes_of(P: O.Panels):
+    """Node positions (N x 3), element normals (N x 3) and weights (N), element-major."""
+    y = P.gauss.reshape(-1, 3).copy()
+    ny = np.repeat(P.normals, NODES, axis=0)
+    w = (P.areas[:, None] * RULE_W[None, :]).reshape(-1)
+    return y, ny, w
+
+
+def operators(y, ny, w, k):
+    """Weighted node operators S, D, K', H (N x N), zero on coincident nodes."""
+    d = y[:, None, :] - y[None, :, :]
+    r = np.sqrt((d * d).sum(-1))
+    same = r == 0
+    r = np.where(same, 1.0, r)
+    ir = 1.0 / r
+    G = np.exp(1j * k * r) * ir / (4 * np.pi)
+    G1 = G * (1j * k - ir)
+    G2 = G * ((1j * k - ir) ** 2 + ir ** 2)
+    dny = (d * ny[None, :, :]).sum(-1)
+    dnx = (d * ny[:, None, :]).sum(-1)
+    nn = ny @ ny.T
+    S = G * w[None, :]
+    D = -G1 * dny * ir * w[None, :]
+    K = G1 * dnx * ir * w[None, :]
+    H = -((G2 - G1 * ir) * dnx * dny * ir * ir + G1 * nn * ir) * w[None, :]
+    for A in (S, D, K, H):
+        A[same] = 0
+    return S, D, K, H
+
+
+def traces(y, ny, k):
+    """Plane-wave traces u (N x 9) and du/dn (N x 9) at the nodes."""
+    dirs = directions()
+    u = np.exp(1j * k * (y @ dirs.T))
+    return u, 1j * k * (ny @ dirs.T) * u
+
+
+def fit_weights(u, f, defect, cutoff=1e-13):
+    """Per element: minimum-norm weights of the scaled trace fit (fluid.jl:145-152).
+
+    Returns W (elements x 7 targets x 14 weights): pressure weights then flux weights."""
+    N = u.shape[0]
+    ne = N // NODES
+    M = np.concatenate([u.reshape(ne, NODES, -1), f.reshape(ne, NODES, -1)], axis=1)
+    sc = np.maximum(np.sqrt((np.abs(M) ** 2).sum(2)), np.finfo(float).eps)  # (ne, 14)
+    A = np.transpose(M / sc[:, :, None], (0, 2, 1))  # (ne, 9, 14), plain transpose
+    U, s, Vh = np.linalg.svd(A, full_matrices=False)
+    keep = s > cutoff * s[:, :1]
+    sinv = np.where(keep, 1.0 / np.where(keep, s, 1.0), 0.0)
+    pinv = np.einsum("eij,ej,ekj->eik", np.conj(np.transpose(Vh, (0, 2, 1))), sinv, np.conj(U))
+    dfx = defect.reshape(ne, NODES, -1)  # (ne, 7 targets, 9)
+    W = np.einsum("eiq,etq->eti", pinv, dfx) / sc[:, None, :]
+    return W, int((~keep).sum())
+
+
+def corrected_operators(P: O.Panels, k):
+    """S, D, K', H with the element corrections, and the nodes (y, ny, w)."""
+    y, ny, w = nodes_of(P)
+    S, D, K, H = operators(y, ny, w, k)
+    u, f = traces(y, ny, k)
+    def_sd = -0.5 * u + S @ f - D @ u
+    def_kh = -0.5 * f + K @ f - H @ u
+    W1, _ = fit_weights(u, f, def_sd)
+    W2, _ = fit_weights(u, f, def_kh)
+    ne = len(w) // NODES
+    for e in range(ne):
+        c = slice(e * NODES, (e + 1) * NODES)
+        D[c, c] += W1[e][:, :NODES]
+        S[c, c] -= W1[e][:, NODES:]
+        H[c, c] += W2[e][:, :NODES]
+        K[c, c] -= W2[e][:, NODES:]
+    return (S, D, K, H), (y, ny, w)
+
+
+def assemble(P: O.Panels, k, burton_miller=True):
+    """M1 = 1/2 I - D - a H and M2 = S + a (1/2 I + K') on the nodes (a = i/k or 0)."""
+    (S, D, K, H), _ = corrected_operators(P, k)
+    a = 1j / k if burton_miller else 0.0
+    I = np.eye(S.shape[0])
+    return 0.5 * I - D - a * H, S + a * (0.5 * I + K)
+
+
+def far_field(y, ny, w, k, xhat, p, q):
+    """f(xhat) = -(1/4 pi) sum_i w_i (i k xhat.n_i p_i + q_i) e^{-i k xhat.y_i}."""
+    xhat = np.asarray(xhat, dtype=np.float64)
+    return complex(-np.sum(w * (1j * k * (ny @ xhat) * p + q) *
+                           np.exp(-1j * k * (y @ xhat))) / (4 * np.pi))
+
+
+def solve(nodes, triangles, boundary, k, incidence_angle=math.pi / 2, incidence_azimuth=0.0,
+          formulation="burton_miller"):
+    """Scattered traces at the nodes of a rigid or pressure-release body (full.jl:130-184,
+    the direct solve in place of GMRES).  Returns (p, q, (y, ny, w))."""
+    P = O.Panels(nodes, triangles)
+    (S, D, K, H), (y, ny, w) = corrected_operators(P, k)
+    a = 1j / k if formulation == "burton_miller" else 0.0
+    I = np.eye(len(w))
+    d = O.incidence_direction(incidence_angle, incidence_azimuth)
+    pin = np.exp(1j * k * (y @ d))
+    qin = 1j * k * (ny @ d) * pin
+    if boundary == "rigid":
+        A = 0.5 * I - D - a * H
+        b = S @ qin + a * (0.5 * qin + K @ qin)
+        p = np.linalg.solve(A, b)
+        q = -qin
+    else:
+        A = S + a * (0.5 * I + K)
+        b = -(D @ pin) + 0.5 * pin - a * (H @ pin)
+        q = np.linalg.solve(A, b)
+        p = -pin
+    return p, q, (y, ny, w)

@@ -1,0 +1,86 @@
+"""The Nyström oracle pinned before it is trusted (no GPU).
+
+Pins: the corrected discrete Green identities hold for every interpolant (the defining
+property of the density-interpolation correction, solvers/bem/quadrature/fluid.jl:138-156);
+the sphere's modal series (solvers/modal/sphere.jl) at the reference's 0.1 dB; error
+decreasing under refinement; the fit keeps full rank over five decades of k times the
+panel size (no singular value reaches the 1e-13 cutoff, so every pseudo-inverse solution
+is the unique minimum-norm one); argument checks of the host interface.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from bemgpu import meshes
+from oracle import modal
+from oracle import nystrom as NY
+from oracle import oracle as O
+
+K38 = 2 * math.pi * 38e3 / 1477.4  # rigid sphere a = 1 cm at 38 kHz, c = 1477.4 m/s
+
+
+def _ts_error(boundary, sub, k=K38, a=0.01):
+    nodes, tris = meshes.icosphere(a, sub)
+    p, q, (y, ny, w) = NY.solve(nodes, tris, boundary, k, math.pi / 2, math.pi / 2)
+    d = O.incidence_direction(math.pi / 2, math.pi / 2)
+    f = NY.far_field(y, ny, w, k, -d, p, q)
+    fm = modal.form_function(boundary, k, a)
+    return 20 * math.log10(abs(f) / abs(fm)), abs(f - fm) / abs(fm)
+
+
+def test_corrected_identities_hold_for_every_interpolant():
+    nodes, tris = meshes.icosphere(0.01, 1)
+    P = O.Panels(nodes, tris)
+    (S, D, K, H), (y, ny, w) = NY.corrected_operators(P, K38)
+    u, f = NY.traces(y, ny, K38)
+    r1 = -0.5 * u + S @ f - D @ u
+    r2 = -0.5 * f + K @ f - H @ u
+    assert np.abs(r1).max() < 1e-11 * np.abs(u).max()
+    assert np.abs(r2).max() < 1e-11 * np.abs(f).max()
+    # and not before the correction
+    S0, D0, K0, H0 = NY.operators(y, ny, w, K38)
+    assert np.abs(-0.5 * u + S0 @ f - D0 @ u).max() > 1e-3 * np.abs(u).max()
+
+
+@pytest.mark.parametrize("boundary", ["rigid", "pressure_release"])
+def test_sphere_against_modal(boundary):
+    db, rel = _ts_error(boundary, 2)
+    assert abs(db) < 0.1, db
+    assert rel < 0.06, rel
+
+
+def test_refinement_reduces_error():
+    e1 = _ts_error("rigid", 1)[1]
+    e2 = _ts_error("rigid", 2)[1]
+    assert e2 < 0.5 * e1, (e1, e2)
+
+
+def test_fit_keeps_full_rank():
+    nodes, tris = meshes.icosphere(0.01, 2)
+    P = O.Panels(nodes, tris)
+    y, ny, w = NY.nodes_of(P)
+    h = math.sqrt(P.areas.mean())
+    for kh in (0.005, 0.05, 0.5, 2.0, 10.0):
+        u, f = NY.traces(y, ny, kh / h)
+        _, dropped = NY.fit_weights(u, f, np.zeros_like(u))
+        assert dropped == 0, kh
+
+
+def test_directions_are_unit_and_distinct():
+    d = NY.directions()
+    assert d.shape == (9, 3)
+    assert np.allclose((d * d).sum(1), 1.0, atol=1e-15)
+    g = d @ d.T
+    assert np.all(np.abs(g - np.eye(9)) < 0.97)  # no repeated or antipodal pair
+
+
+def test_host_rejects_unsupported_nystrom_options():
+    import bemgpu
+    from bemgpu.api import _problem
+    with pytest.raises(bemgpu.ArgumentError):
+        _problem(bemgpu.Rigid(), 1.0, discretization="galerkin")
+    with pytest.raises(bemgpu.ArgumentError):
+        _problem(bemgpu.FluidFilled(1.1, 1.1), 1.0, discretization="nystrom")
+    p = _problem(bemgpu.PressureRelease(), 2.0, discretization="nystrom")
+    assert p.discretization == 1
