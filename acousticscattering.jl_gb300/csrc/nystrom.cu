@@ -17,11 +17,16 @@
 //   1/2 u(x)     = S[du/dn](x)  - D[u](x)
 //   1/2 du/dn(x) = K'[du/dn](x) - H[u](x)
 // and the defect of the uncorrected node rule, row by row and basis function by basis
-// function, is fitted by weights on the seven nodes of the row's element.
+// function, is fitted by weights on the seven nodes of the row's element: pressure
+// weights w_p and flux weights w_f, D += w_p and S -= w_f for the first identity, H += w_p
+// and K' -= w_f for the second.  The fit is linear in the defect and only the combinations
+// M1 = 1/2 I - D - alpha H and M2 = S + alpha (1/2 I + K') are kept, so one fit of the
+// combined defect  e = def_1 + alpha def_2 = M2 F + M1 U - U - alpha F  (uncorrected M1,
+// M2; U, F the basis traces) gives both corrections: M1 -= w_p(e), M2 -= w_f(e).
 //
 // Work split: k_ny_traces (basis traces at the nodes), k_ny_assemble (every pair once:
-// the two system matrices and the defect sums, FP64-issue-bound), k_ny_correct (one
-// thread per element: Householder QR of the 14 x 9 trace matrix, the 14 fits, the
+// the two system matrices and the combined defect sums, FP64-issue-bound), k_ny_correct
+// (one thread per element: Householder QR of the 14 x 9 trace matrix, 7 fits, the
 // corrections).
 #include <cmath>
 
@@ -96,9 +101,9 @@ __global__ void __launch_bounds__(kNyRows) k_ny_assemble(NyInst I) {
   }
   const double k = I.k;
   const z2 al = {I.a_re, I.a_im};
-  z2 acc[2 * kNyBasis];
+  z2 acc[kNyBasis];
 #pragma unroll
-  for (int t = 0; t < 2 * kNyBasis; ++t) acc[t] = {0.0, 0.0};
+  for (int t = 0; t < kNyBasis; ++t) acc[t] = {0.0, 0.0};
   const z2* tr = reinterpret_cast<const z2*>(I.trace);
   z2* M1 = reinterpret_cast<z2*>(I.M1);
   z2* M2 = reinterpret_cast<z2*>(I.M2);
@@ -117,7 +122,6 @@ __global__ void __launch_bounds__(kNyRows) k_ny_assemble(NyInst I) {
     if (!row) continue;
     for (int jj = 0; jj < cnt; ++jj) {
       const int64_t j = t0 + jj;
-      z2 S = {0, 0}, D = {0, 0}, K = {0, 0}, H = {0, 0};
       z2 m1, m2;
       if (j == i) {
         m1 = {0.5, 0.0};
@@ -138,12 +142,13 @@ __global__ void __launch_bounds__(kNyRows) k_ny_assemble(NyInst I) {
         const double dny = dx * s_node[jj][3] + dy * s_node[jj][4] + dz * s_node[jj][5];
         const double dnx = dx * ni[0] + dy * ni[1] + dz * ni[2];
         const double nn = ni[0] * s_node[jj][3] + ni[1] * s_node[jj][4] + ni[2] * s_node[jj][5];
-        S = {G.x * w, G.y * w};
+        const z2 S = {G.x * w, G.y * w};
         const double fd = -dny * ir * w, fk = dnx * ir * w;
-        D = {G1.x * fd, G1.y * fd};
-        K = {G1.x * fk, G1.y * fk};
+        const z2 D = {G1.x * fd, G1.y * fd};
+        const z2 K = {G1.x * fk, G1.y * fk};
         const double f2 = dnx * dny * ir * ir, f1 = nn * ir;
-        H = {-((G2.x - G1.x * ir) * f2 + G1.x * f1) * w, -((G2.y - G1.y * ir) * f2 + G1.y * f1) * w};
+        const z2 H = {-((G2.x - G1.x * ir) * f2 + G1.x * f1) * w,
+                      -((G2.y - G1.y * ir) * f2 + G1.y * f1) * w};
         const z2 aH = zmul(al, H), aK = zmul(al, K);
         m1 = {-D.x - aH.x, -D.y - aH.y};
         m2 = {S.x + aK.x, S.y + aK.y};
@@ -151,20 +156,16 @@ __global__ void __launch_bounds__(kNyRows) k_ny_assemble(NyInst I) {
       M1[i + j * n] = m1;
       M2[i + j * n] = m2;
 #pragma unroll
-      for (int s = 0; s < kNyBasis; ++s) {
-        const z2 u = s_tr[s][jj], f = s_tr[kNyBasis + s][jj];
-        zfma(acc[s], S, f);
-        zfms(acc[s], D, u);
-        zfma(acc[kNyBasis + s], K, f);
-        zfms(acc[kNyBasis + s], H, u);
+      for (int s = 0; s < kNyBasis; ++s) {  // (M2 F + M1 U) of the row
+        zfma(acc[s], m2, s_tr[kNyBasis + s][jj]);
+        zfma(acc[s], m1, s_tr[s][jj]);
       }
     }
   }
   if (!row) return;
   z2* part = reinterpret_cast<z2*>(I.part);
 #pragma unroll
-  for (int t = 0; t < 2 * kNyBasis; ++t)
-    part[((int64_t)blockIdx.y * 2 * kNyBasis + t) * n + i] = acc[t];
+  for (int t = 0; t < kNyBasis; ++t) part[((int64_t)blockIdx.y * kNyBasis + t) * n + i] = acc[t];
 }
 
 // ------------------------------------------------------------------ element corrections
@@ -172,9 +173,8 @@ __global__ void __launch_bounds__(kNyRows) k_ny_assemble(NyInst I) {
 // nodes, each row scaled to unit norm (scale sc).  A = (M / sc)^T; the weights of a row's
 // defect d are the minimum-norm solution of A w~ = d, w = w~ / sc, computed from the
 // Householder QR A^H = Qf R: w~ = Qf R^{-H} d (equal to the pseudo-inverse solution for
-// A of full row rank).  Weights split into pressure (first 7) and flux (last 7) parts:
-//   D += w_p, S -= w_f (pressure identity); H += w_p, K' -= w_f (flux identity),
-// applied to M1 = 1/2 I - D - alpha H and M2 = S + alpha (1/2 I + K').
+// A of full row rank).  d is the combined defect of the row; its pressure weights (first
+// 7) are subtracted from M1, its flux weights (last 7) from M2.
 constexpr int kNyFit = 2 * kNyNodes;  // unknown weights per element
 constexpr int kNyCorrT = 64;
 
@@ -244,19 +244,19 @@ __global__ void __launch_bounds__(kNyCorrT) k_ny_correct(NyInst I) {
   const z2 al = {I.a_re, I.a_im};
   for (int t = 0; t < kNyNodes; ++t) {
     const int64_t row = b + t;
-    z2 dP[kNyNodes], dF[kNyNodes], hP[kNyNodes], hF[kNyNodes];
-    for (int id = 0; id < 2; ++id) {  // 0: pressure identity (S, D); 1: flux identity (K', H)
+    {
+      // combined defect e_s = (M2 F + M1 U)_s - u_s - alpha du_s/dn at the row
       z2 d[kNyBasis];
       for (int s = 0; s < kNyBasis; ++s) {
-        const int slot = id * kNyBasis + s;
         z2 acc = {0.0, 0.0};
         for (int c = 0; c < I.n_chunks; ++c) {
-          const z2 p = part[((int64_t)c * 2 * kNyBasis + slot) * n + row];
+          const z2 p = part[((int64_t)c * kNyBasis + s) * n + row];
           acc.x += p.x;
           acc.y += p.y;
         }
-        const z2 own = tr[(int64_t)(id * kNyBasis + s) * n + row];  // u or du/dn at the row
-        d[s] = {acc.x - 0.5 * own.x, acc.y - 0.5 * own.y};
+        const z2 u = tr[(int64_t)s * n + row], f = tr[(int64_t)(kNyBasis + s) * n + row];
+        const z2 af = zmul(al, f);
+        d[s] = {acc.x - u.x - af.x, acc.y - u.y - af.y};
       }
       // z = R^{-H} d (R^H lower triangular)
       z2 z[kNyBasis];
@@ -277,25 +277,11 @@ __global__ void __launch_bounds__(kNyCorrT) k_ny_correct(NyInst I) {
         }
       }
       for (int j = 0; j < kNyNodes; ++j) {
-        const z2 wp = {wv[j].x / sc[j], wv[j].y / sc[j]};
-        const z2 wf = {wv[kNyNodes + j].x / sc[kNyNodes + j], wv[kNyNodes + j].y / sc[kNyNodes + j]};
-        if (id == 0) {
-          dP[j] = wp;
-          dF[j] = wf;
-        } else {
-          hP[j] = wp;
-          hF[j] = wf;
-        }
+        const int64_t o = row + (b + j) * n;
+        const double sp = sc[j], sf = sc[kNyNodes + j];
+        M1[o] = {M1[o].x - wv[j].x / sp, M1[o].y - wv[j].y / sp};
+        M2[o] = {M2[o].x - wv[kNyNodes + j].x / sf, M2[o].y - wv[kNyNodes + j].y / sf};
       }
-    }
-    for (int j = 0; j < kNyNodes; ++j) {
-      const int64_t o = row + (b + j) * n;
-      // M1 += -dD - alpha dH = -w_p(pressure) - alpha w_p(flux identity)
-      const z2 aH = zmul(al, hP[j]);
-      M1[o] = {M1[o].x - dP[j].x - aH.x, M1[o].y - dP[j].y - aH.y};
-      // M2 += dS + alpha dK' = -w_f(pressure) - alpha w_f(flux identity)
-      const z2 aK = zmul(al, hF[j]);
-      M2[o] = {M2[o].x - dF[j].x - aK.x, M2[o].y - dF[j].y - aK.y};
     }
   }
 }
@@ -303,17 +289,16 @@ __global__ void __launch_bounds__(kNyCorrT) k_ny_correct(NyInst I) {
 }  // namespace
 
 int64_t nystrom_scratch_doubles(int64_t n, int32_t n_chunks) {
-  return 2 * (2 * (int64_t)kNyBasis * n) + 2 * ((int64_t)n_chunks * 2 * kNyBasis * n);
+  return 2 * (2 * (int64_t)kNyBasis * n) + 2 * ((int64_t)n_chunks * kNyBasis * n);
 }
 
+// About four waves of resident CTAs (152 SMs x 5 CTAs of 96-register threads), so the
+// last, partial wave is a small share; ranges a whole number of tiles wide.
 int32_t nystrom_chunks(int64_t n) {
   const int64_t rb = (n + kNyRows - 1) / kNyRows;
-  const int64_t want = 152 * 4;
-  int64_t c = (want + rb - 1) / rb;
-  c = std::max<int64_t>(1, std::min<int64_t>(c, 64));
-  // every range holds at least one tile
-  c = std::min<int64_t>(c, (n + kNyTile - 1) / kNyTile);
-  return (int32_t)std::max<int64_t>(1, c);
+  const int64_t want = std::min<int64_t>(64, std::max<int64_t>(1, (152 * 5 * 4 + rb - 1) / rb));
+  const int64_t per = ((n + want - 1) / want + kNyTile - 1) / kNyTile * kNyTile;
+  return (int32_t)std::max<int64_t>(1, (n + per - 1) / per);
 }
 
 void launch_nystrom(const Launch& L, const NyInst& I0) {

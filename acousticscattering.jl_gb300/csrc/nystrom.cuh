@@ -25,7 +25,7 @@ struct NyInst {
   double* M2;           // S + alpha (1/2 I + K') (complex128, column-major, leading dim n)
   double dirs[3 * kNyBasis];  // unit plane-wave directions of the interpolants
   double* trace;        // interpolant traces [2][kNyBasis][n] complex: u, du/dn at the nodes
-  double* part;         // defect partial sums [n_chunks][2 kNyBasis][n] complex
+  double* part;         // combined-defect partial sums [n_chunks][kNyBasis][n] complex
   int32_t n_chunks;     // column ranges of the assembly (partial sums per range)
   int64_t chunk_cols;   // columns per range (a multiple of kNyTile)
   int32_t* status;      // per element: 0, or 1 when its correction fit met a zero pivot

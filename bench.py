@@ -366,6 +366,28 @@ def run_config0(args):
                      (bemgpu.Context.launch_count() - l0) // steps)
     fm, fd = out["mixed"][0], out["double"][0]
     ms = out["mixed"][1]
+    # the same body in the Nystrom discretisation (7 quadrature-node unknowns per panel,
+    # density-interpolation correction): one solve per step, outside the headline timing
+    ny = {"unknowns": 7 * tris.shape[1]}
+    for prec, reps in (("mixed", 5), ("double", 1)):
+        def one_ny():
+            sol = bemgpu.bem(surf, bemgpu.Rigid(), k, incidence_angle=beta,
+                             incidence_azimuth=alpha, precision=prec, ctx=ctx,
+                             discretization="nystrom")
+            f = bemgpu.scattering_amplitude(sol)
+            d = sol.diagnostics()
+            sol.close()
+            return f, d
+        one_ny()
+        ts = []
+        for _ in range(reps):
+            ctx.timer_start()
+            f, d = one_ny()
+            ts.append(ctx.timer_stop())
+        ny[prec] = {"solves_per_s": 1e3 / float(np.mean(ts)), "ms": float(np.mean(ts)),
+                    "assemble_ms": d["assemble_ms"], "factor_ms": d["factor_ms"],
+                    "solve_ms": d["solve_ms"], "ts_db": 20 * math.log10(abs(f))}
+    ny["ts_db_minus_collocation_fp64"] = ny["double"]["ts_db"] - 20 * math.log10(abs(fd))
     cpu = None
     if not args.no_cpu:
         from oracle import oracle as O
@@ -384,7 +406,7 @@ def run_config0(args):
               "p99_ms": out["double"][3], "ts_db": 20 * math.log10(abs(fd))},
         ts_db=20 * math.log10(abs(fm)),
         ts_error_db_vs_fp64=abs(20 * math.log10(abs(fm)) - 20 * math.log10(abs(fd))),
-        amplitude_rel_error_vs_fp64=abs(fm - fd) / abs(fd),
+        amplitude_rel_error_vs_fp64=abs(fm - fd) / abs(fd), nystrom=ny,
         clocks=out["mixed"][4], gpu_launches=out["mixed"][5], cpu_baseline=cpu)
     print(json.dumps(line))
     return line
