@@ -629,7 +629,8 @@ def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_az
     discretization="nystrom" (Rigid and PressureRelease, dense factor) puts the unknowns on
     the seven quadrature nodes of every panel with the density-interpolation correction of
     the reference's Nyström operators (full.jl:68-128, correction=(method=:dim,)); traces
-    then hold one value per node and point evaluation (pressure) is not available."""
+    then hold one value per node, and pressure() at exterior points recovers the nearest
+    element by the same correction (the reference's exclude_nearest evaluation)."""
     if unsupported:
         raise ArgumentError(f"unsupported option(s): {sorted(unsupported)}")
     if discretization not in C.DISCRETIZATION:

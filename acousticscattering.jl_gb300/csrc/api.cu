@@ -550,6 +550,7 @@ struct FactorData {
   bool mixed = false;      // requested precision
   bool fp32_regular = false;  // regular pairs assembled in FP32
   bool nystrom = false;       // Nyström operators on the node set (mesh = node mesh)
+  std::shared_ptr<MeshData> base_mesh;  // Nyström: the panel mesh of the node set
   int reason = BEMGPU_REASON_NONE;
   double rcond = NAN;
   double matrix_norm = 0.0, anorm = 0.0;
@@ -584,6 +585,7 @@ struct SolutionData {
   bemgpu_diagnostics diag{};
   std::vector<int32_t> parents;         // coupled regions: parent region of each surface,
   std::vector<double> region_k, region_rho;  // wavenumber and density of every region
+  std::shared_ptr<MeshData> base_mesh;  // Nyström: the panel mesh (region test of points)
   bool hmatrix = false;                 // from bemgpu_hmatrix_solve
   bemgpu_hmatrix_stats hm{};
   std::vector<double> gm_hist;          // residual estimates, gm_stride per rhs
@@ -656,6 +658,7 @@ int bind_mesh(bemgpu_ctx* c, FactorData* f, const std::shared_ptr<MeshData>& m) 
   f->nystrom = f->prob.discretization == BEMGPU_NYSTROM;
   if (f->nystrom) {
     f->fp32_regular = false;
+    f->base_mesh = m;
     return nystrom_mesh(c, m.get(), &f->mesh);
   }
   f->mesh = m;
@@ -2043,6 +2046,7 @@ int solve_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<i
     }
     out[t]->nrhs = s.R;
     out[t]->mesh = f->mesh;
+    out[t]->base_mesh = f->base_mesh;
     out[t]->k = f->prob.k;
     out[t]->boundary = f->prob.boundary;
     out[t]->g = f->prob.density_contrast;
@@ -3605,6 +3609,80 @@ int bemgpu_pressure(bemgpu_solution* sol, int32_t rhs, int64_t npts, const doubl
   return bemgpu_pressure_region(sol, rhs, npts, points, field, -1, out);
 }
 
+namespace {
+// Field of a Nyström solution at points (validated by the caller): region and incident
+// value per point from the panel kernel on the panel mesh (its exact solid angles), then
+// the node sum with the nearest element recovered by the interpolant fit (nystrom.cu).
+int nystrom_pressure(bemgpu_ctx* c, SolutionData* s, int32_t rhs, int64_t npts,
+                     const double* points, int32_t field, double* out) {
+  MeshData* base = s->base_mesh.get();
+  if (!base) return fail(c, BEMGPU_EINVAL, "the solution has no panel mesh");
+  const Launch L = c->launch();
+  const int64_t N = s->mesh->n;
+  std::vector<double> pts(points, points + 3 * npts);
+  std::vector<double> dir(s->dirs.begin() + 3 * rhs, s->dirs.begin() + 3 * rhs + 3);
+  Buf dp, dd, dout, dreg, dst, dtr;
+  TRY(upload(c, pts, &dp));
+  TRY(upload(c, dir, &dd));
+  TRY(alloc(c, (size_t)npts * 16, &dout));
+  TRY(alloc(c, (size_t)npts * 4, &dreg));
+  TRY(alloc(c, (size_t)npts * 4, &dst));
+  TRY(alloc(c, (size_t)N * 2 * kNyBasis * 16, &dtr));
+  CUDA_TRY(c, cudaMemsetAsync(dst.p, 0, (size_t)npts * 4, c->stream));
+  PressureInst P{};
+  P.panels = base->panels.as<double>();
+  P.verts = base->verts.as<double>();
+  P.n = base->n;
+  P.dir = dd.as<double>();
+  P.points = dp.as<double>();
+  P.npts = npts;
+  P.out = dout.as<double>();
+  P.region = dreg.as<int32_t>();
+  P.k = P.k_int = s->k;
+  P.g = 1.0;
+  P.eta = base->eta;
+  P.field = BEMGPU_FIELD_INCIDENT;
+  {
+    Prof pr(c, "pressure");
+    launch_pressure(L, P);
+    if (field != BEMGPU_FIELD_INCIDENT) {
+      NyInst T{};
+      T.nodes = s->mesh->panels.as<double>();
+      T.n = N;
+      T.k = s->k;
+      nystrom_directions(T.dirs);
+      T.trace = dtr.as<double>();
+      NyPoints Q{};
+      Q.nodes = T.nodes;
+      Q.n = N;
+      Q.k = s->k;
+      Q.trace = dtr.as<double>();
+      Q.p = s->ps.as<double>() + 2 * (size_t)N * rhs;
+      Q.q = s->qs.as<double>() + 2 * (size_t)N * rhs;
+      Q.points = dp.as<double>();
+      Q.npts = npts;
+      Q.region = dreg.as<int32_t>();
+      Q.out = dout.as<double>();
+      Q.field = field == BEMGPU_FIELD_TOTAL ? 0 : 1;
+      Q.status = dst.as<int32_t>();
+      launch_nystrom_pressure(L, T, Q);
+    }
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  std::vector<int32_t> reg, st;
+  CUDA_TRY(c, cudaMemcpyAsync(out, dout.p, (size_t)npts * 16, cudaMemcpyDeviceToHost, c->stream));
+  TRY(download(c, dreg, &reg, (size_t)npts));
+  TRY(download(c, dst, &st, (size_t)npts));
+  for (int64_t i = 0; i < npts; ++i) {
+    if (field != BEMGPU_FIELD_INCIDENT && reg[(size_t)i] == 1)
+      return fail(c, BEMGPU_EINVAL, "point lies inside the body, where no exterior field exists");
+    if (st[(size_t)i])
+      return fail(c, BEMGPU_EINVAL, "density-interpolation fit is rank-deficient near a point");
+  }
+  return BEMGPU_OK;
+}
+}  // namespace
+
 int bemgpu_pressure_region(bemgpu_solution* sol, int32_t rhs, int64_t npts, const double* points,
                            int32_t field, int32_t region, double* out) {
   if (!sol) return fail(nullptr, BEMGPU_EINVAL, "null solution");
@@ -3613,8 +3691,6 @@ int bemgpu_pressure_region(bemgpu_solution* sol, int32_t rhs, int64_t npts, cons
   std::lock_guard<std::recursive_mutex> lk(c->mu);
   cudaSetDevice(c->device);
   if (rhs < 0 || rhs >= s->nrhs) return fail(c, BEMGPU_EINVAL, "rhs index out of range");
-  if (s->mesh && s->mesh->nystrom)
-    return fail(c, BEMGPU_EINVAL, "pressure at points needs the collocation discretisation");
   if (field < BEMGPU_FIELD_TOTAL || field > BEMGPU_FIELD_INTERIOR)
     return fail(c, BEMGPU_EINVAL, "field must be :total, :scattered, :incident or :interior");
   if (region >= 0 && !s->region)
@@ -3629,6 +3705,7 @@ int bemgpu_pressure_region(bemgpu_solution* sol, int32_t rhs, int64_t npts, cons
   const bool fluid = s->boundary == BEMGPU_FLUID || s->region;
   if (field == BEMGPU_FIELD_INTERIOR && !fluid)
     return fail(c, BEMGPU_EINVAL, "interior field requires a fluid-filled body");
+  if (s->mesh->nystrom) return nystrom_pressure(c, s, rhs, npts, points, field, out);
   std::vector<double> pts(points, points + 3 * npts);
   std::vector<double> dir(s->dirs.begin() + 3 * rhs, s->dirs.begin() + 3 * rhs + 3);
   Buf dp, dd, dout, dreg;

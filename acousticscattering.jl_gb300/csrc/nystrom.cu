@@ -178,6 +178,80 @@ __global__ void __launch_bounds__(kNyRows) k_ny_assemble(NyInst I) {
 constexpr int kNyFit = 2 * kNyNodes;  // unknown weights per element
 constexpr int kNyCorrT = 64;
 
+// Scaled trace matrix of one element and its Householder QR (per thread, local memory).
+struct NyFit {
+  z2 B[kNyFit][kNyBasis];  // A^H, reduced in place to R
+  z2 V[kNyFit][kNyBasis];  // Householder vectors (unit norm), column c from row c on
+  double sc[kNyFit];       // row scales
+};
+
+// Factor the fit of the element whose nodes are b..b+6; false when R has a pivot below
+// 1e-13 of the first (rank-deficient fit).
+__device__ bool ny_fit_factor(NyFit& F, const z2* tr, int64_t n, int64_t b) {
+  for (int j = 0; j < kNyFit; ++j) {
+    const int64_t node = b + (j % kNyNodes);
+    const int t = j < kNyNodes ? 0 : 1;
+    double s2 = 0.0;
+    for (int s = 0; s < kNyBasis; ++s) {
+      const z2 v = tr[(int64_t)(t * kNyBasis + s) * n + node];
+      F.B[j][s] = v;
+      s2 += v.x * v.x + v.y * v.y;
+    }
+    F.sc[j] = fmax(sqrt(s2), 1e-300);
+    for (int s = 0; s < kNyBasis; ++s) F.B[j][s] = {F.B[j][s].x / F.sc[j], -F.B[j][s].y / F.sc[j]};
+  }
+  for (int c = 0; c < kNyBasis; ++c) {
+    double nx = 0.0;
+    for (int j = c; j < kNyFit; ++j) nx += F.B[j][c].x * F.B[j][c].x + F.B[j][c].y * F.B[j][c].y;
+    nx = sqrt(nx);
+    const z2 x0 = F.B[c][c];
+    const double ax0 = hypot(x0.x, x0.y);
+    const z2 ph = ax0 > 0.0 ? z2{x0.x / ax0, x0.y / ax0} : z2{1.0, 0.0};
+    const z2 alpha = {-ph.x * nx, -ph.y * nx};
+    for (int j = 0; j < kNyFit; ++j) F.V[j][c] = {0.0, 0.0};
+    double vn = 0.0;
+    for (int j = c; j < kNyFit; ++j) {
+      F.V[j][c] = j == c ? z2{x0.x - alpha.x, x0.y - alpha.y} : F.B[j][c];
+      vn += F.V[j][c].x * F.V[j][c].x + F.V[j][c].y * F.V[j][c].y;
+    }
+    vn = sqrt(vn);
+    if (!(vn > 0.0)) return false;
+    for (int j = c; j < kNyFit; ++j) F.V[j][c] = {F.V[j][c].x / vn, F.V[j][c].y / vn};
+    for (int q = c; q < kNyBasis; ++q) {
+      z2 dot = {0.0, 0.0};
+      for (int j = c; j < kNyFit; ++j) zfma(dot, zconj(F.V[j][c]), F.B[j][q]);
+      for (int j = c; j < kNyFit; ++j) {
+        const z2 v2 = {2.0 * F.V[j][c].x, 2.0 * F.V[j][c].y};
+        zfms(F.B[j][q], v2, dot);
+      }
+    }
+  }
+  const double r00 = hypot(F.B[0][0].x, F.B[0][0].y);
+  for (int c = 0; c < kNyBasis; ++c)
+    if (!(hypot(F.B[c][c].x, F.B[c][c].y) > 1e-13 * r00)) return false;
+  return true;
+}
+
+// Weights w (14, unscaled: pressure weights then flux weights) of a defect d (9).
+__device__ void ny_fit_solve(const NyFit& F, const z2* d, z2* w) {
+  z2 z[kNyBasis];  // R^{-H} d (R^H lower triangular)
+  for (int q = 0; q < kNyBasis; ++q) {
+    z2 v = d[q];
+    for (int p = 0; p < q; ++p) zfms(v, zconj(F.B[p][q]), z[p]);
+    z[q] = zdiv(v, zconj(F.B[q][q]));
+  }
+  for (int j = 0; j < kNyFit; ++j) w[j] = j < kNyBasis ? z[j] : z2{0.0, 0.0};
+  for (int c = kNyBasis - 1; c >= 0; --c) {  // w = H_0 ... H_8 [z; 0]
+    z2 dot = {0.0, 0.0};
+    for (int j = c; j < kNyFit; ++j) zfma(dot, zconj(F.V[j][c]), w[j]);
+    for (int j = c; j < kNyFit; ++j) {
+      const z2 v2 = {2.0 * F.V[j][c].x, 2.0 * F.V[j][c].y};
+      zfms(w[j], v2, dot);
+    }
+  }
+  for (int j = 0; j < kNyFit; ++j) w[j] = {w[j].x / F.sc[j], w[j].y / F.sc[j]};
+}
+
 __global__ void __launch_bounds__(kNyCorrT) k_ny_correct(NyInst I) {
   const int64_t e = (int64_t)blockIdx.x * kNyCorrT + threadIdx.x;
   const int64_t n = I.n;
@@ -187,103 +261,161 @@ __global__ void __launch_bounds__(kNyCorrT) k_ny_correct(NyInst I) {
   z2* M1 = reinterpret_cast<z2*>(I.M1);
   z2* M2 = reinterpret_cast<z2*>(I.M2);
   const int64_t b = e * kNyNodes;
-  z2 B[kNyFit][kNyBasis];  // A^H, reduced in place to R
-  z2 V[kNyFit][kNyBasis];  // Householder vectors (unit norm), column c from row c on
-  double sc[kNyFit];
-  for (int j = 0; j < kNyFit; ++j) {
-    const int64_t node = b + (j % kNyNodes);
-    const int t = j < kNyNodes ? 0 : 1;
-    double s2 = 0.0;
-    for (int s = 0; s < kNyBasis; ++s) {
-      const z2 v = tr[(int64_t)(t * kNyBasis + s) * n + node];
-      B[j][s] = v;
-      s2 += v.x * v.x + v.y * v.y;
-    }
-    sc[j] = fmax(sqrt(s2), 1e-300);
-    for (int s = 0; s < kNyBasis; ++s) B[j][s] = {B[j][s].x / sc[j], -B[j][s].y / sc[j]};
-  }
-  int singular = 0;
-  for (int c = 0; c < kNyBasis; ++c) {
-    double nx = 0.0;
-    for (int j = c; j < kNyFit; ++j) nx += B[j][c].x * B[j][c].x + B[j][c].y * B[j][c].y;
-    nx = sqrt(nx);
-    const z2 x0 = B[c][c];
-    const double ax0 = hypot(x0.x, x0.y);
-    const z2 ph = ax0 > 0.0 ? z2{x0.x / ax0, x0.y / ax0} : z2{1.0, 0.0};
-    const z2 alpha = {-ph.x * nx, -ph.y * nx};
-    for (int j = 0; j < kNyFit; ++j) V[j][c] = {0.0, 0.0};
-    double vn = 0.0;
-    for (int j = c; j < kNyFit; ++j) {
-      V[j][c] = j == c ? z2{x0.x - alpha.x, x0.y - alpha.y} : B[j][c];
-      vn += V[j][c].x * V[j][c].x + V[j][c].y * V[j][c].y;
-    }
-    vn = sqrt(vn);
-    if (!(vn > 0.0)) {
-      singular = 1;
-      break;
-    }
-    for (int j = c; j < kNyFit; ++j) V[j][c] = {V[j][c].x / vn, V[j][c].y / vn};
-    for (int q = c; q < kNyBasis; ++q) {
-      z2 dot = {0.0, 0.0};
-      for (int j = c; j < kNyFit; ++j) zfma(dot, zconj(V[j][c]), B[j][q]);
-      for (int j = c; j < kNyFit; ++j) {
-        const z2 v2 = {2.0 * V[j][c].x, 2.0 * V[j][c].y};
-        zfms(B[j][q], v2, dot);
-      }
-    }
-  }
-  if (!singular) {
-    const double r00 = hypot(B[0][0].x, B[0][0].y);
-    for (int c = 0; c < kNyBasis; ++c)
-      if (!(hypot(B[c][c].x, B[c][c].y) > 1e-13 * r00)) singular = 1;
-  }
-  if (singular) {  // rank-deficient fit: the element keeps its uncorrected rule
+  NyFit F;
+  if (!ny_fit_factor(F, tr, n, b)) {  // rank-deficient fit: the element keeps its rule
     I.status[e] = 1;
     return;
   }
   const z2 al = {I.a_re, I.a_im};
   for (int t = 0; t < kNyNodes; ++t) {
     const int64_t row = b + t;
-    {
-      // combined defect e_s = (M2 F + M1 U)_s - u_s - alpha du_s/dn at the row
-      z2 d[kNyBasis];
-      for (int s = 0; s < kNyBasis; ++s) {
-        z2 acc = {0.0, 0.0};
-        for (int c = 0; c < I.n_chunks; ++c) {
-          const z2 p = part[((int64_t)c * kNyBasis + s) * n + row];
-          acc.x += p.x;
-          acc.y += p.y;
-        }
-        const z2 u = tr[(int64_t)s * n + row], f = tr[(int64_t)(kNyBasis + s) * n + row];
-        const z2 af = zmul(al, f);
-        d[s] = {acc.x - u.x - af.x, acc.y - u.y - af.y};
+    // combined defect e_s = (M2 F + M1 U)_s - u_s - alpha du_s/dn at the row
+    z2 d[kNyBasis];
+    for (int s = 0; s < kNyBasis; ++s) {
+      z2 acc = {0.0, 0.0};
+      for (int c = 0; c < I.n_chunks; ++c) {
+        const z2 p = part[((int64_t)c * kNyBasis + s) * n + row];
+        acc.x += p.x;
+        acc.y += p.y;
       }
-      // z = R^{-H} d (R^H lower triangular)
-      z2 z[kNyBasis];
-      for (int q = 0; q < kNyBasis; ++q) {
-        z2 v = d[q];
-        for (int p = 0; p < q; ++p) zfms(v, zconj(B[p][q]), z[p]);
-        z[q] = zdiv(v, zconj(B[q][q]));
-      }
-      // w~ = H_0 ... H_8 [z; 0]
-      z2 wv[kNyFit];
-      for (int j = 0; j < kNyFit; ++j) wv[j] = j < kNyBasis ? z[j] : z2{0.0, 0.0};
-      for (int c = kNyBasis - 1; c >= 0; --c) {
-        z2 dot = {0.0, 0.0};
-        for (int j = c; j < kNyFit; ++j) zfma(dot, zconj(V[j][c]), wv[j]);
-        for (int j = c; j < kNyFit; ++j) {
-          const z2 v2 = {2.0 * V[j][c].x, 2.0 * V[j][c].y};
-          zfms(wv[j], v2, dot);
-        }
-      }
-      for (int j = 0; j < kNyNodes; ++j) {
-        const int64_t o = row + (b + j) * n;
-        const double sp = sc[j], sf = sc[kNyNodes + j];
-        M1[o] = {M1[o].x - wv[j].x / sp, M1[o].y - wv[j].y / sp};
-        M2[o] = {M2[o].x - wv[kNyNodes + j].x / sf, M2[o].y - wv[kNyNodes + j].y / sf};
-      }
+      const z2 u = tr[(int64_t)s * n + row], f = tr[(int64_t)(kNyBasis + s) * n + row];
+      const z2 af = zmul(al, f);
+      d[s] = {acc.x - u.x - af.x, acc.y - u.y - af.y};
+    }
+    z2 w[kNyFit];
+    ny_fit_solve(F, d, w);
+    for (int j = 0; j < kNyNodes; ++j) {
+      const int64_t o = row + (b + j) * n;
+      M1[o] = {M1[o].x - w[j].x, M1[o].y - w[j].y};
+      M2[o] = {M2[o].x - w[kNyNodes + j].x, M2[o].y - w[kNyNodes + j].y};
     }
   }
+}
+
+// ------------------------------------------------------------------ point evaluation
+// Scattered field u_s(x) = sum_j w_j [dG/dn_y(x, y_j) p_j - G(x, y_j) q_j] at a point of
+// the exterior (or on the surface, its exterior limit), one CTA per point, in the form
+// the reference uses for point evaluation (fields/pressure.jl:453-467 through
+// quadrature/fluid.jl:104-163 with exclude_nearest=true): the element of the nearest node
+// is left out of the node sum and its contribution recovered from the fit of the
+// interpolants' defect  0 * u(x) + S_excl du/dn - D_excl u  (multiplier 0 outside):
+// u_s += sum_{j in e} (w_p,j p_j + w_f,j q_j).
+constexpr int kNyPtT = 256;
+constexpr int kNyPtSums = 2 * (1 + kNyBasis);  // field + nine defects, complex
+
+__global__ void __launch_bounds__(kNyPtT) k_ny_pressure(NyPoints P) {
+  const int64_t ip = blockIdx.x;
+  if (ip >= P.npts) return;
+  if (P.region[ip] == 1) {  // inside the body: no exterior field (the host reports it)
+    if (threadIdx.x == 0) {
+      P.out[2 * ip] = NAN;
+      P.out[2 * ip + 1] = NAN;
+    }
+    return;
+  }
+  const int64_t n = P.n;
+  const double x[3] = {P.points[3 * ip], P.points[3 * ip + 1], P.points[3 * ip + 2]};
+  __shared__ double s_d[kNyPtT];
+  __shared__ int64_t s_i[kNyPtT];
+  __shared__ double s_sum[kNyPtT / 32][kNyPtSums];
+  // nearest node (smallest index among equal distances)
+  double best = INFINITY;
+  int64_t bi = INT64_MAX;
+  for (int64_t j = threadIdx.x; j < n; j += kNyPtT) {
+    const double* r = P.nodes + j * kPanelDoubles;
+    const double dx = x[0] - r[0], dy = x[1] - r[1], dz = x[2] - r[2];
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 < best) {
+      best = d2;
+      bi = j;
+    }
+  }
+  s_d[threadIdx.x] = best;
+  s_i[threadIdx.x] = bi;
+  __syncthreads();
+  for (int h = kNyPtT / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) {
+      const double od = s_d[threadIdx.x + h];
+      const int64_t oi = s_i[threadIdx.x + h];
+      if (od < s_d[threadIdx.x] || (od == s_d[threadIdx.x] && oi < s_i[threadIdx.x])) {
+        s_d[threadIdx.x] = od;
+        s_i[threadIdx.x] = oi;
+      }
+    }
+    __syncthreads();
+  }
+  const int64_t b = (s_i[0] / kNyNodes) * kNyNodes;
+  const z2* tr = reinterpret_cast<const z2*>(P.trace);
+  const z2* p = reinterpret_cast<const z2*>(P.p);
+  const z2* q = reinterpret_cast<const z2*>(P.q);
+  const double k = P.k;
+  z2 acc[1 + kNyBasis];
+#pragma unroll
+  for (int t = 0; t <= kNyBasis; ++t) acc[t] = {0.0, 0.0};
+  for (int64_t j = threadIdx.x; j < n; j += kNyPtT) {
+    if (j >= b && j < b + kNyNodes) continue;
+    const double* r = P.nodes + j * kPanelDoubles;
+    const double dx = x[0] - r[0], dy = x[1] - r[1], dz = x[2] - r[2];
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    const double rr = sqrt(r2), ir = 1.0 / rr;
+    double sn, cs;
+    sincos(k * rr, &sn, &cs);
+    const double w = r[6];
+    const double gs = kInv4Pi * ir;
+    const z2 G = {cs * gs, sn * gs};
+    const z2 G1 = zmul(G, z2{-ir, k});
+    const double fd = -(dx * r[3] + dy * r[4] + dz * r[5]) * ir * w;
+    const z2 S = {G.x * w, G.y * w};
+    const z2 D = {G1.x * fd, G1.y * fd};
+    zfma(acc[0], D, p[j]);
+    zfms(acc[0], S, q[j]);
+#pragma unroll
+    for (int s = 0; s < kNyBasis; ++s) {
+      zfma(acc[1 + s], S, tr[(int64_t)(kNyBasis + s) * n + j]);
+      zfms(acc[1 + s], D, tr[(int64_t)s * n + j]);
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int t = 0; t <= kNyBasis; ++t) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      acc[t].x += __shfl_down_sync(0xffffffffu, acc[t].x, off);
+      acc[t].y += __shfl_down_sync(0xffffffffu, acc[t].y, off);
+    }
+    if (lane == 0) {
+      s_sum[wid][2 * t] = acc[t].x;
+      s_sum[wid][2 * t + 1] = acc[t].y;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  z2 tot[1 + kNyBasis];
+  for (int t = 0; t <= kNyBasis; ++t) {
+    tot[t] = {0.0, 0.0};
+    for (int g = 0; g < kNyPtT / 32; ++g) {
+      tot[t].x += s_sum[g][2 * t];
+      tot[t].y += s_sum[g][2 * t + 1];
+    }
+  }
+  z2 field = tot[0];
+  NyFit F;
+  if (ny_fit_factor(F, tr, n, b)) {
+    z2 w[kNyFit];
+    ny_fit_solve(F, tot + 1, w);
+    for (int j = 0; j < kNyNodes; ++j) {
+      zfma(field, w[j], p[b + j]);
+      zfma(field, w[kNyNodes + j], q[b + j]);
+    }
+  } else {  // rank-deficient fit: the element's own node rule
+    P.status[ip] = 1;
+  }
+  if (P.field == 0) {  // total: the incident value is already in out
+    field.x += P.out[2 * ip];
+    field.y += P.out[2 * ip + 1];
+  }
+  P.out[2 * ip] = field.x;
+  P.out[2 * ip + 1] = field.y;
 }
 
 }  // namespace
@@ -299,6 +431,15 @@ int32_t nystrom_chunks(int64_t n) {
   const int64_t want = std::min<int64_t>(64, std::max<int64_t>(1, (152 * 5 * 4 + rb - 1) / rb));
   const int64_t per = ((n + want - 1) / want + kNyTile - 1) / kNyTile * kNyTile;
   return (int32_t)std::max<int64_t>(1, (n + per - 1) / per);
+}
+
+void launch_nystrom_pressure(const Launch& L, const NyInst& traces, const NyPoints& P) {
+  k_ny_traces<<<(unsigned)((traces.n + 127) / 128), 128, 0, L.stream>>>(traces);
+  count_launch(1);
+  if (P.npts > 0) {
+    k_ny_pressure<<<(unsigned)P.npts, kNyPtT, 0, L.stream>>>(P);
+    count_launch(1);
+  }
 }
 
 void launch_nystrom(const Launch& L, const NyInst& I0) {

@@ -31,6 +31,22 @@ struct NyInst {
   int32_t* status;      // per element: 0, or 1 when its correction fit met a zero pivot
 };
 
+// Points of a Nyström solution's field evaluation (k_ny_pressure).
+struct NyPoints {
+  const double* nodes;   // node records (as NyInst)
+  int64_t n;
+  double k;
+  const double* trace;   // interpolant traces [2][kNyBasis][n] complex
+  const double* p;       // scattered pressure at the nodes (complex128, n)
+  const double* q;       // scattered normal derivative at the nodes (complex128, n)
+  const double* points;  // 3 x npts
+  int64_t npts;
+  const int32_t* region; // per point from the panel pass: 0 exterior, 1 interior, 2 surface
+  double* out;           // complex128 npts: the incident value on entry, the field on exit
+  int32_t field;         // 0 total, 1 scattered
+  int32_t* status;       // per point: 1 when the nearest element's fit was rank-deficient
+};
+
 // Scratch of launch_nystrom in doubles: traces and defect partials.
 int64_t nystrom_scratch_doubles(int64_t n, int32_t n_chunks);
 // Column ranges for n nodes (enough CTAs to fill the SMs a few times over).
@@ -39,6 +55,9 @@ int32_t nystrom_chunks(int64_t n);
 #ifdef __CUDACC__
 // Assembles M1 and M2 of one instance with the correction applied.
 void launch_nystrom(const Launch& L, const NyInst& I);
+// Interpolant traces (traces.trace, from traces.nodes / n / k / dirs), then the field at
+// every point of P.
+void launch_nystrom_pressure(const Launch& L, const NyInst& traces, const NyPoints& P);
 #endif
 
 }  // namespace bemgpu

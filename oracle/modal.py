@@ -58,3 +58,15 @@ def form_function(boundary, k, a, angle=math.pi, g=1.0, h=1.0, m_max=None):
     for m in range(m_max + 1):
         total += (2 * m + 1) * eval_legendre(m, x) * coefficient(boundary, m, k, a, g, h)
     return -1j / k * total
+
+
+def scattered_field(boundary, k, a, r, cos_theta, g=1.0, h=1.0, m_max=None):
+    """Scattered pressure of a unit plane wave at distance r >= a from the sphere's centre,
+    cos_theta = incidence direction . point direction: sum (2m+1) i^m A_m h_m(kr)
+    P_m(cos theta), the near-field form of form_function (whose r -> infinity limit it is)."""
+    m_max = mode_count(k * a) if m_max is None else m_max
+    total = 0j
+    for m in range(m_max + 1):
+        total += ((2 * m + 1) * (1j ** m) * coefficient(boundary, m, k, a, g, h) *
+                  _hs(m, k * r) * eval_legendre(m, cos_theta))
+    return total

@@ -121,6 +121,64 @@ def assemble(P: O.Panels, k, burton_miller=True):
     return 0.5 * I - D - a * H, S + a * (0.5 * I + K)
 
 
+def _element_pinv(u_e, f_e, cutoff=1e-13):
+    """Pseudo-inverse (14 x 9) of one element's scaled trace fit and its row scales."""
+    M = np.concatenate([u_e, f_e], axis=0)
+    sc = np.maximum(np.sqrt((np.abs(M) ** 2).sum(1)), np.finfo(float).eps)
+    A = (M / sc[:, None]).T
+    U, s, Vh = np.linalg.svd(A, full_matrices=False)
+    keep = s > cutoff * s[0]
+    return (Vh[keep].conj().T / s[keep]) @ U[:, keep].conj().T, sc
+
+
+def _inside(P: O.Panels, x):
+    """Solid angle of the closed surface seen from x (Van Oosterom-Strackee) > 2 pi."""
+    R = P.vertices - x[None, None, :]
+    r = np.linalg.norm(R, axis=2)
+    R0, R1, R2 = R[:, 0], R[:, 1], R[:, 2]
+    num = np.einsum("ij,ij->i", R0, np.cross(R1, R2))
+    den = (r[:, 0] * r[:, 1] * r[:, 2] + np.einsum("ij,ij->i", R0, R1) * r[:, 2] +
+           np.einsum("ij,ij->i", R0, R2) * r[:, 1] + np.einsum("ij,ij->i", R1, R2) * r[:, 0])
+    return 2.0 * np.arctan2(num, den).sum() > 2.0 * np.pi
+
+
+def pressure(P: O.Panels, k, points, p, q, direction, field="scattered"):
+    """Field of a Nyström solution at exterior points, in the reference's point-evaluation
+    form (fields/pressure.jl:453-467 through quadrature/fluid.jl:104-163 with
+    exclude_nearest=true): the element of the nearest node is left out of the node sum
+    u_s = sum_j w_j (dG/dn_y p_j - G q_j) and its contribution recovered from the fit of
+    the interpolants' defect 0 * u(x) + S_excl du/dn - D_excl u (multiplier 0 outside)."""
+    y, ny, w = nodes_of(P)
+    u_all, f_all = traces(y, ny, k)
+    d_inc = np.asarray(direction, dtype=np.float64)
+    out = []
+    for x in np.asarray(points, dtype=np.float64).reshape(-1, 3):
+        inc = np.exp(1j * k * (x @ d_inc))
+        if field == "incident":
+            out.append(inc)
+            continue
+        if _inside(P, x):
+            raise ValueError("point lies inside the body")
+        dv = x[None, :] - y
+        r2 = (dv * dv).sum(1)
+        b = (int(np.argmin(r2)) // NODES) * NODES
+        keep = np.ones(len(w), dtype=bool)
+        keep[b:b + NODES] = False
+        r = np.sqrt(r2[keep])
+        ir = 1.0 / r
+        G = np.exp(1j * k * r) * ir / (4 * np.pi)
+        G1 = G * (1j * k - ir)
+        S = G * w[keep]
+        D = -G1 * (dv[keep] * ny[keep]).sum(1) * ir * w[keep]
+        fld = np.sum(D * p[keep] - S * q[keep])
+        defect = S @ f_all[keep] - D @ u_all[keep]
+        pinv, sc = _element_pinv(u_all[b:b + NODES], f_all[b:b + NODES])
+        wt = (pinv @ defect) / sc
+        fld += wt[:NODES] @ p[b:b + NODES] + wt[NODES:] @ q[b:b + NODES]
+        out.append(fld + inc if field == "total" else fld)
+    return np.array(out)
+
+
 def far_field(y, ny, w, k, xhat, p, q):
     """f(xhat) = -(1/4 pi) sum_i w_i (i k xhat.n_i p_i + q_i) e^{-i k xhat.y_i}."""
     xhat = np.asarray(xhat, dtype=np.float64)

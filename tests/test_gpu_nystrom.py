@@ -4,7 +4,8 @@ Operator entries after the element corrections within 1e-11 of the largest entry
 traces and far field within 1e-9; the mixed factor with refinement within 0.01 dB and the
 reference's backward-error contract (fluid_system.jl:172-309); many incidences from one
 factor equal separate solves (sweeps.jl:680-701); the 1280-panel sphere within the
-reference's 0.1 dB of the modal series; unsupported combinations rejected.
+reference's 0.1 dB of the modal series; the field at points (nearest element recovered
+by the fit) equal to the oracle's; unsupported combinations rejected.
 """
 import math
 
@@ -123,6 +124,35 @@ def test_sphere_1280_panels_against_modal(ctx, boundary):
     sol.close()
 
 
+@pytest.mark.parametrize("boundary", ["rigid", "pressure_release"])
+def test_point_field_matches_oracle(ctx, boundary):
+    a = 0.01
+    nodes, tris = meshes.icosphere(a, 2)
+    surf = bemgpu.mesh(nodes, tris)
+    beta, alpha = 0.7, 0.4
+    sol = bemgpu.bem(surf, _bc(boundary), K38, incidence_angle=beta, incidence_azimuth=alpha,
+                     ctx=ctx, discretization="nystrom")
+    p, q = sol.traces()
+    d = O.incidence_direction(beta, alpha)
+    dirs = np.array([[1.0, 0, 0], [0.0, 0.6, 0.8], [-0.6, 0.0, 0.8], [0.0, 0.0, -1.0]])
+    pts = np.concatenate([rf * a * dirs for rf in (1.005, 1.05, 1.3, 3.0)])
+    P = O.Panels(nodes, tris)
+    got = bemgpu.pressure(sol, pts, field="scattered")
+    want = NY.pressure(P, K38, pts, p, q, d, "scattered")
+    assert np.max(np.abs(got - want) / np.abs(want)) < 1e-9
+    inc = bemgpu.pressure(sol, pts, field="incident")
+    assert np.allclose(inc, np.exp(1j * K38 * (pts @ d)), rtol=1e-14, atol=1e-15)
+    assert np.allclose(bemgpu.pressure(sol, pts), inc + got, rtol=1e-12, atol=1e-15)
+    with pytest.raises(bemgpu.ArgumentError):  # inside the body
+        bemgpu.pressure(sol, np.zeros((1, 3)))
+    far_dir, dist = np.array([0.36, 0.48, 0.8]), 1e4
+    far = bemgpu.pressure(sol, dist * far_dir, field="scattered") * dist \
+        * np.exp(-1j * K38 * dist)
+    amp = bemgpu.scattering_amplitude(sol, direction=far_dir)
+    assert abs(far - amp) <= 1e-3 * abs(amp)
+    sol.close()
+
+
 def test_unsupported_combinations_are_rejected(ctx):
     nodes, tris = meshes.icosphere(0.01, 1)
     surf = bemgpu.mesh(nodes, tris)
@@ -131,7 +161,3 @@ def test_unsupported_combinations_are_rejected(ctx):
     with pytest.raises(bemgpu.ArgumentError):
         bemgpu.bem(surf, bemgpu.Rigid(), K38, ctx=ctx, discretization="nystrom",
                    compression=dict(method="hmatrix"))
-    sol = bemgpu.bem(surf, bemgpu.Rigid(), K38, ctx=ctx, discretization="nystrom")
-    with pytest.raises(bemgpu.ArgumentError):
-        sol.pressure(np.array([[0.0, 0.0, 0.05]]))
-    sol.close()

@@ -50,6 +50,33 @@ def test_sphere_against_modal(boundary):
     assert rel < 0.06, rel
 
 
+@pytest.mark.parametrize("boundary", ["rigid", "pressure_release"])
+def test_point_field_against_modal_near_field(boundary):
+    """Nearest-element exclusion + fit at points from 0.5 % to 200 % of the radius off the
+    sphere: the modal scattered field within 5 % at 320 panels."""
+    a = 0.01
+    nodes, tris = meshes.icosphere(a, 2)
+    P = O.Panels(nodes, tris)
+    p, q, _ = NY.solve(nodes, tris, boundary, K38, math.pi / 2, math.pi / 2)
+    d = O.incidence_direction(math.pi / 2, math.pi / 2)
+    dirs = np.array([[1.0, 0, 0], [0.0, 0.6, 0.8], [-0.6, 0.0, 0.8], [0.0, 0.0, -1.0]])
+    pts = np.concatenate([rf * a * dirs for rf in (1.005, 1.05, 1.3, 3.0)])
+    got = NY.pressure(P, K38, pts, p, q, d, "scattered")
+    want = np.array([modal.scattered_field(boundary, K38, a, np.linalg.norm(x),
+                                           (x @ d) / np.linalg.norm(x)) for x in pts])
+    assert np.max(np.abs(got - want)) < 0.05 * np.max(np.abs(want))
+    with pytest.raises(ValueError):
+        NY.pressure(P, K38, np.zeros((1, 3)), p, q, d, "total")
+
+
+def test_modal_near_field_tends_to_the_form_function():
+    a, r = 0.01, 1e5
+    for b in ("rigid", "pressure_release"):
+        near = modal.scattered_field(b, K38, a, r, -1.0) * r * np.exp(-1j * K38 * r)
+        far = modal.form_function(b, K38, a)
+        assert abs(near - far) < 1e-4 * abs(far)
+
+
 def test_refinement_reduces_error():
     e1 = _ts_error("rigid", 1)[1]
     e2 = _ts_error("rigid", 2)[1]
