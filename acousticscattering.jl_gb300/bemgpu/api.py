@@ -263,8 +263,6 @@ def _problem(boundary, k, formulation=None, precision="double", equilibrate=True
         raise ArgumentError("boundary must be Rigid(), PressureRelease() or FluidFilled(g, h)")
     if discretization not in C.DISCRETIZATION:
         raise ArgumentError("discretization must be :collocation or :nystrom")
-    if discretization == "nystrom" and isinstance(boundary, FluidFilled):
-        raise ArgumentError("the Nyström discretisation covers rigid and pressure-release bodies")
     if formulation not in _FORMULATIONS:
         raise ArgumentError("formulation must be :burton_miller, :cbie or :muller")
     if precision not in ("double", "mixed"):
@@ -626,11 +624,11 @@ def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_az
     (or with method="none") the system is factored densely; gmres_kwargs then have no
     effect, as the direct solve meets any GMRES tolerance.
 
-    discretization="nystrom" (Rigid and PressureRelease, dense factor) puts the unknowns on
-    the seven quadrature nodes of every panel with the density-interpolation correction of
-    the reference's Nyström operators (full.jl:68-128, correction=(method=:dim,)); traces
-    then hold one value per node, and pressure() at exterior points recovers the nearest
-    element by the same correction (the reference's exclude_nearest evaluation)."""
+    discretization="nystrom" (one surface, dense factor) puts the unknowns on the seven
+    quadrature nodes of every panel with the density-interpolation correction of the
+    reference's Nyström operators (full.jl:68-128 and 289-346, correction=(method=:dim,));
+    traces then hold one value per node, and pressure() recovers the nearest element by
+    the same correction (the reference's exclude_nearest evaluation)."""
     if unsupported:
         raise ArgumentError(f"unsupported option(s): {sorted(unsupported)}")
     if discretization not in C.DISCRETIZATION:

@@ -618,9 +618,6 @@ int check_problem(bemgpu_ctx* c, const bemgpu_problem& p, int* kind) {
     return fail(c, BEMGPU_EINVAL, "near_eta must be finite and positive");
   if (p.discretization != BEMGPU_COLLOCATION && p.discretization != BEMGPU_NYSTROM)
     return fail(c, BEMGPU_EINVAL, "discretization must be :collocation or :nystrom");
-  if (p.discretization == BEMGPU_NYSTROM && p.boundary == BEMGPU_FLUID)
-    return fail(c, BEMGPU_EINVAL,
-                "the Nyström discretisation covers rigid and pressure-release bodies");
   if (p.boundary == BEMGPU_RIGID || p.boundary == BEMGPU_PRESSURE_RELEASE) {
     int f = p.formulation == BEMGPU_FORMULATION_DEFAULT ? BEMGPU_BURTON_MILLER : p.formulation;
     if (f != BEMGPU_BURTON_MILLER && f != BEMGPU_CBIE)
@@ -687,20 +684,23 @@ int to_device(bemgpu_ctx* c, const std::vector<T>& h, Buf* out) {
 }
 
 // ------------------------------------------------------------------ assembly
-// M1 and M2 of one Nyström instance (complex128, node order), corrected on every element.
+// Operators of one Nyström instance (complex128, node order), corrected on every element:
+// rigid/soft M1 and M2; fluid bodies the 2N x 2N system of their formulation.
 int assemble_nystrom(bemgpu_ctx* c, FactorData* f) {
   const Launch L = c->launch();
   MeshData* m = f->mesh.get();
   const int64_t N = m->n;
-  f->n = f->N = N;
+  const int32_t fluid = f->kind == kAsmMuller ? 1 : f->kind == kAsmFluidCBIE ? 2 : 0;
+  f->n = N;
+  f->N = fluid ? 2 * N : N;
   f->a32 = false;
   f->rhs_is_m2 = f->prob.boundary == BEMGPU_RIGID;
-  TRY(alloc(c, (size_t)N * N * 16, &f->A));
-  TRY(alloc(c, (size_t)N * N * 16, &f->Mrhs));
+  TRY(alloc(c, (size_t)f->N * f->N * 16, &f->A));
+  if (!fluid) TRY(alloc(c, (size_t)N * N * 16, &f->Mrhs));
   const int32_t chunks = nystrom_chunks(N);
   const int64_t ne = N / kNyNodes;
   Buf scratch, status;
-  TRY(alloc(c, (size_t)nystrom_scratch_doubles(N, chunks) * 8, &scratch));
+  TRY(alloc(c, (size_t)nystrom_scratch_doubles(N, chunks, fluid) * 8, &scratch));
   TRY(alloc(c, (size_t)ne * 4, &status));
   CUDA_TRY(c, cudaMemsetAsync(status.p, 0, (size_t)ne * 4, c->stream));
   NyInst I{};
@@ -709,12 +709,22 @@ int assemble_nystrom(bemgpu_ctx* c, FactorData* f) {
   I.k = f->prob.k;
   I.a_re = 0.0;
   I.a_im = f->kind == kAsmBM ? 1.0 / f->prob.k : 0.0;
-  // rigid: system M1, rhs M2; pressure release: system M2, rhs M1
-  I.M1 = (f->rhs_is_m2 ? f->A : f->Mrhs).as<double>();
-  I.M2 = (f->rhs_is_m2 ? f->Mrhs : f->A).as<double>();
   nystrom_directions(I.dirs);
+  const int64_t tr_doubles = 2 * (2 * (int64_t)kNyBasis * N);
   I.trace = scratch.as<double>();
-  I.part = scratch.as<double>() + 2 * (2 * (int64_t)kNyBasis * N);
+  if (fluid) {
+    I.fluid = fluid;
+    I.k_int = f->prob.k / f->prob.soundspeed_contrast;
+    I.g = f->prob.density_contrast;
+    I.A = f->A.as<double>();
+    I.trace_i = scratch.as<double>() + tr_doubles;
+    I.part = scratch.as<double>() + 2 * tr_doubles;
+  } else {
+    // rigid: system M1, rhs M2; pressure release: system M2, rhs M1
+    I.M1 = (f->rhs_is_m2 ? f->A : f->Mrhs).as<double>();
+    I.M2 = (f->rhs_is_m2 ? f->Mrhs : f->A).as<double>();
+    I.part = scratch.as<double>() + tr_doubles;
+  }
   I.n_chunks = chunks;
   I.status = status.as<int32_t>();
   {
@@ -3485,6 +3495,8 @@ int bemgpu_region_solve(bemgpu_ctx* c, int32_t count, const bemgpu_mesh* const* 
     if (std::fabs(problem->near_eta - surfaces[i]->d->eta) > 0)
       return fail(c, BEMGPU_EINVAL, "near_eta differs from the mesh's (upload with that eta)");
   }
+  if (problem->discretization != BEMGPU_COLLOCATION)
+    return fail(c, BEMGPU_EINVAL, "coupled regions use the collocation discretisation");
   bemgpu_problem q = *problem;
   q.boundary = BEMGPU_FLUID;
   q.density_contrast = q.soundspeed_contrast = 1.0;  // per region below
@@ -3621,13 +3633,15 @@ int nystrom_pressure(bemgpu_ctx* c, SolutionData* s, int32_t rhs, int64_t npts,
   const int64_t N = s->mesh->n;
   std::vector<double> pts(points, points + 3 * npts);
   std::vector<double> dir(s->dirs.begin() + 3 * rhs, s->dirs.begin() + 3 * rhs + 3);
-  Buf dp, dd, dout, dreg, dst, dtr;
+  const bool fluid = s->boundary == BEMGPU_FLUID;
+  Buf dp, dd, dout, dreg, dst, dtr, dtri;
   TRY(upload(c, pts, &dp));
   TRY(upload(c, dir, &dd));
   TRY(alloc(c, (size_t)npts * 16, &dout));
   TRY(alloc(c, (size_t)npts * 4, &dreg));
   TRY(alloc(c, (size_t)npts * 4, &dst));
   TRY(alloc(c, (size_t)N * 2 * kNyBasis * 16, &dtr));
+  if (fluid) TRY(alloc(c, (size_t)N * 2 * kNyBasis * 16, &dtri));
   CUDA_TRY(c, cudaMemsetAsync(dst.p, 0, (size_t)npts * 4, c->stream));
   PressureInst P{};
   P.panels = base->panels.as<double>();
@@ -3642,6 +3656,7 @@ int nystrom_pressure(bemgpu_ctx* c, SolutionData* s, int32_t rhs, int64_t npts,
   P.g = 1.0;
   P.eta = base->eta;
   P.field = BEMGPU_FIELD_INCIDENT;
+  P.fluid = fluid ? 1 : 0;
   {
     Prof pr(c, "pressure");
     launch_pressure(L, P);
@@ -3652,7 +3667,20 @@ int nystrom_pressure(bemgpu_ctx* c, SolutionData* s, int32_t rhs, int64_t npts,
       T.k = s->k;
       nystrom_directions(T.dirs);
       T.trace = dtr.as<double>();
+      if (fluid) {  // the interior wavenumber's traces (k_int) through a second instance
+        NyInst Ti = T;
+        Ti.k = s->k / s->h;
+        Ti.trace = dtri.as<double>();
+        NyPoints none{};
+        launch_nystrom_pressure(L, Ti, none);
+      }
       NyPoints Q{};
+      Q.fluid = fluid ? 1 : 0;
+      Q.k_int = s->k / s->h;
+      Q.g = fluid ? s->g : 1.0;
+      Q.trace_i = fluid ? dtri.as<double>() : nullptr;
+      for (int a = 0; a < 3; ++a) Q.dir[a] = dir[(size_t)a];
+      for (int a = 0; a < 3 * kNyBasis; ++a) Q.dirs[a] = T.dirs[a];
       Q.nodes = T.nodes;
       Q.n = N;
       Q.k = s->k;
@@ -3663,7 +3691,7 @@ int nystrom_pressure(bemgpu_ctx* c, SolutionData* s, int32_t rhs, int64_t npts,
       Q.npts = npts;
       Q.region = dreg.as<int32_t>();
       Q.out = dout.as<double>();
-      Q.field = field == BEMGPU_FIELD_TOTAL ? 0 : 1;
+      Q.field = field;
       Q.status = dst.as<int32_t>();
       launch_nystrom_pressure(L, T, Q);
     }
@@ -3674,8 +3702,13 @@ int nystrom_pressure(bemgpu_ctx* c, SolutionData* s, int32_t rhs, int64_t npts,
   TRY(download(c, dreg, &reg, (size_t)npts));
   TRY(download(c, dst, &st, (size_t)npts));
   for (int64_t i = 0; i < npts; ++i) {
-    if (field != BEMGPU_FIELD_INCIDENT && reg[(size_t)i] == 1)
-      return fail(c, BEMGPU_EINVAL, "point lies inside the body, where no exterior field exists");
+    if (std::isnan(out[2 * i]) && field != BEMGPU_FIELD_INCIDENT) {
+      if (field == BEMGPU_FIELD_INTERIOR)
+        return fail(c, BEMGPU_EINVAL, "interior field requested at an exterior point");
+      return fail(c, BEMGPU_EINVAL,
+                  reg[(size_t)i] == 1 ? "point lies inside the body, where no exterior field exists"
+                                      : "field does not exist at this point");
+    }
     if (st[(size_t)i])
       return fail(c, BEMGPU_EINVAL, "density-interpolation fit is rank-deficient near a point");
   }

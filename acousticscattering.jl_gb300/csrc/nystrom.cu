@@ -292,22 +292,218 @@ __global__ void __launch_bounds__(kNyCorrT) k_ny_correct(NyInst I) {
   }
 }
 
+// ------------------------------------------------------------------ fluid bodies
+// The panel path's fluid blocks on the nodes (pair i != j; the identity parts on the
+// diagonal):
+//   Mueller: [I - De + Di, Se - g Si; -He + Hi/g, I + K'e - K'i]
+//   CBIE:    [1/2 I - De,  Se;        1/2 I + Di,  -g Si]
+// with e / i the operators at k / k_int.  Each wavenumber's operators are corrected on
+// their own (the blocks mix them), so the defects of its identities are summed apart:
+// slots 0 (S/D at k), 1 (K'/H at k), 2 (S/D at k_int), 3 (K'/H at k_int) for Mueller;
+// 0 (S/D at k), 1 (S/D at k_int) for CBIE.
+template <bool MULLER>
+__global__ void __launch_bounds__(kNyRows) k_ny_assemble_fluid(NyInst I) {
+  constexpr int ND = MULLER ? 4 : 2;
+  const int64_t n = I.n, lda = 2 * I.n;
+  const int64_t i = (int64_t)blockIdx.x * kNyRows + threadIdx.x;
+  const int64_t c0 = (int64_t)blockIdx.y * I.chunk_cols;
+  const int64_t c1 = min(n, c0 + I.chunk_cols);
+  __shared__ double s_node[kNyTile][7];
+  __shared__ z2 s_tr[4 * kNyBasis][kNyTile];  // u, du/dn at k, then at k_int
+  const bool row = i < n;
+  double xi[3] = {0, 0, 0}, ni[3] = {0, 0, 0};
+  if (row) {
+    const double* r = I.nodes + i * kPanelDoubles;
+    for (int d = 0; d < 3; ++d) {
+      xi[d] = r[d];
+      ni[d] = r[3 + d];
+    }
+  }
+  const double g = I.g, ginv = 1.0 / I.g;
+  z2 acc[ND * kNyBasis];
+#pragma unroll
+  for (int t = 0; t < ND * kNyBasis; ++t) acc[t] = {0.0, 0.0};
+  const z2* tre = reinterpret_cast<const z2*>(I.trace);
+  const z2* tri = reinterpret_cast<const z2*>(I.trace_i);
+  z2* A = reinterpret_cast<z2*>(I.A);
+  for (int64_t t0 = c0; t0 < c1; t0 += kNyTile) {
+    const int cnt = (int)min((int64_t)kNyTile, c1 - t0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < kNyTile * 7; e += kNyRows) {
+      const int jj = e / 7, f = e % 7;
+      s_node[jj][f] = jj < cnt ? I.nodes[(t0 + jj) * kPanelDoubles + f] : 0.0;
+    }
+    for (int e = threadIdx.x; e < kNyTile * 4 * kNyBasis; e += kNyRows) {
+      const int jj = e % kNyTile, t = e / kNyTile;
+      const z2* src = t < 2 * kNyBasis ? tre : tri;
+      const int tt = t < 2 * kNyBasis ? t : t - 2 * kNyBasis;
+      s_tr[t][jj] = jj < cnt ? src[(int64_t)tt * n + t0 + jj] : z2{0.0, 0.0};
+    }
+    __syncthreads();
+    if (!row) continue;
+    for (int jj = 0; jj < cnt; ++jj) {
+      const int64_t j = t0 + jj;
+      z2 a11, a12, a21, a22;
+      if (j == i) {
+        a11 = {MULLER ? 1.0 : 0.5, 0.0};
+        a12 = {0.0, 0.0};
+        a21 = {MULLER ? 0.0 : 0.5, 0.0};
+        a22 = {MULLER ? 1.0 : 0.0, 0.0};
+      } else {
+        const double dx = xi[0] - s_node[jj][0], dy = xi[1] - s_node[jj][1],
+                     dz = xi[2] - s_node[jj][2];
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
+        const double ir = 1.0 / r;
+        const double w = s_node[jj][6];
+        const double dny = dx * s_node[jj][3] + dy * s_node[jj][4] + dz * s_node[jj][5];
+        const double dnx = dx * ni[0] + dy * ni[1] + dz * ni[2];
+        const double nn = ni[0] * s_node[jj][3] + ni[1] * s_node[jj][4] + ni[2] * s_node[jj][5];
+        const double fd = -dny * ir * w, fk = dnx * ir * w;
+        const double f2 = dnx * dny * ir * ir, f1 = nn * ir;
+        z2 S[2], D[2], K[2], H[2];
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+          const double kk = side == 0 ? I.k : I.k_int;
+          double sn, cs;
+          sincos(kk * r, &sn, &cs);
+          const double gs = kInv4Pi * ir;
+          const z2 G = {cs * gs, sn * gs};
+          const z2 G1 = zmul(G, z2{-ir, kk});
+          S[side] = {G.x * w, G.y * w};
+          D[side] = {G1.x * fd, G1.y * fd};
+          if (MULLER) {
+            const z2 G2 = zmul(G, z2{2.0 * ir * ir - kk * kk, -2.0 * kk * ir});
+            K[side] = {G1.x * fk, G1.y * fk};
+            H[side] = {-((G2.x - G1.x * ir) * f2 + G1.x * f1) * w,
+                       -((G2.y - G1.y * ir) * f2 + G1.y * f1) * w};
+          }
+        }
+        if (MULLER) {
+          a11 = {D[1].x - D[0].x, D[1].y - D[0].y};
+          a12 = {S[0].x - g * S[1].x, S[0].y - g * S[1].y};
+          a21 = {ginv * H[1].x - H[0].x, ginv * H[1].y - H[0].y};
+          a22 = {K[0].x - K[1].x, K[0].y - K[1].y};
+        } else {
+          a11 = {-D[0].x, -D[0].y};
+          a12 = S[0];
+          a21 = D[1];
+          a22 = {-g * S[1].x, -g * S[1].y};
+        }
+#pragma unroll
+        for (int s = 0; s < kNyBasis; ++s) {
+          const z2 ue = s_tr[s][jj], fe = s_tr[kNyBasis + s][jj];
+          const z2 ui = s_tr[2 * kNyBasis + s][jj], fi = s_tr[3 * kNyBasis + s][jj];
+          z2& sde = acc[s];
+          z2& sdi = acc[(MULLER ? 2 : 1) * kNyBasis + s];
+          zfma(sde, S[0], fe);
+          zfms(sde, D[0], ue);
+          zfma(sdi, S[1], fi);
+          zfms(sdi, D[1], ui);
+          if (MULLER) {
+            z2& khe = acc[kNyBasis + s];
+            z2& khi = acc[3 * kNyBasis + s];
+            zfma(khe, K[0], fe);
+            zfms(khe, H[0], ue);
+            zfma(khi, K[1], fi);
+            zfms(khi, H[1], ui);
+          }
+        }
+      }
+      A[i + j * lda] = a11;
+      A[i + (n + j) * lda] = a12;
+      A[(n + i) + j * lda] = a21;
+      A[(n + i) + (n + j) * lda] = a22;
+    }
+  }
+  if (!row) return;
+  z2* part = reinterpret_cast<z2*>(I.part);
+#pragma unroll
+  for (int t = 0; t < ND * kNyBasis; ++t)
+    part[((int64_t)blockIdx.y * ND * kNyBasis + t) * n + i] = acc[t];
+}
+
+// One thread per element: a fit per wavenumber, then for every row of the element the
+// weights of each defect (on-surface multiplier -1/2) applied to the blocks they enter:
+//   S/D at k:      A11 -= w_p, A12 -= w_f          (dD = w_p, dS = -w_f)
+//   K'/H at k:     A21 -= w_p, A22 -= w_f          (dH = w_p, dK' = -w_f)
+//   S/D at k_int:  Mueller A11 += w_p, A12 += g w_f; CBIE A21 += w_p, A22 += g w_f
+//   K'/H at k_int: A21 += w_p / g, A22 += w_f
+template <bool MULLER>
+__global__ void __launch_bounds__(kNyCorrT) k_ny_correct_fluid(NyInst I) {
+  constexpr int ND = MULLER ? 4 : 2;
+  const int64_t e = (int64_t)blockIdx.x * kNyCorrT + threadIdx.x;
+  const int64_t n = I.n, lda = 2 * I.n;
+  if (e >= n / kNyNodes) return;
+  const z2* tre = reinterpret_cast<const z2*>(I.trace);
+  const z2* tri = reinterpret_cast<const z2*>(I.trace_i);
+  const z2* part = reinterpret_cast<const z2*>(I.part);
+  z2* A = reinterpret_cast<z2*>(I.A);
+  const int64_t b = e * kNyNodes;
+  NyFit Fe, Fi;
+  if (!ny_fit_factor(Fe, tre, n, b) || !ny_fit_factor(Fi, tri, n, b)) {
+    I.status[e] = 1;
+    return;
+  }
+  const double g = I.g;
+  for (int t = 0; t < kNyNodes; ++t) {
+    const int64_t row = b + t;
+    for (int id = 0; id < ND; ++id) {
+      const bool interior = MULLER ? id >= 2 : id == 1;
+      const bool flux = MULLER && (id & 1);
+      const z2* tr = interior ? tri : tre;
+      z2 d[kNyBasis];
+      for (int s = 0; s < kNyBasis; ++s) {
+        z2 acc = {0.0, 0.0};
+        for (int c = 0; c < I.n_chunks; ++c) {
+          const z2 p = part[(((int64_t)c * ND + id) * kNyBasis + s) * n + row];
+          acc.x += p.x;
+          acc.y += p.y;
+        }
+        const z2 own = tr[(int64_t)((flux ? kNyBasis : 0) + s) * n + row];
+        d[s] = {acc.x - 0.5 * own.x, acc.y - 0.5 * own.y};
+      }
+      z2 w[kNyFit];
+      ny_fit_solve(interior ? Fi : Fe, d, w);
+      // target block rows: pressure identity -> top rows, flux identity -> bottom rows
+      // (Mueller); CBIE: k rows top, k_int rows bottom
+      const int64_t r = (MULLER ? flux : interior) ? n + row : row;
+      double cp = -1.0, cf = -1.0;  // coefficients of w_p (left block), w_f (right block)
+      if (interior) {
+        cp = (MULLER && flux) ? 1.0 / g : 1.0;
+        cf = flux ? 1.0 : g;
+      }
+      for (int j = 0; j < kNyNodes; ++j) {
+        const int64_t col = b + j;
+        z2& L = A[r + col * lda];
+        z2& R = A[r + (n + col) * lda];
+        L = {L.x + cp * w[j].x, L.y + cp * w[j].y};
+        R = {R.x + cf * w[kNyNodes + j].x, R.y + cf * w[kNyNodes + j].y};
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------------ point evaluation
-// Scattered field u_s(x) = sum_j w_j [dG/dn_y(x, y_j) p_j - G(x, y_j) q_j] at a point of
-// the exterior (or on the surface, its exterior limit), one CTA per point, in the form
-// the reference uses for point evaluation (fields/pressure.jl:453-467 through
-// quadrature/fluid.jl:104-163 with exclude_nearest=true): the element of the nearest node
-// is left out of the node sum and its contribution recovered from the fit of the
-// interpolants' defect  0 * u(x) + S_excl du/dn - D_excl u  (multiplier 0 outside):
-// u_s += sum_{j in e} (w_p,j p_j + w_f,j q_j).
+// Field at a point, one CTA per point, in the form the reference uses for point
+// evaluation (fields/pressure.jl:453-467 through quadrature/fluid.jl:104-163 with
+// exclude_nearest=true): the element of the nearest node is left out of the node sum and
+// its contribution recovered from the fit of the interpolants' defect
+//   mult u(x) + S_excl du/dn - D_excl u,   mult 0 outside the body, -1 inside.
+// Outside: u_s(x) = sum_j w_j [dG/dn_y p_j - G q_j] (scattered traces, k), the element
+// adding sum_{j in e} (w_p,j p_j + w_f,j q_j).  Inside a fluid body: u_i(x) = sum_j w_j
+// [G g (q_j + q_inc,j) - dG/dn_y (p_j + p_inc,j)] at k_int, the element adding
+// -sum_{j in e} (w_f,j g (q + q_inc)_j + w_p,j (p + p_inc)_j).  Point classes as the
+// panel kernel: surface points are exterior for rigid/soft bodies, interior for fluids.
 constexpr int kNyPtT = 256;
 constexpr int kNyPtSums = 2 * (1 + kNyBasis);  // field + nine defects, complex
 
 __global__ void __launch_bounds__(kNyPtT) k_ny_pressure(NyPoints P) {
   const int64_t ip = blockIdx.x;
   if (ip >= P.npts) return;
-  if (P.region[ip] == 1) {  // inside the body: no exterior field (the host reports it)
-    if (threadIdx.x == 0) {
+  const int32_t reg = P.region[ip];
+  const bool interior = reg == 1 || (reg == 2 && P.fluid);
+  if ((interior && !P.fluid) || (P.field == 3 && !interior) || (P.field == 1 && interior)) {
+    if (threadIdx.x == 0) {  // no such field at this point: NaN marks it for the host
       P.out[2 * ip] = NAN;
       P.out[2 * ip + 1] = NAN;
     }
@@ -345,10 +541,25 @@ __global__ void __launch_bounds__(kNyPtT) k_ny_pressure(NyPoints P) {
     __syncthreads();
   }
   const int64_t b = (s_i[0] / kNyNodes) * kNyNodes;
-  const z2* tr = reinterpret_cast<const z2*>(P.trace);
-  const z2* p = reinterpret_cast<const z2*>(P.p);
-  const z2* q = reinterpret_cast<const z2*>(P.q);
-  const double k = P.k;
+  const z2* tr = reinterpret_cast<const z2*>(interior ? P.trace_i : P.trace);
+  const z2* ps = reinterpret_cast<const z2*>(P.p);
+  const z2* qs = reinterpret_cast<const z2*>(P.q);
+  const double k = interior ? P.k_int : P.k;
+  const double ke = P.k, g = P.g;
+  // interior densities: total traces p + p_inc and g (q + q_inc)
+  auto dens = [&](int64_t j, z2& pj, z2& qj) {
+    pj = ps[j];
+    qj = qs[j];
+    if (interior) {
+      const double* r = P.nodes + j * kPanelDoubles;
+      const double ph = ke * (P.dir[0] * r[0] + P.dir[1] * r[1] + P.dir[2] * r[2]);
+      const double dn = ke * (P.dir[0] * r[3] + P.dir[1] * r[4] + P.dir[2] * r[5]);
+      double sn, cs;
+      sincos(ph, &sn, &cs);
+      pj = {pj.x + cs, pj.y + sn};
+      qj = {g * (qj.x - dn * sn), g * (qj.y + dn * cs)};
+    }
+  };
   z2 acc[1 + kNyBasis];
 #pragma unroll
   for (int t = 0; t <= kNyBasis; ++t) acc[t] = {0.0, 0.0};
@@ -367,8 +578,15 @@ __global__ void __launch_bounds__(kNyPtT) k_ny_pressure(NyPoints P) {
     const double fd = -(dx * r[3] + dy * r[4] + dz * r[5]) * ir * w;
     const z2 S = {G.x * w, G.y * w};
     const z2 D = {G1.x * fd, G1.y * fd};
-    zfma(acc[0], D, p[j]);
-    zfms(acc[0], S, q[j]);
+    z2 pj, qj;
+    dens(j, pj, qj);
+    if (interior) {
+      zfma(acc[0], S, qj);
+      zfms(acc[0], D, pj);
+    } else {
+      zfma(acc[0], D, pj);
+      zfms(acc[0], S, qj);
+    }
 #pragma unroll
     for (int s = 0; s < kNyBasis; ++s) {
       zfma(acc[1 + s], S, tr[(int64_t)(kNyBasis + s) * n + j]);
@@ -393,9 +611,17 @@ __global__ void __launch_bounds__(kNyPtT) k_ny_pressure(NyPoints P) {
   z2 tot[1 + kNyBasis];
   for (int t = 0; t <= kNyBasis; ++t) {
     tot[t] = {0.0, 0.0};
-    for (int g = 0; g < kNyPtT / 32; ++g) {
-      tot[t].x += s_sum[g][2 * t];
-      tot[t].y += s_sum[g][2 * t + 1];
+    for (int gq = 0; gq < kNyPtT / 32; ++gq) {
+      tot[t].x += s_sum[gq][2 * t];
+      tot[t].y += s_sum[gq][2 * t + 1];
+    }
+  }
+  if (interior) {  // multiplier -1: the interpolants' values at x
+    for (int s = 0; s < kNyBasis; ++s) {
+      const double* d = P.dirs + 3 * s;
+      double sn, cs;
+      sincos(k * (d[0] * x[0] + d[1] * x[1] + d[2] * x[2]), &sn, &cs);
+      tot[1 + s] = {tot[1 + s].x - cs, tot[1 + s].y - sn};
     }
   }
   z2 field = tot[0];
@@ -403,14 +629,19 @@ __global__ void __launch_bounds__(kNyPtT) k_ny_pressure(NyPoints P) {
   if (ny_fit_factor(F, tr, n, b)) {
     z2 w[kNyFit];
     ny_fit_solve(F, tot + 1, w);
+    const double sg = interior ? -1.0 : 1.0;
     for (int j = 0; j < kNyNodes; ++j) {
-      zfma(field, w[j], p[b + j]);
-      zfma(field, w[kNyNodes + j], q[b + j]);
+      z2 pj, qj;
+      dens(b + j, pj, qj);
+      const z2 wp = {sg * w[j].x, sg * w[j].y};
+      const z2 wf = {sg * w[kNyNodes + j].x, sg * w[kNyNodes + j].y};
+      zfma(field, wp, pj);
+      zfma(field, wf, qj);
     }
-  } else {  // rank-deficient fit: the element's own node rule
+  } else {  // rank-deficient fit
     P.status[ip] = 1;
   }
-  if (P.field == 0) {  // total: the incident value is already in out
+  if (P.field == 0 && !interior) {  // total outside: the incident value is already in out
     field.x += P.out[2 * ip];
     field.y += P.out[2 * ip + 1];
   }
@@ -420,8 +651,11 @@ __global__ void __launch_bounds__(kNyPtT) k_ny_pressure(NyPoints P) {
 
 }  // namespace
 
-int64_t nystrom_scratch_doubles(int64_t n, int32_t n_chunks) {
-  return 2 * (2 * (int64_t)kNyBasis * n) + 2 * ((int64_t)n_chunks * kNyBasis * n);
+int32_t nystrom_defects(int32_t fluid) { return fluid == 1 ? 4 : fluid == 2 ? 2 : 1; }
+
+int64_t nystrom_scratch_doubles(int64_t n, int32_t n_chunks, int32_t fluid) {
+  const int64_t traces = (fluid ? 2 : 1) * 2 * (2 * (int64_t)kNyBasis * n);
+  return traces + 2 * ((int64_t)n_chunks * nystrom_defects(fluid) * kNyBasis * n);
 }
 
 // About four waves of resident CTAs (152 SMs x 5 CTAs of 96-register threads), so the
@@ -446,14 +680,30 @@ void launch_nystrom(const Launch& L, const NyInst& I0) {
   NyInst I = I0;
   const int64_t per = (I.n + I.n_chunks - 1) / I.n_chunks;
   I.chunk_cols = (per + kNyTile - 1) / kNyTile * kNyTile;
-  k_ny_traces<<<(unsigned)((I.n + 127) / 128), 128, 0, L.stream>>>(I);
+  const unsigned tb = (unsigned)((I.n + 127) / 128);
+  k_ny_traces<<<tb, 128, 0, L.stream>>>(I);
   count_launch(1);
+  if (I.fluid) {  // the interior wavenumber's traces
+    NyInst J = I;
+    J.k = I.k_int;
+    J.trace = I.trace_i;
+    k_ny_traces<<<tb, 128, 0, L.stream>>>(J);
+    count_launch(1);
+  }
   dim3 grid((unsigned)((I.n + kNyRows - 1) / kNyRows), (unsigned)I.n_chunks);
-  k_ny_assemble<<<grid, kNyRows, 0, L.stream>>>(I);
-  count_launch(1);
   const int64_t ne = I.n / kNyNodes;
-  k_ny_correct<<<(unsigned)((ne + kNyCorrT - 1) / kNyCorrT), kNyCorrT, 0, L.stream>>>(I);
-  count_launch(1);
+  const unsigned cb = (unsigned)((ne + kNyCorrT - 1) / kNyCorrT);
+  if (I.fluid == 1) {
+    k_ny_assemble_fluid<true><<<grid, kNyRows, 0, L.stream>>>(I);
+    k_ny_correct_fluid<true><<<cb, kNyCorrT, 0, L.stream>>>(I);
+  } else if (I.fluid == 2) {
+    k_ny_assemble_fluid<false><<<grid, kNyRows, 0, L.stream>>>(I);
+    k_ny_correct_fluid<false><<<cb, kNyCorrT, 0, L.stream>>>(I);
+  } else {
+    k_ny_assemble<<<grid, kNyRows, 0, L.stream>>>(I);
+    k_ny_correct<<<cb, kNyCorrT, 0, L.stream>>>(I);
+  }
+  count_launch(2);
 }
 
 }  // namespace bemgpu

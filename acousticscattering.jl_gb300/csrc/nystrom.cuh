@@ -25,11 +25,22 @@ struct NyInst {
   double* M2;           // S + alpha (1/2 I + K') (complex128, column-major, leading dim n)
   double dirs[3 * kNyBasis];  // unit plane-wave directions of the interpolants
   double* trace;        // interpolant traces [2][kNyBasis][n] complex: u, du/dn at the nodes
-  double* part;         // combined-defect partial sums [n_chunks][kNyBasis][n] complex
+  double* part;         // defect partial sums [n_chunks][defects][kNyBasis][n] complex
   int32_t n_chunks;     // column ranges of the assembly (partial sums per range)
   int64_t chunk_cols;   // columns per range (a multiple of kNyTile)
   int32_t* status;      // per element: 0, or 1 when its correction fit met a zero pivot
+  // fluid bodies (fluid != 0; M1, M2 unused): the 2n x 2n system of the panel path's
+  // Mueller (1) or CBIE (2) blocks, with operators at k and at k_int, each corrected by
+  // plane waves of its own wavenumber
+  int32_t fluid;
+  double k_int, g;      // interior wavenumber, density contrast
+  double* A;            // system (complex128, column-major, leading dim 2n)
+  double* trace_i;      // interpolant traces at k_int, layout of trace
 };
+
+// Defect sums per row and column range: 1 (rigid/soft, combined), 4 (Mueller: S/D and
+// K'/H identities at k and k_int), 2 (fluid CBIE: S/D identities at k and k_int).
+int32_t nystrom_defects(int32_t fluid);
 
 // Points of a Nyström solution's field evaluation (k_ny_pressure).
 struct NyPoints {
@@ -43,12 +54,20 @@ struct NyPoints {
   int64_t npts;
   const int32_t* region; // per point from the panel pass: 0 exterior, 1 interior, 2 surface
   double* out;           // complex128 npts: the incident value on entry, the field on exit
-  int32_t field;         // 0 total, 1 scattered
+  int32_t field;         // 0 total, 1 scattered, 3 interior (bemgpu_field)
   int32_t* status;       // per point: 1 when the nearest element's fit was rank-deficient
+  // fluid bodies: interior points (and surface points) take the interior field
+  // S_int[g (q + q_inc)] - D_int[p + p_inc] at k_int
+  int32_t fluid;
+  double k_int, g;
+  const double* trace_i; // interpolant traces at k_int
+  double dir[3];         // incidence direction
+  double dirs[3 * kNyBasis];  // plane-wave directions of the interpolants
 };
 
-// Scratch of launch_nystrom in doubles: traces and defect partials.
-int64_t nystrom_scratch_doubles(int64_t n, int32_t n_chunks);
+// Scratch of launch_nystrom in doubles: traces (both wavenumbers for fluid bodies) and
+// defect partials.
+int64_t nystrom_scratch_doubles(int64_t n, int32_t n_chunks, int32_t fluid);
 // Column ranges for n nodes (enough CTAs to fill the SMs a few times over).
 int32_t nystrom_chunks(int64_t n);
 

@@ -170,9 +170,9 @@ The reference's `bem(surface::Mesh, boundary, k; ...)` on the GPU.  With
 `compression=(method=:hmatrix, tol=1e-5)` a Rigid or PressureRelease body is solved as the
 reference's `solve_full_bem` does by default: compressed operators and GMRES with
 `gmres_kwargs` (reltol, abstol, restart, maxiter); non-convergence warns as there.
-`discretization=:nystrom` (Rigid/PressureRelease, dense factor) solves on the quadrature
-nodes with the density-interpolation correction, as the reference's default
-`correction=(method=:dim,)` does.
+`discretization=:nystrom` (dense factor) solves on the quadrature nodes with the
+density-interpolation correction, as the reference's default `correction=(method=:dim,)`
+does.
 """
 function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
         incidence_azimuth::Real = 0.0, formulation::Union{Nothing, Symbol} = nothing,

@@ -105,9 +105,9 @@ typedef enum {
  * centroids with analytic singular rules (this library's default).  NYSTROM: unknowns at
  * the seven quadrature nodes of every panel, kernel values times node weights, with a
  * density-interpolation correction of every node's own element, the discretisation of the
- * reference's solve_full_bem (full.jl:68-128 with correction=(method=:dim,)); dense
- * factor only, rigid and pressure-release bodies; pressure() at exterior points leaves the
- * nearest element out of the node sum and recovers it by the same correction.
+ * reference's solve_full_bem (full.jl:68-128 and 289-346 with correction=(method=:dim,));
+ * one surface (rigid, pressure-release or fluid-filled), dense factor; pressure() leaves
+ * the nearest element out of the node sum and recovers it by the same correction.
  */
 typedef enum { BEMGPU_COLLOCATION = 0, BEMGPU_NYSTROM = 1 } bemgpu_discretization;
 

@@ -142,23 +142,33 @@ def _inside(P: O.Panels, x):
     return 2.0 * np.arctan2(num, den).sum() > 2.0 * np.pi
 
 
-def pressure(P: O.Panels, k, points, p, q, direction, field="scattered"):
-    """Field of a Nyström solution at exterior points, in the reference's point-evaluation
-    form (fields/pressure.jl:453-467 through quadrature/fluid.jl:104-163 with
-    exclude_nearest=true): the element of the nearest node is left out of the node sum
-    u_s = sum_j w_j (dG/dn_y p_j - G q_j) and its contribution recovered from the fit of
-    the interpolants' defect 0 * u(x) + S_excl du/dn - D_excl u (multiplier 0 outside)."""
+def pressure(P: O.Panels, k, points, p, q, direction, field="scattered", g=None, h=None):
+    """Field of a Nyström solution at points, in the reference's point-evaluation form
+    (fields/pressure.jl:453-467 through quadrature/fluid.jl:104-163 with
+    exclude_nearest=true): the element of the nearest node is left out of the node sum and
+    its contribution recovered from the fit of the interpolants' defect
+    mult u(x) + S_excl du/dn - D_excl u (mult 0 outside, -1 inside).  Outside:
+    u_s = sum_j w_j (dG/dn_y p_j - G q_j); inside a fluid body (g, h given): the interior
+    field sum_j w_j (G g (q + q_inc)_j - dG/dn_y (p + p_inc)_j) at k / h."""
     y, ny, w = nodes_of(P)
-    u_all, f_all = traces(y, ny, k)
+    fluid = g is not None
     d_inc = np.asarray(direction, dtype=np.float64)
+    pin = np.exp(1j * k * (y @ d_inc))
+    qin = 1j * k * (ny @ d_inc) * pin
     out = []
     for x in np.asarray(points, dtype=np.float64).reshape(-1, 3):
         inc = np.exp(1j * k * (x @ d_inc))
         if field == "incident":
             out.append(inc)
             continue
-        if _inside(P, x):
+        inside = _inside(P, x)
+        if inside and not fluid:
             raise ValueError("point lies inside the body")
+        if (field == "interior") != inside and field != "total":
+            raise ValueError("the field does not exist at this point")
+        kk = k / h if inside else k
+        u_all, f_all = traces(y, ny, kk)
+        dp, dq = (p + pin, g * (q + qin)) if inside else (p, q)
         dv = x[None, :] - y
         r2 = (dv * dv).sum(1)
         b = (int(np.argmin(r2)) // NODES) * NODES
@@ -166,17 +176,32 @@ def pressure(P: O.Panels, k, points, p, q, direction, field="scattered"):
         keep[b:b + NODES] = False
         r = np.sqrt(r2[keep])
         ir = 1.0 / r
-        G = np.exp(1j * k * r) * ir / (4 * np.pi)
-        G1 = G * (1j * k - ir)
+        G = np.exp(1j * kk * r) * ir / (4 * np.pi)
+        G1 = G * (1j * kk - ir)
         S = G * w[keep]
         D = -G1 * (dv[keep] * ny[keep]).sum(1) * ir * w[keep]
-        fld = np.sum(D * p[keep] - S * q[keep])
+        sg = -1.0 if inside else 1.0
+        fld = sg * np.sum(D * dp[keep] - S * dq[keep])
         defect = S @ f_all[keep] - D @ u_all[keep]
+        if inside:
+            defect = defect - np.exp(1j * kk * (directions() @ x))
         pinv, sc = _element_pinv(u_all[b:b + NODES], f_all[b:b + NODES])
         wt = (pinv @ defect) / sc
-        fld += wt[:NODES] @ p[b:b + NODES] + wt[NODES:] @ q[b:b + NODES]
-        out.append(fld + inc if field == "total" else fld)
+        fld += sg * (wt[:NODES] @ dp[b:b + NODES] + wt[NODES:] @ dq[b:b + NODES])
+        out.append(fld + inc if (field == "total" and not inside) else fld)
     return np.array(out)
+
+
+def assemble_fluid(P: O.Panels, k, g, h, formulation="muller"):
+    """The fluid system on the nodes (full.jl:289-346 block algebra, as the panel oracle):
+    Mueller [I - De + Di, Se - g Si; -He + Hi/g, I + K'e - K'i], CBIE [1/2 I - De, Se;
+    1/2 I + Di, -g Si], each wavenumber's operators corrected by its own plane waves."""
+    (Se, De, Ke, He), _ = corrected_operators(P, k)
+    (Si, Di, Ki, Hi), _ = corrected_operators(P, k / h)
+    I = np.eye(Se.shape[0])
+    if formulation == "muller":
+        return np.block([[I - De + Di, Se - g * Si], [-He + Hi / g, I + Ke - Ki]])
+    return np.block([[0.5 * I - De, Se], [0.5 * I + Di, -g * Si]])
 
 
 def far_field(y, ny, w, k, xhat, p, q):
@@ -187,14 +212,30 @@ def far_field(y, ny, w, k, xhat, p, q):
 
 
 def solve(nodes, triangles, boundary, k, incidence_angle=math.pi / 2, incidence_azimuth=0.0,
-          formulation="burton_miller"):
-    """Scattered traces at the nodes of a rigid or pressure-release body (full.jl:130-184,
-    the direct solve in place of GMRES).  Returns (p, q, (y, ny, w))."""
+          formulation=None, g=1.0, h=1.0):
+    """Scattered traces at the nodes (full.jl:130-184 for rigid / pressure-release bodies,
+    full.jl:422-495 for fluid ones, the direct solve in place of GMRES).
+    Returns (p, q, (y, ny, w))."""
     P = O.Panels(nodes, triangles)
+    d = O.incidence_direction(incidence_angle, incidence_azimuth)
+    if boundary == "fluid":
+        formulation = formulation or "muller"
+        y, ny, w = nodes_of(P)
+        n = len(w)
+        pin = np.exp(1j * k * (y @ d))
+        qin = 1j * k * (ny @ d) * pin
+        A = assemble_fluid(P, k, g, h, formulation)
+        if formulation == "muller":
+            x = np.linalg.solve(A, np.concatenate([pin, qin]))
+            return x[:n] - pin, x[n:] - qin, (y, ny, w)
+        b = np.zeros(2 * n, dtype=np.complex128)
+        b[n:] = -(A[n:, :] @ np.concatenate([pin, qin]))
+        x = np.linalg.solve(A, b)
+        return x[:n], x[n:], (y, ny, w)
+    formulation = formulation or "burton_miller"
     (S, D, K, H), (y, ny, w) = corrected_operators(P, k)
     a = 1j / k if formulation == "burton_miller" else 0.0
     I = np.eye(len(w))
-    d = O.incidence_direction(incidence_angle, incidence_azimuth)
     pin = np.exp(1j * k * (y @ d))
     qin = 1j * k * (ny @ d) * pin
     if boundary == "rigid":

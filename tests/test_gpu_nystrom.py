@@ -153,11 +153,75 @@ def test_point_field_matches_oracle(ctx, boundary):
     sol.close()
 
 
+G_FL, H_FL = 1.0357, 1.0279
+
+
+@pytest.mark.parametrize("formulation", ["muller", "cbie"])
+def test_fluid_operators_match_oracle(ctx, formulation):
+    nodes, tris = meshes.icosphere(0.01, 1)
+    surf = bemgpu.mesh(nodes, tris)
+    A = bemgpu.assemble(surf, bemgpu.FluidFilled(G_FL, H_FL), K38, formulation=formulation,
+                        ctx=ctx, discretization="nystrom")
+    R = NY.assemble_fluid(O.Panels(nodes, tris), K38, G_FL, H_FL, formulation)
+    assert A.shape == (2 * 7 * 80, 2 * 7 * 80)
+    assert np.max(np.abs(A - R)) / np.max(np.abs(R)) < 1e-11
+
+
+@pytest.mark.parametrize("formulation", ["muller", "cbie"])
+def test_fluid_solve_and_field_match_oracle(ctx, formulation):
+    a = 0.01
+    nodes, tris = meshes.icosphere(a, 2)
+    surf = bemgpu.mesh(nodes, tris)
+    beta, alpha = 0.7, 0.4
+    bc = bemgpu.FluidFilled(G_FL, H_FL)
+    sol = bemgpu.bem(surf, bc, K38, incidence_angle=beta, incidence_azimuth=alpha,
+                     formulation=formulation, ctx=ctx, discretization="nystrom")
+    p, q = sol.traces()
+    rp, rq, (y, ny, w) = NY.solve(nodes, tris, "fluid", K38, beta, alpha, formulation,
+                                  G_FL, H_FL)
+    for u, v in ((p, rp), (q, rq)):
+        assert np.linalg.norm(u - v) <= 1e-9 * np.linalg.norm(v)
+    d = O.incidence_direction(beta, alpha)
+    ref = NY.far_field(y, ny, w, K38, -d, rp, rq)
+    assert abs(bemgpu.scattering_amplitude(sol) - ref) <= 1e-9 * abs(ref)
+    P = O.Panels(nodes, tris)
+    dirs = np.array([[1.0, 0, 0], [0.0, 0.6, 0.8], [-0.6, 0.0, 0.8]])
+    cen = P.centroids[[3, 101, 250]]  # on the facets: just inside / outside the polyhedron
+    outside = np.concatenate([1.003 * cen] + [rf * a * dirs for rf in (1.005, 1.3)])
+    inside = np.concatenate([0.997 * cen] + [rf * a * dirs for rf in (0.9, 0.5)] +
+                            [np.zeros((1, 3))])
+    got = bemgpu.pressure(sol, outside, field="scattered")
+    want = NY.pressure(P, K38, outside, p, q, d, "scattered", g=G_FL, h=H_FL)
+    assert np.max(np.abs(got - want) / np.abs(want)) < 1e-9
+    got = bemgpu.pressure(sol, inside, field="interior")
+    want = NY.pressure(P, K38, inside, p, q, d, "interior", g=G_FL, h=H_FL)
+    assert np.max(np.abs(got - want) / np.abs(want)) < 1e-9
+    assert np.allclose(bemgpu.pressure(sol, inside), got, rtol=1e-12)
+    with pytest.raises(bemgpu.ArgumentError):
+        bemgpu.pressure(sol, outside, field="interior")
+    sol.close()
+
+
+def test_fluid_mixed_refinement_contract(ctx):
+    nodes, tris = meshes.icosphere(0.01, 2)
+    surf = bemgpu.mesh(nodes, tris)
+    bc = bemgpu.FluidFilled(G_FL, H_FL)
+    sd = bemgpu.bem(surf, bc, K38, ctx=ctx, discretization="nystrom")
+    sm = bemgpu.bem(surf, bc, K38, ctx=ctx, discretization="nystrom", precision="mixed")
+    fd, fm = bemgpu.scattering_amplitude(sd), bemgpu.scattering_amplitude(sm)
+    assert abs(20 * math.log10(abs(fm) / abs(fd))) < 0.01
+    dm = sm.diagnostics()
+    assert dm["normwise_backward_error"] <= 1e-13
+    sd.close()
+    sm.close()
+
+
 def test_unsupported_combinations_are_rejected(ctx):
     nodes, tris = meshes.icosphere(0.01, 1)
     surf = bemgpu.mesh(nodes, tris)
     with pytest.raises(bemgpu.ArgumentError):
-        bemgpu.bem(surf, bemgpu.FluidFilled(1.03, 1.02), K38, ctx=ctx, discretization="nystrom")
+        bemgpu.bem([surf], [bemgpu.FluidFilled(1.03, 1.02)], K38, ctx=ctx,
+                   discretization="nystrom")
     with pytest.raises(bemgpu.ArgumentError):
         bemgpu.bem(surf, bemgpu.Rigid(), K38, ctx=ctx, discretization="nystrom",
                    compression=dict(method="hmatrix"))

@@ -77,6 +77,37 @@ def test_modal_near_field_tends_to_the_form_function():
         assert abs(near - far) < 1e-4 * abs(far)
 
 
+G_FL, H_FL = 1.0357, 1.0279  # the fluid spheroid workload's contrasts
+
+
+@pytest.mark.parametrize("formulation", ["muller", "cbie"])
+def test_fluid_sphere_against_modal(formulation):
+    a = 0.01
+    nodes, tris = meshes.icosphere(a, 2)
+    p, q, (y, ny, w) = NY.solve(nodes, tris, "fluid", K38, math.pi / 2, math.pi / 2,
+                                formulation, G_FL, H_FL)
+    d = O.incidence_direction(math.pi / 2, math.pi / 2)
+    f = NY.far_field(y, ny, w, K38, -d, p, q)
+    fm = modal.form_function("fluid", K38, a, g=G_FL, h=H_FL)
+    assert abs(20 * math.log10(abs(f) / abs(fm))) < 0.1
+    assert abs(f - fm) < 0.015 * abs(fm)
+
+
+def test_fluid_pressure_is_continuous_across_the_surface():
+    a = 0.01
+    nodes, tris = meshes.icosphere(a, 2)
+    P = O.Panels(nodes, tris)
+    p, q, _ = NY.solve(nodes, tris, "fluid", K38, math.pi / 2, math.pi / 2, "muller",
+                       G_FL, H_FL)
+    d = O.incidence_direction(math.pi / 2, math.pi / 2)
+    cen = P.centroids[[3, 101, 250]]  # facet centres: 0.3 % off the facet on either side
+    assert not any(NY._inside(P, x) for x in 1.003 * cen)
+    assert all(NY._inside(P, x) for x in 0.997 * cen)
+    po = NY.pressure(P, K38, 1.003 * cen, p, q, d, "total", g=G_FL, h=H_FL)
+    pi = NY.pressure(P, K38, 0.997 * cen, p, q, d, "total", g=G_FL, h=H_FL)
+    assert np.all(np.abs(po - pi) < 0.03 * np.abs(po))
+
+
 def test_refinement_reduces_error():
     e1 = _ts_error("rigid", 1)[1]
     e2 = _ts_error("rigid", 2)[1]
@@ -107,7 +138,5 @@ def test_host_rejects_unsupported_nystrom_options():
     from bemgpu.api import _problem
     with pytest.raises(bemgpu.ArgumentError):
         _problem(bemgpu.Rigid(), 1.0, discretization="galerkin")
-    with pytest.raises(bemgpu.ArgumentError):
-        _problem(bemgpu.FluidFilled(1.1, 1.1), 1.0, discretization="nystrom")
     p = _problem(bemgpu.PressureRelease(), 2.0, discretization="nystrom")
     assert p.discretization == 1
