@@ -564,12 +564,14 @@ def _hmatrix_options(compression, gmres_kwargs):
     return o
 
 
-def _bem_hmatrix(surface, boundary, k, angles, azimuths, opts, *, formulation, precision, ctx):
+def _bem_hmatrix(surface, boundary, k, angles, azimuths, opts, *, formulation, precision, ctx,
+                 discretization="collocation"):
     if isinstance(boundary, FluidFilled):
         raise ArgumentError(
             "hierarchical compression applies to Rigid and PressureRelease boundaries")
     ctx = ctx or context()
-    p = _problem(boundary, k, formulation=formulation, precision=precision)
+    p = _problem(boundary, k, formulation=formulation, precision=precision,
+                 discretization=discretization)
     angles = np.atleast_1d(np.asarray(angles, dtype=np.float64))
     az = np.broadcast_to(np.asarray(azimuths, dtype=np.float64), angles.shape)
     inc = np.ascontiguousarray(np.stack([angles, az], axis=1).reshape(-1))
@@ -577,7 +579,7 @@ def _bem_hmatrix(surface, boundary, k, angles, azimuths, opts, *, formulation, p
     _check(C.lib().bemgpu_hmatrix_solve(ctx.handle, surface.handle(ctx), ctypes.byref(p),
                                         ctypes.byref(opts), len(angles), C.dptr(inc),
                                         ctypes.byref(h)), ctx.handle)
-    sol = BEMSolution(ctx, h, surface, boundary, k, angles, az)
+    sol = BEMSolution(ctx, h, surface, boundary, k, angles, az, discretization=discretization)
     sol.method = "hmatrix"
     st = sol.hmatrix_stats()
     if not st["gmres_converged"]:
@@ -634,9 +636,8 @@ def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_az
     if discretization not in C.DISCRETIZATION:
         raise ArgumentError("discretization must be :collocation or :nystrom")
     hm = _hmatrix_options(compression, gmres_kwargs)
-    if discretization != "collocation" and (hm is not None or
-                                            isinstance(surface, (list, tuple))):
-        raise ArgumentError("the Nyström discretisation takes one surface and a dense factor")
+    if discretization != "collocation" and isinstance(surface, (list, tuple)):
+        raise ArgumentError("the Nyström discretisation takes one surface")
     if hm is not None:
         if isinstance(surface, (list, tuple)) or parents is not None:
             raise ArgumentError("hierarchical compression applies to a single surface")
@@ -645,7 +646,8 @@ def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_az
         if not (math.isfinite(incidence_angle) and math.isfinite(incidence_azimuth)):
             raise ArgumentError("incidence angles must be finite")
         return _bem_hmatrix(surface, boundary, k, [incidence_angle], [incidence_azimuth], hm,
-                            formulation=formulation, precision=precision, ctx=ctx)
+                            formulation=formulation, precision=precision, ctx=ctx,
+                            discretization=discretization)
     if isinstance(surface, (list, tuple)):
         return _bem_regions(list(surface), boundary, k, parents=parents,
                             incidence_angle=incidence_angle,
@@ -883,11 +885,10 @@ def incidence_angle_sweep(surface: Mesh, boundary, k, angles, *, incidence_azimu
     if not math.isfinite(incidence_azimuth):
         raise ArgumentError("incidence_azimuth must be finite")
     hm = _hmatrix_options(compression, gmres_kwargs)
-    if hm is not None and discretization != "collocation":
-        raise ArgumentError("the Nyström discretisation takes a dense factor")
     if hm is not None:
         sol = _bem_hmatrix(surface, boundary, k, angles, incidence_azimuth, hm,
-                           formulation=formulation, precision=precision, ctx=ctx)
+                           formulation=formulation, precision=precision, ctx=ctx,
+                           discretization=discretization)
         try:
             amps = np.array([scattering_amplitude(sol, rhs=r) for r in range(len(angles))])
             diag = sol.diagnostics()

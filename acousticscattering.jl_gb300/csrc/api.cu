@@ -287,6 +287,7 @@ struct MeshData {
   struct HmPlanCache {
     HmPlan plan;
     Buf perm, iperm, near_dst;
+    Buf ny_dst;  // Nyström node sets: full-block offsets of every same-element pair
   };
   std::map<std::pair<int32_t, double>, std::shared_ptr<HmPlanCache>> hm_plans;
   // Nyström node set: one record per quadrature node (the panel-record layout with the
@@ -437,7 +438,22 @@ int nystrom_mesh(bemgpu_ctx* c, MeshData* m, std::shared_ptr<MeshData>* out) {
         for (int a = 0; a < 3; ++a) o[8 + 3 * g + a] = o[a];
     }
   }
+  // FP32 records relative to the centre (compressed operators with precision mixed)
+  std::vector<float> recf((size_t)d->n * kPanelFloats, 0.0f);
+  for (int64_t i = 0; i < d->n; ++i) {
+    const double* r = d->panels_h.data() + i * kPanelDoubles;
+    float* f = recf.data() + i * kPanelFloats;
+    for (int a = 0; a < 3; ++a) {
+      f[a] = (float)(r[a] - d->center[a]);
+      f[3 + a] = (float)r[3 + a];
+    }
+    f[6] = (float)r[6];
+    f[7] = (float)r[7];
+    for (int q = 0; q < 7; ++q)
+      for (int a = 0; a < 3; ++a) f[8 + 3 * q + a] = f[a];
+  }
   TRY(upload(c, d->panels_h, &d->panels));
+  TRY(upload(c, recf, &d->panelsf));
   m->node_mesh = d;
   *out = d;
   return BEMGPU_OK;
@@ -2823,7 +2839,17 @@ int hm_build(bemgpu_ctx* c, MeshData* m, const bemgpu_problem& p, int kind,
   if (!pc) {  // cluster tree, partition and near-pair destinations of this mesh
     auto fresh = std::make_shared<MeshData::HmPlanCache>();
     std::vector<double> cent, diam;
-    panel_centroids(m->nodes_h.data(), m->tris_h.data(), n, &cent, &diam);
+    if (m->nystrom) {  // node positions, their element's longest edge
+      cent.resize(3 * (size_t)n);
+      diam.resize((size_t)n);
+      for (int64_t i = 0; i < n; ++i) {
+        const double* r = m->panels_h.data() + i * kPanelDoubles;
+        for (int a = 0; a < 3; ++a) cent[3 * (size_t)i + a] = r[a];
+        diam[(size_t)i] = r[7];
+      }
+    } else {
+      panel_centroids(m->nodes_h.data(), m->tris_h.data(), n, &cent, &diam);
+    }
     std::string err;
     if (hm_build_plan(cent.data(), diam.data(), n, o.leaf_size, o.eta, m->eta, &fresh->plan,
                       &err)) {
@@ -2831,6 +2857,33 @@ int hm_build(bemgpu_ctx* c, MeshData* m, const bemgpu_problem& p, int kind,
       return fail(c, BEMGPU_EINVAL, err);
     }
     const HmPlan& P = fresh->plan;
+    // destination of a pair (original indices) inside its full leaf block: the leaf pairs
+    // of the full blocks, looked up per row leaf (blocks of a row leaf sorted by column
+    // leaf); -1 when the pair lies in no full block
+    const int64_t nl = (int64_t)P.leaf_lo.size() - 1;
+    std::vector<int32_t> leaf((size_t)n);
+    for (int64_t l = 0; l < nl; ++l)
+      for (int32_t t = P.leaf_lo[(size_t)l]; t < P.leaf_lo[(size_t)l + 1]; ++t) leaf[(size_t)t] = (int32_t)l;
+    std::vector<std::vector<std::pair<int32_t, int64_t>>> row_blocks((size_t)nl);
+    {
+      int64_t off = 0;
+      for (const HmBlock& B : P.dense) {  // full-block offsets as hm_build lays them out
+        row_blocks[(size_t)leaf[(size_t)B.rlo]].push_back({leaf[(size_t)B.clo], off});
+        off += (int64_t)B.m * B.n;
+      }
+    }
+    for (auto& v : row_blocks) std::sort(v.begin(), v.end());
+    auto pair_dst = [&](int64_t i, int64_t j) -> int64_t {
+      const int32_t pi = P.iperm[(size_t)i], pj = P.iperm[(size_t)j];
+      const auto& v = row_blocks[(size_t)leaf[(size_t)pi]];
+      auto it = std::lower_bound(v.begin(), v.end(),
+                                 std::pair<int32_t, int64_t>{leaf[(size_t)pj], INT64_MIN});
+      if (it == v.end() || it->first != leaf[(size_t)pj]) return -1;
+      const int32_t rlo = P.leaf_lo[(size_t)leaf[(size_t)pi]];
+      const int32_t clo = P.leaf_lo[(size_t)leaf[(size_t)pj]];
+      const int32_t mrows = P.leaf_lo[(size_t)leaf[(size_t)pi] + 1] - rlo;
+      return it->second + (pi - rlo) + (int64_t)(pj - clo) * mrows;
+    };
     std::vector<int64_t> dst((size_t)std::max<int64_t>(1, m->n_near), 0);
     if (m->n_near > 0) {
       std::vector<int64_t> rowptr, cols;
@@ -2839,34 +2892,26 @@ int hm_build(bemgpu_ctx* c, MeshData* m, const bemgpu_problem& p, int kind,
         m->hm_plans.erase({o.leaf_size, o.eta});
         return fail(c, BEMGPU_EINVAL, "internal: near-pair list differs from the mesh's");
       }
-      // destination of every near pair inside its full leaf block: the leaf pairs of the
-      // full blocks, looked up per row leaf (blocks of a row leaf sorted by column leaf)
-      const int64_t nl = (int64_t)P.leaf_lo.size() - 1;
-      std::vector<int32_t> leaf((size_t)n);
-      for (int64_t l = 0; l < nl; ++l)
-        for (int32_t t = P.leaf_lo[(size_t)l]; t < P.leaf_lo[(size_t)l + 1]; ++t) leaf[(size_t)t] = (int32_t)l;
-      std::vector<std::vector<std::pair<int32_t, int64_t>>> row_blocks((size_t)nl);
-      int64_t off = 0;
-      for (const HmBlock& B : P.dense) {  // full-block offsets as hm_build lays them out
-        row_blocks[(size_t)leaf[(size_t)B.rlo]].push_back({leaf[(size_t)B.clo], off});
-        off += (int64_t)B.m * B.n;
-      }
-      for (auto& v : row_blocks) std::sort(v.begin(), v.end());
       for (int64_t i = 0; i < n; ++i)
         for (int64_t q = rowptr[i]; q < rowptr[i + 1]; ++q) {
-          const int32_t pi = P.iperm[(size_t)i], pj = P.iperm[(size_t)cols[q]];
-          const auto& v = row_blocks[(size_t)leaf[(size_t)pi]];
-          auto it = std::lower_bound(v.begin(), v.end(),
-                                     std::pair<int32_t, int64_t>{leaf[(size_t)pj], INT64_MIN});
-          if (it == v.end() || it->first != leaf[(size_t)pj]) {
+          dst[(size_t)q] = pair_dst(i, cols[q]);
+          if (dst[(size_t)q] < 0) {
             m->hm_plans.erase({o.leaf_size, o.eta});
             return fail(c, BEMGPU_EINVAL, "internal: near pair outside the full blocks");
           }
-          const int32_t rlo = P.leaf_lo[(size_t)leaf[(size_t)pi]];
-          const int32_t clo = P.leaf_lo[(size_t)leaf[(size_t)pj]];
-          const int32_t mrows = P.leaf_lo[(size_t)leaf[(size_t)pi] + 1] - rlo;
-          dst[(size_t)q] = it->second + (pi - rlo) + (int64_t)(pj - clo) * mrows;
         }
+    }
+    if (m->nystrom) {  // every same-element pair (node i, node 7 (i / 7) + j)
+      std::vector<int64_t> nd((size_t)n * kNyNodes);
+      for (int64_t i = 0; i < n; ++i)
+        for (int j = 0; j < kNyNodes; ++j) {
+          nd[(size_t)i * kNyNodes + j] = pair_dst(i, (i / kNyNodes) * kNyNodes + j);
+          if (nd[(size_t)i * kNyNodes + j] < 0) {
+            m->hm_plans.erase({o.leaf_size, o.eta});
+            return fail(c, BEMGPU_EINVAL, "internal: element pair outside the full blocks");
+          }
+        }
+      TRY(upload(c, nd, &fresh->ny_dst));
     }
     TRY(upload(c, P.perm, &fresh->perm));
     TRY(upload(c, P.iperm, &fresh->iperm));
@@ -3051,6 +3096,58 @@ int hm_build(bemgpu_ctx* c, MeshData* m, const bemgpu_problem& p, int kind,
   TRY(upload(c, ptr, &H->leaf_ptr));
   TRY(upload(c, ent, &H->leaf_ent));
   CUDA_TRY(c, cudaGetLastError());
+  if (m->nystrom) {
+    // Nyström node operators: diagonal, combined defect of the interpolants through the
+    // compressed products, element corrections inside the full blocks
+    const int32_t nb = kNyBasis;
+    Buf trace, up, fp, y, y2, scr, status;
+    TRY(alloc(c, (size_t)n * 2 * nb * 16, &trace));
+    TRY(alloc(c, (size_t)n * nb * 16, &up));
+    TRY(alloc(c, (size_t)n * nb * 16, &fp));
+    TRY(alloc(c, (size_t)n * nb * 16, &y));
+    TRY(alloc(c, (size_t)n * nb * 16, &y2));
+    TRY(alloc(c, H->scratch_bytes(nb), &scr));
+    TRY(alloc(c, (size_t)std::max<int64_t>(1, n / kNyNodes) * 4, &status));
+    CUDA_TRY(c, cudaMemsetAsync(status.p, 0, status.bytes, c->stream));
+    NyInst T{};
+    T.nodes = m->panels.as<double>();
+    T.n = n;
+    T.k = k;
+    nystrom_directions(T.dirs);
+    T.trace = trace.as<double>();
+    NyPoints none{};
+    NyHm Y{};
+    Y.trace = trace.as<double>();
+    Y.Y = y2.as<double>();
+    Y.iperm = pc->iperm.as<int32_t>();
+    Y.dst = pc->ny_dst.as<int64_t>();
+    Y.D1 = H->D1.p;
+    Y.D2 = H->D2.p;
+    Y.n = n;
+    Y.a_re = a_re;
+    Y.a_im = a_im;
+    Y.f32 = H->f32 ? 1 : 0;
+    Y.status = status.as<int32_t>();
+    {
+      Prof pr(c, "hm_dense");
+      launch_nystrom_pressure(L, T, none);  // the interpolant traces only
+      launch_nystrom_hm_diag(L, Y);
+      launch_hm_permute(L, trace.as<double>(), n, up.as<double>(), n, pc->perm.as<int32_t>(), n,
+                        nb);
+      launch_hm_permute(L, trace.as<double>() + 2 * (size_t)n * nb, n, fp.as<double>(), n,
+                        pc->perm.as<int32_t>(), n, nb);
+      launch_hm_matvec(L, H->op(0, scr.p, nb), up.as<double>(), n, y.as<double>(), n, nullptr,
+                       0, 0.0, 1.0, nb, nullptr, 0);
+      launch_hm_matvec(L, H->op(1, scr.p, nb), fp.as<double>(), n, y2.as<double>(), n,
+                       y.as<double>(), n, 1.0, 1.0, nb, nullptr, 0);
+      launch_nystrom_hm_correct(L, Y);
+    }
+    CUDA_TRY(c, cudaGetLastError());
+    std::vector<int32_t> st;
+    TRY(download(c, status, &st, (size_t)std::max<int64_t>(1, n / kNyNodes)));
+    for (int32_t v : st)
+      if (v) return fail(c, BEMGPU_EINVAL, "density-interpolation fit is rank-deficient");
+  }
   bemgpu_hmatrix_stats& S = H->st;
   std::memset(&S, 0, sizeof S);
   S.lowrank_blocks = H->n_lr;
@@ -3233,9 +3330,6 @@ int hm_problem(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_problem* pro
   if (*kind != kAsmBM && *kind != kAsmCBIE)
     return fail(c, BEMGPU_EINVAL,
                 "hierarchical compression applies to Rigid and PressureRelease boundaries");
-  if (problem->discretization != BEMGPU_COLLOCATION)
-    return fail(c, BEMGPU_EINVAL,
-                "hierarchical compression applies to the collocation discretisation");
   if (std::fabs(problem->near_eta - mesh->d->eta) > 0)
     return fail(c, BEMGPU_EINVAL, "near_eta differs from the mesh's (upload with that eta)");
   return check_hm_options(c, *opt);
@@ -3303,7 +3397,10 @@ int bemgpu_hmatrix_solve(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_pr
   int kind = 0;
   TRY(hm_problem(c, mesh, problem, opt, &kind));
   const bemgpu_problem& p = *problem;
-  MeshData* m = mesh->d.get();
+  // the Nyström discretisation compresses the node operators of the node set
+  std::shared_ptr<MeshData> md = mesh->d;
+  if (p.discretization == BEMGPU_NYSTROM) TRY(nystrom_mesh(c, mesh->d.get(), &md));
+  MeshData* m = md.get();
   const int64_t n = m->n;
   std::vector<double> dirs(3 * (size_t)nrhs);
   for (int32_t r = 0; r < nrhs; ++r) {
@@ -3321,7 +3418,8 @@ int bemgpu_hmatrix_solve(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_pr
   Timer tsol(c->stream);
   auto sd = std::make_shared<SolutionData>();
   sd->c = c;
-  sd->mesh = mesh->d;
+  sd->mesh = md;
+  if (m->nystrom) sd->base_mesh = mesh->d;
   sd->boundary = p.boundary;
   sd->k = p.k;
   sd->nrhs = nrhs;
@@ -3450,6 +3548,8 @@ int bemgpu_hmatrix_apply(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_pr
   cudaSetDevice(c->device);
   int kind = 0;
   TRY(hm_problem(c, mesh, problem, opt, &kind));
+  if (problem->discretization != BEMGPU_COLLOCATION)
+    return fail(c, BEMGPU_EINVAL, "hmatrix_apply takes the collocation discretisation");
   MeshData* m = mesh->d.get();
   const int64_t n = m->n;
   HmData H;

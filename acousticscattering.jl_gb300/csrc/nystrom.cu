@@ -31,6 +31,7 @@
 #include <cmath>
 
 #include "nystrom.cuh"
+#include "quad_math.cuh"
 
 namespace bemgpu {
 
@@ -483,6 +484,55 @@ __global__ void __launch_bounds__(kNyCorrT) k_ny_correct_fluid(NyInst I) {
   }
 }
 
+// ------------------------------------------------------------------ compressed operators
+template <typename R>
+__global__ void k_ny_hm_diag(NyHm H) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= H.n) return;
+  const int64_t o = H.dst[i * kNyNodes + (i % kNyNodes)];
+  cx<R>* d1 = static_cast<cx<R>*>(H.D1);
+  cx<R>* d2 = static_cast<cx<R>*>(H.D2);
+  d1[o] = cx<R>{(R)0.5, (R)0};
+  d2[o] = cx<R>{(R)(0.5 * H.a_re), (R)(0.5 * H.a_im)};
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kNyCorrT) k_ny_hm_correct(NyHm H) {
+  const int64_t e = (int64_t)blockIdx.x * kNyCorrT + threadIdx.x;
+  const int64_t n = H.n;
+  if (e >= n / kNyNodes) return;
+  const z2* tr = reinterpret_cast<const z2*>(H.trace);
+  const z2* Y = reinterpret_cast<const z2*>(H.Y);
+  cx<R>* d1 = static_cast<cx<R>*>(H.D1);
+  cx<R>* d2 = static_cast<cx<R>*>(H.D2);
+  const int64_t b = e * kNyNodes;
+  NyFit F;
+  if (!ny_fit_factor(F, tr, n, b)) {
+    H.status[e] = 1;
+    return;
+  }
+  const z2 al = {H.a_re, H.a_im};
+  for (int t = 0; t < kNyNodes; ++t) {
+    const int64_t row = b + t;
+    const int64_t pr = H.iperm[row];
+    z2 d[kNyBasis];
+    for (int s = 0; s < kNyBasis; ++s) {
+      const z2 y = Y[pr + (int64_t)s * n];
+      const z2 u = tr[(int64_t)s * n + row], f = tr[(int64_t)(kNyBasis + s) * n + row];
+      const z2 af = zmul(al, f);
+      d[s] = {y.x - u.x - af.x, y.y - u.y - af.y};
+    }
+    z2 w[kNyFit];
+    ny_fit_solve(F, d, w);
+    for (int j = 0; j < kNyNodes; ++j) {
+      const int64_t o = H.dst[row * kNyNodes + j];
+      d1[o] = cx<R>{(R)((double)d1[o].x - w[j].x), (R)((double)d1[o].y - w[j].y)};
+      d2[o] = cx<R>{(R)((double)d2[o].x - w[kNyNodes + j].x),
+                    (R)((double)d2[o].y - w[kNyNodes + j].y)};
+    }
+  }
+}
+
 // ------------------------------------------------------------------ point evaluation
 // Field at a point, one CTA per point, in the form the reference uses for point
 // evaluation (fields/pressure.jl:453-467 through quadrature/fluid.jl:104-163 with
@@ -674,6 +724,25 @@ void launch_nystrom_pressure(const Launch& L, const NyInst& traces, const NyPoin
     k_ny_pressure<<<(unsigned)P.npts, kNyPtT, 0, L.stream>>>(P);
     count_launch(1);
   }
+}
+
+void launch_nystrom_hm_diag(const Launch& L, const NyHm& H) {
+  const unsigned g = (unsigned)((H.n + 255) / 256);
+  if (H.f32)
+    k_ny_hm_diag<float><<<g, 256, 0, L.stream>>>(H);
+  else
+    k_ny_hm_diag<double><<<g, 256, 0, L.stream>>>(H);
+  count_launch(1);
+}
+
+void launch_nystrom_hm_correct(const Launch& L, const NyHm& H) {
+  const int64_t ne = H.n / kNyNodes;
+  const unsigned g = (unsigned)((ne + kNyCorrT - 1) / kNyCorrT);
+  if (H.f32)
+    k_ny_hm_correct<float><<<g, kNyCorrT, 0, L.stream>>>(H);
+  else
+    k_ny_hm_correct<double><<<g, kNyCorrT, 0, L.stream>>>(H);
+  count_launch(1);
 }
 
 void launch_nystrom(const Launch& L, const NyInst& I0) {

@@ -65,6 +65,23 @@ struct NyPoints {
   double dirs[3 * kNyBasis];  // plane-wave directions of the interpolants
 };
 
+// Element corrections of compressed (hierarchical) rigid/soft node operators: the same
+// fit as the dense path with the combined defect  M2 F + M1 U - U - alpha F  taken from
+// products of the compressed M1, M2 (nine columns, permuted order), written into the full
+// leaf blocks that hold every same-element pair.
+struct NyHm {
+  const double* trace;   // node-order interpolant traces [2][kNyBasis][n] complex
+  const double* Y;       // (M1 U + M2 F) in the tree's permuted order, n x kNyBasis complex
+  const int32_t* iperm;  // node -> permuted position
+  const int64_t* dst;    // n x 7: full-block offset of the pair (node i, node 7 (i / 7) + j)
+  void* D1;              // full-block pools of M1 and M2 (complex64 when f32)
+  void* D2;
+  int64_t n;
+  double a_re, a_im;     // Burton-Miller coupling
+  int32_t f32;
+  int32_t* status;       // per element: 1 when its fit was rank-deficient
+};
+
 // Scratch of launch_nystrom in doubles: traces (both wavenumbers for fluid bodies) and
 // defect partials.
 int64_t nystrom_scratch_doubles(int64_t n, int32_t n_chunks, int32_t fluid);
@@ -74,6 +91,10 @@ int32_t nystrom_chunks(int64_t n);
 #ifdef __CUDACC__
 // Assembles M1 and M2 of one instance with the correction applied.
 void launch_nystrom(const Launch& L, const NyInst& I);
+// The diagonal of the uncorrected node operators (1/2 in M1, alpha / 2 in M2) into the
+// full blocks (before the defect products), and the element corrections (after them).
+void launch_nystrom_hm_diag(const Launch& L, const NyHm& H);
+void launch_nystrom_hm_correct(const Launch& L, const NyHm& H);
 // Interpolant traces (traces.trace, from traces.nodes / n / k / dirs), then the field at
 // every point of P.
 void launch_nystrom_pressure(const Launch& L, const NyInst& traces, const NyPoints& P);

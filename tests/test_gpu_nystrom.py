@@ -216,6 +216,69 @@ def test_fluid_mixed_refinement_contract(ctx):
     sm.close()
 
 
+def test_compressed_node_operators_match_dense(ctx):
+    """The reference's default configuration: Nyström nodes + compressed operators +
+    GMRES.  At tol 1e-10 and reltol 1e-11 the solution equals the dense oracle's."""
+    nodes, tris = meshes.icosphere(0.01, 2)
+    surf = bemgpu.mesh(nodes, tris)
+    beta, alpha = 0.7, 0.4
+    sol = bemgpu.bem(surf, bemgpu.Rigid(), K38, incidence_angle=beta, incidence_azimuth=alpha,
+                     ctx=ctx, discretization="nystrom",
+                     compression=dict(method="hmatrix", tol=1e-10, leaf_size=32),
+                     gmres_kwargs=dict(reltol=1e-11, restart=500, maxiter=4000))
+    st = sol.hmatrix_stats()
+    assert st["lowrank_blocks"] > 0 and st["gmres_converged"]
+    p, q = sol.traces()
+    rp, rq, (y, ny, w) = NY.solve(nodes, tris, "rigid", K38, beta, alpha)
+    for u, v in ((p, rp), (q, rq)):
+        assert np.linalg.norm(u - v) <= 1e-8 * np.linalg.norm(v)
+    d = O.incidence_direction(beta, alpha)
+    ref = NY.far_field(y, ny, w, K38, -d, rp, rq)
+    assert abs(bemgpu.scattering_amplitude(sol) - ref) <= 1e-8 * abs(ref)
+    sol.close()
+
+
+def test_compressed_soft_gmres_follows_the_oracle(ctx):
+    """The Nyström soft system's eigenvalues straddle the imaginary axis, so restarted GMRES
+    stalls on it (the dense factor solves it); the compressed GPU solve follows the
+    oracle's GMRES on the dense matrix step by step and warns as the reference does."""
+    nodes, tris = meshes.icosphere(0.01, 2)
+    surf = bemgpu.mesh(nodes, tris)
+    kw = dict(reltol=1e-8, restart=150, maxiter=300)
+    with pytest.warns(RuntimeWarning):
+        sol = bemgpu.bem(surf, bemgpu.PressureRelease(), K38, incidence_angle=0.7,
+                         incidence_azimuth=0.4, ctx=ctx, discretization="nystrom",
+                         compression=dict(method="hmatrix", tol=1e-10, leaf_size=32),
+                         gmres_kwargs=kw)
+    P = O.Panels(nodes, tris)
+    M1, M2 = NY.assemble(P, K38, True)
+    y, ny, w = NY.nodes_of(P)
+    d = O.incidence_direction(0.7, 0.4)
+    b = M1 @ np.exp(1j * K38 * (y @ d))
+    x, info = O.gmres(M2, b, **kw)
+    hist = sol.residual_history(0)
+    assert not info["converged"] and len(hist) == len(info["history"])
+    assert np.allclose(hist, info["history"], rtol=1e-6)
+    sol.close()
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_compressed_node_operators_at_the_reference_defaults(ctx, precision):
+    nodes, tris = meshes.icosphere(0.01, 3)
+    surf = bemgpu.mesh(nodes, tris)
+    dense = bemgpu.bem(surf, bemgpu.Rigid(), K38, ctx=ctx, discretization="nystrom")
+    sol = bemgpu.bem(surf, bemgpu.Rigid(), K38, ctx=ctx, discretization="nystrom",
+                     precision=precision, compression=dict(method="hmatrix", tol=1e-5))
+    fd, fh = bemgpu.scattering_amplitude(dense), bemgpu.scattering_amplitude(sol)
+    assert abs(20 * math.log10(abs(fh) / abs(fd))) < 0.05
+    assert sol.hmatrix_stats()["compression"] < 0.5
+    pts = np.array([[0.0, 0.0, 0.013], [0.02, 0.0, 0.0]])
+    ph, pd = bemgpu.pressure(sol, pts), bemgpu.pressure(dense, pts)
+    assert np.all(np.abs(ph - pd) < 1e-3 * np.abs(pd))
+    dense.close()
+    sol.close()
+
+
 def test_unsupported_combinations_are_rejected(ctx):
     nodes, tris = meshes.icosphere(0.01, 1)
     surf = bemgpu.mesh(nodes, tris)
@@ -223,5 +286,5 @@ def test_unsupported_combinations_are_rejected(ctx):
         bemgpu.bem([surf], [bemgpu.FluidFilled(1.03, 1.02)], K38, ctx=ctx,
                    discretization="nystrom")
     with pytest.raises(bemgpu.ArgumentError):
-        bemgpu.bem(surf, bemgpu.Rigid(), K38, ctx=ctx, discretization="nystrom",
+        bemgpu.bem(surf, bemgpu.FluidFilled(1.03, 1.02), K38, ctx=ctx, discretization="nystrom",
                    compression=dict(method="hmatrix"))
