@@ -4,7 +4,7 @@
 // surface quadrature nodes (solvers/bem/full.jl:68-128, Inti.single_double_layer and
 // Inti.adj_double_layer_hypersingular with correction=(method=:dim,)), and corrects the
 // singular and nearly singular quadrature with a Green-identity fit over each target's
-// nearest element (the structure of solvers/bem/quadrature/fluid.jl:104-163: defect of
+// nearest element (the structure of solvers/bem/quadrature/fluid.jl:94-163: defect of
 // the discrete identity on a basis of Helmholtz solutions, scaled minimum-norm fit of the
 // element's node weights).  The basis here is kNyBasis plane waves (Faria, Perez-Arancibia
 // and Bonnet 2021, doi:10.1016/j.cma.2021.113703, for the general-purpose kernel
@@ -535,7 +535,7 @@ __global__ void __launch_bounds__(kNyCorrT) k_ny_hm_correct(NyHm H) {
 
 // ------------------------------------------------------------------ point evaluation
 // Field at a point, one CTA per point, in the form the reference uses for point
-// evaluation (fields/pressure.jl:453-467 through quadrature/fluid.jl:104-163 with
+// evaluation (fields/pressure.jl:448-467 through quadrature/fluid.jl:94-163 with
 // exclude_nearest=true): the element of the nearest node is left out of the node sum and
 // its contribution recovered from the fit of the interpolants' defect
 //   mult u(x) + S_excl du/dn - D_excl u,   mult 0 outside the body, -1 inside.

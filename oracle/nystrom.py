@@ -7,12 +7,12 @@ Restates the reference's rigid/soft Nyström system on the surface quadrature no
   Burton-Miller / CBIE combinations and right-hand sides of ``_assemble_full_boundary`` and
   ``_solve_full_boundary`` (solvers/bem/full.jl:68-128, 130-184);
 * the density-interpolation correction in the structure of ``_fluid_layer_operators``
-  (solvers/bem/quadrature/fluid.jl:104-163): the defect of the discrete Green identity
+  (solvers/bem/quadrature/fluid.jl:94-163): the defect of the discrete Green identity
   ``mult * u + S du/dn - D u`` (and its normal-derivative form ``mult * du/dn + K' du/dn -
   H u``, ``mult = -1/2`` on the surface) on a basis of Helmholtz solutions, fitted per
   target on its nearest element (for on-surface targets, the target's own element) by a
   scaled minimum-norm solve through an SVD with the 1e-13 relative cutoff
-  (fluid.jl:145-152); corrections ``S -= w_flux``, ``D += w_pressure`` (fluid.jl:153-155).
+  (fluid.jl:130-136); corrections ``S -= w_flux``, ``D += w_pressure`` (fluid.jl:137-139).
 
 The basis is nine plane waves exp(i k d . y) with fixed integer directions (the general
 correction of the reference lives in Inti.jl, a third-party package not present here; the
@@ -77,7 +77,7 @@ def traces(y, ny, k):
 
 
 def fit_weights(u, f, defect, cutoff=1e-13):
-    """Per element: minimum-norm weights of the scaled trace fit (fluid.jl:145-152).
+    """Per element: minimum-norm weights of the scaled trace fit (fluid.jl:130-136).
 
     Returns W (elements x 7 targets x 14 weights): pressure weights then flux weights."""
     N = u.shape[0]
@@ -144,7 +144,7 @@ def _inside(P: O.Panels, x):
 
 def pressure(P: O.Panels, k, points, p, q, direction, field="scattered", g=None, h=None):
     """Field of a Nyström solution at points, in the reference's point-evaluation form
-    (fields/pressure.jl:453-467 through quadrature/fluid.jl:104-163 with
+    (fields/pressure.jl:448-467 through quadrature/fluid.jl:94-163 with
     exclude_nearest=true): the element of the nearest node is left out of the node sum and
     its contribution recovered from the fit of the interpolants' defect
     mult u(x) + S_excl du/dn - D_excl u (mult 0 outside, -1 inside).  Outside:

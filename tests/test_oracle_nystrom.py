@@ -1,7 +1,7 @@
 """The Nyström oracle pinned before it is trusted (no GPU).
 
 Pins: the corrected discrete Green identities hold for every interpolant (the defining
-property of the density-interpolation correction, solvers/bem/quadrature/fluid.jl:138-156);
+property of the density-interpolation correction, solvers/bem/quadrature/fluid.jl:124-149);
 the sphere's modal series (solvers/modal/sphere.jl) at the reference's 0.1 dB; error
 decreasing under refinement; the fit keeps full rank over five decades of k times the
 panel size (no singular value reaches the 1e-13 cutoff, so every pseudo-inverse solution
