@@ -878,7 +878,7 @@ def run_config5(args):
                   "achieved": achieved, "peak": hbm, "unit": "GB/s",
                   "frac": achieved / hbm if achieved else None, "peak_source": f"{which} HBM",
                   # ncu DRAM bytes of the four product kernels over the algorithmic bytes,
-                  # same workload (profiles/hmatrix_aca_products_rigid_spheroid_20480_mixed.md)
+                  # one capture of the same workload (362.57 MB read+written, 360.53 MB)
                   "traffic": NCU_HM_TRAFFIC * mv_bytes, "algorithmic_bytes_per_launch": mv_bytes},
         clocks=m["clocks"], gpu_launches=m["launches"], cpu_baseline=cpu)
     print(json.dumps(line))
