@@ -170,9 +170,9 @@ The reference's `bem(surface::Mesh, boundary, k; ...)` on the GPU.  With
 `compression=(method=:hmatrix, tol=1e-5)` a Rigid or PressureRelease body is solved as the
 reference's `solve_full_bem` does by default: compressed operators and GMRES with
 `gmres_kwargs` (reltol, abstol, restart, maxiter); non-convergence warns as there.
-`discretization=:nystrom` (dense factor) solves on the quadrature nodes with the
-density-interpolation correction, as the reference's default `correction=(method=:dim,)`
-does.
+`discretization=:nystrom` solves on the quadrature nodes with the density-interpolation
+correction, as the reference's default `correction=(method=:dim,)` does (dense factor, or
+with `compression` the compressed node operators and GMRES for Rigid/PressureRelease).
 """
 function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
         incidence_azimuth::Real = 0.0, formulation::Union{Nothing, Symbol} = nothing,
@@ -192,7 +192,8 @@ function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
         p = Problem(_boundary_code(boundary),
             formulation === nothing ? Int32(-1) : FORMULATIONS[formulation],
             precision === :mixed ? Int32(1) : Int32(0), Int32(1), Float64(k), 1.0, 1.0,
-            1e-13, Int32(8), Int32(0), 10eps(Float32), 2.0, Int32(0), Int32(0))
+            1e-13, Int32(8), Int32(0), 10eps(Float32), 2.0,
+            discretization === :nystrom ? Int32(1) : Int32(0), Int32(0))
         o = HmatrixOptions(get(compression, :tol, 1e-5), get(compression, :eta, 3.0),
             Int32(get(compression, :leaf_size, 64)), Int32(get(gmres_kwargs, :restart, 150)),
             get(gmres_kwargs, :reltol, 1e-4), get(gmres_kwargs, :abstol, 0.0),
