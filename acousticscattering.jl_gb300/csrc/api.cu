@@ -2772,6 +2772,11 @@ struct HmData {
   int32_t n_lr = 0, n_dense = 0, n_leaf = 0;
   int64_t tstride = 0, pstride = 0;
   bool f32 = false;  // complex64 operators, FP32 entries and products (precision mixed)
+  // Nyström pressure-release systems: inverses of the element blocks of operator ny_op,
+  // applied on the right inside GMRES (the node system's spectrum straddles the imaginary
+  // axis, where restarted GMRES stalls without it)
+  Buf ny_pinv;
+  int ny_op = -1;
   bemgpu_hmatrix_stats st{};
   size_t bytes() const {
     size_t b = leaf_lo.bytes + leaf_ptr.bytes + leaf_ent.bytes + dn.bytes + D1.bytes +
@@ -3147,6 +3152,24 @@ int hm_build(bemgpu_ctx* c, MeshData* m, const bemgpu_problem& p, int kind,
     TRY(download(c, status, &st, (size_t)std::max<int64_t>(1, n / kNyNodes)));
     for (int32_t v : st)
       if (v) return fail(c, BEMGPU_EINVAL, "density-interpolation fit is rank-deficient");
+    if (p.boundary == BEMGPU_PRESSURE_RELEASE) {  // the system operator is M2
+      TRY(alloc(c, (size_t)n * kNyNodes * 16, &H->ny_pinv));
+      CUDA_TRY(c, cudaMemsetAsync(status.p, 0, status.bytes, c->stream));
+      NyPrec B{};
+      B.Pinv = H->ny_pinv.as<double>();
+      B.iperm = pc->iperm.as<int32_t>();
+      B.dst = pc->ny_dst.as<int64_t>();
+      B.D = H->D2.p;
+      B.n = n;
+      B.f32 = H->f32 ? 1 : 0;
+      B.status = status.as<int32_t>();
+      launch_nystrom_prec_build(L, B);
+      CUDA_TRY(c, cudaGetLastError());
+      TRY(download(c, status, &st, (size_t)std::max<int64_t>(1, n / kNyNodes)));
+      for (int32_t v : st)
+        if (v) return fail(c, BEMGPU_ESINGULAR, "singular element block of the node system");
+      H->ny_op = 1;
+    }
   }
   bemgpu_hmatrix_stats& S = H->st;
   std::memset(&S, 0, sizeof S);
@@ -3205,6 +3228,17 @@ int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x,
     CUDA_TRY(c, cudaMemsetAsync(hb.p, 0, hb.bytes, c->stream));
     double* xg = x + 2 * (size_t)r0 * n;
     const double* bg = b + 2 * (size_t)r0 * n;
+    // right preconditioning (Nyström pressure-release systems): GMRES runs on A P^-1 with
+    // the iterate y in W.x; every product takes P^-1 first, and x = P^-1 y at the end
+    const bool prec = op == H.ny_op && H.ny_pinv.p;
+    NyPrec Pc{};
+    Buf pt;
+    if (prec) {
+      TRY(alloc(c, (size_t)g * n * 16, &pt));
+      Pc.Pinv = H.ny_pinv.as<double>();
+      Pc.iperm = H.pc->iperm.as<int32_t>();
+      Pc.n = n;
+    }
     CUDA_TRY(c, cudaMemsetAsync(xg, 0, (size_t)g * n * 16, c->stream));
     CUDA_TRY(c, cudaMemcpyAsync(w.p, bg, (size_t)g * n * 16, cudaMemcpyDeviceToDevice, c->stream));
     GmWork W{};
@@ -3246,8 +3280,14 @@ int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x,
     // steps captured once replays any kSteps consecutive steps of any cycle
     constexpr int32_t kSteps = 4;
     auto step = [&]() {
-      launch_hm_matvec(L, A, W.Vb, (int64_t)(R + 1) * n, W.w, n, nullptr, 0, 0.0, 1.0, g, W.st,
-                       1, W.jcur, n);
+      if (prec) {
+        launch_nystrom_prec_apply(L, Pc, W.Vb, (int64_t)(R + 1) * n, W.jcur, n,
+                                  pt.as<double>(), n, g);
+        launch_hm_matvec(L, A, pt.as<double>(), n, W.w, n, nullptr, 0, 0.0, 1.0, g, W.st, 1);
+      } else {
+        launch_hm_matvec(L, A, W.Vb, (int64_t)(R + 1) * n, W.w, n, nullptr, 0, 0.0, 1.0, g,
+                         W.st, 1, W.jcur, n);
+      }
       launch_gm_arnoldi(L, W, -1);
       launch_gm_rotate(L, W, -1);
     };
@@ -3291,15 +3331,22 @@ int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x,
           }
         }
         launch_gm_update_x(L, W);
-        launch_hm_matvec(L, A, xg, n, W.w, n, bg, n, 1.0, -1.0, g, W.st, 2);
+        if (prec) launch_nystrom_prec_apply(L, Pc, xg, n, nullptr, 0, pt.as<double>(), n, g);
+        launch_hm_matvec(L, A, prec ? pt.as<double>() : xg, n, W.w, n, bg, n, 1.0, -1.0, g,
+                         W.st, 2);
         launch_gm_start(L, W, o.reltol, o.abstol, 0);
       }
       CUDA_TRY(c, cudaGetLastError());
       TRY(active(&na));
     }
-    // explicit residuals b - A x
+    // explicit residuals b - A x (x = P^-1 y under the preconditioner, then kept in xg)
     {
       Prof pr(c, "gmres");
+      if (prec) {
+        launch_nystrom_prec_apply(L, Pc, xg, n, nullptr, 0, pt.as<double>(), n, g);
+        CUDA_TRY(c, cudaMemcpyAsync(xg, pt.p, (size_t)g * n * 16, cudaMemcpyDeviceToDevice,
+                                    c->stream));
+      }
       launch_hm_matvec(L, A, xg, n, W.w, n, bg, n, 1.0, -1.0, g, nullptr, 0);
     }
     std::vector<double> wh;

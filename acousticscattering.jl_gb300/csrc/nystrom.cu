@@ -533,6 +533,75 @@ __global__ void __launch_bounds__(kNyCorrT) k_ny_hm_correct(NyHm H) {
   }
 }
 
+// ------------------------------------------------------------------ block preconditioner
+// Gauss-Jordan inversion with partial pivoting of one element's block, FP64.
+template <typename R>
+__global__ void k_ny_prec_build(NyPrec P) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.n / kNyNodes) return;
+  const cx<R>* D = static_cast<const cx<R>*>(P.D);
+  z2 a[kNyNodes][2 * kNyNodes];
+  for (int t = 0; t < kNyNodes; ++t)
+    for (int j = 0; j < kNyNodes; ++j) {
+      const cx<R> v = D[P.dst[(e * kNyNodes + t) * kNyNodes + j]];
+      a[t][j] = {(double)v.x, (double)v.y};
+      a[t][kNyNodes + j] = {t == j ? 1.0 : 0.0, 0.0};
+    }
+  for (int c = 0; c < kNyNodes; ++c) {
+    int piv = c;
+    double best = hypot(a[c][c].x, a[c][c].y);
+    for (int t = c + 1; t < kNyNodes; ++t) {
+      const double v = hypot(a[t][c].x, a[t][c].y);
+      if (v > best) {
+        best = v;
+        piv = t;
+      }
+    }
+    if (!(best > 0.0)) {
+      P.status[e] = 1;
+      return;
+    }
+    if (piv != c)
+      for (int j = 0; j < 2 * kNyNodes; ++j) {
+        const z2 tmp = a[c][j];
+        a[c][j] = a[piv][j];
+        a[piv][j] = tmp;
+      }
+    const z2 inv = zdiv(z2{1.0, 0.0}, a[c][c]);
+    for (int j = 0; j < 2 * kNyNodes; ++j) a[c][j] = zmul(a[c][j], inv);
+    for (int t = 0; t < kNyNodes; ++t) {
+      if (t == c) continue;
+      const z2 f = a[t][c];
+      for (int j = 0; j < 2 * kNyNodes; ++j) zfms(a[t][j], f, a[c][j]);
+    }
+  }
+  z2* out = reinterpret_cast<z2*>(P.Pinv) + e * kNyNodes * kNyNodes;
+  for (int t = 0; t < kNyNodes; ++t)
+    for (int j = 0; j < kNyNodes; ++j) out[t * kNyNodes + j] = a[t][kNyNodes + j];
+}
+
+// thread = (element, vector): the element's 7 entries gathered from their permuted
+// positions, multiplied by its block inverse, scattered back
+__global__ void k_ny_prec_apply(NyPrec P, const double* src, int64_t lds, const int32_t* jptr,
+                                int64_t jstride, double* dst, int64_t ldd, int32_t nr) {
+  const int64_t ne = P.n / kNyNodes;
+  const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= ne * nr) return;
+  const int64_t e = id % ne;
+  const int r = (int)(id / ne);
+  const z2* s = reinterpret_cast<const z2*>(src) + (int64_t)r * lds +
+                (jptr ? (int64_t)(*jptr) * jstride : 0);
+  z2* d = reinterpret_cast<z2*>(dst) + (int64_t)r * ldd;
+  const z2* B = reinterpret_cast<const z2*>(P.Pinv) + e * kNyNodes * kNyNodes;
+  z2 v[kNyNodes];
+  for (int j = 0; j < kNyNodes; ++j) v[j] = s[P.iperm[e * kNyNodes + j]];
+  for (int t = 0; t < kNyNodes; ++t) {
+    z2 acc = {0.0, 0.0};
+    for (int j = 0; j < kNyNodes; ++j) zfma(acc, B[t * kNyNodes + j], v[j]);
+    d[P.iperm[e * kNyNodes + t]] = acc;
+  }
+}
+
 // ------------------------------------------------------------------ point evaluation
 // Field at a point, one CTA per point, in the form the reference uses for point
 // evaluation (fields/pressure.jl:448-467 through quadrature/fluid.jl:94-163 with
@@ -724,6 +793,25 @@ void launch_nystrom_pressure(const Launch& L, const NyInst& traces, const NyPoin
     k_ny_pressure<<<(unsigned)P.npts, kNyPtT, 0, L.stream>>>(P);
     count_launch(1);
   }
+}
+
+void launch_nystrom_prec_build(const Launch& L, const NyPrec& P) {
+  const int64_t ne = P.n / kNyNodes;
+  const unsigned g = (unsigned)((ne + 127) / 128);
+  if (P.f32)
+    k_ny_prec_build<float><<<g, 128, 0, L.stream>>>(P);
+  else
+    k_ny_prec_build<double><<<g, 128, 0, L.stream>>>(P);
+  count_launch(1);
+}
+
+void launch_nystrom_prec_apply(const Launch& L, const NyPrec& P, const double* src, int64_t lds,
+                               const int32_t* jptr, int64_t jstride, double* dst, int64_t ldd,
+                               int32_t nr) {
+  const int64_t total = P.n / kNyNodes * nr;
+  k_ny_prec_apply<<<(unsigned)((total + 127) / 128), 128, 0, L.stream>>>(P, src, lds, jptr,
+                                                                          jstride, dst, ldd, nr);
+  count_launch(1);
 }
 
 void launch_nystrom_hm_diag(const Launch& L, const NyHm& H) {

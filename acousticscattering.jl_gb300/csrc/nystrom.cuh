@@ -91,6 +91,25 @@ int32_t nystrom_chunks(int64_t n);
 #ifdef __CUDACC__
 // Assembles M1 and M2 of one instance with the correction applied.
 void launch_nystrom(const Launch& L, const NyInst& I);
+// Element-block preconditioner of a compressed Nyström system: the inverse of every
+// element's 7 x 7 diagonal block (node order), applied on the right inside GMRES.
+struct NyPrec {
+  double* Pinv;          // n / 7 blocks of 7 x 7 complex128, row-major (target, source)
+  const int32_t* iperm;  // node -> permuted position
+  const int64_t* dst;    // as NyHm.dst
+  const void* D;         // the system operator's full-block pool (complex64 when f32)
+  int64_t n;
+  int32_t f32;
+  int32_t* status;       // per element: 1 when its block is singular
+};
+// Pinv from the corrected full blocks.
+void launch_nystrom_prec_build(const Launch& L, const NyPrec& P);
+// dst[:, r] = Pinv src[:, r] for nr vectors in permuted order (ld lds / ldd complex);
+// jptr (optional): src offset by (*jptr) * jstride complex entries (the Arnoldi vector).
+void launch_nystrom_prec_apply(const Launch& L, const NyPrec& P, const double* src, int64_t lds,
+                               const int32_t* jptr, int64_t jstride, double* dst, int64_t ldd,
+                               int32_t nr);
+
 // The diagonal of the uncorrected node operators (1/2 in M1, alpha / 2 in M2) into the
 // full blocks (before the defect products), and the element corrections (after them).
 void launch_nystrom_hm_diag(const Launch& L, const NyHm& H);
