@@ -3197,9 +3197,13 @@ int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x,
   const Launch L = c->launch();
   const int32_t R = o.restart, mi = std::max(1, o.maxiter);
   const int32_t chunks = (int32_t)((n + kGmChunk - 1) / kGmChunk);
+  // bytes per right-hand side: Krylov basis, x / w vectors, Hessenberg matrix, partial
+  // dots, history, the products' scratch, rotations, and the preconditioned solve's
+  // P^-1 product (n complex) when the element-block preconditioner applies
+  const bool precond = op == H.ny_op && H.ny_pinv.p;
   const size_t per = ((size_t)(R + 1) * n + 2 * (size_t)n) * 16 + (size_t)(R + 1) * R * 16 +
                      (size_t)chunks * (R + 1) * 16 + (size_t)mi * 8 + H.scratch_bytes(1) +
-                     (size_t)(4 * R + 8) * 16;
+                     (size_t)(4 * R + 8) * 16 + (precond ? (size_t)n * 16 : 0);
   const uint64_t avail = c->budget > c->live ? (c->budget - c->live) : 0;
   const int32_t G = (int32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)nr, avail / 2 / per));
   hist->assign((size_t)nr * mi, 0.0);

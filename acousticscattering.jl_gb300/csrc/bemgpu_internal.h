@@ -9,6 +9,9 @@
 
 #ifdef __CUDACC__
 #include <cuda_runtime.h>
+
+#include <atomic>
+#include <mutex>
 #endif
 
 namespace bemgpu {
@@ -151,6 +154,54 @@ struct TrsvWork {
 
 // ------------------------------------------------------------------ launch wrappers
 #ifdef __CUDACC__
+constexpr int kMaxDevices = 64;
+
+// One-time set-up per device.  Function attributes such as the dynamic shared-memory
+// opt-in apply to the device that is current when they are set, so a launch helper
+// keeps one of these and calls call(fn) before its launch: fn runs once for each device
+// index (under a lock; later calls on that device are one atomic load).
+class PerDeviceOnce {
+ public:
+  template <class F>
+  void call(F&& fn) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+      cudaGetLastError();
+      fn();
+      return;
+    }
+    if (done_[dev].load(std::memory_order_acquire)) return;
+    std::lock_guard<std::mutex> lk(mu_);
+    if (done_[dev].load(std::memory_order_relaxed)) return;
+    fn();
+    done_[dev].store(true, std::memory_order_release);
+  }
+
+ private:
+  std::mutex mu_;
+  std::atomic<bool> done_[kMaxDevices]{};
+};
+
+// Streaming multiprocessors of the current device (looked up once per device).
+inline int device_sm_count() {
+  static std::atomic<int> sms[kMaxDevices]{};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return 1;
+  }
+  int v = sms[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        v <= 0) {
+      cudaGetLastError();
+      return 1;
+    }
+    sms[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
+
 struct Launch {
   cudaStream_t stream;
   int* err_flag;                  // device word set by bounded waits that give up

@@ -567,20 +567,19 @@ void launch_tc_pack(const Launch& L, const TcPackInst* d, int ninst, int64_t max
   count_launch(1);
 }
 
-static int g_sms = 0;
-
 bool tc_encode_cmap(void* map, const void* c, int64_t ldc, int64_t rows, int64_t cols) {
-  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-  static bool looked = false;
-  if (!looked) {
-    looked = true;
+  // the driver entry point is process-wide; a function-local static is initialised once,
+  // thread-safely
+  static const PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q{};
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
                                          &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  }
+      return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    cudaGetLastError();
+    return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+  }();
   if (!encode || (ldc & 1) || rows <= 0 || cols <= 0 ||
       (reinterpret_cast<uintptr_t>(c) & 15) != 0)
     return false;
@@ -599,15 +598,12 @@ void launch_tc_cgemm(const Launch& L, const TcGemmInst* d, int ninst, int64_t to
                      bool red) {
   if (ninst <= 0 || total_tiles <= 0) return;
   const size_t smem = 1024 + kTcStages * kTcStageBytes + 2 * kTcRedBytes + sizeof(TcShared);
-  static bool attr = false;
-  if (!attr) {
+  static PerDeviceOnce attr;
+  attr.call([&] {
     cudaFuncSetAttribute(k_tc_cgemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-    attr = true;
-  }
-  const int64_t grid = total_tiles < g_sms ? total_tiles : g_sms;
+  });
+  const int64_t sms = device_sm_count();
+  const int64_t grid = total_tiles < sms ? total_tiles : sms;
   k_tc_cgemm<<<(unsigned)grid, kTcThreads, smem, L.stream>>>(d, ninst, L.err_flag, red ? 1 : 0);
   count_launch(1);
 }

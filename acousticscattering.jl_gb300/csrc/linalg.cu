@@ -807,12 +807,11 @@ template <typename R, bool EL, bool TR, bool UN, int SW>
 static void trsv_full_t(const Launch& L, const MatInst* d, int ninst, int64_t nmax,
                         int32_t max_rhs) {
   const size_t smem = (size_t)nmax * sizeof(cx<R>);
-  static bool attr = false;
-  if (!attr) {
+  static PerDeviceOnce attr;
+  attr.call([] {
     cudaFuncSetAttribute(k_trsv_full<R, EL, TR, UN, SW>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr = true;
-  }
+  });
   k_trsv_full<R, EL, TR, UN, SW><<<dim3((unsigned)max_rhs, (unsigned)ninst), kTrsvThreads, smem,
                                    L.stream>>>(d);
   count_launch(1);
@@ -881,11 +880,10 @@ __global__ void __launch_bounds__(256) k_linv_neg(const MatInst* __restrict__ in
 
 void launch_linv_neg(const Launch& L, const MatInst* d, int ninst, int64_t k0, float2* const* outs) {
   const size_t smem = (size_t)kLinvB * (kLinvB + 1) * sizeof(cx<float>);
-  static bool attr = false;
-  if (!attr) {
+  static PerDeviceOnce attr;
+  attr.call([&] {
     cudaFuncSetAttribute(k_linv_neg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  });
   k_linv_neg<<<ninst, 256, smem, L.stream>>>(d, k0, outs);
   count_launch(1);
 }
@@ -1217,12 +1215,7 @@ static int prec_is_single(int prec) { return prec == 1; }
 // CTAs per instance of the left-looking panel kernel: as many as keep the batch on the
 // SMs in one wave (a power of two, 2..8: the portable cluster limit).
 static int getf2_cluster(int ninst) {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  }
+  const int sms = device_sm_count();
   int cs = 2;
   while (cs < 8 && (int64_t)ninst * cs * 2 <= sms) cs *= 2;
   return cs;
@@ -1294,12 +1287,12 @@ template <typename R, int NB>
 static void trsm_t(const Launch& L, const MatInst* d, int ninst, int64_t k0, int64_t c_lo,
                    int64_t c_hi) {
   const size_t smem = (size_t)NB * (NB + 1) * sizeof(cx<R>);
-  static bool attr = false;
-  if (!attr && smem > 48 * 1024) {
-    cudaFuncSetAttribute(k_trsm_panel<R, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    attr = true;
-  }
+  static PerDeviceOnce attr;
+  if (smem > 48 * 1024)
+    attr.call([&] {
+      cudaFuncSetAttribute(k_trsm_panel<R, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem);
+    });
   const int64_t per = (int64_t)kTrsmWarps * TrsmCols<R>::value;
   dim3 grid((unsigned)((c_hi - c_lo + per - 1) / per), (unsigned)ninst);
   k_trsm_panel<R, NB><<<grid, kTrsmWarps * 32, smem, L.stream>>>(d, k0, c_lo, c_hi);
@@ -1368,22 +1361,20 @@ template <typename R, bool EL, bool TR, bool UN>
 static void trsv_big_t(const Launch& L, const MatInst* d, int ninst, int64_t nmax,
                        int32_t max_rhs) {
   constexpr size_t smem = diag_smem_bytes<R>();
-  static bool attr = false;
-  if (!attr) {
+  static PerDeviceOnce attr;
+  attr.call([&] {
     cudaFuncSetAttribute(k_trsv_diag<R, EL, TR, UN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
-    attr = true;
-  }
+  });
   // right-hand sides per update CTA: one, or a group sharing the matrix loads
   constexpr int RG = sizeof(R) == 4 ? 8 : 4;
-  static bool uattr = false;
-  if (!uattr) {
+  static PerDeviceOnce uattr;
+  uattr.call([] {
     cudaFuncSetAttribute(k_trsv_big_update<R, EL, TR, RG>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem_bytes<R, RG>());
     cudaFuncSetAttribute(k_trsv_big_update_h<R, EL, RG>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem_bytes<R, RG>());
-    uattr = true;
-  }
+  });
   const int64_t nblk = (nmax + kBigB - 1) / kBigB;
   const unsigned gy = max_rhs >= 4 ? (unsigned)((max_rhs + RG - 1) / RG) : (unsigned)max_rhs;
   auto diag = [&](cudaStream_t s, int64_t r0) {
@@ -1475,11 +1466,10 @@ static void getrs_big_t(const Launch& L, const MatInst* d, int ninst, int64_t nm
 
 void launch_make_perm(const Launch& L, const MatInst* d, int ninst, int64_t nmax) {
   const size_t smem = (size_t)nmax * sizeof(int32_t);
-  static bool attr = false;
-  if (!attr) {
+  static PerDeviceOnce attr;
+  attr.call([] {
     cudaFuncSetAttribute(k_make_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr = true;
-  }
+  });
   k_make_perm<<<ninst, 256, smem, L.stream>>>(d);
   count_launch(1);
 }

@@ -18,7 +18,6 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "bemgpu_internal.h"
@@ -35,10 +34,6 @@ constexpr size_t kPackMax = (size_t)(kNoAllocMaxMN / 128) * (kNoAllocMaxK / 32) 
 constexpr size_t kScratchBytes = kHeaderBytes + 2 * kPackMax;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_scratch_ptr[kMaxDevices] = {nullptr};
 
 struct Layout {
   int* err;
@@ -124,24 +119,35 @@ extern "C" int bemgpu_cgemm_update_noalloc(void* stream, int64_t m, int64_t n, i
     return set_error(BEMGPU_EINVAL, "complex64 operands must be 8-byte aligned");
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+  if (e != cudaSuccess) {
+    cudaGetLastError();
     return set_error(BEMGPU_ENODEV, "no current CUDA device");
-  void* base = nullptr;
-  {
-    // once per device, with that device current: the device address of the array
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[dev]) {
-      e = cudaGetSymbolAddress(&g_scratch_ptr[dev], g_noalloc_scratch);
-      if (e != cudaSuccess) {
-        g_scratch_ptr[dev] = nullptr;
-        return set_error(BEMGPU_ECUDA,
-                         std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      }
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (s) {
+    // the stream must belong to the current device: the array's address below is the
+    // current device's
+    int sdev = -1;
+    e = cudaStreamGetDevice(s, &sdev);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(BEMGPU_EINVAL, std::string("cudaStreamGetDevice: ") +
+                                          cudaGetErrorString(e));
     }
-    base = g_scratch_ptr[dev];
+    if (sdev != dev)
+      return set_error(BEMGPU_EINVAL, "stream belongs to another device than the current one");
+  }
+  // The device address of the array on the current device, looked up on every call (a
+  // cheap query) so that it stays right after a cudaDeviceReset.  The first call on a
+  // device may load the module there, so make it before any stream capture.
+  void* base = nullptr;
+  e = cudaGetSymbolAddress(&base, g_noalloc_scratch);
+  if (e != cudaSuccess || !base) {
+    cudaGetLastError();
+    return set_error(BEMGPU_ECUDA, std::string("cudaGetSymbolAddress: ") +
+                                       cudaGetErrorString(e));
   }
   const Layout Lo = layout(base);
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   k_noalloc_setup<<<1, 1, 0, s>>>(Lo.err, Lo.pack, Lo.gemm, A, lda, B, ldb, C, ldc, m, n, k,
                                   Lo.apack, Lo.bpack);
   count_launch(1);
@@ -150,10 +156,11 @@ extern "C" int bemgpu_cgemm_update_noalloc(void* stream, int64_t m, int64_t n, i
   launch_tc_cgemm(L, Lo.gemm, 1, ((m + 127) / 128) * ((n + 127) / 128));
   e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(BEMGPU_ECUDA, cudaGetErrorString(e));
-  e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return set_error(BEMGPU_ECUDA, cudaGetErrorString(e));
+  // the timeout word, read on the caller's stream (no device-wide synchronisation)
   int h = 0;
-  e = cudaMemcpy(&h, Lo.err, sizeof h, cudaMemcpyDeviceToHost);
+  e = cudaMemcpyAsync(&h, Lo.err, sizeof h, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return set_error(BEMGPU_ECUDA, cudaGetErrorString(e));
+  e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return set_error(BEMGPU_ECUDA, cudaGetErrorString(e));
   if (h != 0) return set_error(BEMGPU_ETIMEOUT, "a bounded device wait gave up");
   return BEMGPU_OK;

@@ -480,10 +480,12 @@ int bemgpu_debug_cgemm(bemgpu_ctx *ctx, int64_t m, int64_t n, int32_t k, const f
  * allocate after start-up.  The operand images, descriptors and timeout word live in a
  * file-scope device array of 4 MiB + 2 KiB that every GPU loading the library holds
  * until the process exits; hence m, n <= 2048 and k <= 128 (larger sizes return
- * BEMGPU_EINVAL).  The first call on a device looks up that array's device address
- * (cudaGetSymbolAddress) with the device current; make that first call before any
- * stream capture.  All calls share the array: calls whose GPU work overlaps race.  The
- * call waits for its stream and returns BEMGPU_ETIMEOUT if a bounded wait gave up.
+ * BEMGPU_EINVAL).  Every call looks up that array's address on the current device
+ * (cudaGetSymbolAddress; the first call on a device may load the module there, so make
+ * it before any stream capture); `stream` must belong to the current device
+ * (BEMGPU_EINVAL otherwise).  All calls share the array: calls whose GPU work overlaps
+ * race.  The call waits for its stream and returns BEMGPU_ETIMEOUT if a bounded wait
+ * gave up.
  * Errors are reported through bemgpu_last_error(NULL, ...).
  */
 int bemgpu_cgemm_update_noalloc(void *stream, int64_t m, int64_t n, int32_t k, const void *A,

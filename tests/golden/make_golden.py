@@ -2,7 +2,8 @@
 
 reference_amplitudes.json
     Independent far-field amplitudes hard-coded in the reference's own tests, read as
-    text from the reference checkout (path in REFERENCE, default /root/reference):
+    text from the reference checkout whose path the REFERENCE environment variable
+    gives (required; e.g. REFERENCE=/root/reference python tests/golden/make_golden.py):
       test/extended/bem/sphere/full3d.jl   "Independent transmission amplitudes"
       test/extended/bem/spheroid/full3d.jl "Full BEM against independent rigid-spheroid
                                             outputs"
@@ -24,7 +25,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path[:0] = [ROOT, os.path.join(ROOT, "acousticscattering.jl_gb300")]
-REFERENCE = os.environ.get("REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("REFERENCE")
 
 _CPLX = r"(-?[0-9.]+(?:e-?[0-9]+)?)\s*([+-])\s*([0-9.]+(?:e-?[0-9]+)?)im"
 
@@ -35,6 +36,8 @@ def _complex(m):
 
 
 def reference_amplitudes():
+    if not REFERENCE:
+        raise SystemExit("set REFERENCE to the reference checkout (AcousticScattering.jl)")
     out = {"source": "reference tests (read as text)", "tolerance": {"db": 0.1, "rel": 0.01}}
     sph = open(os.path.join(REFERENCE, "test/extended/bem/sphere/full3d.jl")).read()
     block = sph[sph.index("Independent transmission amplitudes"):]

@@ -20,13 +20,19 @@ def _surfaces():
 
 def test_same_alone_and_in_the_mix(ctx):
     a, b, c = _surfaces()
+    req = (a, bemgpu.Rigid(), [300.0, 420.0], [0.3, 1.1, 2.0])
     srv = bemgpu.Server(ctx, max_batch=8)
     try:
-        req = (a, bemgpu.Rigid(), [300.0, 420.0], [0.3, 1.1, 2.0])
         t = srv.submit(*req, precision="mixed")
         alone, lat = srv.wait(t)
         assert lat > 0 and np.all(np.isfinite(alone))
-        # the same request among others of different sizes and kinds, submitted together
+    finally:
+        srv.close()
+    # a fresh server (empty factor cache): the same request among others of different
+    # sizes and kinds, submitted together, is assembled, factored and solved inside the
+    # mixed batches, not served from the lone run's factors
+    srv = bemgpu.Server(ctx, max_batch=8)
+    try:
         tickets = [srv.submit(b, bemgpu.FluidFilled(1.0357, 1.0279), [500.0, 700.0], [0.5],
                               precision="mixed"),
                    srv.submit(*req, precision="mixed"),
@@ -34,12 +40,26 @@ def test_same_alone_and_in_the_mix(ctx):
                               precision="mixed"),
                    srv.submit(a, bemgpu.Rigid(), [300.0], [0.7], precision="double")]
         res = [srv.wait(tk)[0] for tk in tickets]
-        assert np.array_equal(res[1], alone)   # bit-identical: batching is not arithmetic
         st = srv.stats()
-        assert st["completed"] == 5 and st["failed"] == 0
-        assert st["cache_hits"] >= 2           # the repeated request reused its factors
     finally:
         srv.close()
+    assert st["cache_hits"] == 0 and st["factorizations"] == 6, st
+    assert np.array_equal(res[1], alone)   # bit-identical: batching is not arithmetic
+    assert st["completed"] == 4 and st["failed"] == 0
+
+
+def test_cached_factors_are_reused(ctx):
+    a, _, _ = _surfaces()
+    req = (a, bemgpu.Rigid(), [300.0, 420.0], [0.3, 1.1])
+    srv = bemgpu.Server(ctx, max_batch=8)
+    try:
+        first = srv.wait(srv.submit(*req, precision="mixed"))[0]
+        again = srv.wait(srv.submit(*req, precision="mixed"))[0]
+        st = srv.stats()
+    finally:
+        srv.close()
+    assert st["cache_hits"] == 2 and st["factorizations"] == 2, st
+    assert np.array_equal(first, again)
 
 
 def test_server_matches_direct_solve(ctx):

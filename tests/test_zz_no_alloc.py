@@ -25,22 +25,31 @@ def _cplx(rng, shape):
     return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
 
 
-def _dev(a):
-    # column-major complex64 on the device: the transpose of a C-contiguous buffer
-    t = torch.from_numpy(np.ascontiguousarray(a.T)).to("cuda")
-    return t
+def _dev(a, ld=None, fill=0):
+    """Column-major complex64 on the device with leading dimension ld >= rows: the
+    transpose of a C-contiguous (cols, ld) buffer whose rows beyond the matrix hold
+    `fill`."""
+    rows, cols = a.shape
+    ld = ld or rows
+    host = np.full((cols, ld), fill, dtype=np.complex64)
+    host[:, :rows] = a.T
+    return torch.from_numpy(host).to("cuda")
 
 
-def _noalloc(A, B, Cm):
+def _noalloc(A, B, Cm, lda=None, ldb=None, ldc=None):
     m, k = A.shape
     n = B.shape[1]
-    dA, dB, dC = _dev(A), _dev(B), _dev(Cm)
+    lda, ldb, ldc = lda or m, ldb or k, ldc or m
+    dA, dB, dC = _dev(A, lda, 7 + 7j), _dev(B, ldb, -5 + 1j), _dev(Cm, ldc, 3 - 2j)
     stream = torch.cuda.current_stream().cuda_stream
     st = C.lib().bemgpu_cgemm_update_noalloc(ctypes.c_void_p(stream), m, n, k,
-                                             ctypes.c_void_p(dA.data_ptr()), m,
-                                             ctypes.c_void_p(dB.data_ptr()), k,
-                                             ctypes.c_void_p(dC.data_ptr()), m)
-    return st, dC.cpu().numpy().T
+                                             ctypes.c_void_p(dA.data_ptr()), lda,
+                                             ctypes.c_void_p(dB.data_ptr()), ldb,
+                                             ctypes.c_void_p(dC.data_ptr()), ldc)
+    full = dC.cpu().numpy()
+    # the rows of C's buffer beyond the matrix must be untouched
+    assert np.all(full[:, m:] == np.complex64(3 - 2j))
+    return st, full[:, :m].T
 
 
 def test_noalloc_matches_allocating_entry_point_twice(ctx):
@@ -54,6 +63,22 @@ def test_noalloc_matches_allocating_entry_point_twice(ctx):
         assert np.linalg.norm(got - want) / scale < 1e-6
         ref = Cm.astype(np.complex128) - A.astype(np.complex128) @ B.astype(np.complex128)
         assert np.linalg.norm(got - ref) / scale < 5e-5
+
+
+@pytest.mark.parametrize("m,n,k,pad", [(300, 200, 40, (5, 3, 9)), (2048, 2048, 128, (0, 0, 0)),
+                                       (129, 2048, 33, (1, 2, 3))])
+def test_noalloc_padded_partial_and_maximal_sizes(ctx, m, n, k, pad):
+    """Leading dimensions larger than the matrices, a K that is no multiple of the
+    32-wide chunk, and the largest accepted size (whose packed images fill the array)."""
+    rng = np.random.default_rng(m + n + k)
+    A, B, Cm = _cplx(rng, (m, k)), _cplx(rng, (k, n)), _cplx(rng, (m, n))
+    st, got = _noalloc(A, B, Cm, m + pad[0], k + pad[1], m + pad[2])
+    assert st == C.OK, bemgpu.api._last_error()
+    ref = Cm.astype(np.complex128) - A.astype(np.complex128) @ B.astype(np.complex128)
+    scale = np.linalg.norm(A) * np.linalg.norm(B)
+    assert np.linalg.norm(got - ref) / scale < 5e-5
+    want = ctx.debug_cgemm(A, B, Cm)
+    assert np.linalg.norm(got - want) / scale < 1e-6
 
 
 def test_noalloc_rejects_sizes_beyond_its_array():
