@@ -36,7 +36,8 @@ class Problem(ctypes.Structure):
 
 class ServerOptions(ctypes.Structure):
     _fields_ = [("max_batch", ctypes.c_int32), ("queue_limit", ctypes.c_int32),
-                ("cache_bytes", ctypes.c_uint64)]
+                ("cache_bytes", ctypes.c_uint64), ("lanes", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class ServerStats(ctypes.Structure):

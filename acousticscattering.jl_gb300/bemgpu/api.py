@@ -802,19 +802,22 @@ def pressure(sol: BEMSolution, points, *, field: str = "total", rhs: int = 0, re
 
 
 class Server:
-    """Continuous-batching request loop of libbemgpu (one worker thread per server).
+    """Continuous-batching request loop of libbemgpu.
 
     submit() queues one surface / boundary problem at several wavenumbers and incidence
     directions and returns a ticket; wait() returns the backscatter amplitudes
-    (nfreq x nangles) and the request's latency.  Requests submitted while a batch runs
-    join the next batch; factors are cached across requests (LRU)."""
+    (nfreq x nangles) and the request's latency.  ``lanes`` batches run on the device at
+    once, each on its own streams; a free lane takes waiting work of one size class, so
+    short requests overtake long ones.  Factors are cached across requests (LRU,
+    ``cache_bytes``; 0 = a quarter of the budget)."""
 
     def __init__(self, ctx: Context | None = None, max_batch: int = 64, queue_limit: int = 4096,
-                 cache_bytes: int = 0):
+                 cache_bytes: int = 0, lanes: int = 2):
         self.ctx = ctx or context()
         o = C.ServerOptions()
         C.lib().bemgpu_server_options_init(ctypes.byref(o))
         o.max_batch, o.queue_limit, o.cache_bytes = max_batch, queue_limit, cache_bytes
+        o.lanes = lanes
         h = ctypes.c_void_p()
         _check(C.lib().bemgpu_server_create(self.ctx.handle, ctypes.byref(o), ctypes.byref(h)),
                self.ctx.handle)

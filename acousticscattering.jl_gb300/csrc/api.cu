@@ -57,11 +57,22 @@ struct bemgpu_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   uint64_t budget = 0;
-  uint64_t live = 0;
+  uint64_t live = 0;   // bytes held by this context's own allocations
+  uint64_t total = 0;  // root context: bytes held by it and its lanes (against budget)
   std::string err;
   int* d_err = nullptr;
+  // free device blocks of this context, reused on its own stream(s) only (stream order
+  // makes a block released with work still queued safe to hand out again)
   std::multimap<size_t, void*> cache;
   uint64_t cached = 0;
+  std::mutex pool_mu;  // guards cache / cached
+  std::mutex acct_mu;  // root context: guards live / total of it and its lanes
+  // A lane is a child context of a serving loop: its own streams, events, timeout word
+  // and block pool, so that batches on different lanes run concurrently; its memory
+  // counts against the parent's budget.
+  bemgpu_ctx* parent = nullptr;
+  std::vector<bemgpu_ctx*> lanes;  // root: live lanes (guarded by lanes_mu)
+  std::mutex lanes_mu;
   bool prof = false;
   bool tensor_lu = true;  // complex64 trailing updates on the tensor cores
   cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -136,58 +147,206 @@ struct Buf {
     return *this;
   }
   ~Buf() { release(); }
-  void release() {
-    if (p && c) {
-      c->cache.emplace(bytes, p);
-      c->cached += bytes;
-      c->live -= bytes;
-    }
-    p = nullptr;
-    bytes = 0;
-  }
+  void release();
   template <class T>
   T* as() const {
     return static_cast<T*>(p);
   }
 };
 
+bemgpu_ctx* root_of(const bemgpu_ctx* c) {
+  return const_cast<bemgpu_ctx*>(c->parent ? c->parent : c);
+}
+
+// Bytes held against the budget by a context and all lanes of its root.
+uint64_t total_live(const bemgpu_ctx* c) {
+  bemgpu_ctx* r = root_of(c);
+  std::lock_guard<std::mutex> lk(r->acct_mu);
+  return r->total;
+}
+
+void account(bemgpu_ctx* c, int64_t delta) {
+  bemgpu_ctx* r = root_of(c);
+  std::lock_guard<std::mutex> lk(r->acct_mu);
+  r->total = (uint64_t)((int64_t)r->total + delta);
+  c->live = (uint64_t)((int64_t)c->live + delta);
+}
+
+void Buf::release() {
+  if (p && c) {
+    {
+      std::lock_guard<std::mutex> lk(c->pool_mu);
+      c->cache.emplace(bytes, p);
+      c->cached += bytes;
+    }
+    account(c, -(int64_t)bytes);
+  }
+  p = nullptr;
+  bytes = 0;
+}
+
+// Frees the free blocks of one context.  A lane's block can be released with work still
+// queued on that lane's stream, so the device is synchronised before anything is freed.
 void drop_cache(bemgpu_ctx* c) {
-  for (auto& kv : c->cache) cudaFree(kv.second);
-  c->cache.clear();
-  c->cached = 0;
+  std::multimap<size_t, void*> blocks;
+  {
+    std::lock_guard<std::mutex> lk(c->pool_mu);
+    blocks.swap(c->cache);
+    c->cached = 0;
+  }
+  if (blocks.empty()) return;
+  cudaDeviceSynchronize();
+  for (auto& kv : blocks) cudaFree(kv.second);
+}
+
+// Free blocks of the root context and every lane (when a cudaMalloc fails).
+void drop_all_caches(bemgpu_ctx* c) {
+  bemgpu_ctx* r = root_of(c);
+  drop_cache(r);
+  std::lock_guard<std::mutex> lk(r->lanes_mu);
+  for (bemgpu_ctx* l : r->lanes) drop_cache(l);
+}
+
+// Streams, ordering events and timeout word of a context or lane (device current).
+cudaError_t init_streams(bemgpu_ctx* c) {
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return e;
+  e = cudaMalloc(&c->d_err, sizeof(int));
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    c->stream = nullptr;
+    return e;
+  }
+  cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+  // look-ahead stream and events of the blocked triangular solves (optional: without them
+  // the solves run on the main stream alone)
+  if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) == cudaSuccess) {
+    c->evpool.resize(kEventPool, nullptr);
+    for (auto& ev : c->evpool)
+      if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) ev = nullptr;
+    if (std::any_of(c->evpool.begin(), c->evpool.end(), [](cudaEvent_t ev) { return !ev; })) {
+      for (auto& ev : c->evpool)
+        if (ev) cudaEventDestroy(ev);
+      c->evpool.clear();
+      cudaStreamDestroy(c->side);
+      c->side = nullptr;
+    }
+  } else {
+    c->side = nullptr;
+  }
+  cudaGetLastError();
+  return cudaStreamSynchronize(c->stream);
+}
+
+void free_streams(bemgpu_ctx* c) {
+  cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->events)
+    for (auto& pr : kv.second) {
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+  c->events.clear();
+  if (c->side) cudaStreamSynchronize(c->side);
+  drop_cache(c);
+  for (auto& ev : c->evpool) cudaEventDestroy(ev);
+  c->evpool.clear();
+  if (c->side) {
+    cudaStreamDestroy(c->side);
+    c->side = nullptr;
+  }
+  if (c->t0) cudaEventDestroy(c->t0);
+  if (c->t1) cudaEventDestroy(c->t1);
+  c->t0 = c->t1 = nullptr;
+  if (c->d_err) cudaFree(c->d_err);
+  c->d_err = nullptr;
+  cudaStreamDestroy(c->stream);
+  c->stream = nullptr;
+}
+
+// A lane of `parent` (see bemgpu_ctx::parent): settings copied, memory counted against
+// the parent's budget.
+int make_lane(bemgpu_ctx* parent, bemgpu_ctx** out) {
+  cudaSetDevice(parent->device);
+  auto* l = new bemgpu_ctx();
+  l->device = parent->device;
+  l->parent = parent;
+  l->budget = parent->budget;
+  l->tensor_lu = parent->tensor_lu;
+  l->autotune = parent->autotune;
+  l->tuned = parent->tuned;
+  cudaError_t e = init_streams(l);
+  if (e != cudaSuccess) {
+    delete l;
+    return cuda_fail(parent, e, "lane streams");
+  }
+  {
+    std::lock_guard<std::mutex> lk(parent->lanes_mu);
+    parent->lanes.push_back(l);
+  }
+  *out = l;
+  return BEMGPU_OK;
+}
+
+// Destroys a lane; every buffer allocated through it must have been released.
+void destroy_lane(bemgpu_ctx* l) {
+  bemgpu_ctx* parent = l->parent;
+  {
+    std::lock_guard<std::mutex> lk(parent->lanes_mu);
+    parent->lanes.erase(std::remove(parent->lanes.begin(), parent->lanes.end(), l),
+                        parent->lanes.end());
+  }
+  cudaSetDevice(l->device);
+  free_streams(l);
+  delete l;
 }
 
 int alloc(bemgpu_ctx* c, size_t bytes, Buf* out) {
   out->release();
   size_t rb = round_bytes(bytes);
-  if (c->live + rb > c->budget) {
-    char m[200];
-    std::snprintf(m, sizeof m, "HBM budget exceeded: %.3f GB live + %.3f GB requested > %.3f GB",
-                  c->live / 1e9, rb / 1e9, c->budget / 1e9);
-    return fail(c, BEMGPU_ENOMEM_BUDGET, m);
+  {
+    bemgpu_ctx* r = root_of(c);
+    std::lock_guard<std::mutex> lk(r->acct_mu);
+    if (r->total + rb > r->budget) {
+      char m[200];
+      std::snprintf(m, sizeof m,
+                    "HBM budget exceeded: %.3f GB live + %.3f GB requested > %.3f GB",
+                    r->total / 1e9, rb / 1e9, r->budget / 1e9);
+      return fail(c, BEMGPU_ENOMEM_BUDGET, m);
+    }
+    r->total += rb;
+    c->live += rb;
   }
-  auto it = c->cache.find(rb);
   void* p = nullptr;
-  if (it != c->cache.end()) {
-    p = it->second;
-    c->cache.erase(it);
-    c->cached -= rb;
-  } else {
+  {
+    std::lock_guard<std::mutex> lk(c->pool_mu);
+    auto it = c->cache.find(rb);
+    if (it != c->cache.end()) {
+      p = it->second;
+      c->cache.erase(it);
+      c->cached -= rb;
+    }
+  }
+  if (!p) {
     cudaError_t e = cudaMalloc(&p, rb);
-    if (e != cudaSuccess) {
+    if (e == cudaErrorMemoryAllocation) {
       cudaGetLastError();
       drop_cache(c);
       e = cudaMalloc(&p, rb);
-      if (e != cudaSuccess) {
-        cudaGetLastError();
-        return cuda_fail(c, e, "cudaMalloc");
-      }
+    }
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      drop_all_caches(c);
+      e = cudaMalloc(&p, rb);
+    }
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      account(c, -(int64_t)rb);
+      return cuda_fail(c, e, "cudaMalloc");
     }
   }
   out->c = c;
   out->p = p;
   out->bytes = rb;
-  c->live += rb;
   return BEMGPU_OK;
 }
 
@@ -2098,8 +2257,9 @@ struct ServerReq {
   std::shared_ptr<MeshData> mesh;
   bemgpu_problem prob{};
   std::vector<double> ks, inc, amps;
-  int32_t nfreq = 0, nangles = 0, next_freq = 0, done_freq = 0;
+  int32_t nfreq = 0, nangles = 0, done_freq = 0, untaken = 0;
   int status = BEMGPU_OK;
+  std::string err;  // message of a failed request
   bool finished = false;
   Clock::time_point t_submit, t_done;
 };
@@ -2117,6 +2277,7 @@ struct CacheEnt {
   std::shared_ptr<FactorData> f;
   uint64_t last = 0;
   size_t bytes = 0;
+  int lane = -1;  // the lane whose running batch uses it (one at a time), or -1
 };
 
 FKey key_of(const ServerReq& r, double k) {
@@ -2126,7 +2287,19 @@ FKey key_of(const ServerReq& r, double k) {
               r.prob.precision, r.prob.assembly};
 }
 
-// device bytes of one factor plus the solve temporaries of nangles right-hand sides
+int64_t order_of(const ServerReq& r) {
+  return r.prob.boundary == BEMGPU_FLUID ? 2 * r.mesh->n : r.mesh->n;
+}
+
+// device bytes of the solve temporaries of one item (nangles right-hand sides)
+size_t solve_bytes(const ServerReq& r) {
+  const size_t N = (size_t)order_of(r);
+  const size_t R = (size_t)r.nangles;
+  const size_t b = N * R * (16 * 6 + 8) + (size_t)kChunks * R * N * 3 * 8;
+  return b + b / 20;
+}
+
+// device bytes of one factor plus the solve temporaries of its right-hand sides
 size_t item_bytes(const ServerReq& r) {
   const size_t n = (size_t)r.mesh->n;
   const bool fl = r.prob.boundary == BEMGPU_FLUID;
@@ -2137,10 +2310,16 @@ size_t item_bytes(const ServerReq& r) {
   size_t b = N * N * (a32 ? 8 : 16) + N * N * (mixed ? 8 : 16) + (fl ? 0 : n * n * (a32 ? 8 : 16));
   b += a32 ? (size_t)r.mesh->n_near * (fl ? 4 : 2) * 16 : 0;
   b += 2 * tc_pack_bytes((int64_t)N, 128) + N * 64;
-  const size_t R = (size_t)r.nangles;
-  b += N * R * (16 * 6 + 8) + (size_t)kChunks * R * N * 3 * 8;
-  return b + b / 20;
+  return b + b / 20 + solve_bytes(r);
 }
+
+// One work item: a (request, wavenumber) pair waiting for a lane.
+struct Pending {
+  std::shared_ptr<ServerReq> req;
+  int32_t fi = 0;
+  FKey key{};
+  int64_t N = 0;
+};
 }  // namespace
 
 struct bemgpu_server {
@@ -2148,23 +2327,33 @@ struct bemgpu_server {
   bemgpu_server_options opt{};
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
-  std::deque<std::shared_ptr<ServerReq>> queue;
+  std::deque<Pending> pending;                       // items in arrival order
   std::map<int64_t, std::shared_ptr<ServerReq>> all;
   std::map<FKey, CacheEnt> cache;
-  uint64_t tick = 0, cached_bytes = 0;
+  std::map<FKey, int> factoring;                     // keys a running batch factors (lane)
+  uint64_t tick = 0, cached_bytes = 0, reserved = 0;
+  int64_t waiting = 0;                               // requests with untaken items
+  int running = 0;                                   // batches on the device
   int64_t next_id = 1;
   bemgpu_server_stats st{};
   bool stop = false;
-  std::thread worker;
+  std::vector<bemgpu_ctx*> lanes;
+  std::vector<int64_t> lane_head;                    // system order heading each lane's batch
+  std::vector<std::thread> workers;
 };
 
 namespace {
 
-void finish_req(bemgpu_server* S, ServerReq& r, int status) {
+void finish_req(bemgpu_server* S, ServerReq& r, int status, const std::string& err = "") {
   if (r.finished) return;
   r.status = status;
+  r.err = err;
   r.finished = true;
   r.t_done = Clock::now();
+  if (r.untaken > 0) {
+    r.untaken = 0;
+    S->waiting--;
+  }
   if (status == BEMGPU_OK)
     S->st.completed++;
   else
@@ -2178,9 +2367,8 @@ struct Item {
 };
 
 // One batch: factor the uncached keys, solve every item, read back backscatter.
-int run_batch(bemgpu_server* S, std::vector<Item>& items,
+int run_batch(bemgpu_ctx* c, std::vector<Item>& items,
               std::map<FKey, std::shared_ptr<FactorData>>& factors, int64_t* nfactored) {
-  bemgpu_ctx* c = S->c;
   std::vector<std::shared_ptr<FactorData>> fresh;
   std::vector<FactorData*> fs;
   for (auto& kv : factors)
@@ -2263,12 +2451,13 @@ int run_batch(bemgpu_server* S, std::vector<Item>& items,
   return BEMGPU_OK;
 }
 
-void evict_lru(bemgpu_server* S, const std::map<FKey, std::shared_ptr<FactorData>>& keep,
-               uint64_t target_cached) {
-  while (S->cached_bytes > target_cached && !S->cache.empty()) {
+// Drops least recently used cache entries that no running batch uses until the cache
+// holds at most target bytes.
+void evict_lru(bemgpu_server* S, uint64_t target) {
+  while (S->cached_bytes > target) {
     auto victim = S->cache.end();
     for (auto it = S->cache.begin(); it != S->cache.end(); ++it) {
-      if (keep.count(it->first)) continue;
+      if (it->second.lane >= 0) continue;
       if (victim == S->cache.end() || it->second.last < victim->second.last) victim = it;
     }
     if (victim == S->cache.end()) break;
@@ -2278,102 +2467,213 @@ void evict_lru(bemgpu_server* S, const std::map<FKey, std::shared_ptr<FactorData
   }
 }
 
-void server_loop(bemgpu_server* S) {
-  cudaSetDevice(S->c->device);
+// Bytes held by the lanes' allocations (cached factors and running batches).
+uint64_t lanes_live(bemgpu_server* S) {
+  bemgpu_ctx* r = S->c;
+  std::lock_guard<std::mutex> lk(r->acct_mu);
+  uint64_t b = 0;
+  for (bemgpu_ctx* l : S->lanes) b += l->live;
+  return b;
+}
+
+// A batch a lane has taken: its items, the factors they use (null = to factor here),
+// and the memory reserved for it.
+struct Batch {
+  std::vector<Item> items;
+  std::map<FKey, std::shared_ptr<FactorData>> factors;
+  std::vector<FKey> fresh, hits;
+  size_t need = 0;
+};
+
+bool same_class(int64_t a, int64_t b) { return a <= 2 * b && b <= 2 * a; }
+
+// Takes the next batch for lane `li` (S->mu held).  Items are considered in arrival
+// order; an item is takeable when its factor is neither being computed nor in use on
+// another lane.  The batch is one size class: items whose system order is within a
+// factor of two of the head's (a batch lasts as long as its largest factorisation, so
+// small systems do not wait behind large ones).  The head is the oldest takeable item,
+// unless another lane already runs that item's class and an item of another class waits:
+// then the oldest such item heads it, so that one large request cannot hold every lane
+// while small ones wait.  Items join while the batch stays within max_batch
+// factorisations and the memory the budget has left after the cache's unevictable part
+// and the other lanes' batches.  Returns false when nothing can be taken now; *fail_head
+// is set when the first item cannot fit even on an idle device with an empty cache.
+bool take_batch(bemgpu_server* S, int li, Batch* B, std::shared_ptr<ServerReq>* fail_head) {
+  bemgpu_ctx* c = S->c;
+  // items of failed requests leave the queue
+  S->pending.erase(std::remove_if(S->pending.begin(), S->pending.end(),
+                                  [](const Pending& p) { return p.req->finished; }),
+                   S->pending.end());
+  const uint64_t usable = (uint64_t)(0.92 * (double)c->budget);
+  const uint64_t total = total_live(c), lanes = lanes_live(S);
+  const uint64_t outside = total > lanes ? total - lanes : 0;
+  uint64_t evictable = 0;
+  for (auto& kv : S->cache)
+    if (kv.second.lane < 0) evictable += kv.second.bytes;
+  const uint64_t held = outside + S->cached_bytes + S->reserved;
+  const uint64_t avail = usable > held ? usable - held : 0;
+  auto takeable = [&](const Pending& p) {
+    auto ce = S->cache.find(p.key);
+    if (ce != S->cache.end()) return ce->second.lane < 0;  // else in use on another lane
+    return S->factoring.count(p.key) == 0;                 // else being factored elsewhere
+  };
+  auto busy_class = [&](int64_t N) {
+    for (size_t l = 0; l < S->lane_head.size(); ++l)
+      if ((int)l != li && S->lane_head[l] > 0 && same_class(N, S->lane_head[l])) return true;
+    return false;
+  };
+  int64_t nhead = -1, first = -1;
+  for (const Pending& p : S->pending) {
+    if (!takeable(p)) continue;
+    if (first < 0) first = p.N;
+    if (!busy_class(p.N)) {
+      nhead = p.N;
+      break;
+    }
+  }
+  if (nhead < 0) nhead = first;
+  if (nhead < 0) return false;
+  int nnew = 0;
+  bool any = false;
+  std::vector<size_t> taken;  // positions in the pending deque
+  for (size_t pos = 0; pos < S->pending.size(); ++pos) {
+    Pending& p = S->pending[pos];
+    const bool here = B->factors.count(p.key) > 0;
+    auto ce = S->cache.find(p.key);
+    const bool hit = !here && ce != S->cache.end();
+    if (!here && !takeable(p)) continue;
+    if (!same_class(p.N, nhead)) continue;
+    if (!here && !hit && nnew >= S->opt.max_batch) continue;
+    const size_t b = (here || hit) ? solve_bytes(*p.req) : item_bytes(*p.req);
+    // a hit's factor stops counting as evictable once this batch uses it
+    const uint64_t ev = evictable - (hit ? std::min<uint64_t>(evictable, ce->second.bytes) : 0);
+    if (B->need + b > avail + ev) {
+      if (!any) {
+        // the first item does not fit: on an idle device with nothing left to evict it
+        // never will
+        if (S->running == 0 && S->reserved == 0 && b > (usable > outside ? usable - outside : 0))
+          *fail_head = p.req;
+        break;
+      }
+      continue;
+    }
+    any = true;
+    B->need += b;
+    if (hit) {
+      ce->second.lane = li;
+      ce->second.last = ++S->tick;
+      evictable = ev;
+      B->factors[p.key] = ce->second.f;
+      B->hits.push_back(p.key);
+      S->st.cache_hits++;
+    } else if (!here) {
+      B->factors[p.key] = nullptr;
+      B->fresh.push_back(p.key);
+      ++nnew;
+    }
+    B->items.push_back(Item{p.req, p.fi, p.key});
+    taken.push_back(pos);
+  }
+  if (B->items.empty()) return false;
+  // make room: least recently used factors that no batch uses go first
+  if (B->need > avail) {
+    const uint64_t over = B->need - avail;
+    evict_lru(S, S->cached_bytes > over ? S->cached_bytes - over : 0);
+  }
+  for (auto& k : B->fresh) S->factoring[k] = li;
+  S->reserved += B->need;
+  S->running++;
+  S->lane_head[li] = nhead;
+  for (size_t pos : taken) {
+    ServerReq& r = *S->pending[pos].req;
+    if (--r.untaken == 0) S->waiting--;
+  }
+  for (auto t = taken.rbegin(); t != taken.rend(); ++t)
+    S->pending.erase(S->pending.begin() + (std::ptrdiff_t)*t);
+  S->st.items += (int64_t)B->items.size();
+  S->st.batches++;
+  return true;
+}
+
+void lane_loop(bemgpu_server* S, int li) {
+  bemgpu_ctx* lc = S->lanes[li];
+  cudaSetDevice(lc->device);
   for (;;) {
-    std::vector<Item> items;
-    std::map<FKey, std::shared_ptr<FactorData>> factors;  // null = to factor
+    Batch B;
     {
       std::unique_lock<std::mutex> lk(S->mu);
-      S->cv_work.wait(lk, [&] { return S->stop || !S->queue.empty(); });
-      if (S->stop) break;
-      uint64_t live = 0, budget = 0;
-      {
-        std::lock_guard<std::recursive_mutex> ck(S->c->mu);
-        live = S->c->live;
-        budget = S->c->budget;
-      }
-      // memory the batch may take: the budget minus what is live outside the cache
-      const uint64_t usable = (uint64_t)(0.92 * (double)budget);
-      const uint64_t base = live > S->cached_bytes ? live - S->cached_bytes : 0;
-      uint64_t need = 0;
-      int nnew = 0;
-      bool full = false;
-      while (!S->queue.empty() && !full) {
-        auto r = S->queue.front();
-        while (r->next_freq < r->nfreq) {
-          const FKey key = key_of(*r, r->ks[r->next_freq]);
-          const bool have = S->cache.count(key) || factors.count(key);
-          const size_t b = item_bytes(*r);
-          if (!have && (nnew >= S->opt.max_batch || base + need + b > usable)) {
-            full = true;
-            break;
-          }
-          if (!have) {
-            factors[key] = nullptr;
-            ++nnew;
-            need += b;
-          } else if (S->cache.count(key)) {
-            factors[key] = S->cache[key].f;
-            S->cache[key].last = ++S->tick;
-            S->st.cache_hits++;
-          }
-          items.push_back(Item{r, r->next_freq, key});
-          r->next_freq++;
+      for (;;) {
+        if (S->stop) return;
+        std::shared_ptr<ServerReq> fail_head;
+        if (take_batch(S, li, &B, &fail_head)) break;
+        if (fail_head) {
+          finish_req(S, *fail_head, BEMGPU_ENOMEM_BUDGET,
+                     "the request's factor does not fit the HBM budget");
+          S->cv_done.notify_all();
+          continue;
         }
-        if (r->next_freq == r->nfreq) S->queue.pop_front();
+        S->cv_work.wait(lk);
       }
-      if (items.empty()) {
-        // the oldest item alone does not fit: fail its request
-        auto r = S->queue.front();
-        S->queue.pop_front();
-        finish_req(S, *r, BEMGPU_ENOMEM_BUDGET);
-        S->cv_done.notify_all();
-        continue;
-      }
-      // make room: cached factors not used by this batch go first
-      const uint64_t room = usable > base + need ? usable - base - need : 0;
-      evict_lru(S, factors, std::min<uint64_t>(room, S->opt.cache_bytes));
-      S->st.items += (int64_t)items.size();
-      S->st.batches++;
     }
     int status;
     int64_t nfactored = 0;
+    std::string err;
     Clock::time_point t0 = Clock::now();
     {
-      std::lock_guard<std::recursive_mutex> ck(S->c->mu);
-      status = run_batch(S, items, factors, &nfactored);
+      std::lock_guard<std::recursive_mutex> ck(lc->mu);
+      status = run_batch(lc, B.items, B.factors, &nfactored);
+      if (status != BEMGPU_OK) err = lc->err;
     }
     const double ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
     {
       std::lock_guard<std::mutex> lk(S->mu);
       S->st.busy_ms += ms;
       S->st.factorizations += nfactored;
-      for (auto& it : items) {
+      S->reserved -= std::min<uint64_t>(S->reserved, B.need);
+      S->running--;
+      S->lane_head[li] = -1;
+      for (auto& k : B.fresh) S->factoring.erase(k);
+      for (auto& k : B.hits) {
+        auto it = S->cache.find(k);
+        if (it == S->cache.end()) continue;
+        if (status != BEMGPU_OK) {  // a factor a failed batch used is not trusted again
+          S->cached_bytes -= it->second.bytes;
+          S->cache.erase(it);
+          continue;
+        }
+        // a promotion during the solve can have grown the factor
+        const size_t b = it->second.f->bytes();
+        S->cached_bytes = S->cached_bytes - it->second.bytes + b;
+        it->second.bytes = b;
+        it->second.lane = -1;
+      }
+      for (auto& it : B.items) {
         ServerReq& r = *it.req;
         if (status != BEMGPU_OK) {
-          finish_req(S, r, status);
+          finish_req(S, r, status, err);
           continue;
         }
         if (++r.done_freq == r.nfreq && !r.finished) finish_req(S, r, BEMGPU_OK);
       }
       if (status == BEMGPU_OK) {
-        for (auto& kv : factors) {
-          if (S->cache.count(kv.first)) continue;
-          const size_t b = kv.second->bytes();
+        for (auto& k : B.fresh) {
+          auto& f = B.factors[k];
+          if (!f || S->cache.count(k)) continue;
+          const size_t b = f->bytes();
           if (b > S->opt.cache_bytes) continue;
-          S->cache[kv.first] = CacheEnt{kv.second, ++S->tick, b};
+          S->cache[k] = CacheEnt{f, ++S->tick, b, -1};
           S->cached_bytes += b;
         }
-        evict_lru(S, {}, S->opt.cache_bytes);
-      } else {
-        // drop the failed requests' remaining items
-        for (auto it = S->queue.begin(); it != S->queue.end();)
-          it = (*it)->finished ? S->queue.erase(it) : it + 1;
       }
+      evict_lru(S, S->opt.cache_bytes);
       S->st.cached_bytes = S->cached_bytes;
+      // the batch's factors that did not enter the cache are freed here, before the
+      // lanes that wait for memory wake up
+      B.factors.clear();
+      B.items.clear();
     }
     S->cv_done.notify_all();
+    S->cv_work.notify_all();
   }
 }
 }  // namespace
@@ -2466,38 +2766,14 @@ int bemgpu_ctx_create(int device, uint64_t hbm_budget_bytes, bemgpu_ctx** out) {
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
   auto* c = new bemgpu_ctx();
   c->device = device;
-  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-  if (e != cudaSuccess) {
-    delete c;
-    return cuda_fail(nullptr, e, "cudaStreamCreate");
-  }
   size_t fr = 0, tot = 0;
   cudaMemGetInfo(&fr, &tot);
   c->budget = hbm_budget_bytes ? hbm_budget_bytes : (uint64_t)(0.9 * (double)fr);
-  e = cudaMalloc(&c->d_err, sizeof(int));
+  e = init_streams(c);
   if (e != cudaSuccess) {
-    cudaStreamDestroy(c->stream);
     delete c;
-    return cuda_fail(nullptr, e, "cudaMalloc");
+    return cuda_fail(nullptr, e, "context streams");
   }
-  cudaMemset(c->d_err, 0, sizeof(int));
-  // look-ahead stream and events of the blocked triangular solves (optional: without them
-  // the solves run on the main stream alone)
-  if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) == cudaSuccess) {
-    c->evpool.resize(kEventPool, nullptr);
-    for (auto& ev : c->evpool)
-      if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) ev = nullptr;
-    if (std::any_of(c->evpool.begin(), c->evpool.end(), [](cudaEvent_t ev) { return !ev; })) {
-      for (auto& ev : c->evpool)
-        if (ev) cudaEventDestroy(ev);
-      c->evpool.clear();
-      cudaStreamDestroy(c->side);
-      c->side = nullptr;
-    }
-  } else {
-    c->side = nullptr;
-  }
-  cudaGetLastError();
   cudaDeviceSynchronize();
   *out = c;
   return BEMGPU_OK;
@@ -2506,22 +2782,7 @@ int bemgpu_ctx_create(int device, uint64_t hbm_budget_bytes, bemgpu_ctx** out) {
 int bemgpu_ctx_destroy(bemgpu_ctx* c) {
   if (!c) return BEMGPU_OK;
   cudaSetDevice(c->device);
-  cudaStreamSynchronize(c->stream);
-  for (auto& kv : c->events)
-    for (auto& pr : kv.second) {
-      cudaEventDestroy(pr.first);
-      cudaEventDestroy(pr.second);
-    }
-  drop_cache(c);
-  for (auto& ev : c->evpool) cudaEventDestroy(ev);
-  if (c->side) {
-    cudaStreamSynchronize(c->side);
-    cudaStreamDestroy(c->side);
-  }
-  if (c->t0) cudaEventDestroy(c->t0);
-  if (c->t1) cudaEventDestroy(c->t1);
-  cudaFree(c->d_err);
-  cudaStreamDestroy(c->stream);
+  free_streams(c);
   delete c;
   return BEMGPU_OK;
 }
@@ -2534,8 +2795,8 @@ int bemgpu_last_error(const bemgpu_ctx* c, char* buf, size_t len) {
 
 int bemgpu_ctx_memory(const bemgpu_ctx* c, uint64_t* used, uint64_t* budget) {
   if (!c) return fail(nullptr, BEMGPU_EINVAL, "null context");
-  if (used) *used = c->live;
-  if (budget) *budget = c->budget;
+  if (used) *used = total_live(c);
+  if (budget) *budget = root_of(c)->budget;
   return BEMGPU_OK;
 }
 
@@ -3204,7 +3465,8 @@ int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x,
   const size_t per = ((size_t)(R + 1) * n + 2 * (size_t)n) * 16 + (size_t)(R + 1) * R * 16 +
                      (size_t)chunks * (R + 1) * 16 + (size_t)mi * 8 + H.scratch_bytes(1) +
                      (size_t)(4 * R + 8) * 16 + (precond ? (size_t)n * 16 : 0);
-  const uint64_t avail = c->budget > c->live ? (c->budget - c->live) : 0;
+  const uint64_t used = total_live(c), budget = root_of(c)->budget;
+  const uint64_t avail = budget > used ? budget - used : 0;
   const int32_t G = (int32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)nr, avail / 2 / per));
   hist->assign((size_t)nr * mi, 0.0);
   iters->assign((size_t)nr, 0);
@@ -3965,6 +4227,8 @@ void bemgpu_server_options_init(bemgpu_server_options* o) {
   o->max_batch = 64;
   o->queue_limit = 4096;
   o->cache_bytes = 0;
+  o->lanes = 2;
+  o->reserved = 0;
 }
 
 int bemgpu_server_create(bemgpu_ctx* c, const bemgpu_server_options* opts, bemgpu_server** out) {
@@ -3976,7 +4240,20 @@ int bemgpu_server_create(bemgpu_ctx* c, const bemgpu_server_options* opts, bemgp
   if (S->opt.max_batch <= 0) S->opt.max_batch = 64;
   if (S->opt.queue_limit <= 0) S->opt.queue_limit = 4096;
   if (!S->opt.cache_bytes) S->opt.cache_bytes = c->budget / 4;
-  S->worker = std::thread(server_loop, S);
+  if (S->opt.lanes <= 0) S->opt.lanes = 2;
+  if (S->opt.lanes > 8) S->opt.lanes = 8;
+  for (int i = 0; i < S->opt.lanes; ++i) {
+    bemgpu_ctx* l = nullptr;
+    const int st = make_lane(c, &l);
+    if (st != BEMGPU_OK) {
+      for (bemgpu_ctx* x : S->lanes) destroy_lane(x);
+      delete S;
+      return st;
+    }
+    S->lanes.push_back(l);
+  }
+  S->lane_head.assign((size_t)S->opt.lanes, -1);
+  for (int i = 0; i < S->opt.lanes; ++i) S->workers.emplace_back(lane_loop, S, i);
   *out = S;
   return BEMGPU_OK;
 }
@@ -4003,19 +4280,22 @@ int bemgpu_server_submit(bemgpu_server* S, const bemgpu_mesh* mesh, const bemgpu
   r->inc.assign(incidence, incidence + 2 * nangles);
   r->nfreq = nfreq;
   r->nangles = nangles;
+  r->untaken = nfreq;
   r->amps.assign(2 * (size_t)nfreq * nangles, 0.0);
   r->t_submit = Clock::now();
   {
     std::lock_guard<std::mutex> lk(S->mu);
-    if ((int32_t)S->queue.size() >= S->opt.queue_limit)
+    if (S->waiting >= S->opt.queue_limit)
       return fail(S->c, BEMGPU_EBUSY, "request queue full");
     r->id = S->next_id++;
     S->all[r->id] = r;
-    S->queue.push_back(r);
+    const int64_t N = order_of(*r);
+    for (int32_t i = 0; i < nfreq; ++i) S->pending.push_back(Pending{r, i, key_of(*r, ks[i]), N});
+    S->waiting++;
     S->st.submitted++;
     *ticket = r->id;
   }
-  S->cv_work.notify_one();
+  S->cv_work.notify_all();
   return BEMGPU_OK;
 }
 
@@ -4035,8 +4315,9 @@ int bemgpu_server_wait(bemgpu_server* S, int64_t ticket, int32_t timeout_ms, dou
   if (latency_ms)
     *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
   const int st = r->status;
+  const std::string msg = r->err.empty() ? "request failed" : "request failed: " + r->err;
   S->all.erase(it);
-  if (st != BEMGPU_OK) return fail(S->c, st, "request failed");
+  if (st != BEMGPU_OK) return fail(S->c, st, msg);
   return BEMGPU_OK;
 }
 
@@ -4053,16 +4334,20 @@ int bemgpu_server_destroy(bemgpu_server* S) {
   {
     std::lock_guard<std::mutex> lk(S->mu);
     S->stop = true;
-    for (auto& r : S->queue) finish_req(S, *r, BEMGPU_EBUSY);
-    S->queue.clear();
+    for (auto& p : S->pending) finish_req(S, *p.req, BEMGPU_EBUSY, "server destroyed");
+    S->pending.clear();
   }
   S->cv_work.notify_all();
-  if (S->worker.joinable()) S->worker.join();
+  for (auto& w : S->workers)
+    if (w.joinable()) w.join();
   S->cv_done.notify_all();
   {
-    std::lock_guard<std::recursive_mutex> ck(S->c->mu);
-    S->cache.clear();
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->cache.clear();  // the cached factors' blocks go back to their lanes' pools
+    S->cached_bytes = 0;
   }
+  for (bemgpu_ctx* l : S->lanes) destroy_lane(l);
+  S->lanes.clear();
   delete S;
   return BEMGPU_OK;
 }

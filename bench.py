@@ -600,93 +600,143 @@ def run_config3(args):
     return line
 
 
-def run_config4(args):
-    """Open-loop Poisson request stream into the continuous-batching server: bodies from
-    the uneven distribution (panels 500..16000), 1-32 frequencies and 1-64 incidence
-    angles per request; latency = completion - arrival."""
-    import bemgpu
+def _request_stream(nreq, pool):
+    """The served request stream: each request draws one body from a pool of `pool`
+    seeded bodies of the uneven distribution (panels 500..16000), 1-32 frequencies
+    (5 % apart from the body's frequency) and 1-64 polar incidence angles."""
     from bemgpu import meshes
-    ctx = bemgpu.Context(0, hbm_budget_bytes=int(150e9))
-    nreq = args.requests
     rng = np.random.default_rng(SEED + 4)
+    bodies = [meshes.random_body(SEED + 4, i, (500, 16000)) for i in range(pool)]
     reqs = []
-    for i in range(nreq):
-        b = meshes.random_body(SEED + 4, i, (500, 16000))
-        nodes, tris = meshes.body_of_revolution(b["b"], b["aspect"], b["coeffs"], b["nlon"],
-                                                b["nrings"])
+    for _ in range(nreq):
+        bi = int(rng.integers(0, pool))
         nf = int(rng.integers(1, 33))
         na = int(rng.integers(1, 65))
-        f0 = b["frequency"]
-        freqs = f0 * (1.0 + 0.05 * np.arange(nf))
-        ang = rng.uniform(0.0, math.pi, size=na)
-        surf = bemgpu.mesh(nodes, tris)
-        surf.handle(ctx)  # meshes resident before the stream starts
-        reqs.append((b, surf, None, 2 * math.pi * freqs / 1500.0, ang))
+        freqs = bodies[bi]["frequency"] * (1.0 + 0.05 * np.arange(nf))
+        reqs.append((bi, 2 * math.pi * freqs / 1500.0, rng.uniform(0.0, math.pi, size=na)))
+    return bodies, reqs
 
-    def serve(precision, rate, subset):
-        srv = bemgpu.Server(ctx, max_batch=64, cache_bytes=int(40e9))
-        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(subset)))
-        tickets = []
-        t0 = time.perf_counter()
-        import threading as th
-        lat = {}
 
-        def waiter():
-            for tk, i in tickets_q:
-                out, ms = srv.wait(tk, timeout_ms=-1)
-                lat[i] = (ms, out)
-        tickets_q = []
+def _serve(srv_factory, surfs, bodies, reqs, subset, rate, seed):
+    """Open-loop Poisson arrivals at `rate` requests/s into a fresh server; latency =
+    completion - submission, measured by the library."""
+    import queue
+    import threading as th
+
+    import bemgpu
+    srv = srv_factory()
+    arrivals = np.cumsum(np.random.default_rng(seed).exponential(1.0 / rate, size=len(subset)))
+    tickets = queue.Queue()
+    lat, errors = {}, []
+
+    def waiter():
+        while True:
+            item = tickets.get()
+            if item is None:
+                return
+            tk, i = item
+            try:
+                lat[i] = srv.wait(tk, timeout_ms=-1)
+            except Exception as e:  # noqa: BLE001 - reported in the result line
+                errors.append(f"request {i}: {e}")
+    wt = th.Thread(target=waiter)
+    t0 = time.perf_counter()
+    wt.start()
+    try:
         for j, i in enumerate(subset):
             now = time.perf_counter() - t0
             if arrivals[j] > now:
                 time.sleep(arrivals[j] - now)
-            b, surf, _, ks, ang = reqs[i]
-            bc = bemgpu.Rigid() if b["boundary"] == "rigid" else bemgpu.PressureRelease()
-            tk = srv.submit(surf, bc, ks, ang, precision=precision)
-            tickets_q.append((tk, i))
-        wt = th.Thread(target=waiter)
-        wt.start()
+            bi, ks, ang = reqs[i]
+            bc = bemgpu.Rigid() if bodies[bi]["boundary"] == "rigid" else bemgpu.PressureRelease()
+            tickets.put((srv.submit(surfs[bi], bc, ks, ang, precision=srv.precision), i))
+    finally:
+        tickets.put(None)
         wt.join()
-        wall = time.perf_counter() - t0
-        st = srv.stats()
-        srv.close()
-        lats = np.array([lat[i][0] for i in subset])
-        solves = sum(len(reqs[i][3]) * len(reqs[i][4]) for i in subset)
-        return dict(wall_s=wall, solves=solves, solves_per_s=solves / wall,
-                    p50_ms=float(np.percentile(lats, 50)), p99_ms=float(np.percentile(lats, 99)),
-                    stats=st), {i: lat[i][1] for i in subset}
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    if errors:
+        raise RuntimeError(f"{len(errors)} requests failed; first: {errors[0]}")
+    lats = np.array([lat[i][1] for i in subset])
+    solves = sum(len(reqs[i][1]) * len(reqs[i][2]) for i in subset)
+    return dict(wall_s=wall, requests=len(subset), solves=solves, solves_per_s=solves / wall,
+                rate_per_s=rate, p50_ms=float(np.percentile(lats, 50)),
+                p99_ms=float(np.percentile(lats, 99)), max_ms=float(lats.max()),
+                stats=st), {i: lat[i][0] for i in subset}
 
-    # offered load: 70% of the closed-loop capacity measured on a random quarter of the
-    # requests (all submitted at once)
-    warm = sorted(int(i) for i in rng.choice(nreq, size=max(1, nreq // 4), replace=False))
-    res_w, _ = serve("mixed", 1e6, warm)
-    per_req = res_w["wall_s"] / len(warm)
-    rate = args.rate or 0.7 / max(per_req, 1e-3)
+
+def run_config4(args):
+    """Open-loop Poisson request stream into the continuous-batching server: 10^4
+    requests (bodies of revolution, 500-16000 panels, 1-32 frequencies, 1-64 incidence
+    angles), HBM budget 150 GB, offered at 70 % of the capacity measured closed-loop on
+    the first 2 % of the requests.  The same stream's first --fp64-requests requests are
+    then served in FP64 (at 70 % of the FP64 capacity measured closed-loop on them, which
+    is far lower: the GB300's FP64 rate bounds its LU) and in mixed precision at that same
+    rate, for the latency and the TS error of mixed against FP64 on identical requests."""
+    import bemgpu
+    ctx = bemgpu.Context(0, hbm_budget_bytes=int(150e9))
+    bodies, reqs = _request_stream(args.requests, args.pool)
+    surfs = []
+    for b in bodies:
+        nodes, tris = bemgpu.meshes.body_of_revolution(b["b"], b["aspect"], b["coeffs"],
+                                                       b["nlon"], b["nrings"])
+        s_ = bemgpu.mesh(nodes, tris)
+        s_.handle(ctx)  # meshes resident before the stream starts
+        surfs.append(s_)
+
+    def factory(precision):
+        def make():
+            srv = bemgpu.Server(ctx, max_batch=64, cache_bytes=int(40e9), lanes=args.lanes)
+            srv.precision = precision
+            return srv
+        return make
+
+    def capacity(precision, subset):
+        res, out = _serve(factory(precision), surfs, bodies, reqs, subset, 1e6, SEED + 40)
+        return res["requests"] / res["wall_s"], out
+
+    warm = list(range(min(len(reqs), max(32, args.requests // 50))))
+    cap_m, _ = capacity("mixed", warm)
+    rate = args.rate or 0.7 * cap_m
     clocks = Clocks(0)
     clocks.start()
-    res_m, out_m = serve("mixed", rate, list(range(nreq)))
+    l0 = bemgpu.Context.launch_count()
+    res_m, out_m = _serve(factory("mixed"), surfs, bodies, reqs, list(range(len(reqs))), rate,
+                          SEED + 41)
+    launches = bemgpu.Context.launch_count() - l0
     clk = clocks.stop()
-    # FP64 arm on the six smallest requests (panels x frequencies): the FP64 LU runs at
-    # the GB300's FP64 rate, far below its tensor-core throughput
-    cost = [reqs[i][1].n_panels ** 3 * len(reqs[i][3]) for i in range(nreq)]
-    sub = [int(i) for i in np.argsort(cost)[:6]]
-    res_d, out_d = serve("double", 1e6, sub)
-    err = []
-    for i in sub:
-        a, b2 = out_m[i], out_d[i]
-        err.append(float(np.max(np.abs(20 * np.log10(np.abs(a)) - 20 * np.log10(np.abs(b2))))))
+    # FP64 and mixed on the same first requests, at 70 % of the FP64 capacity
+    sub = list(range(min(len(reqs), args.fp64_requests)))
+    cap_d, _ = capacity("double", sub)
+    rate_d = 0.7 * cap_d
+    res_d, out_d = _serve(factory("double"), surfs, bodies, reqs, sub, rate_d, SEED + 42)
+    res_ms, out_ms = _serve(factory("mixed"), surfs, bodies, reqs, sub, rate_d, SEED + 42)
+    err = [float(np.max(np.abs(20 * np.log10(np.abs(out_ms[i])) -
+                               20 * np.log10(np.abs(out_d[i]))))) for i in sub]
+    same = all(np.array_equal(out_ms[i], out_m[i]) for i in sub)
     line = _base_line(
         "BEM solves/s & p99 latency, served Poisson stream", res_m["solves_per_s"], "solves/s",
         res_m["wall_s"] * 1e3, args,
-        {"workload": f"{nreq} Poisson requests, bodies of revolution 500-16000 panels, 1-32 "
-                     "frequencies, 1-64 angles, continuous batching with a factor cache",
-         "requests": nreq, "rate_per_s": rate, "seed": SEED + 4},
+        {"workload": f"{len(reqs)} Poisson requests over {args.pool} seeded bodies of "
+                     "revolution (500-16000 panels), 1-32 frequencies, 1-64 angles, HBM "
+                     "budget 150 GB, continuous batching on "
+                     f"{args.lanes} lanes with a factor cache", "requests": len(reqs),
+         "pool": args.pool, "seed": SEED + 4, "lanes": args.lanes},
         dtype="c64 factor + fp64 refinement",
-        latency_ms={"p50": res_m["p50_ms"], "p99": res_m["p99_ms"]},
+        latency_ms={"p50": res_m["p50_ms"], "p99": res_m["p99_ms"], "max": res_m["max_ms"]},
+        offered_rate_per_s=rate, closed_loop_capacity_per_s=cap_m,
         server=res_m["stats"],
-        fp64_closed_loop={"requests": len(sub), "solves_per_s": res_d["solves_per_s"],
-                          "p50_ms": res_d["p50_ms"], "p99_ms": res_d["p99_ms"]},
-        ts_error_db={"max": max(err), "requests": len(sub)}, clocks=clk)
+        fp64_same_stream={"requests": len(sub), "rate_per_s": rate_d,
+                          "fp64": {k2: v for k2, v in res_d.items() if k2 != "stats"},
+                          "mixed": {k2: v for k2, v in res_ms.items() if k2 != "stats"},
+                          "solves_per_s_ratio_mixed_over_fp64":
+                              res_ms["solves_per_s"] / res_d["solves_per_s"],
+                          "closed_loop_capacity_ratio": cap_m / cap_d},
+        ts_error_db={"max": max(err), "requests": len(sub),
+                     "vs": "the same requests served in FP64"},
+        same_bits_in_two_different_streams=same,
+        clocks=clk, gpu_launches=int(launches))
     print(json.dumps(line))
     return line
 
@@ -937,7 +987,11 @@ def main():
                          "sphere; 2 large single solve x 181 angles; 3 uneven batch; 4 serving; "
                          "5 compressed operators + GMRES (the reference's default rigid path)")
     ap.add_argument("--bodies", type=int, default=256, help="config 3: bodies")
-    ap.add_argument("--requests", type=int, default=200, help="config 4: requests")
+    ap.add_argument("--requests", type=int, default=10000, help="config 4: requests")
+    ap.add_argument("--pool", type=int, default=512, help="config 4: distinct bodies")
+    ap.add_argument("--lanes", type=int, default=2, help="config 4: server lanes")
+    ap.add_argument("--fp64-requests", type=int, default=16,
+                    help="config 4: requests of the stream also served in FP64")
     ap.add_argument("--rate", type=float, default=0.0, help="config 4: arrivals/s (0: 70%% load)")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -376,17 +376,22 @@ int bemgpu_solution_destroy(bemgpu_solution *sol);
 
 /* ------------------------------------------------------------------ serving */
 /*
- * Request loop over one context (a worker thread inside the library).  A request is one
- * surface and boundary problem at nfreq wavenumbers and nangles incidence directions;
- * each (request, wavenumber) is one work item.  Continuous batching: the worker
- * repeatedly takes every pending item that fits the HBM budget (oldest first, at most
- * max_batch factorisations per batch), factors the ones whose (mesh, k, boundary,
- * precision) factor is not cached, solves all of them in one batched launch sequence
- * and completes the requests whose items are all done; requests submitted while a
- * batch runs join the next one.  Factors stay cached (LRU, cache_bytes) for reuse by
+ * Request loop over one context.  A request is one surface and boundary problem at nfreq
+ * wavenumbers and nangles incidence directions; each (request, wavenumber) is one work
+ * item.  Continuous batching over `lanes` worker threads, each with its own CUDA streams,
+ * so that several batches are on the device at once: whenever a lane is free it takes a
+ * batch of one size class (items whose system order is within a factor of two of the
+ * head item's; the head is the oldest waiting item, or the oldest of another class when
+ * another lane already runs that class, so a small request overtakes a large one), at
+ * most max_batch factorisations, within the HBM budget left by the other lanes' batches
+ * and the cache; it factors the items whose (mesh, k, boundary, precision) factor is not
+ * cached, solves all of them in one batched launch sequence and completes the requests
+ * whose items are all done.  Requests that arrive while batches run are admitted as soon
+ * as a lane and memory free up.  Factors stay cached (LRU, cache_bytes) for reuse by
  * later requests on the same mesh and wavenumber (sweeps.jl:680-701 reuses a factor
- * across angles within one call).  Every item is computed exactly as alone: batching
- * changes which launch carries it, not its arithmetic.
+ * across angles within one call); a factor is computed once and used by one lane at a
+ * time.  Every item is computed exactly as alone: batching changes which launch carries
+ * it, not its arithmetic.
  */
 typedef struct bemgpu_server bemgpu_server;
 
@@ -394,6 +399,8 @@ typedef struct {
   int32_t max_batch;     /* factorisations per batch (default 64) */
   int32_t queue_limit;   /* pending requests before submit returns BEMGPU_EBUSY (4096) */
   uint64_t cache_bytes;  /* bytes of cached factors kept between batches (default budget/4) */
+  int32_t lanes;         /* batches on the device at once, each on its own streams (2; 1..8) */
+  int32_t reserved;
 } bemgpu_server_options;
 
 typedef struct {

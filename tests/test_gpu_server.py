@@ -96,3 +96,36 @@ def test_server_many_requests_complete(ctx):
         assert st["completed"] == 12 and st["batches"] >= 2
     finally:
         srv.close()
+
+
+def test_small_request_overtakes_a_large_one(ctx):
+    """Two lanes: a small request submitted just after a large one is taken by the free
+    lane, completes first, and gives the same bits as when it runs alone."""
+    import time
+
+    small = (bemgpu.mesh(*meshes.icosphere(0.01, 2)), bemgpu.Rigid(), [320.0], [0.4, 1.3])
+    big_mesh = bemgpu.mesh(*meshes.uv_spheroid(0.05, 0.0125, 96, 40))   # 7680 panels
+    big = (big_mesh, bemgpu.Rigid(), [200.0, 230.0, 260.0, 290.0], [0.2])
+    srv = bemgpu.Server(ctx, lanes=2)
+    try:
+        alone = srv.wait(srv.submit(*small, precision="mixed"))[0]
+    finally:
+        srv.close()
+    srv = bemgpu.Server(ctx, lanes=2)
+    try:
+        t0 = time.perf_counter()
+        tb = srv.submit(*big, precision="mixed")
+        tb_sub = time.perf_counter() - t0
+        ts = srv.submit(*small, precision="mixed")
+        ts_sub = time.perf_counter() - t0
+        out_s, lat_s = srv.wait(ts)
+        out_b, lat_b = srv.wait(tb)
+        st = srv.stats()
+    finally:
+        srv.close()
+    done_small = ts_sub * 1e3 + lat_s
+    done_big = tb_sub * 1e3 + lat_b
+    assert done_small < done_big, (done_small, done_big)
+    assert np.array_equal(out_s, alone)
+    assert np.all(np.isfinite(out_b))
+    assert st["batches"] >= 2 and st["cache_hits"] == 0, st
