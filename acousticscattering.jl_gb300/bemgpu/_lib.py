@@ -31,7 +31,7 @@ class Problem(ctypes.Structure):
                 ("refine_tolerance", ctypes.c_double), ("refine_maxiter", ctypes.c_int32),
                 ("assembly", ctypes.c_int32), ("condition_guard", ctypes.c_double),
                 ("near_eta", ctypes.c_double), ("discretization", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("condition_limit", ctypes.c_int32), ("norm_floor", ctypes.c_double)]
 
 
 class ServerOptions(ctypes.Structure):
@@ -64,7 +64,10 @@ class Diagnostics(ctypes.Structure):
                 ("assemble_ms", ctypes.c_double), ("factor_ms", ctypes.c_double),
                 ("solve_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
                 ("device_bytes", ctypes.c_int64), ("nrhs", ctypes.c_int32),
-                ("info", ctypes.c_int32)]
+                ("info", ctypes.c_int32), ("condition_number", ctypes.c_double),
+                ("scaled_condition_number", ctypes.c_double), ("conditioning", ctypes.c_int32),
+                ("condition_limit", ctypes.c_int32), ("derivative_exterior", ctypes.c_int32),
+                ("derivative_interior", ctypes.c_int32)]
 
 
 class HmatrixOptions(ctypes.Structure):
@@ -165,6 +168,8 @@ SIGNATURES = {
     "bemgpu_cgemm_update_noalloc": (ctypes.c_int, [_vp, _i64, _i64, _i32, _vp, _i64, _vp, _i64,
                                                    _vp, _i64]),
     "bemgpu_ctx_set_tensor_lu": (ctypes.c_int, [_vp, _i32]),
+    "bemgpu_ctx_set_graphs": (ctypes.c_int, [_vp, _i32]),
+    "bemgpu_ctx_graph_stats": (ctypes.c_int, [_vp, _i64p, _i64p]),
     "bemgpu_debug_cgemm": (ctypes.c_int, [_vp, _i64, _i64, _i32,
                                           ctypes.POINTER(ctypes.c_float),
                                           ctypes.POINTER(ctypes.c_float),

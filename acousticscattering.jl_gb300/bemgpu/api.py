@@ -136,6 +136,17 @@ class Context:
                                            ctypes.byref(ms)), self.handle)
         return n.value, ms.value
 
+    def set_graphs(self, enable: bool = True):
+        """Capture and replay the batched LU's launch sequence as CUDA graphs (default on)."""
+        _check(C.lib().bemgpu_ctx_set_graphs(self.handle, int(bool(enable))), self.handle)
+
+    def graph_stats(self) -> dict:
+        """Batched-LU graphs captured and replayed so far."""
+        cap, rep = ctypes.c_int64(), ctypes.c_int64()
+        _check(C.lib().bemgpu_ctx_graph_stats(self.handle, ctypes.byref(cap), ctypes.byref(rep)),
+               self.handle)
+        return {"captures": cap.value, "replays": rep.value}
+
     def set_tensor_lu(self, enable: bool):
         """Complex64 LU trailing updates on the tensor cores (default) or CUDA cores."""
         _check(C.lib().bemgpu_ctx_set_tensor_lu(self.handle, int(enable)), self.handle)
@@ -258,7 +269,8 @@ def mesh(nodes, triangles, *, units: str = "m") -> Mesh:
 # ------------------------------------------------------------------ problems
 def _problem(boundary, k, formulation=None, precision="double", equilibrate=True,
              refinement=None, near_eta=2.0, assembly=None,
-             discretization="collocation") -> C.Problem:
+             discretization="collocation", condition_limit=512,
+             norm_floor=0.0) -> C.Problem:
     if not isinstance(boundary, AbstractBoundaryCondition):
         raise ArgumentError("boundary must be Rigid(), PressureRelease() or FluidFilled(g, h)")
     if discretization not in C.DISCRETIZATION:
@@ -283,6 +295,13 @@ def _problem(boundary, k, formulation=None, precision="double", equilibrate=True
         raise ArgumentError("k must be finite and positive")
     if precision == "mixed" and not equilibrate:
         raise ArgumentError("mixed precision requires equilibrate=true")
+    if not isinstance(condition_limit, (int, np.integer)) or condition_limit < 0:
+        raise ArgumentError("condition_limit must be nonnegative")
+    norm_floor = float(norm_floor)
+    if not (math.isfinite(norm_floor) and norm_floor >= 0):
+        raise ArgumentError("norm_floor must be finite and nonnegative")
+    if precision == "mixed" and norm_floor != 0.0:
+        raise ArgumentError("mixed precision does not support norm_floor")
     tol = refinement.get("tolerance", 1e-13)
     if not (math.isfinite(tol) and 0 < tol < 1):
         raise ArgumentError("invalid refinement tolerance")
@@ -314,6 +333,8 @@ def _problem(boundary, k, formulation=None, precision="double", equilibrate=True
     p.near_eta = float(near_eta)
     p.assembly = C.ASSEMBLY[assembly]
     p.discretization = C.DISCRETIZATION[discretization]
+    p.condition_limit = int(condition_limit)
+    p.norm_floor = norm_floor
     return p
 
 
@@ -336,6 +357,18 @@ def _diag_dict(d: C.Diagnostics, extra=None) -> dict:
     out["coupling"] = complex(d.coupling_re, d.coupling_im)
     out["method"] = "mixed_refinement" if d.precision == C.MIXED else "direct"
     out["equilibrate"] = bool(d.equilibrate)
+    # the reference's factor diagnostics (solvers/bem/full.jl:364-409, 330-341)
+    svd = d.conditioning == 1
+    out["conditioning"] = "svd" if svd else "not_computed"
+    out["condition_number"] = d.condition_number if svd else None
+    out["scaled_condition_number"] = d.scaled_condition_number if svd else None
+    names = {0: "not_used", 1: "direct"}
+    fluid_muller = out["formulation"] == "muller"
+    out["derivative_evaluation"] = ({"exterior": names[d.derivative_exterior],
+                                     "interior": names[d.derivative_interior]}
+                                    if fluid_muller else None)
+    for f_ in ("derivative_exterior", "derivative_interior"):
+        out.pop(f_)
     if extra:
         out.update(extra)
     return out
@@ -613,7 +646,8 @@ def hmatrix_apply(surface: Mesh, boundary, k, X, *, op=0, formulation=None, tol=
 def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_azimuth=0.0,
         formulation=None, precision="double", equilibrate=True, refinement=None,
         assembly=None, ctx: Context | None = None, parents=None, compression=None,
-        gmres_kwargs=None, discretization="collocation", **unsupported) -> BEMSolution:
+        gmres_kwargs=None, discretization="collocation", condition_limit=512, norm_floor=0.0,
+        **unsupported) -> BEMSolution:
     """Full-3D BEM on a supplied surface (solvers/bem/surface.jl:10-23), or, given lists of
     surfaces and FluidFilled materials, the coupled fluid regions of
     bem(surfaces, materials, k; parents) (solvers/bem/regions.jl:132-150).
@@ -630,7 +664,12 @@ def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_az
     quadrature nodes of every panel with the density-interpolation correction of the
     reference's Nyström operators (full.jl:68-128 and 289-346, correction=(method=:dim,));
     traces then hold one value per node, and pressure() recovers the nearest element by
-    the same correction (the reference's exclude_nearest evaluation)."""
+    the same correction (the reference's exclude_nearest evaluation).
+
+    condition_limit and norm_floor are the reference's factor options (full.jl:364-409):
+    systems of order at most condition_limit report SVD condition numbers in
+    diagnostics(); norm_floor bounds the equilibration's scales from below (double
+    precision only)."""
     if unsupported:
         raise ArgumentError(f"unsupported option(s): {sorted(unsupported)}")
     if discretization not in C.DISCRETIZATION:
@@ -665,7 +704,8 @@ def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_az
         raise ArgumentError("k must be finite and positive")
     f = Factor(surface, boundary, k, ctx=ctx, formulation=formulation, precision=precision,
                equilibrate=equilibrate, refinement=refinement, assembly=assembly,
-               discretization=discretization)
+               discretization=discretization, condition_limit=condition_limit,
+               norm_floor=norm_floor)
     try:
         return f.solve([incidence_angle], [incidence_azimuth])
     finally:
@@ -877,7 +917,8 @@ class SweepResult:
 def incidence_angle_sweep(surface: Mesh, boundary, k, angles, *, incidence_azimuth=0.0,
                           formulation=None, precision="double", equilibrate=True,
                           refinement=None, assembly=None, ctx=None, compression=None,
-                          gmres_kwargs=None, discretization="collocation") -> SweepResult:
+                          gmres_kwargs=None, discretization="collocation", condition_limit=512,
+                          norm_floor=0.0) -> SweepResult:
     """Backscatter at many polar incidence angles from one factorisation
     (postprocessing/sweeps.jl:626-701): assembled and factored once, all angles
     solved as one multi-right-hand-side batch.  With compression=(method=:hmatrix, ...)
@@ -900,7 +941,8 @@ def incidence_angle_sweep(surface: Mesh, boundary, k, angles, *, incidence_azimu
         return SweepResult(angles, amps, 20 * np.log10(np.abs(amps)), diag)
     f = Factor(surface, boundary, k, ctx=ctx, formulation=formulation, precision=precision,
                equilibrate=equilibrate, refinement=refinement, assembly=assembly,
-               discretization=discretization)
+               discretization=discretization, condition_limit=condition_limit,
+               norm_floor=norm_floor)
     try:
         sol = f.solve(angles, incidence_azimuth)
         amps = np.array([scattering_amplitude(sol, rhs=r) for r in range(len(angles))])

@@ -27,6 +27,7 @@
 #include "linalg.cuh"
 #include "nystrom.cuh"
 #include "refine.cuh"
+#include "condition.cuh"
 #include "gemm_tc.cuh"
 #include "hmatrix.cuh"
 #include "hmatrix_plan.h"
@@ -80,6 +81,14 @@ struct bemgpu_ctx {
   // launch-shape autotuner: the fastest measured choice per (kernel family, shape class)
   std::map<std::string, int> tuned;
   bool autotune = true;
+
+  // CUDA graphs of the tensor-core LU's launch sequence, one per exact batch shape
+  // (getrf_tc); a shape is captured the second time it is met
+  bool graphs = true;
+  std::map<std::string, std::shared_ptr<struct LuGraph>> lu_graphs;
+  std::map<std::string, int> lu_seen;
+  uint64_t lu_tick = 0;
+  int64_t lu_captures = 0, lu_replays = 0;
 
   std::recursive_mutex mu;
   cudaStream_t side = nullptr;           // look-ahead stream of the triangular solves
@@ -240,6 +249,7 @@ cudaError_t init_streams(bemgpu_ctx* c) {
 
 void free_streams(bemgpu_ctx* c) {
   cudaStreamSynchronize(c->stream);
+  c->lu_graphs.clear();  // their descriptor buffers go back to the pool first
   for (auto& kv : c->events)
     for (auto& pr : kv.second) {
       cudaEventDestroy(pr.first);
@@ -274,6 +284,7 @@ int make_lane(bemgpu_ctx* parent, bemgpu_ctx** out) {
   l->tensor_lu = parent->tensor_lu;
   l->autotune = parent->autotune;
   l->tuned = parent->tuned;
+  l->graphs = parent->graphs;
   cudaError_t e = init_streams(l);
   if (e != cudaSuccess) {
     delete l;
@@ -728,6 +739,9 @@ struct FactorData {
   std::shared_ptr<MeshData> base_mesh;  // Nyström: the panel mesh of the node set
   int reason = BEMGPU_REASON_NONE;
   double rcond = NAN;
+  // systems of order <= condition_limit: a copy of A and its scales, whose SVD condition
+  // numbers are computed on the first diagnostics read (shared with the solutions)
+  std::shared_ptr<struct CondState> cond;
   double matrix_norm = 0.0, anorm = 0.0;
   int32_t info_h = 0;
   double assemble_ms = 0.0, factor_ms = 0.0;
@@ -749,6 +763,7 @@ struct bemgpu_factor {
 namespace {
 struct SolutionData {
   bemgpu_ctx* c = nullptr;
+  std::shared_ptr<struct CondState> cond;  // the factor's conditioning data (see FactorData)
   std::shared_ptr<MeshData> mesh;
   int boundary = 0;
   double k = 0.0, g = 1.0, h = 1.0;
@@ -787,6 +802,12 @@ int check_problem(bemgpu_ctx* c, const bemgpu_problem& p, int* kind) {
     if (!(std::isfinite(p.condition_guard) && p.condition_guard >= 0))
       return fail(c, BEMGPU_EINVAL, "invalid condition guard");
   }
+  if (p.condition_limit < 0)
+    return fail(c, BEMGPU_EINVAL, "condition_limit must be nonnegative");
+  if (!(std::isfinite(p.norm_floor) && p.norm_floor >= 0))
+    return fail(c, BEMGPU_EINVAL, "norm_floor must be finite and nonnegative");
+  if (p.precision == BEMGPU_MIXED && p.norm_floor != 0.0)
+    return fail(c, BEMGPU_EINVAL, "mixed precision does not support norm_floor");
   if (p.assembly < BEMGPU_ASSEMBLY_DEFAULT || p.assembly > BEMGPU_ASSEMBLY_SINGLE)
     return fail(c, BEMGPU_EINVAL, "assembly must be :default, :double or :single");
   if (!(std::isfinite(p.near_eta) && p.near_eta > 0))
@@ -1177,10 +1198,31 @@ int estimate_rcond(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
 //   factor half 1; interchanges of both halves on the columns outside [K0, K0 + 256)
 //   P3: U12top = L11a^{-1} A12top            P4: A12bot -= Lmid U12top
 //   P5: U12bot = L11b^{-1} A12bot            P6: A22 -= L21 U12 (K = kk0 + kk1)
+}  // namespace
+
+// A captured launch sequence of the tensor-core LU for one exact batch shape, with the
+// descriptor arrays its kernels take as arguments (rewritten before every replay).
+struct LuGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  Buf dm, dpack, dgem, dipack, digem, d_p0, d_p1;
+  uint64_t last = 0;
+  long long kernels = 0;  // kernel launches in the graph
+  LuGraph() = default;
+  LuGraph(const LuGraph&) = delete;
+  LuGraph& operator=(const LuGraph&) = delete;
+  ~LuGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+};
+
+namespace {
+constexpr size_t kLuGraphs = 16;  // captured shapes kept per context (least recently used go)
+
 int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatInst>& mi,
              Buf& d, int64_t nmax) {
   const Launch L = c->launch();
-  const MatInst* dm = d.as<MatInst>();
   const int ni = (int)fs.size();
   constexpr int HB = kTcPanel;       // half width (128)
   constexpr int SB = 2 * kTcPanel;   // outer step (256)
@@ -1360,26 +1402,81 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
           }
         }
       }
+  // Every launch's grid and arguments follow from the batch shape (the orders of the
+  // instances, the epilogue kind, profiling) and the descriptor arrays' addresses.  The
+  // sequence is captured in a CUDA graph the second time a shape is met and replayed
+  // from then on, with the descriptors of the new batch written into the graph's arrays.
+  // (Not while profiling: the per-family event timing reads events around each group of
+  // launches, which a replayed graph does not give back.)
+  std::shared_ptr<LuGraph> G;
+  bool capture = false;
+  if (c->graphs && !c->prof) {
+    std::string key = std::to_string(ni) + (red ? "r" : "s");
+    for (const MatInst& m : mi) key += "/" + std::to_string(m.n) + ":" + std::to_string(m.lda);
+    auto it = c->lu_graphs.find(key);
+    if (it != c->lu_graphs.end()) {
+      G = it->second;
+    } else if (++c->lu_seen[key] >= 2) {
+      if (c->lu_graphs.size() >= kLuGraphs) {  // make room: least recently used shape
+        auto victim = c->lu_graphs.begin();
+        for (auto jt = c->lu_graphs.begin(); jt != c->lu_graphs.end(); ++jt)
+          if (jt->second->last < victim->second->last) victim = jt;
+        c->lu_graphs.erase(victim);
+      }
+      G = std::make_shared<LuGraph>();
+      c->lu_graphs[key] = G;
+      capture = true;
+    }
+    if (G) G->last = ++c->lu_tick;
+  }
   Buf dpack, dgem, dipack, digem;
-  TRY(to_device(c, packs, &dpack));
-  TRY(to_device(c, gems, &dgem));
-  TRY(to_device(c, ipacks, &dipack));
-  TRY(to_device(c, igems, &digem));
+  Buf* bm = nullptr;  // the MatInst array the launches take
+  if (G) {
+    auto put = [&](auto& host, Buf* b) -> int {
+      using T = typename std::decay_t<decltype(host)>::value_type;
+      const size_t bytes = host.size() * sizeof(T);
+      if (!b->p) TRY(alloc(c, std::max<size_t>(bytes, 1), b));
+      if (bytes)
+        CUDA_TRY(c, cudaMemcpyAsync(b->p, host.data(), bytes, cudaMemcpyHostToDevice, c->stream));
+      return BEMGPU_OK;
+    };
+    TRY(put(mi, &G->dm));
+    TRY(put(packs, &G->dpack));
+    TRY(put(gems, &G->dgem));
+    TRY(put(ipacks, &G->dipack));
+    TRY(put(igems, &G->digem));
+    TRY(put(p0, &G->d_p0));
+    TRY(put(p1, &G->d_p1));
+    bm = &G->dm;
+  } else {
+    TRY(to_device(c, packs, &dpack));
+    TRY(to_device(c, gems, &dgem));
+    TRY(to_device(c, ipacks, &dipack));
+    TRY(to_device(c, igems, &digem));
+    bm = &d;
+  }
+  const MatInst* dm = bm->as<MatInst>();
+  Buf& Dpack = G ? G->dpack : dpack;
+  Buf& Dgem = G ? G->dgem : dgem;
+  Buf& Dipack = G ? G->dipack : dipack;
+  Buf& Digem = G ? G->digem : digem;
+  Buf& Dp0 = G ? G->d_p0 : d_p0;
+  Buf& Dp1 = G ? G->d_p1 : d_p1;
   auto pack = [&](int64_t st, int ph) {
     const size_t q = (size_t)st * kNPack + ph;
     if (prow[q] > 0)
-      launch_tc_pack(L, dpack.as<TcPackInst>() + q * ni, ni, prow[q], pkk[q]);
+      launch_tc_pack(L, Dpack.as<TcPackInst>() + q * ni, ni, prow[q], pkk[q]);
   };
   // phases ph and ph + 1 in one launch (2 ni instances)
   auto pack2 = [&](int64_t st, int ph) {
     const size_t q = (size_t)st * kNPack + ph;
     const int64_t rows = std::max(prow[q], prow[q + 1]);
     const int kk = std::max(pkk[q], pkk[q + 1]);
-    if (rows > 0) launch_tc_pack(L, dpack.as<TcPackInst>() + q * ni, 2 * ni, rows, kk);
+    if (rows > 0) launch_tc_pack(L, Dpack.as<TcPackInst>() + q * ni, 2 * ni, rows, kk);
   };
   auto gemm = [&](int64_t st, int ph) {
     const size_t q = (size_t)st * kNGem + ph;
-    if (tiles[q] > 0) launch_tc_cgemm(L, dgem.as<TcGemmInst>() + q * ni, ni, tiles[q], red);
+    if (tiles[q] > 0) launch_tc_cgemm(L, Dgem.as<TcGemmInst>() + q * ni, ni, tiles[q], red);
   };
   auto any = [&](int64_t st, int ph) { return tiles[(size_t)st * kNGem + ph] > 0; };
   auto factor_half = [&](int64_t H) {
@@ -1407,9 +1504,9 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
         if (itiles[idx] > 0) {
           Prof pr(c, "gemm_panel");
           if (red) {  // tensor cores, reduction epilogue
-            launch_tc_pack(L, dipack.as<TcPackInst>() + idx * 2 * ni, 2 * ni, irows[idx],
+            launch_tc_pack(L, Dipack.as<TcPackInst>() + idx * 2 * ni, 2 * ni, irows[idx],
                            kPanelNB);
-            launch_tc_cgemm(L, digem.as<TcGemmInst>() + idx * ni, ni, itiles[idx], true);
+            launch_tc_cgemm(L, Digem.as<TcGemmInst>() + idx * ni, ni, itiles[idx], true);
           } else {
             launch_gemm_update(L, dm, ni, k0, kPanelNB, nmax, k0 + kPanelNB, H + HB, 1);
           }
@@ -1417,53 +1514,80 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
       }
     }
   };
-  for (int64_t st = 0; st < steps; ++st) {
-    const int64_t K0 = st * SB, H1 = K0 + HB;
-    factor_half(K0);
-    if (H1 < nmax) {
-      {
-        Prof pr(c, "laswp");
-        launch_laswp(L, dm, ni, K0, HB, H1, H1 + HB, H1, H1, 1);
+  auto issue = [&]() {
+    for (int64_t st = 0; st < steps; ++st) {
+      const int64_t K0 = st * SB, H1 = K0 + HB;
+      factor_half(K0);
+      if (H1 < nmax) {
+        {
+          Prof pr(c, "laswp");
+          launch_laswp(L, dm, ni, K0, HB, H1, H1 + HB, H1, H1, 1);
+        }
+        {
+          Prof pr(c, "trsm");
+          launch_linv_neg(L, dm, ni, K0, Dp0.as<float2* const>());
+          pack2(st, kNeg0);  // -N and A12r
+          gemm(st, kG1);
+        }
+        {
+          Prof pr(c, "tc_pack");
+          pack2(st, kP2a);   // L21a and U12r
+        }
+        {
+          Prof pr(c, "gemm_tc");
+          gemm(st, kG2);
+        }
+        factor_half(H1);
       }
       {
+        Prof pr(c, "laswp");
+        launch_laswp(L, dm, ni, K0, HB, 0, nmax, K0, K0 + SB, 1);
+        if (H1 < nmax) launch_laswp(L, dm, ni, H1, HB, 0, nmax, H1, K0 + SB, 1);
+      }
+      if (!any(st, kG6)) continue;
+      {
         Prof pr(c, "trsm");
-        launch_linv_neg(L, dm, ni, K0, d_p0.as<float2* const>());
-        pack2(st, kNeg0);  // -N and A12r
-        gemm(st, kG1);
+        pack(st, kP3b);
+        gemm(st, kG3);
+        pack2(st, kP4a);   // Lmid and U12top
+        gemm(st, kG4);
+        launch_linv_neg(L, dm, ni, H1, Dp1.as<float2* const>());
+        pack2(st, kNeg1);  // -N (second half) and A12bot
+        gemm(st, kG5);
       }
       {
         Prof pr(c, "tc_pack");
-        pack2(st, kP2a);   // L21a and U12r
+        pack2(st, kP6a);   // L21 and U12
       }
       {
         Prof pr(c, "gemm_tc");
-        gemm(st, kG2);
+        gemm(st, kG6);
       }
-      factor_half(H1);
     }
-    {
-      Prof pr(c, "laswp");
-      launch_laswp(L, dm, ni, K0, HB, 0, nmax, K0, K0 + SB, 1);
-      if (H1 < nmax) launch_laswp(L, dm, ni, H1, HB, 0, nmax, H1, K0 + SB, 1);
+  };
+  if (!G) {
+    issue();
+  } else {
+    if (capture) {
+      CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      const long long k0 = launch_total();
+      issue();
+      G->kernels = launch_total() - k0;
+      cudaGraph_t g = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+      if (ce != cudaSuccess) {
+        c->lu_graphs.clear();
+        return cuda_fail(c, ce, "cudaStreamEndCapture");
+      }
+      G->graph = g;
+      CUDA_TRY(c, cudaGraphInstantiate(&G->exec, g, 0));
     }
-    if (!any(st, kG6)) continue;
-    {
-      Prof pr(c, "trsm");
-      pack(st, kP3b);
-      gemm(st, kG3);
-      pack2(st, kP4a);   // Lmid and U12top
-      gemm(st, kG4);
-      launch_linv_neg(L, dm, ni, H1, d_p1.as<float2* const>());
-      pack2(st, kNeg1);  // -N (second half) and A12bot
-      gemm(st, kG5);
-    }
-    {
-      Prof pr(c, "tc_pack");
-      pack2(st, kP6a);   // L21 and U12
-    }
-    {
-      Prof pr(c, "gemm_tc");
-      gemm(st, kG6);
+    CUDA_TRY(c, cudaGraphLaunch(G->exec, c->stream));
+    if (capture) {
+      c->lu_captures++;
+    } else {
+      c->lu_replays++;
+      count_launch((int)G->kernels);  // the graph's kernels run again
     }
   }
   CUDA_TRY(c, cudaGetLastError());
@@ -1618,6 +1742,125 @@ int promote(bemgpu_ctx* c, std::vector<FactorData*>& fs, std::vector<Buf>& part)
   return BEMGPU_OK;
 }
 
+// The reference's conditioning diagnostics (full.jl:364-409) of one factor: for systems of
+// order at most condition_limit, the 2-norm condition numbers of A and of the
+// equilibrated A from their singular values (condition.cu).  The factorisation keeps a
+// copy of A and of its scales; the SVDs run on the first diagnostics read (an FP64
+// Jacobi SVD of a 500 x 500 system takes about 0.2 s on a GB300, 30 times its solve).
+struct CondState {
+  bemgpu_ctx* c = nullptr;
+  int64_t N = 0;
+  bool equilibrate = true;
+  Buf A, rows, cols;  // complex128 copy of the system, its row and column scales
+  bool done = false;
+  double cond = NAN, scaled = NAN;
+};
+
+int prepare_conditioning(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
+  std::vector<VecInst> expand;
+  for (FactorData* f : fs) {
+    f->cond.reset();
+    const int64_t N = f->N;
+    if (N > f->prob.condition_limit) continue;
+    auto cs = std::make_shared<CondState>();
+    cs->c = c;
+    cs->N = N;
+    cs->equilibrate = f->prob.equilibrate != 0;
+    TRY(alloc(c, (size_t)N * N * 16, &cs->A));
+    TRY(alloc(c, (size_t)N * 8, &cs->rows));
+    TRY(alloc(c, (size_t)N * 8, &cs->cols));
+    CUDA_TRY(c, cudaMemcpyAsync(cs->rows.p, f->rows.p, (size_t)N * 8, cudaMemcpyDeviceToDevice,
+                                c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(cs->cols.p, f->cols.p, (size_t)N * 8, cudaMemcpyDeviceToDevice,
+                                c->stream));
+    if (f->a32) {  // compact storage: complex64 entries + FP64 near corrections
+      VecInst v;
+      std::memset(&v, 0, sizeof v);
+      v.A = f->A.p;
+      v.n = N;
+      v.lda = N;
+      v.out = cs->A.p;
+      set_compact(v, f);
+      expand.push_back(v);
+    } else {
+      CUDA_TRY(c, cudaMemcpyAsync(cs->A.p, f->A.p, (size_t)N * N * 16, cudaMemcpyDeviceToDevice,
+                                  c->stream));
+    }
+    f->cond = cs;
+  }
+  if (!expand.empty()) {
+    Buf de;
+    TRY(to_device(c, expand, &de));
+    int64_t nmax = 0, mn = 0;
+    for (auto& v : expand) {
+      nmax = std::max(nmax, v.n);
+      mn = std::max(mn, v.n_near);
+    }
+    const Launch L = c->launch();
+    launch_expand_a32(L, de.as<VecInst>(), (int)expand.size(), nmax);
+    launch_near_add(L, de.as<VecInst>(), (int)expand.size(), mn, 1);
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // `de` is released on return
+  }
+  return BEMGPU_OK;
+}
+
+// Singular values of A and of the scaled A on working copies; cond = max / min.
+int compute_conditioning(CondState* cs) {
+  if (cs->done) return BEMGPU_OK;
+  bemgpu_ctx* c = cs->c;
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  const Launch L = c->launch();
+  const int64_t N = cs->N;
+  Buf work[2], sig[2], flags;
+  SvdInst si[2];
+  TRY(alloc(c, 8, &flags));
+  for (int k = 0; k < 2; ++k) {
+    TRY(alloc(c, (size_t)N * N * 16, &work[k]));
+    TRY(alloc(c, (size_t)N * 8, &sig[k]));
+    CUDA_TRY(c, cudaMemcpyAsync(work[k].p, cs->A.p, (size_t)N * N * 16,
+                                cudaMemcpyDeviceToDevice, c->stream));
+    std::memset(&si[k], 0, sizeof si[k]);
+    si[k].a = work[k].as<double2>();
+    si[k].n = N;
+    si[k].lda = N;
+    if (k == 1 && cs->equilibrate) {
+      si[k].rows = cs->rows.as<double>();
+      si[k].cols = cs->cols.as<double>();
+    }
+    si[k].rotated = flags.as<int32_t>() + k;
+    si[k].sigma = sig[k].as<double>();
+  }
+  std::vector<SvdInst> hsi(si, si + 2);
+  Buf ds;
+  TRY(to_device(c, hsi, &ds));
+  launch_svd_scale(L, ds.as<SvdInst>(), 2, N);
+  const int64_t m = (N + 1) & ~int64_t(1);
+  const double tol = 4.0 * 2.220446049250313e-16 * std::sqrt((double)N);
+  std::vector<int32_t> rot;
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    CUDA_TRY(c, cudaMemsetAsync(flags.p, 0, 8, c->stream));
+    for (int64_t r = 0; r < m - 1; ++r) launch_jacobi_round(L, ds.as<SvdInst>(), 2, N, r, tol);
+    CUDA_TRY(c, cudaGetLastError());
+    TRY(download(c, flags, &rot, 2));
+    if (rot[0] == 0 && rot[1] == 0) break;
+  }
+  launch_column_norms(L, ds.as<SvdInst>(), 2, N);
+  CUDA_TRY(c, cudaGetLastError());
+  double cn[2];
+  for (int k = 0; k < 2; ++k) {
+    std::vector<double> sv;
+    TRY(download(c, sig[k], &sv, (size_t)N));
+    const double mx = *std::max_element(sv.begin(), sv.end());
+    const double mn = *std::min_element(sv.begin(), sv.end());
+    cn[k] = mn > 0.0 ? mx / mn : INFINITY;
+  }
+  cs->cond = cn[0];
+  cs->scaled = cs->equilibrate ? cn[1] : cn[0];
+  cs->done = true;
+  return BEMGPU_OK;
+}
+
 int factorize_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
   const Launch L = c->launch();
   std::vector<Buf> part(fs.size());
@@ -1648,6 +1891,7 @@ int factorize_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
     v.rows_inv = f->rows_inv.as<float>();
     set_compact(v, f);
     v.part = part[t].as<double>();
+    v.norm_floor = f->prob.norm_floor;
     nmax = std::max(nmax, f->N);
   }
   Buf d;
@@ -1661,6 +1905,7 @@ int factorize_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs) {
       launch_fill(L, f->rows.as<double>(), f->N, 1.0);
       launch_fill(L, f->cols.as<double>(), f->N, 1.0);
     }
+  TRY(prepare_conditioning(c, fs));
   std::vector<int32_t> flags;
   TRY(scale_copy_batch(c, fs, part, false, &flags));
   std::vector<FactorData*> single, dbl, prom;
@@ -1877,6 +2122,25 @@ int residual_pass(bemgpu_ctx* c, std::vector<SolveInst*>& ss,
   stats->resize(ss.size());
   for (size_t t = 0; t < ss.size(); ++t)
     TRY(download(c, ss[t]->stats, &(*stats)[t], (size_t)ss[t]->R * kStats));
+  return BEMGPU_OK;
+}
+
+// Conditioning (filled when read, see CondState) and derivative-evaluation fields of a
+// factor's diagnostics.
+void factor_conditioning(const FactorData* f, bemgpu_diagnostics* dg) {
+  dg->conditioning = f->cond ? 1 : 0;
+  dg->condition_number = dg->scaled_condition_number = NAN;
+  dg->condition_limit = f->prob.condition_limit;
+  const bool muller = f->kind == kAsmMuller || (f->kind == kAsmRegion && !f->region_cbie);
+  dg->derivative_exterior = dg->derivative_interior = muller ? 1 : 0;
+}
+
+// The condition numbers of a diagnostics record whose conditioning data is `cs`.
+int read_conditioning(const std::shared_ptr<CondState>& cs, bemgpu_diagnostics* dg) {
+  if (!cs) return BEMGPU_OK;
+  TRY(compute_conditioning(cs.get()));
+  dg->condition_number = cs->cond;
+  dg->scaled_condition_number = cs->scaled;
   return BEMGPU_OK;
 }
 
@@ -2213,6 +2477,7 @@ int solve_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<i
     dg.device_bytes = (int64_t)f->bytes();
     dg.nrhs = s.R;
     dg.info = f->info_h;
+    factor_conditioning(f, &dg);
     for (int r = 0; r < s.R; ++r) {
       const double* q = &st[t][(size_t)r * kStats];
       double an = std::sqrt(q[4]), bn = std::sqrt(q[5]);
@@ -2232,6 +2497,7 @@ int solve_batch(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<i
     out[t]->nrhs = s.R;
     out[t]->mesh = f->mesh;
     out[t]->base_mesh = f->base_mesh;
+    out[t]->cond = f->cond;
     out[t]->k = f->prob.k;
     out[t]->boundary = f->prob.boundary;
     out[t]->g = f->prob.density_contrast;
@@ -2713,6 +2979,8 @@ void bemgpu_problem_init(bemgpu_problem* p) {
   p->refine_maxiter = 8;
   p->condition_guard = 10.0 * 1.1920928955078125e-07;
   p->near_eta = 2.0;
+  p->condition_limit = 512;
+  p->norm_floor = 0.0;
 }
 
 int bemgpu_mesh_validate(const double* nodes, int64_t n_nodes, const int64_t* triangles,
@@ -2929,7 +3197,8 @@ int bemgpu_factor_diagnostics(const bemgpu_factor* f, bemgpu_diagnostics* out) {
   out->factor_ms = d->factor_ms;
   out->device_bytes = (int64_t)d->bytes();
   out->info = d->info_h;
-  return BEMGPU_OK;
+  factor_conditioning(d, out);
+  return read_conditioning(d->cond, out);
 }
 
 int bemgpu_solve(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_problem* problem,
@@ -3807,6 +4076,8 @@ int bemgpu_hmatrix_solve(bemgpu_ctx* c, const bemgpu_mesh* mesh, const bemgpu_pr
   sd->hmatrix = true;
   bemgpu_diagnostics& dg = sd->diag;
   std::memset(&dg, 0, sizeof dg);
+  dg.condition_number = dg.scaled_condition_number = NAN;  // no factor: not computed
+  dg.condition_limit = p.condition_limit;
   dg.unknown_count = n;
   dg.quadrature_nodes = n;
   dg.near_pairs = m->n_near;
@@ -4018,7 +4289,7 @@ int bemgpu_region_traces(const bemgpu_solution* sol, int32_t rhs, double* p, dou
 int bemgpu_solution_diagnostics(const bemgpu_solution* sol, bemgpu_diagnostics* out) {
   if (!sol || !out) return fail(nullptr, BEMGPU_EINVAL, "null argument");
   *out = sol->d->diag;
-  return BEMGPU_OK;
+  return read_conditioning(sol->d->cond, out);
 }
 
 int bemgpu_solution_destroy(bemgpu_solution* sol) {
@@ -4613,6 +4884,25 @@ int bemgpu_profile_read(bemgpu_ctx* c, const char* family, int64_t* launches, do
     }
   if (launches) *launches = cnt;
   if (total_ms) *total_ms = ms;
+  return BEMGPU_OK;
+}
+
+int bemgpu_ctx_set_graphs(bemgpu_ctx* c, int32_t enable) {
+  if (!c) return fail(nullptr, BEMGPU_EINVAL, "null context");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  c->graphs = enable != 0;
+  if (!c->graphs) {
+    c->lu_graphs.clear();
+    c->lu_seen.clear();
+  }
+  return BEMGPU_OK;
+}
+
+int bemgpu_ctx_graph_stats(const bemgpu_ctx* c, int64_t* captures, int64_t* replays) {
+  if (!c) return fail(nullptr, BEMGPU_EINVAL, "null context");
+  if (captures) *captures = c->lu_captures;
+  if (replays) *replays = c->lu_replays;
   return BEMGPU_OK;
 }
 

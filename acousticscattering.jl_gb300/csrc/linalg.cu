@@ -1190,11 +1190,14 @@ __global__ void k_copy_xy(const MatInst* __restrict__ insts, int to_y) {
     st<R>(M.x, off + i, ld<R>(M.y, off + i));
 }
 
-// perm from LAPACK pivots: apply the interchanges in order to the identity.
+// perm from LAPACK pivots: apply the interchanges in order to the identity, in shared
+// memory (SMEM, orders up to the shared-memory capacity) or in place in global memory.
+template <bool SMEM>
 __global__ void __launch_bounds__(256) k_make_perm(const MatInst* __restrict__ insts) {
   const MatInst& M = insts[blockIdx.x];
   if (!M.active || !M.perm) return;
-  extern __shared__ int32_t sperm[];
+  extern __shared__ int32_t sperm_smem[];
+  int32_t* sperm = SMEM ? sperm_smem : M.perm;
   const int64_t n = M.n;
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) sperm[i] = (int32_t)i;
   __syncthreads();
@@ -1206,7 +1209,8 @@ __global__ void __launch_bounds__(256) k_make_perm(const MatInst* __restrict__ i
       sperm[p] = t;
     }
   __syncthreads();
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) M.perm[i] = sperm[i];
+  if (SMEM)
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) M.perm[i] = sperm[i];
 }
 
 // ------------------------------------------------------------------ launch wrappers
@@ -1465,12 +1469,19 @@ static void getrs_big_t(const Launch& L, const MatInst* d, int ninst, int64_t nm
 }
 
 void launch_make_perm(const Launch& L, const MatInst* d, int ninst, int64_t nmax) {
+  constexpr size_t kMaxSmem = 227 * 1024;
   const size_t smem = (size_t)nmax * sizeof(int32_t);
+  if (smem > kMaxSmem) {  // beyond 58112 unknowns: interchanges in global memory
+    k_make_perm<false><<<ninst, 256, 0, L.stream>>>(d);
+    count_launch(1);
+    return;
+  }
   static PerDeviceOnce attr;
   attr.call([] {
-    cudaFuncSetAttribute(k_make_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_make_perm<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kMaxSmem);
   });
-  k_make_perm<<<ninst, 256, smem, L.stream>>>(d);
+  k_make_perm<true><<<ninst, 256, smem, L.stream>>>(d);
   count_launch(1);
 }
 

@@ -97,6 +97,7 @@ __global__ void k_rowstats_finish(const VecInst* __restrict__ insts) {
     mx = fmax(mx, V.part[2 * (c * V.n + i)]);
     sm += V.part[2 * (c * V.n + i) + 1];
   }
+  mx = fmax(mx, V.norm_floor);  // the reference's norm_floor (full.jl:388-394)
   V.rows[i] = (mx == 0.0) ? 1.0 : mx;
   V.rows_inv[i] = (float)(1.0 / V.rows[i]);
   V.rowsum[i] = sm;
@@ -124,7 +125,10 @@ __device__ __forceinline__ void colmax_body(const VecInst& V) {
   for (; i < n; i += 32) mx = fmaxf(mx, mag_at<A32>(V, base + i) * V.rows_inv[i]);
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
-  if (lane == 0) V.cols[j] = (mx == 0.f) ? 1.0 : (double)mx;
+  if (lane == 0) {
+    const double cm = fmax((double)mx, V.norm_floor);
+    V.cols[j] = (cm == 0.0) ? 1.0 : cm;
+  }
 }
 __global__ void k_colmax(const VecInst* __restrict__ insts) {
   const VecInst& V = insts[blockIdx.y];

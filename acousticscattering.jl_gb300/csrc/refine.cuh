@@ -46,6 +46,7 @@ struct VecInst {
   float4* xs;                // x split as FP32 (hi.re, hi.im, lo.re, lo.im), n x nrhs
   float* xa;                 // |x| in FP32, n x nrhs
   float* cols_inv32;         // 1 / cols in FP32 (n)
+  double norm_floor;         // equilibration: lower bound of the row and column scales
 };
 
 #ifdef __CUDACC__

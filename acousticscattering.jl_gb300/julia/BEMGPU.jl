@@ -12,8 +12,10 @@
 module BEMGPU
 
 using LinearAlgebra
+import AcousticScattering
 import AcousticScattering: bem, scattering_amplitude, target_strength, diagnostics, pressure,
-    BEMSolution, Rigid, PressureRelease, FluidFilled
+    BEMSolution, Rigid, PressureRelease, FluidFilled, Mesh, incidence_angle_sweep,
+    frequency_sweep, IncidenceAngleSweep, FrequencySweep
 
 const libbemgpu = joinpath(@__DIR__, "..", "bemgpu", "libbemgpu.so")
 
@@ -34,7 +36,8 @@ struct Problem
     condition_guard::Float64
     near_eta::Float64
     discretization::Int32   # 0 collocation, 1 Nyström (the reference's correction=(method=:dim,))
-    reserved::Int32
+    condition_limit::Int32  # SVD condition numbers up to this order (full.jl:364-409)
+    norm_floor::Float64     # lower bound of the equilibration scales (double precision)
 end
 
 struct Diagnostics
@@ -63,6 +66,12 @@ struct Diagnostics
     device_bytes::Int64
     nrhs::Int32
     info::Int32
+    condition_number::Float64
+    scaled_condition_number::Float64
+    conditioning::Int32
+    condition_limit::Int32
+    derivative_exterior::Int32
+    derivative_interior::Int32
 end
 
 function last_error(ctx)
@@ -117,6 +126,27 @@ function upload(ctx::Context, nodes::AbstractMatrix{<:Real}, triangles::Abstract
     m = GPUMesh(r[], n, t)
     finalizer(x -> ccall((:bemgpu_mesh_destroy, libbemgpu), Cint, (Ptr{Cvoid},), x.ptr), m)
     return m
+end
+
+"""
+    upload(ctx, surface::AcousticScattering.Mesh) -> GPUMesh
+
+The nodes and flat triangles of a surface built by the reference's `mesh(nodes,
+triangles)` (geometry/surface.jl:271-298; its `_SurfaceGeometry` body keeps the supplied
+nodes in meters and one corner list per triangle), validated and uploaded.
+"""
+function upload(ctx::Context, surface::Mesh)
+    geom = surface.body
+    geom isa AcousticScattering._SurfaceGeometry || throw(ArgumentError(
+        "BEMGPU solves supplied triangle surfaces (mesh(nodes, triangles)); mesh generated " *
+        "bodies with mesh(nodes, triangles) first"))
+    all(c -> length(c) == 3, geom.connectivity) ||
+        throw(ArgumentError("BEMGPU needs flat three-node triangles"))
+    tris = Matrix{Int64}(undef, 3, length(geom.connectivity))
+    for (j, c) in enumerate(geom.connectivity)
+        tris[:, j] .= c
+    end
+    return upload(ctx, geom.nodes, tris)
 end
 
 struct _GPUBEMData
@@ -179,7 +209,8 @@ function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
         precision::Symbol = :double, equilibrate::Bool = true,
         refinement::NamedTuple = (;), assembly::Symbol = :default,
         compression::NamedTuple = (method = :none,), gmres_kwargs::NamedTuple = (;),
-        discretization::Symbol = :collocation, ctx::Context = context())
+        discretization::Symbol = :collocation, condition_limit::Integer = 512,
+        norm_floor::Real = 0.0, ctx::Context = context())
     isfinite(k) && k > 0 || throw(ArgumentError("k must be finite and positive"))
     discretization in (:collocation, :nystrom) ||
         throw(ArgumentError("discretization must be :collocation or :nystrom"))
@@ -193,7 +224,8 @@ function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
             formulation === nothing ? Int32(-1) : FORMULATIONS[formulation],
             precision === :mixed ? Int32(1) : Int32(0), Int32(1), Float64(k), 1.0, 1.0,
             1e-13, Int32(8), Int32(0), 10eps(Float32), 2.0,
-            discretization === :nystrom ? Int32(1) : Int32(0), Int32(0))
+            discretization === :nystrom ? Int32(1) : Int32(0), Int32(condition_limit),
+        Float64(norm_floor))
         o = HmatrixOptions(get(compression, :tol, 1e-5), get(compression, :eta, 3.0),
             Int32(get(compression, :leaf_size, 64)), Int32(get(gmres_kwargs, :restart, 150)),
             get(gmres_kwargs, :reltol, 1e-4), get(gmres_kwargs, :abstol, 0.0),
@@ -224,7 +256,8 @@ function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
         get(refinement, :tolerance, 1e-13), Int32(get(refinement, :maxiter, 8)),
         assembly === :double ? Int32(1) : assembly === :single ? Int32(2) : Int32(0),
         get(refinement, :condition_guard, 10eps(Float32)), 2.0,
-        discretization === :nystrom ? Int32(1) : Int32(0), Int32(0))
+        discretization === :nystrom ? Int32(1) : Int32(0), Int32(condition_limit),
+        Float64(norm_floor))
     inc = Float64[incidence_angle, incidence_azimuth]
     r = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:bemgpu_solve, libbemgpu), Cint,
@@ -236,6 +269,133 @@ function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
     return BEMSolution(AcousticScattering._SurfaceGeometry(m.nodes, m.triangles), boundary,
         Float64(k), :full, data)
 end
+
+"""
+    bem(surface::AcousticScattering.Mesh, boundary, k; kwargs...)
+
+The reference's own entry point, `bem(surface::Mesh, boundary, k; ...)`
+(solvers/bem/surface.jl:10-23), for a surface from `mesh(nodes, triangles)`: the surface
+is uploaded (`upload(ctx, surface)`) and solved as `bem(gpu_mesh, boundary, k; ...)`.
+"""
+bem(surface::Mesh, boundary::Union{Rigid, PressureRelease, FluidFilled}, k::Real;
+    ctx::Context = context(), kwargs...) = bem(upload(ctx, surface), boundary, k; ctx, kwargs...)
+
+function _problem(boundary, k; formulation = nothing, precision = :double,
+        equilibrate = true, refinement = (;), assembly = :default,
+        discretization = :collocation, condition_limit = 512, norm_floor = 0.0)
+    g, h = boundary isa FluidFilled ?
+           (boundary.density_contrast, boundary.soundspeed_contrast) : (1.0, 1.0)
+    return Problem(_boundary_code(boundary),
+        formulation === nothing ? Int32(-1) : FORMULATIONS[formulation],
+        precision === :mixed ? Int32(1) : Int32(0), Int32(equilibrate), Float64(k), g, h,
+        get(refinement, :tolerance, 1e-13), Int32(get(refinement, :maxiter, 8)),
+        assembly === :double ? Int32(1) : assembly === :single ? Int32(2) : Int32(0),
+        get(refinement, :condition_guard, 10eps(Float32)), 2.0,
+        discretization === :nystrom ? Int32(1) : Int32(0), Int32(condition_limit),
+        Float64(norm_floor))
+end
+
+function _backscatter(solution::Ptr{Cvoid}, nrhs::Integer)
+    out = zeros(Float64, 2)
+    amps = Vector{ComplexF64}(undef, nrhs)
+    for r in 1:nrhs
+        check(ccall((:bemgpu_far_field, libbemgpu), Cint,
+            (Ptr{Cvoid}, Int32, Int64, Ptr{Float64}, Ptr{Float64}),
+            solution, r - 1, 1, C_NULL, out))
+        amps[r] = complex(out[1], out[2])
+    end
+    return amps
+end
+
+"""
+    incidence_angle_sweep(gpu_mesh | surface::Mesh, boundary, k, angles;
+        incidence_azimuth=0, formulation, precision=:double, equilibrate=true,
+        refinement=(;), assembly=:default, discretization=:collocation)
+
+The reference's dense-factor `incidence_angle_sweep` (postprocessing/sweeps.jl:626-701):
+assembled and factored once, every polar angle (radians from +x) solved as one
+multi-right-hand-side batch; backscatter amplitudes and target strengths in the
+reference's `IncidenceAngleSweep`.
+"""
+function incidence_angle_sweep(m::GPUMesh, boundary::Union{Rigid, PressureRelease, FluidFilled},
+        k::Real, angles::AbstractVector{<:Real}; incidence_azimuth::Real = 0.0,
+        ctx::Context = context(), kwargs...)
+    isempty(angles) && throw(ArgumentError("a sweep needs at least one sample"))
+    all(isfinite, angles) || throw(ArgumentError("sweep coordinates must be finite"))
+    isfinite(incidence_azimuth) || throw(ArgumentError("incidence azimuth must be finite"))
+    p = _problem(boundary, k; kwargs...)
+    f = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:bemgpu_factor_create, libbemgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ref{Problem}, Ptr{Ptr{Cvoid}}), ctx.ptr, m.ptr, p, f), ctx.ptr)
+    try
+        inc = Float64[x for a in angles for x in (Float64(a), Float64(incidence_azimuth))]
+        r = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:bemgpu_factor_solve, libbemgpu), Cint,
+            (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Ptr{Cvoid}}), f[], length(angles), inc, r),
+            ctx.ptr)
+        amps = try
+            _backscatter(r[], length(angles))
+        finally
+            ccall((:bemgpu_solution_destroy, libbemgpu), Cint, (Ptr{Cvoid},), r[])
+        end
+        return IncidenceAngleSweep(Float64.(angles), 20 .* log10.(abs.(amps)), amps, String[])
+    finally
+        ccall((:bemgpu_factor_destroy, libbemgpu), Cint, (Ptr{Cvoid},), f[])
+    end
+end
+
+incidence_angle_sweep(surface::Mesh, boundary::Union{Rigid, PressureRelease, FluidFilled},
+    k::Real, angles::AbstractVector{<:Real}; ctx::Context = context(), kwargs...) =
+    incidence_angle_sweep(upload(ctx, surface), boundary, k, angles; ctx, kwargs...)
+
+"""
+    frequency_sweep(gpu_mesh | surface::Mesh, boundary, frequencies, sound_speed;
+        incidence_angle=π/2, incidence_azimuth=0, kwargs...)
+
+Backscatter over frequencies (postprocessing/sweeps.jl:103-110 computes the same
+`FrequencySweep` by calling `bem` once per frequency): every frequency's system is
+assembled, factored and solved in one batched launch sequence.
+"""
+function frequency_sweep(m::GPUMesh, boundary::Union{Rigid, PressureRelease, FluidFilled},
+        frequencies::AbstractVector{<:Real}, sound_speed::Real;
+        incidence_angle::Real = π / 2, incidence_azimuth::Real = 0.0,
+        ctx::Context = context(), kwargs...)
+    isfinite(sound_speed) && sound_speed > 0 ||
+        throw(ArgumentError("sound_speed must be finite and positive"))
+    all(>(0), frequencies) || throw(ArgumentError("frequencies must be positive"))
+    ks = 2π .* Float64.(frequencies) ./ Float64(sound_speed)
+    count = length(ks)
+    probs = [_problem(boundary, k; kwargs...) for k in ks]
+    meshes = fill(m.ptr, count)
+    factors = fill(C_NULL, count)
+    check(ccall((:bemgpu_factor_create_batch, libbemgpu), Cint,
+        (Ptr{Cvoid}, Int32, Ptr{Ptr{Cvoid}}, Ptr{Problem}, Ptr{Ptr{Cvoid}}),
+        ctx.ptr, count, meshes, probs, factors), ctx.ptr)
+    sols = fill(C_NULL, count)
+    try
+        nrhs = fill(Int32(1), count)
+        inc = [Float64[incidence_angle, incidence_azimuth] for _ in 1:count]
+        incp = [pointer(v) for v in inc]
+        GC.@preserve inc check(ccall((:bemgpu_factor_solve_batch, libbemgpu), Cint,
+            (Ptr{Cvoid}, Int32, Ptr{Ptr{Cvoid}}, Ptr{Int32}, Ptr{Ptr{Float64}},
+                Ptr{Ptr{Cvoid}}), ctx.ptr, count, factors, nrhs, incp, sols), ctx.ptr)
+        amps = [_backscatter(s, 1)[1] for s in sols]
+        return FrequencySweep(Float64.(frequencies), ks, 20 .* log10.(abs.(amps)), amps,
+            String[])
+    finally
+        for s in sols
+            s == C_NULL || ccall((:bemgpu_solution_destroy, libbemgpu), Cint, (Ptr{Cvoid},), s)
+        end
+        for f in factors
+            f == C_NULL || ccall((:bemgpu_factor_destroy, libbemgpu), Cint, (Ptr{Cvoid},), f)
+        end
+    end
+end
+
+frequency_sweep(surface::Mesh, boundary::Union{Rigid, PressureRelease, FluidFilled},
+    frequencies::AbstractVector{<:Real}, sound_speed::Real; ctx::Context = context(),
+    kwargs...) = frequency_sweep(upload(ctx, surface), boundary, frequencies, sound_speed;
+    ctx, kwargs...)
 
 """
     bem(gpu_meshes::Vector{GPUMesh}, materials::Vector{FluidFilled}, k;
@@ -251,7 +411,8 @@ function bem(ms::AbstractVector{GPUMesh}, materials::AbstractVector{<:FluidFille
         parents::AbstractVector{<:Integer} = collect(0:(length(ms) - 1)),
         incidence_angle::Real = π / 2, incidence_azimuth::Real = 0.0,
         formulation::Symbol = :muller, precision::Symbol = :double, equilibrate::Bool = true,
-        refinement::NamedTuple = (;), assembly::Symbol = :default, ctx::Context = context())
+        refinement::NamedTuple = (;), assembly::Symbol = :default,
+        condition_limit::Integer = 512, ctx::Context = context())
     count = length(ms)
     length(materials) == length(parents) == count ||
         throw(ArgumentError("supply one material and parent per interface"))
@@ -259,7 +420,8 @@ function bem(ms::AbstractVector{GPUMesh}, materials::AbstractVector{<:FluidFille
         precision === :mixed ? Int32(1) : Int32(0), Int32(equilibrate), Float64(k), 1.0, 1.0,
         get(refinement, :tolerance, 1e-13), Int32(get(refinement, :maxiter, 8)),
         assembly === :double ? Int32(1) : assembly === :single ? Int32(2) : Int32(0),
-        get(refinement, :condition_guard, 10eps(Float32)), 2.0, Int32(0), Int32(0))
+        get(refinement, :condition_guard, 10eps(Float32)), 2.0, Int32(0),
+        Int32(condition_limit), 0.0)
     handles = Ptr{Cvoid}[m.ptr for m in ms]
     dens = Float64[m.density_contrast for m in materials]
     speeds = Float64[m.soundspeed_contrast for m in materials]
@@ -337,7 +499,13 @@ function diagnostics(sol::BEMSolution{_GPUBEMData})
         normwise_backward_error = d.normwise_backward_error,
         componentwise_backward_error = d.componentwise_backward_error,
         coupling = complex(d.coupling_re, d.coupling_im), method = d.precision == 1 ?
-                                                                    :mixed_refinement : :direct)
+                                                                    :mixed_refinement : :direct,
+        equilibrate = d.equilibrate == 1, condition_limit = d.condition_limit,
+        conditioning = d.conditioning == 1 ? :svd : :not_computed,
+        condition_number = d.conditioning == 1 ? d.condition_number : nothing,
+        scaled_condition_number = d.conditioning == 1 ? d.scaled_condition_number : nothing,
+        derivative_evaluation = d.derivative_exterior == 0 ? nothing :
+                                (exterior = :direct, interior = :direct))
 end
 
 end # module

@@ -577,8 +577,23 @@ def run_config3(args):
         ts.append(ctx.timer_stop())
     launches = (bemgpu.Context.launch_count() - l0) // args.steps
     clk = clocks.stop()
+    gstats = ctx.graph_stats()
+    # the same steps with the launch-shape tuner and the captured LU graphs switched off
+    ctx.set_autotune(False)
+    ctx.set_graphs(False)
+    step("mixed", allidx)
+    ts_plain = []
+    for _ in range(args.steps):
+        ctx.timer_start()
+        ap = step("mixed", allidx)
+        ts_plain.append(ctx.timer_stop())
+    ctx.set_autotune(True)
+    ctx.set_graphs(True)
+    same_bits = all(np.array_equal(am[i], ap[i]) for i in allidx)
+    # FP64 on a subset spanning the sizes: the FP64 LU of all 256 bodies at the GB300's
+    # FP64 rate would take about a quarter of an hour
     order = np.argsort(sizes)
-    sub = [int(i) for i in order[:: max(1, count // 8)]][:8]
+    sub = [int(i) for i in order[:: max(1, count // args.fp64_bodies)]][: args.fp64_bodies]
     ctx.timer_start()
     a64 = step("double", sub)
     fp64_ms = ctx.timer_stop()
@@ -594,7 +609,14 @@ def run_config3(args):
         dtype="c64 factor + fp64 refinement",
         fp64={"solves_per_s": len(sub) * 1e3 / fp64_ms, "bodies": len(sub),
               "panels": [sizes[i] for i in sub]},
-        ts_error_db={"max": float(max(err)), "per_body": [float(e) for e in err]},
+        ts_error_db={"max": float(max(err)), "per_body": [float(e) for e in err],
+                     "vs": "GPU FP64 on the subset (the GPU FP64 path is pinned to the CPU "
+                           "oracle on four of these bodies by the GPU tests)"},
+        untuned={"solves_per_s": count * 1e3 / float(np.mean(ts_plain)),
+                 "ms_per_step": float(np.mean(ts_plain)),
+                 "note": "launch-shape tuner and captured LU graphs off",
+                 "same_bits": same_bits},
+        lu_graphs=gstats,
         clocks=clk, gpu_launches=launches)
     print(json.dumps(line))
     return line
@@ -987,6 +1009,8 @@ def main():
                          "sphere; 2 large single solve x 181 angles; 3 uneven batch; 4 serving; "
                          "5 compressed operators + GMRES (the reference's default rigid path)")
     ap.add_argument("--bodies", type=int, default=256, help="config 3: bodies")
+    ap.add_argument("--fp64-bodies", type=int, default=16,
+                    help="config 3: bodies also solved in FP64")
     ap.add_argument("--requests", type=int, default=10000, help="config 4: requests")
     ap.add_argument("--pool", type=int, default=512, help="config 4: distinct bodies")
     ap.add_argument("--lanes", type=int, default=2, help="config 4: server lanes")

@@ -134,7 +134,10 @@ typedef struct {
   double condition_guard;      /* single rcond guard (default 10 eps(float32)) */
   double near_eta;             /* near-pair radius in source diameters (default 2) */
   int32_t discretization;      /* bemgpu_discretization (default COLLOCATION) */
-  int32_t reserved;
+  int32_t condition_limit;     /* systems of at most this order get SVD condition numbers
+                                  in their diagnostics (default 512, full.jl:364-409) */
+  double norm_floor;           /* lower bound of the equilibration's row and column scales
+                                  (default 0; precision DOUBLE only, as the reference) */
 } bemgpu_problem;
 
 /* Diagnostics of one solution; names follow the reference's diagnostics() fields. */
@@ -160,6 +163,20 @@ typedef struct {
   int64_t device_bytes;            /* bytes held by the factor */
   int32_t nrhs;
   int32_t info;                    /* first exact zero pivot (1-based) of the factor, 0 if none */
+  /* the reference's factor diagnostics (full.jl:364-409): 2-norm condition numbers of the
+     system and of the equilibrated system from their singular values when the order is at
+     most condition_limit (conditioning = 1, :svd), else conditioning = 0 (:not_computed)
+     and both numbers NaN.  The factorisation keeps a copy of such a system; its SVDs run
+     on the device when the diagnostics are first read. */
+  double condition_number;
+  double scaled_condition_number;
+  int32_t conditioning;
+  int32_t condition_limit;
+  /* fluid Muller systems: how K' and H were evaluated, exterior and interior (the
+     reference's derivative_evaluation, full.jl:201-212, 330-341): 1 direct quadrature;
+     0 not used (rigid, soft, fluid CBIE) */
+  int32_t derivative_exterior;
+  int32_t derivative_interior;
 } bemgpu_diagnostics;
 
 /* ------------------------------------------------------------------ host utilities */
@@ -463,6 +480,17 @@ int bemgpu_hmatrix_apply(bemgpu_ctx *ctx, const bemgpu_mesh *mesh, const bemgpu_
  * choices (fixed rules are used).  No reference counterpart.
  */
 int bemgpu_ctx_set_autotune(bemgpu_ctx *ctx, int32_t enable);
+/*
+ * CUDA graphs of the batched LU (default 1): the launch sequence of the tensor-core
+ * factorisation of a batch is captured the second time a batch of the same shape (the
+ * instances' orders) is factored, and replayed for later batches of that shape, with the
+ * new batch's descriptors written into the graph's arrays (16 shapes per context, least
+ * recently used dropped; not while profiling is on).  Results are bit-identical with
+ * graphs on or off.  enable = 0 drops the captured graphs.  No reference counterpart.
+ */
+int bemgpu_ctx_set_graphs(bemgpu_ctx *ctx, int32_t enable);
+/* Batched-LU graphs captured and replayed by the context so far. */
+int bemgpu_ctx_graph_stats(const bemgpu_ctx *ctx, int64_t *captures, int64_t *replays);
 /*
  * Complex64 trailing updates of the mixed-precision LU on the tensor cores (split-BF16
  * tcgen05 GEMM, default 1) or on the CUDA cores (0).  No reference counterpart: a

@@ -476,12 +476,13 @@ def solve_gmres(nodes, triangles, boundary, k, incidence_angle=math.pi / 2,
 
 
 # ---------------------------------------------------------------- dense factor/solve
-def equilibrate(A):
-    """Row max, then column max of the row-scaled matrix (full.jl:388-394)."""
-    rows = np.max(np.abs(A), axis=1)
+def equilibrate(A, norm_floor=0.0):
+    """Row max, then column max of the row-scaled matrix, each bounded below by
+    norm_floor (full.jl:388-394)."""
+    rows = np.maximum(np.max(np.abs(A), axis=1), norm_floor)
     rows[rows == 0] = 1.0
     scaled = A / rows[:, None]
-    cols = np.max(np.abs(scaled), axis=0)
+    cols = np.maximum(np.max(np.abs(scaled), axis=0), norm_floor)
     cols[cols == 0] = 1.0
     return rows, cols, scaled / cols[None, :]
 
@@ -489,10 +490,10 @@ def equilibrate(A):
 class DoubleFactor:
     """Equilibrated complex128 LU (full.jl:364-409 with precision=:double)."""
 
-    def __init__(self, A, equilibrate_rows=True):
+    def __init__(self, A, equilibrate_rows=True, norm_floor=0.0):
         self.A = A
         if equilibrate_rows:
-            self.rows, self.cols, S = equilibrate(A)
+            self.rows, self.cols, S = equilibrate(A, norm_floor)
         else:
             self.rows = self.cols = None
             S = A.copy()
@@ -627,7 +628,7 @@ class MixedRefinement:
 # ---------------------------------------------------------------- the solve chain
 def solve(nodes, triangles, boundary, k, incidence_angle=math.pi / 2,
           incidence_azimuth=0.0, formulation=None, g=1.0, h=1.0, precision="double",
-          equilibrate_rows=True, directions=None, eta=NEAR_ETA, panels=None):
+          equilibrate_rows=True, directions=None, eta=NEAR_ETA, panels=None, norm_floor=0.0):
     """Scattered traces and far-field amplitudes for one (mesh, boundary, k, incidence).
 
     boundary: "rigid", "pressure_release" or "fluid".  Returns a dict with p_scat,
@@ -647,7 +648,7 @@ def solve(nodes, triangles, boundary, k, incidence_angle=math.pi / 2,
             A, b = M1, M2 @ q_inc
         else:
             A, b = M2, M1 @ p_inc
-        F = DoubleFactor(A, equilibrate_rows)
+        F = DoubleFactor(A, equilibrate_rows, norm_floor)
         x = F.solve(b)
         if boundary == "rigid":
             p_s, q_s = x, -q_inc
@@ -667,7 +668,7 @@ def solve(nodes, triangles, boundary, k, incidence_angle=math.pi / 2,
             x = res["x"]
             info.update(res)
         else:
-            F = DoubleFactor(A, equilibrate_rows)
+            F = DoubleFactor(A, equilibrate_rows, norm_floor)
             x = F.solve(b)
         p_s, q_s = x[:n], x[n:]
         if formulation == "muller":

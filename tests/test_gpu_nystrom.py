@@ -315,35 +315,69 @@ def _reference_amplitudes():
         return json.load(f)
 
 
-def test_reference_rigid_spheroid_amplitudes(ctx):
-    """The amplitudes the reference's own tests hard-code for its Nyström solve of a rigid
-    spheroid (test/extended/bem/spheroid/full3d.jl:9-24): met within the reference's
-    0.1 dB at 1280 panels (2 % in amplitude, where the collocation path is at 2.6 %)."""
+def _check_amplitudes(got, refs, db, rel):
+    for f, b in zip(got, refs):
+        assert abs(20 * math.log10(abs(f) / abs(b))) < db, (f, b)
+        assert abs(f - b) < rel * abs(b), (f, b, abs(f - b) / abs(b))
+
+
+def test_reference_rigid_spheroid_amplitudes_collocation(ctx):
+    """The amplitudes the reference's tests hard-code for a rigid spheroid
+    (test/extended/bem/spheroid/full3d.jl:9-24) at the reference's own tolerance, 0.1 dB
+    and 1 % (full3d.jl:21-22): the collocation discretisation on 11520 panels (96 x 60;
+    the oracle's error there is 0.85 %), mixed precision."""
     s = _reference_amplitudes()["rigid_spheroid"]
-    nodes, tris = meshes.uv_spheroid(s["a"], s["b"], 32, 20)
+    nodes, tris = meshes.uv_spheroid(s["a"], s["b"], 96, 60)
+    sol = bemgpu.bem(bemgpu.mesh(nodes, tris), bemgpu.Rigid(), s["k"],
+                     incidence_angle=s["incidence_angle"],
+                     incidence_azimuth=s["incidence_azimuth"], ctx=ctx, precision="mixed")
+    got = [sol.far_field(np.array(r["direction"]))[0] for r in s["references"]]
+    sol.close()
+    _check_amplitudes(got, [complex(*r["amplitude"]) for r in s["references"]], 0.1, 0.01)
+
+
+def test_reference_rigid_spheroid_amplitudes(ctx):
+    """The same amplitudes from the Nyström discretisation (the reference's own) on 5120
+    panels (64 x 40, 35840 node unknowns): within the reference's 0.1 dB.  Its amplitude
+    error falls slowly with the flat-facet mesh -- 1.96 %, 1.49 % and 1.23 % at 1280, 2880
+    and 5120 panels (measured on a GB300) -- so 1 % needs about 10^4 panels (a 70 000-node
+    dense system); 1.3 % is the bound asserted here."""
+    s = _reference_amplitudes()["rigid_spheroid"]
+    nodes, tris = meshes.uv_spheroid(s["a"], s["b"], 64, 40)
     surf = bemgpu.mesh(nodes, tris)
     sol = bemgpu.bem(surf, bemgpu.Rigid(), s["k"], incidence_angle=s["incidence_angle"],
                      incidence_azimuth=s["incidence_azimuth"], ctx=ctx,
-                     discretization="nystrom")
-    for r in s["references"]:
-        f = sol.far_field(np.array(r["direction"]))[0]
-        b = complex(*r["amplitude"])
-        assert abs(20 * math.log10(abs(f) / abs(b))) < 0.1
-        assert abs(f - b) < 0.02 * abs(b)
+                     discretization="nystrom", precision="mixed")
+    got = [sol.far_field(np.array(r["direction"]))[0] for r in s["references"]]
     sol.close()
+    _check_amplitudes(got, [complex(*r["amplitude"]) for r in s["references"]], 0.1, 0.013)
+
+
+@pytest.mark.parametrize("heavy", [False, True])
+def test_reference_fluid_sphere_amplitudes_collocation(ctx, heavy):
+    """The reference's hard-coded amplitudes of the gas-filled (g 0.0012, h 0.23) and the
+    heavy (g 1000, h 2) fluid sphere at k a = 1 (sphere/full3d.jl:209-234) at the
+    reference's 0.1 dB and 1 %: the collocation discretisation on 1280 panels."""
+    c = [c for c in _reference_amplitudes()["fluid_sphere"]
+         if c["k"] == 1.0 and (c["g"] > 1) == heavy][0]
+    nodes, tris = meshes.icosphere(1.0, 3)
+    sol = bemgpu.bem(bemgpu.mesh(nodes, tris), bemgpu.FluidFilled(c["g"], c["h"]), c["k"],
+                     incidence_angle=0.0, ctx=ctx, precision="mixed")
+    got = sol.far_field(np.array(c["directions"]))
+    sol.close()
+    _check_amplitudes(got, [complex(x, y) for x, y in c["amplitudes"]], 0.1, 0.01)
 
 
 def test_reference_gas_sphere_amplitudes(ctx):
-    """The reference's hard-coded amplitudes of a gas-filled sphere (g 0.0012, h 0.23, k a
-    = 1; sphere/full3d.jl:209-234): within 0.1 dB and 1.5 % at 1280 panels."""
+    """The gas-filled sphere's amplitudes (g 0.0012, h 0.23, k a = 1) from the Nyström
+    discretisation: 1.07 % / 0.053 dB at 1280 panels, 0.48 % / 0.024 dB at 2880 (measured
+    on a GB300; the 2880-panel solve takes four minutes in FP64, to which the condition
+    guard promotes this system), so 1280 panels with 1.2 % is asserted here."""
     c = [c for c in _reference_amplitudes()["fluid_sphere"] if c["k"] == 1.0 and c["g"] < 1][0]
     nodes, tris = meshes.icosphere(1.0, 3)
     surf = bemgpu.mesh(nodes, tris)
     sol = bemgpu.bem(surf, bemgpu.FluidFilled(c["g"], c["h"]), c["k"], incidence_angle=0.0,
                      ctx=ctx, discretization="nystrom", precision="mixed")
     got = sol.far_field(np.array(c["directions"]))
-    for f, (x, y) in zip(got, c["amplitudes"]):
-        b = complex(x, y)
-        assert abs(20 * math.log10(abs(f) / abs(b))) < 0.1
-        assert abs(f - b) < 0.015 * abs(b)
     sol.close()
+    _check_amplitudes(got, [complex(x, y) for x, y in c["amplitudes"]], 0.1, 0.012)

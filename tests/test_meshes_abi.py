@@ -118,6 +118,11 @@ def test_problem_defaults_follow_reference():
     assert p.refine_tolerance == 1e-13 and p.refine_maxiter == 8
     assert p.condition_guard == pytest.approx(10 * np.finfo(np.float32).eps)
     assert p.equilibrate == 1 and p.formulation == C.FORMULATION_DEFAULT
+    # the reference's _factor_fluid_system defaults (full.jl:364-366)
+    assert p.condition_limit == 512 and p.norm_floor == 0.0
+    o = C.ServerOptions()
+    C.lib().bemgpu_server_options_init(ctypes.byref(o))
+    assert o.max_batch == 64 and o.lanes == 2
 
 
 @pytest.mark.parametrize("kw,msg", [
@@ -130,6 +135,9 @@ def test_problem_defaults_follow_reference():
     (dict(precision="mixed", refinement={"tolerance": math.nan}), "tolerance"),
     (dict(precision="mixed", refinement={"unknown": 1}), "unknown refinement"),
     (dict(incidence_angle=math.nan), "incidence"),
+    (dict(condition_limit=-1), "condition_limit"),
+    (dict(norm_floor=-1.0), "norm_floor"), (dict(norm_floor=math.nan), "norm_floor"),
+    (dict(precision="mixed", norm_floor=1.0), "norm_floor"),
 ])
 def test_bem_argument_errors_before_any_device_work(kw, msg):
     nodes, tris = _tetra()
