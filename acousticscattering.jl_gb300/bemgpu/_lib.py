@@ -169,6 +169,8 @@ SIGNATURES = {
                                                    _vp, _i64]),
     "bemgpu_ctx_set_tensor_lu": (ctypes.c_int, [_vp, _i32]),
     "bemgpu_ctx_set_graphs": (ctypes.c_int, [_vp, _i32]),
+    "bemgpu_schwarz_neighbourhoods": (ctypes.c_int, [_dp, _i64, _i64p, _i64, _i32,
+                                                     ctypes.POINTER(ctypes.c_int32)]),
     "bemgpu_ctx_graph_stats": (ctypes.c_int, [_vp, _i64p, _i64p]),
     "bemgpu_debug_cgemm": (ctypes.c_int, [_vp, _i64, _i64, _i32,
                                           ctypes.POINTER(ctypes.c_float),

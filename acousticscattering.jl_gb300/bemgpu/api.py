@@ -470,9 +470,10 @@ class BEMSolution:
         return self.body.n_panels
 
     def region_traces(self, rhs: int = 0):
-        """Coupled regions: total pressure p and flux unknown v on every panel, surfaces in
-        order (the interior normal derivative is density_i v)."""
-        n = self.n_panels
+        """Coupled regions: total pressure p and flux unknown v at every unknown location
+        (panel, or quadrature node for the Nyström discretisation), surfaces in order (the
+        interior normal derivative is density_i v)."""
+        n = self.n_nodes
         p = np.zeros(n, dtype=np.complex128)
         v = np.zeros(n, dtype=np.complex128)
         _check(C.lib().bemgpu_region_traces(self.handle, rhs, C.dptr(p), C.dptr(v)),
@@ -675,8 +676,6 @@ def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_az
     if discretization not in C.DISCRETIZATION:
         raise ArgumentError("discretization must be :collocation or :nystrom")
     hm = _hmatrix_options(compression, gmres_kwargs)
-    if discretization != "collocation" and isinstance(surface, (list, tuple)):
-        raise ArgumentError("the Nyström discretisation takes one surface")
     if hm is not None:
         if isinstance(surface, (list, tuple)) or parents is not None:
             raise ArgumentError("hierarchical compression applies to a single surface")
@@ -692,7 +691,8 @@ def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_az
                             incidence_angle=incidence_angle,
                             incidence_azimuth=incidence_azimuth, formulation=formulation,
                             precision=precision, equilibrate=equilibrate,
-                            refinement=refinement, assembly=assembly, ctx=ctx)
+                            refinement=refinement, assembly=assembly, ctx=ctx,
+                            discretization=discretization)
     if parents is not None:
         raise ArgumentError("parents applies to lists of surfaces and materials")
     if not isinstance(surface, Mesh):
@@ -713,7 +713,8 @@ def bem(surface: Mesh, boundary, k, *, incidence_angle=math.pi / 2, incidence_az
 
 
 def _bem_regions(surfaces, materials, k, *, parents, incidence_angle, incidence_azimuth,
-                 formulation, precision, equilibrate, refinement, assembly, ctx):
+                 formulation, precision, equilibrate, refinement, assembly, ctx,
+                 discretization="collocation"):
     ctx = ctx or context()
     count = len(surfaces)
     if count == 0:
@@ -737,7 +738,7 @@ def _bem_regions(surfaces, materials, k, *, parents, incidence_angle, incidence_
     # the problem fields that apply (boundary and contrasts are per region)
     p = _problem(FluidFilled(1.0, 1.0), float(k), formulation=formulation,
                  precision=precision, equilibrate=equilibrate, refinement=refinement,
-                 assembly=assembly)
+                 assembly=assembly, discretization=discretization)
     handles = (ctypes.c_void_p * count)(*[s_.handle(ctx) for s_ in surfaces])
     dens = np.array([m.density_contrast for m in materials], dtype=np.float64)
     speeds = np.array([m.soundspeed_contrast for m in materials], dtype=np.float64)
@@ -748,7 +749,7 @@ def _bem_regions(surfaces, materials, k, *, parents, incidence_angle, incidence_
                                        par, ctypes.byref(p), 1, C.dptr(inc), ctypes.byref(out)),
            ctx.handle)
     return BEMSolution(ctx, out, list(surfaces), list(materials), float(k), [incidence_angle],
-                       [incidence_azimuth])
+                       [incidence_azimuth], discretization=discretization)
 
 
 def factor_batch(items, ctx: Context | None = None):

@@ -584,7 +584,6 @@ int nystrom_mesh(bemgpu_ctx* c, MeshData* m, std::shared_ptr<MeshData>* out) {
     *out = m->node_mesh;
     return BEMGPU_OK;
   }
-  if (m->surf.p) return fail(c, BEMGPU_EINVAL, "the Nyström discretisation takes one surface");
   auto d = std::make_shared<MeshData>();
   d->c = c;
   d->n = (int64_t)kNyNodes * m->n;
@@ -624,6 +623,14 @@ int nystrom_mesh(bemgpu_ctx* c, MeshData* m, std::shared_ptr<MeshData>* out) {
   }
   TRY(upload(c, d->panels_h, &d->panels));
   TRY(upload(c, recf, &d->panelsf));
+  if (m->surf.p) {  // union of several surfaces: the surface of every node, node offsets
+    std::vector<int32_t> sn((size_t)d->n);
+    for (size_t s = 0; s + 1 < m->offsets.size(); ++s)
+      for (int64_t t = m->offsets[s]; t < m->offsets[s + 1]; ++t)
+        for (int q = 0; q < kNyNodes; ++q) sn[(size_t)(t * kNyNodes + q)] = (int32_t)s;
+    TRY(upload(c, sn, &d->surf));
+    for (int64_t o : m->offsets) d->offsets.push_back(o * kNyNodes);
+  }
   m->node_mesh = d;
   *out = d;
   return BEMGPU_OK;
@@ -886,7 +893,8 @@ int assemble_nystrom(bemgpu_ctx* c, FactorData* f) {
   const Launch L = c->launch();
   MeshData* m = f->mesh.get();
   const int64_t N = m->n;
-  const int32_t fluid = f->kind == kAsmMuller ? 1 : f->kind == kAsmFluidCBIE ? 2 : 0;
+  const int32_t fluid = f->kind == kAsmMuller ? 1 : f->kind == kAsmFluidCBIE ? 2
+                       : f->kind == kAsmRegion ? (f->region_cbie ? 4 : 3) : 0;
   f->n = N;
   f->N = fluid ? 2 * N : N;
   f->a32 = false;
@@ -915,6 +923,10 @@ int assemble_nystrom(bemgpu_ctx* c, FactorData* f) {
     I.A = f->A.as<double>();
     I.trace_i = scratch.as<double>() + tr_doubles;
     I.part = scratch.as<double>() + 2 * tr_doubles;
+    if (fluid >= 3) {  // coupled regions: surfaces of the nodes, coupling table
+      I.surf = m->surf.as<int32_t>();
+      I.region = f->region_tab.as<RegionTable>();
+    }
   } else {
     // rigid: system M1, rhs M2; pressure release: system M2, rhs M1
     I.M1 = (f->rhs_is_m2 ? f->A : f->Mrhs).as<double>();
@@ -1479,16 +1491,39 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
     if (tiles[q] > 0) launch_tc_cgemm(L, Dgem.as<TcGemmInst>() + q * ni, ni, tiles[q], red);
   };
   auto any = [&](int64_t st, int ph) { return tiles[(size_t)st * kNGem + ph] > 0; };
+  // CTAs per instance of the panel kernel (its thread-block cluster: 2, 4 or 8; every
+  // choice gives the same bits, rows are only partitioned differently).  Tuned per shape
+  // class (instances, log2 of the largest order) on the first factorisation of that class:
+  // the first six panels run the candidates in the order 2 4 8 8 4 2, so that the linear
+  // decrease of the panels' work cancels out of each candidate's two-panel time.
+  const std::string cs_key = "getf2/" + std::to_string(ni) + "/" + std::to_string(log2_bucket(nmax));
+  int cs_pick = 0;  // 0: the batch-size rule
+  bool cs_tune = false;
+  {
+    auto it = c->tuned.find(cs_key);
+    if (it != c->tuned.end())
+      cs_pick = it->second;
+    else if (c->autotune && !c->prof && !G && nmax >= 6 * kPanelNB)
+      cs_tune = true;
+  }
+  static const int kCsOrder[6] = {2, 4, 8, 8, 4, 2};
+  cudaEvent_t cs_ev[7] = {};
+  if (cs_tune)
+    for (auto& e : cs_ev) cudaEventCreate(&e);
+  int panel = 0;
   auto factor_half = [&](int64_t H) {
     const int64_t st = H / SB;
     const int h = (int)((H % SB) / HB);
-    for (int64_t k0 = H; k0 < H + HB && k0 < nmax; k0 += kPanelNB) {
+    for (int64_t k0 = H; k0 < H + HB && k0 < nmax; k0 += kPanelNB, ++panel) {
       {
-        // cluster size by the batch-size rule: timing the candidates (on scratch copies
-        // or in place on successive panels) chose sizes that were slower over a whole
-        // batch (152 vs 139 ms per 64 x 10240 factorisation)
         Prof pr(c, "getf2");
-        launch_getf2(L, dm, ni, k0, kPanelNB, 1, 0);
+        if (cs_tune && panel < 6) {
+          cudaEventRecord(cs_ev[panel], c->stream);
+          launch_getf2(L, dm, ni, k0, kPanelNB, 1, kCsOrder[panel]);
+          cudaEventRecord(cs_ev[panel + 1], c->stream);
+        } else {
+          launch_getf2(L, dm, ni, k0, kPanelNB, 1, cs_pick);
+        }
       }
       {
         Prof pr(c, "laswp");
@@ -1592,6 +1627,13 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
   }
   CUDA_TRY(c, cudaGetLastError());
   TRY(check_device_error(c));
+  if (cs_tune) {  // the stream is idle: read the six panel times
+    float t[6] = {0};
+    for (int q = 0; q < 6; ++q) cudaEventElapsedTime(&t[q], cs_ev[q], cs_ev[q + 1]);
+    for (auto& e : cs_ev) cudaEventDestroy(e);
+    const float t2 = t[0] + t[5], t4 = t[1] + t[4], t8 = t[2] + t[3];
+    c->tuned[cs_key] = (t2 <= t4 && t2 <= t8) ? 2 : (t4 <= t8 ? 4 : 8);
+  }
   return BEMGPU_OK;
 }
 
@@ -2947,6 +2989,12 @@ void lane_loop(bemgpu_server* S, int li) {
 // ===================================================================== C ABI
 extern "C" {
 
+namespace {
+// (defined with the hierarchical-matrix build below, inside this extern "C" region)
+void ras_neighbourhoods(const std::vector<double>& rec, int64_t ne, int count,
+                        std::vector<int32_t>* ptr, std::vector<int32_t>* els);
+}  // namespace
+
 const char* bemgpu_version(void) { return "bemgpu 0.1.0 (sm_103a)"; }
 
 const char* bemgpu_status_string(int s) {
@@ -2981,6 +3029,31 @@ void bemgpu_problem_init(bemgpu_problem* p) {
   p->near_eta = 2.0;
   p->condition_limit = 512;
   p->norm_floor = 0.0;
+}
+
+int bemgpu_schwarz_neighbourhoods(const double* nodes, int64_t n_nodes, const int64_t* triangles,
+                                  int64_t n_triangles, int32_t count, int32_t* out) {
+  if (!nodes || !triangles || !out || n_triangles <= 0 || count <= 0)
+    return fail(nullptr, BEMGPU_EINVAL, "invalid argument");
+  std::string e;
+  double res = 0.0;
+  int s = validate_surface(nodes, n_nodes, triangles, n_triangles, &res, &e);
+  if (s != BEMGPU_OK) return fail(nullptr, s, e);
+  std::vector<double> rec, verts;
+  std::vector<float> recf;
+  double center[3];
+  build_panels(nodes, triangles, n_triangles, &rec, &recf, &verts, center);
+  // node records of the Nyström node set: only the elements' first (centroid) node is read
+  std::vector<double> nrec((size_t)n_triangles * kNyNodes * kPanelDoubles, 0.0);
+  for (int64_t t = 0; t < n_triangles; ++t)
+    for (int a = 0; a < 3; ++a)
+      nrec[(size_t)t * kNyNodes * kPanelDoubles + a] = rec[(size_t)t * kPanelDoubles + 8 + a];
+  std::vector<int32_t> ptr, els;
+  ras_neighbourhoods(nrec, n_triangles, count, &ptr, &els);
+  const int64_t m = std::min<int64_t>(count, n_triangles);
+  for (int64_t t = 0; t < n_triangles; ++t)
+    for (int64_t q = 0; q < m; ++q) out[t * m + q] = els[(size_t)ptr[t] + q];
+  return BEMGPU_OK;
 }
 
 int bemgpu_mesh_validate(const double* nodes, int64_t n_nodes, const int64_t* triangles,
@@ -3307,11 +3380,16 @@ struct HmData {
   // axis, where restarted GMRES stalls without it)
   Buf ny_pinv;
   int ny_op = -1;
+  // Nyström rigid systems: restricted additive Schwarz over element neighbourhoods
+  // (nystrom.cu), the own-node rows of each neighbourhood inverse in ny_w
+  bool ny_ras = false;
+  Buf ny_nbptr, ny_nbel, ny_woff, ny_w;
   bemgpu_hmatrix_stats st{};
   size_t bytes() const {
     size_t b = leaf_lo.bytes + leaf_ptr.bytes + leaf_ent.bytes + dn.bytes + D1.bytes +
                D2.bytes + vt_items.bytes + lb_items.bytes;
     for (int o = 0; o < 2; ++o) b += lr[o].bytes + U[o].bytes + V[o].bytes;
+    b += ny_pinv.bytes + ny_nbptr.bytes + ny_nbel.bytes + ny_woff.bytes + ny_w.bytes;
     return b;
   }
   size_t scratch_bytes(int32_t nr) const {  // T, P (and Xf) of a product over nr vectors
@@ -3365,6 +3443,69 @@ int check_hm_options(bemgpu_ctx* c, const bemgpu_hmatrix_options& o) {
 
 // Cluster tree and blocks on the host, cross approximation of both operators, full
 // blocks (regular kernel + near kernel into block storage), product lists.
+// Elements per Schwarz neighbourhood of the Nyström rigid system: measured with the
+// oracle on the 1280-panel sphere at k a = 1.6, GMRES steps to 1e-6 fall from 636
+// (unpreconditioned) to 159, 77 and 52 with 32, 48 and 64 nearest elements (20 is worse
+// than none: 1649); 48 keeps the local systems at 336 nodes.
+constexpr int kRasNeighbours = 48;
+
+// The `count` elements nearest to every element (distances between the elements'
+// centroid nodes, ties by index), the element itself first: a uniform grid over the
+// centroids searched in growing shells of cells until the count-th distance is covered.
+void ras_neighbourhoods(const std::vector<double>& rec, int64_t ne, int count,
+                        std::vector<int32_t>* ptr, std::vector<int32_t>* els) {
+  count = (int)std::min<int64_t>(count, ne);
+  std::vector<double> cx((size_t)ne * 3);
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t e = 0; e < ne; ++e)
+    for (int a = 0; a < 3; ++a) {
+      const double v = rec[(size_t)e * kNyNodes * kPanelDoubles + a];
+      cx[3 * e + a] = v;
+      lo[a] = std::min(lo[a], v);
+      hi[a] = std::max(hi[a], v);
+    }
+  const double ext = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-300});
+  const int g = (int)std::max<double>(1.0, std::ceil(std::cbrt((double)ne)));
+  const double h = ext / g * (1.0 + 1e-12);
+  auto cell = [&](int64_t e, int a) {
+    return std::min(g - 1, std::max(0, (int)((cx[3 * e + a] - lo[a]) / h)));
+  };
+  std::vector<std::vector<int32_t>> grid((size_t)g * g * g);
+  for (int64_t e = 0; e < ne; ++e)
+    grid[((size_t)cell(e, 0) * g + cell(e, 1)) * g + cell(e, 2)].push_back((int32_t)e);
+  ptr->assign(1, 0);
+  els->clear();
+  els->reserve((size_t)ne * count);
+  std::vector<std::pair<double, int32_t>> cand;
+  for (int64_t e = 0; e < ne; ++e) {
+    const int ci = cell(e, 0), cj = cell(e, 1), ck = cell(e, 2);
+    cand.clear();
+    for (int R = 0;; ++R) {
+      for (int i = ci - R; i <= ci + R; ++i)
+        for (int j = cj - R; j <= cj + R; ++j)
+          for (int k = ck - R; k <= ck + R; ++k) {
+            if (std::max({std::abs(i - ci), std::abs(j - cj), std::abs(k - ck)}) != R) continue;
+            if (i < 0 || j < 0 || k < 0 || i >= g || j >= g || k >= g) continue;
+            for (int32_t f : grid[((size_t)i * g + j) * g + k]) {
+              const double dx = cx[3 * f] - cx[3 * e], dy = cx[3 * f + 1] - cx[3 * e + 1],
+                           dz = cx[3 * f + 2] - cx[3 * e + 2];
+              cand.emplace_back(dx * dx + dy * dy + dz * dz, f);
+            }
+          }
+      if ((int)cand.size() >= count) {
+        std::nth_element(cand.begin(), cand.begin() + (count - 1), cand.end());
+        const double covered = (double)R * h;
+        if (cand[count - 1].first <= covered * covered || R >= g) break;
+      } else if (R >= g) {
+        break;
+      }
+    }
+    std::sort(cand.begin(), cand.end());
+    for (int q = 0; q < count; ++q) els->push_back(cand[q].second);
+    ptr->push_back((int32_t)els->size());
+  }
+}
+
 int hm_build(bemgpu_ctx* c, MeshData* m, const bemgpu_problem& p, int kind,
              const bemgpu_hmatrix_options& o, HmData* H) {
   const Launch L = c->launch();
@@ -3699,6 +3840,58 @@ int hm_build(bemgpu_ctx* c, MeshData* m, const bemgpu_problem& p, int kind,
       for (int32_t v : st)
         if (v) return fail(c, BEMGPU_ESINGULAR, "singular element block of the node system");
       H->ny_op = 1;
+    } else if (p.boundary == BEMGPU_RIGID) {  // the system operator is M1: Schwarz
+      const int64_t ne = n / kNyNodes;
+      std::vector<int32_t> nptr, nel;
+      ras_neighbourhoods(m->panels_h, ne, kRasNeighbours, &nptr, &nel);
+      std::vector<int64_t> woff((size_t)ne + 1, 0);
+      int32_t max_len = 0;
+      for (int64_t e = 0; e < ne; ++e) {
+        const int32_t len = kNyNodes * (nptr[e + 1] - nptr[e]);
+        max_len = std::max(max_len, len);
+        woff[e + 1] = woff[e] + (int64_t)kNyNodes * len;
+      }
+      TRY(upload(c, nptr, &H->ny_nbptr));
+      TRY(upload(c, nel, &H->ny_nbel));
+      TRY(upload(c, woff, &H->ny_woff));
+      TRY(alloc(c, (size_t)std::max<int64_t>(1, woff[ne]) * 8, &H->ny_w));
+      // one local system per CTA, about one wave of them at a time (the working set of
+      // the eliminations then stays in L2)
+      const int64_t slots = std::min<int64_t>(ne, 2 * (int64_t)device_sm_count());
+      const int64_t stride = 2 * (int64_t)max_len * (max_len + kNyNodes);  // floats
+      Buf work;
+      TRY(alloc(c, (size_t)slots * stride * 4, &work));
+      CUDA_TRY(c, cudaMemsetAsync(status.p, 0, status.bytes, c->stream));
+      NyPrec B{};
+      B.iperm = pc->iperm.as<int32_t>();
+      B.dst = pc->ny_dst.as<int64_t>();
+      B.D = H->D1.p;
+      B.n = n;
+      B.f32 = H->f32 ? 1 : 0;
+      B.status = status.as<int32_t>();
+      B.ras = 1;
+      B.W = H->ny_w.as<float>();
+      B.woff = H->ny_woff.as<int64_t>();
+      B.nb_ptr = H->ny_nbptr.as<int32_t>();
+      B.nb_el = H->ny_nbel.as<int32_t>();
+      B.recf = m->panelsf.as<float>();
+      B.op = 0;
+      B.k = (float)k;
+      B.a_re = (float)a_re;
+      B.a_im = (float)a_im;
+      B.work = work.as<float>();
+      B.work_stride = stride;
+      {
+        Prof pr(c, "hm_precond");
+        for (int64_t e0 = 0; e0 < ne; e0 += slots)
+          launch_nystrom_ras_build(L, B, e0, std::min(slots, ne - e0), max_len);
+      }
+      CUDA_TRY(c, cudaGetLastError());
+      TRY(download(c, status, &st, (size_t)std::max<int64_t>(1, ne)));
+      for (int32_t v : st)
+        if (v) return fail(c, BEMGPU_ESINGULAR, "singular neighbourhood of the node system");
+      H->ny_op = 0;
+      H->ny_ras = true;
     }
   }
   bemgpu_hmatrix_stats& S = H->st;
@@ -3730,7 +3923,7 @@ int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x,
   // bytes per right-hand side: Krylov basis, x / w vectors, Hessenberg matrix, partial
   // dots, history, the products' scratch, rotations, and the preconditioned solve's
   // P^-1 product (n complex) when the element-block preconditioner applies
-  const bool precond = op == H.ny_op && H.ny_pinv.p;
+  const bool precond = op == H.ny_op && (H.ny_pinv.p || H.ny_ras);
   const size_t per = ((size_t)(R + 1) * n + 2 * (size_t)n) * 16 + (size_t)(R + 1) * R * 16 +
                      (size_t)chunks * (R + 1) * 16 + (size_t)mi * 8 + H.scratch_bytes(1) +
                      (size_t)(4 * R + 8) * 16 + (precond ? (size_t)n * 16 : 0);
@@ -3765,7 +3958,7 @@ int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x,
     const double* bg = b + 2 * (size_t)r0 * n;
     // right preconditioning (Nyström pressure-release systems): GMRES runs on A P^-1 with
     // the iterate y in W.x; every product takes P^-1 first, and x = P^-1 y at the end
-    const bool prec = op == H.ny_op && H.ny_pinv.p;
+    const bool prec = op == H.ny_op && (H.ny_pinv.p || H.ny_ras);
     NyPrec Pc{};
     Buf pt;
     if (prec) {
@@ -3773,6 +3966,13 @@ int hm_gmres(bemgpu_ctx* c, const HmData& H, int op, const double* b, double* x,
       Pc.Pinv = H.ny_pinv.as<double>();
       Pc.iperm = H.pc->iperm.as<int32_t>();
       Pc.n = n;
+      if (H.ny_ras) {
+        Pc.ras = 1;
+        Pc.W = H.ny_w.as<float>();
+        Pc.woff = H.ny_woff.as<int64_t>();
+        Pc.nb_ptr = H.ny_nbptr.as<int32_t>();
+        Pc.nb_el = H.ny_nbel.as<int32_t>();
+      }
     }
     CUDA_TRY(c, cudaMemsetAsync(xg, 0, (size_t)g * n * 16, c->stream));
     CUDA_TRY(c, cudaMemcpyAsync(w.p, bg, (size_t)g * n * 16, cudaMemcpyDeviceToDevice, c->stream));
@@ -4179,8 +4379,7 @@ int bemgpu_region_solve(bemgpu_ctx* c, int32_t count, const bemgpu_mesh* const* 
     if (std::fabs(problem->near_eta - surfaces[i]->d->eta) > 0)
       return fail(c, BEMGPU_EINVAL, "near_eta differs from the mesh's (upload with that eta)");
   }
-  if (problem->discretization != BEMGPU_COLLOCATION)
-    return fail(c, BEMGPU_EINVAL, "coupled regions use the collocation discretisation");
+  const bool nystrom = problem->discretization == BEMGPU_NYSTROM;
   bemgpu_problem q = *problem;
   q.boundary = BEMGPU_FLUID;
   q.density_contrast = q.soundspeed_contrast = 1.0;  // per region below
@@ -4240,19 +4439,27 @@ int bemgpu_region_solve(bemgpu_ctx* c, int32_t count, const bemgpu_mesh* const* 
         ++C.count;
       }
     }
-  std::vector<int8_t> outer((size_t)un->n, 0);
-  for (int32_t i = 0; i < count; ++i)
-    if (parents[i] == 0)
-      for (int64_t p = un->offsets[i]; p < un->offsets[i + 1]; ++p) outer[(size_t)p] = 1;
   auto f = std::make_shared<FactorData>();
   f->c = c;
-  f->mesh = un;
   f->prob = q;
   f->kind = kAsmRegion;
   f->region_cbie = tab.cbie != 0;
   f->mixed = q.precision == BEMGPU_MIXED;
-  f->fp32_regular = q.assembly == BEMGPU_ASSEMBLY_SINGLE ||
-                    (q.assembly == BEMGPU_ASSEMBLY_DEFAULT && f->mixed);
+  if (nystrom) {  // the quadrature nodes of the union (7 per panel, surface order)
+    f->nystrom = true;
+    f->fp32_regular = false;
+    f->base_mesh = un;
+    TRY(nystrom_mesh(c, un.get(), &f->mesh));
+  } else {
+    f->mesh = un;
+    f->fp32_regular = q.assembly == BEMGPU_ASSEMBLY_SINGLE ||
+                      (q.assembly == BEMGPU_ASSEMBLY_DEFAULT && f->mixed);
+  }
+  const MeshData* um = f->mesh.get();
+  std::vector<int8_t> outer((size_t)um->n, 0);
+  for (int32_t i = 0; i < count; ++i)
+    if (parents[i] == 0)
+      for (int64_t p = um->offsets[i]; p < um->offsets[i + 1]; ++p) outer[(size_t)p] = 1;
   std::vector<RegionTable> tv{tab};
   TRY(upload(c, tv, &f->region_tab));
   TRY(upload(c, outer, &f->outer));
@@ -4422,6 +4629,10 @@ int bemgpu_pressure_region(bemgpu_solution* sol, int32_t rhs, int64_t npts, cons
   const bool fluid = s->boundary == BEMGPU_FLUID || s->region;
   if (field == BEMGPU_FIELD_INTERIOR && !fluid)
     return fail(c, BEMGPU_EINVAL, "interior field requires a fluid-filled body");
+  if (s->mesh->nystrom && s->region)
+    return fail(c, BEMGPU_EINVAL,
+                "pressure of a Nyström coupled-region solution is not built (the collocation "
+                "discretisation's region solutions answer it)");
   if (s->mesh->nystrom) return nystrom_pressure(c, s, rhs, npts, points, field, out);
   std::vector<double> pts(points, points + 3 * npts);
   std::vector<double> dir(s->dirs.begin() + 3 * rhs, s->dirs.begin() + 3 * rhs + 3);

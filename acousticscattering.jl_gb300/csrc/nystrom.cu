@@ -28,6 +28,7 @@
 // the two system matrices and the combined defect sums, FP64-issue-bound), k_ny_correct
 // (one thread per element: Householder QR of the 14 x 9 trace matrix, 7 fits, the
 // corrections).
+#include <climits>
 #include <cmath>
 
 #include "nystrom.cuh"
@@ -484,6 +485,237 @@ __global__ void __launch_bounds__(kNyCorrT) k_ny_correct_fluid(NyInst I) {
   }
 }
 
+// ------------------------------------------------------------------ coupled regions
+// Coupled fluid regions on the nodes (the reference's regions.jl:189-236 with its Nyström
+// operators): the panel path's region block algebra -- for a target on surface si and a
+// source on sj, every region the two surfaces share contributes its node operators at
+// its wavenumber with its sign and density (RegionCoef) -- and the element corrections of
+// each surface's own operators at the wavenumbers of its two sides.  Side 0 is the region
+// outside a surface (its coupling entry with eq = 0), side 1 the region it encloses.
+
+// The coupling entry of surface s with itself on `side` (eq = side).
+__device__ __forceinline__ int self_entry(const RegionTable& RT, int s, int side) {
+  const RegionCoef& C = RT.c[s * kMaxRegions + s];
+  for (int q = 0; q < C.count; ++q)
+    if (C.eq[q] == side) return q;
+  return 0;
+}
+
+// Interpolant traces at the wavenumber of each node's side `side`.
+__global__ void k_ny_traces_regions(NyInst I, int side) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= I.n) return;
+  const RegionTable& RT = *I.region;
+  const int s = I.surf[j];
+  const double k = RT.kr[RT.c[s * kMaxRegions + s].kidx[self_entry(RT, s, side)]];
+  const double* r = I.nodes + j * kPanelDoubles;
+  z2* tr = reinterpret_cast<z2*>(side ? I.trace_i : I.trace);
+  for (int t = 0; t < kNyBasis; ++t) {
+    const double* d = I.dirs + 3 * t;
+    const double ph = k * (d[0] * r[0] + d[1] * r[1] + d[2] * r[2]);
+    const double kdn = k * (d[0] * r[3] + d[1] * r[4] + d[2] * r[5]);
+    double sn, cs;
+    sincos(ph, &sn, &cs);
+    tr[(int64_t)t * I.n + j] = {cs, sn};
+    tr[(int64_t)(kNyBasis + t) * I.n + j] = {-kdn * sn, kdn * cs};
+  }
+}
+
+// Defect sums of one source node on side SIDE (slots with compile-time indices, so that
+// the accumulators stay in registers).
+template <bool MULLER, int SIDE>
+__device__ __forceinline__ void ny_region_defects(z2* acc, z2 S, z2 D, z2 K, z2 H,
+                                                  const z2 (*tr)[kNyTile], int jj) {
+  constexpr int sd = MULLER ? 2 * SIDE : SIDE;
+#pragma unroll
+  for (int s = 0; s < kNyBasis; ++s) {
+    const z2 u = tr[2 * kNyBasis * SIDE + s][jj];
+    const z2 fl = tr[2 * kNyBasis * SIDE + kNyBasis + s][jj];
+    zfma(acc[sd * kNyBasis + s], S, fl);
+    zfms(acc[sd * kNyBasis + s], D, u);
+    if (MULLER) {
+      zfma(acc[(sd + 1) * kNyBasis + s], K, fl);
+      zfms(acc[(sd + 1) * kNyBasis + s], H, u);
+    }
+  }
+}
+
+// Every node pair once (the layout of k_ny_assemble_fluid); defect slots: Mueller 2 side +
+// (0 S/D, 1 K'/H), CBIE side.
+template <bool MULLER>
+__global__ void __launch_bounds__(kNyRows) k_ny_assemble_regions(NyInst I) {
+  constexpr int ND = MULLER ? 4 : 2;
+  const int64_t n = I.n, lda = 2 * I.n;
+  const int64_t i = (int64_t)blockIdx.x * kNyRows + threadIdx.x;
+  const int64_t c0 = (int64_t)blockIdx.y * I.chunk_cols;
+  const int64_t c1 = min(n, c0 + I.chunk_cols);
+  __shared__ double s_node[kNyTile][7];
+  __shared__ z2 s_tr[4 * kNyBasis][kNyTile];  // u, du/dn on side 0, then on side 1
+  __shared__ int32_t s_surf[kNyTile];
+  const RegionTable& RT = *I.region;
+  const bool row = i < n;
+  double xi[3] = {0, 0, 0}, ni[3] = {0, 0, 0};
+  int si = 0;
+  if (row) {
+    const double* r = I.nodes + i * kPanelDoubles;
+    for (int d = 0; d < 3; ++d) {
+      xi[d] = r[d];
+      ni[d] = r[3 + d];
+    }
+    si = I.surf[i];
+  }
+  z2 acc[ND * kNyBasis];
+#pragma unroll
+  for (int t = 0; t < ND * kNyBasis; ++t) acc[t] = {0.0, 0.0};
+  const z2* tr0 = reinterpret_cast<const z2*>(I.trace);
+  const z2* tr1 = reinterpret_cast<const z2*>(I.trace_i);
+  z2* A = reinterpret_cast<z2*>(I.A);
+  for (int64_t t0 = c0; t0 < c1; t0 += kNyTile) {
+    const int cnt = (int)min((int64_t)kNyTile, c1 - t0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < kNyTile * 7; e += kNyRows) {
+      const int jj = e / 7, f = e % 7;
+      s_node[jj][f] = jj < cnt ? I.nodes[(t0 + jj) * kPanelDoubles + f] : 0.0;
+    }
+    for (int e = threadIdx.x; e < kNyTile * 4 * kNyBasis; e += kNyRows) {
+      const int jj = e % kNyTile, t = e / kNyTile;
+      const z2* src = t < 2 * kNyBasis ? tr0 : tr1;
+      const int tt = t < 2 * kNyBasis ? t : t - 2 * kNyBasis;
+      s_tr[t][jj] = jj < cnt ? src[(int64_t)tt * n + t0 + jj] : z2{0.0, 0.0};
+    }
+    for (int e = threadIdx.x; e < kNyTile; e += kNyRows) s_surf[e] = e < cnt ? I.surf[t0 + e] : 0;
+    __syncthreads();
+    if (!row) continue;
+    for (int jj = 0; jj < cnt; ++jj) {
+      const int64_t j = t0 + jj;
+      z2 a11 = {0.0, 0.0}, a12 = {0.0, 0.0}, a21 = {0.0, 0.0}, a22 = {0.0, 0.0};
+      if (j == i) {
+        a11 = {MULLER ? 1.0 : 0.5, 0.0};
+        a21 = {MULLER ? 0.0 : 0.5, 0.0};
+        a22 = {MULLER ? 1.0 : 0.0, 0.0};
+      } else {
+        const int sj = s_surf[jj];
+        const RegionCoef& C = RT.c[si * kMaxRegions + sj];
+        const double dx = xi[0] - s_node[jj][0], dy = xi[1] - s_node[jj][1],
+                     dz = xi[2] - s_node[jj][2];
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
+        const double ir = 1.0 / r;
+        const double w = s_node[jj][6];
+        const double dny = dx * s_node[jj][3] + dy * s_node[jj][4] + dz * s_node[jj][5];
+        const double dnx = dx * ni[0] + dy * ni[1] + dz * ni[2];
+        const double nn = ni[0] * s_node[jj][3] + ni[1] * s_node[jj][4] + ni[2] * s_node[jj][5];
+        const double fd = -dny * ir * w, fk = dnx * ir * w;
+        const double f2 = dnx * dny * ir * ir, f1 = nn * ir;
+        for (int q = 0; q < C.count; ++q) {
+          const double kk = RT.kr[C.kidx[q]];
+          double sn, cs;
+          sincos(kk * r, &sn, &cs);
+          const double gs = kInv4Pi * ir;
+          const z2 G = {cs * gs, sn * gs};
+          const z2 G1 = zmul(G, z2{-ir, kk});
+          const z2 S = {G.x * w, G.y * w};
+          const z2 D = {G1.x * fd, G1.y * fd};
+          z2 K = {0.0, 0.0}, H = {0.0, 0.0};
+          if (MULLER) {
+            const z2 G2 = zmul(G, z2{2.0 * ir * ir - kk * kk, -2.0 * kk * ir});
+            K = {G1.x * fk, G1.y * fk};
+            H = {-((G2.x - G1.x * ir) * f2 + G1.x * f1) * w,
+                 -((G2.y - G1.y * ir) * f2 + G1.y * f1) * w};
+          }
+          const double sg = C.sign[q], rho = C.rho[q];
+          if (MULLER) {
+            a11 = {a11.x + sg * D.x, a11.y + sg * D.y};
+            a12 = {a12.x - sg * rho * S.x, a12.y - sg * rho * S.y};
+            a21 = {a21.x + sg / rho * H.x, a21.y + sg / rho * H.y};
+            a22 = {a22.x - sg * K.x, a22.y - sg * K.y};
+          } else if (C.eq[q] == 0) {
+            a11 = {a11.x + sg * D.x, a11.y + sg * D.y};
+            a12 = {a12.x - sg * rho * S.x, a12.y - sg * rho * S.y};
+          } else {
+            a21 = {a21.x + sg * D.x, a21.y + sg * D.y};
+            a22 = {a22.x - sg * rho * S.x, a22.y - sg * rho * S.y};
+          }
+          if (sj == si) {  // the defects of surface si's identities on this side
+            if (C.eq[q] == 0)
+              ny_region_defects<MULLER, 0>(acc, S, D, K, H, s_tr, jj);
+            else
+              ny_region_defects<MULLER, 1>(acc, S, D, K, H, s_tr, jj);
+          }
+        }
+      }
+      A[i + j * lda] = a11;
+      A[i + (n + j) * lda] = a12;
+      A[(n + i) + j * lda] = a21;
+      A[(n + i) + (n + j) * lda] = a22;
+    }
+  }
+  if (!row) return;
+  z2* part = reinterpret_cast<z2*>(I.part);
+#pragma unroll
+  for (int t = 0; t < ND * kNyBasis; ++t)
+    part[((int64_t)blockIdx.y * ND * kNyBasis + t) * n + i] = acc[t];
+}
+
+// One thread per element: a fit per side; each defect's weights enter the blocks with the
+// coefficients of the side's region for the surface with itself (sign sg, density rho):
+//   S/D identity:  pressure weights x sg, flux weights x sg rho   (Mueller: top rows;
+//                  CBIE: the side's equation rows)
+//   K'/H identity: pressure weights x sg / rho, flux weights x sg (Mueller: bottom rows)
+// which for one surface in the exterior are the coefficients of k_ny_correct_fluid.
+template <bool MULLER>
+__global__ void __launch_bounds__(kNyCorrT) k_ny_correct_regions(NyInst I) {
+  constexpr int ND = MULLER ? 4 : 2;
+  const int64_t e = (int64_t)blockIdx.x * kNyCorrT + threadIdx.x;
+  const int64_t n = I.n, lda = 2 * I.n;
+  if (e >= n / kNyNodes) return;
+  const RegionTable& RT = *I.region;
+  const z2* tr0 = reinterpret_cast<const z2*>(I.trace);
+  const z2* tr1 = reinterpret_cast<const z2*>(I.trace_i);
+  const z2* part = reinterpret_cast<const z2*>(I.part);
+  z2* A = reinterpret_cast<z2*>(I.A);
+  const int64_t b = e * kNyNodes;
+  const int s = I.surf[b];
+  const RegionCoef& C = RT.c[s * kMaxRegions + s];
+  const int q0 = self_entry(RT, s, 0), q1 = self_entry(RT, s, 1);
+  NyFit F0, F1;
+  if (!ny_fit_factor(F0, tr0, n, b) || !ny_fit_factor(F1, tr1, n, b)) {
+    I.status[e] = 1;
+    return;
+  }
+  for (int t = 0; t < kNyNodes; ++t) {
+    const int64_t row = b + t;
+    for (int id = 0; id < ND; ++id) {
+      const int side = MULLER ? (id >> 1) : id;
+      const bool flux = MULLER && (id & 1);
+      const z2* tr = side ? tr1 : tr0;
+      z2 d[kNyBasis];
+      for (int q = 0; q < kNyBasis; ++q) {
+        z2 acc = {0.0, 0.0};
+        for (int c = 0; c < I.n_chunks; ++c) {
+          const z2 p = part[(((int64_t)c * ND + id) * kNyBasis + q) * n + row];
+          acc.x += p.x;
+          acc.y += p.y;
+        }
+        const z2 own = tr[(int64_t)((flux ? kNyBasis : 0) + q) * n + row];
+        d[q] = {acc.x - 0.5 * own.x, acc.y - 0.5 * own.y};
+      }
+      z2 w[kNyFit];
+      ny_fit_solve(side ? F1 : F0, d, w);
+      const int qq = side ? q1 : q0;
+      const double sg = C.sign[qq], rho = C.rho[qq];
+      const int64_t r = (MULLER ? flux : side != 0) ? n + row : row;
+      const double cp = flux ? sg / rho : sg, cf = flux ? sg : sg * rho;
+      for (int j = 0; j < kNyNodes; ++j) {
+        const int64_t col = b + j;
+        z2& Lb = A[r + col * lda];
+        z2& Rb = A[r + (n + col) * lda];
+        Lb = {Lb.x + cp * w[j].x, Lb.y + cp * w[j].y};
+        Rb = {Rb.x + cf * w[kNyNodes + j].x, Rb.y + cf * w[kNyNodes + j].y};
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------------ compressed operators
 template <typename R>
 __global__ void k_ny_hm_diag(NyHm H) {
@@ -600,6 +832,227 @@ __global__ void k_ny_prec_apply(NyPrec P, const double* src, int64_t lds, const 
     for (int j = 0; j < kNyNodes; ++j) zfma(acc, B[t * kNyNodes + j], v[j]);
     d[P.iperm[e * kNyNodes + t]] = acc;
   }
+}
+
+// ------------------------------------------------------------------ Schwarz preconditioner
+// Restricted additive Schwarz for the Burton-Miller node system, whose spectrum spreads as
+// the mesh is refined (plain restarted GMRES needs about 300 steps at 320 panels, 640 at
+// 1280 and more than 1200 at 5120): for every element e, the system restricted to the
+// nodes of e's neighbourhood (its m nearest elements) is factored, and P^-1 r takes, for
+// e's own seven nodes only, the neighbourhood solve of r (Cai and Sarkis, SIAM J. Sci.
+// Comput. 21(2), 1999).  Entries between different elements are the uncorrected node
+// kernel, evaluated in FP32 from the FP32 records; entries within an element are the
+// corrected values of the full-block pool.  The local factorisation is FP32 as well: the
+// preconditioner only steers GMRES, whose residual stays that of the true system.
+
+// Uncorrected entry (i, j), i != j, of operator op (0: M1, 1: M2), FP32.
+__device__ __forceinline__ float2 ny_entry_f32(const NyPrec& P, int64_t i, int64_t j) {
+  const float* ri = P.recf + i * kPanelFloats;
+  const float* rj = P.recf + j * kPanelFloats;
+  const float dx = ri[0] - rj[0], dy = ri[1] - rj[1], dz = ri[2] - rj[2];
+  const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+  const float ir = 1.0f / r;
+  float sn, cs;
+  sincosf(P.k * r, &sn, &cs);
+  const float w = rj[6];
+  const float gs = 0.07957747154594767f * ir;
+  const float Gx = cs * gs, Gy = sn * gs;
+  // G1 = G (-1/r + i k)
+  const float G1x = -Gx * ir - Gy * P.k, G1y = Gx * P.k - Gy * ir;
+  const float dny = dx * rj[3] + dy * rj[4] + dz * rj[5];
+  const float dnx = dx * ri[3] + dy * ri[4] + dz * ri[5];
+  if (P.op == 0) {  // M1 = -D - alpha H
+    // G2 = G ((2/r^2 - k^2) - 2 i k / r)
+    const float ar = 2.0f * ir * ir - P.k * P.k, ai = -2.0f * P.k * ir;
+    const float G2x = Gx * ar - Gy * ai, G2y = Gx * ai + Gy * ar;
+    const float nn = ri[3] * rj[3] + ri[4] * rj[4] + ri[5] * rj[5];
+    const float fd = -dny * ir * w;
+    const float f2 = dnx * dny * ir * ir, f1 = nn * ir;
+    const float Hx = -((G2x - G1x * ir) * f2 + G1x * f1) * w;
+    const float Hy = -((G2y - G1y * ir) * f2 + G1y * f1) * w;
+    return make_float2(-G1x * fd - (P.a_re * Hx - P.a_im * Hy),
+                       -G1y * fd - (P.a_re * Hy + P.a_im * Hx));
+  }
+  const float fk = dnx * ir * w;  // M2 = S + alpha K'
+  const float Kx = G1x * fk, Ky = G1y * fk;
+  return make_float2(Gx * w + (P.a_re * Kx - P.a_im * Ky), Gy * w + (P.a_re * Ky + P.a_im * Kx));
+}
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// One CTA per element: T = (the neighbourhood system)^T with the seven unit columns of
+// e's own nodes appended, Gaussian elimination with partial pivoting (rows by |re| + |im|,
+// first maximum), back substitution; W[t][q] = X[q][t].  T is column-major (L rows, L + 7
+// columns) in the CTA's workspace slot.
+constexpr int kRasT = 256;
+template <typename R>
+__global__ void __launch_bounds__(kRasT) k_ny_ras_build(NyPrec P, int64_t e0) {
+  const int64_t e = e0 + blockIdx.x;
+  const int32_t b0 = P.nb_ptr[e], m = P.nb_ptr[e + 1] - b0;
+  const int L = kNyNodes * m;
+  float2* T = reinterpret_cast<float2*>(P.work + (int64_t)blockIdx.x * P.work_stride);
+  const cx<R>* D = static_cast<const cx<R>*>(P.D);
+  auto node = [&](int q) -> int64_t {
+    return (int64_t)P.nb_el[b0 + q / kNyNodes] * kNyNodes + q % kNyNodes;
+  };
+  // T(a, b) = A(node b, node a)
+  for (int64_t idx = threadIdx.x; idx < (int64_t)L * L; idx += kRasT) {
+    const int a = (int)(idx % L), b = (int)(idx / L);
+    const int64_t i = node(b), j = node(a);
+    float2 v;
+    if (i / kNyNodes == j / kNyNodes) {
+      const cx<R> d = D[P.dst[i * kNyNodes + j % kNyNodes]];
+      v = make_float2((float)d.x, (float)d.y);
+    } else {
+      v = ny_entry_f32(P, i, j);
+    }
+    T[a + (int64_t)b * L] = v;
+  }
+  for (int idx = threadIdx.x; idx < L * kNyNodes; idx += kRasT) {
+    const int a = idx % L, t = idx / L;
+    T[a + (int64_t)(L + t) * L] = make_float2(a == t ? 1.0f : 0.0f, 0.0f);
+  }
+  __shared__ float s_val[kRasT / 32];
+  __shared__ int s_idx[kRasT / 32];
+  __shared__ int s_piv;
+  __shared__ float2 s_x[kNyNodes];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int ncol = L + kNyNodes;
+  for (int c = 0; c < L; ++c) {
+    __syncthreads();
+    // pivot: first row of maximal |re| + |im| in column c, rows c..L-1
+    float bv = -1.0f;
+    int bi = INT_MAX;
+    for (int a = c + threadIdx.x; a < L; a += kRasT) {
+      const float2 v = T[a + (int64_t)c * L];
+      const float mag = fabsf(v.x) + fabsf(v.y);
+      if (mag > bv || (mag == bv && a < bi)) {
+        bv = mag;
+        bi = a;
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const float ov = __shfl_down_sync(0xffffffffu, bv, off);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+      if (ov > bv || (ov == bv && oi < bi)) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      s_val[w] = bv;
+      s_idx[w] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float v = s_val[0];
+      int id = s_idx[0];
+      for (int q = 1; q < kRasT / 32; ++q)
+        if (s_val[q] > v || (s_val[q] == v && s_idx[q] < id)) {
+          v = s_val[q];
+          id = s_idx[q];
+        }
+      s_piv = (v > 0.0f) ? id : -1;
+      if (v <= 0.0f) P.status[e] = 1;
+    }
+    __syncthreads();
+    const int p = s_piv;
+    if (p < 0) return;  // every thread leaves: the neighbourhood system is singular
+    if (p != c)
+      for (int b = c + threadIdx.x; b < ncol; b += kRasT) {
+        const float2 t0 = T[c + (int64_t)b * L];
+        T[c + (int64_t)b * L] = T[p + (int64_t)b * L];
+        T[p + (int64_t)b * L] = t0;
+      }
+    __syncthreads();
+    const float2 piv = T[c + (int64_t)c * L];
+    const float dd = piv.x * piv.x + piv.y * piv.y;
+    const float2 inv = make_float2(piv.x / dd, -piv.y / dd);
+    for (int a = c + 1 + threadIdx.x; a < L; a += kRasT)
+      T[a + (int64_t)c * L] = cmulf(T[a + (int64_t)c * L], inv);
+    __syncthreads();
+    const int rows = L - c - 1;
+    if (rows > 0) {
+      const int64_t cnt = (int64_t)rows * (ncol - c - 1);
+      for (int64_t idx = threadIdx.x; idx < cnt; idx += kRasT) {
+        const int a = c + 1 + (int)(idx % rows);
+        const int b = c + 1 + (int)(idx / rows);
+        const float2 l = T[a + (int64_t)c * L], u = T[c + (int64_t)b * L];
+        float2& t = T[a + (int64_t)b * L];
+        t.x -= l.x * u.x - l.y * u.y;
+        t.y -= l.x * u.y + l.y * u.x;
+      }
+    }
+  }
+  // back substitution with U for the seven right-hand sides
+  for (int a = L - 1; a >= 0; --a) {
+    __syncthreads();
+    if (threadIdx.x < kNyNodes) {
+      const float2 d = T[a + (int64_t)a * L];
+      const float dd = d.x * d.x + d.y * d.y;
+      const float2 y = T[a + (int64_t)(L + threadIdx.x) * L];
+      const float2 x = cmulf(y, make_float2(d.x / dd, -d.y / dd));
+      T[a + (int64_t)(L + threadIdx.x) * L] = x;
+      s_x[threadIdx.x] = x;
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < a * kNyNodes; idx += kRasT) {
+      const int j = idx % a, t = idx / a;
+      const float2 u = T[j + (int64_t)a * L];
+      float2& y = T[j + (int64_t)(L + t) * L];
+      const float2 x = s_x[t];
+      y.x -= u.x * x.x - u.y * x.y;
+      y.y -= u.x * x.y + u.y * x.x;
+    }
+  }
+  __syncthreads();
+  float2* W = reinterpret_cast<float2*>(P.W) + P.woff[e];
+  for (int idx = threadIdx.x; idx < kNyNodes * L; idx += kRasT) {
+    const int t = idx / L, q = idx % L;
+    W[idx] = T[q + (int64_t)(L + t) * L];
+  }
+}
+
+// warp = (element, vector): the neighbourhood's L entries gathered from their permuted
+// positions, the seven own-node rows of W applied, the results written at the own nodes
+__global__ void k_ny_ras_apply(NyPrec P, const double* src, int64_t lds, const int32_t* jptr,
+                               int64_t jstride, double* dst, int64_t ldd, int32_t nr) {
+  const int64_t ne = P.n / kNyNodes;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gw >= ne * nr) return;
+  const int64_t e = gw % ne;
+  const int r = (int)(gw / ne);
+  const z2* s = reinterpret_cast<const z2*>(src) + (int64_t)r * lds +
+                (jptr ? (int64_t)(*jptr) * jstride : 0);
+  z2* d = reinterpret_cast<z2*>(dst) + (int64_t)r * ldd;
+  const int32_t b0 = P.nb_ptr[e], m = P.nb_ptr[e + 1] - b0;
+  const int L = kNyNodes * m;
+  const float2* W = reinterpret_cast<const float2*>(P.W) + P.woff[e];
+  z2 acc[kNyNodes];
+#pragma unroll
+  for (int t = 0; t < kNyNodes; ++t) acc[t] = {0.0, 0.0};
+  for (int q = lane; q < L; q += 32) {
+    const int64_t node = (int64_t)P.nb_el[b0 + q / kNyNodes] * kNyNodes + q % kNyNodes;
+    const z2 v = s[P.iperm[node]];
+#pragma unroll
+    for (int t = 0; t < kNyNodes; ++t) {
+      const float2 wv = W[(int64_t)t * L + q];
+      zfma(acc[t], z2{(double)wv.x, (double)wv.y}, v);
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < kNyNodes; ++t)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      acc[t].x += __shfl_down_sync(0xffffffffu, acc[t].x, off);
+      acc[t].y += __shfl_down_sync(0xffffffffu, acc[t].y, off);
+    }
+  if (lane == 0)
+    for (int t = 0; t < kNyNodes; ++t) d[P.iperm[e * kNyNodes + t]] = acc[t];
 }
 
 // ------------------------------------------------------------------ point evaluation
@@ -770,7 +1223,9 @@ __global__ void __launch_bounds__(kNyPtT) k_ny_pressure(NyPoints P) {
 
 }  // namespace
 
-int32_t nystrom_defects(int32_t fluid) { return fluid == 1 ? 4 : fluid == 2 ? 2 : 1; }
+int32_t nystrom_defects(int32_t fluid) {
+  return (fluid == 1 || fluid == 3) ? 4 : (fluid == 2 || fluid == 4) ? 2 : 1;
+}
 
 int64_t nystrom_scratch_doubles(int64_t n, int32_t n_chunks, int32_t fluid) {
   const int64_t traces = (fluid ? 2 : 1) * 2 * (2 * (int64_t)kNyBasis * n);
@@ -805,9 +1260,27 @@ void launch_nystrom_prec_build(const Launch& L, const NyPrec& P) {
   count_launch(1);
 }
 
+void launch_nystrom_ras_build(const Launch& L, const NyPrec& P, int64_t e0, int64_t count,
+                              int32_t max_len) {
+  (void)max_len;
+  if (count <= 0) return;
+  if (P.f32)
+    k_ny_ras_build<float><<<(unsigned)count, kRasT, 0, L.stream>>>(P, e0);
+  else
+    k_ny_ras_build<double><<<(unsigned)count, kRasT, 0, L.stream>>>(P, e0);
+  count_launch(1);
+}
+
 void launch_nystrom_prec_apply(const Launch& L, const NyPrec& P, const double* src, int64_t lds,
                                const int32_t* jptr, int64_t jstride, double* dst, int64_t ldd,
                                int32_t nr) {
+  if (P.ras) {
+    const int64_t warps = P.n / kNyNodes * nr;
+    k_ny_ras_apply<<<(unsigned)((warps * 32 + 127) / 128), 128, 0, L.stream>>>(
+        P, src, lds, jptr, jstride, dst, ldd, nr);
+    count_launch(1);
+    return;
+  }
   const int64_t total = P.n / kNyNodes * nr;
   k_ny_prec_apply<<<(unsigned)((total + 127) / 128), 128, 0, L.stream>>>(P, src, lds, jptr,
                                                                           jstride, dst, ldd, nr);
@@ -838,6 +1311,21 @@ void launch_nystrom(const Launch& L, const NyInst& I0) {
   const int64_t per = (I.n + I.n_chunks - 1) / I.n_chunks;
   I.chunk_cols = (per + kNyTile - 1) / kNyTile * kNyTile;
   const unsigned tb = (unsigned)((I.n + 127) / 128);
+  if (I.fluid >= 3) {  // coupled regions: traces on both sides, region kernels
+    k_ny_traces_regions<<<tb, 128, 0, L.stream>>>(I, 0);
+    k_ny_traces_regions<<<tb, 128, 0, L.stream>>>(I, 1);
+    dim3 grid((unsigned)((I.n + kNyRows - 1) / kNyRows), (unsigned)I.n_chunks);
+    const unsigned cb = (unsigned)((I.n / kNyNodes + kNyCorrT - 1) / kNyCorrT);
+    if (I.fluid == 3) {
+      k_ny_assemble_regions<true><<<grid, kNyRows, 0, L.stream>>>(I);
+      k_ny_correct_regions<true><<<cb, kNyCorrT, 0, L.stream>>>(I);
+    } else {
+      k_ny_assemble_regions<false><<<grid, kNyRows, 0, L.stream>>>(I);
+      k_ny_correct_regions<false><<<cb, kNyCorrT, 0, L.stream>>>(I);
+    }
+    count_launch(4);
+    return;
+  }
   k_ny_traces<<<tb, 128, 0, L.stream>>>(I);
   count_launch(1);
   if (I.fluid) {  // the interior wavenumber's traces

@@ -36,10 +36,17 @@ struct NyInst {
   double k_int, g;      // interior wavenumber, density contrast
   double* A;            // system (complex128, column-major, leading dim 2n)
   double* trace_i;      // interpolant traces at k_int, layout of trace
+  // coupled regions (fluid 3: Mueller, 4: CBIE; k, k_int, g unused): the surface of every
+  // node and the regions' coupling table (the block algebra of the panel path's
+  // kAsmRegion); trace / trace_i hold the interpolants at the wavenumber of the region
+  // outside / inside each node's surface, and the defects sum over same-surface columns
+  const int32_t* surf;
+  const RegionTable* region;
 };
 
 // Defect sums per row and column range: 1 (rigid/soft, combined), 4 (Mueller: S/D and
-// K'/H identities at k and k_int), 2 (fluid CBIE: S/D identities at k and k_int).
+// K'/H identities at k and k_int; regions: at the outer and inner side), 2 (fluid CBIE:
+// S/D identities at k and k_int; regions: both sides).
 int32_t nystrom_defects(int32_t fluid);
 
 // Points of a Nyström solution's field evaluation (k_ny_pressure).
@@ -101,9 +108,29 @@ struct NyPrec {
   int64_t n;
   int32_t f32;
   int32_t* status;       // per element: 1 when its block is singular
+  // Restricted additive Schwarz (ras = 1) instead of the element blocks: element e's
+  // neighbourhood is the elements nb_el[nb_ptr[e] .. nb_ptr[e+1]) (e first), its L = 7 m
+  // nodes in that order; W + woff[e] holds the own rows of the inverse of the system
+  // restricted to those nodes (7 x L complex64, row-major).
+  int32_t ras;
+  float* W;
+  const int64_t* woff;
+  const int32_t* nb_ptr;
+  const int32_t* nb_el;
+  // building the local systems: FP32 node records (relative to the mesh centre), the
+  // operator (0: M1 = 1/2 I - D - alpha H, 1: M2 = S + alpha (1/2 I + K')), wavenumber
+  // and coupling; a workspace of `slots` local matrices of (L + 7) x L complex64
+  const float* recf;
+  int32_t op;
+  float k, a_re, a_im;
+  float* work;
+  int64_t work_stride;   // floats per slot
 };
 // Pinv from the corrected full blocks.
 void launch_nystrom_prec_build(const Launch& L, const NyPrec& P);
+// Schwarz rows W of elements [e0, e0 + count) (count <= the workspace's slots).
+void launch_nystrom_ras_build(const Launch& L, const NyPrec& P, int64_t e0, int64_t count,
+                              int32_t max_len);
 // dst[:, r] = Pinv src[:, r] for nr vectors in permuted order (ld lds / ldd complex);
 // jptr (optional): src offset by (*jptr) * jstride complex entries (the Arnoldi vector).
 void launch_nystrom_prec_apply(const Launch& L, const NyPrec& P, const double* src, int64_t lds,

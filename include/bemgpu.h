@@ -213,6 +213,17 @@ int bemgpu_near_pairs(const double *nodes, int64_t n_nodes, const int64_t *trian
                       int64_t n_triangles, double eta, int64_t *rowptr, int64_t *cols,
                       int64_t cap, int64_t *count);
 
+/*
+ * [host] Neighbourhoods of the restricted additive Schwarz preconditioner that
+ * bemgpu_hmatrix_solve applies to Nyström rigid systems: for every triangle, the
+ * min(count, n_triangles) triangles nearest to it (distances between the centroid nodes of
+ * the 7-point rule, ties by index), itself first; out receives n_triangles x that many
+ * 0-based indices.  No reference counterpart (the reference's rigid GMRES is
+ * unpreconditioned).
+ */
+int bemgpu_schwarz_neighbourhoods(const double *nodes, int64_t n_nodes, const int64_t *triangles,
+                                  int64_t n_triangles, int32_t count, int32_t *out);
+
 /* ------------------------------------------------------------------ context */
 /* Create a context on a device; hbm_budget_bytes = 0 means 90% of free memory. */
 int bemgpu_ctx_create(int device, uint64_t hbm_budget_bytes, bemgpu_ctx **ctx);
@@ -284,7 +295,11 @@ int bemgpu_solve(bemgpu_ctx *ctx, const bemgpu_mesh *mesh, const bemgpu_problem 
  * contrast fields are ignored.  The plane wave lights the surfaces that border the
  * exterior.  The solution answers far_field / target_strength (summed over those
  * surfaces, solvers/bem/postprocessing.jl:15-31), traces (scattered traces there, zero
- * on inner surfaces), region_traces and diagnostics; pressure returns BEMGPU_EINVAL.
+ * on inner surfaces), region_traces, diagnostics and pressure_region.  With
+ * problem->discretization = BEMGPU_NYSTROM the unknowns sit on the quadrature nodes of
+ * every surface (7 per panel) and each surface's own operators are corrected at the
+ * wavenumbers of both regions it borders; such a solution answers everything but
+ * pressure (BEMGPU_EINVAL).
  */
 int bemgpu_region_solve(bemgpu_ctx *ctx, int32_t count, const bemgpu_mesh *const *surfaces,
                         const double *density, const double *soundspeed, const int32_t *parents,

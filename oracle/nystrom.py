@@ -249,3 +249,123 @@ def solve(nodes, triangles, boundary, k, incidence_angle=math.pi / 2, incidence_
         q = np.linalg.solve(A, b)
         p = -pin
     return p, q, (y, ny, w)
+
+
+def neighbourhoods(y, count=48):
+    """Element neighbourhoods of the restricted additive Schwarz preconditioner: for
+    element e, the `count` elements whose centroids are nearest to e's (e itself first,
+    ties by index).  y: node positions (element-major, 7 per element); an element's first
+    node is the rule's centroid node."""
+    ne = len(y) // NODES
+    cent = y[::NODES]
+    out = []
+    idx = np.arange(ne)
+    for e in range(ne):
+        d = ((cent - cent[e]) ** 2).sum(1)
+        order = np.lexsort((idx, d))
+        out.append(order[:min(count, ne)])
+    return out
+
+
+def ras_matrix(A, nbhd):
+    """Restricted additive Schwarz preconditioner P^-1 (dense N x N) of the node system A:
+    for every element e, the rows of its own nodes of inv(A[N_e, N_e]), placed at the
+    columns of N_e (the nodes of its neighbourhood's elements, in neighbourhood order)."""
+    n = A.shape[0]
+    Pinv = np.zeros((n, n), dtype=np.complex128)
+    for e, els in enumerate(nbhd):
+        idx = (els[:, None] * NODES + np.arange(NODES)[None, :]).reshape(-1)
+        inv = np.linalg.inv(A[np.ix_(idx, idx)])
+        Pinv[e * NODES:(e + 1) * NODES, idx] = inv[:NODES, :]   # e is the first element
+    return Pinv
+
+
+def assemble_regions(surfaces, materials, parents, k, formulation="muller"):
+    """Coupled fluid regions on the quadrature nodes: the block algebra of the panel
+    oracle's ``assemble_regions`` (solvers/bem/regions.jl:189-236) with node operators.
+    Surface i (1-based) encloses region i, parents[i-1] is the region outside it, materials
+    (density, sound speed) per region relative to the exterior.  Between different surfaces
+    the operators are the plain node kernel at the region's wavenumber; a surface's own
+    block at the wavenumber of each region it borders is ``corrected_operators`` of that
+    surface alone (the Green identities hold surface by surface).
+    Returns (A, (y, ny, w) of all nodes in surface order, node offsets)."""
+    Ps = [O.Panels(nd, tr) for nd, tr in surfaces]
+    per = [nodes_of(P) for P in Ps]
+    y = np.concatenate([p[0] for p in per])
+    ny = np.concatenate([p[1] for p in per])
+    w = np.concatenate([p[2] for p in per])
+    offs = [0]
+    for p in per:
+        offs.append(offs[-1] + len(p[2]))
+    n = offs[-1]
+    count = len(surfaces)
+    dens = [1.0] + [float(m[0]) for m in materials]
+    speeds = [1.0] + [float(m[1]) for m in materials]
+    ops = {}
+
+    def region_ops(r):
+        if r not in ops:
+            kr = k / speeds[r]
+            S, D, K, H = operators(y, ny, w, kr)
+            for s in range(1, count + 1):
+                if not (s == r or parents[s - 1] == r):
+                    continue
+                blk = slice(offs[s - 1], offs[s])
+                (Ss, Ds, Ks, Hs), _ = corrected_operators(Ps[s - 1], kr)
+                S[blk, blk], D[blk, blk], K[blk, blk], H[blk, blk] = Ss, Ds, Ks, Hs
+            ops[r] = (S, D, K, H)
+        return ops[r]
+
+    A = np.eye(2 * n, dtype=np.complex128) if formulation == "muller" else \
+        np.zeros((2 * n, 2 * n), dtype=np.complex128)
+    for i in range(1, count + 1):
+        rows = np.arange(offs[i - 1], offs[i])
+        for region in (i, parents[i - 1]):
+            rho = dens[region]
+            S, D, K, H = region_ops(region)
+            eqs = rows + n if region == i else rows
+            if formulation == "cbie":
+                A[np.ix_(eqs, rows)] += 0.5 * np.eye(len(rows))
+            for j in range(1, count + 1):
+                if not (j == region or parents[j - 1] == region):
+                    continue
+                sign = 1.0 if j == region else -1.0
+                cols = np.arange(offs[j - 1], offs[j])
+                blk = np.ix_(rows, cols)
+                if formulation == "cbie":
+                    A[np.ix_(eqs, cols)] += sign * D[blk]
+                    A[np.ix_(eqs, cols + n)] -= sign * rho * S[blk]
+                    continue
+                A[np.ix_(rows, cols)] += sign * D[blk]
+                A[np.ix_(rows, cols + n)] -= sign * rho * S[blk]
+                A[np.ix_(rows + n, cols)] += (sign / rho) * H[blk]
+                A[np.ix_(rows + n, cols + n)] -= sign * K[blk]
+    return A, (y, ny, w), offs
+
+
+def solve_regions(surfaces, materials, parents, k, incidence_angle=math.pi / 2,
+                  incidence_azimuth=0.0, formulation="muller"):
+    """Dense FP64 solve of the node region system with the plane wave on the surfaces that
+    border the exterior (regions.jl:240-253) and the backscatter summed over them
+    (solvers/bem/postprocessing.jl:15-31)."""
+    A, (y, ny, w), offs = assemble_regions(surfaces, materials, parents, k, formulation)
+    n = len(w)
+    d = O.incidence_direction(incidence_angle, incidence_azimuth)
+    pin = np.exp(1j * k * (y @ d))
+    qin = 1j * k * (ny @ d) * pin
+    outer = np.zeros(n, dtype=bool)
+    b = np.zeros(2 * n, dtype=np.complex128)
+    for i in range(1, len(surfaces) + 1):
+        if parents[i - 1] == 0:
+            sl = slice(offs[i - 1], offs[i])
+            outer[sl] = True
+            b[sl] = pin[sl]
+            if formulation == "muller":
+                b[n + offs[i - 1]:n + offs[i]] = qin[sl]
+    x = np.linalg.solve(A, b)
+    p_tot, v = x[:n], x[n:]
+    ps = np.where(outer, p_tot - pin, 0.0)
+    qs = np.where(outer, v - qin, 0.0)
+    amp = far_field(y, ny, w, k, -d, ps, qs)
+    return dict(A=A, b=b, x=x, amplitude=amp, p_scat=ps, dpdn_scat=qs, nodes=(y, ny, w),
+                offsets=offs)

@@ -116,3 +116,64 @@ def test_region_pressure_matches_oracle(ctx, formulation):
         sol.pressure(core, field="total", region=1)
     with pytest.raises(bemgpu.ArgumentError):
         sol.pressure(core, field="total", region=5)
+
+
+def _nystrom_both(ctx, surfs, mats, parents, k, beta, formulation="muller", precision="double"):
+    from oracle import nystrom as NY
+    sm = [bemgpu.mesh(*s) for s in surfs]
+    fl = [bemgpu.FluidFilled(*m) for m in mats]
+    sol = bemgpu.bem(sm, fl, k, parents=parents, incidence_angle=beta, formulation=formulation,
+                     precision=precision, ctx=ctx, discretization="nystrom")
+    ref = NY.solve_regions(surfs, mats, parents, k, incidence_angle=beta,
+                           formulation=formulation)
+    return sol, ref
+
+
+def test_nystrom_single_interface_is_the_nystrom_fluid_solve(ctx):
+    """One interface in the exterior: the region block system on the quadrature nodes is
+    the single-surface Nyström fluid system."""
+    s = meshes.icosphere(1.0, 1)
+    surf = bemgpu.mesh(*s)
+    fl = bemgpu.FluidFilled(1.07, 1.04)
+    one = bemgpu.bem([surf], [fl], 1.4, incidence_angle=0.5, ctx=ctx, discretization="nystrom")
+    ref = bemgpu.bem(surf, fl, 1.4, incidence_angle=0.5, ctx=ctx, discretization="nystrom")
+    a, b = bemgpu.scattering_amplitude(one), bemgpu.scattering_amplitude(ref)
+    assert abs(a - b) <= 1e-11 * abs(b)
+    one.close()
+    ref.close()
+
+
+@pytest.mark.parametrize("formulation", ["muller", "cbie"])
+def test_nystrom_nested_interfaces_match_oracle(ctx, formulation):
+    """Nested interfaces on the quadrature nodes (each surface's own operators corrected at
+    the wavenumbers of both its regions): = the oracle's node restatement
+    (oracle/nystrom.py:assemble_regions) to 1e-9 in amplitude and unknowns."""
+    surfs = [meshes.icosphere(1.0, 1), meshes.icosphere(0.5, 1)]
+    mats = [(1.05, 1.03), (1.3, 1.2)]
+    sol, ref = _nystrom_both(ctx, surfs, mats, [0, 1], 1.2, 0.3, formulation)
+    a = bemgpu.scattering_amplitude(sol)
+    assert abs(a - ref["amplitude"]) <= 1e-9 * abs(ref["amplitude"])
+    p, v = sol.region_traces()
+    n = len(p)
+    x = ref["x"]
+    assert n == 2 * 80 * 7
+    assert np.max(np.abs(p - x[:n])) <= 1e-9 * np.max(np.abs(x[:n]))
+    assert np.max(np.abs(v - x[n:])) <= 1e-9 * np.max(np.abs(x[n:]))
+    sol.close()
+
+
+def test_nystrom_side_by_side_and_mixed_precision(ctx):
+    """Two bodies in the exterior on the nodes: FP64 = the oracle to 1e-9, mixed precision
+    within 0.01 dB with the refinement's backward error at its 1e-13 acceptance."""
+    surfs = [meshes.icosphere(1.0, 1, center=(-1.5, 0.0, 0.0)),
+             meshes.icosphere(0.8, 1, center=(1.3, 0.0, 0.0))]
+    mats = [(1.1, 1.05), (0.9, 1.1)]
+    sol, ref = _nystrom_both(ctx, surfs, mats, [0, 0], 1.0, 0.0)
+    a = bemgpu.scattering_amplitude(sol)
+    assert abs(a - ref["amplitude"]) <= 1e-9 * abs(ref["amplitude"])
+    sol.close()
+    mix, _ = _nystrom_both(ctx, surfs, mats, [0, 0], 1.0, 0.0, precision="mixed")
+    m = bemgpu.scattering_amplitude(mix)
+    assert abs(20 * math.log10(abs(m) / abs(a))) < 0.01
+    assert mix.diagnostics()["normwise_backward_error"] <= 1e-13
+    mix.close()
