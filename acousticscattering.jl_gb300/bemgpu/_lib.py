@@ -74,7 +74,7 @@ class HmatrixOptions(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("eta", ctypes.c_double),
                 ("leaf_size", ctypes.c_int32), ("restart", ctypes.c_int32),
                 ("reltol", ctypes.c_double), ("abstol", ctypes.c_double),
-                ("maxiter", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("maxiter", ctypes.c_int32), ("neighbours", ctypes.c_int32)]
 
 
 class HmatrixStats(ctypes.Structure):

@@ -583,14 +583,15 @@ def _hmatrix_options(compression, gmres_kwargs):
         return None
     if method != "hmatrix":
         raise ArgumentError("compression method must be :none or :hmatrix")
-    if set(comp) - {"tol", "eta", "leaf_size"}:
-        raise ArgumentError(f"unknown compression option(s): "
-                            f"{sorted(set(comp) - {'tol', 'eta', 'leaf_size'})}")
+    keys = {"tol", "eta", "leaf_size", "neighbours"}
+    if set(comp) - keys:
+        raise ArgumentError(f"unknown compression option(s): {sorted(set(comp) - keys)}")
     o = C.HmatrixOptions()
     C.lib().bemgpu_hmatrix_options_init(ctypes.byref(o))
     o.tol = float(comp.get("tol", o.tol))
     o.eta = float(comp.get("eta", o.eta))
     o.leaf_size = int(comp.get("leaf_size", o.leaf_size))
+    o.neighbours = int(comp.get("neighbours", o.neighbours))
     o.reltol = float(gm.get("reltol", o.reltol))
     o.abstol = float(gm.get("abstol", o.abstol))
     o.restart = int(gm.get("restart", o.restart))

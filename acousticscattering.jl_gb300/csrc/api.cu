@@ -1491,39 +1491,17 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
     if (tiles[q] > 0) launch_tc_cgemm(L, Dgem.as<TcGemmInst>() + q * ni, ni, tiles[q], red);
   };
   auto any = [&](int64_t st, int ph) { return tiles[(size_t)st * kNGem + ph] > 0; };
-  // CTAs per instance of the panel kernel (its thread-block cluster: 2, 4 or 8; every
-  // choice gives the same bits, rows are only partitioned differently).  Tuned per shape
-  // class (instances, log2 of the largest order) on the first factorisation of that class:
-  // the first six panels run the candidates in the order 2 4 8 8 4 2, so that the linear
-  // decrease of the panels' work cancels out of each candidate's two-panel time.
-  const std::string cs_key = "getf2/" + std::to_string(ni) + "/" + std::to_string(log2_bucket(nmax));
-  int cs_pick = 0;  // 0: the batch-size rule
-  bool cs_tune = false;
-  {
-    auto it = c->tuned.find(cs_key);
-    if (it != c->tuned.end())
-      cs_pick = it->second;
-    else if (c->autotune && !c->prof && !G && nmax >= 6 * kPanelNB)
-      cs_tune = true;
-  }
-  static const int kCsOrder[6] = {2, 4, 8, 8, 4, 2};
-  cudaEvent_t cs_ev[7] = {};
-  if (cs_tune)
-    for (auto& e : cs_ev) cudaEventCreate(&e);
-  int panel = 0;
   auto factor_half = [&](int64_t H) {
     const int64_t st = H / SB;
     const int h = (int)((H % SB) / HB);
-    for (int64_t k0 = H; k0 < H + HB && k0 < nmax; k0 += kPanelNB, ++panel) {
+    for (int64_t k0 = H; k0 < H + HB && k0 < nmax; k0 += kPanelNB) {
       {
+        // cluster size by the batch-size rule: timing the candidates on the first panels
+        // of a shape class (in place, in the order 2 4 8 8 4 2 to cancel the panels' work
+        // trend) chose sizes that were slower over the whole batch (184 vs 132 ms of
+        // panels per 64 x 10240 factorisation), as did timing them on scratch copies
         Prof pr(c, "getf2");
-        if (cs_tune && panel < 6) {
-          cudaEventRecord(cs_ev[panel], c->stream);
-          launch_getf2(L, dm, ni, k0, kPanelNB, 1, kCsOrder[panel]);
-          cudaEventRecord(cs_ev[panel + 1], c->stream);
-        } else {
-          launch_getf2(L, dm, ni, k0, kPanelNB, 1, cs_pick);
-        }
+        launch_getf2(L, dm, ni, k0, kPanelNB, 1, 0);
       }
       {
         Prof pr(c, "laswp");
@@ -1627,13 +1605,6 @@ int getrf_tc(bemgpu_ctx* c, std::vector<FactorData*>& fs, const std::vector<MatI
   }
   CUDA_TRY(c, cudaGetLastError());
   TRY(check_device_error(c));
-  if (cs_tune) {  // the stream is idle: read the six panel times
-    float t[6] = {0};
-    for (int q = 0; q < 6; ++q) cudaEventElapsedTime(&t[q], cs_ev[q], cs_ev[q + 1]);
-    for (auto& e : cs_ev) cudaEventDestroy(e);
-    const float t2 = t[0] + t[5], t4 = t[1] + t[4], t8 = t[2] + t[3];
-    c->tuned[cs_key] = (t2 <= t4 && t2 <= t8) ? 2 : (t4 <= t8 ? 4 : 8);
-  }
   return BEMGPU_OK;
 }
 
@@ -3438,16 +3409,13 @@ int check_hm_options(bemgpu_ctx* c, const bemgpu_hmatrix_options& o) {
   if (!(std::isfinite(o.reltol) && o.reltol >= 0 && std::isfinite(o.abstol) && o.abstol >= 0))
     return fail(c, BEMGPU_EINVAL, "GMRES tolerances must be finite and nonnegative");
   if (o.maxiter < 0) return fail(c, BEMGPU_EINVAL, "maxiter must be a nonnegative integer");
+  if (o.neighbours < 0 || o.neighbours > 128)
+    return fail(c, BEMGPU_EINVAL, "neighbours must lie in [0, 128]");
   return BEMGPU_OK;
 }
 
 // Cluster tree and blocks on the host, cross approximation of both operators, full
 // blocks (regular kernel + near kernel into block storage), product lists.
-// Elements per Schwarz neighbourhood of the Nyström rigid system: measured with the
-// oracle on the 1280-panel sphere at k a = 1.6, GMRES steps to 1e-6 fall from 636
-// (unpreconditioned) to 159, 77 and 52 with 32, 48 and 64 nearest elements (20 is worse
-// than none: 1649); 48 keeps the local systems at 336 nodes.
-constexpr int kRasNeighbours = 48;
 
 // The `count` elements nearest to every element (distances between the elements'
 // centroid nodes, ties by index), the element itself first: a uniform grid over the
@@ -3840,10 +3808,10 @@ int hm_build(bemgpu_ctx* c, MeshData* m, const bemgpu_problem& p, int kind,
       for (int32_t v : st)
         if (v) return fail(c, BEMGPU_ESINGULAR, "singular element block of the node system");
       H->ny_op = 1;
-    } else if (p.boundary == BEMGPU_RIGID) {  // the system operator is M1: Schwarz
+    } else if (p.boundary == BEMGPU_RIGID && o.neighbours > 0) {  // system M1: Schwarz
       const int64_t ne = n / kNyNodes;
       std::vector<int32_t> nptr, nel;
-      ras_neighbourhoods(m->panels_h, ne, kRasNeighbours, &nptr, &nel);
+      ras_neighbourhoods(m->panels_h, ne, o.neighbours, &nptr, &nel);
       std::vector<int64_t> woff((size_t)ne + 1, 0);
       int32_t max_len = 0;
       for (int64_t e = 0; e < ne; ++e) {
@@ -4129,6 +4097,14 @@ void bemgpu_hmatrix_options_init(bemgpu_hmatrix_options* o) {
   o->reltol = 1e-4;
   o->abstol = 0.0;
   o->maxiter = 1200;
+  // no Schwarz preconditioner unless asked for (the reference's rigid GMRES is
+  // unpreconditioned).  It pays on coarse meshes -- with the oracle on the 1280-panel
+  // sphere at k a = 1.6, GMRES steps to 1e-6 fall from 630 to 159, 78 and 52 with 32, 48
+  // and 64 nearest elements (20 is worse than none: 1649) -- but a one-level Schwarz
+  // method degrades as the mesh is refined: with 48 neighbours GMRES(150) stalls at a
+  // relative residual of 1.5e-2 on a 2304-panel sphere (oracle, FP64 local inverses)
+  // and of 0.95 on the 5120-panel sphere (GPU), where plain GMRES reaches 3e-6
+  o->neighbours = 0;
 }
 
 int bemgpu_hmatrix_plan(const double* nodes, int64_t n_nodes, const int64_t* triangles,

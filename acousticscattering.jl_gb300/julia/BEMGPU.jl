@@ -171,7 +171,7 @@ struct HmatrixOptions
     reltol::Float64
     abstol::Float64
     maxiter::Int32
-    pad::Int32
+    neighbours::Int32       # Schwarz neighbourhood of Nyström rigid systems (0 = none)
 end
 
 struct HmatrixStats
@@ -229,7 +229,7 @@ function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
         o = HmatrixOptions(get(compression, :tol, 1e-5), get(compression, :eta, 3.0),
             Int32(get(compression, :leaf_size, 64)), Int32(get(gmres_kwargs, :restart, 150)),
             get(gmres_kwargs, :reltol, 1e-4), get(gmres_kwargs, :abstol, 0.0),
-            Int32(get(gmres_kwargs, :maxiter, 1200)), Int32(0))
+            Int32(get(gmres_kwargs, :maxiter, 1200)), Int32(get(compression, :neighbours, 0)))
         inc = Float64[incidence_angle, incidence_azimuth]
         r = Ref{Ptr{Cvoid}}(C_NULL)
         check(ccall((:bemgpu_hmatrix_solve, libbemgpu), Cint,

@@ -672,6 +672,10 @@ def _serve(srv_factory, surfs, bodies, reqs, subset, rate, seed):
             bi, ks, ang = reqs[i]
             bc = bemgpu.Rigid() if bodies[bi]["boundary"] == "rigid" else bemgpu.PressureRelease()
             tickets.put((srv.submit(surfs[bi], bc, ks, ang, precision=srv.precision), i))
+            if (j + 1) % 500 == 0:
+                print(f"# submitted {j + 1} of {len(subset)} at "
+                      f"{time.perf_counter() - t0:.0f} s, {len(lat)} done", file=sys.stderr,
+                      flush=True)
     finally:
         tickets.put(None)
         wt.join()

@@ -326,7 +326,11 @@ typedef struct {
   double reltol;      /* GMRES: stop when the residual <= max(reltol |b|, abstol) (1e-4) */
   double abstol;      /* (default 0) */
   int32_t maxiter;    /* GMRES Arnoldi steps (default 1200) */
-  int32_t pad;
+  int32_t neighbours; /* Nyström rigid systems: elements per neighbourhood of a restricted
+                         additive Schwarz right preconditioner, 0 = none (default), 1..128;
+                         no reference counterpart (the reference's rigid GMRES is
+                         unpreconditioned).  48 cuts GMRES steps 8x on meshes up to about
+                         1300 panels and stalls GMRES on finer ones (one-level method) */
 } bemgpu_hmatrix_options;
 
 typedef struct {

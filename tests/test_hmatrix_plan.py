@@ -84,11 +84,15 @@ def test_plan_rejects_bad_options():
     L = C.lib()
     o = C.HmatrixOptions()
     L.bemgpu_hmatrix_options_init(ctypes.byref(o))
+    # the reference's defaults (solvers/bem/full.jl:56-58); no Schwarz preconditioner
+    assert (o.tol, o.eta, o.restart, o.reltol, o.maxiter, o.neighbours) == \
+        (1e-5, 3.0, 150, 1e-4, 1200, 0)
     nodes = np.ascontiguousarray(np.asarray(nodes, dtype=np.float64).reshape(3, -1).T)
     tris = np.ascontiguousarray(np.asarray(tris, dtype=np.int64).reshape(3, -1).T)
     counts = np.zeros(4, dtype=np.int64)
     for field, bad in (("tol", 0.0), ("tol", 1.5), ("eta", -1.0), ("leaf_size", 4),
-                       ("restart", 0), ("maxiter", -1), ("reltol", float("nan"))):
+                       ("restart", 0), ("maxiter", -1), ("reltol", float("nan")),
+                       ("neighbours", -1), ("neighbours", 129)):
         o2 = C.HmatrixOptions()
         ctypes.pointer(o2)[0] = o
         setattr(o2, field, bad)
