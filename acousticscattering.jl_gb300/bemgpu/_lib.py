@@ -45,7 +45,8 @@ class ServerStats(ctypes.Structure):
                 ("failed", ctypes.c_int64), ("items", ctypes.c_int64),
                 ("factorizations", ctypes.c_int64), ("cache_hits", ctypes.c_int64),
                 ("batches", ctypes.c_int64), ("evictions", ctypes.c_int64),
-                ("busy_ms", ctypes.c_double), ("cached_bytes", ctypes.c_uint64)]
+                ("busy_ms", ctypes.c_double), ("cached_bytes", ctypes.c_uint64),
+                ("retries", ctypes.c_int64)]
 
 
 class Diagnostics(ctypes.Structure):
@@ -169,6 +170,7 @@ SIGNATURES = {
                                                    _vp, _i64]),
     "bemgpu_ctx_set_tensor_lu": (ctypes.c_int, [_vp, _i32]),
     "bemgpu_ctx_set_graphs": (ctypes.c_int, [_vp, _i32]),
+    "bemgpu_ctx_inject_alloc_failures": (ctypes.c_int, [_vp, _i32]),
     "bemgpu_schwarz_neighbourhoods": (ctypes.c_int, [_dp, _i64, _i64p, _i64, _i32,
                                                      ctypes.POINTER(ctypes.c_int32)]),
     "bemgpu_ctx_graph_stats": (ctypes.c_int, [_vp, _i64p, _i64p]),

@@ -140,6 +140,11 @@ class Context:
         """Capture and replay the batched LU's launch sequence as CUDA graphs (default on)."""
         _check(C.lib().bemgpu_ctx_set_graphs(self.handle, int(bool(enable))), self.handle)
 
+    def inject_alloc_failures(self, count: int):
+        """Test hook: the next ``count`` device allocations of this context and its lanes
+        fail as if cudaMalloc had run out of memory (0 cancels)."""
+        _check(C.lib().bemgpu_ctx_inject_alloc_failures(self.handle, int(count)), self.handle)
+
     def graph_stats(self) -> dict:
         """Batched-LU graphs captured and replayed so far."""
         cap, rep = ctypes.c_int64(), ctypes.c_int64()

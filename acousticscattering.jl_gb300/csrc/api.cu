@@ -61,6 +61,8 @@ struct bemgpu_ctx {
   uint64_t live = 0;   // bytes held by this context's own allocations
   uint64_t total = 0;  // root context: bytes held by it and its lanes (against budget)
   std::string err;
+  cudaError_t last_cuda = cudaSuccess;  // CUDA error of the last failed call (cuda_fail)
+  std::atomic<int32_t> inject_oom{0};   // root: allocations still to fail (test hook)
   int* d_err = nullptr;
   // free device blocks of this context, reused on its own stream(s) only (stream order
   // makes a block released with work still queued safe to hand out again)
@@ -111,6 +113,7 @@ int fail(bemgpu_ctx* c, int code, const std::string& msg) {
 
 int cuda_fail(bemgpu_ctx* c, cudaError_t e, const char* what) {
   std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  if (c) c->last_cuda = e;
   return fail(c, BEMGPU_ECUDA, m);
 }
 
@@ -328,6 +331,16 @@ int alloc(bemgpu_ctx* c, size_t bytes, Buf* out) {
     c->live += rb;
   }
   void* p = nullptr;
+  {
+    std::atomic<int32_t>& inj = root_of(c)->inject_oom;
+    int32_t left = inj.load();
+    while (left > 0 && !inj.compare_exchange_weak(left, left - 1)) {
+    }
+    if (left > 0) {  // a failure requested by bemgpu_ctx_inject_alloc_failures
+      account(c, -(int64_t)rb);
+      return cuda_fail(c, cudaErrorMemoryAllocation, "cudaMalloc");
+    }
+  }
   {
     std::lock_guard<std::mutex> lk(c->pool_mu);
     auto it = c->cache.find(rb);
@@ -2592,12 +2605,15 @@ size_t item_bytes(const ServerReq& r) {
   return b + b / 20 + solve_bytes(r);
 }
 
-// One work item: a (request, wavenumber) pair waiting for a lane.
+// One work item: a (request, wavenumber) pair waiting for a lane.  `retry`: its batch
+// failed to allocate device memory once; it runs again when no other batch is on the
+// device, and fails for good if that fails too.
 struct Pending {
   std::shared_ptr<ServerReq> req;
   int32_t fi = 0;
   FKey key{};
   int64_t N = 0;
+  bool retry = false;
 };
 }  // namespace
 
@@ -2643,6 +2659,7 @@ struct Item {
   std::shared_ptr<ServerReq> req;
   int32_t fi;
   FKey key;
+  bool retry;
 };
 
 // One batch: factor the uncached keys, solve every item, read back backscatter.
@@ -2791,6 +2808,10 @@ bool take_batch(bemgpu_server* S, int li, Batch* B, std::shared_ptr<ServerReq>* 
     if (kv.second.lane < 0) evictable += kv.second.bytes;
   const uint64_t held = outside + S->cached_bytes + S->reserved;
   const uint64_t avail = usable > held ? usable - held : 0;
+  // an item whose batch ran out of device memory waits until no batch is on the device
+  if (S->running > 0)
+    for (const Pending& p : S->pending)
+      if (p.retry) return false;
   auto takeable = [&](const Pending& p) {
     auto ce = S->cache.find(p.key);
     if (ce != S->cache.end()) return ce->second.lane < 0;  // else in use on another lane
@@ -2850,7 +2871,7 @@ bool take_batch(bemgpu_server* S, int li, Batch* B, std::shared_ptr<ServerReq>* 
       B->fresh.push_back(p.key);
       ++nnew;
     }
-    B->items.push_back(Item{p.req, p.fi, p.key});
+    B->items.push_back(Item{p.req, p.fi, p.key, p.retry});
     taken.push_back(pos);
   }
   if (B->items.empty()) return false;
@@ -2897,11 +2918,14 @@ void lane_loop(bemgpu_server* S, int li) {
     int status;
     int64_t nfactored = 0;
     std::string err;
+    bool oom = false;
     Clock::time_point t0 = Clock::now();
     {
       std::lock_guard<std::recursive_mutex> ck(lc->mu);
+      lc->last_cuda = cudaSuccess;
       status = run_batch(lc, B.items, B.factors, &nfactored);
       if (status != BEMGPU_OK) err = lc->err;
+      oom = status == BEMGPU_ECUDA && lc->last_cuda == cudaErrorMemoryAllocation;
     }
     const double ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
     {
@@ -2926,14 +2950,25 @@ void lane_loop(bemgpu_server* S, int li) {
         it->second.bytes = b;
         it->second.lane = -1;
       }
+      // a batch that ran out of device memory (the budget counts live blocks, not the
+      // other lanes' free ones or the driver's own) goes back to the head of the queue
+      // once, to run when the device holds no other batch
+      std::vector<Pending> again;
       for (auto& it : B.items) {
         ServerReq& r = *it.req;
         if (status != BEMGPU_OK) {
+          if (oom && !it.retry && !r.finished) {
+            again.push_back(Pending{it.req, it.fi, it.key, order_of(r), true});
+            if (r.untaken++ == 0) S->waiting++;
+            continue;
+          }
           finish_req(S, r, status, err);
           continue;
         }
         if (++r.done_freq == r.nfreq && !r.finished) finish_req(S, r, BEMGPU_OK);
       }
+      S->pending.insert(S->pending.begin(), again.begin(), again.end());
+      S->st.retries += (int64_t)again.size();
       if (status == BEMGPU_OK) {
         for (auto& k : B.fresh) {
           auto& f = B.factors[k];
@@ -2951,6 +2986,7 @@ void lane_loop(bemgpu_server* S, int li) {
       B.factors.clear();
       B.items.clear();
     }
+    if (oom) drop_all_caches(lc);  // the retry starts from a device without free blocks
     S->cv_done.notify_all();
     S->cv_work.notify_all();
   }
@@ -5083,6 +5119,12 @@ int bemgpu_ctx_set_graphs(bemgpu_ctx* c, int32_t enable) {
     c->lu_graphs.clear();
     c->lu_seen.clear();
   }
+  return BEMGPU_OK;
+}
+
+int bemgpu_ctx_inject_alloc_failures(bemgpu_ctx* c, int32_t count) {
+  if (!c || count < 0) return fail(c, BEMGPU_EINVAL, "invalid arguments");
+  root_of(c)->inject_oom.store(count);
   return BEMGPU_OK;
 }
 

@@ -445,6 +445,8 @@ typedef struct {
   int64_t evictions;
   double busy_ms;        /* device time of all batches */
   uint64_t cached_bytes;
+  int64_t retries;       /* items re-run after their batch ran out of device memory (once
+                            each, with no other batch on the device) */
 } bemgpu_server_stats;
 
 void bemgpu_server_options_init(bemgpu_server_options *o);
@@ -508,6 +510,12 @@ int bemgpu_ctx_set_autotune(bemgpu_ctx *ctx, int32_t enable);
  * graphs on or off.  enable = 0 drops the captured graphs.  No reference counterpart.
  */
 int bemgpu_ctx_set_graphs(bemgpu_ctx *ctx, int32_t enable);
+/*
+ * Test hook for the out-of-memory path: the next `count` device allocations of the
+ * context and its lanes fail as if cudaMalloc had returned cudaErrorMemoryAllocation (the
+ * driver is not called; 0 cancels).  No reference counterpart.
+ */
+int bemgpu_ctx_inject_alloc_failures(bemgpu_ctx *ctx, int32_t count);
 /* Batched-LU graphs captured and replayed by the context so far. */
 int bemgpu_ctx_graph_stats(const bemgpu_ctx *ctx, int64_t *captures, int64_t *replays);
 /*

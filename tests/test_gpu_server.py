@@ -48,6 +48,41 @@ def test_same_alone_and_in_the_mix(ctx):
     assert st["completed"] == 4 and st["failed"] == 0
 
 
+def test_batch_out_of_device_memory_runs_again_alone(ctx):
+    """A batch whose device allocation fails (injected on the host: the allocator sees
+    cudaErrorMemoryAllocation without calling the driver) goes back to the head of the
+    queue once and runs again when no other batch is on the device, with the same bits as
+    without the failure; when the re-run fails too, the request fails with the error."""
+    a, _, _ = _surfaces()
+    req = (a, bemgpu.Rigid(), [300.0, 420.0], [0.3, 1.1])
+    srv = bemgpu.Server(ctx, max_batch=8)
+    try:
+        ref = srv.wait(srv.submit(*req, precision="mixed"))[0]   # the mesh is resident now
+    finally:
+        srv.close()
+    for failures in (1, 2):
+        srv = bemgpu.Server(ctx, max_batch=8)
+        try:
+            ctx.inject_alloc_failures(failures)
+            t = srv.submit(*req, precision="mixed")
+            if failures == 1:
+                got = srv.wait(t)[0]
+            else:
+                with pytest.raises(bemgpu.BEMGPUError, match="out of memory"):
+                    srv.wait(t)
+            st = srv.stats()
+        finally:
+            ctx.inject_alloc_failures(0)
+            srv.close()
+        assert st["retries"] == 2, st          # both frequencies of the batch, once
+        if failures == 1:
+            assert np.array_equal(got, ref) and st["completed"] == 1 and st["failed"] == 0
+        else:
+            assert st["completed"] == 0 and st["failed"] == 1
+    with pytest.raises(bemgpu.ArgumentError):
+        ctx.inject_alloc_failures(-1)
+
+
 def test_cached_factors_are_reused(ctx):
     a, _, _ = _surfaces()
     req = (a, bemgpu.Rigid(), [300.0, 420.0], [0.3, 1.1])
