@@ -207,8 +207,40 @@ void drop_cache(bemgpu_ctx* c) {
     c->cached = 0;
   }
   if (blocks.empty()) return;
-  cudaDeviceSynchronize();
-  for (auto& kv : blocks) cudaFree(kv.second);
+  // a block whose free fails (or that cannot be freed because the device could not be
+  // synchronised) goes back to the pool rather than being lost
+  std::multimap<size_t, void*> kept;
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    cudaGetLastError();
+    kept.swap(blocks);
+  }
+  for (auto& kv : blocks)
+    if (cudaFree(kv.second) != cudaSuccess) {
+      cudaGetLastError();
+      kept.insert(kv);
+    }
+  if (kept.empty()) return;
+  std::lock_guard<std::mutex> lk(c->pool_mu);
+  for (auto& kv : kept) {
+    c->cache.insert(kv);
+    c->cached += kv.first;
+  }
+}
+
+// Bytes of free blocks held by the pools of a root context and its lanes.
+uint64_t pooled_bytes(bemgpu_ctx* c) {
+  bemgpu_ctx* r = root_of(c);
+  uint64_t b = 0;
+  {
+    std::lock_guard<std::mutex> lk(r->pool_mu);
+    b += r->cached;
+  }
+  std::lock_guard<std::mutex> lk(r->lanes_mu);
+  for (bemgpu_ctx* l : r->lanes) {
+    std::lock_guard<std::mutex> pk(l->pool_mu);
+    b += l->cached;
+  }
+  return b;
 }
 
 // Free blocks of the root context and every lane (when a cudaMalloc fails).
@@ -287,7 +319,10 @@ int make_lane(bemgpu_ctx* parent, bemgpu_ctx** out) {
   l->tensor_lu = parent->tensor_lu;
   l->autotune = parent->autotune;
   l->tuned = parent->tuned;
-  l->graphs = parent->graphs;
+  // lanes do not capture graphs: served batches rarely repeat a shape, and a capture on
+  // one lane would forbid the device-wide synchronisation another lane's pool release
+  // needs while it lasts
+  l->graphs = false;
   cudaError_t e = init_streams(l);
   if (e != cudaSuccess) {
     delete l;
@@ -365,7 +400,15 @@ int alloc(bemgpu_ctx* c, size_t bytes, Buf* out) {
     if (e != cudaSuccess) {
       cudaGetLastError();
       account(c, -(int64_t)rb);
-      return cuda_fail(c, e, "cudaMalloc");
+      if (e != cudaErrorMemoryAllocation) return cuda_fail(c, e, "cudaMalloc");
+      size_t fr = 0, tot = 0;
+      cudaMemGetInfo(&fr, &tot);
+      char m[240];
+      std::snprintf(m, sizeof m,
+                    "cudaMalloc of %.3f GB (device: %.3f GB free of %.3f GB; this library: "
+                    "%.3f GB live, %.3f GB in its pools)",
+                    rb / 1e9, fr / 1e9, tot / 1e9, total_live(c) / 1e9, pooled_bytes(c) / 1e9);
+      return cuda_fail(c, e, m);
     }
   }
   out->c = c;
@@ -2986,7 +3029,19 @@ void lane_loop(bemgpu_server* S, int li) {
       B.factors.clear();
       B.items.clear();
     }
-    if (oom) drop_all_caches(lc);  // the retry starts from a device without free blocks
+    if (oom) {
+      drop_all_caches(lc);  // the retry starts from a device without free blocks
+    } else {
+      // the pools keep blocks by exact size, and served systems come in many sizes: a
+      // lane whose free blocks exceed an eighth of the budget returns them to the driver
+      // (outside the budget they would otherwise crowd the other lane's allocations)
+      bool trim;
+      {
+        std::lock_guard<std::mutex> pk(lc->pool_mu);
+        trim = lc->cached > root_of(lc)->budget / 8;
+      }
+      if (trim) drop_cache(lc);
+    }
     S->cv_done.notify_all();
     S->cv_work.notify_all();
   }

@@ -59,7 +59,8 @@ class Clocks:
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,"
+         "memory.used,memory.total")
 
     def __init__(self, device=0):
         self.device = device
@@ -94,7 +95,7 @@ class Clocks:
                 self.proc.kill()
         if self.thread:
             self.thread.join(timeout=5)
-        sm, mx, reasons = [], 0.0, set()
+        sm, mx, reasons, mem = [], 0.0, set(), []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in self.rows:
             try:
@@ -105,9 +106,17 @@ class Clocks:
             for name, v in zip(names, r[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(name)
-        return {"sm_mhz": float(np.median(sm)) if sm else None,
-                "sm_max_mhz": mx or None, "reasons": sorted(reasons),
-                "samples": len(sm)}
+            try:
+                mem.append((float(r[9]), float(r[10])))
+            except (IndexError, ValueError):
+                pass
+        out = {"sm_mhz": float(np.median(sm)) if sm else None,
+               "sm_max_mhz": mx or None, "reasons": sorted(reasons),
+               "samples": len(sm)}
+        if mem:  # device memory in use (all processes) during the region, MiB
+            out["memory_used_mib_max"] = max(u for u, _ in mem)
+            out["memory_total_mib"] = mem[0][1]
+        return out
 
 
 def measured_peaks(sustained=False):

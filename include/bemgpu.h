@@ -506,8 +506,9 @@ int bemgpu_ctx_set_autotune(bemgpu_ctx *ctx, int32_t enable);
  * factorisation of a batch is captured the second time a batch of the same shape (the
  * instances' orders) is factored, and replayed for later batches of that shape, with the
  * new batch's descriptors written into the graph's arrays (16 shapes per context, least
- * recently used dropped; not while profiling is on).  Results are bit-identical with
- * graphs on or off.  enable = 0 drops the captured graphs.  No reference counterpart.
+ * recently used dropped; not while profiling is on, nor on server lanes).  Results are
+ * bit-identical with graphs on or off.  enable = 0 drops the captured graphs.  No
+ * reference counterpart.
  */
 int bemgpu_ctx_set_graphs(bemgpu_ctx *ctx, int32_t enable);
 /*
