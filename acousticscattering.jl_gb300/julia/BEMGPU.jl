@@ -483,6 +483,97 @@ function pressure(sol::BEMSolution{_GPUBEMData}, points; field::Symbol = :total,
     return single ? values[1] : values
 end
 
+# ------------------------------------------------------------------ serving
+struct ServerOptions
+    max_batch::Int32
+    queue_limit::Int32
+    cache_bytes::UInt64
+    lanes::Int32
+    reserved::Int32
+end
+
+struct ServerStats
+    submitted::Int64
+    completed::Int64
+    failed::Int64
+    items::Int64
+    factorizations::Int64
+    cache_hits::Int64
+    batches::Int64
+    evictions::Int64
+    busy_ms::Float64
+    cached_bytes::UInt64
+    retries::Int64
+end
+
+"""
+    Server(ctx=context(); max_batch=64, queue_limit=4096, cache_bytes=0, lanes=2)
+
+The library's continuous-batching request loop (no reference counterpart): `submit`
+queues one surface / boundary problem at several wavenumbers and incidence directions and
+returns a ticket, `wait` returns its backscatter amplitudes (nfreq × nangles) and latency
+in ms.  `lanes` batches run on the device at once; factors are cached across requests.
+"""
+mutable struct Server
+    ptr::Ptr{Cvoid}
+    ctx::Context
+    shapes::Dict{Int64, Tuple{Int, Int}}
+    function Server(ctx::Context = context(); max_batch::Integer = 64,
+            queue_limit::Integer = 4096, cache_bytes::Integer = 0, lanes::Integer = 2)
+        o = ServerOptions(Int32(max_batch), Int32(queue_limit), UInt64(cache_bytes),
+            Int32(lanes), Int32(0))
+        r = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:bemgpu_server_create, libbemgpu), Cint,
+            (Ptr{Cvoid}, Ref{ServerOptions}, Ptr{Ptr{Cvoid}}), ctx.ptr, o, r), ctx.ptr)
+        s = new(r[], ctx, Dict{Int64, Tuple{Int, Int}}())
+        finalizer(close, s)
+        return s
+    end
+end
+
+function submit(s::Server, m::GPUMesh, boundary, ks::AbstractVector{<:Real},
+        angles::AbstractVector{<:Real}; azimuth::Real = 0.0, kwargs...)
+    isempty(ks) && throw(ArgumentError("at least one wavenumber"))
+    p = _problem(boundary, ks[1]; kwargs...)
+    inc = Float64[v for a in angles for v in (Float64(a), Float64(azimuth))]
+    t = Ref{Int64}(0)
+    check(ccall((:bemgpu_server_submit, libbemgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ref{Problem}, Int32, Ptr{Float64}, Int32, Ptr{Float64},
+            Ptr{Int64}),
+        s.ptr, m.ptr, p, length(ks), Float64.(collect(ks)), length(angles), inc, t), s.ctx.ptr)
+    s.shapes[t[]] = (length(ks), length(angles))
+    return t[]
+end
+
+function Base.wait(s::Server, ticket::Integer; timeout_ms::Integer = -1)
+    nf, na = s.shapes[ticket]
+    out = zeros(Float64, 2 * nf * na)
+    lat = Ref{Float64}(0.0)
+    st = ccall((:bemgpu_server_wait, libbemgpu), Cint,
+        (Ptr{Cvoid}, Int64, Int32, Ptr{Float64}, Ptr{Float64}),
+        s.ptr, ticket, Int32(timeout_ms), out, lat)
+    st == 6 && error("request not finished")  # BEMGPU_ETIMEOUT: the ticket stays valid
+    delete!(s.shapes, ticket)
+    check(st, s.ctx.ptr)
+    amps = [complex(out[2q - 1], out[2q]) for q in 1:(nf * na)]
+    return permutedims(reshape(amps, na, nf)), lat[]   # nfreq × nangles
+end
+
+function stats(s::Server)
+    st = Ref{ServerStats}()
+    check(ccall((:bemgpu_server_stats_get, libbemgpu), Cint, (Ptr{Cvoid}, Ref{ServerStats}),
+        s.ptr, st), s.ctx.ptr)
+    return st[]
+end
+
+function Base.close(s::Server)
+    if s.ptr != C_NULL
+        ccall((:bemgpu_server_destroy, libbemgpu), Cint, (Ptr{Cvoid},), s.ptr)
+        s.ptr = C_NULL
+    end
+    return nothing
+end
+
 target_strength(sol::BEMSolution{_GPUBEMData}; kwargs...) =
     20 * log10(abs(scattering_amplitude(sol; kwargs...)))
 
