@@ -1,0 +1,61 @@
+"""Host logic of bench.py that needs no GPU: the served-stream driver reports failed
+requests in its line (and counts only completed ones) instead of aborting a long run, and
+the nvidia-smi sampler's clock, throttle-reason and memory parsing."""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+
+
+class _FakeServer:
+    """Stands in for bemgpu.Server: request 3 fails the way an out-of-memory batch
+    reported itself before the server re-ran such batches."""
+    precision = "mixed"
+
+    def __init__(self):
+        self.n = 0
+
+    def submit(self, surface, boundary, ks, angles, precision):
+        self.n += 1
+        return self.n - 1
+
+    def wait(self, ticket, timeout_ms=-1):
+        if ticket == 3:
+            raise RuntimeError("CUDA error: request failed: cudaMalloc: out of memory")
+        return np.full((1, 2), 1.0 + 0.5j), 10.0 * (ticket + 1)
+
+    def stats(self):
+        return {"completed": 4, "failed": 1}
+
+    def close(self):
+        pass
+
+
+def test_served_stream_reports_failed_requests():
+    bodies = [{"boundary": "rigid"}]
+    reqs = [(0, np.array([100.0]), np.array([0.1, 0.2]))] * 5
+    res, out = bench._serve(_FakeServer, [None], bodies, reqs, list(range(5)), 1e6, 7)
+    assert res["failed_requests"] == 1 and "out of memory" in res["first_error"]
+    assert sorted(out) == [0, 1, 2, 4]
+    assert res["solves"] == 4 * 2 and res["requests"] == 5
+    lats = [10.0, 20.0, 30.0, 50.0]
+    assert res["p50_ms"] == np.percentile(lats, 50) and res["max_ms"] == 50.0
+
+
+def test_clock_sampler_parses_reasons_and_memory():
+    c = bench.Clocks(0)
+    c.rows = [["0", "2070", "2070", "900.1", "0x0", "Not Active", "Not Active", "Not Active",
+               "Active", "150000", "284208"],
+              ["0", "1995", "2070", "1380.0", "0x4", "Not Active", "Not Active", "Not Active",
+               "Active", "281487", "284208"],
+              ["0", "[N/A]", "2070"]]
+    out = c.stop()
+    assert out["sm_max_mhz"] == 2070.0 and out["samples"] == 2
+    assert out["sm_mhz"] == np.median([2070.0, 1995.0])
+    assert out["reasons"] == ["sw_power_cap"]
+    assert out["memory_used_mib_max"] == 281487.0 and out["memory_total_mib"] == 284208.0
