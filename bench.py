@@ -783,6 +783,71 @@ def run_config4(args):
     return line
 
 
+def run_config4_phases(args):
+    """Where a served stream's device time goes: the items (request, frequency) of the
+    stream's first --requests requests, grouped as the server groups them (one size class
+    of at most 64 factorisations and about 100 GB per batch), factored and solved through
+    the batch API with per-family CUDA-event times; once with every request's angles and
+    once with one angle per item."""
+    import bemgpu
+    ctx = bemgpu.Context(0, hbm_budget_bytes=int(150e9))
+    bodies, reqs = _request_stream(args.requests, args.pool)
+    surfs = {}
+    for bi in sorted({r[0] for r in reqs}):
+        b = bodies[bi]
+        nodes, tris = bemgpu.meshes.body_of_revolution(b["b"], b["aspect"], b["coeffs"],
+                                                       b["nlon"], b["nrings"])
+        surfs[bi] = bemgpu.mesh(nodes, tris)
+        surfs[bi].handle(ctx)
+    items = sorted(((bi, float(k), ang) for bi, ks, ang in reqs for k in ks),
+                   key=lambda it: surfs[it[0]].n_panels)
+    groups, cur = [], []
+    for it in items:
+        n = surfs[it[0]].n_panels
+        if cur and (n > 2 * surfs[cur[0][0]].n_panels or len(cur) >= 64 or
+                    24.0 * sum(surfs[c[0]].n_panels ** 2 for c in cur + [it]) > 100e9):
+            groups.append(cur)
+            cur = []
+        cur.append(it)
+    groups.append(cur)
+    fams = ("assemble", "near", "equilibrate", "scale_copy", "getf2", "laswp", "trsm",
+            "tc_pack", "gemm_tc", "gemm_panel", "getrs", "gecon", "residual", "forcing",
+            "incident", "far_field")
+
+    def run(one_angle):
+        ctx.timer_start()
+        for g in groups:
+            its = [(surfs[bi], bemgpu.Rigid() if bodies[bi]["boundary"] == "rigid"
+                    else bemgpu.PressureRelease(), k, dict(precision="mixed"))
+                   for bi, k, _ in g]
+            fs = bemgpu.factor_batch(its, ctx)
+            angs = [list(a[:1]) if one_angle else list(a) for _, _, a in g]
+            sols = bemgpu.solve_batch(fs, angs, [[0.0] * len(a) for a in angs])
+            for s_ in sols:
+                bemgpu.scattering_amplitude(s_)
+                s_.close()
+            for f in fs:
+                f.close()
+        return ctx.timer_stop()
+
+    out = {}
+    for one in (False, True):
+        run(one)  # warm-up (tuner, first-time setup)
+        ctx.profile(True)
+        ctx.profile_reset()
+        ms = run(one)
+        prof = {f: round(ctx.profile_read(f)[1], 1) for f in fams}
+        ctx.profile(False)
+        out["one_angle" if one else "all_angles"] = {"ms": ms, "phase_ms": prof}
+    line = {"metric": "device time by phase of served items (batched closed loop)",
+            "requests": len(reqs), "items": len(items), "batches": len(groups),
+            "panels_per_batch_head": [surfs[g[0][0]].n_panels for g in groups],
+            "angles_per_item_mean": float(np.mean([len(a) for _, _, a in items])), **out,
+            "note": "profiled runs: per-family CUDA events on the main stream"}
+    print(json.dumps(line))
+    return line
+
+
 # ------------------------------------------------------------------ CPU baseline
 def _oracle_one(k, nodes, tris, precision):
     from oracle import oracle as O
@@ -1037,9 +1102,14 @@ def main():
     ap.add_argument("--fp64-requests", type=int, default=16,
                     help="config 4: requests of the stream also served in FP64")
     ap.add_argument("--rate", type=float, default=0.0, help="config 4: arrivals/s (0: 70%% load)")
+    ap.add_argument("--phases", action="store_true",
+                    help="config 4: device time by phase of the stream's first --requests "
+                         "requests, batched closed loop, instead of serving them")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == 4 and args.phases:
+        run_config4_phases(args)
     elif args.config == 1:
         run_ours(args)
     else:
