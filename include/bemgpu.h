@@ -427,7 +427,9 @@ int bemgpu_solution_destroy(bemgpu_solution *sol);
  * later requests on the same mesh and wavenumber (sweeps.jl:680-701 reuses a factor
  * across angles within one call); a factor is computed once and used by one lane at a
  * time.  Every item is computed exactly as alone: batching changes which launch carries
- * it, not its arithmetic.
+ * it, not its arithmetic.  A batch whose device allocation runs out of memory (the budget
+ * counts live blocks, not the caching pools' free ones) is re-run once, when no other
+ * batch is on the device; a second failure fails its requests.
  */
 typedef struct bemgpu_server bemgpu_server;
 
