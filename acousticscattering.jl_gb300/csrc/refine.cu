@@ -294,11 +294,14 @@ __global__ void k_split_x(const VecInst* __restrict__ insts) {
 // Compact products in FP32 pair arithmetic.  A complex64 entry times the split x
 // (hi + lo): each product a * hi is exact as p + e (round-to-nearest product and its FMA
 // error), p enters a (s, t) pair by TwoSum (s + t carries the sum exactly up to the FP32
-// rounding of t), and e and a * lo go into t.  Every 16 columns the pair is folded into
-// FP64, so t never holds more than 16 terms' errors: the partial sums carry about 46
-// bits, the accuracy of the FP64 products of the complex128 path at a small fraction of
-// its FP64 instruction count.  The intrinsics keep the compiler from contracting or
-// reassociating the error-free steps.
+// rounding of t), and e and a * lo go into t.  Every 32 columns (128 real products) the
+// pair is folded into FP64, so t holds at most that many terms' errors.  What is left is
+// the FP32 rounding of t: for an exact solution the computed residual stays below about
+// 6e-14 of |b| + |A||x| in every row of small Burton-Miller and Mueller systems, where a
+// dominant diagonal block carries most of a row (median about 3e-15; an operation-by-
+// operation emulation on the CPU), under the refinement's 1e-13 acceptance, at a small
+// fraction of the FP64 instruction count of the complex128 path.  The intrinsics keep the
+// compiler from contracting or reassociating the error-free steps.
 struct FPair {
   float s, t;
 };
