@@ -156,7 +156,10 @@ struct _GPUBEMData
     incidence_angle::Float64
     incidence_azimuth::Float64
     diagnostics::Diagnostics
+    compressed::Bool        # compressed operators + GMRES (its diagnostics add GMRES's)
 end
+_GPUBEMData(sol, nodes, triangles, angle, azimuth, d) =
+    _GPUBEMData(sol, nodes, triangles, angle, azimuth, d, false)
 
 _boundary_code(::Rigid) = Int32(0)
 _boundary_code(::PressureRelease) = Int32(1)
@@ -244,7 +247,8 @@ function bem(m::GPUMesh, boundary, k::Real; incidence_angle::Real = π / 2,
         d = Ref{Diagnostics}()
         ccall((:bemgpu_solution_diagnostics, libbemgpu), Cint, (Ptr{Cvoid}, Ref{Diagnostics}),
             r[], d)
-        data = _GPUBEMData(r[], m.nodes, m.triangles, incidence_angle, incidence_azimuth, d[])
+        data = _GPUBEMData(r[], m.nodes, m.triangles, incidence_angle, incidence_azimuth, d[],
+            true)
         return BEMSolution(AcousticScattering._SurfaceGeometry(m.nodes, m.triangles), boundary,
             Float64(k), :full, data)
     end
@@ -577,8 +581,37 @@ end
 target_strength(sol::BEMSolution{_GPUBEMData}; kwargs...) =
     20 * log10(abs(scattering_amplitude(sol; kwargs...)))
 
+"""
+    residual_history(sol) -> Vector{Float64}
+
+GMRES residual estimates, one per Arnoldi step, of a compressed-operator solution (the
+reference's `residual_history` diagnostic, full.jl:160-176).
+"""
+function residual_history(sol::BEMSolution{_GPUBEMData})
+    cnt = Ref{Int32}(0)
+    check(ccall((:bemgpu_gmres_history, libbemgpu), Cint,
+        (Ptr{Cvoid}, Int32, Ptr{Float64}, Int32, Ptr{Int32}),
+        sol.data.solution, 0, C_NULL, 0, cnt))
+    out = zeros(Float64, max(1, cnt[]))
+    check(ccall((:bemgpu_gmres_history, libbemgpu), Cint,
+        (Ptr{Cvoid}, Int32, Ptr{Float64}, Int32, Ptr{Int32}),
+        sol.data.solution, 0, out, length(out), cnt))
+    return out[1:cnt[]]
+end
+
 function diagnostics(sol::BEMSolution{_GPUBEMData})
-    d = sol.data.diagnostics
+    if sol.data.compressed  # the reference's GMRES diagnostics (full.jl:160-176)
+        st = Ref{HmatrixStats}()
+        check(ccall((:bemgpu_hmatrix_stats_get, libbemgpu), Cint,
+            (Ptr{Cvoid}, Ref{HmatrixStats}), sol.data.solution, st))
+        return merge(_diagnostics(sol.data.diagnostics), (; method = :gmres,
+            converged = st[].gmres_converged == 1, iterations = Int(st[].gmres_iterations),
+            residual_history = residual_history(sol), compression = st[]))
+    end
+    return _diagnostics(sol.data.diagnostics)
+end
+
+function _diagnostics(d::Diagnostics)
     reasons = (:none, :conversion, :single_singular, :condition, :nonfinite,
         :iteration_limit, :stagnation)
     return (; unknown_count = d.unknown_count, quadrature_nodes = d.quadrature_nodes,
