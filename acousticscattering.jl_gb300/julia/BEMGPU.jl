@@ -161,6 +161,21 @@ end
 _GPUBEMData(sol, nodes, triangles, angle, azimuth, d) =
     _GPUBEMData(sol, nodes, triangles, angle, azimuth, d, false)
 
+# the reference's `_FullBEMSurfaceData` fields p_scat and dpdn_scat (types.jl:2-11): the
+# scattered traces at every unknown location, read from the device when asked for
+function Base.getproperty(d::_GPUBEMData, name::Symbol)
+    if name === :p_scat || name === :dpdn_scat
+        n = Int(getfield(d, :diagnostics).quadrature_nodes)
+        p = zeros(Float64, 2n)
+        q = zeros(Float64, 2n)
+        check(ccall((:bemgpu_traces, libbemgpu), Cint,
+            (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Float64}), getfield(d, :solution), 0, p, q))
+        v = name === :p_scat ? p : q
+        return [complex(v[2i - 1], v[2i]) for i in 1:n]
+    end
+    return getfield(d, name)
+end
+
 _boundary_code(::Rigid) = Int32(0)
 _boundary_code(::PressureRelease) = Int32(1)
 _boundary_code(::FluidFilled) = Int32(2)
