@@ -1,6 +1,7 @@
 """Host logic of bench.py that needs no GPU: the served-stream driver reports failed
-requests in its line (and counts only completed ones) instead of aborting a long run, and
-the nvidia-smi sampler's clock, throttle-reason and memory parsing."""
+requests in its line (and counts only completed ones) instead of aborting a long run, the
+nvidia-smi sampler's clock, throttle-reason and memory parsing, the memory grouping of the
+uneven batch, and the seeded request stream (a shorter run serves a prefix of a longer)."""
 import os
 import sys
 
@@ -59,3 +60,24 @@ def test_clock_sampler_parses_reasons_and_memory():
     assert out["sm_mhz"] == np.median([2070.0, 1995.0])
     assert out["reasons"] == ["sw_power_cap"]
     assert out["memory_used_mib_max"] == 281487.0 and out["memory_total_mib"] == 284208.0
+
+
+def test_memory_groups_cover_every_instance_within_the_budget():
+    sizes = [500, 12000, 800, 7000, 7000, 3000, 11000, 600]
+    per = 24.0
+    budget = 12000 ** 2 * per * 1.5
+    groups = bench._memory_groups(sizes, budget, per)
+    assert [i for g in groups for i in g] == list(range(len(sizes)))   # in order, once each
+    for g in groups:
+        assert len(g) == 1 or sum(sizes[i] ** 2 * per for i in g) <= budget
+
+
+def test_request_stream_is_seeded_and_prefix_stable():
+    """The served stream's first requests are the same whatever its length, so a shorter
+    run measures a prefix of the longer one."""
+    b1, r1 = bench._request_stream(20, 16)
+    b2, r2 = bench._request_stream(50, 16)
+    assert b1 == b2
+    for (i1, k1, a1), (i2, k2, a2) in zip(r1, r2[:20]):
+        assert i1 == i2 and np.array_equal(k1, k2) and np.array_equal(a1, a2)
+    assert all(1 <= len(k) <= 32 and 1 <= len(a) <= 64 for _, k, a in r2)
