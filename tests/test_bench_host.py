@@ -81,3 +81,19 @@ def test_request_stream_is_seeded_and_prefix_stable():
     for (i1, k1, a1), (i2, k2, a2) in zip(r1, r2[:20]):
         assert i1 == i2 and np.array_equal(k1, k2) and np.array_equal(a1, a2)
     assert all(1 <= len(k) <= 32 and 1 <= len(a) <= 64 for _, k, a in r2)
+
+
+def test_lu_update_flops_account_for_the_factorisation():
+    """The roofline's algorithmic flops (the LU's tensor-core updates, 8 real flops per
+    complex multiply-add) are most of a complex LU's 8/3 N^3, short of it by the panel
+    and triangular-block work, which grows with the block width."""
+    N = 10240
+    f256 = bench.lu_update_flops(N, 256)
+    f128 = bench.lu_update_flops(N, 128)
+    total = 8.0 / 3.0 * N ** 3
+    assert 0.95 < f256 / total < 1.0 and 0.95 < f128 / total < 1.0
+    assert f128 > f256          # narrower steps leave less outside the updates
+    # one K = 256 trailing update of an m x m block: 8 m^2 K flops, C read and written
+    # once (16 B per complex64 entry) and the two operand images read once
+    assert bench._upd(5504, 5504, 256) == (8.0 * 5504 ** 2 * 256,
+                                           16.0 * 5504 ** 2 + 8.0 * 256 * 2 * 5504)
